@@ -1,0 +1,162 @@
+"""Loader and ctypes mirror of the covgpu C ABI (include/covgpu.h).
+
+The shared library is required: there is no CPU fallback. Importing this
+module does not need a GPU; calling a kernel does.
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+MAX_VARIANTS = 8
+MAX_LAYERS = 16
+N_DATES = 19
+N_DURS = 5
+N_DRAWS = 10
+N_RES_INT = 30
+RES_SEVERE_NOW = 28
+RES_CRITICAL_NOW = 29
+N_RES_VAR = 6
+N_RES_F = 3
+FX_NAB_BITS = 24
+FX_IMM_BITS = 32
+NO_VARIANT = 0xFF
+EDGE_TILE = 4096          # edges per edge-pass block (covgpu.cu EDGE_TILE)
+AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
+AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
+
+OK, OVERFLOW, TIMEOUT, BADARG, CUDA_ERROR = 0, 1, 2, 3, 4
+STATUS_NAMES = {OK: 'OK', OVERFLOW: 'OVERFLOW', TIMEOUT: 'TIMEOUT', BADARG: 'BADARG', CUDA_ERROR: 'CUDA_ERROR'}
+
+DIST_CODES = {'lognormal_int': 0, 'lognorm_int': 0, 'lognormal': 1, 'lognorm': 1, 'normal': 2, 'norm': 2,
+              'normal_int': 3, 'normal_pos': 4}
+DIST_ZERO = 5
+DUR_ORDER = ['exp2inf', 'inf2sym', 'sym2sev', 'sev2crit', 'asym2rec', 'mild2rec', 'sev2rec', 'crit2rec', 'crit2die']
+
+
+class CovgpuError(RuntimeError):
+    """A covgpu entry point returned a non-OK status."""
+
+    def __init__(self, fn, rc):
+        super().__init__(f'{fn} failed with status {STATUS_NAMES.get(rc, rc)}')
+        self.rc = rc
+
+
+class DurPar(C.Structure):
+    _fields_ = [('code', C.c_int32), ('_pad', C.c_int32), ('a', C.c_double), ('b', C.c_double)]
+
+
+class SimParams(C.Structure):
+    _fields_ = [
+        ('agent_off', C.c_int64), ('n_agents', C.c_int32), ('n_variants', C.c_int32),
+        ('n_layers', C.c_int32), ('npts', C.c_int32), ('key0', C.c_uint32), ('key1', C.c_uint32),
+        ('use_waning', C.c_int32), ('nab_kin_len', C.c_int32),
+        ('n_beds_hosp', C.c_int64), ('n_beds_icu', C.c_int64),
+        ('frac_time', C.c_float), ('load_ratio', C.c_float), ('high_cap', C.c_float), ('asymp_factor', C.c_float),
+        ('trans_redux', C.c_float), ('nab_boost', C.c_float), ('no_hosp_factor', C.c_float),
+        ('no_icu_factor', C.c_float),
+        ('rel_symp', C.c_float * MAX_VARIANTS), ('rel_severe', C.c_float * MAX_VARIANTS),
+        ('rel_crit', C.c_float * MAX_VARIANTS), ('rel_death', C.c_float * MAX_VARIANTS),
+        ('immunity', C.c_float * (MAX_VARIANTS * MAX_VARIANTS)),
+        ('rel_imm_asymp', C.c_double), ('rel_imm_mild', C.c_double), ('rel_imm_severe', C.c_double),
+        ('nab_norm', C.c_double),
+        ('ve_exp_alpha', C.c_double * 3), ('ve_beta', C.c_double * 3),
+        ('dur', DurPar * len(DUR_ORDER)), ('nab_init', DurPar),
+        ('nab_kin', C.c_void_p), ('beta_tab', C.c_void_p), ('beta_layer_tab', C.c_void_p), ('vx_imm', C.c_void_p),
+        ('n_vaccines', C.c_int32), ('_pad2', C.c_int32),
+        ('res_int', C.c_void_p), ('res_var', C.c_void_p), ('res_fx', C.c_void_p),
+    ]
+
+
+class Layer(C.Structure):
+    _fields_ = [('p1', C.c_void_p), ('p2', C.c_void_p), ('beta', C.c_void_p), ('n_edges', C.c_int64),
+                ('tile_begin', C.c_int64), ('sim', C.c_int32), ('layer', C.c_int32), ('dynamic', C.c_int32),
+                ('beta_const', C.c_float), ('iso_factor', C.c_float), ('quar_factor', C.c_float),
+                ('_pad', C.c_int32)]
+
+
+class AgentBlock(C.Structure):
+    _fields_ = [('begin', C.c_int64), ('end', C.c_int64), ('sim', C.c_int32), ('_pad', C.c_int32)]
+
+
+class State(C.Structure):
+    _fields_ = [
+        ('n', C.c_int64), ('n_sims', C.c_int32), ('n_segments', C.c_int32), ('n_tiles', C.c_int64),
+        ('n_agent_blocks', C.c_int64),
+        ('flags', C.c_void_p), ('vstate', C.c_void_p),
+        ('symp_prob', C.c_void_p), ('severe_prob', C.c_void_p), ('crit_prob', C.c_void_p), ('death_prob', C.c_void_p),
+        ('rel_trans', C.c_void_p), ('rel_sus', C.c_void_p),
+        ('n_infections', C.c_void_p), ('n_breakthroughs', C.c_void_p),
+        ('peak_nab', C.c_void_p), ('nab', C.c_void_p), ('t_nab_event', C.c_void_p),
+        ('vaccine_source', C.c_void_p),
+        ('sus_imm', C.c_void_p), ('symp_imm', C.c_void_p), ('sev_imm', C.c_void_p),
+        ('imm_stride_variants', C.c_int32), ('_pad0', C.c_int32),
+        ('dates', C.c_void_p), ('durs', C.c_void_p),
+        ('viral_load', C.c_void_p), ('roles', C.c_void_p), ('claim', C.c_void_p),
+        ('events', C.c_void_p), ('event_capacity', C.c_int64), ('event_count', C.c_void_p),
+        ('log', C.c_void_p), ('log_capacity', C.c_int64), ('log_count', C.c_void_p),
+        ('status', C.c_void_p), ('hospicu', C.c_void_p),
+        ('sims', C.c_void_p), ('segments', C.c_void_p), ('agent_blocks', C.c_void_p),
+        ('draw_table', C.c_void_p), ('edge_uniforms', C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded covgpu library (built in-tree on first use if missing)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB_PATH
+        if not os.path.exists(path):
+            _build.build()
+        L = C.CDLL(path)
+        vp, i32, i64, f32, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_uint64
+        sp = C.POINTER(State)
+        L.covgpu_version.restype = C.c_int
+        L.covgpu_abi_layout.argtypes = [C.POINTER(C.c_int64), i32]
+        L.covgpu_abi_layout.restype = C.c_int
+        L.covgpu_viral_load.argtypes = [i32, vp, vp, vp, i64, f32, f32, f32, vp, vp]
+        L.covgpu_trans_sus.argtypes = [vp, vp, vp, vp, f32, vp, vp, vp, vp, f32, f32, f32, vp, i64, vp, vp, vp]
+        L.covgpu_infections_scratch_bytes.argtypes = [i64]
+        L.covgpu_infections_scratch_bytes.restype = i64
+        L.covgpu_infections.argtypes = [f32, vp, vp, vp, i64, vp, vp, vp, u64, i32, i32, i32, vp, vp, i64, vp, vp,
+                                        vp, i64, vp]
+        L.covgpu_agent_step.argtypes = [sp, i32, i32, i32, vp]
+        L.covgpu_edge_pass.argtypes = [sp, i32, vp]
+        L.covgpu_infect_claims.argtypes = [sp, i32, vp]
+        L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
+        L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
+        L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
+        for name in ('covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections', 'covgpu_agent_step',
+                     'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_materialize',
+                     'covgpu_run_days'):
+            getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def check(fn, rc):
+    if rc != OK:
+        raise CovgpuError(fn, rc)
+
+
+def call(name, *args):
+    rc = getattr(lib(), name)(*args)
+    check(name, rc)
+    return rc
+
+
+def abi_layout():
+    """(library values, ctypes values) of the ABI layout check."""
+    out = (C.c_int64 * 16)()
+    m = lib().covgpu_abi_layout(out, 16)
+    mine = [C.sizeof(SimParams), C.sizeof(Layer), C.sizeof(AgentBlock), 16, 16, C.sizeof(State),
+            State.sims.offset, State.edge_uniforms.offset, SimParams.res_fx.offset]
+    return list(out[:m]), mine
+
+
+EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
+            'covgpu_infections', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
+            'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days']

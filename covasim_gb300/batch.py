@@ -1,0 +1,117 @@
+"""``BatchSim``: many independent sims in one device state and one launch sequence.
+
+Replaces the process fan-out of ``cv.MultiSim`` / ``multi_run``
+(covasim/run.py:36-180, 1406-1519): every sim's agents and edges are
+concatenated in HBM with per-sim offsets, each sim keeps its own parameter
+block (seed, beta, change_beta schedule, population size ...), and each day is
+one agent pass, one edge pass and one infect pass over all sims together; the
+whole day loop is captured as one CUDA graph. Because every draw is keyed by
+the sim's own seed and its local agent/edge indices, a sim gives the same
+results alone or in any batch.
+"""
+import copy
+
+import numpy as np
+
+from . import parameters as cvpar
+from . import immunity as cvimm
+from . import defaults as cvd
+from . import _lib as L
+from .sim import Sim, build_spec, choose_seed_infections, CALL_SEED
+from .state import BatchState
+
+__all__ = ['BatchSim']
+
+
+class BatchSim:
+    """Run a list of sims (or ``n_runs`` reseeded copies of one) as one batch.
+
+    Args:
+        sims: a Sim, or a list of Sims (not yet run)
+        n_runs: with a single Sim, run this many copies with rand_seed + i (run.py:1363-1365)
+        use_graph: capture the day loop in a CUDA graph
+    """
+
+    def __init__(self, sims, n_runs=None, use_graph=True, log=False):
+        if isinstance(sims, Sim):
+            base = sims
+            n_runs = n_runs or 1
+            sims = []
+            for i in range(n_runs):
+                s = copy.deepcopy(base)
+                s['rand_seed'] = base['rand_seed'] + i
+                sims.append(s)
+        self.sims = list(sims)
+        self.use_graph = use_graph
+        self.log = log
+        self.state = None
+
+    def initialize(self):
+        specs = []
+        self.npts = None
+        for s in self.sims:
+            if s['variants']:
+                raise NotImplementedError('variants with importations are not batched yet; run them as single sims')
+            s.validate_pars()
+            s.init_variants()
+            if s['prognoses'] is None:
+                s['prognoses'] = cvpar.get_prognoses(s['prog_by_age'])
+            cvimm.init_immunity(s.pars, s.npts)
+            s.init_results()
+            s.init_interventions()
+            spec, popdict, person = build_spec(s.pars, s.popdict, getattr(s, '_person', None), s['interventions'])
+            s.popdict, s._person, s.spec = popdict, person, spec
+            specs.append(spec)
+        npts = {sp.npts for sp in specs}
+        if len(npts) != 1:
+            raise ValueError('all sims of a batch must have the same number of days')
+        self.npts = npts.pop()
+        self.state = BatchState(specs, log=self.log)
+        return self
+
+    def seed_infections(self):
+        for k, s in enumerate(self.sims):
+            if s['pop_infected']:
+                inds = choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected'])
+                self.state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+
+    def run(self, use_graph=None):
+        if self.state is None:
+            self.initialize()
+        use_graph = self.use_graph if use_graph is None else use_graph
+        self.seed_infections()
+        self.state.run_days(0, self.npts, open_prev=False, close_last=True, use_graph=use_graph)
+        status = self.state.status()
+        if status:
+            raise L.CovgpuError('device status', status)
+        return self
+
+    def results(self, k):
+        """Raw per-day device results of sim k (see BatchState.results)."""
+        return self.state.results(k)
+
+    def series(self, key):
+        """[n_sims, npts] array of one per-day result."""
+        return np.stack([self.state.results(k)[key] for k in range(len(self.sims))])
+
+    def finalize(self):
+        """Fill each Sim's results as Sim.finalize does."""
+        for k, s in enumerate(self.sims):
+            s.state = self.state
+            s.t = self.npts
+            s.complete = True
+            res = self.state.results(k)
+            for key, vals in res.items():
+                if key.startswith('_'):
+                    continue
+                if key in s.results['variant']:
+                    s.results['variant'][key].values[:] = vals
+                elif key in s.results:
+                    s.results[key].values[:] = vals
+            for key in cvd.result_flows:
+                s.results[f'cum_{key}'].values[:] = np.cumsum(s.results[f'new_{key}'].values)
+            s.results['cum_infections'].values += s['pop_infected']
+            s.results_ready = True
+            s.t -= 1
+            s.compute_states()
+        return self.sims

@@ -1,0 +1,968 @@
+// covgpu: GB300-native (sm_103a) kernels for Covasim 3.1.7's per-day step.
+//
+// Kernels (all HBM/L2-bound integer and float32 work; no tensor cores):
+//   k_viral_load / k_trans_sus / k_infections_*  the reference's three numba
+//       functions (covasim/utils.py:38-128) as standalone drop-ins;
+//   k_agent_step     one dense pass per agent per day: update_states_pre
+//       (people.py:164-312,368-374) + check_immunity (immunity.py:303-350) +
+//       update_nab (immunity.py:205-213) + stocks/flows (sim.py:651-674) +
+//       viral load and source/target role bitmaps for the edge pass;
+//   k_edge_pass      every layer segment and variant of every sim: compute_trans_sus
+//       folded in, both directions of each edge from one 128-bit read, Philox
+//       Bernoullis, warp-ballot compaction of events, atomicMin first-infector claim;
+//   k_infect_claims / k_infect_list   People.infect (people.py:435-586) +
+//       update_peak_nab (immunity.py:138-202).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <stddef.h>
+#include <math.h>
+#include "covgpu.h"
+#include "covgpu_device.cuh"
+
+using namespace covgpu;
+
+namespace {
+
+constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
+constexpr int EDGE_THREADS = 256;
+constexpr int EDGE_VEC = 4;            // edges per 128-bit load
+constexpr int64_t EDGE_TILE = 4096;    // edges per edge-pass block (must match the host)
+constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
+constexpr int INF_THREADS = 256;
+constexpr int INF_PER_THREAD = INF_TILE / INF_THREADS;
+
+inline int launch_status() {
+  return cudaGetLastError() == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
+}
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ============================================================ standalone kernels
+
+__global__ void k_viral_load(int t, const float* __restrict__ ts, const float* __restrict__ tr,
+                             const float* __restrict__ td, int64_t n, float frac_time, float load_ratio,
+                             float high_cap, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = viral_load_one(t, ts[i], tr[i], td[i], frac_time, load_ratio, high_cap);
+}
+
+// utils.py:82-90: rel_trans*inf*f_quar*f_asymp*f_iso*beta_layer*viral_load and
+// rel_sus*sus*f_quar*(1-immunity), float32 left to right (a factor of 1.0 is exact).
+__global__ void k_trans_sus(const float* __restrict__ rt, const float* __restrict__ rs,
+                            const uint8_t* __restrict__ inf, const uint8_t* __restrict__ sus, float beta_layer,
+                            const float* __restrict__ vl, const uint8_t* __restrict__ symp,
+                            const uint8_t* __restrict__ iso, const uint8_t* __restrict__ quar, float asymp_factor,
+                            float iso_factor, float quar_factor, const float* __restrict__ imm, int64_t n,
+                            float* __restrict__ ort, float* __restrict__ ors) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool q = quar[i];
+    float a = __fmul_rn(rt[i], inf[i] ? 1.0f : 0.0f);
+    a = __fmul_rn(a, q ? quar_factor : 1.0f);
+    a = __fmul_rn(a, symp[i] ? 1.0f : asymp_factor);
+    a = __fmul_rn(a, iso[i] ? iso_factor : 1.0f);
+    a = __fmul_rn(a, beta_layer);
+    a = __fmul_rn(a, vl[i]);
+    float b = __fmul_rn(rs[i], sus[i] ? 1.0f : 0.0f);
+    b = __fmul_rn(b, q ? quar_factor : 1.0f);
+    b = __fmul_rn(b, __fsub_rn(1.0f, imm[i]));
+    ort[i] = a;
+    ors[i] = b;
+  }
+}
+
+// utils.py:113-124 for one (direction, edge): in inf_inds (source trans != 0),
+// drawn (beta != 0) and u < p in float64.
+struct InfArgs {
+  float beta; const int32_t* p1; const int32_t* p2; const float* lb; int64_t E;
+  const float* rt; const float* rs; const double* uni; uint32_t k0, k1; int day, variant, layer;
+};
+__device__ __forceinline__ bool inf_hit(const InfArgs& a, int dir, int64_t e, int32_t& src, int32_t& tgt) {
+  src = dir ? a.p2[e] : a.p1[e];
+  tgt = dir ? a.p1[e] : a.p2[e];
+  const float st = a.rt[src];
+  if (st == 0.0f) return false;
+  const float p = __fmul_rn(__fmul_rn(__fmul_rn(a.beta, a.lb[e]), st), a.rs[tgt]);
+  if (p == 0.0f) return false;
+  double u;
+  if (a.uni) {
+    u = a.uni[(int64_t)dir * a.E + e];
+  } else {
+    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)a.day,
+                                      TAG_EDGE | ((uint32_t)a.variant << 8) | (uint32_t)a.layer), a.k0, a.k1);
+    u = dir ? u01_52(w.z, w.w) : u01_52(w.x, w.y);
+  }
+  return u < (double)p;
+}
+
+__global__ void __launch_bounds__(INF_THREADS) k_infections_count(InfArgs a, int64_t ntiles, int32_t* counts) {
+  const int dir = blockIdx.y;
+  const int64_t tile = blockIdx.x;
+  const int64_t e0 = tile * INF_TILE + (int64_t)threadIdx.x * INF_PER_THREAD;
+  int c = 0;
+  for (int j = 0; j < INF_PER_THREAD; ++j) {
+    const int64_t e = e0 + j;
+    int32_t s, g;
+    if (e < a.E && inf_hit(a, dir, e, s, g)) ++c;
+  }
+  __shared__ int s_sum;
+  if (threadIdx.x == 0) s_sum = 0;
+  __syncthreads();
+  c = __reduce_add_sync(0xffffffffu, (unsigned)c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_sum, c);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[(int64_t)dir * ntiles + tile] = s_sum;
+}
+
+// single-block exclusive scan of m counts into int64 offsets; total into *total
+__global__ void __launch_bounds__(1024) k_scan(const int32_t* counts, int64_t m, int64_t* offs, int64_t* total,
+                                               int64_t capacity, int32_t* status) {
+  __shared__ int64_t s_part[1024];
+  const int64_t per = (m + blockDim.x - 1) / blockDim.x;
+  const int64_t b = threadIdx.x * per, e = min(b + per, m);
+  int64_t sum = 0;
+  for (int64_t i = b; i < e; ++i) sum += counts[i];
+  s_part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < (int)blockDim.x; off <<= 1) {  // Hillis-Steele inclusive scan
+    const int64_t v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0;
+    __syncthreads();
+    s_part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int64_t run = s_part[threadIdx.x] - sum;
+  for (int64_t i = b; i < e; ++i) { offs[i] = run; run += counts[i]; }
+  if (threadIdx.x == blockDim.x - 1) {
+    *total = s_part[threadIdx.x];
+    if (s_part[threadIdx.x] > capacity && status) atomicOr(status, COVGPU_OVERFLOW);
+  }
+}
+
+// ordered write: block-level exclusive scan of per-thread hit counts keeps edge order
+__global__ void __launch_bounds__(INF_THREADS) k_infections_write(InfArgs a, int64_t ntiles, const int64_t* offs,
+                                                                  int32_t* out_src, int32_t* out_tgt, int64_t cap) {
+  const int dir = blockIdx.y;
+  const int64_t tile = blockIdx.x;
+  const int64_t e0 = tile * INF_TILE + (int64_t)threadIdx.x * INF_PER_THREAD;
+  uint32_t hits = 0;
+  int32_t hs[INF_PER_THREAD], ht[INF_PER_THREAD];
+#pragma unroll
+  for (int j = 0; j < INF_PER_THREAD; ++j) {
+    const int64_t e = e0 + j;
+    int32_t s = 0, g = 0;
+    if (e < a.E && inf_hit(a, dir, e, s, g)) hits |= 1u << j;
+    hs[j] = s;
+    ht[j] = g;
+  }
+  const int c = __popc(hits);
+  // block exclusive scan of c (warp shuffle scan + warp totals in shared memory)
+  __shared__ int s_warp[INF_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < INF_THREADS / 32 ? s_warp[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += v;
+    }
+    if (lane < INF_THREADS / 32) s_warp[lane] = wi - w;
+  }
+  __syncthreads();
+  int64_t pos = offs[(int64_t)dir * ntiles + tile] + s_warp[warp] + (incl - c);
+#pragma unroll
+  for (int j = 0; j < INF_PER_THREAD; ++j) {
+    if (hits & (1u << j)) {
+      if (pos < cap) { out_src[pos] = hs[j]; out_tgt[pos] = ht[j]; }
+      ++pos;
+    }
+  }
+}
+
+// ============================================================ fused agent pass
+
+
+__global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, int t, int do_prev, int do_day) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const int nv = sp.n_variants;
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tp = t - 1;
+
+  // shared counters: [0, N_RES_INT) day-t ints, then prev-day stocks, then variant slots
+  __shared__ unsigned int s_cnt[COVGPU_N_RES_INT];           // day t flows + severe/critical now
+  __shared__ unsigned int s_prev[N_STOCKS];                   // day t-1 stocks
+  __shared__ unsigned int s_var[COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS];  // [slot][v]
+  __shared__ double s_f[AGENT_THREADS / 32][3];
+  for (int k = threadIdx.x; k < COVGPU_N_RES_INT; k += blockDim.x) s_cnt[k] = 0;
+  for (int k = threadIdx.x; k < N_STOCKS; k += blockDim.x) s_prev[k] = 0;
+  for (int k = threadIdx.x; k < COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS; k += blockDim.x) s_var[k] = 0;
+  if (do_day && blockIdx.x == 0 && threadIdx.x == 0) *st.event_count = 0ull;
+  __syncthreads();
+
+  uint32_t f = valid ? st.flags[i] : 0u;
+  uint32_t vs = valid ? st.vstate[i] : 0xFFFFFFFFu;
+  const uint32_t f_in = f, vs_in = vs;
+  double nab_sum = 0.0, sus_sum = 0.0, symp_sum = 0.0;
+
+  // ---------------------------------------------------------- close day t-1
+  if (do_prev) {
+    // sim.py:652-656: stocks at the end of day t-1
+#pragma unroll
+    for (int k = 0; k < N_STOCKS; ++k) {
+      const unsigned c = __reduce_add_sync(0xffffffffu, (valid && (f & STOCK_BITS[k])) ? 1u : 0u);
+      if (lane == 0 && c) atomicAdd(&s_prev[k], c);
+    }
+    for (int v = 0; v < nv; ++v) {
+      const unsigned ce = __reduce_add_sync(0xffffffffu, (valid && ((f >> (EXPV_SHIFT + v)) & 1u)) ? 1u : 0u);
+      const unsigned ci = __reduce_add_sync(0xffffffffu, (valid && ((f >> (INFV_SHIFT + v)) & 1u)) ? 1u : 0u);
+      if (lane == 0 && ce) atomicAdd(&s_var[RV_N_EXPOSED * COVGPU_MAX_VARIANTS + v], ce);
+      if (lane == 0 && ci) atomicAdd(&s_var[RV_N_INFECTIOUS * COVGPU_MAX_VARIANTS + v], ci);
+    }
+    if (valid) {
+      float nab = 0.0f;
+      if (sp.use_waning) {
+        nab = st.nab[i];
+        const float peak = st.peak_nab[i];
+        if (peak != 0.0f) {  // sim.py:666-669 -> immunity.py:205-213 at t-1
+          int k = tp - st.t_nab_event[i];
+          if (k < 0 || k >= sp.nab_kin_len) {
+            atomicOr(st.status, COVGPU_BADARG);
+            k = k < 0 ? 0 : sp.nab_kin_len - 1;
+          }
+          float x = (float)__dadd_rn((double)nab, __dmul_rn(sp.nab_kin[k], (double)peak));
+          if (x < 0.0f) x = 0.0f;
+          if (x > peak) x = peak;
+          nab = x;
+          st.nab[i] = nab;
+        }
+      }
+      if (!(f & B_DEAD) && nab != 0.0f) nab_sum = (double)nab;  // sim.py:672
+    }
+  }
+
+  // ---------------------------------------------------------- day t
+  uint32_t src_bit = 0, tgt_bit = 0;
+  if (do_day) {
+    unsigned c_inf = 0, c_symp = 0, c_sev = 0, c_crit = 0, c_rec = 0, c_dead = 0, c_kdead = 0;
+    int inf_v = -1;
+    if (valid) {
+      const float tf = (float)t;
+      uint32_t ev = vs & 0xFFu, iv = (vs >> 8) & 0xFFu, rv = (vs >> 16) & 0xFFu;
+      const bool is_exp = f & B_EXP;  // people.py:170 snapshot
+      if (is_exp) {
+        if (!(f & B_INF)) {  // check_infectious, people.py:222-232
+          const float d = date_row(st, COVGPU_DATE_INFECTIOUS)[i];
+          if (defined(d) && tf >= d) {
+            f |= B_INF;
+            iv = ev;
+            if (iv < (uint32_t)nv) { f |= 1u << (INFV_SHIFT + iv); inf_v = (int)iv; }
+            c_inf = 1;
+          }
+        }
+        if (!(f & B_SYMP)) {  // check_symptomatic, people.py:235-239
+          const float d = date_row(st, COVGPU_DATE_SYMPTOMATIC)[i];
+          if (defined(d) && tf >= d) { f |= B_SYMP; c_symp = 1; }
+        }
+        if (!(f & B_SEV)) {  // check_severe, people.py:242-246
+          const float d = date_row(st, COVGPU_DATE_SEVERE)[i];
+          if (defined(d) && tf >= d) { f |= B_SEV; c_sev = 1; }
+        }
+        if (!(f & B_CRIT)) {  // check_critical, people.py:249-253
+          const float d = date_row(st, COVGPU_DATE_CRITICAL)[i];
+          if (defined(d) && tf >= d) { f |= B_CRIT; c_crit = 1; }
+        }
+        if (!(f & B_REC)) {  // check_recovery, people.py:256-291
+          const float d = date_row(st, COVGPU_DATE_RECOVERED)[i];
+          if (defined(d) && tf >= d) {
+            f &= ~(B_EXP | B_INF | B_SYMP | B_SEV | B_CRIT | BYVAR_MASK);
+            f |= B_REC;
+            rv = ev;
+            iv = NOV;
+            ev = NOV;
+            if (sp.use_waning) { f |= B_SUS; f &= ~B_DIAG; }
+            c_rec = 1;
+          }
+        }
+      }
+      if (f & B_ISO) {  // check_exit_iso, people.py:368-374
+        const float d = date_row(st, COVGPU_DATE_END_ISOLATION)[i];
+        if (defined(d) && tf >= d) f &= ~B_ISO;
+      }
+      if (is_exp && !(f & B_DEAD)) {  // check_death, people.py:294-312
+        const float d = date_row(st, COVGPU_DATE_DEAD)[i];
+        if (defined(d) && tf >= d) {
+          f |= B_DEAD;
+          if (f & B_DIAG) { f |= B_KDEAD; c_kdead = 1; }
+          f &= ~(B_SUS | B_EXP | B_INF | B_SYMP | B_SEV | B_CRIT | B_KCONT | B_QUAR | B_REC);
+          iv = ev = rv = NOV;
+          c_dead = 1;
+        }
+      }
+      vs = (vs & 0xFF000000u) | (rv << 16) | (iv << 8) | ev;
+
+      if (sp.use_waning) {  // check_immunity, immunity.py:303-350, float64
+        const float dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
+        const bool was_inf = tf >= dr;  // false for NaN
+        const double nab = (double)st.nab[i];
+        for (int v = 0; v < nv; ++v) {
+          double nat = 0.0, vac = 0.0;
+          if (was_inf && rv < (uint32_t)nv) nat = (double)sp.immunity[v * COVGPU_MAX_VARIANTS + rv];
+          if ((f & B_VACC) && sp.vx_imm) {
+            const int src = st.vaccine_source[i];
+            if (src >= 0 && src < sp.n_vaccines) vac = (double)sp.vx_imm[src * nv + v];
+          }
+          const double eff = __dmul_rn(nab, fmax(nat, vac));
+          const float a = calc_ve(eff, sp.ve_exp_alpha[0], sp.ve_beta[0]);
+          const float b = calc_ve(eff, sp.ve_exp_alpha[1], sp.ve_beta[1]);
+          const float c = calc_ve(eff, sp.ve_exp_alpha[2], sp.ve_beta[2]);
+          const int64_t off = (int64_t)v * st.n + i;
+          st.sus_imm[off] = a;
+          st.symp_imm[off] = b;
+          st.sev_imm[off] = c;
+          sus_sum = __dadd_rn(sus_sum, (double)a);
+          symp_sum = __dadd_rn(symp_sum, (double)b);
+        }
+      }
+
+      // viral load (sim.py:601-608) and edge-pass roles for the infectious / susceptible
+      if (f & B_INF) {
+        const float rt = st.rel_trans[i];
+        st.viral_load[i] = viral_load_one(t, date_row(st, COVGPU_DATE_INFECTIOUS)[i],
+                                          date_row(st, COVGPU_DATE_RECOVERED)[i], date_row(st, COVGPU_DATE_DEAD)[i],
+                                          sp.frac_time, sp.load_ratio, sp.high_cap);
+        src_bit = (rt != 0.0f && iv < (uint32_t)nv) ? 1u : 0u;
+      }
+      if ((f & B_SUS) && st.rel_sus[i] != 0.0f) tgt_bit = 1u;
+      if (f != f_in) st.flags[i] = f;
+      if (vs != vs_in) st.vstate[i] = vs;
+    }
+    // flows (people.py:172-180) and the severe/critical counts of sim.py:579-580
+    const unsigned cv[9] = {c_inf, c_symp, c_sev, c_crit, c_rec, c_dead, c_kdead,
+                            (valid && (f & B_SEV)) ? 1u : 0u, (valid && (f & B_CRIT)) ? 1u : 0u};
+    const int slot[9] = {R_INFECTIOUS, R_SYMPTOMATIC, R_SEVERE, R_CRITICAL, R_RECOVERIES, R_DEATHS,
+                         R_KNOWN_DEATHS, COVGPU_RES_SEVERE_NOW, COVGPU_RES_CRITICAL_NOW};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const unsigned c = __reduce_add_sync(0xffffffffu, cv[k]);
+      if (lane == 0 && c) atomicAdd(&s_cnt[slot[k]], c);
+    }
+    for (int v = 0; v < nv; ++v) {
+      const unsigned c = __reduce_add_sync(0xffffffffu, inf_v == v ? 1u : 0u);
+      if (lane == 0 && c) atomicAdd(&s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + v], c);
+    }
+    // role bitmaps: warp w of this block covers the 32-aligned word (i - lane) / 32
+    const uint32_t sm = __ballot_sync(0xffffffffu, src_bit), tm = __ballot_sync(0xffffffffu, tgt_bit);
+    if (lane == 0 && blk.begin + warp * 32 < blk.end) {
+      const int64_t w = (blk.begin + warp * 32) >> 5;
+      reinterpret_cast<uint2*>(st.roles)[w] = make_uint2(sm, tm);
+    }
+  }
+
+  // ---------------------------------------------------------- block totals
+  nab_sum = warp_sum(nab_sum);
+  sus_sum = warp_sum(sus_sum);
+  symp_sum = warp_sum(symp_sum);
+  if (lane == 0) { s_f[warp][0] = nab_sum; s_f[warp][1] = sus_sum; s_f[warp][2] = symp_sum; }
+  __syncthreads();
+  const int npts = sp.npts;
+  int64_t* res_t = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
+  int64_t* res_tp = sp.res_int + (int64_t)tp * COVGPU_N_RES_INT;
+  if (do_day && t < npts) {
+    for (int k = threadIdx.x; k < COVGPU_N_RES_INT; k += blockDim.x)
+      if (s_cnt[k]) atomicAdd(reinterpret_cast<unsigned long long*>(&res_t[k]), (unsigned long long)s_cnt[k]);
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+      const unsigned c = s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + v];
+      if (c) atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_INFECTIOUS) * nv + v]),
+                       (unsigned long long)c);
+    }
+  }
+  if (do_prev && tp >= 0) {
+    for (int k = threadIdx.x; k < N_STOCKS; k += blockDim.x)
+      if (s_prev[k]) atomicAdd(reinterpret_cast<unsigned long long*>(&res_tp[R_N_FIRST + k]), (unsigned long long)s_prev[k]);
+    for (int k = threadIdx.x; k < 2 * nv; k += blockDim.x) {
+      const int slot = k < nv ? RV_N_EXPOSED : RV_N_INFECTIOUS, v = k < nv ? k : k - nv;
+      const unsigned c = s_var[slot * COVGPU_MAX_VARIANTS + v];
+      if (c) atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)tp * COVGPU_N_RES_VAR + slot) * nv + v]),
+                       (unsigned long long)c);
+    }
+  }
+  // float sums: fixed-order in-block sum, then a fixed-point integer atomic
+  // (order independent, so the totals are bit-reproducible)
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0, c = 0;
+    for (int w = 0; w < AGENT_THREADS / 32; ++w) { a = __dadd_rn(a, s_f[w][0]); b = __dadd_rn(b, s_f[w][1]); c = __dadd_rn(c, s_f[w][2]); }
+    if (do_prev && tp >= 0 && a != 0.0)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)tp * COVGPU_N_RES_F + 0]),
+                (unsigned long long)llrint(ldexp(a, COVGPU_FX_NAB_BITS)));
+    if (do_day && t < npts && (b != 0.0 || c != 0.0)) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)t * COVGPU_N_RES_F + 1]),
+                (unsigned long long)llrint(ldexp(b, COVGPU_FX_IMM_BITS)));
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)t * COVGPU_N_RES_F + 2]),
+                (unsigned long long)llrint(ldexp(c, COVGPU_FX_IMM_BITS)));
+    }
+  }
+}
+
+// ============================================================ fused edge pass
+
+struct Roles { uint32_t src, tgt; };
+__device__ __forceinline__ Roles role_of(const uint32_t* __restrict__ roles, int32_t a) {
+  const uint2 w = __ldg(reinterpret_cast<const uint2*>(roles) + (a >> 5));
+  const uint32_t b = (uint32_t)a & 31u;
+  return Roles{(w.x >> b) & 1u, (w.y >> b) & 1u};
+}
+
+struct SegCtx {
+  const covgpu_layer* L;
+  const covgpu_sim_params* sp;
+  float beta_layer;
+  int nv;
+};
+
+// compute_trans_sus folded into compute_infections for one direction s -> g
+// (utils.py:88-89 then 117-123); returns true on a transmission.
+__device__ __noinline__ bool edge_dir(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
+                                      int32_t s, int32_t g, float lb, uint4& w, int& w_variant,
+                                      uint32_t& v_out) {
+  const covgpu_sim_params& sp = *c.sp;
+  const uint32_t v = (__ldg(st.vstate + s) >> 8) & 0xFFu;
+  if (v >= (uint32_t)c.nv) return false;
+  const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
+  float rte = __ldg(st.rel_trans + s);
+  if (fs & B_QUAR) rte = __fmul_rn(rte, c.L->quar_factor);
+  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, sp.asymp_factor);
+  if (fs & B_ISO) rte = __fmul_rn(rte, c.L->iso_factor);
+  rte = __fmul_rn(rte, c.beta_layer);
+  rte = __fmul_rn(rte, __ldg(st.viral_load + s));
+  if (rte == 0.0f) return false;
+  float rse = __ldg(st.rel_sus + g);
+  if (fg & B_QUAR) rse = __fmul_rn(rse, c.L->quar_factor);
+  rse = __fmul_rn(rse, __fsub_rn(1.0f, __ldg(st.sus_imm + (int64_t)v * st.n + g)));
+  const float beta = __ldg(sp.beta_tab + (int64_t)t * c.nv + v);
+  const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
+  if (p == 0.0f) return false;
+  double u;
+  if (st.edge_uniforms) {
+    const int seg = (int)(c.L - st.segments);
+    u = st.edge_uniforms[seg][((int64_t)v * 2 + dir) * c.L->n_edges + e];
+  } else {
+    if (w_variant != (int)v) {
+      w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
+                            TAG_EDGE | (v << 8) | (uint32_t)c.L->layer), sp.key0, sp.key1);
+      w_variant = (int)v;
+    }
+    u = dir ? u01_52(w.z, w.w) : u01_52(w.x, w.y);
+  }
+  v_out = v;
+  return u < (double)p;
+}
+
+__device__ __forceinline__ uint64_t event_key(int t, uint32_t v, int layer, int dir, int64_t e) {
+  return ((uint64_t)(0xFFFFu - (uint32_t)t) << 48) | ((uint64_t)v << 45) | ((uint64_t)layer << 41) |
+         ((uint64_t)dir << 40) | (uint64_t)e;
+}
+
+// warp-aggregated append of (key, target, source); all lanes of the warp call it
+__device__ __forceinline__ void emit(const covgpu_state& st, bool has, uint64_t key, int32_t tgt, int32_t src) {
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  const int leader = __ffs(m) - 1;
+  if (lane == leader) base = atomicAdd(st.event_count, (unsigned long long)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (has) {
+    atomicMin(reinterpret_cast<unsigned long long*>(st.claim + tgt), (unsigned long long)key);
+    const unsigned long long pos = base + __popc(m & ((1u << lane) - 1u));
+    if ((int64_t)pos < st.event_capacity) {
+      covgpu_event ev;
+      ev.key = key; ev.target = tgt; ev.source = src;
+      st.events[pos] = ev;
+    } else {
+      atomicOr(st.status, COVGPU_OVERFLOW);
+    }
+  }
+}
+
+__device__ __forceinline__ void edge_one(const covgpu_state& st, const SegCtx& c, int t, int64_t e, bool in_range,
+                                         int32_t a, int32_t b) {
+  bool c0 = false, c1 = false;
+  if (in_range) {
+    const Roles ra = role_of(st.roles, a), rb = role_of(st.roles, b);
+    c0 = ra.src & rb.tgt;
+    c1 = rb.src & ra.tgt;
+  }
+  bool h0 = false, h1 = false;
+  uint32_t v0 = 0, v1 = 0;
+  if (c0 || c1) {
+    const float lb = c.L->beta ? __ldg(c.L->beta + e) : c.L->beta_const;
+    uint4 w = make_uint4(0, 0, 0, 0);
+    int wv = -1;
+    if (c0) h0 = edge_dir(st, c, t, e, 0, a, b, lb, w, wv, v0);
+    if (c1) h1 = edge_dir(st, c, t, e, 1, b, a, lb, w, wv, v1);
+  }
+  emit(st, h0, h0 ? event_key(t, v0, c.L->layer, 0, e) : 0ull, b, a);
+  emit(st, h1, h1 ? event_key(t, v1, c.L->layer, 1, e) : 0ull, a, b);
+}
+
+__global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  __shared__ int s_seg;
+  if (threadIdx.x == 0) {  // segment owning this tile: last segment with tile_begin <= blockIdx.x
+    int lo = 0, hi = st.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    s_seg = lo;
+  }
+  __syncthreads();
+  const covgpu_layer* L = st.segments + s_seg;
+  SegCtx c;
+  c.L = L;
+  c.sp = st.sims + L->sim;
+  c.nv = c.sp->n_variants;
+  c.beta_layer = c.sp->beta_layer_tab[(int64_t)t * c.sp->n_layers + L->layer];
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
+  const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
+  const int64_t n_local = c.sp->n_agents;
+  const int64_t off = c.sp->agent_off;
+  for (int64_t eb = e0 + (int64_t)threadIdx.x * EDGE_VEC; eb < e0 + EDGE_TILE; eb += (int64_t)EDGE_THREADS * EDGE_VEC) {
+    int32_t a[EDGE_VEC], b[EDGE_VEC];
+    if (L->dynamic) {
+      // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
+      // endpoints uniform over the sim's agents (Philox keyed by edge and day)
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        const int64_t e = eb + j;
+        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L->layer),
+                               c.sp->key0, c.sp->key1);
+        a[j] = (int32_t)(off + uniform_index(w.x, w.y, (uint64_t)n_local));
+        b[j] = (int32_t)(off + uniform_index(w.z, w.w, (uint64_t)n_local));
+      }
+    } else if (eb + EDGE_VEC <= e1) {
+      const int4 pa = __ldg(reinterpret_cast<const int4*>(L->p1 + eb));
+      const int4 pb = __ldg(reinterpret_cast<const int4*>(L->p2 + eb));
+      a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
+      b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        const int64_t e = eb + j;
+        a[j] = e < e1 ? L->p1[e] : 0;
+        b[j] = e < e1 ? L->p2[e] : 0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < EDGE_VEC; ++j) edge_one(st, c, t, eb + j, eb + j < e1, a[j], b[j]);
+  }
+}
+
+// ============================================================ infect
+
+struct DrawSet { double z[6]; double u[4]; };
+
+__device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i,
+                                          int64_t local, int t, int call_tag, DrawSet& d) {
+  if (st.draw_table) {
+    const double* r = st.draw_table + i * COVGPU_N_DRAWS;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) d.z[k] = r[k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) d.u[k] = r[6 + k];
+    return;
+  }
+  const uint32_t tag = TAG_INFECT | (uint32_t)call_tag;
+  const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
+  const uint4 b1 = philox(make_uint4((uint32_t)local, 1u, (uint32_t)t, tag), sp.key0, sp.key1);
+  const uint4 b2 = philox(make_uint4((uint32_t)local, 2u, (uint32_t)t, tag), sp.key0, sp.key1);
+  box_muller(b0.x, b0.y, d.z[0], d.z[1]);
+  box_muller(b0.z, b0.w, d.z[2], d.z[3]);
+  box_muller(b1.x, b1.y, d.z[4], d.z[5]);
+  d.u[0] = u01_32(b1.z);
+  d.u[1] = u01_32(b1.w);
+  d.u[2] = u01_32(b2.x);
+  d.u[3] = u01_32(b2.y);
+}
+
+// people.py:435-586 for one agent (already deduplicated), plus update_peak_nab
+__device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, int sim, int64_t i, int t, int v,
+                           int32_t source, int layer_tag, int call_tag, bool hosp_max, bool icu_max) {
+  uint32_t f = st.flags[i];
+  if (!(f & B_SUS)) return;  // people.py:468-472: keep only susceptibles
+  const int nv = sp.n_variants;
+  const int64_t local = i - sp.agent_off;
+  // people.py:486-491: breakthrough infections (peak_nab defined)
+  const bool breakthrough = st.peak_nab[i] != 0.0f;
+  if (breakthrough && st.n_breakthroughs[i] == 0) st.rel_trans[i] = __fmul_rn(st.rel_trans[i], sp.trans_redux);
+  // people.py:494-505
+  float* d_rec = date_row(st, COVGPU_DATE_RECOVERED);
+  const bool reinfection = defined(d_rec[i]);
+  f &= ~(B_SUS | B_NAIVE | B_REC | B_DIAG);
+  f |= B_EXP | (1u << (EXPV_SHIFT + v));
+  st.n_infections[i] += 1;
+  if (breakthrough) st.n_breakthroughs[i] += 1;
+  st.vstate[i] = (st.vstate[i] & 0xFFFFFF00u) | (uint32_t)v;
+  atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_INFECTIONS]), 1ull);
+  if (reinfection)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_REINFECTIONS]), 1ull);
+  atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_INFECTIONS) * nv + v]), 1ull);
+  // people.py:508-511: infection log
+  if (st.log) {
+    const unsigned long long pos = atomicAdd(st.log_count, 1ull);
+    if ((int64_t)pos < st.log_capacity) {
+      covgpu_log_rec r;
+      r.source = source; r.target = (int32_t)local; r.day = t;
+      r.layer_variant = (layer_tag & 0xFF) | (v << 8) | (sim << 16);
+      st.log[pos] = r;
+    } else {
+      atomicOr(st.status, COVGPU_OVERFLOW);
+    }
+  }
+  DrawSet d;
+  get_draws(st, sp, i, local, t, call_tag, d);
+  float* d_inf = date_row(st, COVGPU_DATE_INFECTIOUS);
+  float* d_sym = date_row(st, COVGPU_DATE_SYMPTOMATIC);
+  float* d_sev = date_row(st, COVGPU_DATE_SEVERE);
+  float* d_crit = date_row(st, COVGPU_DATE_CRITICAL);
+  float* d_dead = date_row(st, COVGPU_DATE_DEAD);
+  float* u_exp2inf = dur_row(st, COVGPU_DUR_EXP2INF);
+  float* u_inf2sym = dur_row(st, COVGPU_DUR_INF2SYM);
+  float* u_sym2sev = dur_row(st, COVGPU_DUR_SYM2SEV);
+  float* u_sev2crit = dur_row(st, COVGPU_DUR_SEV2CRIT);
+  float* u_disease = dur_row(st, COVGPU_DUR_DISEASE);
+  const float nanf_ = f32nan();
+  const float tf = (float)t;
+  // people.py:514-520
+  const float de = (float)sample_dist(sp.dur[COVGPU_D_EXP2INF], d.z[0]);
+  u_exp2inf[i] = de;
+  date_row(st, COVGPU_DATE_EXPOSED)[i] = tf;
+  const float di = __fadd_rn(de, tf);
+  d_inf[i] = di;
+  d_sym[i] = nanf_; d_sev[i] = nanf_; d_crit[i] = nanf_;
+  date_row(st, COVGPU_DATE_DIAGNOSED)[i] = nanf_;
+  float rec = nanf_;
+  int symp_class;  // 0 asymptomatic, 1 mild, 2 severe (immunity.py:185-188)
+  // people.py:523-527
+  const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
+                                  __fsub_rn(1.0f, st.symp_imm[(int64_t)v * st.n + i]));
+  if (!(d.u[0] < (double)sp_symp)) {  // CASE 1: asymptomatic, people.py:530-532
+    const double dr = sample_dist(sp.dur[COVGPU_D_ASYM2REC], d.z[4]);
+    rec = (float)__dadd_rn((double)di, dr);
+    u_disease[i] = (float)__dadd_rn((double)de, dr);
+    symp_class = 0;
+  } else {  // CASE 2: symptomatic, people.py:535-541
+    const float dis = (float)sample_dist(sp.dur[COVGPU_D_INF2SYM], d.z[1]);
+    u_inf2sym[i] = dis;
+    const float ds = __fadd_rn(di, dis);
+    d_sym[i] = ds;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SYMPTOMATIC) * nv + v]), 1ull);
+    const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
+                                  __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
+    if (!(d.u[1] < (double)p_sev)) {  // CASE 2.1 mild, people.py:544-547
+      const double dr = sample_dist(sp.dur[COVGPU_D_MILD2REC], d.z[4]);
+      rec = (float)__dadd_rn((double)ds, dr);
+      u_disease[i] = (float)__dadd_rn((double)__fadd_rn(de, dis), dr);
+      symp_class = 1;
+    } else {  // CASE 2.2 severe, people.py:550-554
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
+      const float dss = (float)sample_dist(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
+      u_sym2sev[i] = dss;
+      const float dsev = __fadd_rn(ds, dss);
+      d_sev[i] = dsev;
+      const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], st.crit_prob[i]), hosp_max ? sp.no_hosp_factor : 1.0f);
+      symp_class = 2;
+      if (!(d.u[2] < (double)p_crit)) {  // CASE 2.2.1 not critical, people.py:557-559
+        const double dr = sample_dist(sp.dur[COVGPU_D_SEV2REC], d.z[4]);
+        rec = (float)__dadd_rn((double)dsev, dr);
+        u_disease[i] = (float)__dadd_rn((double)__fadd_rn(__fadd_rn(de, dis), dss), dr);
+      } else {  // CASE 2.2.2 critical, people.py:562-566
+        const float dsc = (float)sample_dist(sp.dur[COVGPU_D_SEV2CRIT], d.z[3]);
+        u_sev2crit[i] = dsc;
+        const float dcrit = __fadd_rn(dsev, dsc);
+        d_crit[i] = dcrit;
+        const float p_death = __fmul_rn(__fmul_rn(sp.rel_death[v], st.death_prob[i]), icu_max ? sp.no_icu_factor : 1.0f);
+        const float dsum = __fadd_rn(__fadd_rn(__fadd_rn(de, dis), dss), dsc);
+        if (!(d.u[3] < (double)p_death)) {  // CASE 2.2.2.1 alive, people.py:569-571
+          const double dr = sample_dist(sp.dur[COVGPU_D_CRIT2REC], d.z[4]);
+          rec = (float)__dadd_rn((double)dcrit, dr);
+          u_disease[i] = (float)__dadd_rn((double)dsum, dr);
+        } else {  // CASE 2.2.2.2 dead, people.py:574-577
+          const double dr = sample_dist(sp.dur[COVGPU_D_CRIT2DIE], d.z[4]);
+          d_dead[i] = (float)__dadd_rn((double)dcrit, dr);
+          u_disease[i] = (float)__dadd_rn((double)dsum, dr);
+          rec = nanf_;
+        }
+      }
+    }
+  }
+  d_rec[i] = rec;
+  // people.py:580-584 -> immunity.py:138-202 update_peak_nab (natural infection)
+  if (sp.use_waning) {
+    if (st.nab[i] > 0.0f) {
+      st.peak_nab[i] = __fmul_rn(st.peak_nab[i], sp.nab_boost);
+    } else {
+      const double init = sample_dist(sp.nab_init, d.z[5]);
+      const double rel = symp_class == 0 ? sp.rel_imm_asymp : (symp_class == 1 ? sp.rel_imm_mild : sp.rel_imm_severe);
+      st.peak_nab[i] = (float)__dmul_rn(__dmul_rn(exp2(init), rel), sp.nab_norm);
+    }
+    st.t_nab_event[i] = t;
+  }
+  st.flags[i] = f;
+  // no longer a target for the rest of the day (matters for infections before the edge pass)
+  atomicAnd(st.roles + 2 * (i >> 5) + 1, ~(1u << (i & 31)));
+}
+
+__device__ __forceinline__ int sim_of(const covgpu_state& st, int64_t i) {
+  int lo = 0, hi = st.n_sims - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (st.sims[mid].agent_off <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// sim.py:579-580: beds exceeded, from the severe/critical counts after the day's transitions
+__device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_sim_params& sp, int s, int t,
+                                         bool& hosp, bool& icu) {
+  if (st.hospicu) { hosp = st.hospicu[2 * s] != 0; icu = st.hospicu[2 * s + 1] != 0; return; }
+  const int64_t* r = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
+  hosp = sp.n_beds_hosp >= 0 && r[COVGPU_RES_SEVERE_NOW] > sp.n_beds_hosp;
+  icu = sp.n_beds_icu >= 0 && r[COVGPU_RES_CRITICAL_NOW] > sp.n_beds_icu;
+}
+
+__global__ void k_infect_claims(covgpu_state st, int t) {
+  const unsigned long long cnt = *st.event_count;
+  const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const covgpu_event ev = st.events[j];
+    if (st.claim[ev.target] != ev.key) continue;  // not the first infector of this target
+    const int s = sim_of(st, ev.target);
+    const covgpu_sim_params& sp = st.sims[s];
+    const int v = (int)((ev.key >> 45) & 7u), layer = (int)((ev.key >> 41) & 15u);
+    bool hosp, icu;
+    hosp_icu(st, sp, s, t, hosp, icu);
+    infect_one(st, sp, s, ev.target, t, v, (int32_t)(ev.source - sp.agent_off), layer, 0, hosp, icu);
+  }
+}
+
+__global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64_t n, int sim, int v,
+                              int layer_tag, int call_tag) {
+  const covgpu_sim_params& sp = st.sims[sim];
+  bool hosp, icu;
+  hosp_icu(st, sp, sim, t, hosp, icu);
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+    infect_one(st, sp, sim, inds[j], t, v, -1, layer_tag, call_tag, hosp, icu);
+}
+
+__global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1, int32_t* p2) {
+  const covgpu_layer& L = st.segments[seg];
+  const covgpu_sim_params& sp = st.sims[L.sim];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < L.n_edges; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L.layer),
+                           sp.key0, sp.key1);
+    p1[e] = (int32_t)uniform_index(w.x, w.y, (uint64_t)sp.n_agents);
+    p2[e] = (int32_t)uniform_index(w.z, w.w, (uint64_t)sp.n_agents);
+  }
+}
+
+int grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (int)b;
+}
+
+// ------------------------------------------------------------ graph cache for covgpu_run_days
+struct GraphEntry {
+  bool used = false;
+  covgpu_state st;
+  int t0 = 0, t1 = 0, open_prev = 0, close_last = 0;
+  cudaGraphExec_t exec = nullptr;
+};
+GraphEntry g_graphs[8];
+int g_graph_next = 0;
+
+int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
+  for (int t = t0; t < t1; ++t) {
+    k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
+    if (st->n_tiles > 0) k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+    k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
+  }
+  if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0);
+  return launch_status();
+}
+
+}  // namespace
+
+// ============================================================ C ABI
+
+extern "C" {
+
+int covgpu_version(void) { return 1; }
+
+int covgpu_abi_layout(int64_t* out, int32_t n) {
+  const int64_t v[] = {(int64_t)sizeof(covgpu_sim_params), (int64_t)sizeof(covgpu_layer),
+                       (int64_t)sizeof(covgpu_agent_block), (int64_t)sizeof(covgpu_event),
+                       (int64_t)sizeof(covgpu_log_rec), (int64_t)sizeof(covgpu_state),
+                       (int64_t)offsetof(covgpu_state, sims), (int64_t)offsetof(covgpu_state, edge_uniforms),
+                       (int64_t)offsetof(covgpu_sim_params, res_fx)};
+  const int m = (int)(sizeof(v) / sizeof(v[0]));
+  for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
+  return m;
+}
+
+int covgpu_viral_load(int32_t t, const float* date_inf, const float* date_rec, const float* date_dead, int64_t n,
+                      float frac_time, float load_ratio, float high_cap, float* out_load, void* stream) {
+  if (n < 0 || (n > 0 && (!date_inf || !date_rec || !date_dead || !out_load))) return COVGPU_BADARG;
+  if (n == 0) return COVGPU_OK;
+  k_viral_load<<<grid_for(n, 256), 256, 0, S(stream)>>>(t, date_inf, date_rec, date_dead, n, frac_time, load_ratio,
+                                                         high_cap, out_load);
+  return launch_status();
+}
+
+int covgpu_trans_sus(const float* rel_trans, const float* rel_sus, const uint8_t* inf, const uint8_t* sus,
+                     float beta_layer, const float* viral_load, const uint8_t* symp, const uint8_t* iso,
+                     const uint8_t* quar, float asymp_factor, float iso_factor, float quar_factor,
+                     const float* immunity_factors, int64_t n, float* out_rel_trans, float* out_rel_sus,
+                     void* stream) {
+  if (n < 0) return COVGPU_BADARG;
+  if (n == 0) return COVGPU_OK;
+  if (!rel_trans || !rel_sus || !inf || !sus || !viral_load || !symp || !iso || !quar || !immunity_factors ||
+      !out_rel_trans || !out_rel_sus)
+    return COVGPU_BADARG;
+  k_trans_sus<<<grid_for(n, 256), 256, 0, S(stream)>>>(rel_trans, rel_sus, inf, sus, beta_layer, viral_load, symp, iso,
+                                                        quar, asymp_factor, iso_factor, quar_factor, immunity_factors,
+                                                        n, out_rel_trans, out_rel_sus);
+  return launch_status();
+}
+
+int64_t covgpu_infections_scratch_bytes(int64_t n_edges) {
+  if (n_edges < 0) return -1;
+  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
+  const int64_t m = 2 * (ntiles > 0 ? ntiles : 1);
+  return m * (int64_t)sizeof(int64_t) + m * (int64_t)sizeof(int32_t) + 256;
+}
+
+int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas, int64_t n_edges,
+                      const float* rel_trans, const float* rel_sus, const double* uniforms, uint64_t seed, int32_t day,
+                      int32_t variant, int32_t layer, int32_t* out_src, int32_t* out_tgt, int64_t capacity,
+                      int64_t* out_count, int32_t* status, void* scratch, int64_t scratch_bytes, void* stream) {
+  if (n_edges < 0 || capacity < 0 || !out_count) return COVGPU_BADARG;
+  if (variant < 0 || variant >= COVGPU_MAX_VARIANTS || layer < 0 || layer >= COVGPU_MAX_LAYERS) return COVGPU_BADARG;
+  if (scratch_bytes < covgpu_infections_scratch_bytes(n_edges) || !scratch) return COVGPU_BADARG;
+  cudaStream_t s = S(stream);
+  if (n_edges == 0) {
+    return cudaMemsetAsync(out_count, 0, sizeof(int64_t), s) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
+  }
+  if (!p1 || !p2 || !layer_betas || !rel_trans || !rel_sus || (capacity > 0 && (!out_src || !out_tgt)))
+    return COVGPU_BADARG;
+  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
+  if (ntiles > 0x7FFFFFFF) return COVGPU_BADARG;
+  const int64_t m = 2 * ntiles;
+  int64_t* offs = reinterpret_cast<int64_t*>(scratch);
+  int32_t* counts = reinterpret_cast<int32_t*>(offs + m);
+  InfArgs a;
+  a.beta = beta; a.p1 = p1; a.p2 = p2; a.lb = layer_betas; a.E = n_edges; a.rt = rel_trans; a.rs = rel_sus;
+  a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32); a.day = day; a.variant = variant;
+  a.layer = layer;
+  dim3 grid((unsigned)ntiles, 2);
+  k_infections_count<<<grid, INF_THREADS, 0, s>>>(a, ntiles, counts);
+  k_scan<<<1, 1024, 0, s>>>(counts, m, offs, out_count, capacity, status);
+  k_infections_write<<<grid, INF_THREADS, 0, s>>>(a, ntiles, offs, out_src, out_tgt, capacity);
+  return launch_status();
+}
+
+static int check_state(const covgpu_state* st) {
+  if (!st || st->n <= 0 || st->n_sims <= 0 || st->n_agent_blocks <= 0) return COVGPU_BADARG;
+  if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->events ||
+      !st->event_count || !st->status)
+    return COVGPU_BADARG;
+  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0)) return COVGPU_BADARG;
+  if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
+  return COVGPU_OK;
+}
+
+int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_t do_day, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day);
+  return launch_status();
+}
+
+int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  if (st->n_tiles == 0) return COVGPU_OK;
+  k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, S(stream)>>>(*st, t);
+  return launch_status();
+}
+
+int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, S(stream)>>>(*st, t);
+  return launch_status();
+}
+
+int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds, int32_t sim,
+                       int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (n_inds < 0 || sim < 0 || sim >= st->n_sims || variant < 0 || variant >= COVGPU_MAX_VARIANTS) return COVGPU_BADARG;
+  if (n_inds == 0) return COVGPU_OK;
+  if (!inds) return COVGPU_BADARG;
+  k_infect_list<<<grid_for(n_inds, 128), 128, 0, S(stream)>>>(*st, t, inds, n_inds, sim, variant, layer_tag, call_tag);
+  return launch_status();
+}
+
+int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t, int32_t* p1, int32_t* p2,
+                             void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (segment < 0 || segment >= st->n_segments || !p1 || !p2) return COVGPU_BADARG;
+  k_layer_materialize<<<grid_for(1 << 22, 256), 256, 0, S(stream)>>>(*st, segment, t, p1, p2);
+  return launch_status();
+}
+
+int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open_prev, int32_t close_last,
+                    int32_t use_graph, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t0 < 0 || t1 < t0 || t1 >= 0xFFFF) return COVGPU_BADARG;
+  open_prev = (open_prev && t0 > 0) ? 1 : 0;
+  cudaStream_t s = S(stream);
+  if (!use_graph) return enqueue_days(st, t0, t1, open_prev, close_last, s);
+  GraphEntry* hit = nullptr;
+  for (auto& g : g_graphs)
+    if (g.used && g.t0 == t0 && g.t1 == t1 && g.close_last == close_last && g.open_prev == open_prev &&
+        memcmp(&g.st, st, sizeof(covgpu_state)) == 0) { hit = &g; break; }
+  if (!hit) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return COVGPU_CUDA_ERROR;
+    enqueue_days(st, t0, t1, open_prev, close_last, s);
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) return COVGPU_CUDA_ERROR;
+    GraphEntry& g = g_graphs[g_graph_next];
+    g_graph_next = (g_graph_next + 1) % 8;
+    if (g.used && g.exec) cudaGraphExecDestroy(g.exec);
+    g.used = false;
+    if (cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) { cudaGraphDestroy(graph); return COVGPU_CUDA_ERROR; }
+    cudaGraphDestroy(graph);
+    g.st = *st; g.t0 = t0; g.t1 = t1; g.open_prev = open_prev; g.close_last = close_last; g.used = true;
+    hit = &g;
+  }
+  return cudaGraphLaunch(hit->exec, s) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Device-side building blocks of the covgpu library (sm_103a).
+//
+// All float32 arithmetic that the reference performs in float32 is written as
+// explicit round-to-nearest intrinsics (__fmul_rn, __fadd_rn, ...) in the
+// reference's left-to-right order, and the library is compiled with
+// -fmad=false, so no product is contracted into an FMA: results are the
+// reference's bit for bit.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "covgpu.h"
+
+namespace covgpu {
+
+// ---------------------------------------------------------------- state bits
+// defaults.py:59-76 in order
+constexpr uint32_t B_SUS = 1u << 0, B_NAIVE = 1u << 1, B_EXP = 1u << 2, B_INF = 1u << 3,
+                   B_SYMP = 1u << 4, B_SEV = 1u << 5, B_CRIT = 1u << 6, B_TESTED = 1u << 7,
+                   B_DIAG = 1u << 8, B_REC = 1u << 9, B_KDEAD = 1u << 10, B_DEAD = 1u << 11,
+                   B_KCONT = 1u << 12, B_QUAR = 1u << 13, B_ISO = 1u << 14, B_VACC = 1u << 15;
+constexpr int EXPV_SHIFT = 16, INFV_SHIFT = 24;
+constexpr uint32_t BYVAR_MASK = 0xFFFF0000u;
+constexpr uint32_t NOV = COVGPU_NO_VARIANT;
+
+// per-sim-day integer result slots: flows (defaults.py:167-183) ...
+enum { R_INFECTIONS = 0, R_REINFECTIONS, R_INFECTIOUS, R_SYMPTOMATIC, R_SEVERE, R_CRITICAL,
+       R_RECOVERIES, R_DEATHS, R_TESTS, R_DIAGNOSES, R_KNOWN_DEATHS, R_QUARANTINED, R_ISOLATED,
+       R_DOSES, R_VACCINATED,
+       // ... then the stocks (defaults.py:145-159)
+       R_N_FIRST = 15 };
+constexpr int N_STOCKS = 13;
+__device__ __constant__ uint32_t STOCK_BITS[N_STOCKS] = {
+    B_SUS, B_EXP, B_INF, B_SYMP, B_SEV, B_CRIT, B_REC, B_DEAD, B_DIAG, B_KDEAD, B_QUAR, B_ISO, B_VACC};
+// per-sim-day-variant slots
+enum { RV_INFECTIONS = 0, RV_SYMPTOMATIC, RV_SEVERE, RV_INFECTIOUS, RV_N_EXPOSED, RV_N_INFECTIOUS };
+
+// ---------------------------------------------------------------- Philox-4x32-10
+// Salmon et al., SC'11. Round constants and Weyl increments of that paper.
+constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
+constexpr uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
+constexpr uint32_t TAG_EDGE = 0x01000000u, TAG_LAYER = 0x02000000u, TAG_INFECT = 0x03000000u;
+
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += PH_W0; k1 += PH_W1; }
+    const uint32_t hi0 = __umulhi(PH_M0, c.x), lo0 = PH_M0 * c.x;
+    const uint32_t hi1 = __umulhi(PH_M1, c.z), lo1 = PH_M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+  }
+  return c;
+}
+
+// exact double in (0,1): (k + 0.5) * 2^-52 with k the top 26 bits of a and of b
+__device__ __forceinline__ double u01_52(uint32_t a, uint32_t b) {
+  const uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);
+  return __dmul_rn(__dadd_rn((double)k, 0.5), 2.220446049250313080847263336181640625e-16);
+}
+// exact double in (0,1): (a + 0.5) * 2^-32
+__device__ __forceinline__ double u01_32(uint32_t a) {
+  return __dmul_rn(__dadd_rn((double)a, 0.5), 2.3283064365386962890625e-10);
+}
+// floor(x * n / 2^64) for x = a:b
+__device__ __forceinline__ int64_t uniform_index(uint32_t a, uint32_t b, uint64_t n) {
+  const uint64_t x = ((uint64_t)a << 32) | b;
+  return (int64_t)__umul64hi(x, n);
+}
+__device__ __forceinline__ void box_muller(uint32_t wa, uint32_t wb, double& z0, double& z1) {
+  const double u1 = u01_32(wa), u2 = u01_32(wb);
+  const double r = sqrt(__dmul_rn(-2.0, log(u1)));
+  const double th = __dmul_rn(6.283185307179586231995926937088, u2);  // (2.0 * pi) * u2
+  z0 = __dmul_rn(r, cos(th));
+  z1 = __dmul_rn(r, sin(th));
+}
+
+// ---------------------------------------------------------------- small helpers
+__device__ __forceinline__ float f32nan() { return __int_as_float(0x7fc00000); }
+__device__ __forceinline__ bool defined(float x) { return !isnan(x); }
+__device__ __forceinline__ float* date_row(const covgpu_state& st, int d) { return st.dates + (int64_t)d * st.n; }
+__device__ __forceinline__ float* dur_row(const covgpu_state& st, int d) { return st.durs + (int64_t)d * st.n; }
+
+// utils.py:156-236: a sample that is a function of one standard normal z
+__device__ __forceinline__ double sample_dist(const covgpu_dur_par& d, double z) {
+  switch (d.code) {
+    case COVGPU_DIST_LOGNORMAL_INT: return rint(exp(__dadd_rn(d.a, __dmul_rn(d.b, z))));
+    case COVGPU_DIST_LOGNORMAL: return exp(__dadd_rn(d.a, __dmul_rn(d.b, z)));
+    case COVGPU_DIST_NORMAL: return __dadd_rn(d.a, __dmul_rn(d.b, z));
+    case COVGPU_DIST_NORMAL_INT: return rint(fabs(__dadd_rn(d.a, __dmul_rn(d.b, z))));
+    case COVGPU_DIST_NORMAL_POS: return fabs(__dadd_rn(d.a, __dmul_rn(d.b, z)));
+    default: return 0.0;
+  }
+}
+
+// utils.py:39-79 for one agent, float32 as numba types it (the int32 t and the
+// float32 arrays meet in a float32 ufunc loop).
+__device__ __forceinline__ float viral_load_one(int t, float ts, float tr, float td, float frac_time,
+                                                float load_ratio, float high_cap) {
+  const float stop = isnan(td) ? tr : td;
+  const float total = __fsub_rn(stop, ts);
+  const float trans_day = __fmul_rn(frac_time, total);
+  const float trans_point = (trans_day > high_cap) ? __fdiv_rn(high_cap, total) : frac_time;
+  const bool early = __fdiv_rn(__fsub_rn((float)t, ts), total) < trans_point;
+  const float den = __fadd_rn(1.0f, __fmul_rn(frac_time, __fsub_rn(load_ratio, 1.0f)));
+  return __fdiv_rn(early ? load_ratio : 1.0f, den);
+}
+
+// immunity.py:216-247 calc_VE in float64, stored as float32
+__device__ __forceinline__ float calc_ve(double eff, double exp_alpha, double beta) {
+  const double lo = __dmul_rn(exp_alpha, pow(eff, beta));
+  return (float)__ddiv_rn(lo, __dadd_rn(1.0, lo));
+}
+
+// ---------------------------------------------------------------- block reduction helpers
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = __dadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+  return x;
+}
+
+}  // namespace covgpu

@@ -1,0 +1,399 @@
+"""``Sim``: the reference's cv.Sim interface with the day loop on the GPU.
+
+``Sim(pars).run()`` builds the population on the host, uploads it once, and
+runs every day on the device: the fused agent pass, the all-layer edge pass
+and infect. With no host-side interventions the whole run is one CUDA graph
+launch (``use_graph=True``). Follows covasim/sim.py:94-125 (initialize),
+505-532 (seed infections), 558-685 (step), 688-761 (run), 764-870 (finalize).
+
+Random numbers come from counter-based Philox streams keyed by the sim's seed,
+so results are reproducible bit for bit, in any batch position, and agree
+with the CPU oracle run in its Philox mode.
+"""
+import copy
+import time
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import defaults as cvd
+from . import parameters as cvpar
+from . import population as cvpop
+from . import immunity as cvimm
+from . import interventions as cvi
+from .people import People, Layer, Contacts
+from .state import SimSpec, BatchState
+
+__all__ = ['Sim', 'Result', 'AlreadyRunError', 'choose_seed_infections', 'build_spec']
+
+SEED_INFECTION_TAG = 0x5EED
+POPULATION_TAG = 0x9090
+PROGNOSIS_TAG = 0x7070
+CALL_SEED, CALL_IMPORT = 1, 2
+
+
+class AlreadyRunError(RuntimeError):
+    """sim.py:1550: the sim was asked to run past its end or to rerun."""
+
+
+class Result:
+    """A per-day result series (covasim/base.py:117-193), array-like."""
+
+    def __init__(self, name=None, npts=None, scale=True, values=None, n_variants=0):
+        self.name = name
+        self.scale = scale
+        if values is None:
+            shape = (n_variants, npts) if n_variants else (npts,)
+            values = np.zeros(shape, dtype=cvd.result_float)
+        self.values = np.asarray(values, dtype=cvd.result_float)
+
+    def __getitem__(self, k):
+        return self.values[k]
+
+    def __setitem__(self, k, v):
+        self.values[k] = v
+
+    def __len__(self):
+        return len(self.values)
+
+    def __array__(self, dtype=None, copy=None):
+        return self.values if dtype is None else self.values.astype(dtype)
+
+    def __repr__(self):
+        return f'Result({self.name}): {self.values!r}'
+
+    @property
+    def low(self):
+        return getattr(self, '_low', None)
+
+
+def choose_seed_infections(seed, n, k):
+    """The agents infected on day 0 (sim.py:528-530): k distinct agents from a
+    PCG64 stream keyed by the sim's seed."""
+    rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, SEED_INFECTION_TAG]))
+    return np.sort(rng.choice(int(n), size=int(k), replace=False)).astype(np.int64)
+
+
+def _layers_from_popdict(pars, popdict):
+    layers = []
+    for lkey in pars['beta_layer'].keys():
+        c = popdict['contacts'].get(lkey, dict(p1=np.zeros(0, np.int32), p2=np.zeros(0, np.int32)))
+        p1 = np.asarray(c['p1'], dtype=np.int32)
+        p2 = np.asarray(c['p2'], dtype=np.int32)
+        beta = np.asarray(c.get('beta', np.ones(len(p1))), dtype=np.float32)
+        dyn = bool(pars['dynam_layer'].get(lkey, 0))
+        if not dyn and len(p1) > 1 and np.any(p1[1:] < p1[:-1]):
+            order = np.argsort(p1, kind='stable')
+            p1, p2, beta = p1[order], p2[order], beta[order]
+        layers.append(dict(key=lkey, p1=p1, p2=p2, beta=beta, dynamic=dyn))
+    return layers
+
+
+def build_spec(pars, popdict=None, person=None, interventions=None):
+    """Population + prognoses + per-day tables of one sim -> (SimSpec, popdict, person)."""
+    seed = int(pars['rand_seed'])
+    npts = int(pars['n_days']) + 1
+    if popdict is None:
+        popdict = cvpop.make_randpop(pars, rng=np.random.default_rng([seed, POPULATION_TAG]))
+    if person is None:
+        person = cvpop.set_prognoses(np.asarray(popdict['age']), pars, np.random.default_rng([seed, PROGNOSIS_TAG]))
+    layers = _layers_from_popdict(pars, popdict)
+    keys = [ly['key'] for ly in layers]
+    betas = {'overall': pars['beta'], **{k: pars['beta_layer'][k] for k in keys}}
+    beta_sched = np.zeros(npts)
+    bl_sched = np.zeros((npts, len(keys)))
+    for t in range(npts):
+        for iv in interventions or []:
+            iv.apply_day(t, betas)
+        beta_sched[t] = betas['overall']
+        bl_sched[t] = [betas[k] for k in keys]
+    return SimSpec(pars, person, layers, beta_sched, bl_sched), popdict, person
+
+
+class Sim:
+    """A Covasim simulation whose per-day step runs on the GPU.
+
+    Args:
+        pars (dict): parameters (see ``covasim_gb300.make_pars``); keyword
+            arguments are merged in
+        popdict (dict): optional population (uid, age, sex, contacts)
+        use_graph (bool): capture the day loop in a CUDA graph
+    """
+
+    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, **kwargs):
+        self.label = label
+        self.pars = cvpar.make_pars()
+        self.update_pars(pars, **kwargs)
+        self.popdict = popdict
+        self.use_graph = use_graph
+        self.people = None
+        self.state = None
+        self.t = None
+        self.results = {}
+        self.initialized = False
+        self.complete = False
+        self.results_ready = False
+        self._event_capacity = None
+        self._log_capacity = None
+
+    # ------------------------------------------------------------------ pars
+    def __getitem__(self, key):
+        return self.pars[key]
+
+    def __setitem__(self, key, value):
+        self.pars[key] = value
+
+    def update_pars(self, pars=None, **kwargs):
+        """sim.py:259-281."""
+        pars = {**(pars or {}), **kwargs}
+        if not pars:
+            return
+        for k1, k2 in dict(n_agents='pop_size', init_infected='pop_infected').items():
+            if k1 in pars:
+                pars[k2] = pars.pop(k1)
+        if pars.get('pop_type'):
+            cvpar.reset_layer_pars(pars, force=False)
+        if pars.get('prog_by_age') is not None:
+            pars['prognoses'] = cvpar.get_prognoses(by_age=pars['prog_by_age'])
+        unknown = [k for k in pars if k not in self.pars]
+        if unknown:
+            raise KeyError(f'Key(s) {unknown} not found; available keys are {list(self.pars.keys())}')
+        self.pars.update(pars)
+
+    @property
+    def npts(self):
+        return int(self['n_days']) + 1
+
+    @property
+    def tvec(self):
+        return np.arange(self.npts)
+
+    def layer_keys(self):
+        return list(self['beta_layer'].keys())
+
+    # ------------------------------------------------------------------ initialize
+    def validate_pars(self):
+        p = self.pars
+        p['pop_size'] = int(p['pop_size'])
+        p['pop_infected'] = int(p['pop_infected'])
+        if p['pop_scale'] not in (None, 1, 1.0):
+            raise NotImplementedError('pop_scale > 1 (dynamic rescaling) is not supported on the GPU path')
+        if p['frac_susceptible'] != 1.0:
+            raise NotImplementedError('frac_susceptible < 1 is not supported on the GPU path')
+        if p['n_imports']:
+            raise NotImplementedError('n_imports > 0 is not supported on the GPU path yet')
+        if p['pop_infected'] > p['pop_size']:
+            raise ValueError('pop_infected is larger than pop_size')
+        for lp in cvpar.LAYER_PARS:
+            if np.isscalar(p[lp]):
+                p[lp] = {k: p[lp] for k in self.layer_keys()}
+
+    def init_variants(self):
+        """sim.py:477-495."""
+        for v in self['variants']:
+            if not isinstance(v, cvimm.variant):
+                raise TypeError(f'Variant {v} is not a cv.variant object; please create using cv.variant()')
+            if not v.initialized:
+                v.initialize(self.pars)
+        self['n_variants'] = len(self['variant_pars'])
+
+    def init_interventions(self):
+        self._host_interventions = []
+        for iv in self['interventions']:
+            if isinstance(iv, cvi.Intervention):
+                iv.initialize(self)
+                if not hasattr(iv, 'apply_day'):
+                    raise NotImplementedError(f'intervention {type(iv).__name__} is not supported on the GPU path yet')
+            elif callable(iv):
+                raise NotImplementedError('function interventions are not supported on the GPU path yet')
+
+    def initialize(self, reset=False, **kwargs):
+        """sim.py:94-125."""
+        self.t = 0
+        self.validate_pars()
+        self.init_variants()
+        if self['prognoses'] is None:
+            self['prognoses'] = cvpar.get_prognoses(self['prog_by_age'])
+        cvimm.init_immunity(self.pars, self.npts)
+        self.init_results()
+        self.init_interventions()
+        spec, popdict, person = build_spec(self.pars, self.popdict, getattr(self, '_person', None),
+                                           self['interventions'])
+        self.popdict = popdict
+        self._person = person
+        self.spec = spec
+        self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity)
+        contacts = Contacts()
+        for ly in spec.layers:
+            contacts[ly['key']] = Layer(ly['p1'], ly['p2'], ly['beta'], label=ly['key'])
+        self.people = People(self.state, 0, self.pars, contacts)
+        self.people['age'] = np.asarray(popdict['age'], dtype=cvd.default_float)
+        self.people['sex'] = np.asarray(popdict['sex'], dtype=cvd.default_float)
+        self._open_day = None     # day whose closing pass (stocks, update_nab) is pending
+        self._seeded = False
+        self.initialized = True
+        self.complete = False
+        self.results_ready = False
+        return self
+
+    def init_results(self):
+        """sim.py:284-351 (the keys the GPU path fills)."""
+        npts, nv = self.npts, self['n_variants']
+        self.results = {}
+        for key in cvd.result_flows:
+            self.results[f'cum_{key}'] = Result(f'cum_{key}', npts)
+            self.results[f'new_{key}'] = Result(f'new_{key}', npts)
+        for key in cvd.result_stocks:
+            self.results[f'n_{key}'] = Result(f'n_{key}', npts)
+        for key in ('n_imports', 'n_alive', 'n_naive', 'n_preinfectious', 'n_removed', 'prevalence', 'incidence',
+                    'frac_vaccinated', 'pop_nabs', 'pop_protection', 'pop_symp_protection'):
+            self.results[key] = Result(key, npts)
+        self.results['variant'] = {}
+        for key in cvd.result_flows_by_variant:
+            self.results['variant'][f'cum_{key}'] = Result(f'cum_{key}', npts, n_variants=nv)
+            self.results['variant'][f'new_{key}'] = Result(f'new_{key}', npts, n_variants=nv)
+        for key in cvd.result_stocks_by_variant:
+            self.results['variant'][f'n_{key}'] = Result(f'n_{key}', npts, n_variants=nv)
+        self.results['t'] = self.tvec
+        self.results_ready = False
+
+    # ------------------------------------------------------------------ day loop
+    def _seed(self):
+        """sim.py:505-532 (frac_susceptible == 1): seed infections on day 0."""
+        if self['pop_infected'] and not self._seeded:
+            inds = choose_seed_infections(self['rand_seed'], self['pop_size'], self['pop_infected'])
+            self.state.infect_list(0, inds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        self._seeded = True
+
+    def _variant_days(self):
+        days = set()
+        for v in self['variants']:
+            days.update(int(d) for d in np.atleast_1d(v.days))
+        return days
+
+    def _apply_variants(self, t):
+        """immunity.py:117-130 variant.apply: import n_imports agents chosen among the susceptible."""
+        for v in self['variants']:
+            if t in np.atleast_1d(v.days):
+                sus = np.nonzero(self.people['susceptible'])[0]
+                rng = np.random.default_rng([int(self['rand_seed']), 0x1A1A, t, v.index])
+                n_imp = min(v.n_imports, len(sus))
+                inds = rng.choice(sus, n_imp, replace=False)
+                self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.MAX_LAYERS + 1,
+                                       call_tag=CALL_IMPORT + v.index)
+
+    def step(self):
+        """One day (sim.py:558-685), then that day's closing pass."""
+        if not self.initialized:
+            self.initialize()
+        if self.complete:
+            raise AlreadyRunError('Simulation already complete (call sim.initialize() to re-run)')
+        t = self.t
+        if t == 0:
+            self._seed()
+        self.people.__dict__['t'] = t
+        self.state.agent_step(t, do_prev=self._open_day is not None, do_day=True)
+        self._apply_variants(t)
+        self.state.edge_pass(t)
+        self.state.infect_claims(t)
+        self.state.agent_step(t + 1, do_prev=True, do_day=False)
+        self._open_day = None
+        self.t += 1
+        if self.t == self.npts:
+            self.complete = True
+
+    def run(self, do_plot=False, until=None, restore_pars=True, reset_seed=True, verbose=None, use_graph=None):
+        """sim.py:688-761: run to ``until`` (default: the end) and finalize."""
+        if not self.initialized:
+            self.initialize()
+        until = self.npts if until is None else int(until)
+        if until > self.npts:
+            raise AlreadyRunError(f'Requested to run until t={until} but the simulation end is t={self.npts}')
+        if self.t >= until:
+            raise AlreadyRunError(f'Simulation is currently at t={self.t}, requested to run until t={until} '
+                                  'which has already been reached')
+        if self.complete:
+            raise AlreadyRunError('Simulation is already complete (call sim.initialize() to re-run)')
+        use_graph = self.use_graph if use_graph is None else use_graph
+        T = time.perf_counter()
+        host_days = sorted(d for d in self._variant_days() if self.t <= d < until)
+        if self.t == 0:
+            self._seed()
+        while self.t < until:
+            if self['timelimit'] and time.perf_counter() - T > self['timelimit']:
+                break
+            if self['stopping_func'] and self['stopping_func'](self):
+                break
+            nxt = next((d for d in host_days if d >= self.t), until)
+            if nxt > self.t:  # days without host work: one fused launch sequence (or graph)
+                self.state.run_days(self.t, nxt, close_last=True, use_graph=use_graph)
+                self.t = nxt
+            if self.t < until and self.t == nxt:  # a day with host work
+                self.step()
+        if self.t >= self.npts:
+            self.complete = True
+        status = self.state.status()
+        if status:
+            if status & L.OVERFLOW:
+                return self._rerun_bigger(until)
+            raise L.CovgpuError('device status', status)
+        if self.complete:
+            self.finalize()
+        return self
+
+    def _rerun_bigger(self, until):
+        """A fixed-capacity device buffer overflowed: the run is deterministic, so
+        redo it from the start with twice the capacity."""
+        self._event_capacity = 2 * self.state.event_capacity
+        self._log_capacity = 2 * max(self.state.log_capacity, 1)
+        self.initialize()
+        return self.run(until=until)
+
+    # ------------------------------------------------------------------ results
+    def finalize(self, verbose=None, restore_pars=True):
+        """sim.py:764-815 (no rescaling on the GPU path)."""
+        if self.results_ready:
+            raise AlreadyRunError('Simulation has already been finalized')
+        res = self.state.results(0)
+        for key, vals in res.items():
+            if key.startswith('_'):
+                continue
+            if key in self.results['variant']:
+                self.results['variant'][key].values[:] = vals
+            elif key in self.results:
+                self.results[key].values[:] = vals
+        for key in cvd.result_flows:
+            self.results[f'cum_{key}'].values[:] = np.cumsum(self.results[f'new_{key}'].values)
+        for key in cvd.result_flows_by_variant:
+            self.results['variant'][f'cum_{key}'].values[:] = np.cumsum(self.results['variant'][f'new_{key}'].values,
+                                                                        axis=1)
+        self.results['cum_infections'].values += self['pop_infected']
+        self.results['variant']['cum_infections_by_variant'].values[0] += self['pop_infected']
+        self.results_ready = True
+        self.t -= 1
+        self.compute_states()
+        self.summary = {k: v.values[-1] for k, v in self.results.items() if isinstance(v, Result)}
+        return self
+
+    def compute_states(self):
+        """sim.py:828-850."""
+        res = self.results
+        count_recov = 1 - self['use_waning']
+        n = self['pop_size']
+        res['n_alive'].values[:] = n - res['cum_deaths'].values
+        res['n_naive'].values[:] = n - res['cum_deaths'].values - res['n_recovered'].values - res['n_exposed'].values
+        res['n_susceptible'].values[:] = res['n_alive'].values - res['n_exposed'].values - count_recov * res['cum_recoveries'].values
+        res['n_preinfectious'].values[:] = res['n_exposed'].values - res['n_infectious'].values
+        res['n_removed'].values[:] = count_recov * res['cum_recoveries'].values + res['cum_deaths'].values
+        with np.errstate(divide='ignore', invalid='ignore'):
+            res['prevalence'].values[:] = res['n_exposed'].values / res['n_alive'].values
+            res['incidence'].values[:] = res['new_infections'].values / res['n_susceptible'].values
+            res['frac_vaccinated'].values[:] = res['n_vaccinated'].values / res['n_alive'].values
+
+    def raw_results(self):
+        """Per-day device results before finalize's post-processing (stocks as counted)."""
+        return self.state.results(0)
+
+    def infection_log(self):
+        return self.people.infection_log

@@ -1,0 +1,527 @@
+"""Device-resident agent state for a batch of sims, and the fused-kernel calls.
+
+Layout in HBM (``n`` = total agents, each sim starting at a multiple of 32):
+
+* ``flags``   uint32[n]   the 16 boolean states (bit i = defaults.STATES[i]),
+                          exposed_by_variant in bits 16-23, infectious_by_variant in 24-31
+* ``vstate``  uint32[n]   exposed / infectious / recovered variant, one byte each (0xFF = NaN)
+* per-person float32[n]: symp/severe/crit/death prob, rel_trans, rel_sus, peak_nab, nab
+* int32[n]: n_infections, n_breakthroughs, t_nab_event, vaccine_source
+* ``sus_imm``/``symp_imm``/``sev_imm`` float32[nv_max, n]
+* ``dates`` float32[19, n], ``durs`` float32[5, n] (NaN = undefined)
+* per-day working buffers: viral_load float32[n], roles uint32[2, n/32] (source and
+  target bitmaps, interleaved per 32 agents), claim uint64[n], event list, infection log
+* contact layers: one (p1, p2[, beta]) segment per (sim, layer), int32 global agent
+  indices sorted by p1; dynamic layers store no edges (redrawn from Philox each day)
+
+A single simulation is a batch of one; ``covasim_gb300.Sim`` and
+``covasim_gb300.BatchSim`` both drive this class.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import defaults as cvd
+
+F32, I32, I64, F64 = torch.float32, torch.int32, torch.int64, torch.float64
+
+STATE_BIT = cvd.STATE_BIT
+SUS_NAIVE = (1 << STATE_BIT['susceptible']) | (1 << STATE_BIT['naive'])
+VSTATE_NONE = 0x00FFFFFF
+
+
+def _align(x, a):
+    return (x + a - 1) // a * a
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def dur_par(dist):
+    """Pack one duration distribution (utils.py:156-236 sample()) as (code, a, b)."""
+    name = dist['dist']
+    if name not in L.DIST_CODES:
+        raise NotImplementedError(f'duration distribution "{name}" is not supported on the GPU path')
+    code = L.DIST_CODES[name]
+    p1, p2 = dist['par1'], dist['par2']
+    if code in (0, 1):
+        if not p1 > 0:
+            return L.DurPar(L.DIST_ZERO, 0, 0.0, 0.0)
+        mean = np.log(p1 ** 2 / np.sqrt(p2 ** 2 + p1 ** 2))   # utils.py:224
+        sigma = np.sqrt(np.log(p2 ** 2 / p1 ** 2 + 1))         # utils.py:225
+        return L.DurPar(code, 0, float(mean), float(sigma))
+    return L.DurPar(code, 0, float(p1), float(p2))
+
+
+class SimSpec:
+    """Everything the device needs to know about one sim.
+
+    Args:
+        pars: full parameter dict (prognoses applied; nab_kin and immunity set if waning)
+        person: per-person host arrays: symp_prob, severe_prob, crit_prob, death_prob, rel_trans, rel_sus
+        layers: list of dicts(key, p1, p2, beta, dynamic) in layer order
+        beta_sched: float64 [npts] overall beta per day (change_beta applied)
+        beta_layer_sched: float64 [npts, n_layers] per-layer beta per day
+    """
+
+    def __init__(self, pars, person, layers, beta_sched=None, beta_layer_sched=None):
+        self.pars = pars
+        self.person = person
+        self.layers = layers
+        self.n = int(pars['pop_size'])
+        self.npts = int(pars['n_days']) + 1
+        self.nv = int(pars['n_variants'])
+        if self.nv > L.MAX_VARIANTS:
+            raise ValueError(f'at most {L.MAX_VARIANTS} variants are supported')
+        if len(layers) > L.MAX_LAYERS:
+            raise ValueError(f'at most {L.MAX_LAYERS} layers are supported')
+        keys = [ly['key'] for ly in layers]
+        self.beta_sched = (np.full(self.npts, float(pars['beta'])) if beta_sched is None
+                           else np.asarray(beta_sched, dtype=np.float64))
+        if beta_layer_sched is None:
+            beta_layer_sched = np.array([[float(pars['beta_layer'][k]) for k in keys]] * self.npts)
+        self.beta_layer_sched = np.asarray(beta_layer_sched, dtype=np.float64).reshape(self.npts, len(keys))
+
+    def beta_table(self):
+        """sim.py:626: float32(beta * rel_beta * variant rel_beta) per day and variant."""
+        p = self.pars
+        tab = np.zeros((self.npts, self.nv), dtype=np.float32)
+        for v in range(self.nv):
+            label = p['variant_map'][v]
+            rb = p['variant_pars'][label]['rel_beta']
+            tab[:, v] = [np.float32(b * p['rel_beta'] * rb) for b in self.beta_sched]
+        return tab
+
+
+class BatchState:
+    """Agent and layer arrays of one or more sims in device memory."""
+
+    def __init__(self, specs, device='cuda', event_capacity=None, log_capacity=None, log=True):
+        if not torch.cuda.is_available():
+            raise RuntimeError('covasim_gb300 needs a CUDA device: the GPU path has no CPU fallback')
+        self.lib = L.lib()
+        self.device = torch.device(device)
+        self.specs = list(specs)
+        S = len(self.specs)
+        offs, n = [], 0
+        for sp in self.specs:
+            offs.append(n)
+            n = _align(n + sp.n, L.AGENT_ALIGN)
+        self.offsets = offs
+        self.n = max(n, L.AGENT_ALIGN)
+        self.nv_max = max(sp.nv for sp in self.specs)
+        dev = self.device
+        n = self.n
+        t = {}
+        t['flags'] = torch.zeros(n, dtype=I32, device=dev)
+        t['vstate'] = torch.full((n,), VSTATE_NONE, dtype=I32, device=dev)
+        for k in ('symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus', 'peak_nab', 'nab',
+                  'viral_load'):
+            t[k] = torch.zeros(n, dtype=F32, device=dev)
+        for k in ('n_infections', 'n_breakthroughs', 't_nab_event', 'vaccine_source'):
+            t[k] = torch.zeros(n, dtype=I32, device=dev)
+        for k in ('sus_imm', 'symp_imm', 'sev_imm'):
+            t[k] = torch.zeros((self.nv_max, n), dtype=F32, device=dev)
+        t['dates'] = torch.full((L.N_DATES, n), float('nan'), dtype=F32, device=dev)
+        t['durs'] = torch.full((L.N_DURS, n), float('nan'), dtype=F32, device=dev)
+        t['roles'] = torch.zeros(2 * ((n + 31) // 32), dtype=I32, device=dev)
+        t['claim'] = torch.full((n,), -1, dtype=I64, device=dev)
+        n_real = sum(sp.n for sp in self.specs)
+        self.event_capacity = int(event_capacity or (2 * n_real + 65536))
+        t['events'] = torch.zeros((self.event_capacity, 4), dtype=I32, device=dev)
+        t['event_count'] = torch.zeros(1, dtype=I64, device=dev)
+        self.log_enabled = log
+        self.log_capacity = int(log_capacity or (3 * n_real + 65536)) if log else 0
+        t['log'] = torch.zeros((max(self.log_capacity, 1), 4), dtype=I32, device=dev)
+        t['log_count'] = torch.zeros(1, dtype=I64, device=dev)
+        t['status'] = torch.zeros(1, dtype=I32, device=dev)
+        self.t = t
+
+        # per-sim tables, concatenated
+        self.res_int = torch.zeros(sum(sp.npts for sp in self.specs) * L.N_RES_INT, dtype=I64, device=dev)
+        self.res_var = torch.zeros(sum(sp.npts * L.N_RES_VAR * sp.nv for sp in self.specs), dtype=I64, device=dev)
+        self.res_fx = torch.zeros(sum(sp.npts for sp in self.specs) * L.N_RES_F, dtype=I64, device=dev)
+        beta_tabs, bl_tabs, kins = [], [], []
+        for sp in self.specs:
+            beta_tabs.append(sp.beta_table().ravel())
+            bl_tabs.append(sp.beta_layer_sched.astype(np.float32).ravel())
+            kin = sp.pars.get('nab_kin')
+            kins.append(np.asarray(kin if kin is not None else np.zeros(1), dtype=np.float64))
+        self.beta_tab = torch.from_numpy(np.concatenate(beta_tabs)).to(dev)
+        self.beta_layer_tab = torch.from_numpy(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32)).to(dev)
+        self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)
+
+        self._init_people()
+        self._build_layers()
+        self._build_sims(beta_tabs, bl_tabs, kins)
+        self._build_agent_blocks()
+        self.draw_table = None
+        self.edge_uniform_tensors = None
+        self.hospicu = None
+        self._refresh_state()
+
+    # ------------------------------------------------------------------ building
+    def _init_people(self):
+        t = self.t
+        flags = np.zeros(self.n, dtype=np.int32)
+        host = {k: np.zeros(self.n, dtype=np.float32) for k in ('symp_prob', 'severe_prob', 'crit_prob',
+                                                                'death_prob', 'rel_trans', 'rel_sus')}
+        for sp, off in zip(self.specs, self.offsets):
+            flags[off:off + sp.n] = SUS_NAIVE
+            for k in host:
+                host[k][off:off + sp.n] = np.asarray(sp.person[k], dtype=np.float32)
+        t['flags'].copy_(torch.from_numpy(flags))
+        for k, v in host.items():
+            t[k].copy_(torch.from_numpy(v))
+
+    def _build_layers(self):
+        self.segments = []   # (ctypes Layer, tensors kept alive)
+        self.layer_tensors = []
+        self.segment_index = {}  # (sim, layer) -> segment index
+        tiles = 0
+        for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
+            for li, ly in enumerate(sp.layers):
+                p1 = np.asarray(ly['p1'], dtype=np.int64)
+                n_edges = len(p1)
+                if n_edges == 0:
+                    continue
+                rec = L.Layer()
+                rec.n_edges = n_edges
+                rec.sim = s
+                rec.layer = li
+                rec.iso_factor = np.float32(sp.pars['iso_factor'][ly['key']])
+                rec.quar_factor = np.float32(sp.pars['quar_factor'][ly['key']])
+                keep = []
+                if ly.get('dynamic'):
+                    rec.dynamic = 1
+                    rec.beta_const = 1.0
+                else:
+                    p2 = np.asarray(ly['p2'], dtype=np.int64)
+                    beta = np.asarray(ly.get('beta', np.ones(n_edges)), dtype=np.float32)
+                    if len(p1) > 1 and np.any(p1[1:] < p1[:-1]):
+                        order = np.argsort(p1, kind='stable')
+                        p1, p2, beta = p1[order], p2[order], beta[order]
+                    if p1.min() < 0 or p1.max() >= sp.n or p2.min() < 0 or p2.max() >= sp.n:
+                        raise ValueError(f'layer {ly["key"]}: agent index out of range')
+                    tp1 = torch.from_numpy((p1 + off).astype(np.int32)).to(self.device)
+                    tp2 = torch.from_numpy((p2 + off).astype(np.int32)).to(self.device)
+                    if tp1.data_ptr() % 16 or tp2.data_ptr() % 16:
+                        raise RuntimeError('edge arrays must be 16-byte aligned')
+                    rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
+                    keep += [tp1, tp2]
+                    if np.all(beta == beta[0]):
+                        rec.beta = None
+                        rec.beta_const = float(beta[0])
+                    else:
+                        tb = torch.from_numpy(beta).to(self.device)
+                        rec.beta = tb.data_ptr()
+                        keep.append(tb)
+                rec.tile_begin = tiles
+                tiles += (n_edges + L.EDGE_TILE - 1) // L.EDGE_TILE
+                self.segment_index[(s, li)] = len(self.segments)
+                self.segments.append(rec)
+                self.layer_tensors.append(keep)
+        self.n_tiles = tiles
+        arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
+        self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+
+    def _build_sims(self, beta_tabs, bl_tabs, kins):
+        recs = []
+        ri = rv = rf = bt = bl = kn = 0
+        self.res_slices = []
+        for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
+            p = sp.pars
+            r = L.SimParams()
+            r.agent_off = off
+            r.n_agents = sp.n
+            r.n_variants = sp.nv
+            r.n_layers = len(sp.layers)
+            r.npts = sp.npts
+            seed = int(p['rand_seed']) & 0xFFFFFFFFFFFFFFFF
+            r.key0, r.key1 = seed & 0xFFFFFFFF, seed >> 32
+            r.use_waning = int(bool(p['use_waning']))
+            r.nab_kin_len = len(kins[s])
+            r.n_beds_hosp = -1 if p['n_beds_hosp'] is None else int(p['n_beds_hosp'])
+            r.n_beds_icu = -1 if p['n_beds_icu'] is None else int(p['n_beds_icu'])
+            vd = p['viral_dist']
+            r.frac_time, r.load_ratio, r.high_cap = (np.float32(vd['frac_time']), np.float32(vd['load_ratio']),
+                                                     np.float32(vd['high_cap']))
+            r.asymp_factor = np.float32(p['asymp_factor'])
+            r.trans_redux = np.float32(p['trans_redux'])
+            r.nab_boost = np.float32(p['nab_boost'])
+            r.no_hosp_factor = np.float32(p['no_hosp_factor'])
+            r.no_icu_factor = np.float32(p['no_icu_factor'])
+            for v in range(sp.nv):  # people.py:475-480
+                label = p['variant_map'][v]
+                vals = {}
+                for k in ('rel_symp_prob', 'rel_severe_prob', 'rel_crit_prob', 'rel_death_prob'):
+                    x = p[k]
+                    if v:
+                        x *= p['variant_pars'][label][k]
+                    vals[k] = np.float32(x)
+                r.rel_symp[v], r.rel_severe[v] = vals['rel_symp_prob'], vals['rel_severe_prob']
+                r.rel_crit[v], r.rel_death[v] = vals['rel_crit_prob'], vals['rel_death_prob']
+            imm = p.get('immunity')
+            if imm is not None:
+                imm = np.asarray(imm, dtype=np.float32)
+                for a in range(sp.nv):
+                    for b in range(sp.nv):
+                        r.immunity[a * L.MAX_VARIANTS + b] = imm[a, b]
+            ris = p['rel_imm_symp']
+            r.rel_imm_asymp, r.rel_imm_mild, r.rel_imm_severe = float(ris['asymp']), float(ris['mild']), float(ris['severe'])
+            ne = p['nab_eff']
+            r.nab_norm = 1 + ne['alpha_inf_diff']
+            for j, (a, b) in enumerate([('alpha_inf', 'beta_inf'), ('alpha_symp_inf', 'beta_symp_inf'),
+                                        ('alpha_sev_symp', 'beta_sev_symp')]):
+                r.ve_exp_alpha[j] = float(np.exp(ne[a]))   # immunity.py:245
+                r.ve_beta[j] = float(ne[b])
+            for j, key in enumerate(L.DUR_ORDER):
+                r.dur[j] = dur_par(p['dur'][key])
+            nab_init = p['nab_init']
+            r.nab_init = dur_par(nab_init) if nab_init is not None else L.DurPar(L.DIST_ZERO, 0, 0.0, 0.0)
+            r.nab_kin = self.nab_kin.data_ptr() + 8 * kn
+            r.beta_tab = self.beta_tab.data_ptr() + 4 * bt
+            r.beta_layer_tab = self.beta_layer_tab.data_ptr() + 4 * bl
+            r.vx_imm = None
+            r.n_vaccines = 0
+            r.res_int = self.res_int.data_ptr() + 8 * ri
+            r.res_var = self.res_var.data_ptr() + 8 * rv
+            r.res_fx = self.res_fx.data_ptr() + 8 * rf
+            self.res_slices.append((ri, rv, rf))
+            ri += sp.npts * L.N_RES_INT
+            rv += sp.npts * L.N_RES_VAR * sp.nv
+            rf += sp.npts * L.N_RES_F
+            bt += len(beta_tabs[s])
+            bl += len(bl_tabs[s])
+            kn += len(kins[s])
+            recs.append(r)
+        arr = (L.SimParams * len(recs))(*recs)
+        self.sim_recs = recs
+        self.sims_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+
+    def _build_agent_blocks(self):
+        dt = np.dtype([('begin', '<i8'), ('end', '<i8'), ('sim', '<i4'), ('_pad', '<i4')])
+        parts = []
+        for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
+            nb = (sp.n + L.AGENT_BLOCK - 1) // L.AGENT_BLOCK
+            b = np.zeros(nb, dtype=dt)
+            b['begin'] = off + np.arange(nb, dtype=np.int64) * L.AGENT_BLOCK
+            b['end'] = np.minimum(b['begin'] + L.AGENT_BLOCK, off + sp.n)
+            b['sim'] = s
+            parts.append(b)
+        blocks = np.concatenate(parts)
+        self.n_agent_blocks = len(blocks)
+        self.blocks_dev = torch.from_numpy(blocks.view(np.uint8).copy()).to(self.device)
+
+    def _refresh_state(self):
+        t = self.t
+        st = L.State()
+        st.n = self.n
+        st.n_sims = len(self.specs)
+        st.n_segments = len(self.segments)
+        st.n_tiles = self.n_tiles
+        st.n_agent_blocks = self.n_agent_blocks
+        for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
+                  'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
+                  'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'events', 'event_count',
+                  'log_count', 'status'):
+            setattr(st, k, t[k].data_ptr())
+        st.imm_stride_variants = self.nv_max
+        st.event_capacity = self.event_capacity
+        st.log = t['log'].data_ptr() if self.log_enabled else None
+        st.log_capacity = self.log_capacity
+        st.hospicu = self.hospicu.data_ptr() if self.hospicu is not None else None
+        st.sims = self.sims_dev.data_ptr()
+        st.segments = self.seg_dev.data_ptr() if self.segments else None
+        st.agent_blocks = self.blocks_dev.data_ptr()
+        st.draw_table = self.draw_table.data_ptr() if self.draw_table is not None else None
+        if self.edge_uniform_tensors is not None:
+            ptrs = np.array([u.data_ptr() for u in self.edge_uniform_tensors], dtype=np.uint64)
+            self._eu_ptrs = torch.from_numpy(ptrs.view(np.int64)).to(self.device)
+            st.edge_uniforms = self._eu_ptrs.data_ptr()
+        else:
+            st.edge_uniforms = None
+        self.cstate = st
+        self.cstate_ptr = C.pointer(self.cstate)
+
+    # ------------------------------------------------------------------ test hooks
+    def set_draw_table(self, table):
+        """Inject per-agent infection draws [n, N_DRAWS] (global index); None returns to Philox."""
+        self.draw_table = None if table is None else torch.as_tensor(table, dtype=F64, device=self.device).contiguous()
+        self._refresh_state()
+
+    def set_edge_uniforms(self, per_segment):
+        """Inject edge uniforms: list (one per segment) of float64 [n_variants, 2, n_edges] indexed by
+        (source variant, direction, edge); None returns to Philox."""
+        if per_segment is None:
+            self.edge_uniform_tensors = None
+        else:
+            self.edge_uniform_tensors = [torch.as_tensor(u, dtype=F64, device=self.device).contiguous()
+                                         for u in per_segment]
+        self._refresh_state()
+
+    def set_hospicu(self, flags):
+        """Force hosp_max/icu_max per sim ([n_sims, 2] ints); None: from the day's counts."""
+        self.hospicu = None if flags is None else torch.as_tensor(np.asarray(flags, dtype=np.int32).ravel(),
+                                                                  device=self.device)
+        self._refresh_state()
+
+    # ------------------------------------------------------------------ kernels
+    def agent_step(self, t, do_prev=True, do_day=True):
+        L.call('covgpu_agent_step', self.cstate_ptr, int(t), int(do_prev), int(do_day), _stream())
+
+    def edge_pass(self, t):
+        L.call('covgpu_edge_pass', self.cstate_ptr, int(t), _stream())
+
+    def infect_claims(self, t):
+        L.call('covgpu_infect_claims', self.cstate_ptr, int(t), _stream())
+
+    def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=1):
+        """Infect explicit agents of one sim (local indices; deduplicated and sorted here)."""
+        inds = np.unique(np.asarray(inds, dtype=np.int64))
+        if len(inds) == 0:
+            return
+        if inds.min() < 0 or inds.max() >= self.specs[sim].n:
+            raise IndexError('agent index out of range')
+        g = torch.from_numpy((inds + self.offsets[sim]).astype(np.int32)).to(self.device)
+        self._keep_inds = g
+        L.call('covgpu_infect_list', self.cstate_ptr, int(t), g.data_ptr(), len(inds), int(sim), int(variant),
+               int(layer_tag), int(call_tag), _stream())
+
+    def run_days(self, t0, t1, open_prev=False, close_last=True, use_graph=True):
+        L.call('covgpu_run_days', self.cstate_ptr, int(t0), int(t1), int(open_prev), int(close_last), int(use_graph),
+               _stream())
+
+    def materialize_layer(self, sim, layer, t):
+        """Endpoints of a dynamic layer on day t (local indices)."""
+        seg = self.segment_index[(sim, layer)]
+        n_edges = self.segments[seg].n_edges
+        p1 = torch.empty(n_edges, dtype=I32, device=self.device)
+        p2 = torch.empty(n_edges, dtype=I32, device=self.device)
+        L.call('covgpu_layer_materialize', self.cstate_ptr, int(seg), int(t), p1.data_ptr(), p2.data_ptr(),
+               _stream())
+        return p1, p2
+
+    def status(self):
+        return int(self.t['status'].item())
+
+    def clear_status(self):
+        self.t['status'].zero_()
+
+    # ------------------------------------------------------------------ accessors
+    def sl(self, sim):
+        off = self.offsets[sim]
+        return slice(off, off + self.specs[sim].n)
+
+    def flag(self, key, sim=0):
+        bit = STATE_BIT[key]
+        return ((self.t['flags'][self.sl(sim)] >> bit) & 1).bool()
+
+    def by_variant(self, key, sim=0):
+        shift = cvd.EXPOSED_BY_VARIANT_SHIFT if key == 'exposed_by_variant' else cvd.INFECTIOUS_BY_VARIANT_SHIFT
+        f = self.t['flags'][self.sl(sim)]
+        return torch.stack([((f >> (shift + v)) & 1).bool() for v in range(self.specs[sim].nv)])
+
+    def variant_field(self, key, sim=0):
+        shift = 8 * cvd.VARIANT_STATES.index(key)
+        b = (self.t['vstate'][self.sl(sim)] >> shift) & 0xFF
+        out = b.to(F32)
+        out[b == L.NO_VARIANT] = float('nan')
+        return out
+
+    def get(self, key, sim=0):
+        """One of the reference's People keys for one sim, as a torch tensor on the device."""
+        s = self.sl(sim)
+        if key in STATE_BIT:
+            return self.flag(key, sim)
+        if key in cvd.BY_VARIANT_STATES:
+            return self.by_variant(key, sim)
+        if key in cvd.VARIANT_STATES:
+            return self.variant_field(key, sim)
+        if key in cvd.DATES:
+            return self.t['dates'][cvd.DATES.index(key), s]
+        if key in cvd.DURS:
+            return self.t['durs'][cvd.DURS.index(key), s]
+        if key in cvd.IMM_STATES:
+            return self.t[key][:self.specs[sim].nv, s]
+        if key in self.t:
+            return self.t[key][s]
+        if key == 'uid':
+            return torch.arange(self.specs[sim].n, dtype=I32, device=self.device)
+        if key == 'doses':
+            return torch.zeros(self.specs[sim].n, dtype=I32, device=self.device)
+        raise KeyError(f'Key "{key}" is not a valid attribute of people')
+
+    def set(self, key, values, sim=0):
+        """Write one of the reference's People keys for one sim (host or device values)."""
+        s = self.sl(sim)
+        if key in STATE_BIT:
+            bit = 1 << STATE_BIT[key]
+            v = torch.as_tensor(np.asarray(values, dtype=bool) if not torch.is_tensor(values) else values,
+                                device=self.device).to(torch.int32)
+            f = self.t['flags'][s]
+            f.copy_((f & ~bit) | (v * bit))
+        elif key in cvd.BY_VARIANT_STATES:
+            shift = cvd.EXPOSED_BY_VARIANT_SHIFT if key == 'exposed_by_variant' else cvd.INFECTIOUS_BY_VARIANT_SHIFT
+            vals = torch.as_tensor(np.asarray(values, dtype=bool), device=self.device).to(torch.int32)
+            f = self.t['flags'][s]
+            for v in range(vals.shape[0]):
+                bit = 1 << (shift + v)
+                f.copy_((f & ~bit) | (vals[v] * bit))
+        elif key in cvd.VARIANT_STATES:
+            shift = 8 * cvd.VARIANT_STATES.index(key)
+            x = np.asarray(values, dtype=np.float64)
+            b = np.where(np.isnan(x), L.NO_VARIANT, np.nan_to_num(x)).astype(np.int32)
+            bt = torch.from_numpy(b).to(self.device)
+            vs = self.t['vstate'][s]
+            vs.copy_((vs & ~(0xFF << shift)) | (bt << shift))
+        elif key in cvd.DATES:
+            self.t['dates'][cvd.DATES.index(key), s].copy_(torch.as_tensor(np.asarray(values, np.float32)))
+        elif key in cvd.DURS:
+            self.t['durs'][cvd.DURS.index(key), s].copy_(torch.as_tensor(np.asarray(values, np.float32)))
+        elif key in cvd.IMM_STATES:
+            self.t[key][:self.specs[sim].nv, s].copy_(torch.as_tensor(np.asarray(values, np.float32)))
+        elif key in self.t and key not in ('roles', 'claim', 'events', 'log', 'status'):
+            dst = self.t[key][s]
+            dst.copy_(torch.as_tensor(np.asarray(values), dtype=dst.dtype))
+        else:
+            raise KeyError(f'Key "{key}" cannot be set')
+
+    def results(self, sim=0):
+        """Per-day results of one sim as float64 numpy arrays, keyed like sim.results."""
+        sp = self.specs[sim]
+        ri, rv, rf = self.res_slices[sim]
+        npts, nv = sp.npts, sp.nv
+        ints = self.res_int[ri:ri + npts * L.N_RES_INT].view(npts, L.N_RES_INT).cpu().numpy().astype(np.float64)
+        var = self.res_var[rv:rv + npts * L.N_RES_VAR * nv].view(npts, L.N_RES_VAR, nv).cpu().numpy().astype(np.float64)
+        fx = self.res_fx[rf:rf + npts * L.N_RES_F].view(npts, L.N_RES_F).cpu().numpy()
+        out = {}
+        for k, key in enumerate(cvd.RES_INT_KEYS):
+            out[key] = ints[:, k]
+        out['_severe_now'] = ints[:, L.RES_SEVERE_NOW]
+        out['_critical_now'] = ints[:, L.RES_CRITICAL_NOW]
+        for k, key in enumerate(cvd.RES_VAR_KEYS):
+            out[key] = var[:, k, :].T.copy()
+        n_alive = sp.n - out['n_dead']
+        out['pop_nabs'] = np.ldexp(fx[:, 0].astype(np.float64), -L.FX_NAB_BITS) / n_alive
+        denom = nv * sp.n
+        out['pop_protection'] = np.ldexp(fx[:, 1].astype(np.float64), -L.FX_IMM_BITS) / denom
+        out['pop_symp_protection'] = np.ldexp(fx[:, 2].astype(np.float64), -L.FX_IMM_BITS) / denom
+        return out
+
+    def infection_log(self, sim=None):
+        """Infection-log records (source, target, date, layer index, variant), sorted like the reference's."""
+        if not self.log_enabled:
+            return np.zeros((0, 5), dtype=np.int64)
+        n = min(int(self.t['log_count'].item()), self.log_capacity)
+        rec = self.t['log'][:n].cpu().numpy().astype(np.int64)
+        out = np.stack([rec[:, 0], rec[:, 1], rec[:, 2], rec[:, 3] & 0xFF, (rec[:, 3] >> 8) & 0xFF,
+                        rec[:, 3] >> 16], axis=1)
+        if sim is not None:
+            out = out[out[:, 5] == sim]
+        # the reference appends per infect() call: by day, variant, layer, then target
+        order = np.lexsort((out[:, 1], out[:, 3], out[:, 4], out[:, 2], out[:, 5]))
+        return out[order, :5]

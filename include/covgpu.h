@@ -1,0 +1,280 @@
+/*
+ * covgpu.h -- C ABI of the GB300 (sm_103a) implementation of Covasim 3.1.7's
+ * per-day step hot path.
+ *
+ * Every entry point takes device pointers, sizes and a cudaStream_t (passed
+ * as void*), enqueues work on that stream, never synchronises unless stated,
+ * never frees caller memory and returns an int status (COVGPU_*); no entry
+ * point traps or asserts on the device. Data-dependent failures found on the
+ * device (buffer overflow) are reported in a device status word that the
+ * caller reads back when convenient.
+ *
+ * Reference interfaces replaced (paths inside the Covasim source tree):
+ *   covgpu_viral_load        covasim/utils.py:38-79   compute_viral_load
+ *   covgpu_trans_sus         covasim/utils.py:81-90   compute_trans_sus
+ *   covgpu_infections        covasim/utils.py:92-128  compute_infections
+ *   covgpu_agent_step        covasim/people.py:164-186 update_states_pre (+ the checks at
+ *                            people.py:211-312,368-374), covasim/immunity.py:303-350
+ *                            check_immunity, immunity.py:205-213 update_nab and the
+ *                            per-day counts of covasim/sim.py:651-674
+ *   covgpu_edge_pass         covasim/sim.py:601-649: viral load + compute_trans_sus +
+ *                            compute_infections over every variant and layer, with the
+ *                            dynamic-layer resampling of covasim/base.py:1849-1876
+ *   covgpu_infect_claims     covasim/people.py:435-586 infect (+ immunity.py:138-202
+ *                            update_peak_nab) for the day's transmissions
+ *   covgpu_infect_list       covasim/people.py:435-586 infect for an explicit index list
+ *                            (seed infections, sim.py:505-532; importations)
+ *   covgpu_layer_materialize covasim/base.py:1849-1876 Layer.update (dynamic layer view)
+ */
+#ifndef COVGPU_H
+#define COVGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define COVGPU_OK          0
+#define COVGPU_OVERFLOW    1   /* a fixed-capacity device buffer was too small */
+#define COVGPU_TIMEOUT     2   /* a bounded device wait gave up                */
+#define COVGPU_BADARG      3   /* rejected on the host before any launch       */
+#define COVGPU_CUDA_ERROR  4   /* a CUDA runtime call failed                   */
+
+/* ---- limits ------------------------------------------------------------ */
+#define COVGPU_MAX_VARIANTS 8
+#define COVGPU_MAX_LAYERS   16
+#define COVGPU_N_DATES      19
+#define COVGPU_N_DURS       5
+#define COVGPU_N_DRAWS      10  /* draws consumed by one infection (see covgpu_infect_*) */
+
+/* ---- packed per-agent state word (bit i of flags) ---------------------- */
+/* bits 0..15 are defaults.py:59-76 in order: susceptible, naive, exposed,
+ * infectious, symptomatic, severe, critical, tested, diagnosed, recovered,
+ * known_dead, dead, known_contact, quarantined, isolated, vaccinated;
+ * bits 16..23 exposed_by_variant[v]; bits 24..31 infectious_by_variant[v]. */
+#define COVGPU_NO_VARIANT 0xFFu  /* byte value of an undefined variant field */
+
+/* date block rows (index into dates[COVGPU_N_DATES][n]) */
+enum {
+  COVGPU_DATE_SUSCEPTIBLE = 0, COVGPU_DATE_NAIVE, COVGPU_DATE_EXPOSED, COVGPU_DATE_INFECTIOUS,
+  COVGPU_DATE_SYMPTOMATIC, COVGPU_DATE_SEVERE, COVGPU_DATE_CRITICAL, COVGPU_DATE_TESTED,
+  COVGPU_DATE_DIAGNOSED, COVGPU_DATE_RECOVERED, COVGPU_DATE_KNOWN_DEAD, COVGPU_DATE_DEAD,
+  COVGPU_DATE_KNOWN_CONTACT, COVGPU_DATE_QUARANTINED, COVGPU_DATE_ISOLATED,
+  COVGPU_DATE_VACCINATED, COVGPU_DATE_POS_TEST, COVGPU_DATE_END_QUARANTINE,
+  COVGPU_DATE_END_ISOLATION
+};
+enum { COVGPU_DUR_EXP2INF = 0, COVGPU_DUR_INF2SYM, COVGPU_DUR_SYM2SEV, COVGPU_DUR_SEV2CRIT,
+       COVGPU_DUR_DISEASE };
+
+/* duration distributions (utils.py:156-236 sample(), one standard normal per draw) */
+enum { COVGPU_DIST_LOGNORMAL_INT = 0, COVGPU_DIST_LOGNORMAL, COVGPU_DIST_NORMAL,
+       COVGPU_DIST_NORMAL_INT, COVGPU_DIST_NORMAL_POS, COVGPU_DIST_ZERO };
+/* order of the nine duration parameters in covgpu_sim_params.dur */
+enum { COVGPU_D_EXP2INF = 0, COVGPU_D_INF2SYM, COVGPU_D_SYM2SEV, COVGPU_D_SEV2CRIT,
+       COVGPU_D_ASYM2REC, COVGPU_D_MILD2REC, COVGPU_D_SEV2REC, COVGPU_D_CRIT2REC,
+       COVGPU_D_CRIT2DIE, COVGPU_N_DUR_PARS };
+
+/* per-sim-day integer results: the 15 flows of defaults.py:167-183, then the
+ * 13 stocks of defaults.py:145-159, then the severe/critical counts seen by
+ * infect() that day (sim.py:579-580) */
+#define COVGPU_N_RES_INT 30
+#define COVGPU_RES_SEVERE_NOW 28
+#define COVGPU_RES_CRITICAL_NOW 29
+/* per-sim-day-variant integer results: 4 variant flows (defaults.py:185-190),
+ * then the 2 by-variant stocks (defaults.py:160-163) */
+#define COVGPU_N_RES_VAR 6
+/* per-sim-day float sums, as signed 64-bit fixed point (integer atomics make
+ * them independent of block order, so every run gives the same bits): sum of
+ * NAbs of the living (sim.py:672) scaled by 2^24, sums of sus_imm and of
+ * symp_imm over [nv, n] (sim.py:673-674) scaled by 2^32; the host divides */
+#define COVGPU_N_RES_F 3
+#define COVGPU_FX_NAB_BITS 24
+#define COVGPU_FX_IMM_BITS 32
+
+/* ---- device-side descriptors ------------------------------------------- */
+typedef struct covgpu_dur_par { int32_t code; int32_t _pad; double a; double b; } covgpu_dur_par;
+
+/* One sim's parameter block (device memory, one entry per sim). */
+typedef struct covgpu_sim_params {
+  int64_t agent_off;          /* first global agent index (multiple of 32)          */
+  int32_t n_agents;
+  int32_t n_variants;
+  int32_t n_layers;
+  int32_t npts;               /* days + 1                                           */
+  uint32_t key0, key1;        /* Philox key (64-bit seed)                           */
+  int32_t use_waning;
+  int32_t nab_kin_len;
+  int64_t n_beds_hosp;        /* -1: unconstrained                                  */
+  int64_t n_beds_icu;
+  float frac_time, load_ratio, high_cap, asymp_factor;
+  float trans_redux, nab_boost, no_hosp_factor, no_icu_factor;
+  float rel_symp[COVGPU_MAX_VARIANTS], rel_severe[COVGPU_MAX_VARIANTS];
+  float rel_crit[COVGPU_MAX_VARIANTS], rel_death[COVGPU_MAX_VARIANTS];
+  float immunity[COVGPU_MAX_VARIANTS * COVGPU_MAX_VARIANTS]; /* [variant][recovered_variant] */
+  double rel_imm_asymp, rel_imm_mild, rel_imm_severe, nab_norm; /* nab_norm = 1 + alpha_inf_diff */
+  double ve_exp_alpha[3], ve_beta[3];                         /* sus, symp, sev              */
+  covgpu_dur_par dur[COVGPU_N_DUR_PARS];
+  covgpu_dur_par nab_init;
+  const double* nab_kin;          /* [nab_kin_len]                                   */
+  const float* beta_tab;          /* [npts][n_variants] float32 beta per day/variant */
+  const float* beta_layer_tab;    /* [npts][n_layers]                                */
+  const float* vx_imm;            /* [n_vaccines][n_variants] or NULL                */
+  int32_t n_vaccines;
+  int32_t _pad2;
+  int64_t* res_int;               /* [npts][COVGPU_N_RES_INT]                        */
+  int64_t* res_var;               /* [npts][COVGPU_N_RES_VAR][n_variants]            */
+  int64_t* res_fx;                /* [npts][COVGPU_N_RES_F] fixed-point sums         */
+} covgpu_sim_params;
+
+/* One contact layer of one sim (device memory, one entry per layer segment). */
+typedef struct covgpu_layer {
+  const int32_t* p1;              /* global agent indices, sorted ascending (static) */
+  const int32_t* p2;
+  const float* beta;              /* per-edge beta, or NULL: every edge has beta_const */
+  int64_t n_edges;
+  int64_t tile_begin;             /* first edge-pass tile of this segment            */
+  int32_t sim;
+  int32_t layer;                  /* layer index within the sim (0..n_layers-1)      */
+  int32_t dynamic;                /* 1: edges redrawn every day (p1/p2 unused)       */
+  float beta_const;
+  float iso_factor, quar_factor;
+  int32_t _pad;
+} covgpu_layer;
+
+/* One agent block of the agent kernel: agents [begin, end) of one sim. */
+typedef struct covgpu_agent_block { int64_t begin; int64_t end; int32_t sim; int32_t _pad; } covgpu_agent_block;
+
+/* One transmission event recorded by the edge pass. */
+typedef struct covgpu_event { uint64_t key; int32_t target; int32_t source; } covgpu_event;
+
+/* One infection-log record (people.py:508-511): local source (-1 for seed
+ * infections and importations) and target, day, and layer | variant << 8 | sim << 16. */
+typedef struct covgpu_log_rec { int32_t source; int32_t target; int32_t day; int32_t layer_variant; } covgpu_log_rec;
+
+/* Everything the fused kernels touch. Host struct; the library copies it into
+ * kernel parameters. All pointers are device pointers. */
+typedef struct covgpu_state {
+  int64_t n;                      /* global agents, including 32-alignment padding  */
+  int32_t n_sims;
+  int32_t n_segments;             /* layer segments over all sims                   */
+  int64_t n_tiles;                /* edge-pass tiles over all segments              */
+  int64_t n_agent_blocks;
+  /* per-agent state */
+  uint32_t* flags;
+  uint32_t* vstate;               /* bytes: exposed, infectious, recovered variant   */
+  float* symp_prob; float* severe_prob; float* crit_prob; float* death_prob;
+  float* rel_trans; float* rel_sus;
+  int32_t* n_infections; int32_t* n_breakthroughs;
+  float* peak_nab; float* nab; int32_t* t_nab_event;
+  int32_t* vaccine_source;
+  float* sus_imm; float* symp_imm; float* sev_imm;   /* [n_variants_max][n]           */
+  int32_t imm_stride_variants;    /* rows of the imm blocks (max variants over sims) */
+  int32_t _pad0;
+  float* dates;                   /* [COVGPU_N_DATES][n]                             */
+  float* durs;                    /* [COVGPU_N_DURS][n]                              */
+  /* per-day working buffers */
+  float* viral_load;              /* [n]                                             */
+  uint32_t* roles;                /* [2 * ceil(n/32)]: source word, target word      */
+  uint64_t* claim;                /* [n] first-infector claim (day-tagged)           */
+  covgpu_event* events;           /* [event_capacity]                                */
+  int64_t event_capacity;
+  unsigned long long* event_count;/* device counter                                  */
+  covgpu_log_rec* log;            /* [log_capacity] or NULL                          */
+  int64_t log_capacity;
+  unsigned long long* log_count;
+  int32_t* status;                /* device status word (COVGPU_OVERFLOW ...)        */
+  const int32_t* hospicu;         /* optional [2 * n_sims] forced hosp_max / icu_max;
+                                     NULL: from the day's severe/critical counts     */
+  /* descriptors */
+  const covgpu_sim_params* sims;  /* [n_sims]                                        */
+  const covgpu_layer* segments;   /* [n_segments]                                    */
+  const covgpu_agent_block* agent_blocks; /* [n_agent_blocks]                        */
+  /* test mode: per-agent injected draws [n][COVGPU_N_DRAWS] (NULL: Philox) and
+   * injected edge uniforms (NULL: Philox), per segment a [n_variants][2][n_edges]
+   * table indexed by (source variant, direction, edge) */
+  const double* draw_table;
+  const double* const* edge_uniforms; /* [n_segments] -> [n_variants][2][n_edges] */
+} covgpu_state;
+
+/* ---- standalone kernels: the reference's numba functions ----------------- */
+
+/* compute_viral_load (utils.py:38-79). float32 arithmetic as numba types it. */
+int covgpu_viral_load(int32_t t, const float* date_inf, const float* date_rec, const float* date_dead,
+                      int64_t n, float frac_time, float load_ratio, float high_cap,
+                      float* out_load, void* stream);
+
+/* compute_trans_sus (utils.py:81-90). Booleans as one byte per agent. */
+int covgpu_trans_sus(const float* rel_trans, const float* rel_sus, const uint8_t* inf, const uint8_t* sus,
+                     float beta_layer, const float* viral_load, const uint8_t* symp, const uint8_t* iso,
+                     const uint8_t* quar, float asymp_factor, float iso_factor, float quar_factor,
+                     const float* immunity_factors, int64_t n, float* out_rel_trans, float* out_rel_sus,
+                     void* stream);
+
+/* compute_infections (utils.py:92-128, non-legacy). Output order is the
+ * reference's: direction p1->p2 in edge order, then p2->p1 in edge order.
+ * uniforms: [2][n_edges] float64 draws per (direction, edge), or NULL to
+ * draw from Philox keyed (seed, day, variant, layer, edge). *out_count
+ * (device) receives the number of transmissions; if it exceeds capacity only
+ * the first capacity are written and COVGPU_OVERFLOW is stored in *status.
+ * scratch: device memory of covgpu_infections_scratch_bytes(n_edges) bytes. */
+int64_t covgpu_infections_scratch_bytes(int64_t n_edges);
+int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas,
+                      int64_t n_edges, const float* rel_trans, const float* rel_sus,
+                      const double* uniforms, uint64_t seed, int32_t day, int32_t variant, int32_t layer,
+                      int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
+                      int32_t* status, void* scratch, int64_t scratch_bytes, void* stream);
+
+/* ---- fused per-day kernels over a batch of sims ------------------------- */
+
+/* One dense pass over every agent of every sim. With do_prev, first closes
+ * day t-1 (stock counts, update_nab, NAb sum); with do_day, then runs day t's
+ * update_states_pre (all checks, in the reference's order), check_immunity,
+ * the flow counts, the viral load of the infectious and the source/target
+ * role bitmaps the edge pass reads. Also resets the day's event counter. */
+int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_t do_day, void* stream);
+
+/* Transmission over every layer segment and variant: both directions of each
+ * edge from one read, Bernoulli draws from Philox (or st->edge_uniforms),
+ * events appended to st->events and the first infector of each target
+ * claimed with a 64-bit atomicMin on (day, variant, layer, direction, edge). */
+int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream);
+
+/* infect() for the winning event of each target. */
+int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
+
+/* infect() for an explicit list of global agent indices (unique). layer_tag is
+ * recorded in the infection log (>= COVGPU_MAX_LAYERS for non-layer sources);
+ * call_tag selects the Philox stream (1: seed infections, 2: importations). */
+int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds,
+                       int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream);
+
+/* Write the day-t endpoints of one dynamic layer segment into p1/p2 (the
+ * same edges the edge pass draws that day). */
+int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t, int32_t* p1, int32_t* p2,
+                             void* stream);
+
+/* Run days [t0, t1) of every sim: per day agent_step, edge_pass,
+ * infect_claims. open_prev: day t0-1 still needs its closing pass (stocks,
+ * update_nab), which day t0's agent pass then does first; close_last: end
+ * with the closing pass of day t1-1. With use_graph the whole sequence is
+ * captured once into a CUDA graph and launched (a capture is reused while
+ * the state and the arguments are unchanged). */
+int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open_prev, int32_t close_last,
+                    int32_t use_graph, void* stream);
+
+/* Library/ABI version. */
+int covgpu_version(void);
+
+/* ABI layout check (no device work): writes up to n values: sizeof of
+ * covgpu_sim_params, covgpu_layer, covgpu_agent_block, covgpu_event,
+ * covgpu_log_rec, covgpu_state, then the offsets of covgpu_state.sims,
+ * covgpu_state.edge_uniforms and covgpu_sim_params.res_fx. Returns the number
+ * of values available. */
+int covgpu_abi_layout(int64_t* out, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COVGPU_H */

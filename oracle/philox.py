@@ -1,0 +1,149 @@
+"""Philox-4x32-10 counter-based generator in numpy, plus the draw conversions.
+
+TEST INFRASTRUCTURE ONLY (part of the CPU oracle): the CUDA library implements
+the same generator and the same conversions, so that the oracle run in
+"philox" mode reproduces a GPU simulation draw for draw.
+
+Philox-4x32-10 is the published generator of Salmon et al., "Parallel random
+numbers: as easy as 1, 2, 3" (SC'11). Round function, multipliers and Weyl key
+increments follow that paper.
+
+Stream layout (shared with the CUDA side; all words little-endian uint32):
+
+  key     = (seed_lo, seed_hi)                        64-bit per-sim seed
+  counter = (c0, c1, c2, c3)
+    edge Bernoulli      : (edge_lo, edge_hi, day, TAG_EDGE  | variant << 8 | layer)
+    dynamic-layer edges : (edge_lo, edge_hi, day, TAG_LAYER | layer)
+    infect draws        : (agent,   block,   day, TAG_INFECT | call_tag)
+
+Draw conversions:
+  u52(a, b)  = ((a >> 6) << 26 | (b >> 6)) ... see ``u01_52``: exact doubles in (0, 1)
+  u32(a)     = (a + 0.5) * 2**-32, exact double in (0, 1)
+  Box-Muller = sqrt(-2 ln u1) * (cos 2 pi u2, sin 2 pi u2)
+"""
+import numpy as np
+
+PHILOX_M0 = np.uint64(0xD2511F53)
+PHILOX_M1 = np.uint64(0xCD9E8D57)
+PHILOX_W0 = np.uint32(0x9E3779B9)
+PHILOX_W1 = np.uint32(0xBB67AE85)
+
+TAG_EDGE = 0x01000000
+TAG_LAYER = 0x02000000
+TAG_INFECT = 0x03000000
+
+_MASK32 = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32_10(c0, c1, c2, c3, k0, k1):
+    """Vectorised Philox-4x32-10. All inputs broadcast; returns 4 uint32 arrays."""
+    c0 = np.asarray(c0, dtype=np.uint32).astype(np.uint64)
+    c1 = np.asarray(c1, dtype=np.uint32).astype(np.uint64)
+    c2 = np.asarray(c2, dtype=np.uint32).astype(np.uint64)
+    c3 = np.asarray(c3, dtype=np.uint32).astype(np.uint64)
+    c0, c1, c2, c3 = np.broadcast_arrays(c0, c1, c2, c3)
+    k0 = np.uint64(np.uint32(k0))
+    k1 = np.uint64(np.uint32(k1))
+    w0 = np.uint64(PHILOX_W0)
+    w1 = np.uint64(PHILOX_W1)
+    for r in range(10):
+        if r:
+            k0 = (k0 + w0) & _MASK32
+            k1 = (k1 + w1) & _MASK32
+        p0 = PHILOX_M0 * c0
+        p1 = PHILOX_M1 * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & _MASK32
+        hi1, lo1 = p1 >> np.uint64(32), p1 & _MASK32
+        c0, c1, c2, c3 = hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0
+    return (c0.astype(np.uint32), c1.astype(np.uint32),
+            c2.astype(np.uint32), c3.astype(np.uint32))
+
+
+def seed_key(seed):
+    """Split a (non-negative) integer seed into the two 32-bit key words."""
+    s = int(seed) & 0xFFFFFFFFFFFFFFFF
+    return s & 0xFFFFFFFF, s >> 32
+
+
+def u01_52(a, b):
+    """Exact double in (0, 1) from two words: (k + 0.5) * 2**-52, k = 52 random bits."""
+    a = np.asarray(a, dtype=np.uint64)
+    b = np.asarray(b, dtype=np.uint64)
+    k = ((a >> np.uint64(6)) << np.uint64(26)) | (b >> np.uint64(6))
+    return (k.astype(np.float64) + 0.5) * (2.0 ** -52)
+
+
+def u01_32(a):
+    """Exact double in (0, 1) from one word: (a + 0.5) * 2**-32."""
+    return (np.asarray(a, dtype=np.uint32).astype(np.float64) + 0.5) * (2.0 ** -32)
+
+
+def box_muller(w_a, w_b):
+    """Two standard normals from two words (32-bit uniforms)."""
+    u1 = u01_32(w_a)
+    u2 = u01_32(w_b)
+    r = np.sqrt(-2.0 * np.log(u1))
+    th = 2.0 * np.pi * u2
+    return r * np.cos(th), r * np.sin(th)
+
+
+def uniform_index(a, b, n):
+    """Uniform integer in [0, n) from a 64-bit word pair: floor(x * n / 2**64)."""
+    a = np.asarray(a, dtype=np.uint64)
+    b = np.asarray(b, dtype=np.uint64)
+    n = np.uint64(n)
+    # 64x64 -> high 64 bits, computed from 32-bit halves (x = a<<32 | b).
+    n_lo = n & _MASK32
+    n_hi = n >> np.uint64(32)
+    t0 = b * n_lo
+    t1 = a * n_lo + (t0 >> np.uint64(32))
+    t2 = b * n_hi + (t1 & _MASK32)
+    hi = a * n_hi + (t1 >> np.uint64(32)) + (t2 >> np.uint64(32))
+    return hi.astype(np.int64)
+
+
+def edge_uniforms(k0, k1, day, layer, variant, edges):
+    """Per-edge Bernoulli uniforms for both directions: (u_dir0, u_dir1)."""
+    e = np.asarray(edges, dtype=np.int64)
+    w = philox4x32_10(e & 0xFFFFFFFF, e >> 32, day,
+                      TAG_EDGE | (int(variant) << 8) | int(layer), k0, k1)
+    return u01_52(w[0], w[1]), u01_52(w[2], w[3])
+
+
+def dynamic_edges(k0, k1, day, layer, n_edges, n_agents):
+    """Endpoints of a dynamic layer on one day: n_edges i.i.d. uniform pairs."""
+    e = np.arange(n_edges, dtype=np.int64)
+    w = philox4x32_10(e & 0xFFFFFFFF, e >> 32, day, TAG_LAYER | int(layer), k0, k1)
+    p1 = uniform_index(w[0], w[1], n_agents)
+    p2 = uniform_index(w[2], w[3], n_agents)
+    return p1.astype(np.int32), p2.astype(np.int32)
+
+
+# Slots of the per-infection draw table (shared with the CUDA side).
+N_EXP2INF, N_INF2SYM, N_SYM2SEV, N_SEV2CRIT, N_FINAL, N_NAB = 0, 1, 2, 3, 4, 5
+U_SYMP, U_SEV, U_CRIT, U_DEATH = 6, 7, 8, 9
+N_DRAWS = 10
+
+
+def infect_draws(k0, k1, day, call_tag, agents):
+    """The ten draws one infection consumes, as a float64 table [n, 10].
+
+    Three Philox blocks per agent: block 0 gives the normals for exp2inf,
+    inf2sym, sym2sev, sev2crit; block 1 the normals for the final duration and
+    the initial NAb level plus the symptomatic and severe uniforms; block 2 the
+    critical and death uniforms.
+    """
+    a = np.asarray(agents, dtype=np.int64)
+    tag = TAG_INFECT | int(call_tag)
+    out = np.empty((len(a), N_DRAWS), dtype=np.float64)
+    b0 = philox4x32_10(a, 0, day, tag, k0, k1)
+    b1 = philox4x32_10(a, 1, day, tag, k0, k1)
+    b2 = philox4x32_10(a, 2, day, tag, k0, k1)
+    out[:, N_EXP2INF], out[:, N_INF2SYM] = box_muller(b0[0], b0[1])
+    out[:, N_SYM2SEV], out[:, N_SEV2CRIT] = box_muller(b0[2], b0[3])
+    out[:, N_FINAL], out[:, N_NAB] = box_muller(b1[0], b1[1])
+    out[:, U_SYMP] = u01_32(b1[2])
+    out[:, U_SEV] = u01_32(b1[3])
+    out[:, U_CRIT] = u01_32(b2[0])
+    out[:, U_DEATH] = u01_32(b2[1])
+    return out

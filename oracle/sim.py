@@ -1,0 +1,198 @@
+"""CPU restatement of Covasim 3.1.7's day loop (covasim/sim.py:558-685).
+
+TEST INFRASTRUCTURE ONLY. The product never imports this module; tests and
+the CPU-baseline leg of bench.py do.
+
+Two random-number modes:
+
+* ``rng='philox'``: every draw is keyed exactly like the CUDA library keys it
+  (edge Bernoullis by (seed, day, layer, variant, edge); infection draws by
+  (seed, day, agent, call); dynamic layers by (seed, day, layer, edge)), so a
+  GPU run and this loop agree draw for draw.
+* ``rng='mt'``: two MT19937 streams seeded with the sim's seed, one standing in
+  for numba's (edge Bernoullis, ``choose``/``choose_r``) and one for numpy's
+  (``infect`` and ``set_prognoses``), consumed in the reference's call order.
+"""
+import numpy as np
+
+from . import philox as ph
+from .kernels import compute_viral_load, compute_trans_sus, compute_infections
+from .people import (OraclePeople, TableDraws, SequentialDraws, philox_table, update_nab,
+                     STATES, FLOWS, FLOWS_VARIANT)
+
+F32 = np.float32
+
+RESULT_STOCKS = ['susceptible', 'exposed', 'infectious', 'symptomatic', 'severe', 'critical',
+                 'recovered', 'dead', 'diagnosed', 'known_dead', 'quarantined', 'isolated',
+                 'vaccinated']
+RESULT_STOCKS_BY_VARIANT = ['exposed_by_variant', 'infectious_by_variant']
+
+# call tags of infect() draws in philox mode (shared with the CUDA library)
+CALL_TRANSMISSION = 0
+CALL_SEED = 1
+CALL_IMPORT = 2
+
+SEED_INFECTION_TAG = 0x5EED
+
+
+def choose_seed_infections(seed, n, k):
+    """Agents infected on day 0 in philox mode: a PCG64 stream keyed by the seed."""
+    rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, SEED_INFECTION_TAG]))
+    return np.sort(rng.choice(n, size=int(k), replace=False)).astype(np.int64)
+
+
+def set_prognoses(people, pars, rs):
+    """covasim/people.py:139-161 with draws from ``rs`` (numpy RandomState)."""
+    progs = pars['prognoses']
+    inds = np.digitize(people.age, progs['age_cutoffs']) - 1
+    people.symp_prob[:] = progs['symp_probs'][inds]
+    people.severe_prob[:] = progs['severe_probs'][inds] * progs['comorbidities'][inds]
+    people.crit_prob[:] = progs['crit_probs'][inds]
+    people.death_prob[:] = progs['death_probs'][inds]
+    people.rel_sus[:] = progs['sus_ORs'][inds]
+    bd = pars['beta_dist']
+    nbn_n = bd['par2']
+    nbn_p = bd['par2'] / (bd['par1'] / bd.get('step', 1) + bd['par2'])
+    draws = rs.negative_binomial(n=nbn_n, p=nbn_p, size=len(inds)) * bd.get('step', 1)
+    people.rel_trans[:] = progs['trans_ORs'][inds] * draws
+
+
+class OracleSim:
+    """One simulation on the CPU.
+
+    Args:
+        pars: full parameter dict (prognoses, nab_kin and immunity filled in)
+        person: dict of initial per-person arrays (at least age, symp_prob,
+            severe_prob, crit_prob, death_prob, rel_trans, rel_sus)
+        contacts: {layer key: dict(p1, p2, beta)}; layer order is layer index
+        rng: 'philox' or 'mt'
+        beta_schedule: optional per-day overall beta (change_beta), length npts
+    """
+
+    def __init__(self, pars, person, contacts, rng='philox', beta_schedule=None, seed_inds=None):
+        self.pars = pars
+        self.n = int(pars['pop_size'])
+        self.npts = int(pars['n_days']) + 1
+        self.people = OraclePeople(pars, self.n)
+        for k, v in person.items():
+            self.people[k] = np.array(v, dtype=self.people[k].dtype)
+        self.contacts = {k: {c: np.array(v[c]) for c in ('p1', 'p2', 'beta')} for k, v in contacts.items()}
+        self.layer_keys = list(self.contacts.keys())
+        self.rng = rng
+        self.seed = int(pars['rand_seed'])
+        self.k0, self.k1 = ph.seed_key(self.seed)
+        if rng == 'mt':
+            self.rs_numba = np.random.RandomState(self.seed)
+            self.rs_numpy = np.random.RandomState(self.seed)
+        self.beta_schedule = beta_schedule
+        self.seed_inds = seed_inds
+        self.t = 0
+        self.results = {}
+        for key in FLOWS + [f'n_{k}' for k in RESULT_STOCKS] + ['pop_nabs', 'pop_protection', 'pop_symp_protection']:
+            self.results[key] = np.zeros(self.npts)
+        nv = pars['n_variants']
+        for key in FLOWS_VARIANT + [f'n_{k}' for k in RESULT_STOCKS_BY_VARIANT]:
+            self.results[key] = np.zeros((nv, self.npts))
+
+    # ------------------------------------------------------------------
+    def _draws(self, call_tag):
+        if self.rng == 'philox':
+            return TableDraws(philox_table(self.seed, self.t, call_tag))
+        return SequentialDraws(self.rs_numpy)
+
+    def init_infections(self):
+        """sim.py:505-532 (frac_susceptible == 1)."""
+        p = self.pars
+        if p['pop_infected']:
+            if self.seed_inds is not None:
+                inds = np.asarray(self.seed_inds)
+            elif self.rng == 'philox':
+                inds = choose_seed_infections(self.seed, self.n, p['pop_infected'])
+            else:
+                inds = self.rs_numba.choice(self.n, int(p['pop_infected']), replace=False)
+            self.people.infect(inds=inds, layer='seed_infection', draws=self._draws(CALL_SEED))
+
+    def update_contacts(self):
+        """people.py:199-206 -> base.py:1849-1876 (Layer.update, frac=1)."""
+        for li, lkey in enumerate(self.layer_keys):
+            if self.pars['dynam_layer'].get(lkey, 0):
+                layer = self.contacts[lkey]
+                n_new = len(layer['p1'])
+                if self.rng == 'philox':
+                    p1, p2 = ph.dynamic_edges(self.k0, self.k1, self.t, li, n_new, self.n)
+                    layer['p1'], layer['p2'] = p1, p2
+                else:
+                    inds = self.rs_numba.permutation(n_new)
+                    layer['p1'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
+                    layer['p2'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
+                layer['beta'] = np.ones(n_new, dtype=F32)
+
+    def step(self):
+        p = self.pars
+        t = self.t
+        people = self.people
+        if t == 0:
+            self.init_infections()
+        people.update_states_pre(t=t)
+        self.update_contacts()
+        hosp_max = people.severe.sum() > p['n_beds_hosp'] if p['n_beds_hosp'] is not None else False
+        icu_max = people.critical.sum() > p['n_beds_icu'] if p['n_beds_icu'] is not None else False
+        if self.beta_schedule is not None:
+            p['beta'] = self.beta_schedule[t]
+
+        vd = p['viral_dist']
+        viral_load = compute_viral_load(t, people.date_infectious, people.date_recovered, people.date_dead,
+                                        F32(vd['frac_time']), F32(vd['load_ratio']), F32(vd['high_cap']))
+        nv = p['n_variants']
+        for variant in range(nv):
+            label = p['variant_map'][variant]
+            beta = F32(p['beta'] * p['rel_beta'] * p['variant_pars'][label]['rel_beta'])
+            inf_variant = people.infectious * (people.infectious_variant == variant)
+            if not inf_variant.any():
+                continue
+            for li, lkey in enumerate(self.layer_keys):
+                layer = self.contacts[lkey]
+                rel_trans, rel_sus = compute_trans_sus(
+                    people.rel_trans, people.rel_sus, inf_variant, people.susceptible,
+                    F32(p['beta_layer'][lkey]), viral_load, people.symptomatic, people.isolated,
+                    people.quarantined, F32(p['asymp_factor']), F32(p['iso_factor'][lkey]),
+                    F32(p['quar_factor'][lkey]), people.sus_imm[variant, :])
+                if self.rng == 'philox':
+                    u0, u1 = ph.edge_uniforms(self.k0, self.k1, t, li, variant, np.arange(len(layer['p1'])))
+                    uniforms = np.stack([u0, u1])
+                else:
+                    rs = self.rs_numba
+                    uniforms = lambda d, edge_inds: rs.random_sample(len(edge_inds))
+                src, tgt = compute_infections(beta, layer['p1'], layer['p2'], layer['beta'],
+                                              rel_trans, rel_sus, uniforms)
+                people.infect(inds=tgt, hosp_max=hosp_max, icu_max=icu_max, source=src, layer=lkey,
+                              variant=variant, draws=self._draws(CALL_TRANSMISSION))
+
+        # sim.py:651-663: stocks and flows
+        for key in RESULT_STOCKS:
+            self.results[f'n_{key}'][t] = np.count_nonzero(people[key])
+        for key in RESULT_STOCKS_BY_VARIANT:
+            for v in range(nv):
+                self.results[f'n_{key}'][v, t] = np.count_nonzero(people[key][v, :])
+        for key, count in people.flows.items():
+            self.results[key][t] += count
+        for key, count in people.flows_variant.items():
+            for v in range(nv):
+                self.results[key][v, t] += count[v]
+        # sim.py:666-674: NAb update and population means
+        if p['use_waning']:
+            has_nabs = people.peak_nab.nonzero()[0]
+            if len(has_nabs):
+                update_nab(people, inds=has_nabs)
+        inds_alive = (~people.dead).nonzero()[0]
+        nab_alive = people.nab[inds_alive]
+        self.results['pop_nabs'][t] = np.sum(nab_alive[nab_alive.nonzero()[0]]) / len(inds_alive)
+        self.results['pop_protection'][t] = np.nanmean(people.sus_imm)
+        self.results['pop_symp_protection'][t] = np.nanmean(people.symp_imm)
+        self.t += 1
+
+    def run(self, until=None):
+        until = self.npts if until is None else until
+        while self.t < until:
+            self.step()
+        return self

@@ -1,0 +1,83 @@
+"""Shared helpers for the tests: golden-fixture loading and state comparison."""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, 'golden')
+
+from oracle.people import (PERSON, STATES, VARIANT_STATES, BY_VARIANT_STATES, IMM_STATES, NAB_STATES,  # noqa: E402
+                           VACC_STATES, DATES, DURS, OraclePeople)
+
+ALL_KEYS = PERSON + STATES + VARIANT_STATES + BY_VARIANT_STATES + IMM_STATES + NAB_STATES + VACC_STATES + DATES + DURS
+FLOAT_KEYS = [k for k in ALL_KEYS if k not in STATES + BY_VARIANT_STATES + ['uid', 'n_infections', 'n_breakthroughs',
+                                                                              't_nab_event', 'doses', 'vaccine_source']]
+
+
+def unjson(x):
+    if isinstance(x, dict):
+        if '__array__' in x:
+            return np.array(x['__array__'], dtype=x['dtype'])
+        return {k: unjson(v) for k, v in x.items()}
+    if isinstance(x, list):
+        return [unjson(v) for v in x]
+    return x
+
+
+def fix_pars(p):
+    """JSON round trip turns int dict keys into strings; restore them."""
+    p = dict(p)
+    if 'variant_map' in p:
+        p['variant_map'] = {int(k): v for k, v in p['variant_map'].items()}
+    if 'vaccine_map' in p:
+        p['vaccine_map'] = {int(k): v for k, v in p['vaccine_map'].items()}
+    return p
+
+
+def load_npz(name):
+    return dict(np.load(os.path.join(GOLDEN, name), allow_pickle=False))
+
+
+def load_day(name):
+    d = load_npz(f'ref_day_{name}.npz')
+    pars = fix_pars(unjson(json.loads(str(d['pars']))))
+    return d, pars
+
+
+def snap(d, prefix):
+    return {k: d[f'{prefix}.{k}'] for k in ALL_KEYS}
+
+
+def oracle_people(d, prefix, pars):
+    n = len(d[f'{prefix}.uid'])
+    p = OraclePeople(pars, n)
+    for k in ALL_KEYS:
+        p[k] = np.array(d[f'{prefix}.{k}'], copy=True)
+    return p
+
+
+def n_layers(d):
+    return len([k for k in d if k.startswith('d.L') and k.endswith('.p1')])
+
+
+def assert_state_equal(get, ref, keys=ALL_KEYS, float_rtol=0.0, label=''):
+    """``get(key)`` -> array; ``ref`` dict of reference arrays. Exact for ints/bools,
+    ``float_rtol`` relative tolerance for floats (NaN must match NaN)."""
+    for k in keys:
+        a = np.asarray(get(k))
+        b = np.asarray(ref[k])
+        assert a.shape == b.shape, (label, k, a.shape, b.shape)
+        if k in FLOAT_KEYS and float_rtol:
+            assert np.array_equal(np.isnan(a), np.isnan(b)), (label, k, 'NaN pattern')
+            m = ~np.isnan(b)
+            np.testing.assert_allclose(a[m], b[m], rtol=float_rtol, atol=0, err_msg=f'{label} {k}')
+        else:
+            if a.dtype.kind == 'f' or b.dtype.kind == 'f':
+                ok = np.array_equal(a.astype(np.float64), b.astype(np.float64), equal_nan=True)
+            else:
+                ok = np.array_equal(a.astype(np.int64), b.astype(np.int64))
+            if not ok:
+                bad = np.nonzero(~((a == b) | (np.isnan(a.astype(float)) & np.isnan(b.astype(float)))))
+                raise AssertionError(f'{label} {k}: {len(bad[0])} mismatches, first at {bad[0][:5]}: '
+                                     f'{a[bad][:5]} vs {b[bad][:5]}')

@@ -1,0 +1,421 @@
+"""Generate the golden fixtures from Covasim 3.1.7's own code.
+
+Run from the repository root, where the reference source tree is available:
+
+    python tests/golden/make_golden.py            # all fixtures
+    python tests/golden/make_golden.py --only day # one group
+
+It executes the reference's function bodies through ``refload`` (see its
+docstring), records every random draw they make, and writes small compressed
+fixtures next to this script. Tests replay the recorded draws, so the oracle
+and the CUDA kernels are checked against the reference's own outputs for the
+reference's own draws. Nothing at test time reads the reference tree.
+
+Fixtures:
+  ref_pars.json        make_pars() + prognoses + nab_kin + immunity (random and hybrid)
+  ref_kernels.npz      compute_viral_load / compute_trans_sus / compute_infections cases
+  ref_day_<name>.npz   one day of the hot path on a mid-epidemic state: states before and
+                       after update_states_pre (with check_immunity), viral load, per
+                       (variant, layer) trans/sus, infections and infect() results with the
+                       draws mapped to per-edge / per-agent slots, and update_nab
+  ref_sims.npz         whole reference runs (inputs and daily results) for MT-mode replay
+  ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
+                       20k-agent random sim (60 days), reference code with MT19937 streams
+"""
+import argparse
+import copy
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+import refload  # noqa: E402
+from oracle import philox as ph  # noqa: E402
+from oracle.kernels import compute_infections as o_compute_infections  # noqa: E402
+from oracle.people import OraclePeople, TableDraws, dist_consumes_draws  # noqa: E402
+from oracle.people import STATES, PERSON, VARIANT_STATES, BY_VARIANT_STATES, IMM_STATES  # noqa: E402
+from oracle.people import NAB_STATES, VACC_STATES, DATES, DURS  # noqa: E402
+
+ALL_KEYS = PERSON + STATES + VARIANT_STATES + BY_VARIANT_STATES + IMM_STATES + NAB_STATES + VACC_STATES + DATES + DURS
+
+
+def jsonable(x):
+    if isinstance(x, dict):
+        return {str(k): jsonable(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [jsonable(v) for v in x]
+    if isinstance(x, np.ndarray):
+        return {'__array__': x.tolist(), 'dtype': str(x.dtype)}
+    if isinstance(x, (np.floating,)):
+        return float(x)
+    if isinstance(x, (np.integer,)):
+        return int(x)
+    if callable(x):
+        return None
+    return x
+
+
+def snapshot(people, prefix):
+    return {f'{prefix}.{k}': np.array(people[k], copy=True) for k in ALL_KEYS}
+
+
+# ------------------------------------------------------------------------- draw mapping
+class LogDraws:
+    """Replays a recorded numpy-stream log through oracle.infect and fills a per-agent table."""
+
+    def __init__(self, log):
+        self.log = list(log)
+        self.table = {}
+
+    def begin(self, inds):
+        self.inds = np.asarray(inds)
+        for a in self.inds:
+            self.table.setdefault(int(a), np.full(ph.N_DRAWS, np.nan))
+
+    def _pop(self, kind, n):
+        k, vals, info = self.log.pop(0)
+        assert k == kind and len(vals) == n, (k, kind, len(vals), n)
+        return vals, info
+
+    def normal(self, slot, inds, dist):
+        from oracle.people import sample_from_normal
+        if not dist_consumes_draws(dist):
+            return sample_from_normal(dist, np.zeros(len(inds)))
+        z, _ = self._pop('normal', len(inds))
+        for a, v in zip(inds, z):
+            self.table[int(a)][slot] = v
+        return sample_from_normal(dist, z)
+
+    def uniform(self, slot, inds):
+        u, _ = self._pop('uniform', len(inds))
+        for a, v in zip(inds, u):
+            self.table[int(a)][slot] = v
+        return u
+
+    def as_arrays(self):
+        keys = np.array(sorted(self.table), dtype=np.int64)
+        tab = np.array([self.table[k] for k in keys]).reshape(len(keys), ph.N_DRAWS)
+        return keys, tab
+
+
+def map_edge_uniforms(log, beta, p1, p2, layer_betas, rel_trans, rel_sus):
+    """Slot table [2, E] of the reference's compute_infections draws (2.0 = not drawn)."""
+    U = np.full((2, len(p1)), 2.0)
+    log = list(log)
+
+    def uni(d, edge_inds):
+        k, vals, _ = log.pop(0)
+        assert k == 'uniform' and len(vals) == len(edge_inds)
+        U[d, edge_inds] = vals
+        return vals
+    src, tgt = o_compute_infections(beta, p1, p2, layer_betas, rel_trans, rel_sus, uni)
+    assert not log
+    return U, src, tgt
+
+
+# ------------------------------------------------------------------------- fixtures
+class _SimPars(dict):
+    """What init_immunity needs of a sim: item access to the pars and ``npts``."""
+
+    def __init__(self, pars, npts):
+        super().__init__(pars)
+        self.npts = npts
+
+
+def make_pars_fixture(ref):
+    out = {}
+    for pop_type in ('random', 'hybrid'):
+        pars = ref.make_pars(pop_type=pop_type)
+        s = _SimPars(pars, int(pars['n_days']) + 1)
+        ref.cvi.init_immunity(s)
+        pars['nab_kin'] = s['nab_kin']
+        pars['immunity'] = s['immunity']
+        out[pop_type] = jsonable(pars)
+    pars = ref.make_pars(pop_type='hybrid')
+    pars['variant_map'] = {0: 'wild', 1: 'alpha', 2: 'delta'}
+    pars['variant_pars'] = {k: ref.cvpar.get_variant_pars(variant=k) for k in ('wild', 'alpha', 'delta')}
+    pars['n_variants'] = 3
+    s = _SimPars(pars, 61)
+    ref.cvi.init_immunity(s, create=True)
+    out['immunity_3var'] = jsonable(s['immunity'])
+    with open(os.path.join(HERE, 'ref_pars.json'), 'w') as f:
+        json.dump(out, f)
+    print('ref_pars.json written')
+
+
+def make_kernels_fixture(ref):
+    rng = np.random.default_rng(20240611)
+    out = {}
+    # --- compute_viral_load: NaN starts, dead vs recovered, capped/uncapped, zero-length, ties
+    n = 4096
+    ts = rng.integers(0, 40, n).astype(np.float32)
+    rec = ts + rng.integers(0, 30, n).astype(np.float32)
+    dead = np.where(rng.random(n) < 0.2, ts + rng.integers(0, 25, n), np.nan).astype(np.float32)
+    ts[rng.random(n) < 0.1] = np.nan
+    rec[rng.random(n) < 0.1] = np.nan
+    vl_cases = []
+    for i, (t, fr, lr, hc) in enumerate([(20, 0.3, 2.0, 4.0), (5, 0.3, 2.0, 4.0), (33, 0.5, 3.0, 2.0),
+                                         (0, 0.3, 2.0, 100.0)]):
+        vl = ref.cvu.compute_viral_load(t, ts, rec, dead, fr, lr, hc)
+        out[f'vl{i}.out'] = vl
+        vl_cases.append([t, fr, lr, hc])
+    out['vl.ts'], out['vl.rec'], out['vl.dead'] = ts, rec, dead
+    out['vl.cases'] = np.array(vl_cases, dtype=np.float64)
+
+    # --- compute_trans_sus
+    rt = (rng.random(n) * 2).astype(np.float32)
+    rt[rng.random(n) < 0.1] = 0
+    rs = rng.choice([0.34, 0.67, 1.0, 1.24, 1.47], n).astype(np.float32)
+    inf, sus, symp, iso, quar = (rng.random((5, n)) < np.array([[0.3], [0.6], [0.5], [0.2], [0.2]]))
+    vl = ref.cvu.compute_viral_load(20, ts, rec, dead, 0.3, 2.0, 4.0)
+    imm = np.where(rng.random(n) < 0.3, rng.random(n), 0).astype(np.float32)
+    ts_cases = [(3.0, 1.0, 0.3, 0.6), (0.3, 0.8, 0.1, 0.2), (1.0, 0.0, 0.0, 1.0)]
+    for i, (bl, af, isf, qf) in enumerate(ts_cases):
+        a, b = ref.cvu.compute_trans_sus(rt, rs, inf, sus, bl, vl, symp, iso, quar, af, isf, qf, imm)
+        out[f'ts{i}.rel_trans'], out[f'ts{i}.rel_sus'] = a, b
+    for k, v in dict(rt=rt, rs=rs, inf=inf, sus=sus, symp=symp, iso=iso, quar=quar, vl=vl, imm=imm).items():
+        out[f'ts.{k}'] = v
+    out['ts.cases'] = np.array(ts_cases, dtype=np.float64)
+
+    # --- compute_infections: sparse sources, self-loops, duplicate targets, p > 1, empty layer
+    n_agents = 3000
+    inf_cases = []
+    for i, (E, beta, frac_src, big) in enumerate([(20000, 0.016, 0.05, False), (15000, 0.3, 0.2, False),
+                                                 (5000, 50.0, 0.1, True), (0, 0.016, 0.1, False),
+                                                 (40000, 0.05, 0.5, False)]):
+        p1 = np.sort(rng.integers(0, n_agents, E)).astype(np.int32)
+        p2 = rng.integers(0, n_agents, E).astype(np.int32)
+        if E:
+            p2[:10] = p1[:10]  # self-loops
+        lb = np.where(rng.random(E) < 0.5, 1.0, rng.random(E) * 2).astype(np.float32)
+        rtr = np.where(rng.random(n_agents) < frac_src, rng.random(n_agents), 0).astype(np.float32)
+        rsu = np.where(rng.random(n_agents) < 0.7, rng.random(n_agents) * 1.5, 0).astype(np.float32)
+        if big:
+            rtr *= 10
+        ref.cvu.set_seed(100 + i)
+        ref.draws()
+        src, tgt = ref.cvu.compute_infections(beta, p1, p2, lb, rtr, rsu)
+        nb_log, _ = ref.draws()
+        U, osrc, otgt = map_edge_uniforms(nb_log, np.float32(beta), p1, p2, lb, rtr, rsu)
+        assert np.array_equal(src, osrc) and np.array_equal(tgt, otgt)
+        for k, v in dict(p1=p1, p2=p2, lb=lb, rt=rtr, rs=rsu, U=U, src=src, tgt=tgt).items():
+            out[f'inf{i}.{k}'] = v
+        inf_cases.append(beta)
+    out['inf.betas'] = np.array(inf_cases, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, 'ref_kernels.npz'), **out)
+    print('ref_kernels.npz written')
+
+
+def ref_sim_with_variants(ref, n, seed, days_before, nv=1, pop_type='hybrid', n_beds=None):
+    pars = ref.make_pars(pop_size=n, n_days=days_before + 5, pop_type=pop_type, rand_seed=seed)
+    if nv > 1:
+        labels = ['wild', 'alpha', 'delta'][:nv]
+        pars['variant_map'] = {i: k for i, k in enumerate(labels)}
+        pars['variant_pars'] = {k: ref.cvpar.get_variant_pars(variant=k) for k in labels}
+        pars['n_variants'] = nv
+        pars['immunity'] = None
+    if n_beds is not None:
+        pars['n_beds_hosp'], pars['n_beds_icu'] = n_beds
+    sim = refload.RefSim(ref, pars)
+    if nv > 1:
+        sim.pars['immunity'] = None
+        ref.cvi.init_immunity(sim, create=True)
+    rs = np.random.RandomState(seed + 1000)
+    while sim.t < days_before:
+        if nv > 1 and sim.t in (6, 12):  # import later variants, as variant.apply would
+            v = 1 if sim.t == 6 else min(2, nv - 1)
+            sus = sim.people.susceptible.nonzero()[0]
+            imp = rs.choice(sus, min(15, len(sus)), replace=False)
+            sim.people.infect(inds=imp, layer='importation', variant=v)
+        sim.step()
+    return sim
+
+
+def run_day(ref, sim, out, prefix):
+    """One day of the hot path on a copy of sim.people, with every output recorded."""
+    people = copy.deepcopy(sim.people)
+    people.pars = sim.pars
+    t = sim.t
+    p = sim.pars
+    out.update(snapshot(people, f'{prefix}.S0'))
+    ref.draws()
+    people.update_states_pre(t=t)
+    out.update(snapshot(people, f'{prefix}.S1'))
+    for k, v in people.flows.items():
+        out[f'{prefix}.flows.{k}'] = np.array(v)
+    for k, v in people.flows_variant.items():
+        out[f'{prefix}.flows_variant.{k}'] = np.array(v)
+    hosp_max = people.count('severe') > p['n_beds_hosp'] if p['n_beds_hosp'] is not None else False
+    icu_max = people.count('critical') > p['n_beds_icu'] if p['n_beds_icu'] is not None else False
+    out[f'{prefix}.hosp_icu'] = np.array([hosp_max, icu_max])
+    vd = p['viral_dist']
+    vl = ref.cvu.compute_viral_load(t, people.date_infectious, people.date_recovered, people.date_dead,
+                                    np.float32(vd['frac_time']), np.float32(vd['load_ratio']),
+                                    np.float32(vd['high_cap']))
+    out[f'{prefix}.viral_load'] = vl
+    nv = p['n_variants']
+    layers = list(people.contacts.keys())
+    out[f'{prefix}.layer_keys'] = np.array(layers)
+    for li, lkey in enumerate(layers):
+        L = people.contacts[lkey]
+        out[f'{prefix}.L{li}.p1'], out[f'{prefix}.L{li}.p2'], out[f'{prefix}.L{li}.beta'] = L['p1'], L['p2'], L['beta']
+    for v in range(nv):
+        label = p['variant_map'][v]
+        beta = np.float32(p['beta'] * p['rel_beta'] * p['variant_pars'][label]['rel_beta'])
+        inf_variant = people.infectious * (people.infectious_variant == v)
+        out[f'{prefix}.v{v}.beta'] = np.array(beta)
+        for li, lkey in enumerate(layers):
+            L = people.contacts[lkey]
+            rt, rs = ref.cvu.compute_trans_sus(people.rel_trans, people.rel_sus, inf_variant, people.susceptible,
+                                               np.float32(p['beta_layer'][lkey]), vl, people.symptomatic,
+                                               people.isolated, people.quarantined, p['asymp_factor'],
+                                               np.float32(p['iso_factor'][lkey]), np.float32(p['quar_factor'][lkey]),
+                                               people.sus_imm[v, :])
+            key = f'{prefix}.v{v}.L{li}'
+            out[f'{key}.rel_trans'], out[f'{key}.rel_sus'] = rt, rs
+            ref.draws()
+            src, tgt = ref.cvu.compute_infections(beta, L['p1'], L['p2'], L['beta'], rt, rs)
+            nb_log, _ = ref.draws()
+            U, osrc, otgt = map_edge_uniforms(nb_log, beta, L['p1'], L['p2'], L['beta'], rt, rs)
+            assert np.array_equal(src, osrc) and np.array_equal(tgt, otgt)
+            out[f'{key}.U'], out[f'{key}.src'], out[f'{key}.tgt'] = U, src, tgt
+            inds = people.infect(inds=tgt, hosp_max=hosp_max, icu_max=icu_max, source=src, layer=lkey, variant=v)
+            _, np_log = ref.draws()
+            out[f'{key}.infected'] = np.asarray(inds)
+            out[f'{key}.n_draw_log'] = np.array(len(np_log))
+            out[f'{key}.np_log'] = np.concatenate([e[1].ravel() for e in np_log]) if np_log else np.zeros(0)
+            out[f'{key}.np_log_lens'] = np.array([len(e[1]) for e in np_log], dtype=np.int64)
+            out[f'{key}.np_log_kinds'] = np.array([e[0] == 'normal' for e in np_log], dtype=bool)
+            out.update(snapshot(people, f'{key}.after'))
+    out.update(snapshot(people, f'{prefix}.S2'))
+    if p['use_waning']:
+        has_nabs = people.peak_nab.nonzero()[0]
+        if len(has_nabs):
+            ref.cvi.update_nab(people, inds=has_nabs)
+    out.update(snapshot(people, f'{prefix}.S3'))
+    return people
+
+
+def map_infect_tables(out, prefix, pars):
+    """Turn each (variant, layer)'s recorded infect log into a per-agent draw table."""
+    from oracle.people import OraclePeople as OP
+    nv = pars['n_variants']
+    n = len(out[f'{prefix}.S0.uid'])
+    people = OP(pars, n)
+    for k in ALL_KEYS:
+        people[k] = np.array(out[f'{prefix}.S1.{k}'], copy=True)
+    people.t = int(out[f'{prefix}.t'])
+    nlayers = len([k for k in out if k.startswith(f'{prefix}.L') and k.endswith('.p1')])
+    hosp_max, icu_max = out[f'{prefix}.hosp_icu']
+    for v in range(nv):
+        for li in range(nlayers):
+            key = f'{prefix}.v{v}.L{li}'
+            flat, lens, kinds = out[f'{key}.np_log'], out[f'{key}.np_log_lens'], out[f'{key}.np_log_kinds']
+            log, pos = [], 0
+            for ln, isn in zip(lens, kinds):
+                log.append(('normal' if isn else 'uniform', flat[pos:pos + ln], {}))
+                pos += ln
+            ld = LogDraws(log)
+            people.infect(inds=out[f'{key}.tgt'], hosp_max=hosp_max, icu_max=icu_max, source=out[f'{key}.src'],
+                          layer=str(li), variant=v, draws=ld)
+            assert not ld.log, 'unconsumed draws'
+            agents, tab = ld.as_arrays()
+            out[f'{key}.draw_agents'], out[f'{key}.draw_table'] = agents, tab
+            for k in ALL_KEYS:
+                a, b = people[k], out[f'{key}.after.{k}']
+                assert np.array_equal(a, b, equal_nan=True), (key, k)
+            del out[f'{key}.np_log'], out[f'{key}.np_log_lens'], out[f'{key}.np_log_kinds'], out[f'{key}.n_draw_log']
+
+
+def make_day_fixtures(ref):
+    cases = [
+        # name, n, seed, day, variants, pop_type, beds
+        ('hybrid', 2000, 11, 24, 1, 'hybrid', None),
+        ('variants', 2000, 12, 30, 3, 'hybrid', (2, 1)),
+        ('random', 1500, 13, 35, 1, 'random', None),
+    ]
+    for name, n, seed, day, nv, pop_type, beds in cases:
+        sim = ref_sim_with_variants(ref, n, seed, day, nv=nv, pop_type=pop_type, n_beds=beds)
+        out = {}
+        prefix = 'd'
+        out[f'{prefix}.t'] = np.array(sim.t)
+        run_day(ref, sim, out, prefix)
+        map_infect_tables(out, prefix, sim.pars)
+        out['pars'] = np.array(json.dumps(jsonable(sim.pars)))
+        # drop redundant per-layer 'after' snapshots except the last (keeps the fixture small)
+        for k in [k for k in out if '.after.' in k]:
+            del out[k]
+        np.savez_compressed(os.path.join(HERE, f'ref_day_{name}.npz'), **out)
+        print(f'ref_day_{name}.npz written', sum(v.nbytes for v in out.values()) // 1024, 'KiB raw')
+
+
+def make_sims_fixture(ref):
+    out = {}
+    cases = [('random', 1500, 40, 3, 0), ('hybrid', 1500, 50, 4, 0), ('hybrid', 1200, 45, 9, 1)]
+    for i, (pop_type, n, days, seed, dyn) in enumerate(cases):
+        pars = ref.make_pars(pop_size=n, n_days=days, pop_type=pop_type, rand_seed=seed)
+        if dyn:
+            pars['dynam_layer']['c'] = 1
+        sim = refload.RefSim(ref, pars)
+        for k in ('age', 'sex', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus'):
+            out[f's{i}.person.{k}'] = sim.people[k].copy()
+        layers = list(sim.people.contacts.keys())
+        for li, lk in enumerate(layers):
+            for c in ('p1', 'p2', 'beta'):
+                out[f's{i}.L{li}.{c}'] = sim.people.contacts[lk][c].copy()
+        out[f's{i}.pars'] = np.array(json.dumps(jsonable(sim.pars)))
+        sim.run()
+        for k, v in sim.results.items():
+            if k == 'variant':
+                for kk, vv in v.items():
+                    out[f's{i}.res.{kk}'] = vv
+            else:
+                out[f's{i}.res.{k}'] = v
+        for k in ('exposed', 'recovered', 'dead', 'susceptible', 'date_recovered', 'peak_nab', 'nab'):
+            out[f's{i}.final.{k}'] = sim.people[k].copy()
+    out['n'] = np.array(len(cases))
+    np.savez_compressed(os.path.join(HERE, 'ref_sims.npz'), **out)
+    print('ref_sims.npz written')
+
+
+def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
+    keys = ['new_infections', 'new_severe', 'new_deaths', 'new_infectious', 'new_recoveries', 'new_critical',
+            'new_symptomatic', 'n_exposed']
+    res = {k: np.zeros((n_seeds, n_days + 1)) for k in keys}
+    t0 = time.time()
+    for s in range(n_seeds):
+        pars = ref.make_pars(pop_size=pop_size, n_days=n_days, pop_type='random', rand_seed=s)
+        sim = refload.RefSim(ref, pars).run()
+        for k in keys:
+            res[k][s] = sim.results[k]
+        if s % 20 == 0:
+            print(f'  seed {s}: {time.time() - t0:.1f}s, cum inf {sim.results["new_infections"].sum()}')
+    out = {k: v.astype(np.int32) for k, v in res.items()}
+    out['meta'] = np.array([n_seeds, pop_size, n_days])
+    np.savez_compressed(os.path.join(HERE, 'ref_distribution.npz'), **out)
+    print('ref_distribution.npz written', time.time() - t0, 's')
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--only', default=None)
+    ap.add_argument('--seeds', type=int, default=200)
+    args = ap.parse_args()
+    ref = refload.Reference()
+    groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
+                  sims=make_sims_fixture,
+                  distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
+    for name, fn in groups.items():
+        if args.only is None or args.only == name:
+            fn(ref)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,136 @@
+"""CPU checks of the C ABI and the host-side logic (no kernel launches)."""
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+
+import covasim_gb300 as cv
+from covasim_gb300 import _lib as L
+from covasim_gb300 import build as B
+from common import GOLDEN, unjson
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, 'include', 'covgpu.h')).read()
+    return sorted(set(re.findall(r'^\s*(?:int|int64_t)\s+(covgpu_\w+)\s*\(', src, flags=re.M)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    B.build()
+    lib = C.CDLL(B.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(L.EXPORTED) == syms
+
+
+def test_abi_layout_matches_ctypes_mirror():
+    lib_vals, mine = L.abi_layout()
+    assert lib_vals == mine
+
+
+def test_entry_points_reject_bad_arguments_without_a_gpu():
+    lib = L.lib()
+    # rejected on the host before any CUDA call
+    assert lib.covgpu_viral_load(0, None, None, None, -1, 0.3, 2.0, 4.0, None, None) == L.BADARG
+    assert lib.covgpu_infections_scratch_bytes(-5) == -1
+    assert lib.covgpu_infections(0.1, None, None, None, 10, None, None, None, 0, 0, 0, 0, None, None, 0, None, None,
+                                 None, 0, None) == L.BADARG
+    assert lib.covgpu_agent_step(None, 0, 1, 1, None) == L.BADARG
+    assert lib.covgpu_run_days(None, 0, 10, 0, 1, 1, None) == L.BADARG
+    st = L.State()
+    assert lib.covgpu_edge_pass(C.pointer(st), 0, None) == L.BADARG
+
+
+def _same(got, want, path):
+    if isinstance(want, dict):
+        assert isinstance(got, dict), path
+        want_keys = {str(k) for k in want}
+        got_keys = {str(k) for k in got}
+        assert want_keys == got_keys, (path, want_keys ^ got_keys)
+        gmap = {str(k): v for k, v in got.items()}
+        for k, v in want.items():
+            _same(gmap[str(k)], v, f'{path}.{k}')
+    elif isinstance(want, (list, tuple)) and not (want and isinstance(want[0], (int, float))):
+        assert len(got) == len(want), path
+        for i, (g, w) in enumerate(zip(got, want)):
+            _same(g, w, f'{path}[{i}]')
+    elif isinstance(want, str) or want is None or isinstance(want, bool):
+        assert got == want, (path, got, want)
+    else:
+        np.testing.assert_array_equal(np.asarray(got, dtype=float), np.asarray(want, dtype=float), err_msg=path)
+
+
+def test_make_pars_matches_reference_values():
+    ref = json.load(open(os.path.join(GOLDEN, 'ref_pars.json')))
+    for pop_type in ('random', 'hybrid'):
+        want = unjson(ref[pop_type])
+        got = cv.make_pars(pop_type=pop_type)
+        got['prognoses'] = cv.get_prognoses(True)
+        cv.init_immunity(got, int(got['n_days']) + 1)
+        for k, v in want.items():
+            if k in ('verbose', 'interventions', 'analyzers', 'variants'):
+                continue
+            _same(got[k], v, f'{pop_type}.{k}')
+    want3 = np.asarray(unjson(ref['immunity_3var']))
+    p = cv.make_pars(pop_type='hybrid')
+    p['variant_map'] = {0: 'wild', 1: 'alpha', 2: 'delta'}
+    p['variant_pars'] = {k: cv.get_variant_pars(variant=k) for k in ('wild', 'alpha', 'delta')}
+    p['n_variants'] = 3
+    cv.init_immunity(p, 61, create=True)
+    np.testing.assert_array_equal(p['immunity'], want3)
+
+
+def test_population_generators_follow_reference_distributions():
+    pars = cv.make_pars(pop_type='hybrid', pop_size=200_000, rand_seed=3)
+    pop = cv.make_randpop(pars, rng=np.random.default_rng(3))
+    age = pop['age']
+    assert 36 < np.median(age) < 39
+    n = len(age)
+    # community: round(Poisson(20)/2) per agent -> mean 10 undirected edges per agent
+    c = pop['contacts']['c']
+    assert abs(len(c['p1']) / n - 10.0) < 0.05
+    assert np.all(np.diff(c['p1']) >= 0)
+    # households: Poisson(2) cluster sizes, all pairs within a cluster
+    h = pop['contacts']['h']
+    assert np.all(h['p2'] > h['p1'])
+    s_inds = np.nonzero((age >= 6) & (age < 22))[0]
+    s = pop['contacts']['s']
+    assert np.isin(s['p1'], s_inds).all() and np.isin(s['p2'], s_inds).all()
+    w = pop['contacts']['w']
+    w_inds = np.nonzero((age >= 22) & (age < 65))[0]
+    assert abs(len(w['p1']) / len(w_inds) - 8.0) < 0.1
+    # mean household-layer degree: E[m(m-1)/2]/E[m] with m ~ Poisson(2) -> 1.0 edge per agent
+    assert abs(len(h['p1']) / n - 1.0) < 0.03
+
+
+def test_prognoses_and_rel_trans_distribution():
+    pars = cv.make_pars(pop_size=100_000)
+    pars['prognoses'] = cv.get_prognoses(True)
+    age = cv.sample_ages(100_000, np.random.default_rng(0))
+    from covasim_gb300.population import set_prognoses
+    out = set_prognoses(age, pars, np.random.default_rng(1))
+    rt = out['rel_trans']
+    assert abs(rt.mean() - 1.0) < 0.03
+    assert 0.06 < (rt == 0).mean() < 0.12  # negative binomial(mean 1, dispersion 0.45, step 0.01) has P(0) ~ 9%
+
+
+def test_change_beta_schedule():
+    sim = cv.Sim(pop_size=100, n_days=40, interventions=[cv.change_beta(days=[10, 30], changes=[0.5, 0.8]),
+                                                       cv.change_beta(days=20, changes=0.1, layers='a')])
+    sim.validate_pars()
+    sim.init_interventions()
+    from covasim_gb300.sim import build_spec
+    pars = sim.pars
+    pars['prognoses'] = cv.get_prognoses(True)
+    cv.init_immunity(pars, sim.npts)
+    spec, _, _ = build_spec(pars, None, None, pars['interventions'])
+    b = spec.beta_sched
+    assert b[9] == 0.016 and b[10] == 0.016 * 0.5 and b[29] == 0.016 * 0.5 and b[30] == 0.016 * 0.8
+    bl = spec.beta_layer_sched[:, 0]
+    assert bl[19] == 1.0 and bl[20] == 0.1 and bl[40] == 0.1

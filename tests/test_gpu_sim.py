@@ -1,0 +1,162 @@
+"""Whole simulations on the GPU against the oracle run with the same Philox draws,
+batch-versus-single identity, the reference's behavioural known answers, and
+the distribution of outcomes against 200 seeds of the reference's own code."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+import covasim_gb300 as cv
+from common import load_npz, assert_state_equal, ALL_KEYS
+from oracle.sim import OracleSim
+
+pytestmark = pytest.mark.gpu
+
+RES_KEYS = ['new_infections', 'new_reinfections', 'new_infectious', 'new_symptomatic', 'new_severe', 'new_critical',
+            'new_recoveries', 'new_deaths', 'new_known_deaths', 'n_susceptible', 'n_exposed', 'n_infectious',
+            'n_symptomatic', 'n_severe', 'n_critical', 'n_recovered', 'n_dead']
+
+
+def oracle_for(sim):
+    spec = sim.spec
+    contacts = {ly['key']: dict(p1=ly['p1'], p2=ly['p2'], beta=ly['beta']) for ly in spec.layers}
+    pars = copy.deepcopy(sim.pars)
+    pars['interventions'] = []
+    return OracleSim(pars, dict(spec.person), contacts, rng='philox', beta_schedule=spec.beta_sched)
+
+
+def compare_runs(sim, orc, keys=RES_KEYS):
+    raw = sim.raw_results()
+    for k in keys:
+        np.testing.assert_array_equal(raw[k], orc.results[k], err_msg=k)
+    np.testing.assert_allclose(raw['pop_nabs'], orc.results['pop_nabs'], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(raw['pop_protection'], orc.results['pop_protection'], rtol=1e-5, atol=1e-12)
+    people_keys = [k for k in ALL_KEYS if k not in ('age', 'sex', 'uid', 'doses')]
+    assert_state_equal(lambda k: sim.people.gpu(k).cpu().numpy(), {k: orc.people[k] for k in people_keys},
+                       keys=people_keys, float_rtol=1e-6, label='final state')
+
+
+@pytest.mark.parametrize('pop_type,n,days,dyn,seed', [('hybrid', 3000, 45, False, 1), ('random', 4000, 50, False, 2),
+                                                     ('hybrid', 2500, 40, True, 3)])
+def test_sim_matches_oracle_philox(pop_type, n, days, dyn, seed):
+    pars = dict(pop_type=pop_type, pop_size=n, n_days=days, rand_seed=seed, pop_infected=30,
+                interventions=[cv.change_beta(days=25, changes=0.6)])
+    if dyn:
+        pars['dynam_layer'] = dict(h=0, s=0, w=0, c=1)
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim).run()
+    sim.run()
+    compare_runs(sim, orc)
+
+
+def test_step_mode_equals_graph_run():
+    pars = dict(pop_type='hybrid', pop_size=3000, n_days=30, rand_seed=7)
+    a = cv.Sim(pars).run()
+    b = cv.Sim(pars)
+    b.initialize()
+    for _ in range(b.npts):
+        b.step()
+    b.finalize()
+    ra, rb = a.raw_results(), b.raw_results()
+    for k in RES_KEYS + ['pop_nabs', 'pop_protection']:
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+    c = cv.Sim(pars).run(use_graph=False)
+    rc = c.raw_results()
+    for k in RES_KEYS:
+        np.testing.assert_array_equal(ra[k], rc[k], err_msg=k)
+
+
+def test_resume_until_equals_one_run():
+    """test_resume.py:19-52: run(until=) then run() equals one run."""
+    pars = dict(pop_type='random', pop_size=5000, n_days=40, rand_seed=11)
+    a = cv.Sim(pars).run()
+    b = cv.Sim(pars)
+    b.run(until=17)
+    b.run()
+    for k in RES_KEYS:
+        np.testing.assert_array_equal(a.results[k].values, b.results[k].values, err_msg=k)
+
+
+def test_batch_equals_single_runs():
+    sims = [cv.Sim(pop_type='random', pop_size=n, n_days=40, rand_seed=s, beta=b,
+                   interventions=[cv.change_beta(days=20, changes=c)])
+            for n, s, b, c in [(3000, 1, 0.02, 0.5), (10000, 2, 0.015, 0.9), (777, 3, 0.025, 0.3)]]
+    singles = [cv.Sim(copy.deepcopy(s.pars)).run() for s in sims]
+    batch = cv.BatchSim([cv.Sim(copy.deepcopy(s.pars)) for s in sims]).run()
+    for k, single in enumerate(singles):
+        raw = single.raw_results()
+        got = batch.results(k)
+        for key in RES_KEYS + ['pop_nabs']:
+            np.testing.assert_array_equal(got[key], raw[key], err_msg=f'sim {k} {key}')
+
+
+def test_beta_zero_no_transmission():
+    """tests/unittests/test_transmission.py:16-35."""
+    sim = cv.Sim(pop_size=5000, n_days=30, beta=0, pop_infected=50).run()
+    assert sim.results['new_infections'].values.sum() == 0
+    assert sim.results['cum_infections'].values[-1] == 50
+
+
+@pytest.mark.parametrize('delay', [1, 5, 15])
+def test_exposed_to_infectious_delay_exact(delay):
+    """tests/unittests/test_progression.py:17-51: std 0 => everyone infectious on day `delay`."""
+    pars = cv.make_pars(pop_size=500, pop_infected=500, n_days=30)
+    pars['dur']['exp2inf'] = dict(dist='normal', par1=delay, par2=0)
+    pars['rel_symp_prob'] = 0
+    sim = cv.Sim(pars).run()
+    ch = sim.results['new_infectious'].values
+    assert ch[delay] == 500 and ch[:delay].sum() == 0
+
+
+def test_everyone_dies_with_certain_death():
+    """tests/unittests/test_mortality.py:13-24."""
+    pars = cv.make_pars(pop_size=400, pop_infected=400, n_days=60)
+    for k in ('rel_symp_prob', 'rel_severe_prob', 'rel_crit_prob', 'rel_death_prob'):
+        pars[k] = 1e6
+    sim = cv.Sim(pars).run()
+    assert sim.results['cum_deaths'].values[-1] == 400
+
+
+def test_no_deaths_with_zero_death_prob():
+    """tests/unittests/test_mortality.py:26-45."""
+    sim = cv.Sim(pop_size=5000, n_days=60, rel_death_prob=0.0).run()
+    assert sim.results['cum_deaths'].values[-1] == 0
+
+
+def test_waning_raises_reinfections_and_nabs():
+    """tests/test_immunity.py:88-128."""
+    base = dict(pop_size=8000, n_days=150, beta=0.02)
+    s0 = cv.Sim(base, use_waning=False).run()
+    s1 = cv.Sim(base, use_waning=True).run()
+    assert s0.results['cum_reinfections'].values[-1] == 0
+    assert s1.results['cum_reinfections'].values[-1] > 0
+    assert s1.results['pop_nabs'].values.max() > 0 and s0.results['pop_nabs'].values.max() == 0
+    assert s1.results['pop_protection'].values.max() > 0
+
+
+def test_distribution_matches_reference_200_seeds():
+    """200 seeds of the default 20k random sim against 200 seeds of the reference's
+    own code: two-sample KS p > 0.01 and means within 2 standard errors."""
+    from scipy.stats import ks_2samp
+    ref = load_npz('ref_distribution.npz')
+    n_seeds, pop_size, n_days = (int(x) for x in ref['meta'])
+    base = cv.Sim(pop_size=pop_size, n_days=n_days, pop_type='random', rand_seed=0)
+    batch = cv.BatchSim(base, n_runs=n_seeds).run()
+    got = {k: batch.series(k) for k in ('new_infections', 'new_severe', 'new_deaths')}
+    stats = {}
+    for k in ('new_infections', 'new_severe', 'new_deaths'):
+        stats[f'cum_{k}'] = (got[k].sum(1), ref[k].sum(1))
+        for day in (20, 40, 60):
+            stats[f'{k}_d{day}'] = (got[k][:, day], ref[k][:, day])
+    stats['peak_day'] = (got['new_infections'].argmax(1), ref['new_infections'].argmax(1))
+    failures = []
+    for name, (a, b) in stats.items():
+        p = ks_2samp(a, b).pvalue
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        diff = abs(a.mean() - b.mean())
+        if p <= 0.01 or (se > 0 and diff > 2 * se):
+            failures.append((name, p, a.mean(), b.mean(), se))
+    # 19 statistics at the 1% / 2-SE levels: allow one marginal miss from chance alone
+    assert len(failures) <= 1, failures
