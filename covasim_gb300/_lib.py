@@ -121,8 +121,8 @@ def lib():
         L.covgpu_trans_sus.argtypes = [vp, vp, vp, vp, f32, vp, vp, vp, vp, f32, f32, f32, vp, i64, vp, vp, vp]
         L.covgpu_infections_scratch_bytes.argtypes = [i64]
         L.covgpu_infections_scratch_bytes.restype = i64
-        L.covgpu_infections.argtypes = [f32, vp, vp, vp, i64, vp, vp, vp, u64, i32, i32, i32, vp, vp, i64, vp, vp,
-                                        vp, i64, vp]
+        L.covgpu_infections.argtypes = [f32, vp, vp, vp, i64, vp, vp, i64, vp, u64, i32, i32, i32, vp, vp, i64, vp,
+                                        vp, vp, i64, vp]
         L.covgpu_agent_step.argtypes = [sp, i32, i32, i32, vp]
         L.covgpu_edge_pass.argtypes = [sp, i32, vp]
         L.covgpu_infect_claims.argtypes = [sp, i32, vp]

@@ -74,11 +74,16 @@ __global__ void k_trans_sus(const float* __restrict__ rt, const float* __restric
 // drawn (beta != 0) and u < p in float64.
 struct InfArgs {
   float beta; const int32_t* p1; const int32_t* p2; const float* lb; int64_t E;
-  const float* rt; const float* rs; const double* uni; uint32_t k0, k1; int day, variant, layer;
+  const float* rt; const float* rs; int64_t n_agents; const double* uni; uint32_t k0, k1; int day, variant, layer;
+  int32_t* status;
 };
 __device__ __forceinline__ bool inf_hit(const InfArgs& a, int dir, int64_t e, int32_t& src, int32_t& tgt) {
   src = dir ? a.p2[e] : a.p1[e];
   tgt = dir ? a.p1[e] : a.p2[e];
+  if ((uint32_t)src >= (uint64_t)a.n_agents || (uint32_t)tgt >= (uint64_t)a.n_agents) {  // bad index: skip
+    if (a.status) atomicOr(a.status, COVGPU_BADARG);
+    return false;
+  }
   const float st = a.rt[src];
   if (st == 0.0f) return false;
   const float p = __fmul_rn(__fmul_rn(__fmul_rn(a.beta, a.lb[e]), st), a.rs[tgt]);
@@ -791,6 +796,7 @@ struct GraphEntry {
 };
 GraphEntry g_graphs[8];
 int g_graph_next = 0;
+cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the legacy stream cannot capture)
 
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
@@ -854,10 +860,11 @@ int64_t covgpu_infections_scratch_bytes(int64_t n_edges) {
 }
 
 int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas, int64_t n_edges,
-                      const float* rel_trans, const float* rel_sus, const double* uniforms, uint64_t seed, int32_t day,
+                      const float* rel_trans, const float* rel_sus, int64_t n_agents, const double* uniforms,
+                      uint64_t seed, int32_t day,
                       int32_t variant, int32_t layer, int32_t* out_src, int32_t* out_tgt, int64_t capacity,
                       int64_t* out_count, int32_t* status, void* scratch, int64_t scratch_bytes, void* stream) {
-  if (n_edges < 0 || capacity < 0 || !out_count) return COVGPU_BADARG;
+  if (n_edges < 0 || capacity < 0 || n_agents < 0 || !out_count) return COVGPU_BADARG;
   if (variant < 0 || variant >= COVGPU_MAX_VARIANTS || layer < 0 || layer >= COVGPU_MAX_LAYERS) return COVGPU_BADARG;
   if (scratch_bytes < covgpu_infections_scratch_bytes(n_edges) || !scratch) return COVGPU_BADARG;
   cudaStream_t s = S(stream);
@@ -873,7 +880,7 @@ int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const fl
   int32_t* counts = reinterpret_cast<int32_t*>(offs + m);
   InfArgs a;
   a.beta = beta; a.p1 = p1; a.p2 = p2; a.lb = layer_betas; a.E = n_edges; a.rt = rel_trans; a.rs = rel_sus;
-  a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32); a.day = day; a.variant = variant;
+  a.n_agents = n_agents; a.status = status; a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32); a.day = day; a.variant = variant;
   a.layer = layer;
   dim3 grid((unsigned)ntiles, 2);
   k_infections_count<<<grid, INF_THREADS, 0, s>>>(a, ntiles, counts);
@@ -949,10 +956,16 @@ int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open
     if (g.used && g.t0 == t0 && g.t1 == t1 && g.close_last == close_last && g.open_prev == open_prev &&
         memcmp(&g.st, st, sizeof(covgpu_state)) == 0) { hit = &g; break; }
   if (!hit) {
+    if (!g_capture_stream && cudaStreamCreateWithFlags(&g_capture_stream, cudaStreamNonBlocking) != cudaSuccess)
+      return COVGPU_CUDA_ERROR;
     cudaGraph_t graph = nullptr;
-    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return COVGPU_CUDA_ERROR;
-    enqueue_days(st, t0, t1, open_prev, close_last, s);
-    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) return COVGPU_CUDA_ERROR;
+    if (cudaStreamBeginCapture(g_capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return COVGPU_CUDA_ERROR;
+    const int erc = enqueue_days(st, t0, t1, open_prev, close_last, g_capture_stream);
+    if (cudaStreamEndCapture(g_capture_stream, &graph) != cudaSuccess || erc != COVGPU_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return COVGPU_CUDA_ERROR;
+    }
     GraphEntry& g = g_graphs[g_graph_next];
     g_graph_next = (g_graph_next + 1) % 8;
     if (g.used && g.exec) cudaGraphExecDestroy(g.exec);

@@ -465,12 +465,14 @@ class BatchState:
             f = self.t['flags'][s]
             f.copy_((f & ~bit) | (v * bit))
         elif key in cvd.BY_VARIANT_STATES:
+            # bit 31 does not fit a signed int32 scalar: edit the words as uint32 on the host
             shift = cvd.EXPOSED_BY_VARIANT_SHIFT if key == 'exposed_by_variant' else cvd.INFECTIOUS_BY_VARIANT_SHIFT
-            vals = torch.as_tensor(np.asarray(values, dtype=bool), device=self.device).to(torch.int32)
-            f = self.t['flags'][s]
+            vals = np.asarray(values.cpu().numpy() if torch.is_tensor(values) else values, dtype=bool)
+            f = self.t['flags'][s].cpu().numpy().view(np.uint32).copy()
             for v in range(vals.shape[0]):
-                bit = 1 << (shift + v)
-                f.copy_((f & ~bit) | (vals[v] * bit))
+                bit = np.uint32(1 << (shift + v))
+                f = np.where(vals[v], f | bit, f & ~bit).astype(np.uint32)
+            self.t['flags'][s].copy_(torch.from_numpy(f.view(np.int32)))
         elif key in cvd.VARIANT_STATES:
             shift = 8 * cvd.VARIANT_STATES.index(key)
             x = np.asarray(values, dtype=np.float64)

@@ -72,9 +72,11 @@ def _infections_op(beta: float, p1: torch.Tensor, p2: torch.Tensor, layer_betas:
     nbytes = int(L.lib().covgpu_infections_scratch_bytes(E))
     scratch = torch.empty(nbytes, dtype=_U8, device=dev)
     L.call('covgpu_infections', float(np.float32(beta)), _ptr(p1), _ptr(p2), _ptr(layer_betas), E, _ptr(rel_trans),
-           _ptr(rel_sus), _ptr(uniforms), int(seed) & 0xFFFFFFFFFFFFFFFF, int(day), int(variant), int(layer),
+           _ptr(rel_sus), min(rel_trans.numel(), rel_sus.numel()), _ptr(uniforms), int(seed) & 0xFFFFFFFFFFFFFFFF, int(day), int(variant), int(layer),
            _ptr(src), _ptr(tgt), cap, _ptr(count), _ptr(status), scratch.data_ptr(), nbytes, _stream())
     n = int(count.item())
+    if int(status.item()) & L.BADARG:
+        raise IndexError('compute_infections: an edge index is outside the agent arrays')
     return src[:n].clone(), tgt[:n].clone()
 
 

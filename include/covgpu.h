@@ -218,10 +218,12 @@ int covgpu_trans_sus(const float* rel_trans, const float* rel_sus, const uint8_t
  * draw from Philox keyed (seed, day, variant, layer, edge). *out_count
  * (device) receives the number of transmissions; if it exceeds capacity only
  * the first capacity are written and COVGPU_OVERFLOW is stored in *status.
+ * An edge whose p1 or p2 is outside [0, n_agents) is skipped and
+ * COVGPU_BADARG is stored in *status (status may be NULL).
  * scratch: device memory of covgpu_infections_scratch_bytes(n_edges) bytes. */
 int64_t covgpu_infections_scratch_bytes(int64_t n_edges);
 int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas,
-                      int64_t n_edges, const float* rel_trans, const float* rel_sus,
+                      int64_t n_edges, const float* rel_trans, const float* rel_sus, int64_t n_agents,
                       const double* uniforms, uint64_t seed, int32_t day, int32_t variant, int32_t layer,
                       int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
                       int32_t* status, void* scratch, int64_t scratch_bytes, void* stream);

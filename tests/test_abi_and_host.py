@@ -39,8 +39,8 @@ def test_entry_points_reject_bad_arguments_without_a_gpu():
     # rejected on the host before any CUDA call
     assert lib.covgpu_viral_load(0, None, None, None, -1, 0.3, 2.0, 4.0, None, None) == L.BADARG
     assert lib.covgpu_infections_scratch_bytes(-5) == -1
-    assert lib.covgpu_infections(0.1, None, None, None, 10, None, None, None, 0, 0, 0, 0, None, None, 0, None, None,
-                                 None, 0, None) == L.BADARG
+    assert lib.covgpu_infections(0.1, None, None, None, 10, None, None, 5, None, 0, 0, 0, 0, None, None, 0, None,
+                                 None, None, 0, None) == L.BADARG
     assert lib.covgpu_agent_step(None, 0, 1, 1, None) == L.BADARG
     assert lib.covgpu_run_days(None, 0, 10, 0, 1, 1, None) == L.BADARG
     st = L.State()
