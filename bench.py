@@ -1,0 +1,420 @@
+"""Benchmark: agent-days/s of the per-day step on the 1M-agent hybrid 180-day sim.
+
+Workload (one "step" = one full run of the sim): pop_size=1,000,000,
+pop_type='hybrid' (layers h/s/w/c, c redrawn every day), pop_infected=100,
+use_waning=True, n_days=180, float32. Synthetic population from the
+package's generators (same distributions as the reference's). Inputs
+(agents ~160 MB + edges ~62 MB) are larger than L2 (129 MB).
+
+  value        device-resident throughput: the population is in HBM, each
+               step rewinds the state (device copy) and runs 181 days as one
+               CUDA-graph launch (the rewind is inside the timed region)
+  e2e          the same metric through the public API: per step the pinned
+               host population is uploaded by cv.Sim(...).initialize(), run,
+               and the results copied back (finalize)
+  roofline     the dominant kernel, from per-kernel CUDA-event timing of one
+               extra ungraphed run; algorithmic bytes per launch are counted
+               from the day's state counts
+  cpu_baseline the CPU oracle (numpy restatement) on a bounded sample of the
+               same workload: a few days of the 1M hybrid sim
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun (N > 1) every rank runs its own replica (seed + rank); value
+is the sum over ranks, timed as the max over ranks (weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+POP = 1_000_000
+DAYS = 180
+PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--pop-size', type=int, default=POP)
+    ap.add_argument('--days', type=int, default=DAYS)
+    ap.add_argument('--cpu-days', type=int, default=3, help='days of the CPU oracle sample')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--json-out', default=None)
+    return ap.parse_args()
+
+
+def sim_pars(args, seed):
+    return dict(pop_size=args.pop_size, pop_type='hybrid', pop_infected=100, use_waning=True, n_days=args.days,
+                rand_seed=seed, dynam_layer=dict(h=0, s=0, w=0, c=1))
+
+
+# ----------------------------------------------------------------------------- distributed
+def dist_setup():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device='cuda' if torch.cuda.is_available() else 'cpu')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.gpu}', f'--query-gpu={self.Q}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith('active'):
+                    reasons.add(name)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': max(smax) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ----------------------------------------------------------------------------- algorithmic bytes
+def agent_pass_bytes(res, n, nv, t):
+    """Bytes one agent pass must move on day t (closing day t-1 fused in).
+
+    Every agent: flag + variant words read (8), date_recovered read (4), NAb
+    state read (nab, peak_nab, t_nab_event: 12), immunity written (12*nv).
+    Agents with NAbs: nab written (4). Exposed agents: five more date reads
+    (20). Infectious: rel_trans + the two other viral-load dates read (12) and
+    viral load written (4). Susceptible: rel_sus read (4). Role bitmaps: n/4.
+    """
+    ex = res['n_exposed'][t - 1] if t > 0 else 0
+    inf = res['n_infectious'][t - 1] if t > 0 else 0
+    sus = res['n_susceptible'][t - 1] if t > 0 else n
+    with_nabs = n - sus if t > 0 else 0  # upper bound: everyone ever infected has NAbs
+    return 8 * n + 4 * n + 12 * n + 12 * nv * n + 4 * with_nabs + 20 * ex + 16 * inf + 4 * sus + n / 4
+
+
+def edge_pass_bytes(spec, n):
+    """Bytes one edge pass must move: p1/p2 of every stored (static) edge, plus
+    the role bitmaps (n/4, L2-resident). Dynamic-layer edges are generated in
+    registers and move no bytes."""
+    e_static = sum(len(ly['p1']) for ly in spec.layers if not ly['dynamic'])
+    return 8 * e_static + n / 4
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def kernel_profile(sim, npts):
+    """One ungraphed run with CUDA events around each kernel (on the launching stream)."""
+    import torch
+    st = sim.state
+    times = {'agent_step': [], 'edge_pass': [], 'infect_claims': []}
+    stream = torch.cuda.current_stream()
+
+    def timed(name, fn):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        times[name].append((a, b))
+
+    for t in range(npts):
+        timed('agent_step', lambda: st.agent_step(t, do_prev=t > 0, do_day=True))
+        timed('edge_pass', lambda: st.edge_pass(t))
+        timed('infect_claims', lambda: st.infect_claims(t))
+    timed('agent_step', lambda: st.agent_step(npts, do_prev=True, do_day=False))
+    torch.cuda.synchronize()
+    return {k: [a.elapsed_time(b) for a, b in v] for k, v in times.items()}
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def gpu_arm(args, world, rank):
+    import torch
+    import covasim_gb300 as cv
+    from covasim_gb300.sim import choose_seed_infections, CALL_SEED
+    from covasim_gb300 import _lib as L
+
+    seed = 1 + rank
+    sim = cv.Sim(sim_pars(args, seed))
+    t0 = time.perf_counter()
+    sim.initialize()
+    init_s = time.perf_counter() - t0
+    st = sim.state
+    npts = sim.npts
+    snap = st.snapshot()
+    seeds = choose_seed_infections(sim['rand_seed'], sim['pop_size'], sim['pop_infected'])
+
+    def one_run():
+        st.restore(snap)
+        st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
+
+    for _ in range(args.warmup):
+        one_run()
+    torch.cuda.synchronize()
+    if st.status():
+        raise RuntimeError(f'device status {st.status()}')
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        one_run()
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    clk = clocks.stop()
+    elapsed = max_over_ranks(elapsed, world)
+    res = st.results(0)
+    n = sim['pop_size']
+    agent_days = n * args.days
+    value = world * agent_days * args.steps / elapsed
+
+    # per-kernel timing (one extra ungraphed run) for the roofline
+    st.restore(snap)
+    st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+    kt = kernel_profile(sim, npts)
+    res = st.results(0)
+    totals = {k: float(np.sum(v)) for k, v in kt.items()}
+    dom = max(totals, key=totals.get)
+    nv = 1
+    if dom == 'agent_step':
+        bytes_per = [agent_pass_bytes(res, n, nv, t) for t in range(npts + 1)]
+    elif dom == 'edge_pass':
+        bytes_per = [edge_pass_bytes(sim.spec, st.n)] * npts
+    else:
+        bytes_per = [16.0 * max(res['new_infections'][t], 1) for t in range(npts)]
+    avg_ms = totals[dom] / len(kt[dom])
+    achieved = float(np.mean(bytes_per)) / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    roofline = {'bound': 'hbm', 'kernel': f'k_{dom}', 'achieved': round(achieved, 1), 'peak': peak,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4), 'traffic': None,
+                'avg_launch_ms': round(avg_ms, 5),
+                'kernel_ms_total': {k: round(v, 3) for k, v in totals.items()},
+                'kernel_share': {k: round(v / sum(totals.values()), 4) for k, v in totals.items()}}
+    launches_per_step = 1 + 3 * npts + 1
+
+    # end to end through the public API, from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        pop = sim.popdict
+        pin = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).pin_memory()  # noqa: E731
+        host_pop = {'uid': pop['uid'], 'age': pop['age'], 'sex': pop['sex'], 'contacts': {}}
+        h2d = 0
+        for k, c in pop['contacts'].items():
+            host_pop['contacts'][k] = dict(p1=pin(c['p1'], np.int32), p2=pin(c['p2'], np.int32))
+            h2d += 8 * len(c['p1']) if not sim['dynam_layer'].get(k) else 0
+        host_person = {k: pin(v, np.float32) for k, v in sim._person.items()}
+        h2d += sum(4 * len(v) for v in host_person.values())
+        d2h = 0
+
+        def e2e_step():
+            s = cv.Sim(sim_pars(args, seed), popdict=host_pop, person=host_person)
+            s.run()
+            return s
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s = e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+        d2h = 8 * (L.N_RES_INT + L.N_RES_VAR + L.N_RES_F) * npts
+        e2e = {'value': round(world * agent_days * args.steps / e2e_s, 1), 'unit': 'agent-days/s',
+               'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+               'ms_per_step': round(1e3 * e2e_s / args.steps, 3)}
+        assert s.results['cum_infections'].values[-1] > 100
+
+    return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e,
+                launches=launches_per_step * args.steps, init_s=init_s, res=res, spec=sim.spec,
+                cum_infections=float(res['new_infections'].sum() + sim['pop_infected']))
+
+
+# ----------------------------------------------------------------------------- CPU oracle
+def _oracle_worker(args_tuple):
+    """Build a 1M hybrid sim and time `days` days of the CPU oracle (MT19937 mode)."""
+    pop_size, total_days, seed, warm, days = args_tuple
+    import numpy as np  # noqa: F811
+    sys.path.insert(0, ROOT)
+    import covasim_gb300 as cv
+    from oracle.sim import OracleSim, set_prognoses
+    from oracle.people import OraclePeople
+    pars = cv.make_pars(pop_size=pop_size, pop_type='hybrid', pop_infected=100, use_waning=True,
+                        n_days=total_days, rand_seed=seed, dynam_layer=dict(h=0, s=0, w=0, c=1))
+    pars['prognoses'] = cv.get_prognoses(True)
+    cv.init_immunity(pars, total_days + 1)
+    pop = cv.make_randpop(pars, rng=np.random.default_rng(seed))
+    tmp = OraclePeople(pars, pop_size)
+    tmp.age = np.asarray(pop['age'], np.float32)
+    set_prognoses(tmp, pars, np.random.RandomState(seed))
+    person = {k: tmp[k] for k in ('symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus')}
+    contacts = {k: dict(p1=c['p1'], p2=c['p2'], beta=np.ones(len(c['p1']), np.float32))
+                for k, c in ((k, pop['contacts'][k]) for k in pars['beta_layer'])}
+    sim = OracleSim(pars, person, contacts, rng='mt')
+    for _ in range(warm):
+        sim.step()
+    t0 = time.perf_counter()
+    for _ in range(days):
+        sim.step()
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(args, procs=1, warm=1, days=None):
+    days = args.cpu_days if days is None else days
+    if procs == 1:
+        dt = _oracle_worker((args.pop_size, args.days, 1, warm, days))
+        return args.pop_size * days / dt, dt
+    import multiprocessing as mp
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(procs) as pool:
+        dts = pool.map(_oracle_worker, [(args.pop_size, args.days, 1 + i, warm, days) for i in range(procs)])
+    return procs * args.pop_size * days / max(dts), max(dts)
+
+
+def reference_arm(args, world, rank):
+    """The reference's CPU implementation of the path (the numpy restatement: the
+    reference needs numba and sciris, which are not installed), on all host cores,
+    each process running its own 1M hybrid sim; a step is one simulated day."""
+    if rank != 0:
+        return
+    procs = max(1, min(os.cpu_count() or 1, 16))
+    t0 = time.perf_counter()
+    value, dt = cpu_baseline(args, procs=procs, warm=max(args.warmup, 1), days=args.steps)
+    line = {'metric': 'agent-days/s', 'value': round(value, 1), 'unit': 'agent-days/s', 'impl': 'reference',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': round(1e3 * dt / args.steps, 3), 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': f'hybrid {args.pop_size} agents, {args.days} days, waning, c redrawn daily',
+                       'sample': f'{args.steps} timed days after {max(args.warmup, 1)} warm-up days, '
+                                 f'{procs} independent sims in parallel'},
+            'cpu_baseline': {'value': round(value, 1), 'unit': 'agent-days/s', 'cores': procs, 'kind': 'port',
+                             'sample': f'{procs} x 1M-agent hybrid sims, {args.steps} days each (numpy oracle, '
+                                       'MT19937 mode)'},
+            'e2e': {'value': round(value, 1), 'unit': 'agent-days/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0},
+            'wall_s': round(time.perf_counter() - t0, 1)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == 'reference':
+        reference_arm(args, world, rank)
+        return
+    out = gpu_arm(args, world, rank)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, dt = cpu_baseline(args)
+        cpu = {'value': round(v, 1), 'unit': 'agent-days/s', 'cores': 1, 'kind': 'port',
+               'sample': f'{args.cpu_days} days (after 1 warm-up day) of the 1M-agent hybrid sim, numpy oracle in '
+                         f'MT19937 mode, one process ({dt:.1f} s)'}
+    if rank == 0:
+        line = {'metric': 'agent-days/s', 'value': round(out['value'], 1), 'unit': 'agent-days/s',
+                'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+                'ms_per_step': round(1e3 * out['elapsed'] / args.steps, 3), 'higher_is_better': True,
+                'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+                'config': {'workload': f'hybrid {args.pop_size} agents (h/s/w/c, c redrawn daily), '
+                                       f'{args.days} days, waning, pop_infected 100',
+                           'step': 'one full run: rewind state in HBM, seed, 181 days as one CUDA graph',
+                           'l2': 'inputs larger than L2 (agents ~160 MB + static edges ~62 MB)',
+                           'replicas': world, 'cum_infections_per_run': out['cum_infections']},
+                'edge_evaluations_per_s': None,
+                'roofline': out['roofline'], 'cpu_baseline': cpu, 'e2e': out['e2e'],
+                'gpu_launches': out['launches'], 'clocks': out['clocks']}
+        spec = out['spec']
+        e_all = sum(len(ly['p1']) for ly in spec.layers)
+        line['edge_evaluations_per_s'] = round(world * 2 * e_all * args.days * args.steps / out['elapsed'], 1)
+        print(json.dumps(line), flush=True)
+        if args.json_out:
+            with open(args.json_out, 'w') as f:
+                json.dump(line, f, indent=1)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -31,6 +31,7 @@ constexpr int64_t EDGE_TILE = 4096;    // edges per edge-pass block (must match 
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
 constexpr int INF_THREADS = 256;
 constexpr int INF_PER_THREAD = INF_TILE / INF_THREADS;
+constexpr int CALL_TAG_SEED = 1;       // covgpu_infect_list call_tag of the day-0 seed infections
 
 inline int launch_status() {
   return cudaGetLastError() == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
@@ -617,10 +618,15 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   st.n_infections[i] += 1;
   if (breakthrough) st.n_breakthroughs[i] += 1;
   st.vstate[i] = (st.vstate[i] & 0xFFFFFF00u) | (uint32_t)v;
-  atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_INFECTIONS]), 1ull);
-  if (reinfection)
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_REINFECTIONS]), 1ull);
-  atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_INFECTIONS) * nv + v]), 1ull);
+  // seed infections happen before update_states_pre resets the day's flows
+  // (sim.py:571-577, people.py:171), so they are not counted
+  const bool count = call_tag != CALL_TAG_SEED;
+  if (count) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_INFECTIONS]), 1ull);
+    if (reinfection)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_REINFECTIONS]), 1ull);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_INFECTIONS) * nv + v]), 1ull);
+  }
   // people.py:508-511: infection log
   if (st.log) {
     const unsigned long long pos = atomicAdd(st.log_count, 1ull);
@@ -670,7 +676,8 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
     u_inf2sym[i] = dis;
     const float ds = __fadd_rn(di, dis);
     d_sym[i] = ds;
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SYMPTOMATIC) * nv + v]), 1ull);
+    if (count)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SYMPTOMATIC) * nv + v]), 1ull);
     const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
                                   __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
     if (!(d.u[1] < (double)p_sev)) {  // CASE 2.1 mild, people.py:544-547
@@ -679,7 +686,8 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       u_disease[i] = (float)__dadd_rn((double)__fadd_rn(de, dis), dr);
       symp_class = 1;
     } else {  // CASE 2.2 severe, people.py:550-554
-      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
+      if (count)
+        atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
       const float dss = (float)sample_dist(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
       u_sym2sev[i] = dss;
       const float dsev = __fadd_rn(ds, dss);

@@ -79,6 +79,10 @@ def _layers_from_popdict(pars, popdict):
     layers = []
     for lkey in pars['beta_layer'].keys():
         c = popdict['contacts'].get(lkey, dict(p1=np.zeros(0, np.int32), p2=np.zeros(0, np.int32)))
+        if torch.is_tensor(c['p1']):  # device or pinned-host tensors: passed through (p1 must be sorted)
+            layers.append(dict(key=lkey, p1=c['p1'], p2=c['p2'], beta=c.get('beta'),
+                               dynamic=bool(pars['dynam_layer'].get(lkey, 0))))
+            continue
         p1 = np.asarray(c['p1'], dtype=np.int32)
         p2 = np.asarray(c['p2'], dtype=np.int32)
         beta = np.asarray(c.get('beta', np.ones(len(p1))), dtype=np.float32)
@@ -121,11 +125,13 @@ class Sim:
         use_graph (bool): capture the day loop in a CUDA graph
     """
 
-    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, **kwargs):
+    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, **kwargs):
         self.label = label
         self.pars = cvpar.make_pars()
         self.update_pars(pars, **kwargs)
         self.popdict = popdict
+        if person is not None:
+            self._person = person
         self.use_graph = use_graph
         self.people = None
         self.state = None
@@ -226,10 +232,13 @@ class Sim:
         self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity)
         contacts = Contacts()
         for ly in spec.layers:
-            contacts[ly['key']] = Layer(ly['p1'], ly['p2'], ly['beta'], label=ly['key'])
+            if torch.is_tensor(ly['p1']):
+                contacts[ly['key']] = ly
+            else:
+                contacts[ly['key']] = Layer(ly['p1'], ly['p2'], ly['beta'], label=ly['key'])
         self.people = People(self.state, 0, self.pars, contacts)
-        self.people['age'] = np.asarray(popdict['age'], dtype=cvd.default_float)
-        self.people['sex'] = np.asarray(popdict['sex'], dtype=cvd.default_float)
+        self.people['age'] = popdict['age']
+        self.people['sex'] = popdict['sex']
         self._open_day = None     # day whose closing pass (stocks, update_nab) is pending
         self._seeded = False
         self.initialized = True

@@ -166,16 +166,12 @@ class BatchState:
     # ------------------------------------------------------------------ building
     def _init_people(self):
         t = self.t
-        flags = np.zeros(self.n, dtype=np.int32)
-        host = {k: np.zeros(self.n, dtype=np.float32) for k in ('symp_prob', 'severe_prob', 'crit_prob',
-                                                                'death_prob', 'rel_trans', 'rel_sus')}
         for sp, off in zip(self.specs, self.offsets):
-            flags[off:off + sp.n] = SUS_NAIVE
-            for k in host:
-                host[k][off:off + sp.n] = np.asarray(sp.person[k], dtype=np.float32)
-        t['flags'].copy_(torch.from_numpy(flags))
-        for k, v in host.items():
-            t[k].copy_(torch.from_numpy(v))
+            t['flags'][off:off + sp.n] = SUS_NAIVE
+            for k in ('symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus'):
+                x = sp.person[k]
+                src = x if torch.is_tensor(x) else torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32))
+                t[k][off:off + sp.n].copy_(src, non_blocking=True)
 
     def _build_layers(self):
         self.segments = []   # (ctypes Layer, tensors kept alive)
@@ -184,7 +180,7 @@ class BatchState:
         tiles = 0
         for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
             for li, ly in enumerate(sp.layers):
-                p1 = np.asarray(ly['p1'], dtype=np.int64)
+                p1 = ly['p1'] if torch.is_tensor(ly['p1']) else np.asarray(ly['p1'], dtype=np.int64)
                 n_edges = len(p1)
                 if n_edges == 0:
                     continue
@@ -198,6 +194,29 @@ class BatchState:
                 if ly.get('dynamic'):
                     rec.dynamic = 1
                     rec.beta_const = 1.0
+                elif torch.is_tensor(ly['p1']):
+                    # torch inputs (e.g. pinned host memory): uploaded as they are, checked on the device
+                    tp1 = ly['p1'].to(self.device, torch.int32, non_blocking=True)
+                    tp2 = ly['p2'].to(self.device, torch.int32, non_blocking=True)
+                    lo1, hi1 = torch.aminmax(tp1)
+                    lo2, hi2 = torch.aminmax(tp2)
+                    if bool((tp1[1:] < tp1[:-1]).any()):
+                        raise ValueError(f'layer {ly["key"]}: p1 must be sorted')
+                    if min(int(lo1), int(lo2)) < 0 or max(int(hi1), int(hi2)) >= sp.n:
+                        raise ValueError(f'layer {ly["key"]}: agent index out of range')
+                    if off:
+                        tp1 += off
+                        tp2 += off
+                    rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
+                    keep += [tp1, tp2]
+                    b = ly.get('beta')
+                    if b is None or bool((b == b[0]).all()):
+                        rec.beta = None
+                        rec.beta_const = 1.0 if b is None else float(b[0])
+                    else:
+                        tb = b.to(self.device, torch.float32, non_blocking=True)
+                        rec.beta = tb.data_ptr()
+                        keep.append(tb)
                 else:
                     p2 = np.asarray(ly['p2'], dtype=np.int64)
                     beta = np.asarray(ly.get('beta', np.ones(n_edges)), dtype=np.float32)
@@ -404,6 +423,28 @@ class BatchState:
         L.call('covgpu_layer_materialize', self.cstate_ptr, int(seg), int(t), p1.data_ptr(), p2.data_ptr(),
                _stream())
         return p1, p2
+
+    # ------------------------------------------------------------------ snapshots
+    MUTABLE = ('flags', 'vstate', 'rel_trans', 'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event',
+               'sus_imm', 'symp_imm', 'sev_imm', 'dates', 'durs', 'vaccine_source')
+
+    def snapshot(self):
+        """Device copy of every array a run modifies (restore() rewinds to it)."""
+        return {k: self.t[k].clone() for k in self.MUTABLE}
+
+    def restore(self, snap):
+        """Rewind to a snapshot: agent arrays, results, claims, counters and status."""
+        for k, v in snap.items():
+            self.t[k].copy_(v)
+        self.res_int.zero_()
+        self.res_var.zero_()
+        self.res_fx.zero_()
+        self.t['claim'].fill_(-1)
+        self.t['roles'].zero_()
+        self.t['viral_load'].zero_()
+        self.t['event_count'].zero_()
+        self.t['log_count'].zero_()
+        self.t['status'].zero_()
 
     def status(self):
         return int(self.t['status'].item())

@@ -248,7 +248,9 @@ int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
 
 /* infect() for an explicit list of global agent indices (unique). layer_tag is
  * recorded in the infection log (>= COVGPU_MAX_LAYERS for non-layer sources);
- * call_tag selects the Philox stream (1: seed infections, 2: importations). */
+ * call_tag selects the Philox stream (1: seed infections, 2+: importations).
+ * Seed infections (call_tag 1) are not counted in the day's flows: the
+ * reference seeds before update_states_pre resets them (sim.py:571-577). */
 int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds,
                        int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream);
 
