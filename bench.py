@@ -370,8 +370,8 @@ def reference_arm(args, world, rank):
                        'sample': f'{args.steps} timed days after {max(args.warmup, 1)} warm-up days, '
                                  f'{procs} independent sims in parallel'},
             'cpu_baseline': {'value': round(value, 1), 'unit': 'agent-days/s', 'cores': procs, 'kind': 'port',
-                             'sample': f'{procs} x 1M-agent hybrid sims, {args.steps} days each (numpy oracle, '
-                                       'MT19937 mode)'},
+                             'sample': f'{procs} x {args.pop_size}-agent hybrid sims, {args.steps} days each '
+                                       '(numpy oracle, MT19937 mode)'},
             'e2e': {'value': round(value, 1), 'unit': 'agent-days/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0},
             'wall_s': round(time.perf_counter() - t0, 1)}
@@ -389,7 +389,7 @@ def main():
     if rank == 0 and not args.no_cpu:
         v, dt = cpu_baseline(args)
         cpu = {'value': round(v, 1), 'unit': 'agent-days/s', 'cores': 1, 'kind': 'port',
-               'sample': f'{args.cpu_days} days (after 1 warm-up day) of the 1M-agent hybrid sim, numpy oracle in '
+               'sample': f'{args.cpu_days} days (after 1 warm-up day) of the {args.pop_size}-agent hybrid sim, numpy oracle in '
                          f'MT19937 mode, one process ({dt:.1f} s)'}
     if rank == 0:
         line = {'metric': 'agent-days/s', 'value': round(out['value'], 1), 'unit': 'agent-days/s',
