@@ -60,9 +60,11 @@ class SimParams(C.Structure):
         ('immunity', C.c_float * (MAX_VARIANTS * MAX_VARIANTS)),
         ('rel_imm_asymp', C.c_double), ('rel_imm_mild', C.c_double), ('rel_imm_severe', C.c_double),
         ('nab_norm', C.c_double),
-        ('ve_exp_alpha', C.c_double * 3), ('ve_beta', C.c_double * 3),
+        ('ve_alpha', (C.c_float * 2) * 3), ('ve_beta', (C.c_float * 2) * 3),
+        ('ln_immunity', (C.c_float * 2) * (MAX_VARIANTS * MAX_VARIANTS)),
         ('dur', DurPar * len(DUR_ORDER)), ('nab_init', DurPar),
         ('nab_kin', C.c_void_p), ('beta_tab', C.c_void_p), ('beta_layer_tab', C.c_void_p), ('vx_imm', C.c_void_p),
+        ('vx_ln_imm', C.c_void_p),
         ('n_vaccines', C.c_int32), ('_pad2', C.c_int32),
         ('res_int', C.c_void_p), ('res_var', C.c_void_p), ('res_fx', C.c_void_p),
     ]

@@ -34,7 +34,8 @@ def nvcc_flags(extra=()):
 
 def build(verbose=False, force=False, extra=()):
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(CSRC, 'covgpu_device.cuh'), os.path.join(INCLUDE, 'covgpu.h'), __file__]
+    deps = srcs + [os.path.join(CSRC, f) for f in ('covgpu_device.cuh', 'covgpu_ff.cuh', 'covgpu_tables.h')]
+    deps += [os.path.join(INCLUDE, 'covgpu.h'), __file__]
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(d) <= lib_m for d in deps):

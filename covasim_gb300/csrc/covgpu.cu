@@ -19,6 +19,7 @@
 #include <math.h>
 #include "covgpu.h"
 #include "covgpu_device.cuh"
+#include "covgpu_ff.cuh"
 
 using namespace covgpu;
 
@@ -95,7 +96,7 @@ __device__ __forceinline__ bool inf_hit(const InfArgs& a, int dir, int64_t e, in
   } else {
     const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)a.day,
                                       TAG_EDGE | ((uint32_t)a.variant << 8) | (uint32_t)a.layer), a.k0, a.k1);
-    u = dir ? u01_52(w.z, w.w) : u01_52(w.x, w.y);
+    return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);
   }
   return u < (double)p;
 }
@@ -208,7 +209,11 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
   __shared__ unsigned int s_cnt[COVGPU_N_RES_INT];           // day t flows + severe/critical now
   __shared__ unsigned int s_prev[N_STOCKS];                   // day t-1 stocks
   __shared__ unsigned int s_var[COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS];  // [slot][v]
-  __shared__ double s_f[AGENT_THREADS / 32][3];
+  __shared__ long long s_f[AGENT_THREADS / 32][3];
+  __shared__ float s_ln_tab[COVGPU_LN_N][2];
+  __shared__ float s_exp_tab[COVGPU_EXP_N][2];
+  for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
+  for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
   for (int k = threadIdx.x; k < COVGPU_N_RES_INT; k += blockDim.x) s_cnt[k] = 0;
   for (int k = threadIdx.x; k < N_STOCKS; k += blockDim.x) s_prev[k] = 0;
   for (int k = threadIdx.x; k < COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS; k += blockDim.x) s_var[k] = 0;
@@ -218,7 +223,9 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
   uint32_t f = valid ? st.flags[i] : 0u;
   uint32_t vs = valid ? st.vstate[i] : 0xFFFFFFFFu;
   const uint32_t f_in = f, vs_in = vs;
-  double nab_sum = 0.0, sus_sum = 0.0, symp_sum = 0.0;
+  // reporting sums as fixed point (2^24 for NAbs, 2^32 for efficacies): exact integer
+  // reductions, independent of order, and no float64 work per agent
+  long long nab_fx = 0, sus_fx = 0, symp_fx = 0;
 
   // ---------------------------------------------------------- close day t-1
   if (do_prev) {
@@ -245,14 +252,11 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
             atomicOr(st.status, COVGPU_BADARG);
             k = k < 0 ? 0 : sp.nab_kin_len - 1;
           }
-          float x = (float)__dadd_rn((double)nab, __dmul_rn(sp.nab_kin[k], (double)peak));
-          if (x < 0.0f) x = 0.0f;
-          if (x > peak) x = peak;
-          nab = x;
+          nab = update_nab_ff(nab, peak, sp.nab_kin[2 * k], sp.nab_kin[2 * k + 1]);
           st.nab[i] = nab;
         }
       }
-      if (!(f & B_DEAD) && nab != 0.0f) nab_sum = (double)nab;  // sim.py:672
+      if (!(f & B_DEAD) && nab != 0.0f) nab_fx = __float2ll_rn(__fmul_rn(nab, 16777216.0f));  // sim.py:672
     }
   }
 
@@ -316,27 +320,42 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
       }
       vs = (vs & 0xFF000000u) | (rv << 16) | (iv << 8) | ev;
 
-      if (sp.use_waning) {  // check_immunity, immunity.py:303-350, float64
+      if (sp.use_waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
         const float dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
         const bool was_inf = tf >= dr;  // false for NaN
-        const double nab = (double)st.nab[i];
+        const float nab = st.nab[i];
+        ff ln_nab = ff{0.0f, 0.0f};
+        bool have_ln = false;
         for (int v = 0; v < nv; ++v) {
-          double nat = 0.0, vac = 0.0;
-          if (was_inf && rv < (uint32_t)nv) nat = (double)sp.immunity[v * COVGPU_MAX_VARIANTS + rv];
-          if ((f & B_VACC) && sp.vx_imm) {
-            const int src = st.vaccine_source[i];
-            if (src >= 0 && src < sp.n_vaccines) vac = (double)sp.vx_imm[src * nv + v];
+          // imm = max(natural, vaccine); ln(imm) from the host's tables
+          float imm = 0.0f;
+          ff ln_imm = ff{0.0f, 0.0f};
+          if (was_inf && rv < (uint32_t)nv) {
+            const int q = v * COVGPU_MAX_VARIANTS + (int)rv;
+            imm = sp.immunity[q];
+            ln_imm = ff{sp.ln_immunity[q][0], sp.ln_immunity[q][1]};
           }
-          const double eff = __dmul_rn(nab, fmax(nat, vac));
-          const float a = calc_ve(eff, sp.ve_exp_alpha[0], sp.ve_beta[0]);
-          const float b = calc_ve(eff, sp.ve_exp_alpha[1], sp.ve_beta[1]);
-          const float c = calc_ve(eff, sp.ve_exp_alpha[2], sp.ve_beta[2]);
+          if ((f & B_VACC) && sp.vx_imm && sp.vx_ln_imm) {
+            const int src = st.vaccine_source[i];
+            if (src >= 0 && src < sp.n_vaccines && sp.vx_imm[src * nv + v] > imm) {
+              imm = sp.vx_imm[src * nv + v];
+              ln_imm = ff{sp.vx_ln_imm[2 * (src * nv + v)], sp.vx_ln_imm[2 * (src * nv + v) + 1]};
+            }
+          }
+          float a = 0.0f, b = 0.0f, c = 0.0f;
+          if (nab > 0.0f && imm > 0.0f) {  // eff = nab * imm > 0; else every efficacy is 0
+            if (!have_ln) { ln_nab = ff_log(nab, s_ln_tab); have_ln = true; }
+            const ff ln_eff = ff_add(ln_nab, ln_imm);
+            a = ve_ff(ln_eff, ff{sp.ve_alpha[0][0], sp.ve_alpha[0][1]}, ff{sp.ve_beta[0][0], sp.ve_beta[0][1]}, s_exp_tab);
+            b = ve_ff(ln_eff, ff{sp.ve_alpha[1][0], sp.ve_alpha[1][1]}, ff{sp.ve_beta[1][0], sp.ve_beta[1][1]}, s_exp_tab);
+            c = ve_ff(ln_eff, ff{sp.ve_alpha[2][0], sp.ve_alpha[2][1]}, ff{sp.ve_beta[2][0], sp.ve_beta[2][1]}, s_exp_tab);
+          }
           const int64_t off = (int64_t)v * st.n + i;
           st.sus_imm[off] = a;
           st.symp_imm[off] = b;
           st.sev_imm[off] = c;
-          sus_sum = __dadd_rn(sus_sum, (double)a);
-          symp_sum = __dadd_rn(symp_sum, (double)b);
+          sus_fx += __float2ll_rn(__fmul_rn(a, 4294967296.0f));
+          symp_fx += __float2ll_rn(__fmul_rn(b, 4294967296.0f));
         }
       }
 
@@ -375,10 +394,10 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
   }
 
   // ---------------------------------------------------------- block totals
-  nab_sum = warp_sum(nab_sum);
-  sus_sum = warp_sum(sus_sum);
-  symp_sum = warp_sum(symp_sum);
-  if (lane == 0) { s_f[warp][0] = nab_sum; s_f[warp][1] = sus_sum; s_f[warp][2] = symp_sum; }
+  nab_fx = warp_sum_ll(nab_fx);
+  sus_fx = warp_sum_ll(sus_fx);
+  symp_fx = warp_sum_ll(symp_fx);
+  if (lane == 0) { s_f[warp][0] = nab_fx; s_f[warp][1] = sus_fx; s_f[warp][2] = symp_fx; }
   __syncthreads();
   const int npts = sp.npts;
   int64_t* res_t = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
@@ -402,19 +421,18 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
                        (unsigned long long)c);
     }
   }
-  // float sums: fixed-order in-block sum, then a fixed-point integer atomic
-  // (order independent, so the totals are bit-reproducible)
+  // block totals of the fixed-point sums, added with integer atomics (bit-reproducible)
   if (threadIdx.x == 0) {
-    double a = 0, b = 0, c = 0;
-    for (int w = 0; w < AGENT_THREADS / 32; ++w) { a = __dadd_rn(a, s_f[w][0]); b = __dadd_rn(b, s_f[w][1]); c = __dadd_rn(c, s_f[w][2]); }
-    if (do_prev && tp >= 0 && a != 0.0)
+    long long a = 0, b = 0, c = 0;
+    for (int w = 0; w < AGENT_THREADS / 32; ++w) { a += s_f[w][0]; b += s_f[w][1]; c += s_f[w][2]; }
+    if (do_prev && tp >= 0 && a != 0)
       atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)tp * COVGPU_N_RES_F + 0]),
-                (unsigned long long)llrint(ldexp(a, COVGPU_FX_NAB_BITS)));
-    if (do_day && t < npts && (b != 0.0 || c != 0.0)) {
+                (unsigned long long)a);
+    if (do_day && t < npts && (b != 0 || c != 0)) {
       atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)t * COVGPU_N_RES_F + 1]),
-                (unsigned long long)llrint(ldexp(b, COVGPU_FX_IMM_BITS)));
+                (unsigned long long)b);
       atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)t * COVGPU_N_RES_F + 2]),
-                (unsigned long long)llrint(ldexp(c, COVGPU_FX_IMM_BITS)));
+                (unsigned long long)c);
     }
   }
 }
@@ -457,20 +475,17 @@ __device__ __noinline__ bool edge_dir(const covgpu_state& st, const SegCtx& c, i
   const float beta = __ldg(sp.beta_tab + (int64_t)t * c.nv + v);
   const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
   if (p == 0.0f) return false;
-  double u;
-  if (st.edge_uniforms) {
-    const int seg = (int)(c.L - st.segments);
-    u = st.edge_uniforms[seg][((int64_t)v * 2 + dir) * c.L->n_edges + e];
-  } else {
-    if (w_variant != (int)v) {
-      w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
-                            TAG_EDGE | (v << 8) | (uint32_t)c.L->layer), sp.key0, sp.key1);
-      w_variant = (int)v;
-    }
-    u = dir ? u01_52(w.z, w.w) : u01_52(w.x, w.y);
-  }
   v_out = v;
-  return u < (double)p;
+  if (st.edge_uniforms) {  // injected draws (test mode)
+    const int seg = (int)(c.L - st.segments);
+    return st.edge_uniforms[seg][((int64_t)v * 2 + dir) * c.L->n_edges + e] < (double)p;
+  }
+  if (w_variant != (int)v) {
+    w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
+                          TAG_EDGE | (v << 8) | (uint32_t)c.L->layer), sp.key0, sp.key1);
+    w_variant = (int)v;
+  }
+  return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);  // u < p in float64, decided in integers
 }
 
 __device__ __forceinline__ uint64_t event_key(int t, uint32_t v, int layer, int dir, int64_t e) {
@@ -575,7 +590,14 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
 
 // ============================================================ infect
 
-struct DrawSet { double z[6]; double u[4]; };
+struct DrawSet {
+  double z[6];
+  double u[4];       // injected uniforms (test mode)
+  uint32_t uw[4];    // Philox words of the uniforms
+  bool injected;
+  // u_k < p exactly as float64 compares them (integer test for Philox words)
+  __device__ __forceinline__ bool lt(int k, float p) const { return injected ? (u[k] < (double)p) : bern32(uw[k], p); }
+};
 
 __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i,
                                           int64_t local, int t, int call_tag, DrawSet& d) {
@@ -585,8 +607,10 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
     for (int k = 0; k < 6; ++k) d.z[k] = r[k];
 #pragma unroll
     for (int k = 0; k < 4; ++k) d.u[k] = r[6 + k];
+    d.injected = true;
     return;
   }
+  d.injected = false;
   const uint32_t tag = TAG_INFECT | (uint32_t)call_tag;
   const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b1 = philox(make_uint4((uint32_t)local, 1u, (uint32_t)t, tag), sp.key0, sp.key1);
@@ -594,10 +618,10 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   box_muller(b0.x, b0.y, d.z[0], d.z[1]);
   box_muller(b0.z, b0.w, d.z[2], d.z[3]);
   box_muller(b1.x, b1.y, d.z[4], d.z[5]);
-  d.u[0] = u01_32(b1.z);
-  d.u[1] = u01_32(b1.w);
-  d.u[2] = u01_32(b2.x);
-  d.u[3] = u01_32(b2.y);
+  d.uw[0] = b1.z;
+  d.uw[1] = b1.w;
+  d.uw[2] = b2.x;
+  d.uw[3] = b2.y;
 }
 
 // people.py:435-586 for one agent (already deduplicated), plus update_peak_nab
@@ -666,7 +690,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   // people.py:523-527
   const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
                                   __fsub_rn(1.0f, st.symp_imm[(int64_t)v * st.n + i]));
-  if (!(d.u[0] < (double)sp_symp)) {  // CASE 1: asymptomatic, people.py:530-532
+  if (!d.lt(0, sp_symp)) {  // CASE 1: asymptomatic, people.py:530-532
     const double dr = sample_dist(sp.dur[COVGPU_D_ASYM2REC], d.z[4]);
     rec = (float)__dadd_rn((double)di, dr);
     u_disease[i] = (float)__dadd_rn((double)de, dr);
@@ -680,7 +704,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SYMPTOMATIC) * nv + v]), 1ull);
     const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
                                   __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
-    if (!(d.u[1] < (double)p_sev)) {  // CASE 2.1 mild, people.py:544-547
+    if (!d.lt(1, p_sev)) {  // CASE 2.1 mild, people.py:544-547
       const double dr = sample_dist(sp.dur[COVGPU_D_MILD2REC], d.z[4]);
       rec = (float)__dadd_rn((double)ds, dr);
       u_disease[i] = (float)__dadd_rn((double)__fadd_rn(de, dis), dr);
@@ -694,7 +718,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       d_sev[i] = dsev;
       const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], st.crit_prob[i]), hosp_max ? sp.no_hosp_factor : 1.0f);
       symp_class = 2;
-      if (!(d.u[2] < (double)p_crit)) {  // CASE 2.2.1 not critical, people.py:557-559
+      if (!d.lt(2, p_crit)) {  // CASE 2.2.1 not critical, people.py:557-559
         const double dr = sample_dist(sp.dur[COVGPU_D_SEV2REC], d.z[4]);
         rec = (float)__dadd_rn((double)dsev, dr);
         u_disease[i] = (float)__dadd_rn((double)__fadd_rn(__fadd_rn(de, dis), dss), dr);
@@ -705,7 +729,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
         d_crit[i] = dcrit;
         const float p_death = __fmul_rn(__fmul_rn(sp.rel_death[v], st.death_prob[i]), icu_max ? sp.no_icu_factor : 1.0f);
         const float dsum = __fadd_rn(__fadd_rn(__fadd_rn(de, dis), dss), dsc);
-        if (!(d.u[3] < (double)p_death)) {  // CASE 2.2.2.1 alive, people.py:569-571
+        if (!d.lt(3, p_death)) {  // CASE 2.2.2.1 alive, people.py:569-571
           const double dr = sample_dist(sp.dur[COVGPU_D_CRIT2REC], d.z[4]);
           rec = (float)__dadd_rn((double)dcrit, dr);
           u_disease[i] = (float)__dadd_rn((double)dsum, dr);

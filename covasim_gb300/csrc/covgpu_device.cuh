@@ -104,16 +104,11 @@ __device__ __forceinline__ float viral_load_one(int t, float ts, float tr, float
   return __fdiv_rn(early ? load_ratio : 1.0f, den);
 }
 
-// immunity.py:216-247 calc_VE in float64, stored as float32
-__device__ __forceinline__ float calc_ve(double eff, double exp_alpha, double beta) {
-  const double lo = __dmul_rn(exp_alpha, pow(eff, beta));
-  return (float)__ddiv_rn(lo, __dadd_rn(1.0, lo));
-}
 
 // ---------------------------------------------------------------- block reduction helpers
-__device__ __forceinline__ double warp_sum(double x) {
+__device__ __forceinline__ long long warp_sum_ll(long long x) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x = __dadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
   return x;
 }
 

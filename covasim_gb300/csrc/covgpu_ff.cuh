@@ -1,0 +1,170 @@
+// Float-float ("two-float", ~44-bit) arithmetic for the float64 steps of the
+// reference, so that they run on GB300's float32 units.
+//
+// GB300 executes float64 at a small fraction of its float32 rate. The
+// reference computes the NAb efficacy (immunity.py:216-247 calc_VE, called by
+// check_immunity for every agent every day) and update_nab (immunity.py:205-213)
+// in float64 and stores float32; here the same quantities are computed with
+// error-free transformations (two-sum, two-product via fused multiply-add) to
+// about 2^-44 relative and rounded once to float32, which reproduces the
+// reference's float32 result except when the exact value lies within ~2^-40 of
+// a float32 rounding boundary.
+//
+// Only IEEE round-to-nearest add/sub/mul/div and fused multiply-add (used for
+// exact product residuals only) appear, in a fixed order: the numpy mirror in
+// the oracle (oracle/gpu_arith.py) performs the same operations and gets the
+// same bits. ln uses the reduction x = 2^e * c_j * (1 + r), |r| < 2^-7.5, and
+// the series of ln(1 + r); exp uses Cody-Waite reduction by ln2/64, a table
+// of 2^(j/64) and the Taylor series of exp(r), |r| <= ln2/128.
+#pragma once
+#include <stdint.h>
+#include "covgpu_tables.h"
+
+namespace covgpu {
+
+struct ff { float hi, lo; };
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return ff{s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return ff{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff x, ff y) {
+  const ff s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ ff ff_mul(ff x, ff y) {
+  const ff p = two_prod(x.hi, y.hi);
+  return fast_two_sum(p.hi, __fadd_rn(p.lo, __fadd_rn(__fmul_rn(x.hi, y.lo), __fmul_rn(x.lo, y.hi))));
+}
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const ff p = two_prod(q1, b.hi);
+  float r = __fsub_rn(__fsub_rn(a.hi, p.hi), p.lo);
+  r = __fadd_rn(r, a.lo);
+  r = __fsub_rn(r, __fmul_rn(q1, b.lo));
+  return fast_two_sum(q1, __fdiv_rn(r, b.hi));
+}
+
+// ln(x) for finite x > 0, as float-float. tab: COVGPU_LN_TAB (shared memory copy).
+__device__ __forceinline__ ff ff_log(float x, const float (*tab)[2]) {
+  int e_adj = 0;
+  if (x < 1.17549435e-38f) { x = __fmul_rn(x, 16777216.0f); e_adj = -24; }
+  const int bits = __float_as_int(x);
+  int e = ((bits >> 23) & 0xff) - 127 + e_adj;
+  float m = __int_as_float((bits & 0x7fffff) | 0x3f800000);
+  if (m > 1.41421356f) { m = __fmul_rn(m, 0.5f); e += 1; }
+  const int j = (int)rintf(__fmul_rn(__fsub_rn(m, 1.0f), 128.0f));
+  const float c = __fadd_rn(1.0f, __fmul_rn((float)j, 0.0078125f));
+  const float d = __fsub_rn(m, c);
+  const float rh = __fdiv_rn(d, c);
+  const float rl = __fdiv_rn(__fmaf_rn(-rh, c, d), c);
+  // ln(1 + r) = r - r^2/2 + r^3 (1/3 - r/4 + r^2/5 - r^3/6 + r^4/7)
+  const ff sq = two_prod(rh, rh);
+  const float qh = __fmul_rn(sq.hi, 0.5f);
+  const float ql = __fadd_rn(__fmul_rn(sq.lo, 0.5f), __fmul_rn(rh, rl));
+  float poly = __fsub_rn(0.166666672f, __fmul_rn(rh, 0.142857149f));   // 1/6 - r/7
+  poly = __fsub_rn(0.200000003f, __fmul_rn(rh, poly));                  // 1/5 - r(...)
+  poly = __fsub_rn(0.25f, __fmul_rn(rh, poly));                         // 1/4 - r(...)
+  poly = __fsub_rn(0.333333343f, __fmul_rn(rh, poly));                  // 1/3 - r(...)
+  const float tail = __fmul_rn(__fmul_rn(sq.hi, rh), poly);
+  const ff a = two_sum(rh, -qh);
+  const ff l1p = fast_two_sum(a.hi, __fadd_rn(a.lo, __fsub_rn(__fadd_rn(rl, tail), ql)));
+  const float ef = (float)e;
+  const ff s1 = two_sum(__fmul_rn(ef, COVGPU_LN2_HI), tab[j - COVGPU_LN_J0][0]);
+  const ff s2 = two_sum(s1.hi, l1p.hi);
+  const float small = __fadd_rn(__fadd_rn(__fmul_rn(ef, COVGPU_LN2_LO), __fmul_rn(ef, COVGPU_LN2_LO2)),
+                                __fadd_rn(tab[j - COVGPU_LN_J0][1], l1p.lo));
+  return fast_two_sum(s2.hi, __fadd_rn(__fadd_rn(s1.lo, s2.lo), small));
+}
+
+// exp(y) for y <= 0, y.hi >= -87, as float-float. tab: COVGPU_EXP_TAB.
+__device__ __forceinline__ ff ff_exp_neg(ff y, const float (*tab)[2]) {
+  const int k = (int)rintf(__fmul_rn(y.hi, COVGPU_INV_LN2_64));
+  const int j = k & 63;
+  const int m = k >> 6;
+  const float kf = (float)k;
+  const float t0 = __fsub_rn(y.hi, __fmul_rn(kf, COVGPU_LN2_64_HI));
+  const ff pm = two_prod(kf, COVGPU_LN2_64_MID);
+  const ff s = two_sum(t0, -pm.hi);
+  const float e = __fadd_rn(__fsub_rn(__fsub_rn(s.lo, pm.lo), __fmul_rn(kf, COVGPU_LN2_64_LO)), y.lo);
+  const ff r = fast_two_sum(s.hi, e);
+  // exp(r) = 1 + r + r^2 (1/2 + r (1/6 + r (1/24 + r/120)))
+  float poly = __fadd_rn(0.0416666679f, __fmul_rn(r.hi, 0.00833333377f));
+  poly = __fadd_rn(0.166666672f, __fmul_rn(r.hi, poly));
+  poly = __fadd_rn(0.5f, __fmul_rn(r.hi, poly));
+  const float tail = __fmul_rn(__fmul_rn(r.hi, r.hi), poly);
+  const ff a = two_sum(1.0f, r.hi);
+  const ff er = fast_two_sum(a.hi, __fadd_rn(a.lo, __fadd_rn(r.lo, tail)));
+  const ff x = ff_mul(er, ff{tab[j][0], tab[j][1]});
+  const float scale = __int_as_float((m + 127) << 23);  // 2^m, m in [-126, 0]
+  return ff{__fmul_rn(x.hi, scale), __fmul_rn(x.lo, scale)};
+}
+
+// calc_VE (immunity.py:216-247) for eff = nab * imm with ln(imm) given:
+// exp(alpha) * eff^beta / (1 + exp(alpha) * eff^beta) = logistic(z),
+// z = alpha + beta * (ln nab + ln imm); rounded once to float32.
+__device__ __forceinline__ float ve_ff(ff ln_eff, ff alpha, ff beta, const float (*etab)[2]) {
+  const ff z = ff_add(alpha, ff_mul(beta, ln_eff));
+  const bool pos = z.hi >= 0.0f;
+  const ff y = pos ? ff{-z.hi, -z.lo} : z;
+  if (y.hi < -87.0f) return pos ? 1.0f : 0.0f;  // |z| > 87: 1 - 1e-38 rounds to 1; e^-87 flushed to 0
+  const ff x = ff_exp_neg(y, etab);
+  const ff den = fast_two_sum(1.0f, x.hi);
+  const ff q = ff_div(x, ff{den.hi, __fadd_rn(den.lo, x.lo)});
+  if (pos) {
+    const ff om = two_sum(1.0f, -q.hi);
+    return __fadd_rn(om.hi, __fsub_rn(om.lo, q.lo));
+  }
+  return __fadd_rn(q.hi, q.lo);
+}
+
+// update_nab (immunity.py:205-213): nab + kin * peak, rounded once to float32,
+// with kin given as a float pair (hi, lo); then clamped to [0, peak].
+__device__ __forceinline__ float update_nab_ff(float nab, float peak, float kh, float kl) {
+  const ff p = two_prod(kh, peak);
+  const float t = __fmul_rn(kl, peak);
+  const ff s = two_sum(nab, p.hi);
+  float x = __fadd_rn(s.hi, __fadd_rn(s.lo, __fadd_rn(p.lo, t)));
+  if (x < 0.0f) x = 0.0f;
+  if (x > peak) x = peak;
+  return x;
+}
+
+// u < p with u = lhs * 2^-nbits (lhs odd, lhs < 2^nbits) and p a float32,
+// decided exactly in integers: the same answer as comparing the two values
+// in float64, where both are exact.
+__device__ __forceinline__ bool frac_less(uint64_t lhs, int nbits, float p) {
+  if (!(p > 0.0f)) return false;
+  if (p >= 1.0f) return true;
+  const uint32_t bits = __float_as_uint(p);
+  const int ex = (bits >> 23) & 0xff;
+  uint64_t mant = bits & 0x7fffffu;
+  int e2;
+  if (ex) { mant |= 0x800000u; e2 = ex - 150; } else { e2 = -149; }
+  const int sh = e2 + nbits;  // u < p  <=>  lhs < mant * 2^sh
+  if (sh >= 0) return lhs < (mant << sh);   // p < 1: mant * 2^sh < 2^nbits, no overflow
+  if (sh <= -64) return false;
+  const uint64_t q = mant >> (-sh);
+  const uint64_t rem = mant & ((1ull << (-sh)) - 1ull);
+  return lhs < q || (lhs == q && rem != 0);
+}
+// Philox words -> the (0,1) doubles of u01_52 / u01_32, compared with p exactly
+__device__ __forceinline__ bool bern52(uint32_t a, uint32_t b, float p) {
+  const uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);
+  return frac_less(2 * k + 1, 53, p);
+}
+__device__ __forceinline__ bool bern32(uint32_t a, float p) {
+  return frac_less(2 * (uint64_t)a + 1, 33, p);
+}
+
+}  // namespace covgpu

@@ -1,0 +1,90 @@
+"""Generate covgpu_tables.h: float-float tables for the NAb-efficacy math.
+
+ln(c_j) for the reduction points c_j = 1 + j/128 (j = -40..55) and 2^(j/64)
+(j = 0..63), each as a pair of float32 (hi, lo) with hi + lo equal to the
+value to about 2^-48. Values come from Python's decimal module at 50 digits,
+so the tables are the same on every platform. Run from the repository root:
+
+    python covasim_gb300/csrc/gen_tables.py
+"""
+import math
+import os
+import struct
+from decimal import Decimal, getcontext
+
+getcontext().prec = 50
+
+LN_J0, LN_J1 = -40, 55          # c_j = 1 + j/128 covers m in [0.6875, 1.4297]
+EXP_N = 64
+
+
+def f32(x):
+    return struct.unpack('<f', struct.pack('<f', float(x)))[0]
+
+
+def split(d):
+    """Decimal -> (hi, lo) float32 pair."""
+    hi = f32(d)
+    lo = f32(d - Decimal(hi))
+    return hi, lo
+
+
+def ln_table():
+    out = []
+    for j in range(LN_J0, LN_J1 + 1):
+        c = Decimal(1) + Decimal(j) / Decimal(128)
+        out.append(split(c.ln()))
+    return out
+
+
+def exp_table():
+    ln2 = Decimal(2).ln()
+    return [split((Decimal(j) / Decimal(EXP_N) * ln2).exp()) for j in range(EXP_N)]
+
+
+def ln2_64_parts():
+    """ln(2)/64 as C_HI (11 significant bits, so k * C_HI is exact for |k| < 2^13) + C_MID + C_LO."""
+    c = Decimal(2).ln() / Decimal(64)
+    be = math.floor(math.log2(float(c)))
+    hi = float(round(c / Decimal(2) ** (be - 10)) * Decimal(2) ** (be - 10))
+    mid = f32(c - Decimal(hi))
+    lo = f32(c - Decimal(hi) - Decimal(mid))
+    return f32(hi), mid, lo
+
+
+def hexf(x):
+    return float(x).hex() + 'f'
+
+
+def main():
+    lt, et = ln_table(), exp_table()
+    lines = ['// Generated by covasim_gb300/csrc/gen_tables.py -- do not edit.',
+             '// float-float (hi, lo) tables for the NAb efficacy math in covgpu_device.cuh.',
+             '#pragma once',
+             f'#define COVGPU_LN_J0 ({LN_J0})',
+             f'#define COVGPU_LN_N {len(lt)}',
+             f'#define COVGPU_EXP_N {EXP_N}',
+             ]
+    ln2 = Decimal(2).ln()
+    ln2_hi = float(round(ln2 * 2 ** 16) / Decimal(2 ** 16))  # 16 significant bits: e * LN2_HI exact for |e| < 2^8
+    ln2_lo = f32(ln2 - Decimal(ln2_hi))
+    ln2_lo2 = f32(ln2 - Decimal(ln2_hi) - Decimal(ln2_lo))
+    lines += [f'#define COVGPU_LN2_HI {hexf(f32(ln2_hi))}', f'#define COVGPU_LN2_LO {hexf(ln2_lo)}',
+              f'#define COVGPU_LN2_LO2 {hexf(ln2_lo2)}',
+              f'#define COVGPU_INV_LN2_64 {hexf(f32(Decimal(64) / ln2))}']
+    ch, cm, cl = ln2_64_parts()
+    lines += [f'#define COVGPU_LN2_64_HI {hexf(ch)}', f'#define COVGPU_LN2_64_MID {hexf(cm)}',
+              f'#define COVGPU_LN2_64_LO {hexf(cl)}',
+              '__device__ const float COVGPU_LN_TAB[COVGPU_LN_N][2] = {']
+    lines += [f'  {{{hexf(h)}, {hexf(l)}}},' for h, l in lt]
+    lines += ['};', '__device__ const float COVGPU_EXP_TAB[COVGPU_EXP_N][2] = {']
+    lines += [f'  {{{hexf(h)}, {hexf(l)}}},' for h, l in et]
+    lines += ['};', '']
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'covgpu_tables.h')
+    with open(path, 'w') as f:
+        f.write('\n'.join(lines))
+    print(path)
+
+
+if __name__ == '__main__':
+    main()

@@ -18,6 +18,7 @@ A single simulation is a batch of one; ``covasim_gb300.Sim`` and
 ``covasim_gb300.BatchSim`` both drive this class.
 """
 import ctypes as C
+from decimal import Decimal, getcontext
 
 import numpy as np
 import torch
@@ -26,6 +27,7 @@ from . import _lib as L
 from . import defaults as cvd
 
 F32, I32, I64, F64 = torch.float32, torch.int32, torch.int64, torch.float64
+getcontext().prec = 50
 
 STATE_BIT = cvd.STATE_BIT
 SUS_NAIVE = (1 << STATE_BIT['susceptible']) | (1 << STATE_BIT['naive'])
@@ -38,6 +40,21 @@ def _align(x, a):
 
 def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ff_split(x):
+    """A float64 value as a float32 pair (hi, lo), hi + lo = x to ~2^-48."""
+    x = float(x)
+    hi = np.float32(x)
+    return float(hi), float(np.float32(x - float(hi)))
+
+
+def ff_log(x):
+    """ln(x) of a positive value as a float32 pair, from the decimal module (platform independent)."""
+    d = Decimal(float(x)).ln()
+    hi = np.float32(float(d))
+    lo = np.float32(float(d - Decimal(float(hi))))
+    return float(hi), float(lo)
 
 
 def dur_par(dist):
@@ -148,11 +165,14 @@ class BatchState:
         for sp in self.specs:
             beta_tabs.append(sp.beta_table().ravel())
             bl_tabs.append(sp.beta_layer_sched.astype(np.float32).ravel())
-            kin = sp.pars.get('nab_kin')
-            kins.append(np.asarray(kin if kin is not None else np.zeros(1), dtype=np.float64))
+            kin = np.asarray(sp.pars.get('nab_kin') if sp.pars.get('nab_kin') is not None else np.zeros(1),
+                             dtype=np.float64)
+            hi = kin.astype(np.float32)
+            lo = (kin - hi.astype(np.float64)).astype(np.float32)
+            kins.append(np.stack([hi, lo], axis=1).ravel())   # float pairs: hi + lo = nab_kin to ~2^-48
         self.beta_tab = torch.from_numpy(np.concatenate(beta_tabs)).to(dev)
         self.beta_layer_tab = torch.from_numpy(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32)).to(dev)
-        self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)
+        self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)  # float32 pairs
 
         self._init_people()
         self._build_layers()
@@ -262,7 +282,7 @@ class BatchState:
             seed = int(p['rand_seed']) & 0xFFFFFFFFFFFFFFFF
             r.key0, r.key1 = seed & 0xFFFFFFFF, seed >> 32
             r.use_waning = int(bool(p['use_waning']))
-            r.nab_kin_len = len(kins[s])
+            r.nab_kin_len = len(kins[s]) // 2
             r.n_beds_hosp = -1 if p['n_beds_hosp'] is None else int(p['n_beds_hosp'])
             r.n_beds_icu = -1 if p['n_beds_icu'] is None else int(p['n_beds_icu'])
             vd = p['viral_dist']
@@ -295,13 +315,19 @@ class BatchState:
             r.nab_norm = 1 + ne['alpha_inf_diff']
             for j, (a, b) in enumerate([('alpha_inf', 'beta_inf'), ('alpha_symp_inf', 'beta_symp_inf'),
                                         ('alpha_sev_symp', 'beta_sev_symp')]):
-                r.ve_exp_alpha[j] = float(np.exp(ne[a]))   # immunity.py:245
-                r.ve_beta[j] = float(ne[b])
+                r.ve_alpha[j][0], r.ve_alpha[j][1] = ff_split(ne[a])   # exp(alpha) * eff^beta = e^(alpha + beta ln eff)
+                r.ve_beta[j][0], r.ve_beta[j][1] = ff_split(ne[b])
+            if imm is not None:
+                for a in range(sp.nv):
+                    for b in range(sp.nv):
+                        x = float(imm[a, b])
+                        if x > 0:
+                            r.ln_immunity[a * L.MAX_VARIANTS + b][0], r.ln_immunity[a * L.MAX_VARIANTS + b][1] = ff_log(x)
             for j, key in enumerate(L.DUR_ORDER):
                 r.dur[j] = dur_par(p['dur'][key])
             nab_init = p['nab_init']
             r.nab_init = dur_par(nab_init) if nab_init is not None else L.DurPar(L.DIST_ZERO, 0, 0.0, 0.0)
-            r.nab_kin = self.nab_kin.data_ptr() + 8 * kn
+            r.nab_kin = self.nab_kin.data_ptr() + 4 * kn
             r.beta_tab = self.beta_tab.data_ptr() + 4 * bt
             r.beta_layer_tab = self.beta_layer_tab.data_ptr() + 4 * bl
             r.vx_imm = None

@@ -114,13 +114,17 @@ typedef struct covgpu_sim_params {
   float rel_crit[COVGPU_MAX_VARIANTS], rel_death[COVGPU_MAX_VARIANTS];
   float immunity[COVGPU_MAX_VARIANTS * COVGPU_MAX_VARIANTS]; /* [variant][recovered_variant] */
   double rel_imm_asymp, rel_imm_mild, rel_imm_severe, nab_norm; /* nab_norm = 1 + alpha_inf_diff */
-  double ve_exp_alpha[3], ve_beta[3];                         /* sus, symp, sev              */
+  /* calc_VE parameters (immunity.py:216-247) as float pairs (hi, lo): alpha and
+   * beta of the sus, symp and sev axes, and ln of each immunity-matrix entry */
+  float ve_alpha[3][2], ve_beta[3][2];
+  float ln_immunity[COVGPU_MAX_VARIANTS * COVGPU_MAX_VARIANTS][2];
   covgpu_dur_par dur[COVGPU_N_DUR_PARS];
   covgpu_dur_par nab_init;
-  const double* nab_kin;          /* [nab_kin_len]                                   */
+  const float* nab_kin;           /* [nab_kin_len][2] nab_kin as float pairs (hi, lo) */
   const float* beta_tab;          /* [npts][n_variants] float32 beta per day/variant */
   const float* beta_layer_tab;    /* [npts][n_layers]                                */
   const float* vx_imm;            /* [n_vaccines][n_variants] or NULL                */
+  const float* vx_ln_imm;         /* [n_vaccines][n_variants][2] ln(vx_imm) pairs    */
   int32_t n_vaccines;
   int32_t _pad2;
   int64_t* res_int;               /* [npts][COVGPU_N_RES_INT]                        */

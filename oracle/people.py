@@ -179,7 +179,11 @@ class OraclePeople:
         self.flows['new_deaths'] += new_deaths
         self.flows['new_known_deaths'] += new_known_deaths
         if self.pars['use_waning']:
-            check_immunity(self)
+            if getattr(self, 'arith', 'reference') == 'gpu':
+                from .gpu_arith import check_immunity_gpu
+                check_immunity_gpu(self)
+            else:
+                check_immunity(self)
 
     def check_inds(self, current, date, filter_inds=None):
         """people.py:211-219."""

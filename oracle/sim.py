@@ -12,6 +12,10 @@ Two random-number modes:
 * ``rng='mt'``: two MT19937 streams seeded with the sim's seed, one standing in
   for numba's (edge Bernoullis, ``choose``/``choose_r``) and one for numpy's
   (``infect`` and ``set_prognoses``), consumed in the reference's call order.
+
+Philox mode also evaluates the NAb efficacy and update_nab with the CUDA
+library's float-float formulation (``gpu_arith``) by default, so that a GPU
+run and this loop agree bit for bit; MT mode uses the reference's float64.
 """
 import numpy as np
 
@@ -19,6 +23,7 @@ from . import philox as ph
 from .kernels import compute_viral_load, compute_trans_sus, compute_infections
 from .people import (OraclePeople, TableDraws, SequentialDraws, philox_table, update_nab,
                      STATES, FLOWS, FLOWS_VARIANT)
+from .gpu_arith import update_nab_gpu
 
 F32 = np.float32
 
@@ -69,11 +74,15 @@ class OracleSim:
         beta_schedule: optional per-day overall beta (change_beta), length npts
     """
 
-    def __init__(self, pars, person, contacts, rng='philox', beta_schedule=None, seed_inds=None):
+    def __init__(self, pars, person, contacts, rng='philox', beta_schedule=None, seed_inds=None, arith=None):
         self.pars = pars
         self.n = int(pars['pop_size'])
         self.npts = int(pars['n_days']) + 1
         self.people = OraclePeople(pars, self.n)
+        # 'reference': the reference's float64 NAb math; 'gpu': the CUDA library's float-float
+        # formulation of it (gpu_arith), for draw-for-draw comparisons with a GPU run
+        self.arith = arith or ('gpu' if rng == 'philox' else 'reference')
+        self.people.arith = self.arith
         for k, v in person.items():
             self.people[k] = np.array(v, dtype=self.people[k].dtype)
         self.contacts = {k: {c: np.array(v[c]) for c in ('p1', 'p2', 'beta')} for k, v in contacts.items()}
@@ -183,7 +192,10 @@ class OracleSim:
         if p['use_waning']:
             has_nabs = people.peak_nab.nonzero()[0]
             if len(has_nabs):
-                update_nab(people, inds=has_nabs)
+                if self.arith == 'gpu':
+                    update_nab_gpu(people, inds=has_nabs)
+                else:
+                    update_nab(people, inds=has_nabs)
         inds_alive = (~people.dead).nonzero()[0]
         nab_alive = people.nab[inds_alive]
         self.results['pop_nabs'][t] = np.sum(nab_alive[nab_alive.nonzero()[0]]) / len(inds_alive)
