@@ -52,6 +52,9 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--json-out', default=None)
+    ap.add_argument('--profile-run', action='store_true',
+                    help='run one sim of --pop-size agents for --days days, one launch per kernel (no graph), '
+                         'for profilers, and exit')
     return ap.parse_args()
 
 
@@ -378,8 +381,22 @@ def reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def profile_run(args):
+    """One ungraphed run (kernels launched one by one) for ncu captures."""
+    import torch
+    import covasim_gb300 as cv
+    sim = cv.Sim(sim_pars(args, 1))
+    sim.run(use_graph=False)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_run': True, 'pop_size': args.pop_size, 'days': args.days,
+                      'cum_infections': float(sim.results['cum_infections'].values[-1])}))
+
+
 def main():
     args = parse()
+    if args.profile_run:
+        profile_run(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == 'reference':
         reference_arm(args, world, rank)
