@@ -21,6 +21,7 @@ N_RES_F = 3
 FX_NAB_BITS = 24
 FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
+NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
 EDGE_TILE = 4096          # edges per edge-pass block (covgpu.cu EDGE_TILE)
 AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
 AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
@@ -125,6 +126,9 @@ def lib():
         L.covgpu_infections_scratch_bytes.restype = i64
         L.covgpu_infections.argtypes = [f32, vp, vp, vp, i64, vp, vp, i64, vp, u64, i32, i32, i32, vp, vp, i64, vp,
                                         vp, vp, i64, vp]
+        L.covgpu_infections_noalloc.argtypes = [f32, vp, vp, vp, i64, vp, vp, i64, vp, u64, i32, i32, i32, vp, vp,
+                                                i64, vp, vp, vp]
+        L.covgpu_infections_noalloc.restype = C.c_int
         L.covgpu_agent_step.argtypes = [sp, i32, i32, i32, vp]
         L.covgpu_edge_pass.argtypes = [sp, i32, vp]
         L.covgpu_infect_claims.argtypes = [sp, i32, vp]
@@ -160,5 +164,5 @@ def abi_layout():
 
 
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
-            'covgpu_infections', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
+            'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
             'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days']

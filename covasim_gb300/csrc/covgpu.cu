@@ -921,6 +921,67 @@ int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const fl
   return launch_status();
 }
 
+// ---- compute_infections without allocation: scratch in a file-scope device array
+//
+// For callers that may not allocate device memory at all (see the declaration in
+// covgpu.h). The tile counts and offsets that covgpu_infections keeps in caller
+// scratch live here instead; every call rewrites all of the part it reads, so
+// nothing needs clearing between calls, and calls whose kernels overlap on the
+// GPU race on it.
+constexpr int64_t NOALLOC_MAX_EDGES = COVGPU_NOALLOC_MAX_EDGES;
+constexpr int64_t NOALLOC_TILES = (NOALLOC_MAX_EDGES + INF_TILE - 1) / INF_TILE;
+constexpr int64_t NOALLOC_SCRATCH = 2 * NOALLOC_TILES * (int64_t)(sizeof(int64_t) + sizeof(int32_t));
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH];
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of g_noalloc_scratch, per device
+
+// The array's host-side name is not a device address: look the address up once
+// per device, with that device current.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return COVGPU_CUDA_ERROR;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return COVGPU_BADARG;
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return COVGPU_CUDA_ERROR;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return COVGPU_OK;
+}
+
+int covgpu_infections_noalloc(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas,
+                              int64_t n_edges, const float* rel_trans, const float* rel_sus, int64_t n_agents,
+                              const double* uniforms, uint64_t seed, int32_t day, int32_t variant, int32_t layer,
+                              int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
+                              int32_t* status, void* stream) {
+  if (n_edges < 0 || n_edges > NOALLOC_MAX_EDGES) return COVGPU_BADARG;
+  if (capacity < 0 || n_agents < 0 || !out_count) return COVGPU_BADARG;
+  if (variant < 0 || variant >= COVGPU_MAX_VARIANTS || layer < 0 || layer >= COVGPU_MAX_LAYERS) return COVGPU_BADARG;
+  cudaStream_t s = S(stream);
+  if (n_edges == 0) {
+    return cudaMemsetAsync(out_count, 0, sizeof(int64_t), s) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
+  }
+  if (!p1 || !p2 || !layer_betas || !rel_trans || !rel_sus || (capacity > 0 && (!out_src || !out_tgt)))
+    return COVGPU_BADARG;
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc != COVGPU_OK) return rc;
+  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
+  const int64_t m = 2 * ntiles;
+  int64_t* offs = reinterpret_cast<int64_t*>(scratch);
+  int32_t* counts = reinterpret_cast<int32_t*>(offs + m);
+  InfArgs a;
+  a.beta = beta; a.p1 = p1; a.p2 = p2; a.lb = layer_betas; a.E = n_edges; a.rt = rel_trans; a.rs = rel_sus;
+  a.n_agents = n_agents; a.status = status; a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32);
+  a.day = day; a.variant = variant; a.layer = layer;
+  dim3 grid((unsigned)ntiles, 2);
+  k_infections_count<<<grid, INF_THREADS, 0, s>>>(a, ntiles, counts);
+  k_scan<<<1, 1024, 0, s>>>(counts, m, offs, out_count, capacity, status);
+  k_infections_write<<<grid, INF_THREADS, 0, s>>>(a, ntiles, offs, out_src, out_tgt, capacity);
+  return launch_status();
+}
+
 static int check_state(const covgpu_state* st) {
   if (!st || st->n <= 0 || st->n_sims <= 0 || st->n_agent_blocks <= 0) return COVGPU_BADARG;
   if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->events ||

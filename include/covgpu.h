@@ -232,6 +232,30 @@ int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const fl
                       int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
                       int32_t* status, void* scratch, int64_t scratch_bytes, void* stream);
 
+/* compute_infections for callers that cannot allocate device memory. (No
+ * counterpart in the reference, which has no device memory at all.) Some
+ * callers must not call cudaMalloc or any allocating routine: a framework
+ * capturing work into a CUDA graph under its own allocator, a plugin host
+ * that hands out a fixed memory budget, or a latency-critical thread that
+ * cannot afford the device synchronisation an allocation or free may cause.
+ * This variant takes no scratch argument: its tile counts and offsets live in
+ * a file-scope __device__ array of this library, sized for at most
+ * COVGPU_NOALLOC_MAX_EDGES edges (196,608 bytes, held by every GPU that
+ * loads the library until the process exits); larger n_edges is rejected
+ * with COVGPU_BADARG before any launch. Arguments, outputs and statuses are
+ * otherwise those of covgpu_infections, and it allocates nothing. The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress
+ * with that device current); make that first call before any stream capture.
+ * Every call shares the one array and rewrites the part it reads, so calls
+ * need no clearing between them, but calls whose kernels overlap on the GPU
+ * (different streams, or concurrent host threads) race on it: serialise them. */
+#define COVGPU_NOALLOC_MAX_EDGES (1LL << 24)
+int covgpu_infections_noalloc(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas,
+                              int64_t n_edges, const float* rel_trans, const float* rel_sus, int64_t n_agents,
+                              const double* uniforms, uint64_t seed, int32_t day, int32_t variant, int32_t layer,
+                              int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
+                              int32_t* status, void* stream);
+
 /* ---- fused per-day kernels over a batch of sims ------------------------- */
 
 /* One dense pass over every agent of every sim. With do_prev, first closes
