@@ -26,7 +26,8 @@ using namespace covgpu;
 namespace {
 
 constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
-constexpr int EDGE_THREADS = 256;
+constexpr int EP_THREADS = 512;        // threads of a persistent edge-pass block (one block per SM)
+constexpr int64_t EP_MAX_SMEM = 220 * 1024;  // source bitmap in shared memory up to ~1.8M agents per sim
 constexpr int EDGE_VEC = 4;            // edges per 128-bit load
 constexpr int64_t EDGE_TILE = 4096;    // edges per edge-pass block (must match the host)
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
@@ -439,13 +440,6 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
 
 // ============================================================ fused edge pass
 
-struct Roles { uint32_t src, tgt; };
-__device__ __forceinline__ Roles role_of(const uint32_t* __restrict__ roles, int32_t a) {
-  const uint2 w = __ldg(reinterpret_cast<const uint2*>(roles) + (a >> 5));
-  const uint32_t b = (uint32_t)a & 31u;
-  return Roles{(w.x >> b) & 1u, (w.y >> b) & 1u};
-}
-
 struct SegCtx {
   const covgpu_layer* L;
   const covgpu_sim_params* sp;
@@ -515,13 +509,28 @@ __device__ __forceinline__ void emit(const covgpu_state& st, bool has, uint64_t 
   }
 }
 
-__device__ __forceinline__ void edge_one(const covgpu_state& st, const SegCtx& c, int t, int64_t e, bool in_range,
-                                         int32_t a, int32_t b) {
+// Source bit of agent a: from the shared-memory copy of the current sim's source
+// bitmap, or from the role words in global memory.
+template <bool SMEM>
+__device__ __forceinline__ uint32_t src_bit(const covgpu_state& st, const uint32_t* s_src, int64_t w0, int32_t a) {
+  if (SMEM) return (s_src[(a >> 5) - w0] >> (a & 31)) & 1u;
+  return (__ldg(st.roles + 2 * (a >> 5)) >> (a & 31)) & 1u;
+}
+__device__ __forceinline__ uint32_t tgt_bit(const covgpu_state& st, int32_t a) {
+  return (__ldg(st.roles + 2 * (a >> 5) + 1) >> (a & 31)) & 1u;
+}
+
+template <bool SMEM>
+__device__ __forceinline__ void edge_one2(const covgpu_state& st, const SegCtx& c, const uint32_t* s_src, int64_t w0,
+                                          int t, int64_t e, bool in_range, int32_t a, int32_t b) {
   bool c0 = false, c1 = false;
   if (in_range) {
-    const Roles ra = role_of(st.roles, a), rb = role_of(st.roles, b);
-    c0 = ra.src & rb.tgt;
-    c1 = rb.src & ra.tgt;
+    // sources are rare: test them first (shared memory), the other endpoint's target bit only then
+    const uint32_t sa = src_bit<SMEM>(st, s_src, w0, a), sb = src_bit<SMEM>(st, s_src, w0, b);
+    if (sa | sb) {
+      c0 = sa && tgt_bit(st, b);
+      c1 = sb && tgt_bit(st, a);
+    }
   }
   bool h0 = false, h1 = false;
   uint32_t v0 = 0, v1 = 0;
@@ -536,56 +545,109 @@ __device__ __forceinline__ void edge_one(const covgpu_state& st, const SegCtx& c
   emit(st, h1, h1 ? event_key(t, v1, c.L->layer, 1, e) : 0ull, a, b);
 }
 
-__global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
-  __shared__ int s_seg;
-  if (threadIdx.x == 0) {  // segment owning this tile: last segment with tile_begin <= blockIdx.x
+// Persistent edge pass: block b walks its contiguous range of tiles; the
+// current sim's source bitmap sits in shared memory (SMEM) when it fits.
+template <bool SMEM>
+__global__ void __launch_bounds__(EP_THREADS, 1) k_edge_pass(covgpu_state st, int t) {
+  extern __shared__ uint32_t s_src[];
+  const int64_t tb = st.edge_block_tiles[blockIdx.x], te = st.edge_block_tiles[blockIdx.x + 1];
+  if (tb >= te) return;
+  int seg = 0;
+  {  // last segment with tile_begin <= tb
     int lo = 0, hi = st.n_segments - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+      if (st.segments[mid].tile_begin <= tb) lo = mid; else hi = mid - 1;
     }
-    s_seg = lo;
+    seg = lo;
   }
-  __syncthreads();
-  const covgpu_layer* L = st.segments + s_seg;
-  SegCtx c;
-  c.L = L;
-  c.sp = st.sims + L->sim;
-  c.nv = c.sp->n_variants;
-  c.beta_layer = c.sp->beta_layer_tab[(int64_t)t * c.sp->n_layers + L->layer];
-  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
-  const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
-  const int64_t n_local = c.sp->n_agents;
-  const int64_t off = c.sp->agent_off;
-  for (int64_t eb = e0 + (int64_t)threadIdx.x * EDGE_VEC; eb < e0 + EDGE_TILE; eb += (int64_t)EDGE_THREADS * EDGE_VEC) {
-    int32_t a[EDGE_VEC], b[EDGE_VEC];
-    if (L->dynamic) {
-      // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
-      // endpoints uniform over the sim's agents (Philox keyed by edge and day)
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        const int64_t e = eb + j;
-        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L->layer),
-                               c.sp->key0, c.sp->key1);
-        a[j] = (int32_t)(off + uniform_index(w.x, w.y, (uint64_t)n_local));
-        b[j] = (int32_t)(off + uniform_index(w.z, w.w, (uint64_t)n_local));
-      }
-    } else if (eb + EDGE_VEC <= e1) {
-      const int4 pa = __ldg(reinterpret_cast<const int4*>(L->p1 + eb));
-      const int4 pb = __ldg(reinterpret_cast<const int4*>(L->p2 + eb));
-      a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
-      b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        const int64_t e = eb + j;
-        a[j] = e < e1 ? L->p1[e] : 0;
-        b[j] = e < e1 ? L->p2[e] : 0;
-      }
+  int loaded_sim = -1;
+  int64_t w0 = 0;
+  for (int64_t tile = tb; tile < te; ++tile) {
+    while (seg + 1 < st.n_segments && st.segments[seg + 1].tile_begin <= tile) ++seg;
+    const covgpu_layer* L = st.segments + seg;
+    SegCtx c;
+    c.L = L;
+    c.sp = st.sims + L->sim;
+    if (SMEM && L->sim != loaded_sim) {
+      __syncthreads();  // every thread is done with the previous sim's bitmap
+      w0 = c.sp->agent_off >> 5;
+      const int64_t nw = ((int64_t)c.sp->n_agents + 31) >> 5;
+      for (int64_t k = threadIdx.x; k < nw; k += blockDim.x) s_src[k] = __ldg(st.roles + 2 * (w0 + k));
+      __syncthreads();
+      loaded_sim = L->sim;
     }
+    c.nv = c.sp->n_variants;
+    c.beta_layer = c.sp->beta_layer_tab[(int64_t)t * c.sp->n_layers + L->layer];
+    const int64_t e0 = (tile - L->tile_begin) * EDGE_TILE;
+    const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
+    const int64_t n_local = c.sp->n_agents;
+    const int64_t off = c.sp->agent_off;
 #pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) edge_one(st, c, t, eb + j, eb + j < e1, a[j], b[j]);
+    for (int half = 0; half < EDGE_TILE / (EP_THREADS * EDGE_VEC); ++half) {
+      const int64_t eb = e0 + (int64_t)half * EP_THREADS * EDGE_VEC + (int64_t)threadIdx.x * EDGE_VEC;
+      int32_t a[EDGE_VEC], b[EDGE_VEC];
+      if (L->dynamic) {
+        // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
+        // endpoints uniform over the sim's agents (Philox keyed by edge and day)
+#pragma unroll
+        for (int j = 0; j < EDGE_VEC; ++j) {
+          const int64_t e = eb + j;
+          const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
+                                            TAG_LAYER | (uint32_t)L->layer), c.sp->key0, c.sp->key1);
+          a[j] = (int32_t)(off + uniform_index(w.x, w.y, (uint64_t)n_local));
+          b[j] = (int32_t)(off + uniform_index(w.z, w.w, (uint64_t)n_local));
+        }
+      } else if (eb + EDGE_VEC <= e1) {
+        const int4 pa = __ldg(reinterpret_cast<const int4*>(L->p1 + eb));
+        const int4 pb = __ldg(reinterpret_cast<const int4*>(L->p2 + eb));
+        a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
+        b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < EDGE_VEC; ++j) {
+          const int64_t e = eb + j;
+          a[j] = e < e1 ? L->p1[e] : (int32_t)off;
+          b[j] = e < e1 ? L->p2[e] : (int32_t)off;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; ++j) edge_one2<SMEM>(st, c, s_src, w0, t, eb + j, eb + j < e1, a[j], b[j]);
+    }
   }
+}
+
+// Shared memory (bytes) of the source bitmap; 0 when it does not fit and the
+// global-memory variant runs instead.
+int64_t edge_smem_bytes(const covgpu_state* st) {
+  const int64_t bytes = 4 * (int64_t)st->src_words_max;
+  return bytes <= EP_MAX_SMEM ? bytes : 0;
+}
+
+// Allow the shared-memory edge pass its full bitmap; once per device, before
+// any launch (and outside stream capture).
+int configure_edge_pass() {
+  static bool configured[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return COVGPU_CUDA_ERROR;
+  if (!configured[dev]) {
+    if (cudaFuncSetAttribute(k_edge_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EP_MAX_SMEM) !=
+        cudaSuccess)
+      return COVGPU_CUDA_ERROR;
+    configured[dev] = true;
+  }
+  return COVGPU_OK;
+}
+
+int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->n_tiles == 0 || st->n_edge_blocks == 0) return COVGPU_OK;
+  const int64_t smem = edge_smem_bytes(st);
+  if (smem > 0) {
+    k_edge_pass<true><<<(unsigned)st->n_edge_blocks, EP_THREADS, (size_t)smem, s>>>(*st, t);
+  } else {
+    k_edge_pass<false><<<(unsigned)st->n_edge_blocks, EP_THREADS, 0, s>>>(*st, t);
+  }
+  return launch_status();
 }
 
 // ============================================================ infect
@@ -833,7 +895,7 @@ cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the le
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
-    if (st->n_tiles > 0) k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+    launch_edge_pass(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
   if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0);
@@ -987,7 +1049,8 @@ static int check_state(const covgpu_state* st) {
   if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->events ||
       !st->event_count || !st->status)
     return COVGPU_BADARG;
-  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0)) return COVGPU_BADARG;
+  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0 || !st->edge_block_tiles || st->n_edge_blocks <= 0))
+    return COVGPU_BADARG;
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
   return COVGPU_OK;
 }
@@ -1004,9 +1067,9 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  if (st->n_tiles == 0) return COVGPU_OK;
-  k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, S(stream)>>>(*st, t);
-  return launch_status();
+  rc = configure_edge_pass();
+  if (rc) return rc;
+  return launch_edge_pass(st, t, S(stream));
 }
 
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream) {
@@ -1042,6 +1105,8 @@ int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open
   if (rc) return rc;
   if (t0 < 0 || t1 < t0 || t1 >= 0xFFFF) return COVGPU_BADARG;
   open_prev = (open_prev && t0 > 0) ? 1 : 0;
+  rc = configure_edge_pass();
+  if (rc) return rc;
   cudaStream_t s = S(stream);
   if (!use_graph) return enqueue_days(st, t0, t1, open_prev, close_last, s);
   GraphEntry* hit = nullptr;
