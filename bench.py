@@ -51,6 +51,7 @@ def parse():
     ap.add_argument('--cpu-days', type=int, default=3, help='days of the CPU oracle sample')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--batch', type=int, default=16, help='sims of the batched measurement (0: skip)')
     ap.add_argument('--json-out', default=None)
     ap.add_argument('--profile-run', action='store_true',
                     help='run one sim of --pop-size agents for --days days, one launch per kernel (no graph), '
@@ -310,9 +311,59 @@ def gpu_arm(args, world, rank):
                'ms_per_step': round(1e3 * e2e_s / args.steps, 3)}
         assert s.results['cum_infections'].values[-1] > 100
 
-    return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e,
+    batched = batched_arm(args, sim, value, world) if args.batch else None
+
+    return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched,
                 launches=launches_per_step * args.steps, init_s=init_s, res=res, spec=sim.spec,
                 cum_infections=float(res['new_infections'].sum() + sim['pop_infected']))
+
+
+def batched_arm(args, sim, plain_value, world):
+    """B copies of the workload (seeds differ, population shared) in one BatchState:
+    one agent pass, one edge pass and one infect pass per day over all of them,
+    the whole run one CUDA graph. Each batched sim is bit-identical to its solo
+    run (tested), so outcome statistics match the plain path by construction;
+    sim 0 is checked against the plain run here."""
+    import torch
+    import covasim_gb300 as cv
+    from covasim_gb300.sim import choose_seed_infections, CALL_SEED
+    from covasim_gb300 import _lib as L
+    B = args.batch
+    sims = [cv.Sim(sim_pars(args, 1 + k), popdict=sim.popdict, person=sim._person) for k in range(B)]
+    batch = cv.BatchSim(sims).initialize()
+    st = batch.state
+    snap = st.snapshot()
+    seeds = [choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected']) for s in sims]
+    npts = batch.npts
+
+    def one_run():
+        st.restore(snap)
+        for k in range(B):
+            st.infect_list(0, seeds[k], sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
+
+    for _ in range(args.warmup):
+        one_run()
+    torch.cuda.synchronize()
+    barrier(world)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        one_run()
+    ev1.record()
+    torch.cuda.synchronize()
+    elapsed = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    if st.status():
+        raise RuntimeError(f'device status {st.status()}')
+    value = world * B * args.pop_size * args.days * args.steps / elapsed
+    solo = sim.state.results(0)['new_infections']
+    same = bool(np.array_equal(st.results(0)['new_infections'], solo))
+    cum = [float(st.results(k)['new_infections'].sum()) for k in range(B)]
+    return {'value': round(value, 1), 'unit': 'agent-days/s', 'n_sims': B,
+            'ms_per_step': round(1e3 * elapsed / args.steps, 3), 'vs_plain': round(value / plain_value, 3),
+            'sim0_equals_plain_run': same, 'cum_infections_mean': round(float(np.mean(cum)), 1),
+            'cum_infections_sd': round(float(np.std(cum)), 1)}
 
 
 # ----------------------------------------------------------------------------- CPU oracle
@@ -419,7 +470,7 @@ def main():
                            'l2': 'inputs larger than L2 (agents ~160 MB + static edges ~62 MB)',
                            'replicas': world, 'cum_infections_per_run': out['cum_infections']},
                 'edge_evaluations_per_s': None,
-                'roofline': out['roofline'], 'cpu_baseline': cpu, 'e2e': out['e2e'],
+                'roofline': out['roofline'], 'cpu_baseline': cpu, 'e2e': out['e2e'], 'batched': out['batched'],
                 'gpu_launches': out['launches'], 'clocks': out['clocks']}
         spec = out['spec']
         e_all = sum(len(ly['p1']) for ly in spec.layers)

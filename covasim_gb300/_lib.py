@@ -22,8 +22,7 @@ FX_NAB_BITS = 24
 FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
 NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
-EDGE_TILE = 4096          # edges per edge-pass tile (covgpu.cu EDGE_TILE)
-DYNAMIC_TILE_COST = 4     # relative cost of a dynamic-layer tile (edges drawn from Philox) in the work split
+EDGE_TILE = 4096          # edges per edge-pass block (covgpu.cu EDGE_TILE)
 AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
 AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
 
@@ -87,7 +86,6 @@ class State(C.Structure):
     _fields_ = [
         ('n', C.c_int64), ('n_sims', C.c_int32), ('n_segments', C.c_int32), ('n_tiles', C.c_int64),
         ('n_agent_blocks', C.c_int64),
-        ('edge_block_tiles', C.c_void_p), ('n_edge_blocks', C.c_int32), ('src_words_max', C.c_int32),
         ('flags', C.c_void_p), ('vstate', C.c_void_p),
         ('symp_prob', C.c_void_p), ('severe_prob', C.c_void_p), ('crit_prob', C.c_void_p), ('death_prob', C.c_void_p),
         ('rel_trans', C.c_void_p), ('rel_sus', C.c_void_p),

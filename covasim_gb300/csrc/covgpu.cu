@@ -7,9 +7,10 @@
 //       (people.py:164-312,368-374) + check_immunity (immunity.py:303-350) +
 //       update_nab (immunity.py:205-213) + stocks/flows (sim.py:651-674) +
 //       viral load and source/target role bitmaps for the edge pass;
-//   k_edge_pass      every layer segment and variant of every sim: compute_trans_sus
-//       folded in, both directions of each edge from one 128-bit read, Philox
-//       Bernoullis, warp-ballot compaction of events, atomicMin first-infector claim;
+//   k_edge_pass      every layer segment and variant of every sim: edges streamed with
+//       128-bit reads, source->target candidates queued per warp in shared
+//       memory, then compute_trans_sus folded in lane-packed, Philox Bernoullis,
+//       warp-ballot compaction of events, atomicMin first-infector claim;
 //   k_infect_claims / k_infect_list   People.infect (people.py:435-586) +
 //       update_peak_nab (immunity.py:138-202).
 #include <cuda_runtime.h>
@@ -26,10 +27,13 @@ using namespace covgpu;
 namespace {
 
 constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
-constexpr int EP_THREADS = 512;        // threads of a persistent edge-pass block (one block per SM)
-constexpr int64_t EP_MAX_SMEM = 220 * 1024;  // source bitmap in shared memory up to ~1.8M agents per sim
+constexpr int EDGE_THREADS = 256;
 constexpr int EDGE_VEC = 4;            // edges per 128-bit load
 constexpr int64_t EDGE_TILE = 4096;    // edges per edge-pass block (must match the host)
+constexpr int EQ_ROUND = 2 * 32 * EDGE_VEC;  // most candidate directions one warp appends per round
+constexpr int EQ_CAP = 384;            // candidate queue entries per warp (drained when a round could overflow)
+static_assert(2 * EDGE_TILE <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
+static_assert(EDGE_TILE % (EDGE_THREADS * EDGE_VEC) == 0, "whole rounds per tile");
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
 constexpr int INF_THREADS = 256;
 constexpr int INF_PER_THREAD = INF_TILE / INF_THREADS;
@@ -439,46 +443,64 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
 }
 
 // ============================================================ fused edge pass
+//
+// One block per tile of EDGE_TILE edges of one layer segment. Phase A streams
+// the tile (128-bit loads of p1/p2, or the dynamic layer's endpoints from
+// Philox), reads both endpoints' role words and appends every candidate
+// direction source -> target to its warp's queue in shared memory. Phase B
+// drains the queue one candidate per lane, so the gathers of
+// compute_trans_sus run lane-packed instead of serialising the whole warp on
+// the few lanes that hold a source.
 
+struct Roles { uint32_t src, tgt; };
+__device__ __forceinline__ Roles role_of(const uint32_t* __restrict__ roles, int32_t a) {
+  const uint2 w = __ldg(reinterpret_cast<const uint2*>(roles) + (a >> 5));
+  const uint32_t b = (uint32_t)a & 31u;
+  return Roles{(w.x >> b) & 1u, (w.y >> b) & 1u};
+}
+
+// per-tile constants, hoisted out of the segment and sim records
 struct SegCtx {
   const covgpu_layer* L;
-  const covgpu_sim_params* sp;
-  float beta_layer;
-  int nv;
+  const float* edge_beta;    // per-edge layer weights, or null for beta_const
+  const float* beta_t;       // beta_tab row of day t ([n_variants])
+  float beta_const, beta_layer, quar_factor, iso_factor, asymp_factor;
+  uint32_t key0, key1;
+  int nv, layer, seg;
+  int64_t n_edges;
 };
 
 // compute_trans_sus folded into compute_infections for one direction s -> g
-// (utils.py:88-89 then 117-123); returns true on a transmission.
-__device__ __noinline__ bool edge_dir(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
-                                      int32_t s, int32_t g, float lb, uint4& w, int& w_variant,
-                                      uint32_t& v_out) {
-  const covgpu_sim_params& sp = *c.sp;
-  const uint32_t v = (__ldg(st.vstate + s) >> 8) & 0xFFu;
-  if (v >= (uint32_t)c.nv) return false;
+// (utils.py:88-89 then 117-123); returns true on a transmission. Every gather
+// is issued before the first use so that they overlap.
+__device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
+                                         int32_t s, int32_t g, uint32_t& v_out) {
+  const uint32_t vs = __ldg(st.vstate + s);
   const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
-  float rte = __ldg(st.rel_trans + s);
-  if (fs & B_QUAR) rte = __fmul_rn(rte, c.L->quar_factor);
-  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, sp.asymp_factor);
-  if (fs & B_ISO) rte = __fmul_rn(rte, c.L->iso_factor);
+  const float rt = __ldg(st.rel_trans + s), vl = __ldg(st.viral_load + s), rs = __ldg(st.rel_sus + g);
+  const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
+  const uint32_t v = (vs >> 8) & 0xFFu;
+  const uint32_t vc = v < (uint32_t)c.nv ? v : 0u;
+  const float si = __ldg(st.sus_imm + (int64_t)vc * st.n + g);
+  const float beta = __ldg(c.beta_t + vc);
+  if (v >= (uint32_t)c.nv) return false;
+  float rte = rt;
+  if (fs & B_QUAR) rte = __fmul_rn(rte, c.quar_factor);
+  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, c.asymp_factor);
+  if (fs & B_ISO) rte = __fmul_rn(rte, c.iso_factor);
   rte = __fmul_rn(rte, c.beta_layer);
-  rte = __fmul_rn(rte, __ldg(st.viral_load + s));
-  if (rte == 0.0f) return false;
-  float rse = __ldg(st.rel_sus + g);
-  if (fg & B_QUAR) rse = __fmul_rn(rse, c.L->quar_factor);
-  rse = __fmul_rn(rse, __fsub_rn(1.0f, __ldg(st.sus_imm + (int64_t)v * st.n + g)));
-  const float beta = __ldg(sp.beta_tab + (int64_t)t * c.nv + v);
+  rte = __fmul_rn(rte, vl);
+  float rse = rs;
+  if (fg & B_QUAR) rse = __fmul_rn(rse, c.quar_factor);
+  rse = __fmul_rn(rse, __fsub_rn(1.0f, si));
   const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
   if (p == 0.0f) return false;
   v_out = v;
-  if (st.edge_uniforms) {  // injected draws (test mode)
-    const int seg = (int)(c.L - st.segments);
-    return st.edge_uniforms[seg][((int64_t)v * 2 + dir) * c.L->n_edges + e] < (double)p;
-  }
-  if (w_variant != (int)v) {
-    w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
-                          TAG_EDGE | (v << 8) | (uint32_t)c.L->layer), sp.key0, sp.key1);
-    w_variant = (int)v;
-  }
+  if (st.edge_uniforms)  // injected draws (test mode)
+    return st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
+  // one Philox block per (edge, day, variant, layer): words x,y draw direction 0, z,w direction 1
+  const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_EDGE | (v << 8) | (uint32_t)c.layer),
+                         c.key0, c.key1);
   return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);  // u < p in float64, decided in integers
 }
 
@@ -509,144 +531,129 @@ __device__ __forceinline__ void emit(const covgpu_state& st, bool has, uint64_t 
   }
 }
 
-// Source bit of agent a: from the shared-memory copy of the current sim's source
-// bitmap, or from the role words in global memory.
-template <bool SMEM>
-__device__ __forceinline__ uint32_t src_bit(const covgpu_state& st, const uint32_t* s_src, int64_t w0, int32_t a) {
-  if (SMEM) return (s_src[(a >> 5) - w0] >> (a & 31)) & 1u;
-  return (__ldg(st.roles + 2 * (a >> 5)) >> (a & 31)) & 1u;
-}
-__device__ __forceinline__ uint32_t tgt_bit(const covgpu_state& st, int32_t a) {
-  return (__ldg(st.roles + 2 * (a >> 5) + 1) >> (a & 31)) & 1u;
+struct EdgeQueue {               // candidate directions of one warp
+  int32_t s[EQ_CAP];             // source agent
+  int32_t g[EQ_CAP];             // target agent
+  uint16_t m[EQ_CAP];            // (edge within the tile) << 1 | direction
+};
+
+// warp-aggregated append of one candidate per lane with `has`
+__device__ __forceinline__ void queue_push(EdgeQueue& q, int& qn, bool has, int32_t s, int32_t g, uint32_t m) {
+  const unsigned mask = __ballot_sync(0xffffffffu, has);
+  if (has) {
+    const int pos = qn + __popc(mask & ((1u << (threadIdx.x & 31)) - 1u));
+    q.s[pos] = s; q.g[pos] = g; q.m[pos] = (uint16_t)m;
+  }
+  qn += __popc(mask);
 }
 
-template <bool SMEM>
-__device__ __forceinline__ void edge_one2(const covgpu_state& st, const SegCtx& c, const uint32_t* s_src, int64_t w0,
-                                          int t, int64_t e, bool in_range, int32_t a, int32_t b) {
-  bool c0 = false, c1 = false;
-  if (in_range) {
-    // sources are rare: test them first (shared memory), the other endpoint's target bit only then
-    const uint32_t sa = src_bit<SMEM>(st, s_src, w0, a), sb = src_bit<SMEM>(st, s_src, w0, b);
-    if (sa | sb) {
-      c0 = sa && tgt_bit(st, b);
-      c1 = sb && tgt_bit(st, a);
+// phase B: one candidate per lane, then the warp-aggregated event append
+__device__ __forceinline__ void queue_drain(const covgpu_state& st, const SegCtx& c, int t, int64_t e0,
+                                            EdgeQueue& q, int qn) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < qn; base += 32) {
+    const int i = base + lane;
+    bool hit = false;
+    uint32_t v = 0;
+    int32_t s = 0, g = 0;
+    uint32_t m = 0;
+    if (i < qn) {
+      s = q.s[i]; g = q.g[i]; m = q.m[i];
+      hit = edge_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, v);
     }
+    emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), e0 + (m >> 1)) : 0ull, g, s);
   }
-  bool h0 = false, h1 = false;
-  uint32_t v0 = 0, v1 = 0;
-  if (c0 || c1) {
-    const float lb = c.L->beta ? __ldg(c.L->beta + e) : c.L->beta_const;
-    uint4 w = make_uint4(0, 0, 0, 0);
-    int wv = -1;
-    if (c0) h0 = edge_dir(st, c, t, e, 0, a, b, lb, w, wv, v0);
-    if (c1) h1 = edge_dir(st, c, t, e, 1, b, a, lb, w, wv, v1);
-  }
-  emit(st, h0, h0 ? event_key(t, v0, c.L->layer, 0, e) : 0ull, b, a);
-  emit(st, h1, h1 ? event_key(t, v1, c.L->layer, 1, e) : 0ull, a, b);
+  __syncwarp();
 }
 
-// Persistent edge pass: block b walks its contiguous range of tiles; the
-// current sim's source bitmap sits in shared memory (SMEM) when it fits.
-template <bool SMEM>
-__global__ void __launch_bounds__(EP_THREADS, 1) k_edge_pass(covgpu_state st, int t) {
-  extern __shared__ uint32_t s_src[];
-  const int64_t tb = st.edge_block_tiles[blockIdx.x], te = st.edge_block_tiles[blockIdx.x + 1];
-  if (tb >= te) return;
-  int seg = 0;
-  {  // last segment with tile_begin <= tb
+__global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  __shared__ int s_seg;
+  __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
+  if (threadIdx.x == 0) {  // segment owning this tile: last segment with tile_begin <= blockIdx.x
     int lo = 0, hi = st.n_segments - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (st.segments[mid].tile_begin <= tb) lo = mid; else hi = mid - 1;
+      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
     }
-    seg = lo;
+    s_seg = lo;
   }
-  int loaded_sim = -1;
-  int64_t w0 = 0;
-  for (int64_t tile = tb; tile < te; ++tile) {
-    while (seg + 1 < st.n_segments && st.segments[seg + 1].tile_begin <= tile) ++seg;
-    const covgpu_layer* L = st.segments + seg;
-    SegCtx c;
-    c.L = L;
-    c.sp = st.sims + L->sim;
-    if (SMEM && L->sim != loaded_sim) {
-      __syncthreads();  // every thread is done with the previous sim's bitmap
-      w0 = c.sp->agent_off >> 5;
-      const int64_t nw = ((int64_t)c.sp->n_agents + 31) >> 5;
-      for (int64_t k = threadIdx.x; k < nw; k += blockDim.x) s_src[k] = __ldg(st.roles + 2 * (w0 + k));
-      __syncthreads();
-      loaded_sim = L->sim;
-    }
-    c.nv = c.sp->n_variants;
-    c.beta_layer = c.sp->beta_layer_tab[(int64_t)t * c.sp->n_layers + L->layer];
-    const int64_t e0 = (tile - L->tile_begin) * EDGE_TILE;
-    const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
-    const int64_t n_local = c.sp->n_agents;
-    const int64_t off = c.sp->agent_off;
+  __syncthreads();
+  const covgpu_layer* L = st.segments + s_seg;
+  const covgpu_sim_params* sp = st.sims + L->sim;
+  SegCtx c;
+  c.L = L;
+  c.seg = s_seg;
+  c.layer = L->layer;
+  c.n_edges = L->n_edges;
+  c.edge_beta = L->beta;
+  c.beta_const = L->beta_const;
+  c.quar_factor = L->quar_factor;
+  c.iso_factor = L->iso_factor;
+  c.asymp_factor = sp->asymp_factor;
+  c.nv = sp->n_variants;
+  c.key0 = sp->key0;
+  c.key1 = sp->key1;
+  c.beta_t = sp->beta_tab + (int64_t)t * c.nv;
+  c.beta_layer = sp->beta_layer_tab[(int64_t)t * sp->n_layers + c.layer];
+  const bool dynamic = L->dynamic != 0;
+  const int32_t* p1 = L->p1;
+  const int32_t* p2 = L->p2;
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
+  const int64_t e1 = min(e0 + EDGE_TILE, c.n_edges);
+  const int64_t n_local = sp->n_agents;
+  const int32_t off = (int32_t)sp->agent_off;
+  EdgeQueue& q = s_q[threadIdx.x >> 5];
+  int qn = 0;  // warp-uniform queue length
+  constexpr int ROUNDS = EDGE_TILE / (EDGE_THREADS * EDGE_VEC);
+  for (int r = 0; r < ROUNDS; ++r) {
+    const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
+    int32_t a[EDGE_VEC], b[EDGE_VEC];
+    if (dynamic) {
+      // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
+      // endpoints uniform over the sim's agents (Philox keyed by edge and day)
 #pragma unroll
-    for (int half = 0; half < EDGE_TILE / (EP_THREADS * EDGE_VEC); ++half) {
-      const int64_t eb = e0 + (int64_t)half * EP_THREADS * EDGE_VEC + (int64_t)threadIdx.x * EDGE_VEC;
-      int32_t a[EDGE_VEC], b[EDGE_VEC];
-      if (L->dynamic) {
-        // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
-        // endpoints uniform over the sim's agents (Philox keyed by edge and day)
-#pragma unroll
-        for (int j = 0; j < EDGE_VEC; ++j) {
-          const int64_t e = eb + j;
-          const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
-                                            TAG_LAYER | (uint32_t)L->layer), c.sp->key0, c.sp->key1);
-          a[j] = (int32_t)(off + uniform_index(w.x, w.y, (uint64_t)n_local));
-          b[j] = (int32_t)(off + uniform_index(w.z, w.w, (uint64_t)n_local));
-        }
-      } else if (eb + EDGE_VEC <= e1) {
-        const int4 pa = __ldg(reinterpret_cast<const int4*>(L->p1 + eb));
-        const int4 pb = __ldg(reinterpret_cast<const int4*>(L->p2 + eb));
-        a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
-        b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
-      } else {
-#pragma unroll
-        for (int j = 0; j < EDGE_VEC; ++j) {
-          const int64_t e = eb + j;
-          a[j] = e < e1 ? L->p1[e] : (int32_t)off;
-          b[j] = e < e1 ? L->p2[e] : (int32_t)off;
-        }
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        const int64_t e = eb + j;
+        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)c.layer),
+                               c.key0, c.key1);
+        a[j] = off + (int32_t)uniform_index(w.x, w.y, (uint64_t)n_local);
+        b[j] = off + (int32_t)uniform_index(w.z, w.w, (uint64_t)n_local);
       }
+    } else if (eb + EDGE_VEC <= e1) {
+      const int4 pa = __ldg(reinterpret_cast<const int4*>(p1 + eb));
+      const int4 pb = __ldg(reinterpret_cast<const int4*>(p2 + eb));
+      a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
+      b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
+    } else {
 #pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) edge_one2<SMEM>(st, c, s_src, w0, t, eb + j, eb + j < e1, a[j], b[j]);
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        const int64_t e = eb + j;
+        a[j] = e < e1 ? p1[e] : off;
+        b[j] = e < e1 ? p2[e] : off;
+      }
+    }
+    Roles ra[EDGE_VEC], rb[EDGE_VEC];
+#pragma unroll
+    for (int j = 0; j < EDGE_VEC; ++j) { ra[j] = role_of(st.roles, a[j]); rb[j] = role_of(st.roles, b[j]); }
+#pragma unroll
+    for (int j = 0; j < EDGE_VEC; ++j) {
+      const bool in = eb + j < e1;
+      const uint32_t m = (uint32_t)(eb + j - e0) << 1;
+      queue_push(q, qn, in && (ra[j].src & rb[j].tgt), a[j], b[j], m);
+      queue_push(q, qn, in && (rb[j].src & ra[j].tgt), b[j], a[j], m | 1u);
+    }
+    if (qn > EQ_CAP - EQ_ROUND) {
+      queue_drain(st, c, t, e0, q, qn);
+      qn = 0;
     }
   }
-}
-
-// Shared memory (bytes) of the source bitmap; 0 when it does not fit and the
-// global-memory variant runs instead.
-int64_t edge_smem_bytes(const covgpu_state* st) {
-  const int64_t bytes = 4 * (int64_t)st->src_words_max;
-  return bytes <= EP_MAX_SMEM ? bytes : 0;
-}
-
-// Allow the shared-memory edge pass its full bitmap; once per device, before
-// any launch (and outside stream capture).
-int configure_edge_pass() {
-  static bool configured[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return COVGPU_CUDA_ERROR;
-  if (!configured[dev]) {
-    if (cudaFuncSetAttribute(k_edge_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EP_MAX_SMEM) !=
-        cudaSuccess)
-      return COVGPU_CUDA_ERROR;
-    configured[dev] = true;
-  }
-  return COVGPU_OK;
+  if (qn > 0) queue_drain(st, c, t, e0, q, qn);
 }
 
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
-  if (st->n_tiles == 0 || st->n_edge_blocks == 0) return COVGPU_OK;
-  const int64_t smem = edge_smem_bytes(st);
-  if (smem > 0) {
-    k_edge_pass<true><<<(unsigned)st->n_edge_blocks, EP_THREADS, (size_t)smem, s>>>(*st, t);
-  } else {
-    k_edge_pass<false><<<(unsigned)st->n_edge_blocks, EP_THREADS, 0, s>>>(*st, t);
-  }
+  if (st->n_tiles == 0) return COVGPU_OK;
+  k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }
 
@@ -656,9 +663,14 @@ struct DrawSet {
   double z[6];
   double u[4];       // injected uniforms (test mode)
   uint32_t uw[4];    // Philox words of the uniforms
+  uint32_t w23[2];   // Philox words of the (sym2sev, sev2crit) normal pair, transformed on demand
   bool injected;
   // u_k < p exactly as float64 compares them (integer test for Philox words)
   __device__ __forceinline__ bool lt(int k, float p) const { return injected ? (u[k] < (double)p) : bern32(uw[k], p); }
+  // the normals of the severe branch: only severe cases need them
+  __device__ __forceinline__ void severe_normals() {
+    if (!injected) box_muller(w23[0], w23[1], z[2], z[3]);
+  }
 };
 
 __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i,
@@ -678,7 +690,8 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   const uint4 b1 = philox(make_uint4((uint32_t)local, 1u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b2 = philox(make_uint4((uint32_t)local, 2u, (uint32_t)t, tag), sp.key0, sp.key1);
   box_muller(b0.x, b0.y, d.z[0], d.z[1]);
-  box_muller(b0.z, b0.w, d.z[2], d.z[3]);
+  d.w23[0] = b0.z;
+  d.w23[1] = b0.w;
   box_muller(b1.x, b1.y, d.z[4], d.z[5]);
   d.uw[0] = b1.z;
   d.uw[1] = b1.w;
@@ -772,6 +785,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       u_disease[i] = (float)__dadd_rn((double)__fadd_rn(de, dis), dr);
       symp_class = 1;
     } else {  // CASE 2.2 severe, people.py:550-554
+      d.severe_normals();
       if (count)
         atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
       const float dss = (float)sample_dist(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
@@ -1049,7 +1063,7 @@ static int check_state(const covgpu_state* st) {
   if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->events ||
       !st->event_count || !st->status)
     return COVGPU_BADARG;
-  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0 || !st->edge_block_tiles || st->n_edge_blocks <= 0))
+  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0))
     return COVGPU_BADARG;
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
   return COVGPU_OK;
@@ -1067,8 +1081,6 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  rc = configure_edge_pass();
-  if (rc) return rc;
   return launch_edge_pass(st, t, S(stream));
 }
 
@@ -1105,8 +1117,6 @@ int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open
   if (rc) return rc;
   if (t0 < 0 || t1 < t0 || t1 >= 0xFFFF) return COVGPU_BADARG;
   open_prev = (open_prev && t0 > 0) ? 1 : 0;
-  rc = configure_edge_pass();
-  if (rc) return rc;
   cudaStream_t s = S(stream);
   if (!use_graph) return enqueue_days(st, t0, t1, open_prev, close_last, s);
   GraphEntry* hit = nullptr;

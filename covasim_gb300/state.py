@@ -266,26 +266,6 @@ class BatchState:
         self.n_tiles = tiles
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
         self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
-        self._split_edge_work()
-
-    def _split_edge_work(self, blocks=None, dynamic_cost=L.DYNAMIC_TILE_COST):
-        """Contiguous tile ranges for the persistent edge-pass blocks (one per SM),
-        balanced by cost: a tile of a dynamic layer (edges drawn from Philox)
-        costs ``dynamic_cost`` static tiles."""
-        if blocks is None:
-            blocks = torch.cuda.get_device_properties(self.device).multi_processor_count
-        cost = np.zeros(self.n_tiles, dtype=np.float64)
-        for rec in self.segments:
-            nt = (rec.n_edges + L.EDGE_TILE - 1) // L.EDGE_TILE
-            cost[rec.tile_begin:rec.tile_begin + nt] = dynamic_cost if rec.dynamic else 1.0
-        cum = np.concatenate([[0.0], np.cumsum(cost)])
-        targets = cum[-1] * np.arange(blocks + 1) / blocks
-        bounds = np.searchsorted(cum, targets, side='left').astype(np.int64)
-        bounds[0], bounds[-1] = 0, self.n_tiles
-        bounds = np.maximum.accumulate(np.minimum(bounds, self.n_tiles))
-        self.edge_blocks = blocks
-        self.edge_bounds_dev = torch.from_numpy(bounds).to(self.device)
-        self.src_words_max = max((sp.n + 31) // 32 for sp in self.specs)
 
     def _build_sims(self, beta_tabs, bl_tabs, kins):
         recs = []
@@ -389,9 +369,6 @@ class BatchState:
         st.n_segments = len(self.segments)
         st.n_tiles = self.n_tiles
         st.n_agent_blocks = self.n_agent_blocks
-        st.edge_block_tiles = self.edge_bounds_dev.data_ptr()
-        st.n_edge_blocks = self.edge_blocks
-        st.src_words_max = self.src_words_max
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
                   'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'events', 'event_count',

@@ -165,11 +165,6 @@ typedef struct covgpu_state {
   int32_t n_segments;             /* layer segments over all sims                   */
   int64_t n_tiles;                /* edge-pass tiles over all segments              */
   int64_t n_agent_blocks;
-  /* edge-pass work split: block b of the edge pass handles the tiles
-   * [edge_block_tiles[b], edge_block_tiles[b + 1]) (contiguous, balanced by cost) */
-  const int64_t* edge_block_tiles; /* [n_edge_blocks + 1]                          */
-  int32_t n_edge_blocks;
-  int32_t src_words_max;          /* max over sims of ceil(n_agents / 32)           */
   /* per-agent state */
   uint32_t* flags;
   uint32_t* vstate;               /* bytes: exposed, infectious, recovered variant   */
