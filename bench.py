@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 POP = 1_000_000
 DAYS = 180
 PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+# DRAM bytes (read + write) of one launch, from an ncu capture of that launch
+# on this workload (profiles/k_edge_pass_hybrid1M_dram.md); None until captured
+MEASURED_TRAFFIC = {}
 
 
 def parse():
@@ -149,26 +152,32 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- algorithmic bytes
-def agent_pass_bytes(res, n, nv, t):
-    """Bytes one agent pass must move on day t (closing day t-1 fused in).
-
-    Every agent: flag + variant words read (8), date_recovered read (4), NAb
-    state read (nab, peak_nab, t_nab_event: 12), immunity written (12*nv).
-    Agents with NAbs: nab written (4). Exposed agents: five more date reads
-    (20). Infectious: rel_trans + the two other viral-load dates read (12) and
-    viral load written (4). Susceptible: rel_sus read (4). Role bitmaps: n/4.
-    """
-    ex = res['n_exposed'][t - 1] if t > 0 else 0
-    inf = res['n_infectious'][t - 1] if t > 0 else 0
-    sus = res['n_susceptible'][t - 1] if t > 0 else n
-    with_nabs = n - sus if t > 0 else 0  # upper bound: everyone ever infected has NAbs
-    return 8 * n + 4 * n + 12 * n + 12 * nv * n + 4 * with_nabs + 20 * ex + 16 * inf + 4 * sus + n / 4
+# Algorithmic bytes per unit of work (the HBM roofline's numerator), the
+# per-unit figures of the reference's own algorithm:
+#   edge pass  28 B per undirected edge per day: p1, p2 and beta streamed
+#              (12 B) plus rel_trans and rel_sus of both endpoints gathered
+#              (16 B), over every layer including the redrawn one;
+#   agent pass 76 + 12*nv B per agent per day: six date reads (24), two
+#              end-of-isolation/quarantine dates (8), base rel_trans/rel_sus
+#              (8), nab/peak_nab/t_nab_event (12), variant fields (4), flags
+#              read+write (8), nab write (4), effective rel_trans/rel_sus
+#              writes (8), and 3*nv immunity writes (12*nv).
+EDGE_BYTES_PER_EDGE = 28
+AGENT_BYTES_BASE, AGENT_BYTES_PER_VARIANT = 76, 12
 
 
-def edge_pass_bytes(spec, n):
-    """Bytes one edge pass must move: p1/p2 of every stored (static) edge, plus
-    the role bitmaps (n/4, L2-resident). Dynamic-layer edges are generated in
-    registers and move no bytes."""
+def agent_pass_bytes(n, nv):
+    return (AGENT_BYTES_BASE + AGENT_BYTES_PER_VARIANT * nv) * n
+
+
+def edge_pass_bytes(spec):
+    return EDGE_BYTES_PER_EDGE * sum(len(ly['p1']) for ly in spec.layers)
+
+
+def edge_pass_floor_bytes(spec, n):
+    """Bytes the GPU edge pass cannot avoid: p1/p2 of every stored edge and the
+    role bitmaps (dynamic-layer edges are drawn in registers; agent state is
+    gathered only for source->target candidates)."""
     e_static = sum(len(ly['p1']) for ly in spec.layers if not ly['dynamic'])
     return 8 * e_static + n / 4
 
@@ -262,16 +271,20 @@ def gpu_arm(args, world, rank):
     dom = max(totals, key=totals.get)
     nv = 1
     if dom == 'agent_step':
-        bytes_per = [agent_pass_bytes(res, n, nv, t) for t in range(npts + 1)]
+        bytes_launch, unit_desc = agent_pass_bytes(n, nv), f'{AGENT_BYTES_BASE + AGENT_BYTES_PER_VARIANT * nv} B/agent/day'
     elif dom == 'edge_pass':
-        bytes_per = [edge_pass_bytes(sim.spec, st.n)] * npts
+        bytes_launch, unit_desc = edge_pass_bytes(sim.spec), f'{EDGE_BYTES_PER_EDGE} B/undirected edge/day'
     else:
-        bytes_per = [16.0 * max(res['new_infections'][t], 1) for t in range(npts)]
+        bytes_launch = 16.0 * max(float(np.mean(res['new_infections'])), 1.0)
+        unit_desc = '16 B/new infection'
     avg_ms = totals[dom] / len(kt[dom])
-    achieved = float(np.mean(bytes_per)) / (avg_ms / 1e3) / 1e9
+    achieved = bytes_launch / (avg_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    traffic = MEASURED_TRAFFIC.get((dom, n)) if dom == 'edge_pass' else None
     roofline = {'bound': 'hbm', 'kernel': f'k_{dom}', 'achieved': round(achieved, 1), 'peak': peak,
-                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4), 'traffic': None,
+                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4), 'traffic': traffic,
+                'algorithmic_bytes_per_launch': round(bytes_launch), 'bytes_per_unit': unit_desc,
+                'floor_bytes_per_launch': round(edge_pass_floor_bytes(sim.spec, st.n)) if dom == 'edge_pass' else None,
                 'avg_launch_ms': round(avg_ms, 5),
                 'kernel_ms_total': {k: round(v, 3) for k, v in totals.items()},
                 'kernel_share': {k: round(v / sum(totals.values()), 4) for k, v in totals.items()}}

@@ -1,0 +1,153 @@
+"""CPU restatement of Covasim 3.1.7's testing and contact-tracing interventions.
+
+TEST INFRASTRUCTURE ONLY. The product never imports this module; tests import
+it as the checker.
+
+``TestProb`` restates ``test_prob`` (covasim/interventions.py:858-981) and
+``ContactTracing`` restates ``contact_tracing`` (covasim/interventions.py:984-1145),
+for the options the GPU path supports (no swab-delay distribution, no ILI
+prevalence, no subtargeting, no tracing capacity). Their random draws come
+from the oracle sim: the numpy MT19937 stream in the reference's call order
+(``rng='mt'``), or Philox keyed by (agent, day) and (agent, layer, day) like
+the CUDA library's (``rng='philox'``).
+"""
+import numpy as np
+
+from . import philox as ph
+
+
+def get_quar_inds(quar_policy, sim):
+    """interventions.py:682-710 (string and number policies)."""
+    t = sim.t
+    p = sim.people
+    if quar_policy is None:
+        return np.array([], dtype=np.int64)
+    if quar_policy == 'start':
+        return (p.date_quarantined == t - 1).nonzero()[0]
+    if quar_policy == 'end':
+        return (p.date_end_quarantine == t + 1).nonzero()[0]
+    if quar_policy == 'both':
+        return np.concatenate([(p.date_quarantined == t - 1).nonzero()[0], (p.date_end_quarantine == t + 1).nonzero()[0]])
+    if quar_policy == 'daily':
+        return p.quarantined.nonzero()[0]
+    qp = np.atleast_1d(np.asarray(quar_policy))
+    return np.unique(np.concatenate([(p.date_quarantined == t - 1 - q).nonzero()[0] for q in qp]))
+
+
+def find_contacts(p1, p2, inds):
+    """utils.py:131-147 + base.py:1808-1846 (as a sorted array): partners of ``inds``."""
+    p1 = np.asarray(p1)
+    p2 = np.asarray(p2)
+    out = np.concatenate([p2[np.isin(p1, inds)], p1[np.isin(p2, inds)]])
+    return np.unique(out).astype(np.int64)
+
+
+def _active(t, start_day, end_day):
+    return not (t < start_day or (end_day is not None and t > end_day))
+
+
+class TestProb:
+    """interventions.py:858-981 (swab_delay, ili_prev and subtarget unsupported)."""
+
+    def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
+                 sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0, end_day=None):
+        self.symp_prob = symp_prob
+        self.asymp_prob = asymp_prob
+        self.symp_quar_prob = symp_quar_prob if symp_quar_prob is not None else symp_prob
+        self.asymp_quar_prob = asymp_quar_prob if asymp_quar_prob is not None else asymp_prob
+        self.quar_policy = quar_policy if quar_policy else 'start'
+        self.sensitivity = sensitivity
+        self.loss_prob = loss_prob
+        self.test_delay = test_delay
+        self.start_day = start_day
+        self.end_day = end_day
+
+    def apply(self, sim):
+        t = sim.t
+        if not _active(t, self.start_day, self.end_day):
+            return None
+        people = sim.people
+        n = sim.n
+        symp_inds = people.symptomatic.nonzero()[0]
+        asymp_inds = np.setdiff1d(np.arange(n), symp_inds)
+        quar_test_inds = get_quar_inds(self.quar_policy, sim)
+        symp_quar_inds = np.intersect1d(quar_test_inds, symp_inds)
+        asymp_quar_inds = np.intersect1d(quar_test_inds, asymp_inds)
+        diag_inds = people.diagnosed.nonzero()[0]
+        test_probs = np.zeros(n)
+        test_probs[symp_inds] = self.symp_prob
+        test_probs[asymp_inds] = self.asymp_prob
+        test_probs[symp_quar_inds] = self.symp_quar_prob
+        test_probs[asymp_quar_inds] = self.asymp_quar_prob
+        test_probs[diag_inds] = 0.0
+        if sim.rng == 'philox':
+            u_test, u_sens, u_keep = ph.test_draws(sim.k0, sim.k1, t, np.arange(n))
+            test_inds = (u_test < test_probs).nonzero()[0]
+            sens = lambda inds: u_sens[inds]  # noqa: E731
+            keep = lambda inds: u_keep[inds]  # noqa: E731
+        else:
+            rs = sim.rs_numpy
+            test_inds = (rs.random_sample(n) < test_probs).nonzero()[0]
+            sens = keep = lambda inds: rs.random_sample(len(inds))  # noqa: E731
+        people.test(test_inds, sens, keep, test_sensitivity=self.sensitivity, loss_prob=self.loss_prob,
+                    test_delay=self.test_delay)
+        sim.results['new_tests'][t] += len(test_inds)
+        return test_inds
+
+
+class ContactTracing:
+    """interventions.py:984-1145 (capacity unsupported)."""
+
+    def __init__(self, trace_probs=None, trace_time=None, start_day=0, end_day=None, presumptive=False,
+                 quar_period=None):
+        self.trace_probs = trace_probs
+        self.trace_time = trace_time
+        self.start_day = start_day
+        self.end_day = end_day
+        self.presumptive = presumptive
+        self.quar_period = quar_period
+
+    def initialize(self, sim):
+        """interventions.py:1023-1041."""
+        if self.trace_probs is None:
+            self.trace_probs = 1.0
+        if self.trace_time is None:
+            self.trace_time = 0.0
+        if self.quar_period is None:
+            self.quar_period = sim.pars['quar_period']
+        if np.isscalar(self.trace_probs):
+            self.trace_probs = {k: self.trace_probs for k in sim.layer_keys}
+        if np.isscalar(self.trace_time):
+            self.trace_time = {k: self.trace_time for k in sim.layer_keys}
+
+    def apply(self, sim):
+        t = sim.t
+        if not _active(t, self.start_day, self.end_day):
+            return None
+        people = sim.people
+        if not self.presumptive:
+            trace_inds = (people.date_diagnosed == t).nonzero()[0]
+        else:
+            just_tested = (people.date_tested == t).nonzero()[0]
+            trace_inds = just_tested[people.exposed[just_tested]]
+        if not len(trace_inds):
+            return {}
+        contacts = {}
+        for lkey, prob in self.trace_probs.items():
+            if prob == 0:
+                continue
+            layer = sim.contacts[lkey]
+            traceable = find_contacts(layer['p1'], layer['p2'], trace_inds)
+            if len(traceable):
+                if sim.rng == 'philox':
+                    u = ph.trace_draws(sim.k0, sim.k1, t, sim.layer_keys.index(lkey), traceable)
+                else:
+                    u = sim.rs_numpy.random_sample(len(traceable))
+                contacts.setdefault(self.trace_time[lkey], []).extend(traceable[(u < prob).nonzero()[0]])
+        is_dead = people.dead.nonzero()[0]
+        for trace_time, inds in contacts.items():
+            contact_inds = np.setdiff1d(np.asarray(inds, dtype=np.int64), is_dead)
+            people.known_contact[contact_inds] = True
+            people.date_known_contact[contact_inds] = np.fmin(people.date_known_contact[contact_inds], t + trace_time)
+            people.schedule_quarantine(contact_inds, start_date=t + trace_time, period=self.quar_period - trace_time)
+        return contacts

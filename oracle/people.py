@@ -146,6 +146,7 @@ class OraclePeople:
         for key in DATES + DURS:
             setattr(self, key, np.full(n, np.nan, dtype=F32))
         self.infection_log = []
+        self._pending = {}  # people.py:115 _pending_quarantine
         self.init_flows()
 
     def __getitem__(self, key):
@@ -264,6 +265,70 @@ class OraclePeople:
         end_inds = self.check_inds(~self.isolated, self.date_end_isolation, filter_inds=None)
         self.isolated[end_inds] = False
         return end_inds
+
+    # ---------------------------------------------------------------- after interventions
+    def update_states_post(self):
+        """people.py:189-196."""
+        self.flows['new_diagnoses'] += len(self.check_diagnosed())
+        self.flows['new_quarantined'] += self.check_quar()
+        self.flows['new_isolated'] += len(self.check_enter_iso())
+
+    def check_diagnosed(self):
+        """people.py:315-332."""
+        test_pos_inds = self.check_inds(self.diagnosed, self.date_pos_test, filter_inds=None)
+        self.date_pos_test[test_pos_inds] = np.nan
+        diag_inds = self.check_inds(self.diagnosed, self.date_diagnosed, filter_inds=None)
+        self.diagnosed[diag_inds] = True
+        return test_pos_inds
+
+    def check_quar(self):
+        """people.py:335-358; ``_pending_quarantine`` maps a start day to (agent, end day) requests."""
+        n_quarantined = 0
+        for ind, end_day in self._pending.pop(self.t, []):
+            if self.quarantined[ind]:
+                # Python's max keeps its first argument unless the second compares greater
+                cur = self.date_end_quarantine[ind]
+                self.date_end_quarantine[ind] = end_day if end_day > cur else cur
+            elif not (self.dead[ind] or self.recovered[ind] or self.diagnosed[ind] or self.isolated[ind]):
+                self.quarantined[ind] = True
+                self.date_quarantined[ind] = self.t
+                self.date_end_quarantine[ind] = end_day
+                n_quarantined += 1
+        diag_inds = (self.quarantined & (self.date_diagnosed == self.t)).nonzero()[0]
+        self.date_end_quarantine[diag_inds] = self.t
+        end_inds = self.check_inds(~self.quarantined, self.date_end_quarantine, filter_inds=None)
+        self.quarantined[end_inds] = False
+        return n_quarantined
+
+    def check_enter_iso(self):
+        """people.py:361-366."""
+        iso_inds = (self.date_diagnosed == self.t).nonzero()[0]
+        self.isolated[iso_inds] = True
+        self.date_end_isolation[iso_inds] = self.date_recovered[iso_inds]
+        return iso_inds
+
+    def test(self, inds, u_sens, u_keep, test_sensitivity=1.0, loss_prob=0.0, test_delay=0):
+        """people.py:589-617. ``u_sens(is_infectious)`` and ``u_keep(not_diagnosed)``
+        give the uniforms of the sensitivity and loss-to-follow-up trials."""
+        inds = np.unique(inds)
+        self.tested[inds] = True
+        self.date_tested[inds] = self.t
+        is_infectious = inds[self.infectious[inds]]
+        pos_test = u_sens(is_infectious) < test_sensitivity
+        is_inf_pos = is_infectious[pos_test]
+        not_diagnosed = is_inf_pos[np.isnan(self.date_diagnosed[is_inf_pos])]
+        not_lost = u_keep(not_diagnosed) < 1.0 - loss_prob
+        final_inds = not_diagnosed[not_lost]
+        self.date_diagnosed[final_inds] = self.t + test_delay
+        self.date_pos_test[final_inds] = self.t
+        return final_inds
+
+    def schedule_quarantine(self, inds, start_date=None, period=None):
+        """people.py:620-640."""
+        start_date = self.t if start_date is None else int(start_date)
+        period = self.pars['quar_period'] if period is None else int(period)
+        for ind in inds:
+            self._pending.setdefault(start_date, []).append((ind, start_date + period))
 
     # ---------------------------------------------------------------- infection
     def infect(self, inds, hosp_max=None, icu_max=None, source=None, layer=None, variant=0,

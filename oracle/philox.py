@@ -15,6 +15,8 @@ Stream layout (shared with the CUDA side; all words little-endian uint32):
     edge Bernoulli      : (edge_lo, edge_hi, day, TAG_EDGE  | variant << 8 | layer)
     dynamic-layer edges : (edge_lo, edge_hi, day, TAG_LAYER | layer)
     infect draws        : (agent,   block,   day, TAG_INFECT | call_tag)
+    testing draws       : (agent,   block,   day, TAG_TEST)  block 0: test, sensitivity; 1: follow-up
+    tracing draws       : (agent,   layer,   day, TAG_TRACE)
 
 Draw conversions:
   u52(a, b)  = ((a >> 6) << 26 | (b >> 6)) ... see ``u01_52``: exact doubles in (0, 1)
@@ -31,6 +33,8 @@ PHILOX_W1 = np.uint32(0xBB67AE85)
 TAG_EDGE = 0x01000000
 TAG_LAYER = 0x02000000
 TAG_INFECT = 0x03000000
+TAG_TEST = 0x04000000
+TAG_TRACE = 0x05000000
 
 _MASK32 = np.uint64(0xFFFFFFFF)
 
@@ -147,3 +151,19 @@ def infect_draws(k0, k1, day, call_tag, agents):
     out[:, U_CRIT] = u01_32(b2[0])
     out[:, U_DEATH] = u01_32(b2[1])
     return out
+
+
+def test_draws(k0, k1, day, agents):
+    """The three uniforms of one agent's testing on one day: (test, sensitivity,
+    not lost to follow-up), each a 52-bit exact double."""
+    a = np.asarray(agents, dtype=np.int64)
+    b0 = philox4x32_10(a, 0, day, TAG_TEST, k0, k1)
+    b1 = philox4x32_10(a, 1, day, TAG_TEST, k0, k1)
+    return u01_52(b0[0], b0[1]), u01_52(b0[2], b0[3]), u01_52(b1[0], b1[1])
+
+
+def trace_draws(k0, k1, day, layer, agents):
+    """The uniform deciding whether a contact of a traced case in ``layer`` is reached."""
+    a = np.asarray(agents, dtype=np.int64)
+    b = philox4x32_10(a, int(layer), day, TAG_TRACE, k0, k1)
+    return u01_52(b[0], b[1])

@@ -72,9 +72,11 @@ class OracleSim:
         contacts: {layer key: dict(p1, p2, beta)}; layer order is layer index
         rng: 'philox' or 'mt'
         beta_schedule: optional per-day overall beta (change_beta), length npts
+        interventions: optional list of ``oracle.interventions`` objects (testing, tracing)
     """
 
-    def __init__(self, pars, person, contacts, rng='philox', beta_schedule=None, seed_inds=None, arith=None):
+    def __init__(self, pars, person, contacts, rng='philox', beta_schedule=None, seed_inds=None, arith=None,
+                 interventions=None):
         self.pars = pars
         self.n = int(pars['pop_size'])
         self.npts = int(pars['n_days']) + 1
@@ -95,6 +97,10 @@ class OracleSim:
             self.rs_numpy = np.random.RandomState(self.seed)
         self.beta_schedule = beta_schedule
         self.seed_inds = seed_inds
+        self.interventions = list(interventions or [])  # oracle.interventions objects, applied in order
+        for iv in self.interventions:
+            if hasattr(iv, 'initialize'):
+                iv.initialize(self)
         self.t = 0
         self.results = {}
         for key in FLOWS + [f'n_{k}' for k in RESULT_STOCKS] + ['pop_nabs', 'pop_protection', 'pop_symp_protection']:
@@ -148,6 +154,9 @@ class OracleSim:
         icu_max = people.critical.sum() > p['n_beds_icu'] if p['n_beds_icu'] is not None else False
         if self.beta_schedule is not None:
             p['beta'] = self.beta_schedule[t]
+        for iv in self.interventions:  # sim.py:596-598
+            iv.apply(self)
+        people.update_states_post()  # sim.py:600
 
         vd = p['viral_dist']
         viral_load = compute_viral_load(t, people.date_infectious, people.date_recovered, people.date_dead,

@@ -39,6 +39,18 @@ def load_npz(name):
     return dict(np.load(os.path.join(GOLDEN, name), allow_pickle=False))
 
 
+def load_testing_case(d, i):
+    """Inputs of case ``i`` of ref_testing.npz: (pars, person, contacts, test_prob kwargs, contact_tracing kwargs)."""
+    pars = fix_pars(unjson(json.loads(str(d[f's{i}.pars']))))
+    pars['interventions'] = []
+    person = {k[len(f's{i}.person.'):]: v for k, v in d.items() if k.startswith(f's{i}.person.')}
+    nl = len([k for k in d if k.startswith(f's{i}.L') and k.endswith('.p1')])
+    keys = list(pars['beta_layer'].keys())
+    contacts = {keys[li]: {c: d[f's{i}.L{li}.{c}'] for c in ('p1', 'p2', 'beta')} for li in range(nl)}
+    ivs = json.loads(str(d[f's{i}.interventions']))
+    return pars, person, contacts, ivs['test_prob'], ivs['contact_tracing']
+
+
 def load_day(name):
     d = load_npz(f'ref_day_{name}.npz')
     pars = fix_pars(unjson(json.loads(str(d['pars']))))

@@ -19,6 +19,8 @@ Fixtures:
                        (variant, layer) trans/sus, infections and infect() results with the
                        draws mapped to per-edge / per-agent slots, and update_nab
   ref_sims.npz         whole reference runs (inputs and daily results) for MT-mode replay
+  ref_testing.npz      whole reference runs with test_prob + contact_tracing (inputs,
+                       intervention arguments, daily results, final testing/quarantine state)
   ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
                        20k-agent random sim (60 days), reference code with MT19937 streams
 """
@@ -385,6 +387,52 @@ def make_sims_fixture(ref):
     print('ref_sims.npz written')
 
 
+TESTING_CASES = [  # (pop_type, n, days, seed, use_waning, dynamic c, test_prob kwargs, contact_tracing kwargs)
+    ('hybrid', 1500, 40, 3, True, 0, dict(symp_prob=0.2, asymp_prob=0.01), dict(trace_probs=0.5, trace_time=1)),
+    ('hybrid', 1500, 40, 4, True, 1,
+     dict(symp_prob=0.3, asymp_prob=0.02, symp_quar_prob=0.5, asymp_quar_prob=0.1, quar_policy='both',
+          sensitivity=0.9, loss_prob=0.1, test_delay=2),
+     dict(trace_probs={'h': 1.0, 's': 0.5, 'w': 0.5, 'c': 0.2}, trace_time={'h': 0, 's': 1, 'w': 2, 'c': 3})),
+    ('random', 1200, 40, 5, True, 0, dict(symp_prob=0.3, quar_policy='daily', start_day=5, end_day=30),
+     dict(trace_probs=0.8, presumptive=True, start_day=8)),
+    ('hybrid', 1200, 40, 6, False, 0, dict(symp_prob=0.3, quar_policy=[0, 2]),
+     dict(trace_probs=0.7, trace_time=0.5, quar_period=10)),
+]
+TESTING_FINAL = ['diagnosed', 'quarantined', 'isolated', 'known_contact', 'tested', 'date_diagnosed',
+                 'date_quarantined', 'date_end_quarantine', 'date_known_contact', 'date_pos_test', 'date_tested',
+                 'date_end_isolation', 'exposed', 'recovered', 'dead']
+
+
+def make_testing_fixture(ref):
+    """Whole runs with the reference's own test_prob and contact_tracing."""
+    out = {}
+    for i, (pop_type, n, days, seed, waning, dyn, tp_kw, ct_kw) in enumerate(TESTING_CASES):
+        pars = ref.make_pars(pop_size=n, n_days=days, pop_type=pop_type, rand_seed=seed, use_waning=waning)
+        if dyn:
+            pars['dynam_layer']['c'] = 1
+        pars['interventions'] = [ref.cvint.test_prob(**tp_kw), ref.cvint.contact_tracing(**ct_kw)]
+        sim = refload.RefSim(ref, pars)
+        for k in ('age', 'sex', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus'):
+            out[f's{i}.person.{k}'] = sim.people[k].copy()
+        for li, lk in enumerate(sim.people.contacts.keys()):
+            for c in ('p1', 'p2', 'beta'):
+                out[f's{i}.L{li}.{c}'] = sim.people.contacts[lk][c].copy()
+        out[f's{i}.pars'] = np.array(json.dumps(jsonable({k: v for k, v in sim.pars.items() if k != 'interventions'})))
+        out[f's{i}.interventions'] = np.array(json.dumps({'test_prob': tp_kw, 'contact_tracing': ct_kw}))
+        sim.run()
+        for k, v in sim.results.items():
+            if k == 'variant':
+                for kk, vv in v.items():
+                    out[f's{i}.res.{kk}'] = vv
+            else:
+                out[f's{i}.res.{k}'] = v
+        for k in TESTING_FINAL:
+            out[f's{i}.final.{k}'] = sim.people[k].copy()
+    out['n'] = np.array(len(TESTING_CASES))
+    np.savez_compressed(os.path.join(HERE, 'ref_testing.npz'), **out)
+    print('ref_testing.npz written')
+
+
 def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
     keys = ['new_infections', 'new_severe', 'new_deaths', 'new_infectious', 'new_recoveries', 'new_critical',
             'new_symptomatic', 'n_exposed']
@@ -410,7 +458,7 @@ def main():
     args = ap.parse_args()
     ref = refload.Reference()
     groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
-                  sims=make_sims_fixture,
+                  sims=make_sims_fixture, testing=make_testing_fixture,
                   distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
     for name, fn in groups.items():
         if args.only is None or args.only == name:

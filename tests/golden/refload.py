@@ -164,6 +164,15 @@ def load_module_body(fname, namespace, skip_imports=True):
     return namespace
 
 
+def load_classes(fname, names, namespace):
+    """Execute selected top-level class and function definitions of a module
+    into ``namespace`` in file order (so base classes precede subclasses)."""
+    path, tree = _read_tree(fname)
+    body = [n for n in tree.body if isinstance(n, (ast.ClassDef, ast.FunctionDef)) and n.name in names]
+    exec(compile(ast.Module(body=body, type_ignores=[]), path, 'exec'), namespace)
+    return {n.name: namespace[n.name] for n in body}
+
+
 def load_functions(fname, names=None, classname=None, namespace=None, njit_namespace=None):
     """Execute selected function definitions (decorators stripped).
 
@@ -335,6 +344,9 @@ class Reference:
             def keys(pself):
                 return pself.meta.all_states[:]
 
+            def layer_keys(pself):
+                return list(pself.contacts.keys())
+
         for k, f in {**base_methods, **people_methods}.items():
             setattr(RefPeople, k, f)
         self.People = RefPeople
@@ -362,9 +374,25 @@ class Reference:
                               'make_microstructured_contacts', 'make_hybrid_contacts'], namespace=pop_ns))
         pop_ns.update(vars(self.cvpop))
 
+        # interventions.py: the base class, test_prob and contact_tracing with the
+        # helpers they call (their draws come from numpy's stream, as in the package)
+        from collections import defaultdict as _dd
+        iv_sc = types.SimpleNamespace(**vars(sc))
+        iv_sc.ddict = _dd
+        iv_sc.isstring = lambda x: isinstance(x, str)
+        iv_sc.isiterable = lambda x: hasattr(x, '__iter__')
+        iv_sc.pr = print
+        pd_stub = types.SimpleNamespace(Series=type('Series', (), {}), DataFrame=type('DataFrame', (), {}))
+        iv_ns = {'np': np_numpy, 'sc': iv_sc, 'cvu': self.cvu, 'cvd': self.cvd, 'inspect': __import__('inspect'),
+                 'pd': pd_stub,
+                 '__all__': ['Intervention', 'test_prob', 'contact_tracing'], '__name__': 'covasim.interventions'}
+        self.cvint = types.SimpleNamespace(**load_classes(
+            'interventions.py', ['preprocess_day', 'get_day', 'process_daily_data', 'get_subtargets',
+                                 'get_quar_inds', 'Intervention', 'test_prob', 'contact_tracing'], iv_ns))
+
         # sim.py day loop
         sim_ns = {'np': np_numpy, 'sc': sc, 'cvu': self.cvu, 'cvd': self.cvd, 'cvimm': self.cvi,
-                  'cvi': types.SimpleNamespace(Intervention=type('Intervention', (), {}))}
+                  'cvi': types.SimpleNamespace(Intervention=self.cvint.Intervention)}
         self.sim_methods = load_functions('sim.py', classname='Sim', namespace=sim_ns,
                                           names=['step', 'init_infections', 'rescale'])
         sim_ns['AlreadyRunError'] = RuntimeError
@@ -423,6 +451,13 @@ class RefSim:
         people.set_prognoses()
         self.people = people
         ref.cvu.set_seed(pars['rand_seed'])
+        for iv in self.pars['interventions']:  # sim.py:457-474 init_interventions
+            if isinstance(iv, ref.cvint.Intervention):
+                iv.initialize(self)
+
+    def day(self, day, *args):
+        """base.py:356-370 for integer days (and None)."""
+        return None if day is None else int(day)
 
     def __getitem__(self, k):
         return self.pars[k]

@@ -10,7 +10,8 @@ import json
 import numpy as np
 import pytest
 
-from common import load_npz, load_day, snap, oracle_people, n_layers, assert_state_equal, unjson, fix_pars, ALL_KEYS
+from common import (load_npz, load_day, snap, oracle_people, n_layers, assert_state_equal, unjson, fix_pars, ALL_KEYS,
+                    load_testing_case)
 from oracle import kernels as ok
 from oracle.people import TableDraws, update_nab
 from oracle.sim import OracleSim
@@ -100,6 +101,21 @@ def test_whole_runs_match_reference_mt_mode():
             ref = d[f's{i}.res.{k}']
             np.testing.assert_allclose(v, ref, rtol=1e-12, atol=0, err_msg=f'sim {i} {k}')
         for k in ('exposed', 'recovered', 'dead', 'susceptible', 'date_recovered', 'peak_nab', 'nab'):
+            assert np.array_equal(sim.people[k], d[f's{i}.final.{k}'], equal_nan=True), (i, k)
+
+
+def test_testing_and_tracing_runs_match_reference_mt_mode():
+    """test_prob + contact_tracing + update_states_post (interventions.py:858-1145,
+    people.py:189-196,315-366,589-640) against the reference's own code."""
+    from oracle.interventions import TestProb, ContactTracing
+    d = load_npz('ref_testing.npz')
+    for i in range(int(d['n'])):
+        pars, person, contacts, tp, ct = load_testing_case(d, i)
+        sim = OracleSim(pars, person, contacts, rng='mt', interventions=[TestProb(**tp), ContactTracing(**ct)]).run()
+        assert d[f's{i}.res.new_tests'].sum() > 0 and d[f's{i}.res.new_quarantined'].sum() > 0
+        for k, v in sim.results.items():
+            np.testing.assert_array_equal(v, d[f's{i}.res.{k}'], err_msg=f'case {i} {k}')
+        for k in [k[len(f's{i}.final.'):] for k in d if k.startswith(f's{i}.final.')]:
             assert np.array_equal(sim.people[k], d[f's{i}.final.{k}'], equal_nan=True), (i, k)
 
 
