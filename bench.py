@@ -39,8 +39,8 @@ POP = 1_000_000
 DAYS = 180
 PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
 # DRAM bytes (read + write) of one launch, from an ncu capture of that launch
-# on this workload (profiles/k_edge_pass_hybrid1M_dram.md); None until captured
-MEASURED_TRAFFIC = {}
+# on this workload (profiles/k_edge_pass_hybrid1M_dram.md: day 90 of the 1M run)
+MEASURED_TRAFFIC = {('edge_pass', 1_000_000): 90_250_240}
 
 
 def parse():

@@ -47,6 +47,20 @@ class DurPar(C.Structure):
     _fields_ = [('code', C.c_int32), ('_pad', C.c_int32), ('a', C.c_double), ('b', C.c_double)]
 
 
+QP_START, QP_END, QP_DAILY, QP_OFFSETS = 1, 2, 4, 8   # COVGPU_QP_* quarantine testing policies
+
+
+class Testing(C.Structure):
+    _fields_ = [
+        ('test_start', C.c_int32), ('test_end', C.c_int32), ('quar_policy', C.c_int32), ('quar_offsets', C.c_uint32),
+        ('thr_symp', C.c_uint64), ('thr_asymp', C.c_uint64), ('thr_symp_quar', C.c_uint64),
+        ('thr_asymp_quar', C.c_uint64), ('thr_sensitivity', C.c_uint64), ('thr_not_lost', C.c_uint64),
+        ('test_delay', C.c_int32), ('trace_start', C.c_int32), ('trace_end', C.c_int32), ('presumptive', C.c_int32),
+        ('trace_time', C.c_double * MAX_LAYERS), ('thr_trace', C.c_uint64 * MAX_LAYERS),
+        ('trace_start_off', C.c_int32 * MAX_LAYERS), ('trace_period', C.c_int32 * MAX_LAYERS),
+    ]
+
+
 class SimParams(C.Structure):
     _fields_ = [
         ('agent_off', C.c_int64), ('n_agents', C.c_int32), ('n_variants', C.c_int32),
@@ -68,6 +82,7 @@ class SimParams(C.Structure):
         ('vx_ln_imm', C.c_void_p),
         ('n_vaccines', C.c_int32), ('_pad2', C.c_int32),
         ('res_int', C.c_void_p), ('res_var', C.c_void_p), ('res_fx', C.c_void_p),
+        ('testing', Testing),
     ]
 
 
@@ -80,6 +95,12 @@ class Layer(C.Structure):
 
 class AgentBlock(C.Structure):
     _fields_ = [('begin', C.c_int64), ('end', C.c_int64), ('sim', C.c_int32), ('_pad', C.c_int32)]
+
+
+class Lik(C.Structure):
+    _fields_ = [('factor', C.c_void_p), ('ll', C.c_void_p), ('expected', C.c_void_p), ('g_ll', C.c_void_p),
+                ('g_exp', C.c_void_p), ('logq', C.c_void_p), ('w', C.c_void_p), ('npts_max', C.c_int32),
+                ('n_layers_max', C.c_int32), ('nv_max', C.c_int32), ('_pad', C.c_int32)]
 
 
 class State(C.Structure):
@@ -101,6 +122,10 @@ class State(C.Structure):
         ('status', C.c_void_p), ('hospicu', C.c_void_p),
         ('sims', C.c_void_p), ('segments', C.c_void_p), ('agent_blocks', C.c_void_p),
         ('draw_table', C.c_void_p), ('edge_uniforms', C.c_void_p),
+        ('has_testing', C.c_int32), ('pending_slots', C.c_int32), ('trace_bits', C.c_void_p),
+        ('contact_bits', C.c_void_p), ('n_contact_layers', C.c_int32), ('_pad1', C.c_int32),
+        ('pending_quar', C.c_void_p), ('trace_count', C.c_void_p),
+        ('lik', Lik),
     ]
 
 
@@ -132,12 +157,14 @@ def lib():
         L.covgpu_agent_step.argtypes = [sp, i32, i32, i32, vp]
         L.covgpu_edge_pass.argtypes = [sp, i32, vp]
         L.covgpu_infect_claims.argtypes = [sp, i32, vp]
+        L.covgpu_test_trace.argtypes = [sp, i32, vp]
+        L.covgpu_lik_pass.argtypes = [sp, i32, vp]
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
         for name in ('covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections', 'covgpu_agent_step',
                      'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_materialize',
-                     'covgpu_run_days'):
+                     'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_pass'):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -156,13 +183,16 @@ def call(name, *args):
 
 def abi_layout():
     """(library values, ctypes values) of the ABI layout check."""
-    out = (C.c_int64 * 16)()
-    m = lib().covgpu_abi_layout(out, 16)
+    out = (C.c_int64 * 32)()
+    m = lib().covgpu_abi_layout(out, 32)
     mine = [C.sizeof(SimParams), C.sizeof(Layer), C.sizeof(AgentBlock), 16, 16, C.sizeof(State),
-            State.sims.offset, State.edge_uniforms.offset, SimParams.res_fx.offset]
+            State.sims.offset, State.edge_uniforms.offset, SimParams.res_fx.offset, C.sizeof(Testing),
+            SimParams.testing.offset, State.pending_quar.offset, State.trace_count.offset, C.sizeof(Lik),
+            State.lik.offset]
     return list(out[:m]), mine
 
 
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
-            'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days']
+            'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
+            'covgpu_lik_pass']

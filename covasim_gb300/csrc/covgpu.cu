@@ -466,7 +466,7 @@ struct SegCtx {
   const float* beta_t;       // beta_tab row of day t ([n_variants])
   float beta_const, beta_layer, quar_factor, iso_factor, asymp_factor;
   uint32_t key0, key1;
-  int nv, layer, seg;
+  int nv, layer, seg, sim;
   int64_t n_edges;
 };
 
@@ -502,6 +502,64 @@ __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c
   const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_EDGE | (v << 8) | (uint32_t)c.layer),
                          c.key0, c.key1);
   return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);  // u < p in float64, decided in integers
+}
+
+// per-thread likelihood sums of one tile (one sim, one layer)
+struct LikAcc {
+  double ll = 0.0, g = 0.0;
+};
+
+// The likelihood terms of one direction s -> g (see covgpu_lik): the
+// outcome is the edge pass's own draw on the float32 p; the terms use p
+// recomputed in float64 from the unrounded factors and F.
+__device__ __forceinline__ void lik_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
+                                        int32_t s, int32_t g, LikAcc& acc) {
+  const uint32_t vs = __ldg(st.vstate + s);
+  const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
+  const float rt = __ldg(st.rel_trans + s), vl = __ldg(st.viral_load + s), rs = __ldg(st.rel_sus + g);
+  const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
+  const uint32_t v = (vs >> 8) & 0xFFu;
+  const uint32_t vc = v < (uint32_t)c.nv ? v : 0u;
+  const float si = __ldg(st.sus_imm + (int64_t)vc * st.n + g);
+  const float beta = __ldg(c.beta_t + vc);
+  if (v >= (uint32_t)c.nv) return;
+  // float32 p exactly as edge_try computes it, for the outcome
+  float rte = rt;
+  if (fs & B_QUAR) rte = __fmul_rn(rte, c.quar_factor);
+  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, c.asymp_factor);
+  if (fs & B_ISO) rte = __fmul_rn(rte, c.iso_factor);
+  rte = __fmul_rn(__fmul_rn(rte, c.beta_layer), vl);
+  float rse = rs;
+  if (fg & B_QUAR) rse = __fmul_rn(rse, c.quar_factor);
+  rse = __fmul_rn(rse, __fsub_rn(1.0f, si));
+  const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
+  if (p == 0.0f) return;
+  bool hit;
+  if (st.edge_uniforms) {
+    hit = st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
+  } else {
+    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
+                                      TAG_EDGE | (v << 8) | (uint32_t)c.layer), c.key0, c.key1);
+    hit = dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);
+  }
+  // float64 p from the same factors
+  const covgpu_lik& K = st.lik;
+  double r = (double)rt;
+  if (fs & B_QUAR) r = __dmul_rn(r, (double)c.quar_factor);
+  if (!(fs & B_SYMP)) r = __dmul_rn(r, (double)c.asymp_factor);
+  if (fs & B_ISO) r = __dmul_rn(r, (double)c.iso_factor);
+  r = __dmul_rn(r, (double)vl);
+  double q = (double)rs;
+  if (fg & B_QUAR) q = __dmul_rn(q, (double)c.quar_factor);
+  q = __dmul_rn(q, __dsub_rn(1.0, (double)si));
+  const double F = K.factor[(((int64_t)c.sim * K.npts_max + t) * K.n_layers_max + c.layer) * K.nv_max + v];
+  const double p64 = __dmul_rn(__dmul_rn(__dmul_rn(F, (double)lb), r), q);
+  const double l1m = log1p(-p64);
+  const double odds = __ddiv_rn(p64, __dsub_rn(1.0, p64));
+  acc.ll += hit ? log(p64) : l1m;
+  acc.g += hit ? 1.0 : -odds;
+  atomicAdd(K.logq + g, l1m);
+  if (K.g_exp) atomicAdd(K.w + (int64_t)c.layer * st.n + g, odds);
 }
 
 __device__ __forceinline__ uint64_t event_key(int t, uint32_t v, int layer, int dir, int64_t e) {
@@ -548,8 +606,10 @@ __device__ __forceinline__ void queue_push(EdgeQueue& q, int& qn, bool has, int3
 }
 
 // phase B: one candidate per lane, then the warp-aggregated event append
+// (LIK: the likelihood terms instead of the events)
+template <bool LIK>
 __device__ __forceinline__ void queue_drain(const covgpu_state& st, const SegCtx& c, int t, int64_t e0,
-                                            EdgeQueue& q, int qn) {
+                                            EdgeQueue& q, int qn, LikAcc& acc) {
   __syncwarp();
   const int lane = threadIdx.x & 31;
   for (int base = 0; base < qn; base += 32) {
@@ -560,13 +620,21 @@ __device__ __forceinline__ void queue_drain(const covgpu_state& st, const SegCtx
     uint32_t m = 0;
     if (i < qn) {
       s = q.s[i]; g = q.g[i]; m = q.m[i];
-      hit = edge_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, v);
+      if (LIK) lik_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, acc);
+      else hit = edge_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, v);
     }
-    emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), e0 + (m >> 1)) : 0ull, g, s);
+    if (!LIK) emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), e0 + (m >> 1)) : 0ull, g, s);
   }
   __syncwarp();
 }
 
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+template <bool LIK>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
   __shared__ int s_seg;
   __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
@@ -596,6 +664,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   c.key1 = sp->key1;
   c.beta_t = sp->beta_tab + (int64_t)t * c.nv;
   c.beta_layer = sp->beta_layer_tab[(int64_t)t * sp->n_layers + c.layer];
+  c.sim = L->sim;
   const bool dynamic = L->dynamic != 0;
   const int32_t* p1 = L->p1;
   const int32_t* p2 = L->p2;
@@ -605,6 +674,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   const int32_t off = (int32_t)sp->agent_off;
   EdgeQueue& q = s_q[threadIdx.x >> 5];
   int qn = 0;  // warp-uniform queue length
+  LikAcc acc;
   constexpr int ROUNDS = EDGE_TILE / (EDGE_THREADS * EDGE_VEC);
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
@@ -644,16 +714,82 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
       queue_push(q, qn, in && (rb[j].src & ra[j].tgt), b[j], a[j], m | 1u);
     }
     if (qn > EQ_CAP - EQ_ROUND) {
-      queue_drain(st, c, t, e0, q, qn);
+      queue_drain<LIK>(st, c, t, e0, q, qn, acc);
       qn = 0;
     }
   }
-  if (qn > 0) queue_drain(st, c, t, e0, q, qn);
+  if (qn > 0) queue_drain<LIK>(st, c, t, e0, q, qn, acc);
+  if (LIK) {  // the tile's sums: one sim, one layer
+    __shared__ double s_acc[EDGE_THREADS / 32][2];
+    const double a = warp_sum_d(acc.ll), b = warp_sum_d(acc.g);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_acc[warp][0] = a; s_acc[warp][1] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double x = 0.0, y = 0.0;
+      for (int k = 0; k < EDGE_THREADS / 32; ++k) { x += s_acc[k][0]; y += s_acc[k][1]; }
+      const covgpu_lik& K = st.lik;
+      const int64_t day = (int64_t)c.sim * K.npts_max + t;
+      if (x != 0.0) atomicAdd(K.ll + day, x);
+      if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + c.layer, y);
+    }
+  }
 }
 
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
   if (st->n_tiles == 0) return COVGPU_OK;
-  k_edge_pass<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  k_edge_pass<false><<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  return launch_status();
+}
+
+// per target: expected = 1 - prod(1 - p) and its per-layer sensitivities, then
+// the per-target sums are cleared for the next day
+__global__ void __launch_bounds__(AGENT_THREADS) k_lik_agents(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_lik& K = st.lik;
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31;
+  __shared__ double s_e;
+  __shared__ double s_h[COVGPU_MAX_LAYERS];
+  if (threadIdx.x == 0) s_e = 0.0;
+  if (threadIdx.x < COVGPU_MAX_LAYERS) s_h[threadIdx.x] = 0.0;
+  __syncthreads();
+  double qprod = 0.0, e = 0.0;
+  if (valid) {
+    const double lq = K.logq[i];
+    if (lq != 0.0) {
+      qprod = exp(lq);
+      e = 1.0 - qprod;
+      K.logq[i] = 0.0;
+    }
+  }
+  e = warp_sum_d(e);
+  if (lane == 0 && e != 0.0) atomicAdd(&s_e, e);
+  if (K.g_exp) {
+    for (int l = 0; l < sp.n_layers; ++l) {
+      double h = 0.0;
+      if (valid && qprod != 0.0) {
+        double* wl = K.w + (int64_t)l * st.n + i;
+        const double x = *wl;
+        if (x != 0.0) { h = qprod * x; *wl = 0.0; }
+      }
+      h = warp_sum_d(h);
+      if (lane == 0 && h != 0.0) atomicAdd(&s_h[l], h);
+    }
+  }
+  __syncthreads();
+  const int64_t day = (int64_t)blk.sim * K.npts_max + t;
+  if (threadIdx.x == 0 && s_e != 0.0) atomicAdd(K.expected + day, s_e);
+  if (K.g_exp && threadIdx.x < sp.n_layers && s_h[threadIdx.x] != 0.0)
+    atomicAdd(K.g_exp + day * K.n_layers_max + threadIdx.x, s_h[threadIdx.x]);
+}
+
+int launch_lik_pass(const covgpu_state* st, int t, cudaStream_t s) {
+  if (!st->lik.factor) return COVGPU_OK;
+  if (st->n_tiles > 0) k_edge_pass<true><<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  k_lik_agents<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }
 
@@ -888,6 +1024,234 @@ __global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1
   }
 }
 
+// ============================================================ testing and tracing
+//
+// Day t with a test_prob / contact_tracing sim, after the agent pass and any
+// importations (sim.py:596-600): k_test_pass draws who tests and marks the
+// agents to trace, k_trace_scan marks their contacts layer by layer, and
+// k_post_pass notifies the contacts and runs update_states_post.
+
+__device__ __forceinline__ bool day_active(int t, int start, int end) { return t >= start && t <= end; }
+
+// interventions.py:682-710: is agent i a quarantined tester on day t?
+__device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu_testing& T, int64_t i, int t,
+                                            uint32_t f) {
+  const int qp = T.quar_policy;
+  if (!qp) return false;
+  bool q = false;
+  if (qp & (COVGPU_QP_START | COVGPU_QP_OFFSETS)) {
+    const float dq = date_row(st, COVGPU_DATE_QUARANTINED)[i];
+    if ((qp & COVGPU_QP_START) && dq == (float)(t - 1)) q = true;
+    if ((qp & COVGPU_QP_OFFSETS) && defined(dq)) {
+      const float back = (float)(t - 1) - dq;  // exact: both are small integers when it matters
+      if (back >= 0.0f && back < 32.0f && back == floorf(back) && ((T.quar_offsets >> (int)back) & 1u)) q = true;
+    }
+  }
+  if ((qp & COVGPU_QP_END) && date_row(st, COVGPU_DATE_END_QUARANTINE)[i] == (float)(t + 1)) q = true;
+  if ((qp & COVGPU_QP_DAILY) && (f & B_QUAR)) q = true;
+  return q;
+}
+
+// test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
+// then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
+__global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  const bool test_on = day_active(t, T.test_start, T.test_end);
+  const bool trace_on = day_active(t, T.trace_start, T.trace_end);
+  if (!test_on && !trace_on) return;  // uniform over the block (one sim per block)
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t tested = 0, trace = 0;
+  if (valid) {
+    uint32_t f = st.flags[i];
+    float* d_diag = date_row(st, COVGPU_DATE_DIAGNOSED) + i;
+    if (test_on) {
+      uint64_t thr = 0;
+      if (!(f & B_DIAG)) {  // the diagnosed do not test
+        const bool symp = f & B_SYMP;
+        thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
+                                          : (symp ? T.thr_symp : T.thr_asymp);
+      }
+      if (thr) {
+        const uint32_t local = (uint32_t)(i - sp.agent_off);
+        const uint4 w = philox(make_uint4(local, 0u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
+        if (bern52_thr(w.x, w.y, thr)) {
+          tested = 1;
+          st.flags[i] = f | B_TESTED;
+          date_row(st, COVGPU_DATE_TESTED)[i] = (float)t;
+          if ((f & B_INF) && bern52_thr(w.z, w.w, T.thr_sensitivity) && isnan(*d_diag)) {
+            const uint4 w1 = philox(make_uint4(local, 1u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
+            if (bern52_thr(w1.x, w1.y, T.thr_not_lost)) {
+              *d_diag = (float)(t + T.test_delay);
+              date_row(st, COVGPU_DATE_POS_TEST)[i] = (float)t;
+            }
+          }
+        }
+      }
+    }
+    if (trace_on) {
+      if (T.presumptive)
+        trace = (date_row(st, COVGPU_DATE_TESTED)[i] == (float)t && (f & B_EXP)) ? 1u : 0u;
+      else
+        trace = (*d_diag == (float)t) ? 1u : 0u;
+    }
+  }
+  const uint32_t tm = __ballot_sync(0xffffffffu, trace);
+  if (trace_on && lane == 0 && blk.begin + warp * 32 < blk.end) st.trace_bits[(blk.begin + warp * 32) >> 5] = tm;
+  const unsigned n_tested = __reduce_add_sync(0xffffffffu, tested);
+  if (lane == 0 && n_tested)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
+              (unsigned long long)n_tested);
+  if (lane == 0 && tm) atomicAdd(st.trace_count + blk.sim, (unsigned)__popc(tm));
+}
+
+__device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, int32_t a) {
+  return (__ldg(bits + (a >> 5)) >> (a & 31)) & 1u;
+}
+
+// contact_tracing.identify_contacts, the find_contacts half (utils.py:131-147):
+// every edge with a traced endpoint marks the other endpoint in its layer's bitmap
+__global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
+  __shared__ int s_seg;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = st.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    s_seg = lo;
+  }
+  __syncthreads();
+  const covgpu_layer* L = st.segments + s_seg;
+  const covgpu_sim_params& sp = st.sims[L->sim];
+  const covgpu_testing& T = sp.testing;
+  if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
+  const int64_t words = (st.n + 31) >> 5;
+  uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
+  const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
+  const int32_t off = (int32_t)sp.agent_off;
+  constexpr int ROUNDS = EDGE_TILE / (EDGE_THREADS * EDGE_VEC);
+  for (int r = 0; r < ROUNDS; ++r) {
+    const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
+#pragma unroll
+    for (int j = 0; j < EDGE_VEC; ++j) {
+      const int64_t e = eb + j;
+      if (e >= e1) break;
+      int32_t a, b;
+      if (L->dynamic) {
+        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L->layer),
+                               sp.key0, sp.key1);
+        a = off + (int32_t)uniform_index(w.x, w.y, (uint64_t)sp.n_agents);
+        b = off + (int32_t)uniform_index(w.z, w.w, (uint64_t)sp.n_agents);
+      } else {
+        a = __ldg(L->p1 + e);
+        b = __ldg(L->p2 + e);
+      }
+      if (bit_of(st.trace_bits, a)) atomicOr(contact + (b >> 5), 1u << (b & 31));
+      if (bit_of(st.trace_bits, b)) atomicOr(contact + (a >> 5), 1u << (a & 31));
+    }
+  }
+}
+
+// contact_tracing.notify_contacts (interventions.py:1120-1145) with the
+// binomial_filter of identify_contacts, then update_states_post
+// (people.py:189-196: check_diagnosed, check_quar, check_enter_iso)
+__global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t words = (st.n + 31) >> 5;
+  const int64_t w = (blk.begin + warp * 32) >> 5;
+  const bool warp_in = blk.begin + warp * 32 < blk.end;
+  const float tf = (float)t;
+  const int R = st.pending_slots;
+  unsigned c_diag = 0, c_quar = 0, c_iso = 0;
+  uint32_t f = valid ? st.flags[i] : 0u;
+  const uint32_t f_in = f;
+
+  // ---- notify the contacts found by the scan (only on tracing days)
+  if (day_active(t, T.trace_start, T.trace_end) && warp_in) {
+    for (int l = 0; l < sp.n_layers; ++l) {
+      uint32_t* cw = st.contact_bits + (int64_t)l * words + w;
+      const uint32_t word = *cw;
+      __syncwarp();
+      if (!word) continue;
+      if (lane == 0) *cw = 0u;  // leave the bitmap clear for the next tracing day
+      if (!valid || !((word >> lane) & 1u)) continue;
+      const uint32_t local = (uint32_t)(i - sp.agent_off);
+      const uint4 u = philox(make_uint4(local, (uint32_t)l, (uint32_t)t, TAG_TRACE), sp.key0, sp.key1);
+      if (!bern52_thr(u.x, u.y, T.thr_trace[l]) || (f & B_DEAD)) continue;
+      f |= B_KCONT;
+      float* dkc = date_row(st, COVGPU_DATE_KNOWN_CONTACT) + i;
+      const float cand = __double2float_rn(__dadd_rn((double)t, T.trace_time[l]));
+      if (isnan(*dkc) || cand < *dkc) *dkc = cand;  // np.fmin
+      const int start = t + T.trace_start_off[l];
+      int32_t* pq = st.pending_quar + (int64_t)(start % R) * st.n + i;
+      const int32_t end = start + T.trace_period[l];
+      if (*pq < 0 || end > *pq) *pq = end;  // check_quar keeps the latest end of a day's requests
+    }
+  }
+
+  if (valid) {
+    // ---- check_diagnosed, people.py:315-332
+    float* dpt = date_row(st, COVGPU_DATE_POS_TEST) + i;
+    const float dd = date_row(st, COVGPU_DATE_DIAGNOSED)[i];
+    if (!(f & B_DIAG)) {
+      if (defined(*dpt) && tf >= *dpt) { *dpt = __int_as_float(0x7fc00000); c_diag = 1; }
+      if (defined(dd) && tf >= dd) f |= B_DIAG;
+    }
+    // ---- check_quar, people.py:335-358
+    int32_t* pq = st.pending_quar + (int64_t)(t % R) * st.n + i;
+    const int32_t end = *pq;
+    float* deq = date_row(st, COVGPU_DATE_END_QUARANTINE) + i;
+    if (end >= 0) {
+      *pq = -1;
+      if (f & B_QUAR) {
+        if ((float)end > *deq) *deq = (float)end;  // max(current, end_day), first argument kept on ties/NaN
+      } else if (!(f & (B_DEAD | B_REC | B_DIAG | B_ISO))) {
+        f |= B_QUAR;
+        date_row(st, COVGPU_DATE_QUARANTINED)[i] = tf;
+        *deq = (float)end;
+        c_quar = 1;
+      }
+    }
+    if ((f & B_QUAR) && dd == tf) *deq = tf;
+    if ((f & B_QUAR) && defined(*deq) && tf >= *deq) f &= ~B_QUAR;
+    // ---- check_enter_iso, people.py:361-366
+    if (dd == tf) {
+      f |= B_ISO;
+      date_row(st, COVGPU_DATE_END_ISOLATION)[i] = date_row(st, COVGPU_DATE_RECOVERED)[i];
+      c_iso = 1;
+    }
+    if (f != f_in) st.flags[i] = f;
+  }
+  const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
+                 ci = __reduce_add_sync(0xffffffffu, c_iso);
+  int64_t* res = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
+  if (lane == 0 && t < sp.npts) {
+    if (cd) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_DIAGNOSES), (unsigned long long)cd);
+    if (cq) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_QUARANTINED), (unsigned long long)cq);
+    if (ci) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_ISOLATED), (unsigned long long)ci);
+  }
+  // the day's trace count is read only by k_trace_scan, which has finished
+  if (threadIdx.x == 0 && blk.begin == sp.agent_off) st.trace_count[blk.sim] = 0u;
+}
+
+int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
+  if (!st->has_testing) return COVGPU_OK;
+  k_test_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  if (st->n_tiles > 0) k_trace_scan<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  return launch_status();
+}
+
 int grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
   int64_t b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -902,14 +1266,17 @@ struct GraphEntry {
   int t0 = 0, t1 = 0, open_prev = 0, close_last = 0;
   cudaGraphExec_t exec = nullptr;
 };
-GraphEntry g_graphs[8];
+constexpr int N_GRAPHS = 32;  // e.g. the checkpoint segments of a run, in value and gradient mode
+GraphEntry g_graphs[N_GRAPHS];
 int g_graph_next = 0;
 cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the legacy stream cannot capture)
 
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
+    launch_test_trace(st, t, s);
     launch_edge_pass(st, t, s);
+    launch_lik_pass(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
   if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0);
@@ -929,7 +1296,10 @@ int covgpu_abi_layout(int64_t* out, int32_t n) {
                        (int64_t)sizeof(covgpu_agent_block), (int64_t)sizeof(covgpu_event),
                        (int64_t)sizeof(covgpu_log_rec), (int64_t)sizeof(covgpu_state),
                        (int64_t)offsetof(covgpu_state, sims), (int64_t)offsetof(covgpu_state, edge_uniforms),
-                       (int64_t)offsetof(covgpu_sim_params, res_fx)};
+                       (int64_t)offsetof(covgpu_sim_params, res_fx), (int64_t)sizeof(covgpu_testing),
+                       (int64_t)offsetof(covgpu_sim_params, testing), (int64_t)offsetof(covgpu_state, pending_quar),
+                       (int64_t)offsetof(covgpu_state, trace_count), (int64_t)sizeof(covgpu_lik),
+                       (int64_t)offsetof(covgpu_state, lik)};
   const int m = (int)(sizeof(v) / sizeof(v[0]));
   for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
   return m;
@@ -1066,6 +1436,13 @@ static int check_state(const covgpu_state* st) {
   if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0))
     return COVGPU_BADARG;
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
+  if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
+                          st->pending_slots < 1 || st->n_contact_layers < 1))
+    return COVGPU_BADARG;
+  const covgpu_lik& K = st->lik;
+  if (K.factor && (!K.ll || !K.expected || !K.logq || (K.g_exp && !K.w) || K.npts_max < 1 ||
+                   K.n_layers_max < 1 || K.n_layers_max > COVGPU_MAX_LAYERS || K.nv_max < 1))
+    return COVGPU_BADARG;
   return COVGPU_OK;
 }
 
@@ -1082,6 +1459,20 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
   return launch_edge_pass(st, t, S(stream));
+}
+
+int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  return launch_test_trace(st, t, S(stream));
+}
+
+int covgpu_lik_pass(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF || !st->lik.factor) return COVGPU_BADARG;
+  return launch_lik_pass(st, t, S(stream));
 }
 
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream) {
@@ -1135,7 +1526,7 @@ int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open
       return COVGPU_CUDA_ERROR;
     }
     GraphEntry& g = g_graphs[g_graph_next];
-    g_graph_next = (g_graph_next + 1) % 8;
+    g_graph_next = (g_graph_next + 1) % N_GRAPHS;
     if (g.used && g.exec) cudaGraphExecDestroy(g.exec);
     g.used = false;
     if (cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) { cudaGraphDestroy(graph); return COVGPU_CUDA_ERROR; }

@@ -39,6 +39,7 @@ enum { RV_INFECTIONS = 0, RV_SYMPTOMATIC, RV_SEVERE, RV_INFECTIOUS, RV_N_EXPOSED
 constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
 constexpr uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
 constexpr uint32_t TAG_EDGE = 0x01000000u, TAG_LAYER = 0x02000000u, TAG_INFECT = 0x03000000u;
+constexpr uint32_t TAG_TEST = 0x04000000u, TAG_TRACE = 0x05000000u;
 
 __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll

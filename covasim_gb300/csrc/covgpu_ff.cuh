@@ -166,5 +166,10 @@ __device__ __forceinline__ bool bern52(uint32_t a, uint32_t b, float p) {
 __device__ __forceinline__ bool bern32(uint32_t a, float p) {
   return frac_less(2 * (uint64_t)a + 1, 33, p);
 }
+// u01_52(a, b) < p for a float64 p given as its threshold ceil(p * 2^53)
+__device__ __forceinline__ bool bern52_thr(uint32_t a, uint32_t b, uint64_t thr) {
+  const uint64_t k = ((uint64_t)(a >> 6) << 26) | (uint64_t)(b >> 6);
+  return 2 * k + 1 < thr;
+}
 
 }  // namespace covgpu

@@ -1,13 +1,22 @@
-"""Interventions that the GPU day loop consumes as per-day device tables.
+"""Interventions that the GPU day loop consumes as device tables.
 
 ``change_beta`` (covasim/interventions.py:530-586) changes the overall beta or a
 layer's beta from given days on. On the GPU path its effect is folded into the
 per-day beta tables before the run, so the whole day loop can be captured in a
 CUDA graph without a host round trip per day.
+
+``test_prob`` (interventions.py:858-981) and ``contact_tracing``
+(interventions.py:984-1145) become the sim's testing record: thresholds and
+day ranges that the testing, tracing and post passes of the library read
+every day, again with no host round trip.
 """
+import numbers
+
 import numpy as np
 
-__all__ = ['Intervention', 'change_beta']
+from . import _lib as L
+
+__all__ = ['Intervention', 'change_beta', 'test_prob', 'contact_tracing']
 
 
 class Intervention:
@@ -94,3 +103,142 @@ class change_beta(Intervention):
         self.apply_day(sim.t, betas)
         sim['beta'] = betas.pop('overall')
         sim['beta_layer'].update(betas)
+
+
+def _day(d, default):
+    """interventions.py:56-65 preprocess_day for integer days (None keeps the default)."""
+    if d is None:
+        return default
+    if callable(d) or isinstance(d, str):
+        raise NotImplementedError('intervention days must be integers on the GPU path')
+    return int(d)
+
+
+class test_prob(Intervention):
+    """Test each agent with a probability set by its symptom and quarantine state
+    (interventions.py:858-981). Same arguments as the reference; ``swab_delay``,
+    ``ili_prev`` and ``subtarget`` are not supported on the GPU path.
+    """
+
+    def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
+                 subtarget=None, ili_prev=None, sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0,
+                 end_day=None, swab_delay=None, **kwargs):
+        super().__init__(**kwargs)
+        self.symp_prob = symp_prob
+        self.asymp_prob = asymp_prob
+        self.symp_quar_prob = symp_quar_prob if symp_quar_prob is not None else symp_prob
+        self.asymp_quar_prob = asymp_quar_prob if asymp_quar_prob is not None else asymp_prob
+        self.quar_policy = quar_policy if quar_policy else 'start'
+        self.subtarget = subtarget
+        self.ili_prev = ili_prev
+        self.sensitivity = sensitivity
+        self.loss_prob = loss_prob
+        self.test_delay = test_delay
+        self.start_day = start_day
+        self.end_day = end_day
+        self.swab_delay = swab_delay
+
+    def initialize(self, sim):
+        super().initialize()
+        for name in ('subtarget', 'ili_prev', 'swab_delay'):
+            if getattr(self, name) is not None:
+                raise NotImplementedError(f'test_prob({name}=...) is not supported on the GPU path')
+        self.start_day = _day(self.start_day, 0)
+        self.end_day = _day(self.end_day, None)
+        self.days = [self.start_day, self.end_day]
+
+    @staticmethod
+    def _quar_policy(qp):
+        """interventions.py:682-710 -> (COVGPU_QP_* bits, offset bits)."""
+        named = {'start': L.QP_START, 'end': L.QP_END, 'both': L.QP_START | L.QP_END, 'daily': L.QP_DAILY}
+        if qp is None:
+            return 0, 0
+        if isinstance(qp, str):
+            if qp not in named:
+                raise ValueError(f'Quarantine policy "{qp}" not recognized')
+            return named[qp], 0
+        if callable(qp):
+            raise NotImplementedError('function quarantine policies are not supported on the GPU path')
+        offs = 0
+        for q in np.atleast_1d(qp):
+            if float(q) != int(q) or not 0 <= int(q) < 32:
+                raise NotImplementedError('numeric quarantine policies must be integers in [0, 32)')
+            offs |= 1 << int(q)
+        return L.QP_OFFSETS, offs
+
+    def device_testing(self):
+        qp, offs = self._quar_policy(self.quar_policy)
+        if float(self.test_delay) != int(self.test_delay):
+            raise NotImplementedError('test_delay must be a whole number of days on the GPU path')
+        return dict(start_day=self.start_day, end_day=0xFFFE if self.end_day is None else self.end_day,
+                    quar_policy=qp, quar_offsets=offs, symp_prob=float(self.symp_prob),
+                    asymp_prob=float(self.asymp_prob), symp_quar_prob=float(self.symp_quar_prob),
+                    asymp_quar_prob=float(self.asymp_quar_prob), sensitivity=float(self.sensitivity),
+                    loss_prob=float(self.loss_prob), test_delay=int(self.test_delay))
+
+    def apply(self, sim):
+        raise NotImplementedError('test_prob runs on the device as part of the day loop')
+
+
+class contact_tracing(Intervention):
+    """Trace the contacts of the diagnosed (interventions.py:984-1145). Same
+    arguments as the reference; ``capacity`` is not supported on the GPU path.
+    """
+
+    def __init__(self, trace_probs=None, trace_time=None, start_day=0, end_day=None, presumptive=False,
+                 quar_period=None, capacity=None, **kwargs):
+        super().__init__(**kwargs)
+        self.trace_probs = trace_probs
+        self.trace_time = trace_time
+        self.start_day = start_day
+        self.end_day = end_day
+        self.presumptive = presumptive
+        self.capacity = capacity
+        self.quar_period = quar_period
+
+    def initialize(self, sim):
+        """interventions.py:1023-1041."""
+        super().initialize()
+        if self.capacity is not None:
+            raise NotImplementedError('contact_tracing(capacity=...) is not supported on the GPU path')
+        self.start_day = _day(self.start_day, 0)
+        self.end_day = _day(self.end_day, None)
+        self.days = [self.start_day, self.end_day]
+        if self.trace_probs is None:
+            self.trace_probs = 1.0
+        if self.trace_time is None:
+            self.trace_time = 0.0
+        if self.quar_period is None:
+            self.quar_period = sim['quar_period']
+        keys = sim.layer_keys()
+        if isinstance(self.trace_probs, numbers.Number):
+            self.trace_probs = {k: self.trace_probs for k in keys}
+        if isinstance(self.trace_time, numbers.Number):
+            self.trace_time = {k: self.trace_time for k in keys}
+
+    def device_testing(self):
+        return dict(start_day=self.start_day, end_day=0xFFFE if self.end_day is None else self.end_day,
+                    presumptive=bool(self.presumptive), trace_probs=dict(self.trace_probs),
+                    trace_time=dict(self.trace_time), quar_period=self.quar_period)
+
+    def apply(self, sim):
+        raise NotImplementedError('contact_tracing runs on the device as part of the day loop')
+
+
+def device_testing(interventions):
+    """The sim's testing record from its interventions (None without testing)."""
+    test = trace = None
+    for iv in interventions or []:
+        if isinstance(iv, test_prob):
+            if test is not None:
+                raise NotImplementedError('one test_prob per sim is supported on the GPU path')
+            test = iv.device_testing()
+        elif isinstance(iv, contact_tracing):
+            if trace is not None:
+                raise NotImplementedError('one contact_tracing per sim is supported on the GPU path')
+            if test is None and any(isinstance(j, test_prob) for j in interventions):
+                raise NotImplementedError('contact_tracing must follow test_prob in the interventions list')
+            trace = iv.device_testing()
+    if test is None and trace is None:
+        return None
+    return {'test': test, 'trace': trace}

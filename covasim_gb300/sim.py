@@ -109,10 +109,12 @@ def build_spec(pars, popdict=None, person=None, interventions=None):
     bl_sched = np.zeros((npts, len(keys)))
     for t in range(npts):
         for iv in interventions or []:
-            iv.apply_day(t, betas)
+            if hasattr(iv, 'apply_day'):
+                iv.apply_day(t, betas)
         beta_sched[t] = betas['overall']
         bl_sched[t] = [betas[k] for k in keys]
-    return SimSpec(pars, person, layers, beta_sched, bl_sched), popdict, person
+    testing = cvi.device_testing(interventions)
+    return SimSpec(pars, person, layers, beta_sched, bl_sched, testing=testing), popdict, person
 
 
 class Sim:
@@ -209,7 +211,7 @@ class Sim:
         for iv in self['interventions']:
             if isinstance(iv, cvi.Intervention):
                 iv.initialize(self)
-                if not hasattr(iv, 'apply_day'):
+                if not (hasattr(iv, 'apply_day') or hasattr(iv, 'device_testing')):
                     raise NotImplementedError(f'intervention {type(iv).__name__} is not supported on the GPU path yet')
             elif callable(iv):
                 raise NotImplementedError('function interventions are not supported on the GPU path yet')
@@ -304,6 +306,7 @@ class Sim:
         self.people.__dict__['t'] = t
         self.state.agent_step(t, do_prev=self._open_day is not None, do_day=True)
         self._apply_variants(t)
+        self.state.test_trace(t)  # sim.py:596-600 interventions after importations, then update_states_post
         self.state.edge_pass(t)
         self.state.infect_claims(t)
         self.state.agent_step(t + 1, do_prev=True, do_day=False)

@@ -82,9 +82,11 @@ class SimSpec:
         layers: list of dicts(key, p1, p2, beta, dynamic) in layer order
         beta_sched: float64 [npts] overall beta per day (change_beta applied)
         beta_layer_sched: float64 [npts, n_layers] per-layer beta per day
+        testing: test_prob / contact_tracing settings (``interventions.device_testing``) or None
     """
 
-    def __init__(self, pars, person, layers, beta_sched=None, beta_layer_sched=None):
+    def __init__(self, pars, person, layers, beta_sched=None, beta_layer_sched=None, testing=None):
+        self.testing = testing  # dict from the test_prob / contact_tracing interventions, or None
         self.pars = pars
         self.person = person
         self.layers = layers
@@ -111,6 +113,48 @@ class SimSpec:
             rb = p['variant_pars'][label]['rel_beta']
             tab[:, v] = [np.float32(b * p['rel_beta'] * rb) for b in self.beta_sched]
         return tab
+
+
+def prob_threshold(p):
+    """ceil(p * 2^53) as an exact integer: the device's test 2k + 1 < threshold on
+    the 52 random bits k of a uniform (2k + 1) / 2^53 is float64's u < p."""
+    p = float(p)
+    if not p > 0.0:
+        return 0
+    if p >= 1.0:
+        return (1 << 53) + 1
+    num, den = p.as_integer_ratio()
+    return -((-num << 53) // den)
+
+
+def testing_record(spec):
+    """covgpu_testing of one sim (both interventions off when ``spec.testing`` is None)."""
+    r = L.Testing()
+    r.test_start, r.test_end, r.trace_start, r.trace_end = 1, 0, 1, 0
+    T = spec.testing
+    if not T:
+        return r
+    keys = [ly['key'] for ly in spec.layers]
+    if T.get('test') is not None:
+        tp = T['test']
+        r.test_start, r.test_end = tp['start_day'], tp['end_day']
+        r.quar_policy, r.quar_offsets = tp['quar_policy'], tp['quar_offsets']
+        r.thr_symp, r.thr_asymp = prob_threshold(tp['symp_prob']), prob_threshold(tp['asymp_prob'])
+        r.thr_symp_quar, r.thr_asymp_quar = prob_threshold(tp['symp_quar_prob']), prob_threshold(tp['asymp_quar_prob'])
+        r.thr_sensitivity = prob_threshold(tp['sensitivity'])
+        r.thr_not_lost = prob_threshold(1.0 - tp['loss_prob'])  # people.py:611 n_binomial(1.0 - loss_prob, ...)
+        r.test_delay = tp['test_delay']
+    if T.get('trace') is not None:
+        ct = T['trace']
+        r.trace_start, r.trace_end = ct['start_day'], ct['end_day']
+        r.presumptive = int(ct['presumptive'])
+        for li, k in enumerate(keys):
+            prob, tt = ct['trace_probs'].get(k, 0.0), float(ct['trace_time'].get(k, 0.0))
+            r.thr_trace[li] = 0 if prob == 0 else prob_threshold(prob)  # interventions.py:1103 skips prob == 0
+            r.trace_time[li] = tt
+            r.trace_start_off[li] = int(tt)                        # people.py:635 int(t + trace_time)
+            r.trace_period[li] = int(ct['quar_period'] - tt)       # people.py:636 int(quar_period - trace_time)
+    return r
 
 
 class BatchState:
@@ -155,6 +199,22 @@ class BatchState:
         t['log'] = torch.zeros((max(self.log_capacity, 1), 4), dtype=I32, device=dev)
         t['log_count'] = torch.zeros(1, dtype=I64, device=dev)
         t['status'] = torch.zeros(1, dtype=I32, device=dev)
+        # testing and tracing (interventions.py:858-1145): bitmaps, scheduled quarantines
+        self.testing_recs = [testing_record(sp) for sp in self.specs]
+        self.has_testing = any(sp.testing for sp in self.specs)
+        self.pending_slots = 1
+        self.n_contact_layers = max(len(sp.layers) for sp in self.specs) or 1
+        if self.has_testing:
+            for r, sp in zip(self.testing_recs, self.specs):
+                offs_used = [r.trace_start_off[li] for li in range(len(sp.layers)) if r.thr_trace[li]]
+                if min(offs_used, default=0) < 0:
+                    raise ValueError('contact_tracing trace_time must not be negative')
+                self.pending_slots = max(self.pending_slots, max(offs_used, default=0) + 1)
+            words = (n + 31) // 32
+            t['trace_bits'] = torch.zeros(words, dtype=I32, device=dev)
+            t['contact_bits'] = torch.zeros(self.n_contact_layers * words, dtype=I32, device=dev)
+            t['pending_quar'] = torch.full((self.pending_slots, n), -1, dtype=I32, device=dev)
+            t['trace_count'] = torch.zeros(S, dtype=I32, device=dev)
         self.t = t
 
         # per-sim tables, concatenated
@@ -181,6 +241,7 @@ class BatchState:
         self.draw_table = None
         self.edge_uniform_tensors = None
         self.hospicu = None
+        self.lik = None
         self._refresh_state()
 
     # ------------------------------------------------------------------ building
@@ -335,6 +396,7 @@ class BatchState:
             r.res_int = self.res_int.data_ptr() + 8 * ri
             r.res_var = self.res_var.data_ptr() + 8 * rv
             r.res_fx = self.res_fx.data_ptr() + 8 * rf
+            r.testing = self.testing_recs[s]
             self.res_slices.append((ri, rv, rf))
             ri += sp.npts * L.N_RES_INT
             rv += sp.npts * L.N_RES_VAR * sp.nv
@@ -383,12 +445,28 @@ class BatchState:
         st.segments = self.seg_dev.data_ptr() if self.segments else None
         st.agent_blocks = self.blocks_dev.data_ptr()
         st.draw_table = self.draw_table.data_ptr() if self.draw_table is not None else None
+        st.has_testing = int(self.has_testing)
+        st.pending_slots = self.pending_slots
+        st.n_contact_layers = self.n_contact_layers
+        if self.has_testing:
+            for k in ('trace_bits', 'contact_bits', 'pending_quar', 'trace_count'):
+                setattr(st, k, t[k].data_ptr())
         if self.edge_uniform_tensors is not None:
             ptrs = np.array([u.data_ptr() for u in self.edge_uniform_tensors], dtype=np.uint64)
             self._eu_ptrs = torch.from_numpy(ptrs.view(np.int64)).to(self.device)
             st.edge_uniforms = self._eu_ptrs.data_ptr()
         else:
             st.edge_uniforms = None
+        if self.lik is not None:
+            k = self.lik
+            st.lik.factor = k['factor'].data_ptr()
+            st.lik.ll = k['ll'].data_ptr()
+            st.lik.expected = k['expected'].data_ptr()
+            st.lik.g_ll = k['g_ll'].data_ptr() if k['grad'] else None
+            st.lik.g_exp = k['g_exp'].data_ptr() if k['grad'] else None
+            st.lik.logq = k['logq'].data_ptr()
+            st.lik.w = k['w'].data_ptr()
+            st.lik.npts_max, st.lik.n_layers_max, st.lik.nv_max = k['dims']
         self.cstate = st
         self.cstate_ptr = C.pointer(self.cstate)
 
@@ -414,6 +492,59 @@ class BatchState:
                                                                   device=self.device)
         self._refresh_state()
 
+    # ------------------------------------------------------------------ likelihood
+    def enable_lik(self, grad=False):
+        """Allocate the likelihood buffers (covgpu_lik) and switch the passes on.
+        With ``grad`` the per-layer sensitivities are accumulated too."""
+        if self.lik is None:
+            S = len(self.specs)
+            T = max(sp.npts for sp in self.specs)
+            Lm = max(len(sp.layers) for sp in self.specs) or 1
+            V = self.nv_max
+            dev = self.device
+            f64 = torch.float64
+            self.lik = dict(dims=(T, Lm, V), grad=False,
+                            factor=torch.zeros((S, T, Lm, V), dtype=f64, device=dev),
+                            ll=torch.zeros((S, T), dtype=f64, device=dev),
+                            expected=torch.zeros((S, T), dtype=f64, device=dev),
+                            g_ll=torch.zeros((S, T, Lm), dtype=f64, device=dev),
+                            g_exp=torch.zeros((S, T, Lm), dtype=f64, device=dev),
+                            logq=torch.zeros(self.n, dtype=f64, device=dev),
+                            w=torch.zeros((Lm, self.n), dtype=f64, device=dev))
+        self.lik['grad'] = bool(grad)
+        self._refresh_state()
+
+    def disable_lik(self):
+        self.lik = None
+        self._refresh_state()
+
+    def set_lik_factor(self, factor, sim=0):
+        """F[t][layer][variant] of one sim (float64, see covgpu_lik)."""
+        f = torch.as_tensor(np.asarray(factor, dtype=np.float64))
+        T, Lm, V = f.shape
+        self.lik['factor'][sim].zero_()
+        self.lik['factor'][sim, :T, :Lm, :V].copy_(f)
+
+    def zero_lik(self):
+        for k in ('ll', 'expected', 'g_ll', 'g_exp', 'logq', 'w'):
+            self.lik[k].zero_()
+
+    def lik_pass(self, t):
+        L.call('covgpu_lik_pass', self.cstate_ptr, int(t), _stream())
+
+    def set_beta_tables(self, beta_sched, beta_layer_sched, sim=0):
+        """Overwrite one sim's per-day beta tables in place (float64 schedules,
+        rounded as at initialisation); captured graphs read the new values."""
+        spec = self.specs[sim]
+        spec.beta_sched = np.asarray(beta_sched, dtype=np.float64)
+        spec.beta_layer_sched = np.asarray(beta_layer_sched, dtype=np.float64).reshape(spec.npts, len(spec.layers))
+        bt = torch.from_numpy(spec.beta_table().ravel())
+        bl = torch.from_numpy(spec.beta_layer_sched.astype(np.float32).ravel())
+        b0 = sum(s.npts * s.nv for s in self.specs[:sim])
+        l0 = sum(s.npts * len(s.layers) for s in self.specs[:sim])
+        self.beta_tab[b0:b0 + bt.numel()].copy_(bt)
+        self.beta_layer_tab[l0:l0 + bl.numel()].copy_(bl)
+
     # ------------------------------------------------------------------ kernels
     def agent_step(self, t, do_prev=True, do_day=True):
         L.call('covgpu_agent_step', self.cstate_ptr, int(t), int(do_prev), int(do_day), _stream())
@@ -423,6 +554,10 @@ class BatchState:
 
     def infect_claims(self, t):
         L.call('covgpu_infect_claims', self.cstate_ptr, int(t), _stream())
+
+    def test_trace(self, t):
+        """Day t's testing, tracing and update_states_post (no-op without testing)."""
+        L.call('covgpu_test_trace', self.cstate_ptr, int(t), _stream())
 
     def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=1):
         """Infect explicit agents of one sim (local indices; deduplicated and sorted here)."""
@@ -456,7 +591,8 @@ class BatchState:
 
     def snapshot(self):
         """Device copy of every array a run modifies (restore() rewinds to it)."""
-        return {k: self.t[k].clone() for k in self.MUTABLE}
+        keys = self.MUTABLE + (('pending_quar',) if self.has_testing else ())
+        return {k: self.t[k].clone() for k in keys}
 
     def restore(self, snap):
         """Rewind to a snapshot: agent arrays, results, claims, counters and status."""
@@ -471,6 +607,31 @@ class BatchState:
         self.t['event_count'].zero_()
         self.t['log_count'].zero_()
         self.t['status'].zero_()
+        if self.has_testing:
+            for k in ('trace_bits', 'contact_bits', 'trace_count'):
+                self.t[k].zero_()
+
+    def checkpoint(self):
+        """Device copy of the state at a day boundary (with the results so far),
+        for ``rewind``: recomputing from it reproduces the run exactly."""
+        keys = self.MUTABLE + (('pending_quar',) if self.has_testing else ()) + ('log_count',)
+        ck = {k: self.t[k].clone() for k in keys}
+        ck['_res'] = (self.res_int.clone(), self.res_var.clone(), self.res_fx.clone())
+        return ck
+
+    def rewind(self, ck):
+        """Return to a checkpoint (day-local buffers cleared, claims reset)."""
+        for k, v in ck.items():
+            if k != '_res':
+                self.t[k].copy_(v)
+        for dst, src in zip((self.res_int, self.res_var, self.res_fx), ck['_res']):
+            dst.copy_(src)
+        self.t['claim'].fill_(-1)
+        self.t['event_count'].zero_()
+        self.t['status'].zero_()
+        if self.has_testing:
+            for k in ('trace_bits', 'contact_bits', 'trace_count'):
+                self.t[k].zero_()
 
     def status(self):
         return int(self.t['status'].item())

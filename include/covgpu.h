@@ -96,6 +96,34 @@ enum { COVGPU_D_EXP2INF = 0, COVGPU_D_INF2SYM, COVGPU_D_SYM2SEV, COVGPU_D_SEV2CR
 /* ---- device-side descriptors ------------------------------------------- */
 typedef struct covgpu_dur_par { int32_t code; int32_t _pad; double a; double b; } covgpu_dur_par;
 
+/* quar_policy of test_prob (interventions.py:682-710): who counts as a
+ * quarantined tester on day t */
+#define COVGPU_QP_START 1    /* date_quarantined == t - 1   */
+#define COVGPU_QP_END 2      /* date_end_quarantine == t + 1 */
+#define COVGPU_QP_DAILY 4    /* quarantined                 */
+#define COVGPU_QP_OFFSETS 8  /* date_quarantined == t - 1 - q for every bit q of quar_offsets */
+
+/* One sim's test_prob (interventions.py:858-981) and contact_tracing
+ * (interventions.py:984-1145). Days are inclusive ranges; an empty range
+ * (start > end) switches the intervention off. Probabilities p are passed as
+ * thresholds ceil(p * 2^53): a Philox uniform u = (2k + 1) / 2^53 satisfies
+ * u < p exactly when 2k + 1 < threshold, which is float64's u < p. */
+typedef struct covgpu_testing {
+  int32_t test_start, test_end;
+  int32_t quar_policy;            /* COVGPU_QP_* bits                                 */
+  uint32_t quar_offsets;
+  uint64_t thr_symp, thr_asymp, thr_symp_quar, thr_asymp_quar;
+  uint64_t thr_sensitivity;       /* test_sensitivity                                 */
+  uint64_t thr_not_lost;          /* 1 - loss_prob                                    */
+  int32_t test_delay;
+  int32_t trace_start, trace_end;
+  int32_t presumptive;            /* trace the exposed tested today, not the diagnosed */
+  double trace_time[COVGPU_MAX_LAYERS];        /* days from diagnosis to notification */
+  uint64_t thr_trace[COVGPU_MAX_LAYERS];       /* per-layer trace_probs; 0: not traced */
+  int32_t trace_start_off[COVGPU_MAX_LAYERS];  /* int(trace_time): quarantine start offset */
+  int32_t trace_period[COVGPU_MAX_LAYERS];     /* int(quar_period - trace_time)        */
+} covgpu_testing;
+
 /* One sim's parameter block (device memory, one entry per sim). */
 typedef struct covgpu_sim_params {
   int64_t agent_off;          /* first global agent index (multiple of 32)          */
@@ -130,6 +158,7 @@ typedef struct covgpu_sim_params {
   int64_t* res_int;               /* [npts][COVGPU_N_RES_INT]                        */
   int64_t* res_var;               /* [npts][COVGPU_N_RES_VAR][n_variants]            */
   int64_t* res_fx;                /* [npts][COVGPU_N_RES_F] fixed-point sums         */
+  covgpu_testing testing;
 } covgpu_sim_params;
 
 /* One contact layer of one sim (device memory, one entry per layer segment). */
@@ -156,6 +185,33 @@ typedef struct covgpu_event { uint64_t key; int32_t target; int32_t source; } co
 /* One infection-log record (people.py:508-511): local source (-1 for seed
  * infections and importations) and target, day, and layer | variant << 8 | sim << 16. */
 typedef struct covgpu_log_rec { int32_t source; int32_t target; int32_t day; int32_t layer_variant; } covgpu_log_rec;
+
+/* Transmission log-likelihood and expected infections of each day, with
+ * their sensitivities (all device pointers; factor == NULL switches the
+ * likelihood passes off). Every exposed direction source -> target of day t
+ * (the candidates of the edge pass) has
+ *   p = F[t][layer][variant] * edge beta * rel_trans' * rel_sus'
+ * in float64, with rel_trans' = rel_trans * quar/asymp/iso factors * viral
+ * load and rel_sus' = rel_sus * quar factor * (1 - sus_imm) as in
+ * compute_trans_sus (utils.py:82-90) but without beta_layer, which F holds
+ * together with beta, rel_beta and the variant's rel_beta. Its outcome is
+ * the edge pass's own Bernoulli draw. Per sim and day:
+ *   ll       = sum over infecting directions of log p + over the others of log(1 - p)
+ *   expected = sum over targets of 1 - prod over their directions of (1 - p)
+ * and per layer the derivatives with respect to log F[t][layer][*]:
+ *   g_ll     = sum of (infecting ? 1 : -p / (1 - p))
+ *   g_exp    = sum over targets of prod(1 - p) * sum over the layer's directions of p / (1 - p). */
+typedef struct covgpu_lik {
+  const double* factor;           /* [n_sims][npts_max][n_layers_max][nv_max]       */
+  double* ll;                     /* [n_sims][npts_max]                             */
+  double* expected;               /* [n_sims][npts_max]                             */
+  double* g_ll;                   /* [n_sims][npts_max][n_layers_max] or NULL       */
+  double* g_exp;                  /* [n_sims][npts_max][n_layers_max] or NULL       */
+  double* logq;                   /* [n] zero between days (the agent pass of the
+                                     likelihood clears what it reads)               */
+  double* w;                      /* [n_layers_max][n], zero; needed with g_exp     */
+  int32_t npts_max, n_layers_max, nv_max, _pad;
+} covgpu_lik;
 
 /* Everything the fused kernels touch. Host struct; the library copies it into
  * kernel parameters. All pointers are device pointers. */
@@ -200,6 +256,18 @@ typedef struct covgpu_state {
    * table indexed by (source variant, direction, edge) */
   const double* draw_table;
   const double* const* edge_uniforms; /* [n_segments] -> [n_variants][2][n_edges] */
+  /* testing and tracing (all NULL / 0 when no sim tests) */
+  int32_t has_testing;            /* 1: run the testing, tracing and post passes     */
+  int32_t pending_slots;          /* R: days of scheduled quarantines kept ahead     */
+  uint32_t* trace_bits;           /* [ceil(n/32)] agents traced today                */
+  uint32_t* contact_bits;         /* [n_contact_layers][ceil(n/32)] contacts found   */
+  int32_t n_contact_layers;       /* max layers over sims                            */
+  int32_t _pad1;
+  int32_t* pending_quar;          /* [R][n] end day of a quarantine starting on day
+                                     s (slot s mod R), -1: none                      */
+  uint32_t* trace_count;          /* [n_sims] agents traced today                    */
+  covgpu_lik lik;                 /* likelihood passes after each edge pass (factor
+                                     NULL: off)                                      */
 } covgpu_state;
 
 /* ---- standalone kernels: the reference's numba functions ----------------- */
@@ -271,6 +339,21 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
  * claimed with a 64-bit atomicMin on (day, variant, layer, direction, edge). */
 int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream);
 
+/* The testing and tracing interventions of day t, after the agent pass and
+ * any importations, before transmission (sim.py:596-600): test_prob's
+ * Bernoulli draws and People.test (interventions.py:921-981,
+ * people.py:589-617), contact_tracing's case selection, find_contacts over
+ * every layer, binomial_filter and notify (interventions.py:1044-1145,
+ * utils.py:131-147), then update_states_post: check_diagnosed, check_quar
+ * with the scheduled quarantines, check_enter_iso (people.py:189-196,
+ * 315-366). A no-op when st->has_testing is 0. */
+int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream);
+
+/* The likelihood passes of day t (see covgpu_lik): after covgpu_edge_pass
+ * and before covgpu_infect_claims of that day, so that they see the state
+ * the transmission draws saw. BADARG when st->lik.factor is NULL. */
+int covgpu_lik_pass(const covgpu_state* st, int32_t t, void* stream);
+
 /* infect() for the winning event of each target. */
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
 
@@ -287,7 +370,8 @@ int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, i
 int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t, int32_t* p1, int32_t* p2,
                              void* stream);
 
-/* Run days [t0, t1) of every sim: per day agent_step, edge_pass,
+/* Run days [t0, t1) of every sim: per day agent_step, test_trace (when
+ * st->has_testing), edge_pass, lik_pass (when st->lik.factor is set),
  * infect_claims. open_prev: day t0-1 still needs its closing pass (stocks,
  * update_nab), which day t0's agent pass then does first; close_last: end
  * with the closing pass of day t1-1. With use_graph the whole sequence is

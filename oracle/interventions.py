@@ -49,6 +49,8 @@ def _active(t, start_day, end_day):
 class TestProb:
     """interventions.py:858-981 (swab_delay, ili_prev and subtarget unsupported)."""
 
+    __test__ = False  # not a pytest test class
+
     def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
                  sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0, end_day=None):
         self.symp_prob = symp_prob

@@ -1,0 +1,79 @@
+"""test_prob, contact_tracing and update_states_post on the GPU against the
+oracle run with the same Philox draws (interventions.py:858-1145,
+people.py:189-196,315-366,589-640), step mode against the graph run, and a
+batch against its single runs."""
+import copy
+
+import numpy as np
+import pytest
+
+import covasim_gb300 as cv
+from oracle.interventions import TestProb, ContactTracing
+from test_gpu_sim import RES_KEYS, compare_runs, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+TESTING_KEYS = RES_KEYS + ['new_tests', 'new_diagnoses', 'new_quarantined', 'new_isolated', 'n_diagnosed',
+                           'n_quarantined', 'n_isolated']
+
+CASES = [
+    ('hybrid', 3000, 50, 1, True, True, dict(symp_prob=0.2, asymp_prob=0.01), dict(trace_probs=0.5, trace_time=1)),
+    ('hybrid', 2500, 45, 2, True, False,
+     dict(symp_prob=0.3, asymp_prob=0.02, symp_quar_prob=0.5, asymp_quar_prob=0.1, quar_policy='both',
+          sensitivity=0.9, loss_prob=0.1, test_delay=2),
+     dict(trace_probs={'h': 1.0, 's': 0.5, 'w': 0.5, 'c': 0.2}, trace_time={'h': 0, 's': 1, 'w': 2, 'c': 3})),
+    ('random', 3000, 45, 3, True, False, dict(symp_prob=0.3, quar_policy='daily', start_day=5, end_day=30),
+     dict(trace_probs=0.8, presumptive=True, start_day=8)),
+    ('hybrid', 2000, 40, 4, False, True, dict(symp_prob=0.3, quar_policy=[0, 2]),
+     dict(trace_probs=0.7, trace_time=0.5, quar_period=10)),
+]
+
+
+def make_sim(pop_type, n, days, seed, waning, dyn, tp, ct):
+    pars = dict(pop_type=pop_type, pop_size=n, n_days=days, rand_seed=seed, pop_infected=30, use_waning=waning,
+                interventions=[cv.test_prob(**tp), cv.contact_tracing(**ct)])
+    if dyn:
+        pars['dynam_layer'] = dict(h=0, s=0, w=0, c=1)
+    return cv.Sim(pars)
+
+
+@pytest.mark.parametrize('case', range(len(CASES)))
+def test_testing_and_tracing_match_oracle_philox(case):
+    pop_type, n, days, seed, waning, dyn, tp, ct = CASES[case]
+    sim = make_sim(*CASES[case])
+    sim.initialize()
+    orc = oracle_for(sim)
+    orc.interventions = [TestProb(**tp), ContactTracing(**ct)]
+    for iv in orc.interventions:
+        if hasattr(iv, 'initialize'):
+            iv.initialize(orc)
+    orc.run()
+    sim.run()
+    raw = sim.raw_results()
+    assert raw['new_tests'].sum() > 0 and raw['new_diagnoses'].sum() > 0 and raw['new_quarantined'].sum() > 0
+    compare_runs(sim, orc, keys=TESTING_KEYS)
+
+
+def test_testing_step_mode_equals_graph_run():
+    args = CASES[1]
+    a = make_sim(*args).run()
+    b = make_sim(*args)
+    b.initialize()
+    for _ in range(b.npts):
+        b.step()
+    b.finalize()
+    ra, rb = a.raw_results(), b.raw_results()
+    for k in TESTING_KEYS:
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+
+
+def test_testing_batch_equals_single_runs():
+    sims = [make_sim(*c) for c in CASES[:2]] + [cv.Sim(pop_type='random', pop_size=2000, n_days=50, rand_seed=9)]
+    sims[1].pars['n_days'] = sims[2].pars['n_days'] = sims[0].pars['n_days']
+    singles = [cv.Sim(copy.deepcopy(s.pars)).run() for s in sims]
+    batch = cv.BatchSim([cv.Sim(copy.deepcopy(s.pars)) for s in sims]).run()
+    for k, single in enumerate(singles):
+        raw = single.raw_results()
+        got = batch.results(k)
+        for key in TESTING_KEYS:
+            np.testing.assert_array_equal(got[key], raw[key], err_msg=f'sim {k} {key}')
