@@ -55,6 +55,11 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--batch', type=int, default=16, help='sims of the batched measurement (0: skip)')
+    ap.add_argument('--no-adjoint', action='store_true', help='skip the forward/adjoint cost measurement')
+    ap.add_argument('--edge-tile', default='auto', help="edge-pass tile (1024/2048/4096/8192) or 'auto' (autotuner)")
+    ap.add_argument('--workload', default='hybrid1m', choices=['hybrid1m', 'large', 'batch256'],
+                    help='hybrid1m: the headline run; large: 20M-agent hybrid, 3 variants, testing and tracing, '
+                         '365 days; batch256: 256 random-population sims of 10k-500k agents, batched vs one by one')
     ap.add_argument('--json-out', default=None)
     ap.add_argument('--profile-run', action='store_true',
                     help='run one sim of --pop-size agents for --days days, one launch per kernel (no graph), '
@@ -229,6 +234,12 @@ def gpu_arm(args, world, rank):
     init_s = time.perf_counter() - t0
     st = sim.state
     npts = sim.npts
+    tile_ms = None
+    if args.edge_tile == 'auto':  # before the snapshot: tuning leaves the state rewound
+        from covasim_gb300.autotune import tune_edge_tile
+        _, tile_ms = tune_edge_tile(st)
+    else:
+        st.set_edge_tile(int(args.edge_tile))
     snap = st.snapshot()
     seeds = choose_seed_infections(sim['rand_seed'], sim['pop_size'], sim['pop_infected'])
 
@@ -305,7 +316,7 @@ def gpu_arm(args, world, rank):
         d2h = 0
 
         def e2e_step():
-            s = cv.Sim(sim_pars(args, seed), popdict=host_pop, person=host_person)
+            s = cv.Sim(sim_pars(args, seed), popdict=host_pop, person=host_person, edge_tile=st.edge_tile)
             s.run()
             return s
 
@@ -325,10 +336,64 @@ def gpu_arm(args, world, rank):
         assert s.results['cum_infections'].values[-1] > 100
 
     batched = batched_arm(args, sim, value, world) if args.batch else None
+    adjoint = adjoint_arm(args) if not args.no_adjoint else None
 
-    return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched,
+    return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched, adjoint=adjoint,
+                edge_tile=st.edge_tile, tile_ms=tile_ms,
                 launches=launches_per_step * args.steps, init_s=init_s, res=res, spec=sim.spec,
                 cum_infections=float(res['new_infections'].sum() + sim['pop_infected']))
+
+
+def adjoint_arm(args, n=100_000, days=120, every=10, reps=3):
+    """Forward and forward + adjoint cost on the differentiable workload: a
+    100,000-agent hybrid sim, 120 days, change_beta on days 30 and 60, gradients
+    with respect to beta, the 4 layer betas and the 2 multipliers, a state
+    checkpoint every 10 days. The forward runs the sim with the likelihood
+    passes; the adjoint rewinds to each checkpoint and recomputes its days with
+    the gradient accumulators. Wall-clock with device synchronisation."""
+    import torch
+    import covasim_gb300 as cv
+    from covasim_gb300.adjoint import LikelihoodRun
+    pars = dict(pop_size=n, pop_type='hybrid', pop_infected=100, use_waning=True, n_days=days, rand_seed=1,
+                dynam_layer=dict(h=0, s=0, w=0, c=1), interventions=[cv.change_beta(days=[30, 60], changes=[0.7, 0.9])])
+    sim = cv.Sim(pars)
+    sim.initialize()
+    run = LikelihoodRun(sim, checkpoint_every=every)
+    th = run.params.theta0
+    g_exp = np.ones(run.npts)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def plain():
+        st = run.state
+        st.disable_lik()
+        st.restore(run.initial)
+        st.infect_list(0, run.seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.run_days(0, run.npts, open_prev=False, close_last=True, use_graph=True)
+        torch.cuda.synchronize()
+
+    from covasim_gb300 import _lib as L
+    from covasim_gb300.sim import CALL_SEED
+    for _ in range(2):  # warm-up: graph captures of every segment in both modes
+        plain()
+        run.forward(th)
+        run.backward(1.0, g_exp)
+    t_plain = timed(plain)
+    t_fwd = timed(lambda: run.forward(th))
+    t_both = timed(lambda: (run.forward(th), run.backward(1.0, g_exp)))
+    grad = run.backward(1.0, g_exp)
+    return {'workload': f'hybrid {n} agents, {days} days, change_beta days 30/60, {len(th)} parameters, '
+                        f'checkpoint every {every} days',
+            'plain_ms': round(1e3 * t_plain, 3), 'forward_ms': round(1e3 * t_fwd, 3),
+            'forward_adjoint_ms': round(1e3 * t_both, 3), 'adjoint_over_forward': round(t_both / t_fwd, 3),
+            'forward_over_plain': round(t_fwd / t_plain, 3),
+            'grad': {k: float(v) for k, v in zip(run.params.names, grad)}}
 
 
 def batched_arm(args, sim, plain_value, world):
@@ -343,7 +408,7 @@ def batched_arm(args, sim, plain_value, world):
     from covasim_gb300 import _lib as L
     B = args.batch
     sims = [cv.Sim(sim_pars(args, 1 + k), popdict=sim.popdict, person=sim._person) for k in range(B)]
-    batch = cv.BatchSim(sims).initialize()
+    batch = cv.BatchSim(sims, edge_tile=args.edge_tile).initialize()
     st = batch.state
     snap = st.snapshot()
     seeds = [choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected']) for s in sims]
@@ -373,7 +438,7 @@ def batched_arm(args, sim, plain_value, world):
     solo = sim.state.results(0)['new_infections']
     same = bool(np.array_equal(st.results(0)['new_infections'], solo))
     cum = [float(st.results(k)['new_infections'].sum()) for k in range(B)]
-    return {'value': round(value, 1), 'unit': 'agent-days/s', 'n_sims': B,
+    return {'value': round(value, 1), 'unit': 'agent-days/s', 'n_sims': B, 'edge_tile': st.edge_tile,
             'ms_per_step': round(1e3 * elapsed / args.steps, 3), 'vs_plain': round(value / plain_value, 3),
             'sim0_equals_plain_run': same, 'cum_infections_mean': round(float(np.mean(cum)), 1),
             'cum_infections_sd': round(float(np.std(cum)), 1)}
@@ -445,6 +510,148 @@ def reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def _line(metric_value, unit, args, ms, workload, extra):
+    line = {'metric': 'agent-days/s', 'value': round(metric_value, 1), 'unit': unit, 'n_gpus': 1,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms, 3), 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': workload}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+    if args.json_out:
+        with open(args.json_out, 'w') as f:
+            json.dump(line, f, indent=1)
+
+
+def large_arm(args, n=20_000_000, days=365):
+    """20M-agent hybrid sim, 3 co-circulating variants (rel_beta 1.0 / 1.5 / 1.7,
+    the second and third imported on days 60 and 120), waning, test_prob(symp_prob=0.1)
+    and contact_tracing(trace_probs=0.5), 365 days. A step is one whole run: the
+    state is rewound in HBM, the days between importations run as CUDA graphs and
+    the two importation days as single steps."""
+    import torch
+    import covasim_gb300 as cv
+    pars = dict(pop_size=n, pop_type='hybrid', pop_infected=200, use_waning=True, n_days=days, rand_seed=1,
+                dynam_layer=dict(h=0, s=0, w=0, c=1),
+                variants=[cv.variant(dict(rel_beta=1.5), days=60, n_imports=100, label='v1.5'),
+                          cv.variant(dict(rel_beta=1.7), days=120, n_imports=100, label='v1.7')],
+                interventions=[cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)])
+    t0 = time.perf_counter()
+    sim = cv.Sim(pars, edge_tile=4096 if args.edge_tile == 'auto' else int(args.edge_tile))
+    sim.initialize()
+    init_s = time.perf_counter() - t0
+    st = sim.state
+    snap = st.snapshot()
+
+    def one_run():
+        sim.rewind(snap)
+        sim.run()
+
+    for _ in range(args.warmup):
+        one_run()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        one_run()
+    ev1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    el = ev0.elapsed_time(ev1) / 1e3
+    res = st.results(0)
+    e_all = sum(len(ly['p1']) for ly in sim.spec.layers)
+    _line(n * days * args.steps / el, 'agent-days/s', args, 1e3 * el / args.steps,
+          f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), waning, test_prob(symp_prob=0.1), '
+          f'contact_tracing(trace_probs=0.5), {days} days',
+          {'edge_evaluations_per_s': round(2 * e_all * days * args.steps / el, 1), 'init_s': round(init_s, 1),
+           'cum_infections': float(res['new_infections'].sum() + sim['pop_infected']),
+           'cum_tests': float(res['new_tests'].sum()), 'cum_quarantined': float(res['new_quarantined'].sum()),
+           'clocks': clk})
+
+
+def batch_arm(args, n_sims=256, days=120):
+    """256 random-population sims (pop_size log-uniform in [10k, 500k], contacts
+    10/20/30, beta U[0.010, 0.025], change_beta(days=30, changes=U[0.3, 1])), 120
+    days: all in one BatchSim (one launch sequence per day over every sim, one
+    CUDA graph) against the same sims run one by one (one graph each). Each
+    batched sim is bit-identical to its own run, so outcome statistics match
+    exactly; value is the batched agent-days/s, with the one-by-one figure beside it."""
+    import torch
+    import covasim_gb300 as cv
+    from covasim_gb300._lib import MAX_LAYERS
+    from covasim_gb300.sim import CALL_SEED as CALL_SEED_TAG
+    rng = np.random.default_rng(2024)
+    sizes = np.exp(rng.uniform(np.log(10_000), np.log(500_000), n_sims)).astype(int)
+    contacts = rng.choice([10, 20, 30], n_sims)
+    betas = rng.uniform(0.010, 0.025, n_sims)
+    changes = rng.uniform(0.3, 1.0, n_sims)
+
+    def make(k):
+        return cv.Sim(dict(pop_size=int(sizes[k]), pop_type='random', contacts=dict(a=int(contacts[k])),
+                           beta=float(betas[k]), n_days=days, rand_seed=100 + k, pop_infected=20,
+                           interventions=[cv.change_beta(days=30, changes=float(changes[k]))]))
+    t0 = time.perf_counter()
+    sims = [make(k) for k in range(n_sims)]
+    batch = cv.BatchSim(sims, edge_tile=args.edge_tile).initialize()
+    init_s = time.perf_counter() - t0
+    st = batch.state
+    snap = st.snapshot()
+    seeds = [choose_seed(s) for s in sims]
+    npts = days + 1
+
+    def batched():
+        st.restore(snap)
+        for k, inds in enumerate(seeds):
+            st.infect_list(0, inds, sim=k, variant=0, layer_tag=MAX_LAYERS, call_tag=CALL_SEED_TAG)
+        st.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
+
+    singles = []
+    for k in range(n_sims):
+        s = cv.Sim(dict(sims[k].pars), popdict=sims[k].popdict, person=sims[k]._person,
+                   edge_tile=st.edge_tile)
+        s.initialize()
+        singles.append((s, s.state.snapshot()))
+
+    def one_by_one():
+        for s, sn in singles:
+            s.state.restore(sn)
+            s.state.infect_list(0, choose_seed(s), sim=0, variant=0, layer_tag=MAX_LAYERS, call_tag=CALL_SEED_TAG)
+            s.state.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / args.steps
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t_batch = timed(batched)
+    t_single = timed(one_by_one)
+    clk = clocks.stop()
+    agent_days = float(sizes.sum()) * days
+    same = all(np.array_equal(st.results(k)['new_infections'], singles[k][0].state.results(0)['new_infections'])
+               for k in range(n_sims))
+    _line(agent_days / t_batch, 'agent-days/s', args, 1e3 * t_batch,
+          f'{n_sims} random-population sims, {int(sizes.sum())} agents in all (10k-500k each), contacts 10/20/30, '
+          f'beta U[0.010,0.025], change_beta day 30 x U[0.3,1], {days} days',
+          {'one_by_one': {'value': round(agent_days / t_single, 1), 'ms_per_step': round(1e3 * t_single, 3)},
+           'batched_over_one_by_one': round(t_single / t_batch, 3), 'every_sim_equals_its_own_run': same,
+           'edge_tile': st.edge_tile, 'init_s': round(init_s, 1), 'clocks': clk})
+
+
+def choose_seed(sim):
+    from covasim_gb300.sim import choose_seed_infections
+    return choose_seed_infections(sim['rand_seed'], sim['pop_size'], sim['pop_infected'])
+
+
 def profile_run(args):
     """One ungraphed run (kernels launched one by one) for ncu captures."""
     import torch
@@ -465,6 +672,10 @@ def main():
     if args.impl == 'reference':
         reference_arm(args, world, rank)
         return
+    if args.workload != 'hybrid1m':
+        if rank == 0:
+            (large_arm if args.workload == 'large' else batch_arm)(args)
+        return
     out = gpu_arm(args, world, rank)
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -480,10 +691,12 @@ def main():
                 'config': {'workload': f'hybrid {args.pop_size} agents (h/s/w/c, c redrawn daily), '
                                        f'{args.days} days, waning, pop_infected 100',
                            'step': 'one full run: rewind state in HBM, seed, 181 days as one CUDA graph',
+                           'edge_tile': out['edge_tile'], 'edge_tile_autotune_ms_per_run': out['tile_ms'],
                            'l2': 'inputs larger than L2 (agents ~160 MB + static edges ~62 MB)',
                            'replicas': world, 'cum_infections_per_run': out['cum_infections']},
                 'edge_evaluations_per_s': None,
                 'roofline': out['roofline'], 'cpu_baseline': cpu, 'e2e': out['e2e'], 'batched': out['batched'],
+                'adjoint': out['adjoint'],
                 'gpu_launches': out['launches'], 'clocks': out['clocks']}
         spec = out['spec']
         e_all = sum(len(ly['p1']) for ly in spec.layers)

@@ -22,7 +22,8 @@ FX_NAB_BITS = 24
 FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
 NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
-EDGE_TILE = 4096          # edges per edge-pass block (covgpu.cu EDGE_TILE)
+EDGE_TILE = 4096          # default edges per edge-pass tile (block)
+EDGE_TILES = (1024, 2048, 4096, 8192)   # tile sizes the library supports (covgpu_state.edge_tile)
 AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
 AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
 
@@ -106,7 +107,7 @@ class Lik(C.Structure):
 class State(C.Structure):
     _fields_ = [
         ('n', C.c_int64), ('n_sims', C.c_int32), ('n_segments', C.c_int32), ('n_tiles', C.c_int64),
-        ('n_agent_blocks', C.c_int64),
+        ('n_agent_blocks', C.c_int64), ('edge_tile', C.c_int32), ('_pad_tile', C.c_int32),
         ('flags', C.c_void_p), ('vstate', C.c_void_p),
         ('symp_prob', C.c_void_p), ('severe_prob', C.c_void_p), ('crit_prob', C.c_void_p), ('death_prob', C.c_void_p),
         ('rel_trans', C.c_void_p), ('rel_sus', C.c_void_p),
@@ -158,13 +159,13 @@ def lib():
         L.covgpu_edge_pass.argtypes = [sp, i32, vp]
         L.covgpu_infect_claims.argtypes = [sp, i32, vp]
         L.covgpu_test_trace.argtypes = [sp, i32, vp]
-        L.covgpu_lik_pass.argtypes = [sp, i32, vp]
+        L.covgpu_lik_targets.argtypes = [sp, i32, vp]
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
         for name in ('covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections', 'covgpu_agent_step',
                      'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_materialize',
-                     'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_pass'):
+                     'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_targets'):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -195,4 +196,4 @@ def abi_layout():
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
             'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
-            'covgpu_lik_pass']
+            'covgpu_lik_targets']

@@ -179,6 +179,7 @@ class LikelihoodRun:
         if st.status():
             raise L.CovgpuError('likelihood run', st.status())
         out = self._read(grad=False)
+        self.last = out  # per-day ll and expected of this run
         return float(out['ll'].sum()), out['expected']
 
     def recompute(self, theta_eval=None, grad=True):

@@ -32,7 +32,7 @@ class BatchSim:
         use_graph: capture the day loop in a CUDA graph
     """
 
-    def __init__(self, sims, n_runs=None, use_graph=True, log=False):
+    def __init__(self, sims, n_runs=None, use_graph=True, log=False, edge_tile=None):
         if isinstance(sims, Sim):
             base = sims
             n_runs = n_runs or 1
@@ -44,6 +44,7 @@ class BatchSim:
         self.sims = list(sims)
         self.use_graph = use_graph
         self.log = log
+        self.edge_tile = edge_tile  # as Sim's: an int, None (4096) or 'auto'
         self.state = None
 
     def initialize(self):
@@ -66,7 +67,11 @@ class BatchSim:
         if len(npts) != 1:
             raise ValueError('all sims of a batch must have the same number of days')
         self.npts = npts.pop()
-        self.state = BatchState(specs, log=self.log)
+        tile = L.EDGE_TILE if self.edge_tile in (None, 'auto') else int(self.edge_tile)
+        self.state = BatchState(specs, log=self.log, edge_tile=tile)
+        if self.edge_tile == 'auto':
+            from .autotune import tune_edge_tile
+            tune_edge_tile(self.state)
         return self
 
     def seed_infections(self):

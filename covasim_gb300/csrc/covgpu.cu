@@ -29,11 +29,11 @@ namespace {
 constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
 constexpr int EDGE_THREADS = 256;
 constexpr int EDGE_VEC = 4;            // edges per 128-bit load
-constexpr int64_t EDGE_TILE = 4096;    // edges per edge-pass block (must match the host)
+constexpr int EDGE_ROUND = EDGE_THREADS * EDGE_VEC;  // edges one block reads per round
+constexpr int64_t EDGE_TILE_MAX = 8192;  // edge tiles: 1024, 2048, 4096 or 8192 edges (covgpu_state.edge_tile)
 constexpr int EQ_ROUND = 2 * 32 * EDGE_VEC;  // most candidate directions one warp appends per round
 constexpr int EQ_CAP = 384;            // candidate queue entries per warp (drained when a round could overflow)
-static_assert(2 * EDGE_TILE <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
-static_assert(EDGE_TILE % (EDGE_THREADS * EDGE_VEC) == 0, "whole rounds per tile");
+static_assert(2 * EDGE_TILE_MAX <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
 constexpr int INF_THREADS = 256;
 constexpr int INF_PER_THREAD = INF_TILE / INF_THREADS;
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
 
 // ============================================================ fused edge pass
 //
-// One block per tile of EDGE_TILE edges of one layer segment. Phase A streams
+// One block per tile of ROUNDS * 1024 edges of one layer segment. Phase A streams
 // the tile (128-bit loads of p1/p2, or the dynamic layer's endpoints from
 // Philox), reads both endpoints' role words and appends every candidate
 // direction source -> target to its warp's queue in shared memory. Phase B
@@ -470,11 +470,52 @@ struct SegCtx {
   int64_t n_edges;
 };
 
+// per-thread likelihood sums of one tile (one sim, one layer)
+struct LikAcc {
+  double ll = 0.0, g = 0.0;
+};
+
+// The likelihood terms of one candidate direction s -> g (see covgpu_lik):
+// the outcome `hit` is the edge pass's own draw on the float32 p32; the
+// terms use p recomputed in float64 from the unrounded factors and F, capped
+// at 1 (a draw u < p with p >= 1 is certain, and its probability does not
+// change with the parameters).
+__device__ __forceinline__ void lik_terms(const covgpu_state& st, const SegCtx& c, int t, uint32_t v, int32_t g,
+                                          uint32_t fs, uint32_t fg, float rt, float vl, float rs, float lb, float si,
+                                          float p32, bool hit, LikAcc& acc) {
+  const covgpu_lik& K = st.lik;
+  double r = (double)rt;
+  if (fs & B_QUAR) r = __dmul_rn(r, (double)c.quar_factor);
+  if (!(fs & B_SYMP)) r = __dmul_rn(r, (double)c.asymp_factor);
+  if (fs & B_ISO) r = __dmul_rn(r, (double)c.iso_factor);
+  r = __dmul_rn(r, (double)vl);
+  double q = (double)rs;
+  if (fg & B_QUAR) q = __dmul_rn(q, (double)c.quar_factor);
+  q = __dmul_rn(q, __dsub_rn(1.0, (double)si));
+  const double F = K.factor[(((int64_t)c.sim * K.npts_max + t) * K.n_layers_max + c.layer) * K.nv_max + v];
+  double p = __dmul_rn(__dmul_rn(__dmul_rn(F, (double)lb), r), q);
+  if (p >= 1.0) {
+    if (hit) {  // certain transmission: log p = 0, no sensitivity; the target is surely infected
+      atomicAdd(K.logq + g, -INFINITY);
+      return;
+    }
+    p = (double)p32;  // not infected, so p32 < 1: p crossed 1 only by rounding
+  }
+  const double l1m = log1p(-p);
+  const double odds = __ddiv_rn(p, __dsub_rn(1.0, p));
+  acc.ll += hit ? log(p) : l1m;
+  acc.g += hit ? 1.0 : -odds;
+  atomicAdd(K.logq + g, l1m);
+  if (K.g_exp) atomicAdd(K.w + (int64_t)c.layer * st.n + g, odds);
+}
+
 // compute_trans_sus folded into compute_infections for one direction s -> g
 // (utils.py:88-89 then 117-123); returns true on a transmission. Every gather
-// is issued before the first use so that they overlap.
+// is issued before the first use so that they overlap. LIK: also the
+// likelihood terms of the direction, from the same gathered values.
+template <bool LIK>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
-                                         int32_t s, int32_t g, uint32_t& v_out) {
+                                         int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
   const uint32_t vs = __ldg(st.vstate + s);
   const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
   const float rt = __ldg(st.rel_trans + s), vl = __ldg(st.viral_load + s), rs = __ldg(st.rel_sus + g);
@@ -496,70 +537,17 @@ __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c
   const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
   if (p == 0.0f) return false;
   v_out = v;
-  if (st.edge_uniforms)  // injected draws (test mode)
-    return st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
-  // one Philox block per (edge, day, variant, layer): words x,y draw direction 0, z,w direction 1
-  const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_EDGE | (v << 8) | (uint32_t)c.layer),
-                         c.key0, c.key1);
-  return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);  // u < p in float64, decided in integers
-}
-
-// per-thread likelihood sums of one tile (one sim, one layer)
-struct LikAcc {
-  double ll = 0.0, g = 0.0;
-};
-
-// The likelihood terms of one direction s -> g (see covgpu_lik): the
-// outcome is the edge pass's own draw on the float32 p; the terms use p
-// recomputed in float64 from the unrounded factors and F.
-__device__ __forceinline__ void lik_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
-                                        int32_t s, int32_t g, LikAcc& acc) {
-  const uint32_t vs = __ldg(st.vstate + s);
-  const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
-  const float rt = __ldg(st.rel_trans + s), vl = __ldg(st.viral_load + s), rs = __ldg(st.rel_sus + g);
-  const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
-  const uint32_t v = (vs >> 8) & 0xFFu;
-  const uint32_t vc = v < (uint32_t)c.nv ? v : 0u;
-  const float si = __ldg(st.sus_imm + (int64_t)vc * st.n + g);
-  const float beta = __ldg(c.beta_t + vc);
-  if (v >= (uint32_t)c.nv) return;
-  // float32 p exactly as edge_try computes it, for the outcome
-  float rte = rt;
-  if (fs & B_QUAR) rte = __fmul_rn(rte, c.quar_factor);
-  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, c.asymp_factor);
-  if (fs & B_ISO) rte = __fmul_rn(rte, c.iso_factor);
-  rte = __fmul_rn(__fmul_rn(rte, c.beta_layer), vl);
-  float rse = rs;
-  if (fg & B_QUAR) rse = __fmul_rn(rse, c.quar_factor);
-  rse = __fmul_rn(rse, __fsub_rn(1.0f, si));
-  const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
-  if (p == 0.0f) return;
   bool hit;
-  if (st.edge_uniforms) {
+  if (st.edge_uniforms) {  // injected draws (test mode)
     hit = st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
   } else {
+    // one Philox block per (edge, day, variant, layer): words x,y draw direction 0, z,w direction 1
     const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
                                       TAG_EDGE | (v << 8) | (uint32_t)c.layer), c.key0, c.key1);
-    hit = dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);
+    hit = dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);  // u < p in float64, decided in integers
   }
-  // float64 p from the same factors
-  const covgpu_lik& K = st.lik;
-  double r = (double)rt;
-  if (fs & B_QUAR) r = __dmul_rn(r, (double)c.quar_factor);
-  if (!(fs & B_SYMP)) r = __dmul_rn(r, (double)c.asymp_factor);
-  if (fs & B_ISO) r = __dmul_rn(r, (double)c.iso_factor);
-  r = __dmul_rn(r, (double)vl);
-  double q = (double)rs;
-  if (fg & B_QUAR) q = __dmul_rn(q, (double)c.quar_factor);
-  q = __dmul_rn(q, __dsub_rn(1.0, (double)si));
-  const double F = K.factor[(((int64_t)c.sim * K.npts_max + t) * K.n_layers_max + c.layer) * K.nv_max + v];
-  const double p64 = __dmul_rn(__dmul_rn(__dmul_rn(F, (double)lb), r), q);
-  const double l1m = log1p(-p64);
-  const double odds = __ddiv_rn(p64, __dsub_rn(1.0, p64));
-  acc.ll += hit ? log(p64) : l1m;
-  acc.g += hit ? 1.0 : -odds;
-  atomicAdd(K.logq + g, l1m);
-  if (K.g_exp) atomicAdd(K.w + (int64_t)c.layer * st.n + g, odds);
+  if (LIK) lik_terms(st, c, t, v, g, fs, fg, rt, vl, rs, lb, si, p, hit, acc);
+  return hit;
 }
 
 __device__ __forceinline__ uint64_t event_key(int t, uint32_t v, int layer, int dir, int64_t e) {
@@ -606,7 +594,7 @@ __device__ __forceinline__ void queue_push(EdgeQueue& q, int& qn, bool has, int3
 }
 
 // phase B: one candidate per lane, then the warp-aggregated event append
-// (LIK: the likelihood terms instead of the events)
+// (LIK: with the likelihood terms)
 template <bool LIK>
 __device__ __forceinline__ void queue_drain(const covgpu_state& st, const SegCtx& c, int t, int64_t e0,
                                             EdgeQueue& q, int qn, LikAcc& acc) {
@@ -620,10 +608,9 @@ __device__ __forceinline__ void queue_drain(const covgpu_state& st, const SegCtx
     uint32_t m = 0;
     if (i < qn) {
       s = q.s[i]; g = q.g[i]; m = q.m[i];
-      if (LIK) lik_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, acc);
-      else hit = edge_try(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, v);
+      hit = edge_try<LIK>(st, c, t, e0 + (m >> 1), (int)(m & 1u), s, g, v, acc);
     }
-    if (!LIK) emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), e0 + (m >> 1)) : 0ull, g, s);
+    emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), e0 + (m >> 1)) : 0ull, g, s);
   }
   __syncwarp();
 }
@@ -634,8 +621,9 @@ __device__ __forceinline__ double warp_sum_d(double x) {
   return x;
 }
 
-template <bool LIK>
+template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
   __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
   if (threadIdx.x == 0) {  // segment owning this tile: last segment with tile_begin <= blockIdx.x
@@ -668,14 +656,13 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   const bool dynamic = L->dynamic != 0;
   const int32_t* p1 = L->p1;
   const int32_t* p2 = L->p2;
-  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
-  const int64_t e1 = min(e0 + EDGE_TILE, c.n_edges);
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
+  const int64_t e1 = min(e0 + TILE, c.n_edges);
   const int64_t n_local = sp->n_agents;
   const int32_t off = (int32_t)sp->agent_off;
   EdgeQueue& q = s_q[threadIdx.x >> 5];
   int qn = 0;  // warp-uniform queue length
   LikAcc acc;
-  constexpr int ROUNDS = EDGE_TILE / (EDGE_THREADS * EDGE_VEC);
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
     int32_t a[EDGE_VEC], b[EDGE_VEC];
@@ -736,14 +723,26 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   }
 }
 
+template <bool LIK>
+void launch_edge_tiles(const covgpu_state* st, int t, cudaStream_t s) {
+  const dim3 grid((unsigned)st->n_tiles);
+  switch (st->edge_tile) {
+    case 1024: k_edge_pass<LIK, 1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    case 2048: k_edge_pass<LIK, 2><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    case 8192: k_edge_pass<LIK, 8><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    default: k_edge_pass<LIK, 4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+  }
+}
+
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
   if (st->n_tiles == 0) return COVGPU_OK;
-  k_edge_pass<false><<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  if (st->lik.factor) launch_edge_tiles<true>(st, t, s);
+  else launch_edge_tiles<false>(st, t, s);
   return launch_status();
 }
 
-// per target: expected = 1 - prod(1 - p) and its per-layer sensitivities, then
-// the per-target sums are cleared for the next day
+// per target: expected = 1 - prod(1 - p) and its per-layer sensitivities from
+// the sums the likelihood edge pass left, which are cleared for the next day
 __global__ void __launch_bounds__(AGENT_THREADS) k_lik_agents(covgpu_state st, int t) {
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
@@ -786,9 +785,8 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_lik_agents(covgpu_state st, i
     atomicAdd(K.g_exp + day * K.n_layers_max + threadIdx.x, s_h[threadIdx.x]);
 }
 
-int launch_lik_pass(const covgpu_state* st, int t, cudaStream_t s) {
+int launch_lik_targets(const covgpu_state* st, int t, cudaStream_t s) {
   if (!st->lik.factor) return COVGPU_OK;
-  if (st->n_tiles > 0) k_edge_pass<true><<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
   k_lik_agents<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }
@@ -1114,7 +1112,9 @@ __device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, in
 
 // contact_tracing.identify_contacts, the find_contacts half (utils.py:131-147):
 // every edge with a traced endpoint marks the other endpoint in its layer's bitmap
+template <int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
+  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
   if (threadIdx.x == 0) {
     int lo = 0, hi = st.n_segments - 1;
@@ -1131,10 +1131,9 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
   if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
   const int64_t words = (st.n + 31) >> 5;
   uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
-  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * EDGE_TILE;
-  const int64_t e1 = min(e0 + EDGE_TILE, L->n_edges);
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
+  const int64_t e1 = min(e0 + TILE, L->n_edges);
   const int32_t off = (int32_t)sp.agent_off;
-  constexpr int ROUNDS = EDGE_TILE / (EDGE_THREADS * EDGE_VEC);
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
 #pragma unroll
@@ -1247,7 +1246,15 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
 int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   if (!st->has_testing) return COVGPU_OK;
   k_test_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
-  if (st->n_tiles > 0) k_trace_scan<<<(unsigned)st->n_tiles, EDGE_THREADS, 0, s>>>(*st, t);
+  if (st->n_tiles > 0) {
+    const dim3 grid((unsigned)st->n_tiles);
+    switch (st->edge_tile) {
+      case 1024: k_trace_scan<1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      case 2048: k_trace_scan<2><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      case 8192: k_trace_scan<8><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      default: k_trace_scan<4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    }
+  }
   k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }
@@ -1276,7 +1283,7 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
     k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
     launch_test_trace(st, t, s);
     launch_edge_pass(st, t, s);
-    launch_lik_pass(st, t, s);
+    launch_lik_targets(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
   if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0);
@@ -1436,6 +1443,8 @@ static int check_state(const covgpu_state* st) {
   if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0))
     return COVGPU_BADARG;
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
+  if (st->edge_tile != 1024 && st->edge_tile != 2048 && st->edge_tile != 4096 && st->edge_tile != 8192)
+    return COVGPU_BADARG;
   if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
                           st->pending_slots < 1 || st->n_contact_layers < 1))
     return COVGPU_BADARG;
@@ -1468,11 +1477,11 @@ int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream) {
   return launch_test_trace(st, t, S(stream));
 }
 
-int covgpu_lik_pass(const covgpu_state* st, int32_t t, void* stream) {
+int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF || !st->lik.factor) return COVGPU_BADARG;
-  return launch_lik_pass(st, t, S(stream));
+  return launch_lik_targets(st, t, S(stream));
 }
 
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream) {

@@ -125,10 +125,14 @@ class Sim:
             arguments are merged in
         popdict (dict): optional population (uid, age, sex, contacts)
         use_graph (bool): capture the day loop in a CUDA graph
+        edge_tile (int or 'auto'): edges per edge-pass block (1024, 2048, 4096 or
+            8192; default 4096); 'auto' times whole runs with each at initialize
+            (``covasim_gb300.autotune``, cached per workload)
     """
 
-    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, **kwargs):
+    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, edge_tile=None, **kwargs):
         self.label = label
+        self.edge_tile = edge_tile  # edges per edge-pass block; 'auto': autotuned at initialize
         self.pars = cvpar.make_pars()
         self.update_pars(pars, **kwargs)
         self.popdict = popdict
@@ -231,7 +235,12 @@ class Sim:
         self.popdict = popdict
         self._person = person
         self.spec = spec
-        self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity)
+        tile = L.EDGE_TILE if self.edge_tile in (None, 'auto') else int(self.edge_tile)
+        self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity,
+                                edge_tile=tile)
+        if self.edge_tile == 'auto':
+            from .autotune import tune_edge_tile
+            tune_edge_tile(self.state)
         contacts = Contacts()
         for ly in spec.layers:
             if torch.is_tensor(ly['p1']):
@@ -352,6 +361,18 @@ class Sim:
             raise L.CovgpuError('device status', status)
         if self.complete:
             self.finalize()
+        return self
+
+    def rewind(self, snap):
+        """Return an initialised sim to day 0 from ``state.snapshot()`` taken before
+        its first run (device copy, no population rebuild), ready to run again."""
+        self.state.restore(snap)
+        self.t = 0
+        self._seeded = False
+        self._open_day = None
+        self.complete = False
+        self.results_ready = False
+        self.init_results()
         return self
 
     def _rerun_bigger(self, until):

@@ -160,7 +160,10 @@ def testing_record(spec):
 class BatchState:
     """Agent and layer arrays of one or more sims in device memory."""
 
-    def __init__(self, specs, device='cuda', event_capacity=None, log_capacity=None, log=True):
+    def __init__(self, specs, device='cuda', event_capacity=None, log_capacity=None, log=True, edge_tile=L.EDGE_TILE):
+        if int(edge_tile) not in L.EDGE_TILES:
+            raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
+        self.edge_tile = int(edge_tile)
         if not torch.cuda.is_available():
             raise RuntimeError('covasim_gb300 needs a CUDA device: the GPU path has no CPU fallback')
         self.lib = L.lib()
@@ -242,6 +245,7 @@ class BatchState:
         self.edge_uniform_tensors = None
         self.hospicu = None
         self.lik = None
+        self.lik_active = False
         self._refresh_state()
 
     # ------------------------------------------------------------------ building
@@ -258,7 +262,6 @@ class BatchState:
         self.segments = []   # (ctypes Layer, tensors kept alive)
         self.layer_tensors = []
         self.segment_index = {}  # (sim, layer) -> segment index
-        tiles = 0
         for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
             for li, ly in enumerate(sp.layers):
                 p1 = ly['p1'] if torch.is_tensor(ly['p1']) else np.asarray(ly['p1'], dtype=np.int64)
@@ -319,14 +322,28 @@ class BatchState:
                         tb = torch.from_numpy(beta).to(self.device)
                         rec.beta = tb.data_ptr()
                         keep.append(tb)
-                rec.tile_begin = tiles
-                tiles += (n_edges + L.EDGE_TILE - 1) // L.EDGE_TILE
                 self.segment_index[(s, li)] = len(self.segments)
                 self.segments.append(rec)
                 self.layer_tensors.append(keep)
+        self._tile_segments()
+
+    def _tile_segments(self):
+        """Each segment's first tile and the tile count for the current edge tile size."""
+        tiles = 0
+        for rec in self.segments:
+            rec.tile_begin = tiles
+            tiles += (rec.n_edges + self.edge_tile - 1) // self.edge_tile
         self.n_tiles = tiles
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
         self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+
+    def set_edge_tile(self, tile):
+        """Edges per edge-pass block (one of L.EDGE_TILES); the autotuner's knob."""
+        if int(tile) not in L.EDGE_TILES:
+            raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
+        self.edge_tile = int(tile)
+        self._tile_segments()
+        self._refresh_state()
 
     def _build_sims(self, beta_tabs, bl_tabs, kins):
         recs = []
@@ -431,6 +448,7 @@ class BatchState:
         st.n_segments = len(self.segments)
         st.n_tiles = self.n_tiles
         st.n_agent_blocks = self.n_agent_blocks
+        st.edge_tile = self.edge_tile
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
                   'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'events', 'event_count',
@@ -457,7 +475,7 @@ class BatchState:
             st.edge_uniforms = self._eu_ptrs.data_ptr()
         else:
             st.edge_uniforms = None
-        if self.lik is not None:
+        if self.lik is not None and self.lik_active:
             k = self.lik
             st.lik.factor = k['factor'].data_ptr()
             st.lik.ll = k['ll'].data_ptr()
@@ -512,10 +530,12 @@ class BatchState:
                             logq=torch.zeros(self.n, dtype=f64, device=dev),
                             w=torch.zeros((Lm, self.n), dtype=f64, device=dev))
         self.lik['grad'] = bool(grad)
+        self.lik_active = True
         self._refresh_state()
 
     def disable_lik(self):
-        self.lik = None
+        """Switch the likelihood passes off (the buffers are kept for the next enable_lik)."""
+        self.lik_active = False
         self._refresh_state()
 
     def set_lik_factor(self, factor, sim=0):
@@ -529,8 +549,9 @@ class BatchState:
         for k in ('ll', 'expected', 'g_ll', 'g_exp', 'logq', 'w'):
             self.lik[k].zero_()
 
-    def lik_pass(self, t):
-        L.call('covgpu_lik_pass', self.cstate_ptr, int(t), _stream())
+    def lik_targets(self, t):
+        """Per-target half of day t's likelihood (after edge_pass, before infect_claims)."""
+        L.call('covgpu_lik_targets', self.cstate_ptr, int(t), _stream())
 
     def set_beta_tables(self, beta_sched, beta_layer_sched, sim=0):
         """Overwrite one sim's per-day beta tables in place (float64 schedules,

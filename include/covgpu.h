@@ -221,6 +221,9 @@ typedef struct covgpu_state {
   int32_t n_segments;             /* layer segments over all sims                   */
   int64_t n_tiles;                /* edge-pass tiles over all segments              */
   int64_t n_agent_blocks;
+  int32_t edge_tile;              /* edges per edge-pass tile: 1024, 2048, 4096 or
+                                     8192 (segments' tile_begin count these tiles)   */
+  int32_t _pad_tile;
   /* per-agent state */
   uint32_t* flags;
   uint32_t* vstate;               /* bytes: exposed, infectious, recovered variant   */
@@ -336,7 +339,9 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
 /* Transmission over every layer segment and variant: both directions of each
  * edge from one read, Bernoulli draws from Philox (or st->edge_uniforms),
  * events appended to st->events and the first infector of each target
- * claimed with a 64-bit atomicMin on (day, variant, layer, direction, edge). */
+ * claimed with a 64-bit atomicMin on (day, variant, layer, direction, edge).
+ * With st->lik.factor set, also the likelihood terms of every candidate
+ * direction (covgpu_lik). */
 int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream);
 
 /* The testing and tracing interventions of day t, after the agent pass and
@@ -349,10 +354,13 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream);
  * 315-366). A no-op when st->has_testing is 0. */
 int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream);
 
-/* The likelihood passes of day t (see covgpu_lik): after covgpu_edge_pass
- * and before covgpu_infect_claims of that day, so that they see the state
- * the transmission draws saw. BADARG when st->lik.factor is NULL. */
-int covgpu_lik_pass(const covgpu_state* st, int32_t t, void* stream);
+/* The per-target half of day t's likelihood (see covgpu_lik): expected
+ * infections and their sensitivities from the per-target sums that
+ * covgpu_edge_pass accumulates when st->lik.factor is set (it then adds the
+ * likelihood terms of every candidate direction to its usual work). Call
+ * after covgpu_edge_pass and before covgpu_infect_claims of the same day.
+ * BADARG when st->lik.factor is NULL. */
+int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream);
 
 /* infect() for the winning event of each target. */
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
@@ -371,7 +379,7 @@ int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t,
                              void* stream);
 
 /* Run days [t0, t1) of every sim: per day agent_step, test_trace (when
- * st->has_testing), edge_pass, lik_pass (when st->lik.factor is set),
+ * st->has_testing), edge_pass, lik_targets (when st->lik.factor is set),
  * infect_claims. open_prev: day t0-1 still needs its closing pass (stocks,
  * update_nab), which day t0's agent pass then does first; close_last: end
  * with the closing pass of day t1-1. With use_graph the whole sequence is

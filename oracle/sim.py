@@ -97,6 +97,7 @@ class OracleSim:
             self.rs_numpy = np.random.RandomState(self.seed)
         self.beta_schedule = beta_schedule
         self.seed_inds = seed_inds
+        self.exposure_hook = None  # optional f(sim, t, viral_load) before each day's transmission
         self.interventions = list(interventions or [])  # oracle.interventions objects, applied in order
         for iv in self.interventions:
             if hasattr(iv, 'initialize'):
@@ -161,6 +162,8 @@ class OracleSim:
         vd = p['viral_dist']
         viral_load = compute_viral_load(t, people.date_infectious, people.date_recovered, people.date_dead,
                                         F32(vd['frac_time']), F32(vd['load_ratio']), F32(vd['high_cap']))
+        if self.exposure_hook is not None:  # test hook: the state the transmission draws see
+            self.exposure_hook(self, t, viral_load)
         nv = p['n_variants']
         for variant in range(nv):
             label = p['variant_map'][variant]
