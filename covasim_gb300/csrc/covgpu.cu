@@ -31,8 +31,8 @@ constexpr int EDGE_THREADS = 256;
 constexpr int EDGE_VEC = 4;            // edges per 128-bit load
 constexpr int EDGE_ROUND = EDGE_THREADS * EDGE_VEC;  // edges one block reads per round
 constexpr int64_t EDGE_TILE_MAX = 8192;  // edge tiles: 1024, 2048, 4096 or 8192 edges (covgpu_state.edge_tile)
-constexpr int EQ_ROUND = 2 * 32 * EDGE_VEC;  // most candidate directions one warp appends per round
-constexpr int EQ_CAP = 384;            // candidate queue entries per warp (drained when a round could overflow)
+constexpr int EQ_ROUND = 32 * EDGE_VEC;  // most candidates one warp appends per round (one per edge)
+constexpr int EQ_CAP = 256;            // candidate queue entries per warp (drained when a round could overflow)
 static_assert(2 * EDGE_TILE_MAX <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
 constexpr int INF_THREADS = 256;
@@ -372,7 +372,9 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
                                           sp.frac_time, sp.load_ratio, sp.high_cap);
         src_bit = (rt != 0.0f && iv < (uint32_t)nv) ? 1u : 0u;
       }
-      if ((f & B_SUS) && st.rel_sus[i] != 0.0f) tgt_bit = 1u;
+      // exclusive by construction (the infectious are never susceptible); the edge
+      // pass relies on it to queue at most one direction per edge
+      if ((f & B_SUS) && !src_bit && st.rel_sus[i] != 0.0f) tgt_bit = 1u;
       if (f != f_in) st.flags[i] = f;
       if (vs != vs_in) st.vstate[i] = vs;
     }
@@ -394,7 +396,8 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
     const uint32_t sm = __ballot_sync(0xffffffffu, src_bit), tm = __ballot_sync(0xffffffffu, tgt_bit);
     if (lane == 0 && blk.begin + warp * 32 < blk.end) {
       const int64_t w = (blk.begin + warp * 32) >> 5;
-      reinterpret_cast<uint2*>(st.roles)[w] = make_uint2(sm, tm);
+      st.roles[w] = sm;                        // source bitmap
+      st.roles[roles_words(st) + w] = tm;      // target bitmap
     }
   }
 
@@ -452,11 +455,14 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
 // compute_trans_sus run lane-packed instead of serialising the whole warp on
 // the few lanes that hold a source.
 
-struct Roles { uint32_t src, tgt; };
-__device__ __forceinline__ Roles role_of(const uint32_t* __restrict__ roles, int32_t a) {
-  const uint2 w = __ldg(reinterpret_cast<const uint2*>(roles) + (a >> 5));
-  const uint32_t b = (uint32_t)a & 31u;
-  return Roles{(w.x >> b) & 1u, (w.y >> b) & 1u};
+// source bit (infectious with a variant and rel_trans != 0) and target bit
+// (susceptible with rel_sus != 0) of agent a: two separate bitmaps, so that the
+// source bitmap (n/8 bytes), tested for both endpoints of every edge, stays in L1
+__device__ __forceinline__ uint32_t src_bit(const uint32_t* __restrict__ roles, int32_t a) {
+  return (__ldg(roles + (a >> 5)) >> (a & 31)) & 1u;
+}
+__device__ __forceinline__ uint32_t tgt_bit(const covgpu_state& st, int32_t a) {
+  return (__ldg(st.roles + roles_words(st) + (a >> 5)) >> (a & 31)) & 1u;
 }
 
 // per-tile constants, hoisted out of the segment and sim records
@@ -470,43 +476,63 @@ struct SegCtx {
   int64_t n_edges;
 };
 
-// per-thread likelihood sums of one tile (one sim, one layer)
+// per-thread likelihood sums of one tile (one sim, one layer), float-float
 struct LikAcc {
-  double ll = 0.0, g = 0.0;
+  ff ll{0.0f, 0.0f}, g{0.0f, 0.0f};
 };
+
+__device__ __forceinline__ ff ff_mul_f(ff x, float f) {
+  const ff p = two_prod(x.hi, f);
+  return fast_two_sum(p.hi, __fmaf_rn(x.lo, f, p.lo));
+}
+// ln of a positive float-float: ln(hi) + lo / hi (|lo / hi| <= 2^-24, so the
+// dropped term is below 2^-49)
+__device__ __forceinline__ ff ff_log_ff(ff x) {
+  const ff l = ff_log(x.hi, COVGPU_LN_TAB);
+  return fast_two_sum(l.hi, __fadd_rn(l.lo, __fdiv_rn(x.lo, x.hi)));
+}
+__device__ __forceinline__ double ff_to_d(ff x) { return __dadd_rn((double)x.hi, (double)x.lo); }
 
 // The likelihood terms of one candidate direction s -> g (see covgpu_lik):
 // the outcome `hit` is the edge pass's own draw on the float32 p32; the
-// terms use p recomputed in float64 from the unrounded factors and F, capped
-// at 1 (a draw u < p with p >= 1 is certain, and its probability does not
-// change with the parameters).
+// terms use p recomputed from the unrounded factors and F in float-float
+// (~2^-44 relative; GB300's float64 rate is a small fraction of its float32
+// rate), capped at 1 (a draw u < p with p >= 1 is certain, and its
+// probability does not change with the parameters).
 __device__ __forceinline__ void lik_terms(const covgpu_state& st, const SegCtx& c, int t, uint32_t v, int32_t g,
                                           uint32_t fs, uint32_t fg, float rt, float vl, float rs, float lb, float si,
                                           float p32, bool hit, LikAcc& acc) {
   const covgpu_lik& K = st.lik;
-  double r = (double)rt;
-  if (fs & B_QUAR) r = __dmul_rn(r, (double)c.quar_factor);
-  if (!(fs & B_SYMP)) r = __dmul_rn(r, (double)c.asymp_factor);
-  if (fs & B_ISO) r = __dmul_rn(r, (double)c.iso_factor);
-  r = __dmul_rn(r, (double)vl);
-  double q = (double)rs;
-  if (fg & B_QUAR) q = __dmul_rn(q, (double)c.quar_factor);
-  q = __dmul_rn(q, __dsub_rn(1.0, (double)si));
-  const double F = K.factor[(((int64_t)c.sim * K.npts_max + t) * K.n_layers_max + c.layer) * K.nv_max + v];
-  double p = __dmul_rn(__dmul_rn(__dmul_rn(F, (double)lb), r), q);
-  if (p >= 1.0) {
+  ff r{rt, 0.0f};
+  if (fs & B_QUAR) r = ff_mul_f(r, c.quar_factor);
+  if (!(fs & B_SYMP)) r = ff_mul_f(r, c.asymp_factor);
+  if (fs & B_ISO) r = ff_mul_f(r, c.iso_factor);
+  r = ff_mul_f(r, vl);
+  ff q{rs, 0.0f};
+  if (fg & B_QUAR) q = ff_mul_f(q, c.quar_factor);
+  q = ff_mul(q, two_sum(1.0f, -si));
+  const float* Fp = K.factor + 2 * ((((int64_t)c.sim * K.npts_max + t) * K.n_layers_max + c.layer) * K.nv_max + v);
+  ff p = ff_mul(ff_mul(ff_mul_f(ff{Fp[0], Fp[1]}, lb), r), q);
+  if (p.hi > 1.0f || (p.hi == 1.0f && p.lo >= 0.0f)) {
     if (hit) {  // certain transmission: log p = 0, no sensitivity; the target is surely infected
       atomicAdd(K.logq + g, -INFINITY);
       return;
     }
-    p = (double)p32;  // not infected, so p32 < 1: p crossed 1 only by rounding
+    p = ff{p32, 0.0f};  // not infected, so p32 < 1: p crossed 1 only by rounding
   }
-  const double l1m = log1p(-p);
-  const double odds = __ddiv_rn(p, __dsub_rn(1.0, p));
-  acc.ll += hit ? log(p) : l1m;
-  acc.g += hit ? 1.0 : -odds;
-  atomicAdd(K.logq + g, l1m);
-  if (K.g_exp) atomicAdd(K.w + (int64_t)c.layer * st.n + g, odds);
+  ff om = two_sum(1.0f, -p.hi);  // 1 - p, exact in float-float
+  om = fast_two_sum(om.hi, __fsub_rn(om.lo, p.lo));
+  const ff l1m = ff_log_ff(om);
+  const ff odds = ff_div(p, om);
+  if (hit) {
+    acc.ll = ff_add(acc.ll, ff_log_ff(p));
+    acc.g = ff_add(acc.g, ff{1.0f, 0.0f});
+  } else {
+    acc.ll = ff_add(acc.ll, l1m);
+    acc.g = ff_add(acc.g, ff{-odds.hi, -odds.lo});
+  }
+  atomicAdd(K.logq + g, ff_to_d(l1m));
+  if (K.g_exp) atomicAdd(K.w + (int64_t)c.layer * st.n + g, ff_to_d(odds));
 }
 
 // compute_trans_sus folded into compute_infections for one direction s -> g
@@ -690,15 +716,20 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
         b[j] = e < e1 ? p2[e] : off;
       }
     }
-    Roles ra[EDGE_VEC], rb[EDGE_VEC];
+    // sources first (every edge, L1-resident bitmap), then the other endpoint's
+    // target bit only where one endpoint is a source; roles are exclusive, so
+    // an edge has at most one candidate direction
+    uint32_t sa[EDGE_VEC], sb[EDGE_VEC];
 #pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) { ra[j] = role_of(st.roles, a[j]); rb[j] = role_of(st.roles, b[j]); }
+    for (int j = 0; j < EDGE_VEC; ++j) { sa[j] = src_bit(st.roles, a[j]); sb[j] = src_bit(st.roles, b[j]); }
 #pragma unroll
     for (int j = 0; j < EDGE_VEC; ++j) {
       const bool in = eb + j < e1;
       const uint32_t m = (uint32_t)(eb + j - e0) << 1;
-      queue_push(q, qn, in && (ra[j].src & rb[j].tgt), a[j], b[j], m);
-      queue_push(q, qn, in && (rb[j].src & ra[j].tgt), b[j], a[j], m | 1u);
+      const bool d1 = sb[j] != 0u;  // direction p2 -> p1
+      bool cand = false;
+      if (in && (sa[j] | sb[j])) cand = tgt_bit(st, d1 ? a[j] : b[j]) != 0u;
+      queue_push(q, qn, cand, d1 ? b[j] : a[j], d1 ? a[j] : b[j], m | (d1 ? 1u : 0u));
     }
     if (qn > EQ_CAP - EQ_ROUND) {
       queue_drain<LIK>(st, c, t, e0, q, qn, acc);
@@ -708,7 +739,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   if (qn > 0) queue_drain<LIK>(st, c, t, e0, q, qn, acc);
   if (LIK) {  // the tile's sums: one sim, one layer
     __shared__ double s_acc[EDGE_THREADS / 32][2];
-    const double a = warp_sum_d(acc.ll), b = warp_sum_d(acc.g);
+    const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) { s_acc[warp][0] = a; s_acc[warp][1] = b; }
     __syncthreads();
@@ -966,7 +997,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   }
   st.flags[i] = f;
   // no longer a target for the rest of the day (matters for infections before the edge pass)
-  atomicAnd(st.roles + 2 * (i >> 5) + 1, ~(1u << (i & 31)));
+  atomicAnd(st.roles + roles_words(st) + (i >> 5), ~(1u << (i & 31)));
 }
 
 __device__ __forceinline__ int sim_of(const covgpu_state& st, int64_t i) {

@@ -78,6 +78,8 @@ __device__ __forceinline__ void box_muller(uint32_t wa, uint32_t wb, double& z0,
 __device__ __forceinline__ float f32nan() { return __int_as_float(0x7fc00000); }
 __device__ __forceinline__ bool defined(float x) { return !isnan(x); }
 __device__ __forceinline__ float* date_row(const covgpu_state& st, int d) { return st.dates + (int64_t)d * st.n; }
+// words of each role bitmap (source bitmap first, then target bitmap)
+__device__ __forceinline__ int64_t roles_words(const covgpu_state& st) { return (st.n + 31) >> 5; }
 __device__ __forceinline__ float* dur_row(const covgpu_state& st, int d) { return st.durs + (int64_t)d * st.n; }
 
 // utils.py:156-236: a sample that is a function of one standard normal z

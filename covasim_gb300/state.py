@@ -9,8 +9,8 @@ Layout in HBM (``n`` = total agents, each sim starting at a multiple of 32):
 * int32[n]: n_infections, n_breakthroughs, t_nab_event, vaccine_source
 * ``sus_imm``/``symp_imm``/``sev_imm`` float32[nv_max, n]
 * ``dates`` float32[19, n], ``durs`` float32[5, n] (NaN = undefined)
-* per-day working buffers: viral_load float32[n], roles uint32[2, n/32] (source and
-  target bitmaps, interleaved per 32 agents), claim uint64[n], event list, infection log
+* per-day working buffers: viral_load float32[n], roles uint32[2, n/32] (source
+  bitmap, then target bitmap), claim uint64[n], event list, infection log
 * contact layers: one (p1, p2[, beta]) segment per (sim, layer), int32 global agent
   indices sorted by p1; dynamic layers store no edges (redrawn from Philox each day)
 
@@ -522,7 +522,7 @@ class BatchState:
             dev = self.device
             f64 = torch.float64
             self.lik = dict(dims=(T, Lm, V), grad=False,
-                            factor=torch.zeros((S, T, Lm, V), dtype=f64, device=dev),
+                            factor=torch.zeros((S, T, Lm, V, 2), dtype=torch.float32, device=dev),
                             ll=torch.zeros((S, T), dtype=f64, device=dev),
                             expected=torch.zeros((S, T), dtype=f64, device=dev),
                             g_ll=torch.zeros((S, T, Lm), dtype=f64, device=dev),
@@ -539,11 +539,15 @@ class BatchState:
         self._refresh_state()
 
     def set_lik_factor(self, factor, sim=0):
-        """F[t][layer][variant] of one sim (float64, see covgpu_lik)."""
-        f = torch.as_tensor(np.asarray(factor, dtype=np.float64))
+        """F[t][layer][variant] of one sim (float64, see covgpu_lik), stored as
+        float pairs (hi, lo)."""
+        f = np.asarray(factor, dtype=np.float64)
+        hi = f.astype(np.float32)
+        lo = (f - hi.astype(np.float64)).astype(np.float32)
+        pair = torch.from_numpy(np.stack([hi, lo], axis=-1))
         T, Lm, V = f.shape
         self.lik['factor'][sim].zero_()
-        self.lik['factor'][sim, :T, :Lm, :V].copy_(f)
+        self.lik['factor'][sim, :T, :Lm, :V].copy_(pair)
 
     def zero_lik(self):
         for k in ('ll', 'expected', 'g_ll', 'g_exp', 'logq', 'w'):

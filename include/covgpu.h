@@ -191,7 +191,8 @@ typedef struct covgpu_log_rec { int32_t source; int32_t target; int32_t day; int
  * likelihood passes off). Every exposed direction source -> target of day t
  * (the candidates of the edge pass) has
  *   p = F[t][layer][variant] * edge beta * rel_trans' * rel_sus'
- * in float64, with rel_trans' = rel_trans * quar/asymp/iso factors * viral
+ * (float-float, ~2^-44 relative, capped at 1; GB300's float64 rate is a small
+ * fraction of its float32 rate), with rel_trans' = rel_trans * quar/asymp/iso factors * viral
  * load and rel_sus' = rel_sus * quar factor * (1 - sus_imm) as in
  * compute_trans_sus (utils.py:82-90) but without beta_layer, which F holds
  * together with beta, rel_beta and the variant's rel_beta. Its outcome is
@@ -202,7 +203,8 @@ typedef struct covgpu_log_rec { int32_t source; int32_t target; int32_t day; int
  *   g_ll     = sum of (infecting ? 1 : -p / (1 - p))
  *   g_exp    = sum over targets of prod(1 - p) * sum over the layer's directions of p / (1 - p). */
 typedef struct covgpu_lik {
-  const double* factor;           /* [n_sims][npts_max][n_layers_max][nv_max]       */
+  const float* factor;            /* [n_sims][npts_max][n_layers_max][nv_max][2]:
+                                     F as float pairs (hi, lo), hi + lo = F to 2^-48 */
   double* ll;                     /* [n_sims][npts_max]                             */
   double* expected;               /* [n_sims][npts_max]                             */
   double* g_ll;                   /* [n_sims][npts_max][n_layers_max] or NULL       */
@@ -239,7 +241,7 @@ typedef struct covgpu_state {
   float* durs;                    /* [COVGPU_N_DURS][n]                              */
   /* per-day working buffers */
   float* viral_load;              /* [n]                                             */
-  uint32_t* roles;                /* [2 * ceil(n/32)]: source word, target word      */
+  uint32_t* roles;                /* [2][ceil(n/32)]: source bitmap, target bitmap    */
   uint64_t* claim;                /* [n] first-infector claim (day-tagged)           */
   covgpu_event* events;           /* [event_capacity]                                */
   int64_t event_capacity;
