@@ -57,6 +57,8 @@ def parse():
     ap.add_argument('--batch', type=int, default=16, help='sims of the batched measurement (0: skip)')
     ap.add_argument('--no-adjoint', action='store_true', help='skip the forward/adjoint cost measurement')
     ap.add_argument('--edge-tile', default='auto', help="edge-pass tile (1024/2048/4096/8192) or 'auto' (autotuner)")
+    ap.add_argument('--gpu-population', action='store_true',
+                    help='large / batch256 workloads: build the populations on the device')
     ap.add_argument('--workload', default='hybrid1m', choices=['hybrid1m', 'large', 'batch256'],
                     help='hybrid1m: the headline run; large: 20M-agent hybrid, 3 variants, testing and tracing, '
                          '365 days; batch256: 256 random-population sims of 10k-500k agents, batched vs one by one')
@@ -64,6 +66,9 @@ def parse():
     ap.add_argument('--profile-run', action='store_true',
                     help='run one sim of --pop-size agents for --days days, one launch per kernel (no graph), '
                          'for profilers, and exit')
+    ap.add_argument('--profile-testing', action='store_true',
+                    help='profile run: with test_prob(symp_prob=0.1), contact_tracing(trace_probs=0.5) and the '
+                         'likelihood passes, so that every per-day kernel runs')
     return ap.parse_args()
 
 
@@ -536,7 +541,8 @@ def large_arm(args, n=20_000_000, days=365):
                           cv.variant(dict(rel_beta=1.7), days=120, n_imports=100, label='v1.7')],
                 interventions=[cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)])
     t0 = time.perf_counter()
-    sim = cv.Sim(pars, edge_tile=4096 if args.edge_tile == 'auto' else int(args.edge_tile))
+    sim = cv.Sim(pars, edge_tile=4096 if args.edge_tile == 'auto' else int(args.edge_tile),
+                 gpu_population=args.gpu_population)
     sim.initialize()
     init_s = time.perf_counter() - t0
     st = sim.state
@@ -565,6 +571,7 @@ def large_arm(args, n=20_000_000, days=365):
           f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), waning, test_prob(symp_prob=0.1), '
           f'contact_tracing(trace_probs=0.5), {days} days',
           {'edge_evaluations_per_s': round(2 * e_all * days * args.steps / el, 1), 'init_s': round(init_s, 1),
+           'population': 'device' if args.gpu_population else 'host',
            'cum_infections': float(res['new_infections'].sum() + sim['pop_infected']),
            'cum_tests': float(res['new_tests'].sum()), 'cum_quarantined': float(res['new_quarantined'].sum()),
            'clocks': clk})
@@ -590,7 +597,8 @@ def batch_arm(args, n_sims=256, days=120):
     def make(k):
         return cv.Sim(dict(pop_size=int(sizes[k]), pop_type='random', contacts=dict(a=int(contacts[k])),
                            beta=float(betas[k]), n_days=days, rand_seed=100 + k, pop_infected=20,
-                           interventions=[cv.change_beta(days=30, changes=float(changes[k]))]))
+                           interventions=[cv.change_beta(days=30, changes=float(changes[k]))]),
+                      gpu_population=args.gpu_population)
     t0 = time.perf_counter()
     sims = [make(k) for k in range(n_sims)]
     batch = cv.BatchSim(sims, edge_tile=args.edge_tile).initialize()
@@ -644,7 +652,8 @@ def batch_arm(args, n_sims=256, days=120):
           f'beta U[0.010,0.025], change_beta day 30 x U[0.3,1], {days} days',
           {'one_by_one': {'value': round(agent_days / t_single, 1), 'ms_per_step': round(1e3 * t_single, 3)},
            'batched_over_one_by_one': round(t_single / t_batch, 3), 'every_sim_equals_its_own_run': same,
-           'edge_tile': st.edge_tile, 'init_s': round(init_s, 1), 'clocks': clk})
+           'edge_tile': st.edge_tile, 'init_s': round(init_s, 1),
+           'population': 'device' if args.gpu_population else 'host', 'clocks': clk})
 
 
 def choose_seed(sim):
@@ -656,10 +665,23 @@ def profile_run(args):
     """One ungraphed run (kernels launched one by one) for ncu captures."""
     import torch
     import covasim_gb300 as cv
-    sim = cv.Sim(sim_pars(args, 1))
+    pars = sim_pars(args, 1)
+    if args.profile_testing:
+        from covasim_gb300.adjoint import Parameters
+        pars['interventions'] = [cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)]
+        sim = cv.Sim(pars)
+        sim.initialize()
+        st = sim.state
+        st.enable_lik(grad=True)
+        params = Parameters(sim)
+        st.set_lik_factor(params.factor(params.theta0))
+        st.zero_lik()
+    else:
+        sim = cv.Sim(pars)
     sim.run(use_graph=False)
     torch.cuda.synchronize()
     print(json.dumps({'profile_run': True, 'pop_size': args.pop_size, 'days': args.days,
+                      'testing': bool(args.profile_testing),
                       'cum_infections': float(sim.results['cum_infections'].values[-1])}))
 
 

@@ -163,6 +163,20 @@ def lib():
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
+        L.covgpu_pop_scan_scratch.argtypes = [i64]
+        L.covgpu_pop_scan_scratch.restype = i64
+        f64 = C.c_double
+        L.covgpu_pop_ages.argtypes = [i64, vp, vp, vp, i32, u64, vp, vp, vp]
+        L.covgpu_pop_members.argtypes = [i64, vp, f32, f32, vp, vp, vp, vp, vp]
+        L.covgpu_pop_random_counts.argtypes = [i64, f64, f64, u64, i32, vp, vp, vp, vp, vp]
+        L.covgpu_pop_random_fill.argtypes = [i64, vp, vp, u64, i32, vp, vp, vp]
+        L.covgpu_pop_cluster_sizes.argtypes = [i64, f64, u64, i32, vp, vp, vp, vp, vp]
+        L.covgpu_pop_cluster_counts.argtypes = [i64, i64, vp, vp, vp, vp, vp]
+        L.covgpu_pop_cluster_fill.argtypes = [i64, vp, vp, vp, vp]
+        L.covgpu_pop_prognoses.argtypes = [i64, vp, vp, i32, vp, i32, f64, f64, f64, u64, vp, vp, vp, vp, vp, vp, vp,
+                                           vp]
+        for name in POP_FUNCS:
+            getattr(L, name).restype = C.c_int
         for name in ('covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections', 'covgpu_agent_step',
                      'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_materialize',
                      'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_targets'):
@@ -193,7 +207,10 @@ def abi_layout():
     return list(out[:m]), mine
 
 
+POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts', 'covgpu_pop_random_fill',
+             'covgpu_pop_cluster_sizes', 'covgpu_pop_cluster_counts', 'covgpu_pop_cluster_fill', 'covgpu_pop_prognoses']
+
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
             'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
-            'covgpu_lik_targets']
+            'covgpu_lik_targets', 'covgpu_pop_scan_scratch'] + POP_FUNCS

@@ -60,7 +60,8 @@ class BatchSim:
             cvimm.init_immunity(s.pars, s.npts)
             s.init_results()
             s.init_interventions()
-            spec, popdict, person = build_spec(s.pars, s.popdict, getattr(s, '_person', None), s['interventions'])
+            spec, popdict, person = build_spec(s.pars, s.popdict, getattr(s, '_person', None), s['interventions'],
+                                               gpu_population=getattr(s, 'gpu_population', False))
             s.popdict, s._person, s.spec = popdict, person, spec
             specs.append(spec)
         npts = {sp.npts for sp in specs}

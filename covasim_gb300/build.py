@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, 'csrc')
 INCLUDE = os.path.join(ROOT, 'include')
 LIB_NAME = 'libcovgpu.so'
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ['covgpu.cu']
+SOURCES = ['covgpu.cu', 'covgpu_pop.cu']
+OBJ_DIR = os.path.join(HERE, '_build')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 
@@ -28,11 +29,12 @@ def nvcc_path():
 
 
 def nvcc_flags(extra=()):
-    return ['-O3', '-std=c++17', '-lineinfo', '-fmad=false', '--shared', '-Xcompiler', '-fPIC',
+    return ['-O3', '-std=c++17', '-lineinfo', '-fmad=false', '-Xcompiler', '-fPIC',
             '-I', INCLUDE, '-I', CSRC, *ARCH, *extra]
 
 
 def build(verbose=False, force=False, extra=()):
+    """Compile each translation unit in parallel (nvcc -c), then link the shared library."""
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, f) for f in ('covgpu_device.cuh', 'covgpu_ff.cuh', 'covgpu_tables.h')]
     deps += [os.path.join(INCLUDE, 'covgpu.h'), __file__]
@@ -40,15 +42,29 @@ def build(verbose=False, force=False, extra=()):
         lib_m = os.path.getmtime(LIB_PATH)
         if all(os.path.getmtime(d) <= lib_m for d in deps):
             return LIB_PATH
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    nvcc = nvcc_path()
+    objs, procs = [], []
+    for src in srcs:
+        obj = os.path.join(OBJ_DIR, os.path.basename(src) + '.o')
+        cmd = [nvcc, *nvcc_flags(extra), '-c', '-o', obj, src]
+        if verbose:
+            print(' '.join(cmd))
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
+        objs.append(obj)
+    for cmd, p in procs:
+        out, err = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f'nvcc failed ({p.returncode}): {" ".join(cmd)}\n{out}\n{err}')
+        if verbose and (out or err):
+            print(out, err)
     tmp = LIB_PATH + '.tmp'
-    cmd = [nvcc_path(), *nvcc_flags(extra), '-o', tmp, *srcs, '-lcudart']
+    cmd = [nvcc, '--shared', *ARCH, '-o', tmp, *objs, '-lcudart']
     if verbose:
         print(' '.join(cmd))
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f'nvcc failed ({res.returncode}):\n{res.stdout}\n{res.stderr}')
-    if verbose and (res.stdout or res.stderr):
-        print(res.stdout, res.stderr)
+        raise RuntimeError(f'nvcc link failed ({res.returncode}):\n{res.stdout}\n{res.stderr}')
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

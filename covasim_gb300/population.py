@@ -7,14 +7,16 @@ household clusters of Poisson(h) size with all pairs inside each cluster
 (population.py:287-329), and the hybrid school/work/community layers
 (population.py:332-364). Draws come from a numpy ``Generator`` (PCG64); the
 loops over agents of the reference become array operations. Population
-building runs once per sim, before the day loop.
+building runs once per sim, before the day loop. ``make_randpop_device`` and
+``set_prognoses_device`` build the same distributions on the GPU
+(covgpu_pop.cu), with Philox draws.
 """
 import numpy as np
 
 from . import defaults as cvd
 
 __all__ = ['make_randpop', 'make_random_contacts', 'make_microstructured_contacts', 'make_hybrid_contacts',
-           'sample_ages']
+           'sample_ages', 'make_randpop_device', 'set_prognoses_device']
 
 
 def _rng(rng):
@@ -146,4 +148,141 @@ def set_prognoses(age, pars, rng):
     else:
         raise NotImplementedError(f'beta_dist "{bd["dist"]}"')
     out['rel_trans'] = (progs['trans_ORs'][inds] * draws).astype(cvd.default_float)
+    return out
+
+
+# ----------------------------------------------------------------------------- on the device
+def _dev_call(name, *args):
+    from . import _lib as L
+    from .state import _stream
+    L.call(name, *args, _stream())
+
+
+def _dev_scan_scratch(n, device):
+    import torch
+    from . import _lib as L
+    return torch.empty(int(L.lib().covgpu_pop_scan_scratch(int(n))) + 1, dtype=torch.int64, device=device)
+
+
+def _dev_random_layer(n_members, mean, seed, layer, status, device, members=None, dispersion=None):
+    """population.py:241-284 on the device: (p1, p2) int32 tensors, p1 ascending."""
+    import torch
+    if n_members == 0:
+        z = torch.zeros(0, dtype=torch.int32, device=device)
+        return z, z.clone()
+    counts = torch.empty(n_members, dtype=torch.int64, device=device)
+    offsets = torch.empty(n_members + 1, dtype=torch.int64, device=device)
+    _dev_call('covgpu_pop_random_counts', n_members, float(mean), float(dispersion or 0.0), seed, layer,
+              counts.data_ptr(), offsets.data_ptr(), _dev_scan_scratch(n_members, device).data_ptr(),
+              status.data_ptr())
+    n_edges = int(offsets[-1].item())
+    p1 = torch.empty(n_edges, dtype=torch.int32, device=device)
+    p2 = torch.empty(n_edges, dtype=torch.int32, device=device)
+    if n_edges:
+        _dev_call('covgpu_pop_random_fill', n_members, None if members is None else members.data_ptr(),
+                  offsets.data_ptr(), seed, layer, p1.data_ptr(), p2.data_ptr())
+    return p1, p2
+
+
+def _dev_clusters(pop_size, mean, seed, layer, status, device):
+    """population.py:287-329 on the device: every pair inside consecutive Poisson(mean) clusters."""
+    import torch
+    k = int(pop_size / max(float(mean), 0.5) * 1.2) + 64
+    while True:
+        sizes = torch.empty(k, dtype=torch.int64, device=device)
+        starts = torch.empty(k + 1, dtype=torch.int64, device=device)
+        _dev_call('covgpu_pop_cluster_sizes', k, float(mean), seed, layer, sizes.data_ptr(), starts.data_ptr(),
+                  _dev_scan_scratch(k, device).data_ptr(), status.data_ptr())
+        if int(starts[-1].item()) >= pop_size:
+            break
+        k *= 2  # more clusters, same draws for the first k (keyed by cluster index)
+    counts = torch.empty(pop_size, dtype=torch.int64, device=device)
+    offsets = torch.empty(pop_size + 1, dtype=torch.int64, device=device)
+    _dev_call('covgpu_pop_cluster_counts', pop_size, k, starts.data_ptr(), counts.data_ptr(), offsets.data_ptr(),
+              _dev_scan_scratch(pop_size, device).data_ptr())
+    n_edges = int(offsets[-1].item())
+    p1 = torch.empty(n_edges, dtype=torch.int32, device=device)
+    p2 = torch.empty(n_edges, dtype=torch.int32, device=device)
+    if n_edges:
+        _dev_call('covgpu_pop_cluster_fill', pop_size, offsets.data_ptr(), p1.data_ptr(), p2.data_ptr())
+    return p1, p2
+
+
+def make_randpop_device(pars, seed, device='cuda', sex_ratio=0.5):
+    """``make_randpop`` built on the device (covgpu_pop_*): the same distributions,
+    draws from Philox keyed by ``seed``; ages and sexes come back as numpy
+    arrays, the layers as device tensors (p1 ascending)."""
+    import torch
+    from . import _lib as L
+    if sex_ratio != 0.5:
+        raise NotImplementedError('the device generator draws sexes with ratio 0.5')
+    pop_size = int(pars['pop_size'])
+    seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    ad = np.asarray(cvd.default_age_data, dtype=float)
+    lo, width, cdf = ad[:, 0], ad[:, 1] + 1 - ad[:, 0], np.cumsum(ad[:, 2] / ad[:, 2].sum())
+    tabs = [torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(device) for x in (lo, width, cdf)]
+    age = torch.empty(pop_size, dtype=torch.float32, device=device)
+    sex = torch.empty(pop_size, dtype=torch.int32, device=device)
+    _dev_call('covgpu_pop_ages', pop_size, tabs[0].data_ptr(), tabs[1].data_ptr(), tabs[2].data_ptr(), len(ad), seed,
+              age.data_ptr(), sex.data_ptr())
+    contacts = {}
+    microstructure = pars['pop_type']
+    keys = list(pars['contacts'].keys())
+    if microstructure == 'random':
+        for li, (lkey, n) in enumerate(pars['contacts'].items()):
+            p1, p2 = _dev_random_layer(pop_size, n, seed, li, status, device)
+            contacts[lkey] = dict(p1=p1, p2=p2)
+    elif microstructure == 'hybrid':
+        cts = {**dict(h=4, s=20, w=20, c=20), **pars['contacts']}
+        p1, p2 = _dev_clusters(pop_size, cts['h'], seed, 0, status, device)
+        contacts['h'] = dict(p1=p1, p2=p2)
+        p1, p2 = _dev_random_layer(pop_size, cts['c'], seed, 3, status, device)
+        contacts['c'] = dict(p1=p1, p2=p2)
+        for li, (lkey, (a0, a1)) in ((1, ('s', (6, 22))), (2, ('w', (22, 65)))):
+            flags = torch.empty(pop_size, dtype=torch.int64, device=device)
+            pos = torch.empty(pop_size + 1, dtype=torch.int64, device=device)
+            members = torch.empty(pop_size, dtype=torch.int32, device=device)
+            _dev_call('covgpu_pop_members', pop_size, age.data_ptr(), float(a0), float(a1), flags.data_ptr(),
+                      pos.data_ptr(), _dev_scan_scratch(pop_size, device).data_ptr(), members.data_ptr())
+            m = int(pos[-1].item())
+            p1, p2 = _dev_random_layer(m, cts[lkey], seed, li, status, device, members=members[:m])
+            contacts[lkey] = dict(p1=p1, p2=p2)
+    else:
+        raise NotImplementedError(f'Microstructure type "{microstructure}" not found; choices are random or hybrid')
+    if int(status.item()) & L.TIMEOUT:
+        raise L.CovgpuError('population generation (a sampler ran out of tries)', L.TIMEOUT)
+    return dict(uid=np.arange(pop_size, dtype=cvd.default_int), age=age.cpu().numpy().astype(np.float64),
+                sex=sex.cpu().numpy(), contacts=contacts, layer_keys=keys, _age_device=age)
+
+
+def set_prognoses_device(age, pars, seed, device='cuda'):
+    """``set_prognoses`` on the device: dict of float32 device tensors."""
+    import torch
+    from . import _lib as L
+    age = age if torch.is_tensor(age) else torch.as_tensor(np.asarray(age, dtype=np.float32))
+    age = age.to(device, torch.float32).contiguous()
+    n = age.numel()
+    progs = pars['prognoses']
+    cut = torch.from_numpy(np.ascontiguousarray(progs['age_cutoffs'], dtype=np.float64)).to(device)
+    tabs = np.stack([progs['symp_probs'], progs['severe_probs'] * progs['comorbidities'], progs['crit_probs'],
+                     progs['death_probs'], progs['sus_ORs'], progs['trans_ORs']]).astype(np.float64)
+    tabs_d = torch.from_numpy(np.ascontiguousarray(tabs)).to(device)
+    bd = pars['beta_dist']
+    if bd['dist'] == 'neg_binomial':
+        code, p1, p2, step = 0, float(bd['par1']), float(bd['par2']), float(bd.get('step', 1))
+    elif bd['dist'] in ('lognormal', 'lognorm'):
+        code, p1, p2, step = 1, float(bd['par1']), float(bd['par2']), 1.0
+    else:
+        raise NotImplementedError(f'beta_dist "{bd["dist"]}" on the device')
+    out = {k: torch.empty(n, dtype=torch.float32, device=device)
+           for k in ('symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_sus', 'rel_trans')}
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    _dev_call('covgpu_pop_prognoses', n, age.data_ptr(), cut.data_ptr(), len(progs['age_cutoffs']), tabs_d.data_ptr(),
+              code, p1, p2, step, int(seed) & 0xFFFFFFFFFFFFFFFF, *(out[k].data_ptr() for k in
+                                                                  ('symp_prob', 'severe_prob', 'crit_prob',
+                                                                   'death_prob', 'rel_sus', 'rel_trans')),
+              status.data_ptr())
+    if int(status.item()) & L.TIMEOUT:
+        raise L.CovgpuError('prognoses (a sampler ran out of tries)', L.TIMEOUT)
     return out

@@ -37,6 +37,114 @@ class AlreadyRunError(RuntimeError):
     """sim.py:1550: the sim was asked to run past its end or to rerun."""
 
 
+# ----------------------------------------------------------------------------- reporting
+def yield_series(res):
+    """sim.py:853-869 on result arrays: (test_yield, rel_test_yield)."""
+    npts = len(res['new_tests'])
+    ty = np.zeros(npts)
+    rty = np.zeros(npts)
+    inds = np.nonzero(res['new_tests'])[0]
+    ty[inds] = res['new_diagnoses'][inds] / res['new_tests'][inds]
+    inds = np.nonzero(res['n_infectious'])[0]
+    denom = res['n_infectious'][inds] / (res['n_alive'][inds] - res['cum_diagnoses'][inds])
+    rty[inds] = ty[inds] / denom
+    return ty, rty
+
+
+def doubling_series(cum, window=3, max_doubling_time=30):
+    """sim.py:872-895."""
+    cum = np.asarray(cum, dtype=float)
+    now, prev = cum[window:], cum[:-window]
+    use = (prev > 0) & (now > prev)
+    out = np.full(len(cum), np.nan)
+    out[window:][use] = np.minimum(window * np.log(2) / np.log(now[use] / prev[use]), max_doubling_time)
+    return out
+
+
+def mean_infectious_duration(d_rec, d_dead, d_inf):
+    """sim.py:920-932: mean of the outcome dates minus mean of the infectious dates,
+    over the agents with a recovery date then those with a death date (numpy
+    arrays or device tensors; sums in float64)."""
+    if torch.is_tensor(d_rec):
+        m_rec, m_dead = ~torch.isnan(d_rec), ~torch.isnan(d_dead)
+        n_out = int(m_rec.sum().item() + m_dead.sum().item())
+        if not n_out:
+            return 0.0
+        s_out = float(d_rec[m_rec].double().sum() + d_dead[m_dead].double().sum())
+        s_inf = float(d_inf[m_rec].double().sum() + d_inf[m_dead].double().sum())
+    else:
+        m_rec, m_dead = ~np.isnan(d_rec), ~np.isnan(d_dead)
+        n_out = int(m_rec.sum() + m_dead.sum())
+        if not n_out:
+            return 0.0
+        s_out = float(d_rec[m_rec].astype(np.float64).sum() + d_dead[m_dead].astype(np.float64).sum())
+        s_inf = float(d_inf[m_rec].astype(np.float64).sum() + d_inf[m_dead].astype(np.float64).sum())
+    return s_out / n_out - s_inf / n_out
+
+
+def r_eff_daily(mean_inf, new_infections, n_imports, n_infectious, dur, smoothing=2):
+    """sim.py:934-951: mean infectious duration x new infections / infectious, smoothed."""
+    npts = len(new_infections)
+    new_inf = np.asarray(new_infections, dtype=float) - np.asarray(n_imports, dtype=float)
+    n_inf = np.asarray(n_infectious, dtype=float)
+    raw = mean_inf * np.divide(new_inf, n_inf, out=np.zeros(npts), where=n_inf > 0)
+    if len(raw) < 3:
+        return raw
+    initial = int(min(len(raw), dur['exp2inf']['par1'] + dur['asym2rec']['par1']))
+    for ind in range(initial):
+        raw[ind] = raw[ind:initial].mean()
+    values = _smooth(raw, smoothing)
+    values[:smoothing] = raw[:smoothing]
+    values[-smoothing:] = raw[-smoothing:]
+    return values
+
+
+def r_eff_window(npts, day_arrays, log_sources, window=7):
+    """sim.py:954-992: infections caused by the sources of each day (the day of
+    becoming infectious, or of recovery/death), averaged over ``window`` days."""
+    window = int(window)
+    n = len(day_arrays[0])
+    sources = np.zeros(npts)
+    source_day = np.full(n, -1, dtype=np.int64)
+    for t in range(npts):  # the last matching day wins, as in the reference's mapping
+        for d in day_arrays:
+            inds = np.nonzero(d == t)[0]
+            sources[t] += len(inds)
+            source_day[inds] = t
+    src = np.asarray(log_sources, dtype=np.int64)
+    src = src[src >= 0]
+    sd = source_day[src]
+    targets = np.bincount(sd[sd >= 0], minlength=npts).astype(float)[:npts]
+    r = np.divide(targets, sources, out=np.full(npts, np.nan), where=sources > 0)
+    num = np.nancumsum(r * sources)
+    num[window:] = num[window:] - num[:-window]
+    den = np.cumsum(sources)
+    den[window:] = den[window:] - den[:-window]
+    return np.divide(num, den, out=np.full(npts, np.nan), where=den > 0)
+
+
+def gen_time(sources, targets, date_exposed, date_symptomatic):
+    """sim.py:1004-1040 over the transmission records with a source."""
+    sources = np.asarray(sources, dtype=np.int64)
+    keep = sources >= 0
+    src, tgt = sources[keep], np.asarray(targets, dtype=np.int64)[keep]
+    i1 = (date_exposed[tgt] - date_exposed[src]).astype(np.float64)
+    ok = np.isfinite(date_symptomatic[src]) & np.isfinite(date_symptomatic[tgt])
+    i2 = (date_symptomatic[tgt][ok] - date_symptomatic[src][ok]).astype(np.float64)
+    return {'true': np.mean(i1), 'true_std': np.std(i1), 'clinical': np.mean(i2), 'clinical_std': np.std(i2)}
+
+
+def _smooth(data, repeats):
+    """Smoothing used by compute_r_eff: ``repeats`` convolutions with the kernel
+    [1/4, 1/2, 1/4] (same length). The reference calls ``sc.smooth`` of sciris
+    (pinned 1.0.2, not in the reference tree); this is that published algorithm."""
+    out = np.array(data, dtype=float)
+    kernel = np.array([0.25, 0.5, 0.25])
+    for _ in range(int(repeats)):
+        out = np.convolve(out, kernel, mode='same')
+    return out
+
+
 class Result:
     """A per-day result series (covasim/base.py:117-193), array-like."""
 
@@ -94,14 +202,22 @@ def _layers_from_popdict(pars, popdict):
     return layers
 
 
-def build_spec(pars, popdict=None, person=None, interventions=None):
-    """Population + prognoses + per-day tables of one sim -> (SimSpec, popdict, person)."""
+def build_spec(pars, popdict=None, person=None, interventions=None, gpu_population=False):
+    """Population + prognoses + per-day tables of one sim -> (SimSpec, popdict, person).
+    With ``gpu_population`` a missing population is built on the device."""
     seed = int(pars['rand_seed'])
     npts = int(pars['n_days']) + 1
     if popdict is None:
-        popdict = cvpop.make_randpop(pars, rng=np.random.default_rng([seed, POPULATION_TAG]))
+        if gpu_population:
+            popdict = cvpop.make_randpop_device(pars, seed)
+        else:
+            popdict = cvpop.make_randpop(pars, rng=np.random.default_rng([seed, POPULATION_TAG]))
     if person is None:
-        person = cvpop.set_prognoses(np.asarray(popdict['age']), pars, np.random.default_rng([seed, PROGNOSIS_TAG]))
+        if gpu_population and popdict.get('_age_device') is not None:
+            person = cvpop.set_prognoses_device(popdict['_age_device'], pars, seed)
+        else:
+            person = cvpop.set_prognoses(np.asarray(popdict['age']), pars,
+                                         np.random.default_rng([seed, PROGNOSIS_TAG]))
     layers = _layers_from_popdict(pars, popdict)
     keys = [ly['key'] for ly in layers]
     betas = {'overall': pars['beta'], **{k: pars['beta_layer'][k] for k in keys}}
@@ -128,10 +244,14 @@ class Sim:
         edge_tile (int or 'auto'): edges per edge-pass block (1024, 2048, 4096 or
             8192; default 4096); 'auto' times whole runs with each at initialize
             (``covasim_gb300.autotune``, cached per workload)
+        gpu_population (bool): build the population (ages, layers, prognoses) on
+            the device instead of the host (same distributions, Philox draws)
     """
 
-    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, edge_tile=None, **kwargs):
+    def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, edge_tile=None,
+                 gpu_population=False, **kwargs):
         self.label = label
+        self.gpu_population = gpu_population  # build a missing population on the device
         self.edge_tile = edge_tile  # edges per edge-pass block; 'auto': autotuned at initialize
         self.pars = cvpar.make_pars()
         self.update_pars(pars, **kwargs)
@@ -231,7 +351,7 @@ class Sim:
         self.init_results()
         self.init_interventions()
         spec, popdict, person = build_spec(self.pars, self.popdict, getattr(self, '_person', None),
-                                           self['interventions'])
+                                           self['interventions'], gpu_population=self.gpu_population)
         self.popdict = popdict
         self._person = person
         self.spec = spec
@@ -267,7 +387,8 @@ class Sim:
         for key in cvd.result_stocks:
             self.results[f'n_{key}'] = Result(f'n_{key}', npts)
         for key in ('n_imports', 'n_alive', 'n_naive', 'n_preinfectious', 'n_removed', 'prevalence', 'incidence',
-                    'frac_vaccinated', 'pop_nabs', 'pop_protection', 'pop_symp_protection'):
+                    'frac_vaccinated', 'pop_nabs', 'pop_protection', 'pop_symp_protection', 'r_eff', 'doubling_time',
+                    'test_yield', 'rel_test_yield'):
             self.results[key] = Result(key, npts)
         self.results['variant'] = {}
         for key in cvd.result_flows_by_variant:
@@ -405,9 +526,16 @@ class Sim:
         self.results['variant']['cum_infections_by_variant'].values[0] += self['pop_infected']
         self.results_ready = True
         self.t -= 1
-        self.compute_states()
+        self.compute_results()
         self.summary = {k: v.values[-1] for k, v in self.results.items() if isinstance(v, Result)}
         return self
+
+    def compute_results(self):
+        """sim.py:818-825 (the summary is formed by finalize)."""
+        self.compute_states()
+        self.compute_yield()
+        self.compute_doubling()
+        self.compute_r_eff()
 
     def compute_states(self):
         """sim.py:828-850."""
@@ -423,6 +551,47 @@ class Sim:
             res['prevalence'].values[:] = res['n_exposed'].values / res['n_alive'].values
             res['incidence'].values[:] = res['new_infections'].values / res['n_susceptible'].values
             res['frac_vaccinated'].values[:] = res['n_vaccinated'].values / res['n_alive'].values
+
+    def compute_yield(self):
+        """sim.py:853-869: test positivity and its ratio to the prevalence among the undiagnosed."""
+        res = self.results
+        ty, rty = yield_series({k: res[k].values for k in ('new_tests', 'new_diagnoses', 'n_infectious', 'n_alive',
+                                                            'cum_diagnoses')})
+        res['test_yield'].values[:] = ty
+        res['rel_test_yield'].values[:] = rty
+
+    def compute_doubling(self, window=3, max_doubling_time=30):
+        """sim.py:872-895: doubling time of cumulative infections over ``window`` days."""
+        self.results['doubling_time'].values[:] = doubling_series(self.results['cum_infections'].values, window,
+                                                                  max_doubling_time)
+        return self.results['doubling_time'].values
+
+    def compute_r_eff(self, method='daily', smoothing=2, window=7):
+        """sim.py:898-1001: effective reproduction number (methods 'daily',
+        'infectious', 'outcome'); the date means and day counts come from the
+        device arrays."""
+        res = self.results
+        if method == 'daily':
+            g = self.people.gpu
+            mean_inf = mean_infectious_duration(g('date_recovered'), g('date_dead'), g('date_infectious'))
+            values = r_eff_daily(mean_inf, res['new_infections'].values, res['n_imports'].values,
+                                 res['n_infectious'].values, self['dur'], smoothing)
+        elif method in ('infectious', 'outcome'):
+            keys = ['date_infectious'] if method == 'infectious' else ['date_recovered', 'date_dead']
+            log = self.state.infection_log(0)
+            values = r_eff_window(self.npts, [self.people[k] for k in keys], log[:, 0], window)
+        else:
+            raise ValueError(f'Method must be "daily", "infectious", or "outcome", not "{method}"')
+        res['r_eff'].values[:] = values
+        return res['r_eff'].values
+
+    def compute_gen_time(self):
+        """sim.py:1004-1040: mean and sd of the exposure-to-exposure and
+        symptom-to-symptom intervals over the transmission log."""
+        log = self.state.infection_log(0)
+        self.results['gen_time'] = gen_time(log[:, 0], log[:, 1], self.people['date_exposed'],
+                                            self.people['date_symptomatic'])
+        return self.results['gen_time']
 
     def raw_results(self):
         """Per-day device results before finalize's post-processing (stocks as counted)."""

@@ -288,9 +288,9 @@ class BatchState:
                         raise ValueError(f'layer {ly["key"]}: p1 must be sorted')
                     if min(int(lo1), int(lo2)) < 0 or max(int(hi1), int(hi2)) >= sp.n:
                         raise ValueError(f'layer {ly["key"]}: agent index out of range')
-                    if off:
-                        tp1 += off
-                        tp2 += off
+                    if off:  # out of place: .to() returns the caller's tensor when it is already on the device
+                        tp1 = tp1 + off
+                        tp2 = tp2 + off
                     rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
                     keep += [tp1, tp2]
                     b = ly.get('beta')

@@ -329,6 +329,57 @@ int covgpu_infections_noalloc(float beta, const int32_t* p1, const int32_t* p2, 
                               int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
                               int32_t* status, void* stream);
 
+/* ---- synthetic populations on the device --------------------------------
+ * The distributions of covasim/population.py and people.py:139-161, each
+ * agent / member / cluster one thread, variable-length outputs placed by
+ * exclusive scans, draws from Philox keyed by (seed, purpose, layer, index).
+ * Every scan needs `scratch` of covgpu_pop_scan_scratch(n) int64 elements and
+ * writes n + 1 offsets (offsets[n] = total). Rejection samplers are bounded:
+ * an exhausted one stores COVGPU_TIMEOUT in *status. */
+int64_t covgpu_pop_scan_scratch(int64_t n);
+
+/* Ages and sexes (population.py:196-210): a bin by weight (bin_cdf: cumulative
+ * weights), then uniform in [bin_lo, bin_lo + bin_width); sex Bernoulli(0.5)
+ * (sex may be NULL). */
+int covgpu_pop_ages(int64_t n, const double* bin_lo, const double* bin_width, const double* bin_cdf, int32_t n_bins,
+                    uint64_t seed, float* age, int32_t* sex, void* stream);
+
+/* Agents with age_lo <= age < age_hi, ascending (population.py:353-354):
+ * flags [n], pos [n + 1] (pos[n] = number of members), members [n]. */
+int covgpu_pop_members(int64_t n, const float* age, float age_lo, float age_hi, int64_t* flags, int64_t* pos,
+                       int64_t* scratch, int32_t* members, void* stream);
+
+/* A random layer (population.py:241-284): partners per member
+ * round(X / 2) half to even, X ~ Poisson(mean) (dispersion <= 0) or negative
+ * binomial(mean, dispersion); counts [n_members], offsets [n_members + 1]. */
+int covgpu_pop_random_counts(int64_t n_members, double mean, double dispersion, uint64_t seed, int32_t layer,
+                             int64_t* counts, int64_t* offsets, int64_t* scratch, int32_t* status, void* stream);
+/* ... then the edges: p1 = the member (ascending), p2 uniform over the members
+ * (members NULL: agents 0..n_members-1). */
+int covgpu_pop_random_fill(int64_t n_members, const int32_t* members, const int64_t* offsets, uint64_t seed,
+                           int32_t layer, int32_t* p1, int32_t* p2, void* stream);
+
+/* Household clusters (population.py:287-329): n_clusters Poisson(mean) sizes
+ * and their starts [n_clusters + 1]; the caller checks starts[n_clusters] >= n
+ * (else draws more clusters). */
+int covgpu_pop_cluster_sizes(int64_t n_clusters, double mean, uint64_t seed, int32_t layer, int64_t* sizes,
+                             int64_t* starts, int64_t* scratch, int32_t* status, void* stream);
+/* pairs (i, j > i) per agent within its cluster (clusters cut at n): counts
+ * [n], offsets [n + 1]; then the edges. */
+int covgpu_pop_cluster_counts(int64_t n, int64_t n_clusters, const int64_t* starts, int64_t* counts,
+                              int64_t* offsets, int64_t* scratch, void* stream);
+int covgpu_pop_cluster_fill(int64_t n, const int64_t* offsets, int32_t* p1, int32_t* p2, void* stream);
+
+/* set_prognoses (people.py:139-161): the age bin (np.digitize over cutoffs)
+ * selects symp, severe (x comorbidity), crit, death probabilities and rel_sus
+ * from tables [6][n_bins] (float64: those five then trans_ORs); rel_trans =
+ * trans_OR * draw, draw negative binomial (trans_dist 0: mean par1,
+ * dispersion par2, in units of step) or lognormal (1: mean par1, sd par2). */
+int covgpu_pop_prognoses(int64_t n, const float* age, const double* cutoffs, int32_t n_bins, const double* tables,
+                         int32_t trans_dist, double par1, double par2, double step, uint64_t seed, float* symp,
+                         float* severe, float* crit, float* death, float* rel_sus, float* rel_trans, int32_t* status,
+                         void* stream);
+
 /* ---- fused per-day kernels over a batch of sims ------------------------- */
 
 /* One dense pass over every agent of every sim. With do_prev, first closes

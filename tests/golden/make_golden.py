@@ -21,6 +21,8 @@ Fixtures:
   ref_sims.npz         whole reference runs (inputs and daily results) for MT-mode replay
   ref_testing.npz      whole reference runs with test_prob + contact_tracing (inputs,
                        intervention arguments, daily results, final testing/quarantine state)
+  ref_reporting.npz    compute_yield / compute_doubling / compute_r_eff / compute_gen_time
+                       inputs and outputs on a reference run (sciris' smooth restated)
   ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
                        20k-agent random sim (60 days), reference code with MT19937 streams
 """
@@ -433,6 +435,70 @@ def make_testing_fixture(ref):
     print('ref_testing.npz written')
 
 
+class _Res:
+    """The part of the reference's Result the reporting methods use."""
+
+    def __init__(self, values):
+        self.values = np.asarray(values, dtype=np.float64)
+
+    def __getitem__(self, k):
+        return self.values[k]
+
+    def __setitem__(self, k, v):
+        self.values[k] = v
+
+
+def make_reporting_fixture(ref):
+    """Inputs and outputs of the reference's compute_yield, compute_doubling,
+    compute_r_eff (all three methods) and compute_gen_time (sim.py:853-1040) on
+    a whole reference run with testing; sciris' smooth is restated (sciris is
+    not installed)."""
+    from covasim_gb300.sim import _smooth
+    import types
+    pop_type, n, days, seed, waning, dyn, tp_kw, ct_kw = TESTING_CASES[0]
+    pars = ref.make_pars(pop_size=3000, n_days=60, pop_type=pop_type, rand_seed=seed, use_waning=waning)
+    pars['interventions'] = [ref.cvint.test_prob(**tp_kw), ref.cvint.contact_tracing(**ct_kw)]
+    sim = refload.RefSim(ref, pars).run()
+    r = sim.results
+    res = {k: _Res(v) for k, v in r.items() if k != 'variant'}
+    for key in ref.cvd.result_flows:
+        res[f'cum_{key}'] = _Res(np.cumsum(r[f'new_{key}']))
+    res['cum_infections'].values += pars['pop_infected']
+    res['n_alive'] = _Res(pars['pop_size'] - res['cum_deaths'].values)
+    for key in ('test_yield', 'rel_test_yield', 'doubling_time', 'r_eff'):
+        res[key] = _Res(np.zeros(sim.npts))
+    sc_ns = types.SimpleNamespace(**vars(refload.sc))
+    sc_ns.smooth = _smooth
+    ns = {'np': np, 'sc': sc_ns, 'cvu': ref.cvu, 'cvm': types.SimpleNamespace(warn=print)}
+    fns = refload.load_functions('sim.py', classname='Sim', namespace=ns,
+                                 names=['compute_yield', 'compute_doubling', 'compute_r_eff', 'compute_gen_time'])
+    class RefSimStub:
+        def __getitem__(self, k):
+            return self.pars[k]
+    stub = RefSimStub()
+    stub.results, stub.people, stub.npts, stub.tvec, stub.pars = res, sim.people, sim.npts, np.arange(sim.npts), pars
+    out = {}
+    fns['compute_yield'](stub)
+    out['out.test_yield'] = res['test_yield'].values.copy()
+    out['out.rel_test_yield'] = res['rel_test_yield'].values.copy()
+    out['out.doubling_time'] = fns['compute_doubling'](stub).copy()
+    for method in ('daily', 'infectious', 'outcome'):
+        out[f'out.r_eff_{method}'] = np.array(fns['compute_r_eff'](stub, method=method), dtype=np.float64).copy()
+    gt = fns['compute_gen_time'](stub)
+    out['out.gen_time'] = np.array([gt['true'], gt['true_std'], gt['clinical'], gt['clinical_std']])
+    for k in ('new_tests', 'new_diagnoses', 'n_infectious', 'n_alive', 'cum_diagnoses', 'cum_infections',
+              'new_infections', 'n_imports'):
+        out[f'res.{k}'] = res[k].values.copy()
+    for k in ('date_recovered', 'date_dead', 'date_infectious', 'date_exposed', 'date_symptomatic'):
+        out[f'people.{k}'] = sim.people[k].copy()
+    log = sim.people.infection_log
+    out['log.source'] = np.array([-1 if e['source'] is None else e['source'] for e in log], dtype=np.int64)
+    out['log.target'] = np.array([e['target'] for e in log], dtype=np.int64)
+    out['dur'] = np.array(json.dumps(jsonable(pars['dur'])))
+    np.savez_compressed(os.path.join(HERE, 'ref_reporting.npz'), **out)
+    print('ref_reporting.npz written')
+
+
 def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
     keys = ['new_infections', 'new_severe', 'new_deaths', 'new_infectious', 'new_recoveries', 'new_critical',
             'new_symptomatic', 'n_exposed']
@@ -458,7 +524,7 @@ def main():
     args = ap.parse_args()
     ref = refload.Reference()
     groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
-                  sims=make_sims_fixture, testing=make_testing_fixture,
+                  sims=make_sims_fixture, testing=make_testing_fixture, reporting=make_reporting_fixture,
                   distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
     for name, fn in groups.items():
         if args.only is None or args.only == name:

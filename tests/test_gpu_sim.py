@@ -18,12 +18,21 @@ RES_KEYS = ['new_infections', 'new_reinfections', 'new_infectious', 'new_symptom
             'n_symptomatic', 'n_severe', 'n_critical', 'n_recovered', 'n_dead']
 
 
+def _host(x):
+    return x.cpu().numpy() if torch.is_tensor(x) else x
+
+
 def oracle_for(sim):
     spec = sim.spec
-    contacts = {ly['key']: dict(p1=ly['p1'], p2=ly['p2'], beta=ly['beta']) for ly in spec.layers}
+    contacts = {}
+    for ly in spec.layers:
+        p1 = _host(ly['p1'])
+        beta = ly['beta'] if ly.get('beta') is not None else np.ones(len(p1), dtype=np.float32)
+        contacts[ly['key']] = dict(p1=p1, p2=_host(ly['p2']), beta=_host(beta))
     pars = copy.deepcopy(sim.pars)
     pars['interventions'] = []
-    return OracleSim(pars, dict(spec.person), contacts, rng='philox', beta_schedule=spec.beta_sched)
+    return OracleSim(pars, {k: _host(v) for k, v in spec.person.items()}, contacts, rng='philox',
+                     beta_schedule=spec.beta_sched)
 
 
 def compare_runs(sim, orc, keys=RES_KEYS):

@@ -77,3 +77,22 @@ def test_testing_batch_equals_single_runs():
         got = batch.results(k)
         for key in TESTING_KEYS:
             np.testing.assert_array_equal(got[key], raw[key], err_msg=f'sim {k} {key}')
+
+
+def test_reporting_on_a_device_run():
+    """finalize's compute_results and the other reporting methods on device results and log."""
+    from covasim_gb300.sim import r_eff_window, mean_infectious_duration, r_eff_daily
+    sim = make_sim(*CASES[0]).run()
+    res = sim.results
+    assert np.nansum(res['test_yield'].values) > 0 and np.isfinite(res['r_eff'].values).all()
+    mean_inf = mean_infectious_duration(sim.people['date_recovered'], sim.people['date_dead'],
+                                        sim.people['date_infectious'])
+    want = r_eff_daily(mean_inf, res['new_infections'].values, res['n_imports'].values, res['n_infectious'].values,
+                       sim['dur'])
+    np.testing.assert_allclose(res['r_eff'].values, want, rtol=1e-9)
+    log = sim.state.infection_log(0)
+    got = sim.compute_r_eff(method='infectious')
+    want = r_eff_window(sim.npts, [sim.people['date_infectious']], log[:, 0])
+    np.testing.assert_allclose(got, want, rtol=1e-12, equal_nan=True)
+    g = sim.compute_gen_time()
+    assert 2 < g['true'] < 10
