@@ -83,7 +83,7 @@ class SimParams(C.Structure):
         ('vx_ln_imm', C.c_void_p),
         ('n_vaccines', C.c_int32), ('_pad2', C.c_int32),
         ('res_int', C.c_void_p), ('res_var', C.c_void_p), ('res_fx', C.c_void_p),
-        ('testing', Testing),
+        ('testing', Testing), ('seg_of_layer', C.c_int32 * MAX_LAYERS),
     ]
 
 
@@ -91,7 +91,7 @@ class Layer(C.Structure):
     _fields_ = [('p1', C.c_void_p), ('p2', C.c_void_p), ('beta', C.c_void_p), ('n_edges', C.c_int64),
                 ('tile_begin', C.c_int64), ('sim', C.c_int32), ('layer', C.c_int32), ('dynamic', C.c_int32),
                 ('beta_const', C.c_float), ('iso_factor', C.c_float), ('quar_factor', C.c_float),
-                ('_pad', C.c_int32)]
+                ('_pad', C.c_int32), ('rp1', C.c_void_p), ('rp2', C.c_void_p), ('perm2', C.c_void_p)]
 
 
 class AgentBlock(C.Structure):
@@ -163,6 +163,10 @@ def lib():
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
+        L.covgpu_trace_index_scratch.argtypes = [i64]
+        L.covgpu_trace_index_scratch.restype = i64
+        L.covgpu_trace_index.argtypes = [vp, vp, i64, i64, i64, vp, vp, vp, vp, vp]
+        L.covgpu_trace_index.restype = C.c_int
         L.covgpu_pop_scan_scratch.argtypes = [i64]
         L.covgpu_pop_scan_scratch.restype = i64
         f64 = C.c_double
@@ -213,4 +217,5 @@ POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts'
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
             'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
-            'covgpu_lik_targets', 'covgpu_pop_scan_scratch'] + POP_FUNCS
+            'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index',
+            'covgpu_pop_scan_scratch'] + POP_FUNCS

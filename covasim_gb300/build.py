@@ -36,7 +36,8 @@ def nvcc_flags(extra=()):
 def build(verbose=False, force=False, extra=()):
     """Compile each translation unit in parallel (nvcc -c), then link the shared library."""
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(CSRC, f) for f in ('covgpu_device.cuh', 'covgpu_ff.cuh', 'covgpu_tables.h')]
+    deps = srcs + [os.path.join(CSRC, f) for f in ('covgpu_device.cuh', 'covgpu_ff.cuh', 'covgpu_tables.h',
+                                                   'covgpu_scan.cuh')]
     deps += [os.path.join(INCLUDE, 'covgpu.h'), __file__]
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)

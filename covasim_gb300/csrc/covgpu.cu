@@ -21,6 +21,7 @@
 #include "covgpu.h"
 #include "covgpu_device.cuh"
 #include "covgpu_ff.cuh"
+#include "covgpu_scan.cuh"
 
 using namespace covgpu;
 
@@ -775,45 +776,54 @@ int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
 // per target: expected = 1 - prod(1 - p) and its per-layer sensitivities from
 // the sums the likelihood edge pass left, which are cleared for the next day
 __global__ void __launch_bounds__(AGENT_THREADS) k_lik_agents(covgpu_state st, int t) {
+  constexpr int WARPS = AGENT_THREADS / 32;
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_lik& K = st.lik;
   const int64_t i = blk.begin + threadIdx.x;
   const bool valid = i < blk.end;
-  const int lane = threadIdx.x & 31;
-  __shared__ double s_e;
-  __shared__ double s_h[COVGPU_MAX_LAYERS];
-  if (threadIdx.x == 0) s_e = 0.0;
-  if (threadIdx.x < COVGPU_MAX_LAYERS) s_h[threadIdx.x] = 0.0;
-  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nl = sp.n_layers;
+  __shared__ double s_e[WARPS];
+  __shared__ double s_h[WARPS][COVGPU_MAX_LAYERS];
+  const double lq = valid ? K.logq[i] : 0.0;
+  const bool hit = lq != 0.0;  // a target of some candidate direction today
   double qprod = 0.0, e = 0.0;
-  if (valid) {
-    const double lq = K.logq[i];
-    if (lq != 0.0) {
-      qprod = exp(lq);
-      e = 1.0 - qprod;
-      K.logq[i] = 0.0;
-    }
+  if (hit) {
+    qprod = exp(lq);  // 0 for a certain transmission (lq = -inf)
+    e = 1.0 - qprod;
+    K.logq[i] = 0.0;
   }
-  e = warp_sum_d(e);
-  if (lane == 0 && e != 0.0) atomicAdd(&s_e, e);
+  const bool any = __any_sync(0xffffffffu, hit);  // most warps have no target: skip the reductions
+  if (lane == 0) s_e[warp] = 0.0;
+  if (any) {
+    e = warp_sum_d(e);
+    if (lane == 0) s_e[warp] = e;
+  }
   if (K.g_exp) {
-    for (int l = 0; l < sp.n_layers; ++l) {
+    for (int l = 0; l < nl; ++l) {
       double h = 0.0;
-      if (valid && qprod != 0.0) {
+      if (hit) {  // read and clear every layer's sum of a target, also when its product is 0
         double* wl = K.w + (int64_t)l * st.n + i;
         const double x = *wl;
         if (x != 0.0) { h = qprod * x; *wl = 0.0; }
       }
-      h = warp_sum_d(h);
-      if (lane == 0 && h != 0.0) atomicAdd(&s_h[l], h);
+      if (any) h = warp_sum_d(h);
+      if (lane == 0) s_h[warp][l] = any ? h : 0.0;
     }
   }
   __syncthreads();
   const int64_t day = (int64_t)blk.sim * K.npts_max + t;
-  if (threadIdx.x == 0 && s_e != 0.0) atomicAdd(K.expected + day, s_e);
-  if (K.g_exp && threadIdx.x < sp.n_layers && s_h[threadIdx.x] != 0.0)
-    atomicAdd(K.g_exp + day * K.n_layers_max + threadIdx.x, s_h[threadIdx.x]);
+  if (threadIdx.x == 0) {
+    double x = 0.0;
+    for (int k = 0; k < WARPS; ++k) x += s_e[k];
+    if (x != 0.0) atomicAdd(K.expected + day, x);
+  }
+  if (K.g_exp && threadIdx.x < nl) {
+    double x = 0.0;
+    for (int k = 0; k < WARPS; ++k) x += s_h[k][threadIdx.x];
+    if (x != 0.0) atomicAdd(K.g_exp + day * K.n_layers_max + threadIdx.x, x);
+  }
 }
 
 int launch_lik_targets(const covgpu_state* st, int t, cudaStream_t s) {
@@ -1160,6 +1170,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
   const covgpu_sim_params& sp = st.sims[L->sim];
   const covgpu_testing& T = sp.testing;
   if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
+  if (!L->dynamic && L->rp1) return;  // indexed: k_trace_csr visits the traced agents' edges
   const int64_t words = (st.n + 31) >> 5;
   uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
   const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
@@ -1183,6 +1194,34 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
       }
       if (bit_of(st.trace_bits, a)) atomicOr(contact + (b >> 5), 1u << (b & 31));
       if (bit_of(st.trace_bits, b)) atomicOr(contact + (a >> 5), 1u << (a & 31));
+    }
+  }
+}
+
+// find_contacts through the index of each stored layer: a traced agent marks the
+// other endpoint of each of its edges, as p1 and as p2
+__global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  if (!day_active(t, T.trace_start, T.trace_end) || st.trace_count[blk.sim] == 0) return;
+  const int64_t i = blk.begin + threadIdx.x;
+  if (i >= blk.end || !((st.trace_bits[i >> 5] >> (i & 31)) & 1u)) return;
+  const int64_t words = (st.n + 31) >> 5;
+  const int64_t local = i - sp.agent_off;
+  for (int l = 0; l < sp.n_layers; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg < 0 || T.thr_trace[l] == 0) continue;
+    const covgpu_layer& L = st.segments[seg];
+    if (L.dynamic || !L.rp1) continue;
+    uint32_t* contact = st.contact_bits + (int64_t)l * words;
+    for (uint32_t k = L.rp1[local]; k < L.rp1[local + 1]; ++k) {
+      const int32_t b = L.p2[k];
+      atomicOr(contact + (b >> 5), 1u << (b & 31));
+    }
+    for (uint32_t k = L.rp2[local]; k < L.rp2[local + 1]; ++k) {
+      const int32_t a = L.p1[L.perm2[k]];
+      atomicOr(contact + (a >> 5), 1u << (a & 31));
     }
   }
 }
@@ -1286,8 +1325,41 @@ int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
       default: k_trace_scan<4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
     }
   }
+  k_trace_csr<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
+}
+
+// ------------------------------------------------------------ contact-tracing index
+__global__ void k_row_ptr(const int32_t* p, int64_t n_edges, int64_t off, int64_t n_local, uint32_t* rp) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a > n_local) return;
+  const int64_t key = off + a;  // first edge with p >= key
+  int64_t lo = 0, hi = n_edges;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)p[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  rp[a] = (uint32_t)lo;
+}
+__global__ void k_rev_count(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* counts) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  const int64_t a = (int64_t)p2[e] - off;
+  if (a >= 0 && a < n_local) atomicAdd(reinterpret_cast<unsigned long long*>(counts + a), 1ull);
+}
+__global__ void k_rev_offsets(const int64_t* offsets, int64_t n, uint32_t* rp2) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a <= n) rp2[a] = (uint32_t)offsets[a];
+}
+__global__ void k_rev_place(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* cursor,
+                            uint32_t* perm2) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  const int64_t a = (int64_t)p2[e] - off;
+  if (a < 0 || a >= n_local) return;
+  const unsigned long long pos = atomicAdd(reinterpret_cast<unsigned long long*>(cursor + a), 1ull);
+  perm2[pos] = (uint32_t)e;
 }
 
 int grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
@@ -1506,6 +1578,29 @@ int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream) {
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
   return launch_test_trace(st, t, S(stream));
+}
+
+int64_t covgpu_trace_index_scratch(int64_t n_local) {
+  return 2 * (n_local + 1) + (int64_t)scan_blocks_for(n_local, SCAN_TILE) + 1;
+}
+
+int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, int64_t agent_off, int64_t n_local,
+                       uint32_t* rp1, uint32_t* rp2, uint32_t* perm2, int64_t* scratch, void* stream) {
+  if (n_edges < 1 || n_edges > 0xFFFFFFFFLL || n_local < 1 || agent_off < 0 || !p1 || !p2 || !rp1 || !rp2 ||
+      !perm2 || !scratch)
+    return COVGPU_BADARG;
+  cudaStream_t s = S(stream);
+  int64_t* counts = scratch;
+  int64_t* offsets = scratch + (n_local + 1);
+  int64_t* tiles = scratch + 2 * (n_local + 1);
+  k_row_ptr<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(p1, n_edges, agent_off, n_local, rp1);
+  if (cudaMemsetAsync(counts, 0, sizeof(int64_t) * (size_t)n_local, s) != cudaSuccess) return COVGPU_CUDA_ERROR;
+  k_rev_count<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, counts);
+  int rc = scan_i64(counts, offsets, n_local, tiles, s);
+  if (rc) return rc;
+  k_rev_offsets<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(offsets, n_local, rp2);
+  k_rev_place<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, offsets, perm2);
+  return launch_status();
 }
 
 int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream) {

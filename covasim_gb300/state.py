@@ -293,6 +293,7 @@ class BatchState:
                         tp2 = tp2 + off
                     rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
                     keep += [tp1, tp2]
+                    keep += self._trace_index(rec, sp, off, n_edges)
                     b = ly.get('beta')
                     if b is None or bool((b == b[0]).all()):
                         rec.beta = None
@@ -315,6 +316,7 @@ class BatchState:
                         raise RuntimeError('edge arrays must be 16-byte aligned')
                     rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
                     keep += [tp1, tp2]
+                    keep += self._trace_index(rec, sp, off, n_edges)
                     if np.all(beta == beta[0]):
                         rec.beta = None
                         rec.beta_const = float(beta[0])
@@ -326,6 +328,22 @@ class BatchState:
                 self.segments.append(rec)
                 self.layer_tensors.append(keep)
         self._tile_segments()
+
+    def _trace_index(self, rec, sp, off, n_edges):
+        """Contact-tracing index of a stored layer (covgpu_trace_index) when the sim traces."""
+        T = sp.testing
+        if not (T and T.get('trace') is not None):
+            return []
+        dev, n = self.device, sp.n
+        rp1 = torch.empty(n + 1, dtype=I32, device=dev)
+        rp2 = torch.empty(n + 1, dtype=I32, device=dev)
+        perm2 = torch.empty(n_edges, dtype=I32, device=dev)
+        scratch = torch.empty(int(self.lib.covgpu_trace_index_scratch(n)), dtype=I64, device=dev)
+        L.call('covgpu_trace_index', rec.p1, rec.p2, int(n_edges), int(off), int(n), rp1.data_ptr(), rp2.data_ptr(),
+               perm2.data_ptr(), scratch.data_ptr(), _stream())
+        rec.rp1, rec.rp2, rec.perm2 = rp1.data_ptr(), rp2.data_ptr(), perm2.data_ptr()
+        self._index_scratch = scratch  # kept until the build has run on the stream
+        return [rp1, rp2, perm2]
 
     def _tile_segments(self):
         """Each segment's first tile and the tile count for the current edge tile size."""
@@ -414,6 +432,8 @@ class BatchState:
             r.res_var = self.res_var.data_ptr() + 8 * rv
             r.res_fx = self.res_fx.data_ptr() + 8 * rf
             r.testing = self.testing_recs[s]
+            for li in range(L.MAX_LAYERS):
+                r.seg_of_layer[li] = self.segment_index.get((s, li), -1)
             self.res_slices.append((ri, rv, rf))
             ri += sp.npts * L.N_RES_INT
             rv += sp.npts * L.N_RES_VAR * sp.nv

@@ -159,6 +159,7 @@ typedef struct covgpu_sim_params {
   int64_t* res_var;               /* [npts][COVGPU_N_RES_VAR][n_variants]            */
   int64_t* res_fx;                /* [npts][COVGPU_N_RES_F] fixed-point sums         */
   covgpu_testing testing;
+  int32_t seg_of_layer[COVGPU_MAX_LAYERS]; /* layer -> segment index (-1: no edges)   */
 } covgpu_sim_params;
 
 /* One contact layer of one sim (device memory, one entry per layer segment). */
@@ -174,6 +175,12 @@ typedef struct covgpu_layer {
   float beta_const;
   float iso_factor, quar_factor;
   int32_t _pad;
+  /* contact-tracing index of a stored layer (NULL: none; covgpu_trace_index):
+   * the agent a's edges as p1 are [rp1[a], rp1[a+1]), as p2 the edges
+   * perm2[rp2[a] .. rp2[a+1]) (a local to the sim) */
+  const uint32_t* rp1;
+  const uint32_t* rp2;
+  const uint32_t* perm2;
 } covgpu_layer;
 
 /* One agent block of the agent kernel: agents [begin, end) of one sim. */
@@ -414,6 +421,15 @@ int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream);
  * after covgpu_edge_pass and before covgpu_infect_claims of the same day.
  * BADARG when st->lik.factor is NULL. */
 int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream);
+
+/* The contact-tracing index of one stored layer segment (p1 ascending,
+ * global agent indices from agent_off, n_local agents): rp1 and rp2
+ * [n_local + 1], perm2 [n_edges], scratch covgpu_trace_index_scratch(n_local)
+ * int64 elements. With it, covgpu_test_trace visits only the traced agents'
+ * edges of that layer instead of scanning the layer. */
+int64_t covgpu_trace_index_scratch(int64_t n_local);
+int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, int64_t agent_off, int64_t n_local,
+                       uint32_t* rp1, uint32_t* rp2, uint32_t* perm2, int64_t* scratch, void* stream);
 
 /* infect() for the winning event of each target. */
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
