@@ -687,6 +687,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   const int64_t e1 = min(e0 + TILE, c.n_edges);
   const int64_t n_local = sp->n_agents;
   const int32_t off = (int32_t)sp->agent_off;
+  const uint32_t thr = dynamic ? bounded_thr((uint32_t)n_local) : 0u;
   EdgeQueue& q = s_q[threadIdx.x >> 5];
   int qn = 0;  // warp-uniform queue length
   LikAcc acc;
@@ -695,15 +696,11 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
     int32_t a[EDGE_VEC], b[EDGE_VEC];
     if (dynamic) {
       // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
-      // endpoints uniform over the sim's agents (Philox keyed by edge and day)
+      // endpoints uniform over the sim's agents (one Philox block per two edges)
 #pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        const int64_t e = eb + j;
-        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)c.layer),
-                               c.key0, c.key1);
-        a[j] = off + (int32_t)uniform_index(w.x, w.y, (uint64_t)n_local);
-        b[j] = off + (int32_t)uniform_index(w.z, w.w, (uint64_t)n_local);
-      }
+      for (int j = 0; j < EDGE_VEC; j += 2)
+        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)c.layer, c.key0, c.key1, (uint32_t)n_local, thr,
+                     off, a[j], b[j], a[j + 1], b[j + 1]);
     } else if (eb + EDGE_VEC <= e1) {
       const int4 pa = __ldg(reinterpret_cast<const int4*>(p1 + eb));
       const int4 pb = __ldg(reinterpret_cast<const int4*>(p2 + eb));
@@ -1055,11 +1052,17 @@ __global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64
 __global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1, int32_t* p2) {
   const covgpu_layer& L = st.segments[seg];
   const covgpu_sim_params& sp = st.sims[L.sim];
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < L.n_edges; e += (int64_t)gridDim.x * blockDim.x) {
-    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L.layer),
-                           sp.key0, sp.key1);
-    p1[e] = (int32_t)uniform_index(w.x, w.y, (uint64_t)sp.n_agents);
-    p2[e] = (int32_t)uniform_index(w.z, w.w, (uint64_t)sp.n_agents);
+  const uint32_t n = (uint32_t)sp.n_agents, thr = bounded_thr(n);
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; 2 * j < L.n_edges;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    int32_t a0, b0, a1, b1;
+    dynamic_pair((uint64_t)j, (uint32_t)t, (uint32_t)L.layer, sp.key0, sp.key1, n, thr, 0, a0, b0, a1, b1);
+    p1[2 * j] = a0;
+    p2[2 * j] = b0;
+    if (2 * j + 1 < L.n_edges) {
+      p1[2 * j + 1] = a1;
+      p2[2 * j + 1] = b1;
+    }
   }
 }
 
@@ -1176,24 +1179,28 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
   const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
   const int64_t e1 = min(e0 + TILE, L->n_edges);
   const int32_t off = (int32_t)sp.agent_off;
+  const uint32_t thr = L->dynamic ? bounded_thr((uint32_t)sp.n_agents) : 0u;
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
+    if (eb >= e1) break;
+    int32_t a[EDGE_VEC], b[EDGE_VEC];
+    if (L->dynamic) {
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; j += 2)
+        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)L->layer, sp.key0, sp.key1,
+                     (uint32_t)sp.n_agents, thr, off, a[j], b[j], a[j + 1], b[j + 1]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        a[j] = eb + j < e1 ? __ldg(L->p1 + eb + j) : off;
+        b[j] = eb + j < e1 ? __ldg(L->p2 + eb + j) : off;
+      }
+    }
 #pragma unroll
     for (int j = 0; j < EDGE_VEC; ++j) {
-      const int64_t e = eb + j;
-      if (e >= e1) break;
-      int32_t a, b;
-      if (L->dynamic) {
-        const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t, TAG_LAYER | (uint32_t)L->layer),
-                               sp.key0, sp.key1);
-        a = off + (int32_t)uniform_index(w.x, w.y, (uint64_t)sp.n_agents);
-        b = off + (int32_t)uniform_index(w.z, w.w, (uint64_t)sp.n_agents);
-      } else {
-        a = __ldg(L->p1 + e);
-        b = __ldg(L->p2 + e);
-      }
-      if (bit_of(st.trace_bits, a)) atomicOr(contact + (b >> 5), 1u << (b & 31));
-      if (bit_of(st.trace_bits, b)) atomicOr(contact + (a >> 5), 1u << (a & 31));
+      if (eb + j >= e1) break;
+      if (bit_of(st.trace_bits, a[j])) atomicOr(contact + (b[j] >> 5), 1u << (b[j] & 31));
+      if (bit_of(st.trace_bits, b[j])) atomicOr(contact + (a[j] >> 5), 1u << (a[j] & 31));
     }
   }
 }

@@ -40,6 +40,7 @@ constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
 constexpr uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
 constexpr uint32_t TAG_EDGE = 0x01000000u, TAG_LAYER = 0x02000000u, TAG_INFECT = 0x03000000u;
 constexpr uint32_t TAG_TEST = 0x04000000u, TAG_TRACE = 0x05000000u;
+constexpr uint32_t TAG_LAYER_RETRY = 0x07000000u;
 
 __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
@@ -61,6 +62,38 @@ __device__ __forceinline__ double u01_52(uint32_t a, uint32_t b) {
 __device__ __forceinline__ double u01_32(uint32_t a) {
   return __dmul_rn(__dadd_rn((double)a, 0.5), 2.3283064365386962890625e-10);
 }
+// A uniform integer in [0, n) from a 32-bit word x, without bias (Lemire 2019,
+// "Fast random integer generation in an interval"): the high half of x * n,
+// redrawn while the low half is below thr = 2^32 mod n. Redraws (probability
+// below n / 2^32 each) come from the retry stream of (edge, endpoint):
+// Philox (edge, day, TAG_LAYER_RETRY | try << 8 | layer), word x for the first
+// endpoint and y for the second; after 16 tries (never reached in practice)
+// the last draw is kept.
+__device__ __forceinline__ uint32_t bounded_draw(uint32_t x, uint32_t n, uint32_t thr, uint64_t e, int which,
+                                                 uint32_t day, uint32_t layer, uint32_t k0, uint32_t k1) {
+  uint64_t m = (uint64_t)x * n;
+  for (uint32_t r = 0; (uint32_t)m < thr && r < 16; ++r) {
+    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), day, TAG_LAYER_RETRY | (r << 8) | layer), k0, k1);
+    m = (uint64_t)(which ? w.y : w.x) * n;
+  }
+  return (uint32_t)(m >> 32);
+}
+// 2^32 mod n (the rejection threshold of bounded_draw)
+__host__ __device__ __forceinline__ uint32_t bounded_thr(uint32_t n) { return (uint32_t)(-n) % n; }
+
+// Endpoints of the dynamic-layer edges 2j and 2j+1 on one day (base.py:1849-1876:
+// uniform over the sim's n agents): one Philox block (j, day, TAG_LAYER | layer),
+// words x, y -> edge 2j, z, w -> edge 2j+1.
+__device__ __forceinline__ void dynamic_pair(uint64_t j, uint32_t day, uint32_t layer, uint32_t k0, uint32_t k1,
+                                             uint32_t n, uint32_t thr, int32_t off, int32_t& a0, int32_t& b0,
+                                             int32_t& a1, int32_t& b1) {
+  const uint4 w = philox(make_uint4((uint32_t)j, (uint32_t)(j >> 32), day, TAG_LAYER | layer), k0, k1);
+  a0 = off + (int32_t)bounded_draw(w.x, n, thr, 2 * j, 0, day, layer, k0, k1);
+  b0 = off + (int32_t)bounded_draw(w.y, n, thr, 2 * j, 1, day, layer, k0, k1);
+  a1 = off + (int32_t)bounded_draw(w.z, n, thr, 2 * j + 1, 0, day, layer, k0, k1);
+  b1 = off + (int32_t)bounded_draw(w.w, n, thr, 2 * j + 1, 1, day, layer, k0, k1);
+}
+
 // floor(x * n / 2^64) for x = a:b
 __device__ __forceinline__ int64_t uniform_index(uint32_t a, uint32_t b, uint64_t n) {
   const uint64_t x = ((uint64_t)a << 32) | b;

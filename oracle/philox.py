@@ -13,7 +13,8 @@ Stream layout (shared with the CUDA side; all words little-endian uint32):
   key     = (seed_lo, seed_hi)                        64-bit per-sim seed
   counter = (c0, c1, c2, c3)
     edge Bernoulli      : (edge_lo, edge_hi, day, TAG_EDGE  | variant << 8 | layer)
-    dynamic-layer edges : (edge_lo, edge_hi, day, TAG_LAYER | layer)
+    dynamic-layer edges : (pair_lo, pair_hi, day, TAG_LAYER | layer), one block per two edges;
+                          redraws (edge_lo, edge_hi, day, TAG_LAYER_RETRY | try << 8 | layer)
     infect draws        : (agent,   block,   day, TAG_INFECT | call_tag)
     testing draws       : (agent,   block,   day, TAG_TEST)  block 0: test, sensitivity; 1: follow-up
     tracing draws       : (agent,   layer,   day, TAG_TRACE)
@@ -35,6 +36,7 @@ TAG_LAYER = 0x02000000
 TAG_INFECT = 0x03000000
 TAG_TEST = 0x04000000
 TAG_TRACE = 0x05000000
+TAG_LAYER_RETRY = 0x07000000
 
 _MASK32 = np.uint64(0xFFFFFFFF)
 
@@ -114,13 +116,41 @@ def edge_uniforms(k0, k1, day, layer, variant, edges):
     return u01_52(w[0], w[1]), u01_52(w[2], w[3])
 
 
+def bounded_draw(x, n, edges, which, k0, k1, day, layer):
+    """Unbiased integers in [0, n) from 32-bit words (Lemire 2019): the high half of
+    x * n, redrawn while the low half is below 2**32 mod n; redraw r of endpoint
+    ``which`` of edge e is word x (which 0) or y (which 1) of Philox
+    (e, day, TAG_LAYER_RETRY | r << 8 | layer); at most 16 redraws."""
+    n = int(n)
+    thr = np.uint64((2 ** 32 - n) % n)
+    m = np.asarray(x, dtype=np.uint64) * np.uint64(n)
+    edges = np.asarray(edges, dtype=np.int64)
+    bad = (m & _MASK32) < thr
+    for r in range(16):
+        if not bad.any():
+            break
+        idx = np.nonzero(bad)[0]
+        e = edges[idx]
+        w = philox4x32_10(e & 0xFFFFFFFF, e >> 32, day, TAG_LAYER_RETRY | (r << 8) | int(layer), k0, k1)
+        m[idx] = w[which].astype(np.uint64) * np.uint64(n)
+        bad[idx] = (m[idx] & _MASK32) < thr
+    return (m >> np.uint64(32)).astype(np.int64)
+
+
 def dynamic_edges(k0, k1, day, layer, n_edges, n_agents):
-    """Endpoints of a dynamic layer on one day: n_edges i.i.d. uniform pairs."""
-    e = np.arange(n_edges, dtype=np.int64)
-    w = philox4x32_10(e & 0xFFFFFFFF, e >> 32, day, TAG_LAYER | int(layer), k0, k1)
-    p1 = uniform_index(w[0], w[1], n_agents)
-    p2 = uniform_index(w[2], w[3], n_agents)
-    return p1.astype(np.int32), p2.astype(np.int32)
+    """Endpoints of a dynamic layer on one day: n_edges i.i.d. uniform pairs. One
+    Philox block (j, day, TAG_LAYER | layer) serves edges 2j (words x, y) and
+    2j + 1 (words z, w)."""
+    n_pairs = (int(n_edges) + 1) // 2
+    j = np.arange(n_pairs, dtype=np.int64)
+    w = philox4x32_10(j & 0xFFFFFFFF, j >> 32, day, TAG_LAYER | int(layer), k0, k1)
+    p1 = np.empty(2 * n_pairs, dtype=np.int64)
+    p2 = np.empty(2 * n_pairs, dtype=np.int64)
+    p1[0::2] = bounded_draw(w[0], n_agents, 2 * j, 0, k0, k1, day, layer)
+    p2[0::2] = bounded_draw(w[1], n_agents, 2 * j, 1, k0, k1, day, layer)
+    p1[1::2] = bounded_draw(w[2], n_agents, 2 * j + 1, 0, k0, k1, day, layer)
+    p2[1::2] = bounded_draw(w[3], n_agents, 2 * j + 1, 1, k0, k1, day, layer)
+    return p1[:n_edges].astype(np.int32), p2[:n_edges].astype(np.int32)
 
 
 # Slots of the per-infection draw table (shared with the CUDA side).

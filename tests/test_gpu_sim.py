@@ -169,3 +169,18 @@ def test_distribution_matches_reference_200_seeds():
             failures.append((name, p, a.mean(), b.mean(), se))
     # 19 statistics at the 1% / 2-SE levels: allow one marginal miss from chance alone
     assert len(failures) <= 1, failures
+
+
+def test_dynamic_layer_endpoints_match_oracle():
+    """The day's dynamic-layer edges (paired Philox blocks, unbiased bounded draws)."""
+    from oracle import philox as ph
+    sim = cv.Sim(pop_type='hybrid', pop_size=5001, n_days=20, rand_seed=12, dynam_layer=dict(h=0, s=0, w=0, c=1))
+    sim.initialize()
+    keys = [ly['key'] for ly in sim.spec.layers]
+    li = keys.index('c')
+    n_edges = len(sim.spec.layers[li]['p1'])
+    k0, k1 = ph.seed_key(sim['rand_seed'])
+    for t in (0, 3, 17):
+        p1, p2 = sim.state.materialize_layer(0, li, t)
+        w1, w2 = ph.dynamic_edges(k0, k1, t, li, n_edges, 5001)
+        assert np.array_equal(p1.cpu().numpy(), w1) and np.array_equal(p2.cpu().numpy(), w2), t
