@@ -832,7 +832,7 @@ int launch_lik_targets(const covgpu_state* st, int t, cudaStream_t s) {
 // ============================================================ infect
 
 struct DrawSet {
-  double z[6];
+  ff z[6];           // the six standard normals, float-float
   double u[4];       // injected uniforms (test mode)
   uint32_t uw[4];    // Philox words of the uniforms
   uint32_t w23[2];   // Philox words of the (sym2sev, sev2crit) normal pair, transformed on demand
@@ -841,7 +841,7 @@ struct DrawSet {
   __device__ __forceinline__ bool lt(int k, float p) const { return injected ? (u[k] < (double)p) : bern32(uw[k], p); }
   // the normals of the severe branch: only severe cases need them
   __device__ __forceinline__ void severe_normals() {
-    if (!injected) box_muller(w23[0], w23[1], z[2], z[3]);
+    if (!injected) box_muller_ff(w23[0], w23[1], COVGPU_LN_TAB, COVGPU_SINCOS_TAB, z[2], z[3]);
   }
 };
 
@@ -850,7 +850,7 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   if (st.draw_table) {
     const double* r = st.draw_table + i * COVGPU_N_DRAWS;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) d.z[k] = r[k];
+    for (int k = 0; k < 6; ++k) d.z[k] = d2ff(r[k]);
 #pragma unroll
     for (int k = 0; k < 4; ++k) d.u[k] = r[6 + k];
     d.injected = true;
@@ -861,10 +861,10 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b1 = philox(make_uint4((uint32_t)local, 1u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b2 = philox(make_uint4((uint32_t)local, 2u, (uint32_t)t, tag), sp.key0, sp.key1);
-  box_muller(b0.x, b0.y, d.z[0], d.z[1]);
+  box_muller_ff(b0.x, b0.y, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, d.z[0], d.z[1]);
   d.w23[0] = b0.z;
   d.w23[1] = b0.w;
-  box_muller(b1.x, b1.y, d.z[4], d.z[5]);
+  box_muller_ff(b1.x, b1.y, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, d.z[4], d.z[5]);
   d.uw[0] = b1.z;
   d.uw[1] = b1.w;
   d.uw[2] = b2.x;
@@ -925,7 +925,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   const float nanf_ = f32nan();
   const float tf = (float)t;
   // people.py:514-520
-  const float de = (float)sample_dist(sp.dur[COVGPU_D_EXP2INF], d.z[0]);
+  const float de = (float)sample_ff(sp.dur[COVGPU_D_EXP2INF], d.z[0]);
   u_exp2inf[i] = de;
   date_row(st, COVGPU_DATE_EXPOSED)[i] = tf;
   const float di = __fadd_rn(de, tf);
@@ -938,12 +938,12 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
                                   __fsub_rn(1.0f, st.symp_imm[(int64_t)v * st.n + i]));
   if (!d.lt(0, sp_symp)) {  // CASE 1: asymptomatic, people.py:530-532
-    const double dr = sample_dist(sp.dur[COVGPU_D_ASYM2REC], d.z[4]);
+    const double dr = sample_ff(sp.dur[COVGPU_D_ASYM2REC], d.z[4]);
     rec = (float)__dadd_rn((double)di, dr);
     u_disease[i] = (float)__dadd_rn((double)de, dr);
     symp_class = 0;
   } else {  // CASE 2: symptomatic, people.py:535-541
-    const float dis = (float)sample_dist(sp.dur[COVGPU_D_INF2SYM], d.z[1]);
+    const float dis = (float)sample_ff(sp.dur[COVGPU_D_INF2SYM], d.z[1]);
     u_inf2sym[i] = dis;
     const float ds = __fadd_rn(di, dis);
     d_sym[i] = ds;
@@ -952,7 +952,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
     const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
                                   __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
     if (!d.lt(1, p_sev)) {  // CASE 2.1 mild, people.py:544-547
-      const double dr = sample_dist(sp.dur[COVGPU_D_MILD2REC], d.z[4]);
+      const double dr = sample_ff(sp.dur[COVGPU_D_MILD2REC], d.z[4]);
       rec = (float)__dadd_rn((double)ds, dr);
       u_disease[i] = (float)__dadd_rn((double)__fadd_rn(de, dis), dr);
       symp_class = 1;
@@ -960,29 +960,29 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       d.severe_normals();
       if (count)
         atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
-      const float dss = (float)sample_dist(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
+      const float dss = (float)sample_ff(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
       u_sym2sev[i] = dss;
       const float dsev = __fadd_rn(ds, dss);
       d_sev[i] = dsev;
       const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], st.crit_prob[i]), hosp_max ? sp.no_hosp_factor : 1.0f);
       symp_class = 2;
       if (!d.lt(2, p_crit)) {  // CASE 2.2.1 not critical, people.py:557-559
-        const double dr = sample_dist(sp.dur[COVGPU_D_SEV2REC], d.z[4]);
+        const double dr = sample_ff(sp.dur[COVGPU_D_SEV2REC], d.z[4]);
         rec = (float)__dadd_rn((double)dsev, dr);
         u_disease[i] = (float)__dadd_rn((double)__fadd_rn(__fadd_rn(de, dis), dss), dr);
       } else {  // CASE 2.2.2 critical, people.py:562-566
-        const float dsc = (float)sample_dist(sp.dur[COVGPU_D_SEV2CRIT], d.z[3]);
+        const float dsc = (float)sample_ff(sp.dur[COVGPU_D_SEV2CRIT], d.z[3]);
         u_sev2crit[i] = dsc;
         const float dcrit = __fadd_rn(dsev, dsc);
         d_crit[i] = dcrit;
         const float p_death = __fmul_rn(__fmul_rn(sp.rel_death[v], st.death_prob[i]), icu_max ? sp.no_icu_factor : 1.0f);
         const float dsum = __fadd_rn(__fadd_rn(__fadd_rn(de, dis), dss), dsc);
         if (!d.lt(3, p_death)) {  // CASE 2.2.2.1 alive, people.py:569-571
-          const double dr = sample_dist(sp.dur[COVGPU_D_CRIT2REC], d.z[4]);
+          const double dr = sample_ff(sp.dur[COVGPU_D_CRIT2REC], d.z[4]);
           rec = (float)__dadd_rn((double)dcrit, dr);
           u_disease[i] = (float)__dadd_rn((double)dsum, dr);
         } else {  // CASE 2.2.2.2 dead, people.py:574-577
-          const double dr = sample_dist(sp.dur[COVGPU_D_CRIT2DIE], d.z[4]);
+          const double dr = sample_ff(sp.dur[COVGPU_D_CRIT2DIE], d.z[4]);
           d_dead[i] = (float)__dadd_rn((double)dcrit, dr);
           u_disease[i] = (float)__dadd_rn((double)dsum, dr);
           rec = nanf_;
@@ -996,9 +996,9 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
     if (st.nab[i] > 0.0f) {
       st.peak_nab[i] = __fmul_rn(st.peak_nab[i], sp.nab_boost);
     } else {
-      const double init = sample_dist(sp.nab_init, d.z[5]);
+      const double init = sample_ff(sp.nab_init, d.z[5]);
       const double rel = symp_class == 0 ? sp.rel_imm_asymp : (symp_class == 1 ? sp.rel_imm_mild : sp.rel_imm_severe);
-      st.peak_nab[i] = (float)__dmul_rn(__dmul_rn(exp2(init), rel), sp.nab_norm);
+      st.peak_nab[i] = (float)__dmul_rn(__dmul_rn(exp2_ff(d2ff(init)), rel), sp.nab_norm);
     }
     st.t_nab_event[i] = t;
   }

@@ -99,14 +99,6 @@ __device__ __forceinline__ int64_t uniform_index(uint32_t a, uint32_t b, uint64_
   const uint64_t x = ((uint64_t)a << 32) | b;
   return (int64_t)__umul64hi(x, n);
 }
-__device__ __forceinline__ void box_muller(uint32_t wa, uint32_t wb, double& z0, double& z1) {
-  const double u1 = u01_32(wa), u2 = u01_32(wb);
-  const double r = sqrt(__dmul_rn(-2.0, log(u1)));
-  const double th = __dmul_rn(6.283185307179586231995926937088, u2);  // (2.0 * pi) * u2
-  z0 = __dmul_rn(r, cos(th));
-  z1 = __dmul_rn(r, sin(th));
-}
-
 // ---------------------------------------------------------------- small helpers
 __device__ __forceinline__ float f32nan() { return __int_as_float(0x7fc00000); }
 __device__ __forceinline__ bool defined(float x) { return !isnan(x); }
@@ -114,18 +106,6 @@ __device__ __forceinline__ float* date_row(const covgpu_state& st, int d) { retu
 // words of each role bitmap (source bitmap first, then target bitmap)
 __device__ __forceinline__ int64_t roles_words(const covgpu_state& st) { return (st.n + 31) >> 5; }
 __device__ __forceinline__ float* dur_row(const covgpu_state& st, int d) { return st.durs + (int64_t)d * st.n; }
-
-// utils.py:156-236: a sample that is a function of one standard normal z
-__device__ __forceinline__ double sample_dist(const covgpu_dur_par& d, double z) {
-  switch (d.code) {
-    case COVGPU_DIST_LOGNORMAL_INT: return rint(exp(__dadd_rn(d.a, __dmul_rn(d.b, z))));
-    case COVGPU_DIST_LOGNORMAL: return exp(__dadd_rn(d.a, __dmul_rn(d.b, z)));
-    case COVGPU_DIST_NORMAL: return __dadd_rn(d.a, __dmul_rn(d.b, z));
-    case COVGPU_DIST_NORMAL_INT: return rint(fabs(__dadd_rn(d.a, __dmul_rn(d.b, z))));
-    case COVGPU_DIST_NORMAL_POS: return fabs(__dadd_rn(d.a, __dmul_rn(d.b, z)));
-    default: return 0.0;
-  }
-}
 
 // utils.py:39-79 for one agent, float32 as numba types it (the int32 t and the
 // float32 arrays meet in a float32 ufunc loop).

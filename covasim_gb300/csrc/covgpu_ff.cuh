@@ -3,19 +3,22 @@
 //
 // GB300 executes float64 at a small fraction of its float32 rate. The
 // reference computes the NAb efficacy (immunity.py:216-247 calc_VE, called by
-// check_immunity for every agent every day) and update_nab (immunity.py:205-213)
-// in float64 and stores float32; here the same quantities are computed with
-// error-free transformations (two-sum, two-product via fused multiply-add) to
-// about 2^-44 relative and rounded once to float32, which reproduces the
-// reference's float32 result except when the exact value lies within ~2^-40 of
-// a float32 rounding boundary.
+// check_immunity for every agent every day), update_nab (immunity.py:205-213),
+// and the normals, lognormal durations and initial NAb levels of infect
+// (people.py:514-577, immunity.py:138-202) in float64 and stores float32 or
+// whole days; here the same quantities are computed with error-free
+// transformations (two-sum, two-product via fused multiply-add) to about
+// 2^-40 relative and rounded once, which reproduces the reference's result
+// except when the exact value lies that close to a rounding boundary.
 //
 // Only IEEE round-to-nearest add/sub/mul/div and fused multiply-add (used for
 // exact product residuals only) appear, in a fixed order: the numpy mirror in
 // the oracle (oracle/gpu_arith.py) performs the same operations and gets the
 // same bits. ln uses the reduction x = 2^e * c_j * (1 + r), |r| < 2^-7.5, and
 // the series of ln(1 + r); exp uses Cody-Waite reduction by ln2/64, a table
-// of 2^(j/64) and the Taylor series of exp(r), |r| <= ln2/128.
+// of 2^(j/64) and the Taylor series of exp(r), |r| <= ln2/128; cos and sin of
+// 2 pi u reduce exactly to a quadrant and the nearest of the points
+// j pi / 64 and use the Taylor series of the residual |phi| <= pi / 128.
 #pragma once
 #include <stdint.h>
 #include "covgpu_tables.h"
@@ -108,6 +111,123 @@ __device__ __forceinline__ ff ff_exp_neg(ff y, const float (*tab)[2]) {
   const ff x = ff_mul(er, ff{tab[j][0], tab[j][1]});
   const float scale = __int_as_float((m + 127) << 23);  // 2^m, m in [-126, 0]
   return ff{__fmul_rn(x.hi, scale), __fmul_rn(x.lo, scale)};
+}
+
+// exp(y) for any float-float y: exp_neg of -y and a reciprocal for y > 0;
+// 0 below -87 and +inf above 87 (the float32 range of the values it feeds)
+__device__ __forceinline__ ff ff_exp(ff y, const float (*tab)[2]) {
+  if (y.hi < -87.0f) return ff{0.0f, 0.0f};
+  if (y.hi > 87.0f) return ff{__int_as_float(0x7f800000), 0.0f};
+  if (y.hi <= 0.0f) return ff_exp_neg(y, tab);
+  return ff_div(ff{1.0f, 0.0f}, ff_exp_neg(ff{-y.hi, -y.lo}, tab));
+}
+
+// ln of a positive float-float: ln(hi) + lo / hi (|lo / hi| <= 2^-24, so the
+// dropped term is below 2^-49)
+__device__ __forceinline__ ff ff_log_ff(ff x, const float (*tab)[2]) {
+  const ff l = ff_log(x.hi, tab);
+  return fast_two_sum(l.hi, __fadd_rn(l.lo, __fdiv_rn(x.lo, x.hi)));
+}
+
+// sqrt of a positive float-float: the float32 root and one correction by the
+// exact residual x - s^2
+__device__ __forceinline__ ff ff_sqrt(ff x) {
+  const float s = __fsqrt_rn(x.hi);
+  const ff p = two_prod(s, s);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
+  return fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
+}
+
+// the uniform (a + 1/2) * 2^-32 of a 32-bit word, exactly, as float-float
+__device__ __forceinline__ ff u01_ff(uint32_t a) {
+  const unsigned long long k = 2ull * a + 1ull;                   // 33 bits
+  const float hi = __ull2float_rn(k);
+  const float lo = (float)((long long)k - (long long)__float2ull_rz(hi));  // |k - hi| < 2^9: exact
+  return ff{__fmul_rn(hi, 0x1p-33f), __fmul_rn(lo, 0x1p-33f)};
+}
+
+// a 64-bit integer (|k| < 2^48) as float-float, exactly
+__device__ __forceinline__ ff ll_to_ff(long long k) {
+  const float hi = __ll2float_rn(k);
+  return ff{hi, (float)(k - __float2ll_rz(hi))};
+}
+
+// cos and sin of 2 pi u for u = (b + 1/2) * 2^-32: the quadrant and the nearest
+// of the points j pi / 64 from the word's bits (exact), then the Taylor series
+// of the residual angle |phi| <= pi / 128 (tables: COVGPU_SINCOS_TAB)
+__device__ __forceinline__ void ff_cossin_2pi(uint32_t b, const float (*tab)[4], ff& c, ff& s) {
+  const unsigned long long k = 2ull * b + 1ull;                    // 4u = k * 2^-31
+  const unsigned q = (unsigned)(k >> 31);                          // quadrant 0..3
+  const unsigned long long fk = k & 0x7FFFFFFFull;                 // f = fk * 2^-31 in [0, 1)
+  const unsigned j = (unsigned)((fk + (1ull << 25)) >> 26);        // nearest j / 32, j = 0..32
+  const ff r = ll_to_ff((long long)fk - ((long long)j << 26));     // (f - j/32) * 2^31
+  const ff phi = ff_mul(ff{COVGPU_PI_2_HI, COVGPU_PI_2_LO}, ff{__fmul_rn(r.hi, 0x1p-31f), __fmul_rn(r.lo, 0x1p-31f)});
+  const ff p2 = ff_mul(phi, phi);
+  const float x2 = p2.hi;
+  // sin phi = phi - phi^3/6 + phi (phi^4/120 - phi^6/5040); cos phi = 1 - phi^2/2 + phi^4/24 - phi^6/720
+  const ff third = ff_mul(phi, ff_div(p2, ff{6.0f, 0.0f}));
+  const float st = __fmul_rn(__fmul_rn(x2, x2), __fsub_rn(0.00833333377f, __fmul_rn(x2, 0.000198412701f)));
+  const ff sphi = ff_add(ff_add(phi, ff{-third.hi, -third.lo}), two_prod(phi.hi, st));
+  const float ct = __fmul_rn(__fmul_rn(x2, x2), __fsub_rn(0.0416666679f, __fmul_rn(x2, 0.00138888892f)));
+  const ff half = ff{__fmul_rn(p2.hi, 0.5f), __fmul_rn(p2.lo, 0.5f)};
+  const ff cphi = ff_add(ff_add(ff{1.0f, 0.0f}, ff{-half.hi, -half.lo}), ff{ct, 0.0f});
+  const ff sj = ff{tab[j][0], tab[j][1]}, cj = ff{tab[j][2], tab[j][3]};
+  const ff ms = ff_mul(sj, sphi), mc = ff_mul(cj, sphi);
+  const ff sn = ff_add(ff_mul(sj, cphi), mc);                     // sin(j pi/64 + phi)
+  const ff cs = ff_add(ff_mul(cj, cphi), ff{-ms.hi, -ms.lo});      // cos(j pi/64 + phi)
+  switch (q) {                                                      // + q * pi / 2
+    case 0: c = cs; s = sn; break;
+    case 1: c = ff{-sn.hi, -sn.lo}; s = cs; break;
+    case 2: c = ff{-cs.hi, -cs.lo}; s = ff{-sn.hi, -sn.lo}; break;
+    default: c = sn; s = ff{-cs.hi, -cs.lo}; break;
+  }
+}
+
+// Box-Muller in float-float: z0 = r cos(2 pi u2), z1 = r sin(2 pi u2), r = sqrt(-2 ln u1)
+__device__ __forceinline__ void box_muller_ff(uint32_t wa, uint32_t wb, const float (*ln_tab)[2],
+                                              const float (*sc_tab)[4], ff& z0, ff& z1) {
+  const ff l = ff_log_ff(u01_ff(wa), ln_tab);
+  const ff r = ff_sqrt(ff{__fmul_rn(l.hi, -2.0f), __fmul_rn(l.lo, -2.0f)});
+  ff c, s;
+  ff_cossin_2pi(wb, sc_tab, c, s);
+  z0 = ff_mul(r, c);
+  z1 = ff_mul(r, s);
+}
+
+// round half to even of a float-float (|x| < 2^22)
+__device__ __forceinline__ float ff_rint(ff x) {
+  const float k = floorf(x.hi);
+  const float f = __fsub_rn(x.hi, k);                // exact
+  const float d = __fsub_rn(f, 0.5f);                // exact
+  if (d > -x.lo) return __fadd_rn(k, 1.0f);          // above the midpoint
+  if (d < -x.lo) return k;                           // below it
+  return fmodf(k, 2.0f) == 0.0f ? k : __fadd_rn(k, 1.0f);  // a tie: to even
+}
+
+// a float64 as float-float (to about 2^-48)
+__device__ __forceinline__ ff d2ff(double x) {
+  const float hi = __double2float_rn(x);
+  return ff{hi, __double2float_rn(__dsub_rn(x, (double)hi))};
+}
+__device__ __forceinline__ double ff2d(ff x) { return __dadd_rn((double)x.hi, (double)x.lo); }
+
+// utils.py:156-236 sample() of a distribution that is a function of one standard
+// normal z, in float-float; the result as the float64 the reference stores
+__device__ __forceinline__ double sample_ff(const covgpu_dur_par& d, ff z) {
+  const ff y = ff_add(d2ff(d.a), ff_mul(d2ff(d.b), z));
+  switch (d.code) {
+    case COVGPU_DIST_LOGNORMAL_INT: return (double)ff_rint(ff_exp(y, COVGPU_EXP_TAB));
+    case COVGPU_DIST_LOGNORMAL: return ff2d(ff_exp(y, COVGPU_EXP_TAB));
+    case COVGPU_DIST_NORMAL: return ff2d(y);
+    case COVGPU_DIST_NORMAL_INT: return (double)ff_rint(y.hi < 0.0f ? ff{-y.hi, -y.lo} : y);
+    case COVGPU_DIST_NORMAL_POS: return fabs(ff2d(y));
+    default: return 0.0;
+  }
+}
+
+// 2^x for a float-float x: exp(x ln 2)
+__device__ __forceinline__ double exp2_ff(ff x) {
+  return ff2d(ff_exp(ff_mul(x, ff{COVGPU_LN2_FF_HI, COVGPU_LN2_FF_LO}), COVGPU_EXP_TAB));
 }
 
 // calc_VE (immunity.py:216-247) for eff = nab * imm with ln(imm) given:

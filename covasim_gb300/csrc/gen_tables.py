@@ -1,9 +1,11 @@
-"""Generate covgpu_tables.h: float-float tables for the NAb-efficacy math.
+"""Generate covgpu_tables.h: float-float tables for the float64 steps of the path.
 
-ln(c_j) for the reduction points c_j = 1 + j/128 (j = -40..55) and 2^(j/64)
-(j = 0..63), each as a pair of float32 (hi, lo) with hi + lo equal to the
-value to about 2^-48. Values come from Python's decimal module at 50 digits,
-so the tables are the same on every platform. Run from the repository root:
+ln(c_j) for the reduction points c_j = 1 + j/128 (j = -40..55), 2^(j/64)
+(j = 0..63), and sin / cos of j * pi / 64 (j = 0..32), each as a pair of
+float32 (hi, lo) with hi + lo equal to the value to about 2^-48, plus pi / 2
+and ln 2 as pairs. Values come from Python's decimal module at 50 digits
+(sin and cos by their Taylor series, pi by Machin's formula), so the tables
+are the same on every platform. Run from the repository root:
 
     python covasim_gb300/csrc/gen_tables.py
 """
@@ -52,6 +54,42 @@ def ln2_64_parts():
     return f32(hi), mid, lo
 
 
+def pi_decimal():
+    """pi = 16 atan(1/5) - 4 atan(1/239) (Machin), to the context precision."""
+    def atan_inv(n):
+        x = Decimal(1) / n
+        x2, term, total, k = x * x, x, x, 1
+        while True:
+            term *= -x2
+            k += 2
+            nxt = total + term / k
+            if nxt == total:
+                return total
+            total = nxt
+    return 16 * atan_inv(5) - 4 * atan_inv(239)
+
+
+def sin_cos(x):
+    """(sin x, cos x) by their Taylor series, for |x| <= pi / 2."""
+    s, c = Decimal(0), Decimal(0)
+    term, k = x, 1
+    while abs(term) > Decimal(10) ** -60:
+        s += term
+        term = -term * x * x / ((k + 1) * (k + 2))
+        k += 2
+    term, k = Decimal(1), 0
+    while abs(term) > Decimal(10) ** -60:
+        c += term
+        term = -term * x * x / ((k + 1) * (k + 2))
+        k += 2
+    return s, c
+
+
+def sincos_table():
+    pi = pi_decimal()
+    return [tuple(split(v) for v in sin_cos(pi * j / 64)) for j in range(33)]
+
+
 def hexf(x):
     return float(x).hex() + 'f'
 
@@ -79,6 +117,15 @@ def main():
     lines += [f'  {{{hexf(h)}, {hexf(l)}}},' for h, l in lt]
     lines += ['};', '__device__ const float COVGPU_EXP_TAB[COVGPU_EXP_N][2] = {']
     lines += [f'  {{{hexf(h)}, {hexf(l)}}},' for h, l in et]
+    lines += ['};']
+    pi = pi_decimal()
+    ph, pl = split(pi / 2)
+    lh, ll = split(Decimal(2).ln())
+    lines += [f'#define COVGPU_PI_2_HI {hexf(ph)}', f'#define COVGPU_PI_2_LO {hexf(pl)}',
+              f'#define COVGPU_LN2_FF_HI {hexf(lh)}', f'#define COVGPU_LN2_FF_LO {hexf(ll)}',
+              '// sin and cos of j * pi / 64, j = 0..32: {sin hi, sin lo, cos hi, cos lo}',
+              '__device__ const float COVGPU_SINCOS_TAB[33][4] = {']
+    lines += [f'  {{{hexf(sv[0])}, {hexf(sv[1])}, {hexf(cv[0])}, {hexf(cv[1])}}},' for sv, cv in sincos_table()]
     lines += ['};', '']
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'covgpu_tables.h')
     with open(path, 'w') as f:

@@ -254,3 +254,191 @@ def update_nab_gpu(people, inds):
     kh, kl = split_kin(people.pars['nab_kin'])
     k = people.t - people.t_nab_event[inds]
     people.nab[inds] = update_nab_ff(people.nab[inds], people.peak_nab[inds], kh[k], kl[k])
+
+
+# ----------------------------------------------------------------- infection draws (People.infect)
+def _pi_decimal():
+    def atan_inv(n):
+        x = Decimal(1) / n
+        x2, term, total, k = x * x, x, x, 1
+        while True:
+            term *= -x2
+            k += 2
+            nxt = total + term / k
+            if nxt == total:
+                return total
+            total = nxt
+    return 16 * atan_inv(5) - 4 * atan_inv(239)
+
+
+def _sin_cos(x):
+    s, c = Decimal(0), Decimal(0)
+    term, k = x, 1
+    while abs(term) > Decimal(10) ** -60:
+        s += term
+        term = -term * x * x / ((k + 1) * (k + 2))
+        k += 2
+    term, k = Decimal(1), 0
+    while abs(term) > Decimal(10) ** -60:
+        c += term
+        term = -term * x * x / ((k + 1) * (k + 2))
+        k += 2
+    return s, c
+
+
+_PI = _pi_decimal()
+PI_2_HI, PI_2_LO = (F32(v) for v in _split(_PI / 2))
+LN2_FF_HI, LN2_FF_LO = (F32(v) for v in _split(_LN2))
+SINCOS_TAB = np.array([[*_split(s), *_split(c)] for s, c in (_sin_cos(_PI * j / 64) for j in range(33))], F32)
+
+
+def ff_exp(yh, yl):
+    """exp of a float-float (covgpu_ff.cuh ff_exp): 0 below -87, inf above 87."""
+    yh, yl = _a(yh), _a(yl)
+    under, over, pos = yh < F32(-87), yh > F32(87), yh > 0
+    ah = np.where(pos, -yh, yh)
+    al = np.where(pos, -yl, yl)
+    ah = np.where(under | over, F32(0), ah).astype(F32)
+    al = np.where(under | over, F32(0), al).astype(F32)
+    eh, el = ff_exp_neg(ah, al)
+    ih, il = ff_div(np.ones_like(eh), np.zeros_like(el), eh, el)
+    hi = np.where(pos, ih, eh)
+    lo = np.where(pos, il, el)
+    hi = np.where(under, F32(0), np.where(over, F32(np.inf), hi)).astype(F32)
+    lo = np.where(under | over, F32(0), lo).astype(F32)
+    return hi, lo
+
+
+def ff_log_ff(xh, xl):
+    lh, ll = ff_log(xh)
+    return fast_two_sum(lh, ll + _a(xl) / _a(xh))
+
+
+def ff_sqrt(xh, xl):
+    xh, xl = _a(xh), _a(xl)
+    s = np.sqrt(xh)
+    ph, pl = two_prod(s, s)
+    r = ((xh - ph) - pl) + xl
+    return fast_two_sum(s, r / (F32(2) * s))
+
+
+def u01_ff(a):
+    """(a + 1/2) * 2^-32 of 32-bit words as exact float-float pairs."""
+    k = 2 * np.asarray(a, dtype=np.uint64).astype(np.int64) + 1
+    hi = k.astype(np.float64).astype(F32)
+    lo = (k - hi.astype(np.int64)).astype(F32)
+    return hi * F32(2.0 ** -33), lo * F32(2.0 ** -33)
+
+
+def ll_to_ff(k):
+    k = np.asarray(k, dtype=np.int64)
+    hi = k.astype(np.float64).astype(F32)
+    return hi, (k - hi.astype(np.int64)).astype(F32)
+
+
+def ff_cossin_2pi(b):
+    """(cos, sin) of 2 pi (b + 1/2) 2^-32 as float-float pairs (covgpu_ff.cuh ff_cossin_2pi)."""
+    k = 2 * np.asarray(b, dtype=np.uint64).astype(np.int64) + 1
+    q = k >> 31
+    fk = k & 0x7FFFFFFF
+    j = (fk + (1 << 25)) >> 26
+    rh, rl = ll_to_ff(fk - (j << 26))
+    ph, pl = ff_mul(PI_2_HI, PI_2_LO, rh * F32(2.0 ** -31), rl * F32(2.0 ** -31))
+    p2h, p2l = ff_mul(ph, pl, ph, pl)
+    x2 = p2h
+    dh, dl = ff_div(p2h, p2l, F32(6), F32(0))
+    th, tl = ff_mul(ph, pl, dh, dl)
+    st = (x2 * x2) * (F32(0.00833333377) - x2 * F32(0.000198412701))
+    ah, al = ff_add(ph, pl, -th, -tl)
+    bh, bl = two_prod(ph, st)
+    sph, spl = ff_add(ah, al, bh, bl)
+    ct = (x2 * x2) * (F32(0.0416666679) - x2 * F32(0.00138888892))
+    hh, hl = p2h * F32(0.5), p2l * F32(0.5)
+    ch_, cl_ = ff_add(F32(1), F32(0), -hh, -hl)
+    cph, cpl = ff_add(ch_, cl_, ct, F32(0))
+    sjh, sjl, cjh, cjl = (SINCOS_TAB[j, i] for i in range(4))
+    msh, msl = ff_mul(sjh, sjl, sph, spl)
+    mch, mcl = ff_mul(cjh, cjl, sph, spl)
+    x1h, x1l = ff_mul(sjh, sjl, cph, cpl)
+    snh, snl = ff_add(x1h, x1l, mch, mcl)
+    x2h, x2l = ff_mul(cjh, cjl, cph, cpl)
+    csh, csl = ff_add(x2h, x2l, -msh, -msl)
+    ch = np.select([q == 0, q == 1, q == 2], [csh, -snh, -csh], snh).astype(F32)
+    cl = np.select([q == 0, q == 1, q == 2], [csl, -snl, -csl], snl).astype(F32)
+    sh = np.select([q == 0, q == 1, q == 2], [snh, csh, -snh], -csh).astype(F32)
+    sl = np.select([q == 0, q == 1, q == 2], [snl, csl, -snl], -csl).astype(F32)
+    return (ch, cl), (sh, sl)
+
+
+def box_muller_ff(wa, wb):
+    """(z0, z1) as float-float pairs from two Philox words (covgpu_ff.cuh box_muller_ff)."""
+    lh, ll = ff_log_ff(*u01_ff(wa))
+    rh, rl = ff_sqrt(lh * F32(-2), ll * F32(-2))
+    (ch, cl), (sh, sl) = ff_cossin_2pi(wb)
+    return ff_mul(rh, rl, ch, cl), ff_mul(rh, rl, sh, sl)
+
+
+def ff_rint(xh, xl):
+    """Round half to even of a float-float, as a float32."""
+    xh, xl = _a(xh), _a(xl)
+    k = np.floor(xh)
+    d = (xh - k) - F32(0.5)
+    up = d > -xl
+    down = d < -xl
+    even = np.fmod(k, F32(2)) == 0
+    return np.where(up, k + F32(1), np.where(down, k, np.where(even, k, k + F32(1)))).astype(F32)
+
+
+def d2ff(x):
+    x = np.asarray(x, dtype=np.float64)
+    hi = x.astype(F32)
+    return hi, (x - hi.astype(np.float64)).astype(F32)
+
+
+def ff2d(xh, xl):
+    return _a(xh).astype(np.float64) + _a(xl).astype(np.float64)
+
+
+DIST_LOGNORMAL_INT, DIST_LOGNORMAL, DIST_NORMAL, DIST_NORMAL_INT, DIST_NORMAL_POS, DIST_ZERO = range(6)
+
+
+def dist_code(dist):
+    """(code, a, b) of a duration distribution as the host packs it (lognormal: the normal's mean and sd)."""
+    name, p1, p2 = dist['dist'], dist['par1'], dist['par2']
+    codes = {'lognormal_int': 0, 'lognorm_int': 0, 'lognormal': 1, 'lognorm': 1, 'normal': 2, 'norm': 2,
+             'normal_int': 3, 'normal_pos': 4}
+    code = codes[name]
+    if code in (0, 1):
+        if not p1 > 0:
+            return DIST_ZERO, 0.0, 0.0
+        return code, float(np.log(p1 ** 2 / np.sqrt(p2 ** 2 + p1 ** 2))), float(np.sqrt(np.log(p2 ** 2 / p1 ** 2 + 1)))
+    return code, float(p1), float(p2)
+
+
+def sample_ff(dist, zh, zl):
+    """utils.py:156-236 sample() of a one-normal distribution in float-float (covgpu_ff.cuh sample_ff)."""
+    code, a, b = dist_code(dist)
+    zh, zl = _a(zh), _a(zl)
+    if code == DIST_ZERO:
+        return np.zeros(zh.shape)
+    ah, al = d2ff(a)
+    bh, bl = d2ff(b)
+    mh, ml = ff_mul(np.full_like(zh, bh), np.full_like(zl, bl), zh, zl)
+    yh, yl = ff_add(np.full_like(zh, ah), np.full_like(zl, al), mh, ml)
+    if code == DIST_LOGNORMAL_INT:
+        return ff_rint(*ff_exp(yh, yl)).astype(np.float64)
+    if code == DIST_LOGNORMAL:
+        return ff2d(*ff_exp(yh, yl))
+    if code == DIST_NORMAL:
+        return ff2d(yh, yl)
+    if code == DIST_NORMAL_INT:
+        neg = yh < 0
+        return ff_rint(np.where(neg, -yh, yh), np.where(neg, -yl, yl)).astype(np.float64)
+    return np.abs(ff2d(yh, yl))
+
+
+def exp2_ff(x):
+    """2^x of float64 values as the GPU computes update_peak_nab's 2**init (float-float)."""
+    xh, xl = d2ff(x)
+    yh, yl = ff_mul(xh, xl, np.full_like(xh, LN2_FF_HI), np.full_like(xl, LN2_FF_LO))
+    return ff2d(*ff_exp(yh, yl))

@@ -72,13 +72,24 @@ def dist_consumes_draws(dist):
 
 
 class TableDraws:
-    """Per-agent draw table [N_DRAWS] indexed by agent (see philox.N_*)."""
+    """Per-agent draw table [N_DRAWS] indexed by agent (see philox.N_*).
 
-    def __init__(self, table_fn):
+    With ``ff_fn`` (the CUDA library's arithmetic) the normals are float-float
+    pairs and samples are formed in float-float (``gpu_arith.sample_ff``)."""
+
+    def __init__(self, table_fn, ff_fn=None):
         self.table_fn = table_fn  # inds -> float64 [len(inds), N_DRAWS]
+        self.ff_fn = ff_fn        # inds -> (z_hi [n, 6], z_lo [n, 6], u [n, 4])
 
     def begin(self, inds):
         self._inds = np.asarray(inds)
+        if self.ff_fn is not None:
+            if len(self._inds):
+                self._zh, self._zl, self._u = self.ff_fn(self._inds)
+            else:
+                self._zh = self._zl = np.zeros((0, 6), np.float32)
+                self._u = np.zeros((0, 4))
+            return
         self._tab = self.table_fn(self._inds) if len(self._inds) else np.zeros((0, ph.N_DRAWS))
 
     def _rows(self, inds):
@@ -86,9 +97,15 @@ class TableDraws:
         return np.searchsorted(self._inds, np.asarray(inds))
 
     def normal(self, slot, inds, dist):
+        if self.ff_fn is not None:
+            from .gpu_arith import sample_ff
+            r = self._rows(inds)
+            return sample_ff(dist, self._zh[r, slot], self._zl[r, slot])
         return sample_from_normal(dist, self._tab[self._rows(inds), slot])
 
     def uniform(self, slot, inds):
+        if self.ff_fn is not None:
+            return self._u[self._rows(inds), slot - ph.U_SYMP]
         return self._tab[self._rows(inds), slot]
 
 
@@ -114,6 +131,11 @@ class SequentialDraws:
 def philox_table(seed, day, call_tag):
     k0, k1 = ph.seed_key(seed)
     return lambda inds: ph.infect_draws(k0, k1, day, call_tag, inds)
+
+
+def philox_table_ff(seed, day, call_tag):
+    k0, k1 = ph.seed_key(seed)
+    return lambda inds: ph.infect_draws_ff(k0, k1, day, call_tag, inds)
 
 
 class OraclePeople:
@@ -455,7 +477,11 @@ def update_peak_nab(people, inds, nab_pars, symp=None, draws=None):
         people.peak_nab[prior_nab_inds] *= nab_pars['nab_boost']
     if len(no_prior_nab_inds):
         init_nab = draws.normal(ph.N_NAB, no_prior_nab_inds, nab_pars['nab_init'])
-        no_prior_nab = 2 ** init_nab
+        if getattr(people, 'arith', 'reference') == 'gpu':
+            from .gpu_arith import exp2_ff
+            no_prior_nab = exp2_ff(init_nab)  # 2**init in float-float, as the GPU forms it
+        else:
+            no_prior_nab = 2 ** init_nab
         if symp is not None:
             prior_symp = np.full(pars['pop_size'], np.nan)
             prior_symp[symp['asymp']] = pars['rel_imm_symp']['asymp']

@@ -197,3 +197,22 @@ def trace_draws(k0, k1, day, layer, agents):
     a = np.asarray(agents, dtype=np.int64)
     b = philox4x32_10(a, int(layer), day, TAG_TRACE, k0, k1)
     return u01_52(b[0], b[1])
+
+
+def infect_draws_ff(k0, k1, day, call_tag, agents):
+    """The draws of ``infect_draws`` as the CUDA library forms them: the six
+    normals as float-float pairs (Box-Muller in float-float, oracle.gpu_arith)
+    and the four uniforms. Returns (z_hi [n, 6], z_lo [n, 6], u [n, 4])."""
+    from .gpu_arith import box_muller_ff
+    a = np.asarray(agents, dtype=np.int64)
+    tag = TAG_INFECT | int(call_tag)
+    b0 = philox4x32_10(a, 0, day, tag, k0, k1)
+    b1 = philox4x32_10(a, 1, day, tag, k0, k1)
+    b2 = philox4x32_10(a, 2, day, tag, k0, k1)
+    zh = np.empty((len(a), 6), dtype=np.float32)
+    zl = np.empty((len(a), 6), dtype=np.float32)
+    for (wa, wb), (i, j) in (((b0[0], b0[1]), (0, 1)), ((b0[2], b0[3]), (2, 3)), ((b1[0], b1[1]), (4, 5))):
+        (z0h, z0l), (z1h, z1l) = box_muller_ff(wa, wb)
+        zh[:, i], zl[:, i], zh[:, j], zl[:, j] = z0h, z0l, z1h, z1l
+    u = np.stack([u01_32(b1[2]), u01_32(b1[3]), u01_32(b2[0]), u01_32(b2[1])], axis=1)
+    return zh, zl, u

@@ -21,7 +21,7 @@ import numpy as np
 
 from . import philox as ph
 from .kernels import compute_viral_load, compute_trans_sus, compute_infections
-from .people import (OraclePeople, TableDraws, SequentialDraws, philox_table, update_nab,
+from .people import (OraclePeople, TableDraws, SequentialDraws, philox_table, philox_table_ff, update_nab,
                      STATES, FLOWS, FLOWS_VARIANT)
 from .gpu_arith import update_nab_gpu
 
@@ -113,6 +113,8 @@ class OracleSim:
     # ------------------------------------------------------------------
     def _draws(self, call_tag):
         if self.rng == 'philox':
+            if self.arith == 'gpu':  # the CUDA library's float-float normals and samples
+                return TableDraws(None, ff_fn=philox_table_ff(self.seed, self.t, call_tag))
             return TableDraws(philox_table(self.seed, self.t, call_tag))
         return SequentialDraws(self.rs_numpy)
 

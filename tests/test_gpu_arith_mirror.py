@@ -53,5 +53,33 @@ def test_tables_match_the_cuda_header():
     consts = [ga.LN2_HI, ga.LN2_LO, ga.LN2_LO2, ga.INV_LN2_64, ga.LN2_64_HI, ga.LN2_64_MID, ga.LN2_64_LO]
     assert vals[:7] == [float(c) for c in consts]
     tab = np.array(vals[7:], dtype=np.float32)
-    assert np.array_equal(tab[:2 * len(ga.LN_TAB)].reshape(-1, 2), ga.LN_TAB)
-    assert np.array_equal(tab[2 * len(ga.LN_TAB):].reshape(-1, 2), ga.EXP_TAB)
+    n_ln, n_exp = 2 * len(ga.LN_TAB), 2 * len(ga.EXP_TAB)
+    assert np.array_equal(tab[:n_ln].reshape(-1, 2), ga.LN_TAB)
+    assert np.array_equal(tab[n_ln:n_ln + n_exp].reshape(-1, 2), ga.EXP_TAB)
+    rest = tab[n_ln + n_exp:]
+    assert list(rest[:4]) == [ga.PI_2_HI, ga.PI_2_LO, ga.LN2_FF_HI, ga.LN2_FF_LO]
+    assert np.array_equal(rest[4:].reshape(-1, 4), ga.SINCOS_TAB)
+
+
+def test_float_float_infection_draws_track_float64():
+    """Box-Muller, exp and the duration samples in float-float (the GPU's infect
+    arithmetic) against the reference's float64 formulas."""
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 2 ** 32, 300_000, dtype=np.uint64)
+    b = rng.integers(0, 2 ** 32, 300_000, dtype=np.uint64)
+    (z0h, z0l), (z1h, z1l) = ga.box_muller_ff(a, b)
+    u1, u2 = (a.astype(np.float64) + 0.5) * 2.0 ** -32, (b.astype(np.float64) + 0.5) * 2.0 ** -32
+    r = np.sqrt(-2 * np.log(u1))
+    assert np.abs(ga.ff2d(z0h, z0l) - r * np.cos(2 * np.pi * u2)).max() < 1e-12
+    assert np.abs(ga.ff2d(z1h, z1l) - r * np.sin(2 * np.pi * u2)).max() < 1e-12
+    z = rng.standard_normal(300_000)
+    for dist in (dict(dist='lognormal_int', par1=4.5, par2=1.5), dict(dist='lognormal_int', par1=18.1, par2=6.3),
+                 dict(dist='normal_int', par1=3.0, par2=2.0)):
+        code, m, s = ga.dist_code(dist)
+        ref = np.round(np.exp(m + s * z)) if code == 0 else np.round(np.abs(m + s * z))
+        assert np.array_equal(ga.sample_ff(dist, *ga.d2ff(z)), ref), dist
+    x = rng.normal(0, 2, 300_000)
+    assert np.abs(ga.exp2_ff(x) / 2 ** x - 1).max() < 1e-11
+    rint_in = np.array([2.5, 3.5, -2.5, 2.0, 2.0, 7.5], dtype=np.float32)
+    rint_lo = np.array([0, 0, 0, -1e-9, 1e-9, 1e-9], dtype=np.float32)
+    assert list(ga.ff_rint(rint_in, rint_lo)) == [2, 4, -2, 2, 2, 8]
