@@ -56,7 +56,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--batch', type=int, default=16, help='sims of the batched measurement (0: skip)')
     ap.add_argument('--no-adjoint', action='store_true', help='skip the forward/adjoint cost measurement')
-    ap.add_argument('--edge-tile', default='auto', help="edge-pass tile (1024/2048/4096/8192) or 'auto' (autotuner)")
+    ap.add_argument('--edge-tile', default='auto',
+                    help="edge-pass tile (1024/2048/4096/8192, suffix 'r' for the resident bitmap) or 'auto' (autotuner)")
     ap.add_argument('--gpu-population', action='store_true',
                     help='large / batch256 workloads: build the populations on the device')
     ap.add_argument('--workload', default='hybrid1m', choices=['hybrid1m', 'large', 'batch256'],
@@ -244,7 +245,7 @@ def gpu_arm(args, world, rank):
         from covasim_gb300.autotune import tune_edge_tile
         _, tile_ms = tune_edge_tile(st)
     else:
-        st.set_edge_tile(int(args.edge_tile))
+        st.apply_edge_tile(args.edge_tile)
     snap = st.snapshot()
     seeds = choose_seed_infections(sim['rand_seed'], sim['pop_size'], sim['pop_infected'])
 
@@ -321,7 +322,7 @@ def gpu_arm(args, world, rank):
         d2h = 0
 
         def e2e_step():
-            s = cv.Sim(sim_pars(args, seed), popdict=host_pop, person=host_person, edge_tile=st.edge_tile)
+            s = cv.Sim(sim_pars(args, seed), popdict=host_pop, person=host_person, edge_tile=st.edge_tile_label)
             s.run()
             return s
 
@@ -344,7 +345,7 @@ def gpu_arm(args, world, rank):
     adjoint = adjoint_arm(args) if not args.no_adjoint else None
 
     return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched, adjoint=adjoint,
-                edge_tile=st.edge_tile, tile_ms=tile_ms,
+                edge_tile=st.edge_tile_label, tile_ms=tile_ms,
                 launches=launches_per_step * args.steps, init_s=init_s, res=res, spec=sim.spec,
                 cum_infections=float(res['new_infections'].sum() + sim['pop_infected']))
 
@@ -541,7 +542,7 @@ def large_arm(args, n=20_000_000, days=365):
                           cv.variant(dict(rel_beta=1.7), days=120, n_imports=100, label='v1.7')],
                 interventions=[cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)])
     t0 = time.perf_counter()
-    sim = cv.Sim(pars, edge_tile=4096 if args.edge_tile == 'auto' else int(args.edge_tile),
+    sim = cv.Sim(pars, edge_tile=None if args.edge_tile == 'auto' else args.edge_tile,
                  gpu_population=args.gpu_population)
     sim.initialize()
     init_s = time.perf_counter() - t0
@@ -617,7 +618,7 @@ def batch_arm(args, n_sims=256, days=120):
     singles = []
     for k in range(n_sims):
         s = cv.Sim(dict(sims[k].pars), popdict=sims[k].popdict, person=sims[k]._person,
-                   edge_tile=st.edge_tile)
+                   edge_tile=st.edge_tile_label)
         s.initialize()
         singles.append((s, s.state.snapshot()))
 

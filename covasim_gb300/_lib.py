@@ -107,7 +107,7 @@ class Lik(C.Structure):
 class State(C.Structure):
     _fields_ = [
         ('n', C.c_int64), ('n_sims', C.c_int32), ('n_segments', C.c_int32), ('n_tiles', C.c_int64),
-        ('n_agent_blocks', C.c_int64), ('edge_tile', C.c_int32), ('_pad_tile', C.c_int32),
+        ('n_agent_blocks', C.c_int64), ('edge_tile', C.c_int32), ('edge_resident', C.c_int32),
         ('flags', C.c_void_p), ('vstate', C.c_void_p),
         ('symp_prob', C.c_void_p), ('severe_prob', C.c_void_p), ('crit_prob', C.c_void_p), ('death_prob', C.c_void_p),
         ('rel_trans', C.c_void_p), ('rel_sus', C.c_void_p),
@@ -163,6 +163,8 @@ def lib():
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
+        L.covgpu_edge_resident_bytes.argtypes = [sp]
+        L.covgpu_edge_resident_bytes.restype = i64
         L.covgpu_trace_index_scratch.argtypes = [i64]
         L.covgpu_trace_index_scratch.restype = i64
         L.covgpu_trace_index.argtypes = [vp, vp, i64, i64, i64, vp, vp, vp, vp, vp]
@@ -217,5 +219,5 @@ POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts'
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
             'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
-            'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index',
+            'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index', 'covgpu_edge_resident_bytes',
             'covgpu_pop_scan_scratch'] + POP_FUNCS

@@ -39,26 +39,40 @@ def _one_run(state, snap, seeds, t1):
     state.run_days(0, t1, open_prev=False, close_last=True, use_graph=True)
 
 
+def _candidates(state, tiles):
+    """(tile, resident) pairs: every tile, and the resident-bitmap variant where it can run."""
+    out = [(int(t), False) for t in tiles]
+    if state.resident_possible():
+        out += [(int(t), True) for t in tiles if int(t) >= 4096]
+    return out
+
+
+def _label(tile, resident):
+    return f'{tile}{"r" if resident else ""}'
+
+
 def tune_edge_tile(state, days=None, candidates=L.EDGE_TILES, reps=2, cache_file=None):
-    """Pick the edge tile for ``state`` (a freshly initialised ``BatchState`` whose
-    sims have not run) by timing ``reps`` whole runs of ``days`` days (default:
-    all) per candidate. Leaves the state rewound, with the best tile set.
-    Returns (best tile, {tile: ms per run})."""
+    """Pick the edge-pass variant for ``state`` (a freshly initialised ``BatchState``
+    whose sims have not run): each tile size, and for one sim also the variant
+    with the source bitmap resident in shared memory, timed over ``reps`` whole
+    runs of ``days`` days (default: all). Leaves the state rewound with the best
+    variant set. Returns (best label, {label: ms per run}); a label is the tile
+    size, suffixed 'r' for the resident variant."""
     key = workload_signature(state) + f'|days={days}'
     if cache_file and os.path.exists(cache_file) and key not in _CACHE:
         with open(cache_file) as f:
             _CACHE.update(json.load(f))
     snap = state.snapshot()
     if key in _CACHE:
-        best = int(_CACHE[key]['best'])
-        state.set_edge_tile(best)
-        return best, {int(k): v for k, v in _CACHE[key]['ms'].items()}
+        best = str(_CACHE[key]['best'])
+        state.set_edge_tile(int(best.rstrip('r')), resident=best.endswith('r'))
+        return best, dict(_CACHE[key]['ms'])
     t1 = min(sp.npts for sp in state.specs) if days is None else int(days)
     seeds = [choose_seed_infections(sp.pars['rand_seed'], sp.n, sp.pars['pop_infected']) for sp in state.specs]
     stream = torch.cuda.current_stream()
     ms = {}
-    for tile in candidates:
-        state.set_edge_tile(tile)
+    for tile, resident in _candidates(state, candidates):
+        state.set_edge_tile(tile, resident=resident)
         _one_run(state, snap, seeds, t1)  # capture and warm
         times = []
         for _ in range(reps):
@@ -69,9 +83,9 @@ def tune_edge_tile(state, days=None, candidates=L.EDGE_TILES, reps=2, cache_file
             b.record(stream)
             b.synchronize()
             times.append(a.elapsed_time(b))
-        ms[int(tile)] = float(np.median(times))
+        ms[_label(tile, resident)] = float(np.median(times))
     best = min(ms, key=ms.get)
-    state.set_edge_tile(best)
+    state.set_edge_tile(int(best.rstrip('r')), resident=best.endswith('r'))
     state.restore(snap)
     _CACHE[key] = {'best': best, 'ms': ms}
     if cache_file:

@@ -44,7 +44,7 @@ class BatchSim:
         self.sims = list(sims)
         self.use_graph = use_graph
         self.log = log
-        self.edge_tile = edge_tile  # as Sim's: an int, None (4096) or 'auto'
+        self.edge_tile = edge_tile  # as Sim's: None (4096), a tile, a label such as '8192r', or 'auto'
         self.state = None
 
     def initialize(self):
@@ -68,11 +68,8 @@ class BatchSim:
         if len(npts) != 1:
             raise ValueError('all sims of a batch must have the same number of days')
         self.npts = npts.pop()
-        tile = L.EDGE_TILE if self.edge_tile in (None, 'auto') else int(self.edge_tile)
-        self.state = BatchState(specs, log=self.log, edge_tile=tile)
-        if self.edge_tile == 'auto':
-            from .autotune import tune_edge_tile
-            tune_edge_tile(self.state)
+        self.state = BatchState(specs, log=self.log)
+        self.state.apply_edge_tile(self.edge_tile)
         return self
 
     def seed_infections(self):

@@ -648,25 +648,29 @@ __device__ __forceinline__ double warp_sum_d(double x) {
   return x;
 }
 
-template <bool LIK, int ROUNDS>
-__global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
-  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
-  __shared__ int s_seg;
-  __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
-  if (threadIdx.x == 0) {  // segment owning this tile: last segment with tile_begin <= blockIdx.x
-    int lo = 0, hi = st.n_segments - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
-    }
-    s_seg = lo;
+// The segment owning a tile: the last segment with tile_begin <= tile.
+__device__ __forceinline__ int segment_of_tile(const covgpu_state& st, int64_t tile) {
+  int lo = 0, hi = st.n_segments - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (st.segments[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
   }
-  __syncthreads();
-  const covgpu_layer* L = st.segments + s_seg;
+  return lo;
+}
+
+// One tile (TILE edges) of one segment, NT threads: phase A streams the edges
+// and queues the candidate directions of each warp, phase B drains the queues.
+// RES: the sim's source bitmap is resident in shared memory (s_src, one sim).
+template <bool LIK, int NT, int64_t TILE, bool RES>
+__device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg, int64_t tile,
+                                          const uint32_t* s_src, EdgeQueue& q, LikAcc& acc) {
+  constexpr int ROUNDS = (int)(TILE / ((int64_t)NT * EDGE_VEC));
+  static_assert(ROUNDS >= 1 && TILE % ((int64_t)NT * EDGE_VEC) == 0, "whole rounds per tile");
+  const covgpu_layer* L = st.segments + seg;
   const covgpu_sim_params* sp = st.sims + L->sim;
   SegCtx c;
   c.L = L;
-  c.seg = s_seg;
+  c.seg = seg;
   c.layer = L->layer;
   c.n_edges = L->n_edges;
   c.edge_beta = L->beta;
@@ -683,16 +687,14 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   const bool dynamic = L->dynamic != 0;
   const int32_t* p1 = L->p1;
   const int32_t* p2 = L->p2;
-  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
+  const int64_t e0 = (tile - L->tile_begin) * TILE;
   const int64_t e1 = min(e0 + TILE, c.n_edges);
   const int64_t n_local = sp->n_agents;
   const int32_t off = (int32_t)sp->agent_off;
   const uint32_t thr = dynamic ? bounded_thr((uint32_t)n_local) : 0u;
-  EdgeQueue& q = s_q[threadIdx.x >> 5];
   int qn = 0;  // warp-uniform queue length
-  LikAcc acc;
   for (int r = 0; r < ROUNDS; ++r) {
-    const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
+    const int64_t eb = e0 + ((int64_t)r * NT + threadIdx.x) * EDGE_VEC;
     int32_t a[EDGE_VEC], b[EDGE_VEC];
     if (dynamic) {
       // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
@@ -714,12 +716,20 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
         b[j] = e < e1 ? p2[e] : off;
       }
     }
-    // sources first (every edge, L1-resident bitmap), then the other endpoint's
-    // target bit only where one endpoint is a source; roles are exclusive, so
-    // an edge has at most one candidate direction
+    // sources first (every edge: shared memory, or the L1-resident bitmap), then the
+    // other endpoint's target bit only where one endpoint is a source; roles are
+    // exclusive, so an edge has at most one candidate direction
     uint32_t sa[EDGE_VEC], sb[EDGE_VEC];
 #pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) { sa[j] = src_bit(st.roles, a[j]); sb[j] = src_bit(st.roles, b[j]); }
+    for (int j = 0; j < EDGE_VEC; ++j) {
+      if (RES) {
+        sa[j] = (s_src[a[j] >> 5] >> (a[j] & 31)) & 1u;
+        sb[j] = (s_src[b[j] >> 5] >> (b[j] & 31)) & 1u;
+      } else {
+        sa[j] = src_bit(st.roles, a[j]);
+        sb[j] = src_bit(st.roles, b[j]);
+      }
+    }
 #pragma unroll
     for (int j = 0; j < EDGE_VEC; ++j) {
       const bool in = eb + j < e1;
@@ -735,6 +745,30 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
     }
   }
   if (qn > 0) queue_drain<LIK>(st, c, t, e0, q, qn, acc);
+}
+
+// the likelihood sums of one warp for one (sim, layer), then reset
+__device__ __forceinline__ void lik_flush_warp(const covgpu_state& st, int t, int sim, int layer, LikAcc& acc) {
+  const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
+  if ((threadIdx.x & 31) == 0) {
+    const covgpu_lik& K = st.lik;
+    const int64_t day = (int64_t)sim * K.npts_max + t;
+    if (a != 0.0) atomicAdd(K.ll + day, a);
+    if (K.g_ll && b != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + layer, b);
+  }
+  acc = LikAcc();
+}
+
+// One block per tile.
+template <bool LIK, int ROUNDS>
+__global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
+  __shared__ int s_seg;
+  __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
+  if (threadIdx.x == 0) s_seg = segment_of_tile(st, (int64_t)blockIdx.x);
+  __syncthreads();
+  LikAcc acc;
+  edge_tile<LIK, EDGE_THREADS, TILE, false>(st, t, s_seg, (int64_t)blockIdx.x, nullptr, s_q[threadIdx.x >> 5], acc);
   if (LIK) {  // the tile's sums: one sim, one layer
     __shared__ double s_acc[EDGE_THREADS / 32][2];
     const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
@@ -745,11 +779,77 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
       double x = 0.0, y = 0.0;
       for (int k = 0; k < EDGE_THREADS / 32; ++k) { x += s_acc[k][0]; y += s_acc[k][1]; }
       const covgpu_lik& K = st.lik;
-      const int64_t day = (int64_t)c.sim * K.npts_max + t;
+      const covgpu_layer& L = st.segments[s_seg];
+      const int64_t day = (int64_t)L.sim * K.npts_max + t;
       if (x != 0.0) atomicAdd(K.ll + day, x);
-      if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + c.layer, y);
+      if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + L.layer, y);
     }
   }
+}
+
+// Resident-bitmap variant for a single sim: one block of RES_THREADS per SM
+// loads the sim's source bitmap into shared memory once, then walks the tiles
+// with a stride of the grid (stored and redrawn layers interleave, which
+// balances the blocks); the per-warp queues follow the bitmap in shared memory.
+constexpr int RES_THREADS = 1024;
+template <bool LIK, int64_t TILE>
+__global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state st, int t) {
+  extern __shared__ uint4 s_dyn[];
+  uint32_t* s_src = reinterpret_cast<uint32_t*>(s_dyn);
+  const int64_t words = (st.n + 31) >> 5;
+  for (int64_t k = threadIdx.x; k < words; k += RES_THREADS) s_src[k] = __ldg(st.roles + k);
+  EdgeQueue* s_q = reinterpret_cast<EdgeQueue*>(s_dyn + ((words + 3) >> 2));
+  EdgeQueue& q = s_q[threadIdx.x >> 5];
+  __syncthreads();
+  LikAcc acc;
+  for (int64_t tile = blockIdx.x; tile < st.n_tiles; tile += gridDim.x) {
+    const int seg = segment_of_tile(st, tile);
+    edge_tile<LIK, RES_THREADS, TILE, true>(st, t, seg, tile, s_src, q, acc);
+    if (LIK) lik_flush_warp(st, t, st.segments[seg].sim, st.segments[seg].layer, acc);
+  }
+}
+
+// shared memory of the resident-bitmap variant, 0 when it cannot run
+int64_t edge_res_smem(const covgpu_state* st) {
+  if (st->n_sims != 1 || st->edge_tile < RES_THREADS * EDGE_VEC) return 0;
+  const int64_t words = (st->n + 31) >> 5;
+  const int64_t bytes = 16 * ((words + 3) >> 2) + (int64_t)(RES_THREADS / 32) * (int64_t)sizeof(EdgeQueue);
+  static int max_optin = -1;
+  if (max_optin < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+      max_optin = 0;
+  }
+  return bytes <= max_optin ? bytes : 0;
+}
+
+int n_sms() {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 152;
+  }
+  return sms;
+}
+
+// raise the resident variant's dynamic shared-memory limit (before any capture)
+template <bool LIK>
+int configure_res(int64_t smem) {
+  const void* fns[2] = {reinterpret_cast<const void*>(k_edge_pass_res<LIK, 4096>),
+                        reinterpret_cast<const void*>(k_edge_pass_res<LIK, 8192>)};
+  for (const void* f : fns)
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return COVGPU_CUDA_ERROR;
+  return COVGPU_OK;
+}
+int configure_edge_pass(const covgpu_state* st) {
+  if (!st->edge_resident) return COVGPU_OK;
+  const int64_t smem = edge_res_smem(st);
+  if (!smem) return COVGPU_BADARG;
+  const int rc = configure_res<false>(smem);
+  return rc ? rc : configure_res<true>(smem);
 }
 
 template <bool LIK>
@@ -763,10 +863,24 @@ void launch_edge_tiles(const covgpu_state* st, int t, cudaStream_t s) {
   }
 }
 
+template <bool LIK>
+void launch_edge_res(const covgpu_state* st, int t, cudaStream_t s) {
+  const int64_t smem = edge_res_smem(st);
+  const unsigned grid = (unsigned)(st->n_tiles < n_sms() ? st->n_tiles : n_sms());
+  if (st->edge_tile == 8192) k_edge_pass_res<LIK, 8192><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
+  else k_edge_pass_res<LIK, 4096><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
+}
+
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
   if (st->n_tiles == 0) return COVGPU_OK;
-  if (st->lik.factor) launch_edge_tiles<true>(st, t, s);
-  else launch_edge_tiles<false>(st, t, s);
+  if (st->edge_resident) {
+    if (st->lik.factor) launch_edge_res<true>(st, t, s);
+    else launch_edge_res<false>(st, t, s);
+  } else if (st->lik.factor) {
+    launch_edge_tiles<true>(st, t, s);
+  } else {
+    launch_edge_tiles<false>(st, t, s);
+  }
   return launch_status();
 }
 
@@ -872,11 +986,13 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
 }
 
 // people.py:435-586 for one agent (already deduplicated), plus update_peak_nab
-__device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, int sim, int64_t i, int t, int v,
-                           int32_t source, int layer_tag, int call_tag, bool hosp_max, bool icu_max) {
+// outcome bits of one infect_one call, tallied per warp by infect_tally
+constexpr uint32_t O_INF = 1u, O_COUNT = 2u, O_REINF = 4u, O_SYMP = 8u, O_SEV = 16u;
+
+__device__ uint32_t infect_one(const covgpu_state& st, const covgpu_sim_params& sp, int sim, int64_t i, int t, int v,
+                               int32_t source, int layer_tag, int call_tag, bool hosp_max, bool icu_max) {
   uint32_t f = st.flags[i];
-  if (!(f & B_SUS)) return;  // people.py:468-472: keep only susceptibles
-  const int nv = sp.n_variants;
+  if (!(f & B_SUS)) return 0u;  // people.py:468-472: keep only susceptibles
   const int64_t local = i - sp.agent_off;
   // people.py:486-491: breakthrough infections (peak_nab defined)
   const bool breakthrough = st.peak_nab[i] != 0.0f;
@@ -890,26 +1006,10 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   if (breakthrough) st.n_breakthroughs[i] += 1;
   st.vstate[i] = (st.vstate[i] & 0xFFFFFF00u) | (uint32_t)v;
   // seed infections happen before update_states_pre resets the day's flows
-  // (sim.py:571-577, people.py:171), so they are not counted
+  // (sim.py:571-577, people.py:171), so they are not counted; the counts and
+  // the infection log record (people.py:508-511) are written by infect_tally
   const bool count = call_tag != CALL_TAG_SEED;
-  if (count) {
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_INFECTIONS]), 1ull);
-    if (reinfection)
-      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_REINFECTIONS]), 1ull);
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_INFECTIONS) * nv + v]), 1ull);
-  }
-  // people.py:508-511: infection log
-  if (st.log) {
-    const unsigned long long pos = atomicAdd(st.log_count, 1ull);
-    if ((int64_t)pos < st.log_capacity) {
-      covgpu_log_rec r;
-      r.source = source; r.target = (int32_t)local; r.day = t;
-      r.layer_variant = (layer_tag & 0xFF) | (v << 8) | (sim << 16);
-      st.log[pos] = r;
-    } else {
-      atomicOr(st.status, COVGPU_OVERFLOW);
-    }
-  }
+  uint32_t out = O_INF | (count ? O_COUNT : 0u) | (reinfection ? O_REINF : 0u);
   DrawSet d;
   get_draws(st, sp, i, local, t, call_tag, d);
   float* d_inf = date_row(st, COVGPU_DATE_INFECTIOUS);
@@ -947,8 +1047,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
     u_inf2sym[i] = dis;
     const float ds = __fadd_rn(di, dis);
     d_sym[i] = ds;
-    if (count)
-      atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SYMPTOMATIC) * nv + v]), 1ull);
+    out |= O_SYMP;
     const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
                                   __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
     if (!d.lt(1, p_sev)) {  // CASE 2.1 mild, people.py:544-547
@@ -958,8 +1057,7 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
       symp_class = 1;
     } else {  // CASE 2.2 severe, people.py:550-554
       d.severe_normals();
-      if (count)
-        atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_var[((int64_t)t * COVGPU_N_RES_VAR + RV_SEVERE) * nv + v]), 1ull);
+      out |= O_SEV;
       const float dss = (float)sample_ff(sp.dur[COVGPU_D_SYM2SEV], d.z[2]);
       u_sym2sev[i] = dss;
       const float dsev = __fadd_rn(ds, dss);
@@ -1005,6 +1103,57 @@ __device__ void infect_one(const covgpu_state& st, const covgpu_sim_params& sp, 
   st.flags[i] = f;
   // no longer a target for the rest of the day (matters for infections before the edge pass)
   atomicAnd(st.roles + roles_words(st) + (i >> 5), ~(1u << (i & 31)));
+  return out;
+}
+
+// The day's counts (people.py:172-180 flows of infect) and the infection-log
+// records of one warp's infect_one calls: one log atomic per warp, and one
+// atomic per counter for each group of lanes with the same sim and variant.
+// All 32 lanes call it (lanes without an infection pass out = 0).
+__device__ void infect_tally(const covgpu_state& st, int t, uint32_t out, int sim, int v, int32_t source,
+                             int32_t target_local, int layer_tag) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const bool inf = out & O_INF;
+  if (st.log) {
+    const unsigned m = __ballot_sync(full, inf);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(st.log_count, (unsigned long long)__popc(m));
+      base = __shfl_sync(full, base, leader);
+      if (inf) {
+        const unsigned long long pos = base + __popc(m & ((1u << lane) - 1u));
+        if ((int64_t)pos < st.log_capacity) {
+          covgpu_log_rec r;
+          r.source = source; r.target = target_local; r.day = t;
+          r.layer_variant = (layer_tag & 0xFF) | (v << 8) | (sim << 16);
+          st.log[pos] = r;
+        } else {
+          atomicOr(st.status, COVGPU_OVERFLOW);
+        }
+      }
+    }
+  }
+  const bool cnt = inf && (out & O_COUNT);
+  const unsigned b_inf = __ballot_sync(full, cnt);
+  if (!b_inf) return;
+  const unsigned grp = __match_any_sync(full, cnt ? (((unsigned)sim << 8) | (unsigned)v) : 0xffffffffu);
+  const unsigned b_re = __ballot_sync(full, cnt && (out & O_REINF));
+  const unsigned b_sy = __ballot_sync(full, cnt && (out & O_SYMP));
+  const unsigned b_sv = __ballot_sync(full, cnt && (out & O_SEV));
+  if (!cnt || lane != __ffs(grp) - 1) return;  // one leader per (sim, variant) group
+  const covgpu_sim_params& sp = st.sims[sim];
+  const int nv = sp.n_variants;
+  unsigned long long* ri = reinterpret_cast<unsigned long long*>(sp.res_int + (int64_t)t * COVGPU_N_RES_INT);
+  unsigned long long* rv = reinterpret_cast<unsigned long long*>(sp.res_var + (int64_t)t * COVGPU_N_RES_VAR * nv);
+  const unsigned n_inf = __popc(b_inf & grp), n_re = __popc(b_re & grp), n_sy = __popc(b_sy & grp),
+                 n_sv = __popc(b_sv & grp);
+  atomicAdd(ri + R_INFECTIONS, (unsigned long long)n_inf);
+  if (n_re) atomicAdd(ri + R_REINFECTIONS, (unsigned long long)n_re);
+  atomicAdd(rv + RV_INFECTIONS * nv + v, (unsigned long long)n_inf);
+  if (n_sy) atomicAdd(rv + RV_SYMPTOMATIC * nv + v, (unsigned long long)n_sy);
+  if (n_sv) atomicAdd(rv + RV_SEVERE * nv + v, (unsigned long long)n_sv);
 }
 
 __device__ __forceinline__ int sim_of(const covgpu_state& st, int64_t i) {
@@ -1028,15 +1177,27 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
 __global__ void k_infect_claims(covgpu_state st, int t) {
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-    const covgpu_event ev = st.events[j];
-    if (st.claim[ev.target] != ev.key) continue;  // not the first infector of this target
-    const int s = sim_of(st, ev.target);
-    const covgpu_sim_params& sp = st.sims[s];
-    const int v = (int)((ev.key >> 45) & 7u), layer = (int)((ev.key >> 41) & 15u);
-    bool hosp, icu;
-    hosp_icu(st, sp, s, t, hosp, icu);
-    infect_one(st, sp, s, ev.target, t, v, (int32_t)(ev.source - sp.agent_off), layer, 0, hosp, icu);
+  // warp-uniform trip count (infect_tally's ballots need every lane)
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = base + threadIdx.x;
+    uint32_t out = 0;
+    int s = 0, v = 0, layer = 0;
+    int32_t src = -1, tgt = 0;
+    if (j < n) {
+      const covgpu_event ev = st.events[j];
+      if (st.claim[ev.target] == ev.key) {  // the first infector of this target
+        s = sim_of(st, ev.target);
+        const covgpu_sim_params& sp = st.sims[s];
+        v = (int)((ev.key >> 45) & 7u);
+        layer = (int)((ev.key >> 41) & 15u);
+        bool hosp, icu;
+        hosp_icu(st, sp, s, t, hosp, icu);
+        src = (int32_t)(ev.source - sp.agent_off);
+        tgt = (int32_t)(ev.target - sp.agent_off);
+        out = infect_one(st, sp, s, ev.target, t, v, src, layer, 0, hosp, icu);
+      }
+    }
+    infect_tally(st, t, out, s, v, src, tgt, layer);
   }
 }
 
@@ -1045,8 +1206,16 @@ __global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64
   const covgpu_sim_params& sp = st.sims[sim];
   bool hosp, icu;
   hosp_icu(st, sp, sim, t, hosp, icu);
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
-    infect_one(st, sp, sim, inds[j], t, v, -1, layer_tag, call_tag, hosp, icu);
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = base + threadIdx.x;
+    uint32_t out = 0;
+    int32_t tgt = 0;
+    if (j < n) {
+      tgt = (int32_t)(inds[j] - sp.agent_off);
+      out = infect_one(st, sp, sim, inds[j], t, v, -1, layer_tag, call_tag, hosp, icu);
+    }
+    infect_tally(st, t, out, sim, v, -1, tgt, layer_tag);
+  }
 }
 
 __global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1, int32_t* p2) {
@@ -1555,6 +1724,7 @@ static int check_state(const covgpu_state* st) {
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
   if (st->edge_tile != 1024 && st->edge_tile != 2048 && st->edge_tile != 4096 && st->edge_tile != 8192)
     return COVGPU_BADARG;
+  if (st->edge_resident && !edge_res_smem(st)) return COVGPU_BADARG;
   if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
                           st->pending_slots < 1 || st->n_contact_layers < 1))
     return COVGPU_BADARG;
@@ -1573,10 +1743,19 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
   return launch_status();
 }
 
+int64_t covgpu_edge_resident_bytes(const covgpu_state* st) {
+  if (!st || st->n <= 0) return 0;
+  covgpu_state probe = *st;
+  if (probe.edge_tile < RES_THREADS * EDGE_VEC) probe.edge_tile = RES_THREADS * EDGE_VEC;
+  return edge_res_smem(&probe);
+}
+
 int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  rc = configure_edge_pass(st);
+  if (rc) return rc;
   return launch_edge_pass(st, t, S(stream));
 }
 
@@ -1650,6 +1829,8 @@ int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open
   if (rc) return rc;
   if (t0 < 0 || t1 < t0 || t1 >= 0xFFFF) return COVGPU_BADARG;
   open_prev = (open_prev && t0 > 0) ? 1 : 0;
+  rc = configure_edge_pass(st);  // function attributes: outside any capture
+  if (rc) return rc;
   cudaStream_t s = S(stream);
   if (!use_graph) return enqueue_days(st, t0, t1, open_prev, close_last, s);
   GraphEntry* hit = nullptr;

@@ -241,9 +241,10 @@ class Sim:
             arguments are merged in
         popdict (dict): optional population (uid, age, sex, contacts)
         use_graph (bool): capture the day loop in a CUDA graph
-        edge_tile (int or 'auto'): edges per edge-pass block (1024, 2048, 4096 or
-            8192; default 4096); 'auto' times whole runs with each at initialize
-            (``covasim_gb300.autotune``, cached per workload)
+        edge_tile (int, str or 'auto'): edges per edge-pass block (1024, 2048, 4096
+            or 8192; default 4096), suffixed 'r' ('8192r') to keep the source
+            bitmap resident in shared memory; 'auto' times whole runs with each at
+            initialize (``covasim_gb300.autotune``, cached per workload)
         gpu_population (bool): build the population (ages, layers, prognoses) on
             the device instead of the host (same distributions, Philox draws)
     """
@@ -355,12 +356,8 @@ class Sim:
         self.popdict = popdict
         self._person = person
         self.spec = spec
-        tile = L.EDGE_TILE if self.edge_tile in (None, 'auto') else int(self.edge_tile)
-        self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity,
-                                edge_tile=tile)
-        if self.edge_tile == 'auto':
-            from .autotune import tune_edge_tile
-            tune_edge_tile(self.state)
+        self.state = BatchState([spec], event_capacity=self._event_capacity, log_capacity=self._log_capacity)
+        self.state.apply_edge_tile(self.edge_tile)
         contacts = Contacts()
         for ly in spec.layers:
             if torch.is_tensor(ly['p1']):

@@ -164,6 +164,7 @@ class BatchState:
         if int(edge_tile) not in L.EDGE_TILES:
             raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
         self.edge_tile = int(edge_tile)
+        self.edge_resident = False
         if not torch.cuda.is_available():
             raise RuntimeError('covasim_gb300 needs a CUDA device: the GPU path has no CPU fallback')
         self.lib = L.lib()
@@ -355,13 +356,42 @@ class BatchState:
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
         self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
 
-    def set_edge_tile(self, tile):
-        """Edges per edge-pass block (one of L.EDGE_TILES); the autotuner's knob."""
+    def set_edge_tile(self, tile, resident=False):
+        """Edges per edge-pass tile (one of L.EDGE_TILES) and whether the source
+        bitmap is resident in shared memory (one sim only); the autotuner's knobs."""
         if int(tile) not in L.EDGE_TILES:
             raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
         self.edge_tile = int(tile)
+        self.edge_resident = False
         self._tile_segments()
         self._refresh_state()
+        if resident:
+            if int(tile) < 4096 or not self.resident_possible():
+                raise ValueError('the resident-bitmap edge pass needs one sim of at most ~1.1M agents and tiles '
+                                 'of 4096 or 8192 edges')
+            self.edge_resident = True
+            self._refresh_state()
+
+    def resident_possible(self):
+        return int(self.lib.covgpu_edge_resident_bytes(self.cstate_ptr)) > 0
+
+    @property
+    def edge_tile_label(self):
+        """The edge-pass configuration as one value: the tile size, suffixed 'r'
+        when the source bitmap is resident in shared memory ('4096r')."""
+        return f'{self.edge_tile}r' if self.edge_resident else self.edge_tile
+
+    def apply_edge_tile(self, choice):
+        """Set the edge pass from a user choice: None (the default tile), 'auto'
+        (autotuned on this state), a tile size, or a label such as '8192r'."""
+        if choice is None:
+            return
+        if choice == 'auto':
+            from .autotune import tune_edge_tile
+            tune_edge_tile(self)
+            return
+        text = str(choice)
+        self.set_edge_tile(int(text.rstrip('r')), resident=text.endswith('r'))
 
     def _build_sims(self, beta_tabs, bl_tabs, kins):
         recs = []
@@ -469,6 +499,7 @@ class BatchState:
         st.n_tiles = self.n_tiles
         st.n_agent_blocks = self.n_agent_blocks
         st.edge_tile = self.edge_tile
+        st.edge_resident = int(self.edge_resident)
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
                   'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'events', 'event_count',

@@ -232,7 +232,9 @@ typedef struct covgpu_state {
   int64_t n_agent_blocks;
   int32_t edge_tile;              /* edges per edge-pass tile: 1024, 2048, 4096 or
                                      8192 (segments' tile_begin count these tiles)   */
-  int32_t _pad_tile;
+  int32_t edge_resident;          /* 1: one sim's source bitmap resident in shared
+                                     memory (one block per SM; a single sim of at
+                                     most ~1.1M agents, tiles of 4096 or 8192)     */
   /* per-agent state */
   uint32_t* flags;
   uint32_t* vstate;               /* bytes: exposed, infectious, recovered variant   */
@@ -403,6 +405,10 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
  * With st->lik.factor set, also the likelihood terms of every candidate
  * direction (covgpu_lik). */
 int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream);
+
+/* Shared memory the resident-bitmap edge pass needs for this state (one sim;
+ * 0: it cannot run here). Set st->edge_resident only when this is nonzero. */
+int64_t covgpu_edge_resident_bytes(const covgpu_state* st);
 
 /* The testing and tracing interventions of day t, after the agent pass and
  * any importations, before transmission (sim.py:596-600): test_prob's

@@ -12,16 +12,45 @@ pytestmark = pytest.mark.gpu
 
 
 def test_every_edge_tile_gives_the_same_run():
+    """Every tile size, and the resident-bitmap variant of the edge pass, with testing and tracing."""
     ref = None
-    for tile in L.EDGE_TILES:
+    variants = [(t, False) for t in L.EDGE_TILES] + [(4096, True), (8192, True)]
+    for tile, resident in variants:
         sim = make_sim(*CASES[0])
-        sim.edge_tile = tile
+        sim.initialize()
+        assert sim.state.resident_possible()
+        sim.state.set_edge_tile(tile, resident=resident)
         raw = sim.run().raw_results()
         if ref is None:
             ref = raw
         else:
             for k in TESTING_KEYS:
-                np.testing.assert_array_equal(raw[k], ref[k], err_msg=f'tile {tile} {k}')
+                np.testing.assert_array_equal(raw[k], ref[k], err_msg=f'tile {tile} resident {resident} {k}')
+
+
+def test_resident_variant_with_the_likelihood_matches():
+    from covasim_gb300.adjoint import LikelihoodRun
+    out = []
+    for resident in (False, True):
+        sim = cv.Sim(pop_type='hybrid', pop_size=6000, n_days=40, rand_seed=3, pop_infected=40,
+                     dynam_layer=dict(h=0, s=0, w=0, c=1))
+        sim.initialize()
+        sim.state.set_edge_tile(4096, resident=resident)
+        run = LikelihoodRun(sim, checkpoint_every=10)
+        ll, e = run.forward(run.params.theta0)
+        out.append((ll, e, run.backward(1.0, np.ones(run.npts))))
+    (l0, e0, g0), (l1, e1, g1) = out
+    assert abs(l0 - l1) <= 1e-9 * abs(l0)
+    np.testing.assert_allclose(e0, e1, rtol=1e-9)
+    np.testing.assert_allclose(g0, g1, rtol=1e-9)
+
+
+def test_resident_variant_is_refused_for_batches():
+    sims = [cv.Sim(pop_type='random', pop_size=2000, n_days=10, rand_seed=s) for s in (1, 2)]
+    batch = cv.BatchSim(sims).initialize()
+    assert not batch.state.resident_possible()
+    with pytest.raises(ValueError):
+        batch.state.set_edge_tile(4096, resident=True)
 
 
 def test_autotuned_sim_equals_default_run():
