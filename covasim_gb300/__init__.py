@@ -9,7 +9,9 @@ Drop-in pieces of the reference's API (``import covasim_gb300 as cv``):
   ``cv.compute_infections`` -- the reference's numba kernels, on the GPU;
 * ``cv.BatchSim`` -- many sims in one launch (replaces MultiSim's processes);
 * ``cv.make_pars``, ``cv.change_beta``, ``cv.variant`` and the population
-  generators.
+  generators;
+* ``cv.Fit`` / ``cv.compute_gof`` / ``cv.load_data``, ``cv.TransTree`` and
+  ``cv.Calibration`` (trials run as batches of sims).
 
 There is no CPU fallback: the kernels need the in-tree ``libcovgpu.so`` and a
 CUDA device, and fail loudly without them.
@@ -23,5 +25,6 @@ from .interventions import *  # noqa: F401,F403
 from .people import *  # noqa: F401,F403
 from .sim import *  # noqa: F401,F403
 from .batch import *  # noqa: F401,F403
+from .analysis import *  # noqa: F401,F403
 from .utils import *  # noqa: F401,F403
 from ._lib import CovgpuError  # noqa: F401

@@ -11,6 +11,7 @@ so results are reproducible bit for bit, in any batch position, and agree
 with the CPU oracle run in its Philox mode.
 """
 import copy
+import datetime as dt
 import time
 
 import numpy as np
@@ -22,6 +23,7 @@ from . import parameters as cvpar
 from . import population as cvpop
 from . import immunity as cvimm
 from . import interventions as cvi
+from . import analysis as cva
 from .people import People, Layer, Contacts
 from .state import SimSpec, BatchState
 
@@ -247,10 +249,12 @@ class Sim:
             initialize (``covasim_gb300.autotune``, cached per workload)
         gpu_population (bool): build the population (ages, layers, prognoses) on
             the device instead of the host (same distributions, Philox draws)
+        datafile (str, dict or DataTable): data to compare with (``cv.load_data``),
+            used by ``compute_fit`` and ``Calibration``
     """
 
     def __init__(self, pars=None, label=None, popdict=None, use_graph=True, person=None, edge_tile=None,
-                 gpu_population=False, **kwargs):
+                 gpu_population=False, datafile=None, data=None, **kwargs):
         self.label = label
         self.gpu_population = gpu_population  # build a missing population on the device
         self.edge_tile = edge_tile  # edges per edge-pass block; 'auto': autotuned at initialize
@@ -269,6 +273,10 @@ class Sim:
         self.results_ready = False
         self._event_capacity = None
         self._log_capacity = None
+        self.datafile = datafile if datafile is not None else data
+        self.data = None
+        if self.datafile is not None:
+            self.load_data(self.datafile)
 
     # ------------------------------------------------------------------ pars
     def __getitem__(self, key):
@@ -304,6 +312,68 @@ class Sim:
 
     def layer_keys(self):
         return list(self['beta_layer'].keys())
+
+    # ------------------------------------------------------------------ dates and data (base.py:341-421)
+    @property
+    def datevec(self):
+        """The date of each day of the sim."""
+        start = cva.to_date(self['start_day'])
+        return np.array([start + dt.timedelta(days=int(d)) for d in self.tvec], dtype=object)
+
+    def day(self, day, *args):
+        """Days since start_day of a date ('YYYY-MM-DD' or a date object); integers pass through."""
+        days = [day] + list(args)
+        out = [cva.to_day(d, self['start_day']) for d in days]
+        return out[0] if len(out) == 1 else out
+
+    def date(self, ind, *args, dateformat=None, as_date=False):
+        """The date (a 'YYYY-MM-DD' string, or a date with ``as_date``) of sim day(s)."""
+        inds = list(ind) if isinstance(ind, (list, tuple, np.ndarray)) else [ind] + list(args)
+        start = cva.to_date(self['start_day'])
+        out = []
+        for i in inds:
+            d = start + dt.timedelta(days=int(i)) if isinstance(i, (int, np.integer)) else cva.to_date(i)
+            out.append(d if as_date else d.strftime(dateformat or '%Y-%m-%d'))
+        return out[0] if len(out) == 1 and not isinstance(ind, (list, tuple, np.ndarray)) else out
+
+    def load_data(self, datafile=None, verbose=False, **kwargs):
+        """Attach data (misc.py:33-91) for ``compute_fit`` / ``Calibration``."""
+        self.datafile = datafile
+        self.data = cva.load_data(datafile, verbose=verbose, start_day=self['start_day'], **kwargs)
+        return self.data
+
+    def result_keys(self, which='main'):
+        """Names of the per-day results (base.py:424-440)."""
+        if which not in ('main', 'variant', 'all'):
+            raise ValueError(f'Choice "{which}" not available; choices are main, variant, all')
+        keys = []
+        if which in ('main', 'all'):
+            keys += [k for k, v in self.results.items() if isinstance(v, Result)]
+        if which in ('variant', 'all') and 'variant' in self.results:
+            keys += [k for k, v in self.results['variant'].items() if isinstance(v, Result)]
+        return keys
+
+    def compute_fit(self, *args, **kwargs):
+        """The fit to the sim's data (sim.py:1086-1104); stored as ``sim.fit``."""
+        self.fit = cva.Fit(self, *args, **kwargs)
+        return self.fit
+
+    def make_transtree(self, *args, output=True, **kwargs):
+        """The transmission tree (sim.py:1107-1124), built on the device from the infection log."""
+        tt = cva.TransTree(self, *args, **kwargs)
+        if output:
+            return tt
+        self.results['transtree'] = tt
+        return None
+
+    def copy(self):
+        """An unrun copy: its own parameters, the same population and data."""
+        new = Sim(pars=None, label=self.label, popdict=self.popdict, use_graph=self.use_graph,
+                  person=getattr(self, '_person', None), edge_tile=self.edge_tile,
+                  gpu_population=self.gpu_population)
+        new.pars = copy.deepcopy(self.pars)
+        new.datafile, new.data = self.datafile, self.data
+        return new
 
     # ------------------------------------------------------------------ initialize
     def validate_pars(self):
@@ -394,6 +464,7 @@ class Sim:
         for key in cvd.result_stocks_by_variant:
             self.results['variant'][f'n_{key}'] = Result(f'n_{key}', npts, n_variants=nv)
         self.results['t'] = self.tvec
+        self.results['date'] = self.datevec
         self.results_ready = False
 
     # ------------------------------------------------------------------ day loop
@@ -523,6 +594,7 @@ class Sim:
         self.results['variant']['cum_infections_by_variant'].values[0] += self['pop_infected']
         self.results_ready = True
         self.t -= 1
+        self.people.__dict__['t'] = self.t
         self.compute_results()
         self.summary = {k: v.values[-1] for k, v in self.results.items() if isinstance(v, Result)}
         return self

@@ -818,6 +818,22 @@ class BatchState:
         out['pop_symp_protection'] = np.ldexp(fx[:, 2].astype(np.float64), -L.FX_IMM_BITS) / denom
         return out
 
+    def infection_log_tensor(self, sim):
+        """Device tensor [n, 5] int64 of sim's records (source, target, date, layer
+        index, variant) in the order of ``infection_log``: two stable sorts
+        (by target, then by day, variant and layer), as ``np.lexsort`` orders them."""
+        dev = self.t['log'].device
+        if not self.log_enabled:
+            return torch.zeros((0, 5), dtype=torch.int64, device=dev)
+        n = min(int(self.t['log_count'].item()), self.log_capacity)
+        rec = self.t['log'][:n].long()
+        packed = rec[:, 3]
+        rec = rec[(packed >> 16) == sim]
+        out = torch.stack([rec[:, 0], rec[:, 1], rec[:, 2], rec[:, 3] & 0xFF, (rec[:, 3] >> 8) & 0xFF], dim=1)
+        out = out[torch.sort(out[:, 1], stable=True).indices]
+        key = (out[:, 2] << 32) | (out[:, 4] << 16) | out[:, 3]
+        return out[torch.sort(key, stable=True).indices]
+
     def infection_log(self, sim=None):
         """Infection-log records (source, target, date, layer index, variant), sorted like the reference's."""
         if not self.log_enabled:

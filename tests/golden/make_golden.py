@@ -23,6 +23,8 @@ Fixtures:
                        intervention arguments, daily results, final testing/quarantine state)
   ref_reporting.npz    compute_yield / compute_doubling / compute_r_eff / compute_gen_time
                        inputs and outputs on a reference run (sciris' smooth restated)
+  ref_analysis.npz     TransTree / Fit / compute_gof outputs of the reference's own code on a
+                       reference run with testing (pandas and sciris replaced by stand-ins)
   ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
                        20k-agent random sim (60 days), reference code with MT19937 streams
 """
@@ -499,6 +501,248 @@ def make_reporting_fixture(ref):
     print('ref_reporting.npz written')
 
 
+class _Col(np.ndarray):
+    """A numpy column with the two pandas Series attributes the reference's consumers use."""
+
+    def __array_finalize__(self, obj):
+        self._index = getattr(obj, '_index', None)
+
+    @property
+    def values(self):
+        return np.asarray(self)
+
+    def items(self):
+        return zip(list(self._index), np.asarray(self).tolist())
+
+
+class _Frame:
+    """The few DataFrame operations of the reference's Fit and TransTree
+    (pandas is not installed): records or dict construction, columns, column
+    get/set with scalar broadcast, rename, boolean .loc get/set."""
+
+    def __init__(self, data=None, index=None):
+        if isinstance(data, list):
+            keys = list(dict.fromkeys(k for r in data for k in r))
+            data = {k: [r.get(k) for r in data] for k in keys}
+        self._cols = {k: self._arr(v) for k, v in dict(data or {}).items()}
+        self._index = index
+
+    @staticmethod
+    def _arr(v):
+        if isinstance(v, np.ndarray):
+            return v
+        v = list(v)
+        if all(x is None or isinstance(x, (int, float, np.integer, np.floating)) for x in v):
+            if any(x is None for x in v):  # pandas: numbers with None -> float64 with NaN
+                return np.array([np.nan if x is None else x for x in v], dtype=np.float64)
+            return np.asarray(v)
+        return np.array(v, dtype=object)
+
+    @property
+    def columns(self):
+        return list(self._cols)
+
+    def __len__(self):
+        return len(next(iter(self._cols.values()))) if self._cols else 0
+
+    def __getitem__(self, k):
+        c = np.asarray(self._cols[k]).view(_Col)
+        c._index = self._index if self._index is not None else np.arange(len(c))
+        return c
+
+    def __setitem__(self, k, v):
+        self._cols[k] = np.full(len(self), v, dtype=object) if np.isscalar(v) else np.asarray(v)
+
+    def rename(self, columns):
+        return _Frame({columns.get(k, k): v for k, v in self._cols.items()})
+
+    @property
+    def loc(self):
+        frame = self
+
+        class _Loc:
+            def __getitem__(lself, mask):
+                m = np.asarray(mask, dtype=bool)
+                return _Frame({k: v[m] for k, v in frame._cols.items()})
+
+            def __setitem__(lself, key, val):
+                mask, col = key
+                frame._cols[col][np.asarray(mask, dtype=bool)] = val
+        return _Loc()
+
+
+class _ObjDict(dict):
+    """sciris' objdict: attribute access, and [:] for the values as an array."""
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as E:
+            raise AttributeError(k) from E
+
+    def __setattr__(self, k, v):
+        self[k] = v
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return np.array(list(self.values()))[k]
+        return dict.__getitem__(self, k)
+
+
+class _ODict(dict):
+    """sciris' odict with a default factory."""
+
+    def __init__(self, defaultdict=None):
+        super().__init__()
+        self._factory = defaultdict
+
+    def __missing__(self, k):
+        self[k] = v = self._factory()
+        return v
+
+
+def make_analysis_fixture(ref):
+    """Outputs of the reference's own TransTree (analysis.py:1772-2056), Fit
+    (analysis.py:991-1235) and compute_gof (misc.py:707-790) on a reference run
+    with testing and tracing; pandas and sciris are replaced by the small
+    stand-ins above."""
+    import types
+    pop_type, n, days, seed, waning, dyn, tp_kw, ct_kw = TESTING_CASES[0]
+    pars = ref.make_pars(pop_size=n, n_days=days, pop_type=pop_type, rand_seed=seed, use_waning=waning)
+    pars['interventions'] = [ref.cvint.test_prob(**tp_kw), ref.cvint.contact_tracing(**ct_kw)]
+    sim = refload.RefSim(ref, pars).run()
+    people = sim.people
+    log = people.infection_log
+
+    sc_ns = types.SimpleNamespace(**vars(refload.sc))
+    sc_ns.objdict = _ObjDict
+    sc_ns.odict = _ODict
+    sc_ns.isiterable = lambda x: np.iterable(x)
+    sc_ns.prettyobj = object
+    sc_ns.day = lambda d, start_date=None: int(d)  # integer days only in these cases
+    misc_ns = {'np': np, 'sc': sc_ns}
+    gof_fn = refload.load_functions('misc.py', ['compute_gof'], namespace=misc_ns)['compute_gof']
+    cvm = types.SimpleNamespace(warn=print, compute_gof=gof_fn)
+    pd_stub = types.SimpleNamespace(DataFrame=_Frame)
+    ns = {'np': np, 'sc': sc_ns, 'pd': pd_stub, 'cvm': cvm}
+    classes = refload.load_classes('analysis.py', ['Analyzer', 'Fit', 'TransTree'], ns)
+
+    out = {}
+    # -- transmission tree (agent 0 made a source on purpose: the `if source:` convention)
+    log = [dict(e) for e in log]
+    zero_rec = next((k for k, e in enumerate(log) if e['source'] is not None), None)
+    if zero_rec is not None:
+        log[zero_rec]['source'] = 0
+
+    class PeopleStub:
+        def __init__(self):
+            self.t = sim.npts - 1
+            self.infection_log = log
+
+        def __len__(self):
+            return n
+
+        def __getitem__(self, k):
+            return people[k]
+
+    class SimStub:
+        def __init__(self):
+            self.people = PeopleStub()
+            self.results = {'t': np.arange(sim.npts), 'cum_infections': _Res(np.cumsum(sim.results['new_infections']))}
+
+        def __getitem__(self, k):
+            return {'start_day': '2020-03-01', 'rescale': False, 'pop_scale': 1}[k]
+
+    tt = classes['TransTree'](SimStub(), to_networkx=True)
+    out['tt.sources'] = np.array([-1 if s is None else s for s in tt.sources], dtype=np.int64)
+    out['tt.source_dates'] = np.array([-1 if s is None else s for s in tt.source_dates], dtype=np.int64)
+    out['tt.targets_count'] = np.array([len(t) for t in tt.targets], dtype=np.int64)
+    out['tt.targets_flat'] = np.array([g for t in tt.targets for g in t], dtype=np.int64)
+    out['tt.target_dates_flat'] = np.array([d for t in tt.target_dates for d in t], dtype=np.int64)
+    out['tt.n_targets'] = np.asarray(tt.n_targets, dtype=np.float64)
+    out['tt.n_targets_10_25'] = np.asarray(tt.count_targets(10, 25), dtype=np.float64)
+    out['tt.transmissions'] = np.array(tt.transmissions, dtype=np.int64).reshape(-1, 2)
+    out['tt.r0_0'] = np.array(tt.r0(False))
+    out['tt.r0_1'] = np.array(tt.r0(True))
+    det = tt.detailed
+    for k in det.columns:
+        col = det[k].values
+        out[f'tt.detailed.{k}'] = (np.array([str(x) for x in col]) if col.dtype == object
+                                   else np.asarray(col, dtype=np.float64))
+    for k in tt.df.columns:
+        col = tt.df[k].values
+        out[f'tt.df.{k}'] = np.array([str(x) for x in col]) if col.dtype == object else np.asarray(col)
+    out['log.source'] = np.array([-1 if e['source'] is None else e['source'] for e in log], dtype=np.int64)
+    out['log.target'] = np.array([e['target'] for e in log], dtype=np.int64)
+    out['log.date'] = np.array([e['date'] for e in log], dtype=np.int64)
+    out['log.layer'] = np.array([e['layer'] for e in log])
+    out['log.variant'] = np.array([str(e['variant']) for e in log])
+    for k in ('age', 'date_exposed', 'date_symptomatic', 'date_tested', 'date_diagnosed', 'date_severe',
+              'date_critical', 'date_known_contact', 'date_quarantined', 'date_end_quarantine', 'date_recovered'):
+        out[f'people.{k}'] = np.asarray(people[k]).copy()
+    out['meta'] = np.array([n, sim.npts - 1])
+
+    # -- goodness of fit
+    rng = np.random.RandomState(11)
+    a = np.cumsum(rng.poisson(5, 40)).astype(float)
+    b = a * rng.uniform(0.8, 1.2, 40)
+    gof_cases = [dict(), dict(normalize=False), dict(use_frac=True), dict(use_squared=True, as_scalar='mean'),
+                 dict(as_scalar='median'), dict(normalize=False, use_squared=True, as_scalar='sum'),
+                 dict(use_frac=True, eps=1e-3, as_scalar='sum')]
+    out['gof.actual'], out['gof.predicted'] = a, b
+    out['gof.cases'] = np.array(json.dumps(gof_cases))
+    for i, kw in enumerate(gof_cases):
+        out[f'gof.out{i}'] = np.asarray(gof_fn(a, b, **kw), dtype=np.float64)
+
+    # -- Fit against synthetic data: some dates outside the sim, missing values, a custom key
+    import datetime as dt
+    start = dt.date(2020, 3, 1)
+    sim_dates = [start + dt.timedelta(days=d) for d in range(sim.npts)]
+    res = {}
+    for key in ref.cvd.result_flows:
+        res[f'cum_{key}'] = _Res(np.cumsum(sim.results[f'new_{key}']))
+        res[f'new_{key}'] = _Res(sim.results[f'new_{key}'])
+    res['cum_infections'].values += pars['pop_infected']
+    data_days = np.arange(-5, sim.npts + 5, 2)
+    data_dates = [start + dt.timedelta(days=int(d)) for d in data_days]
+    dcols = {}
+    for key in ('cum_diagnoses', 'cum_deaths', 'cum_tests', 'new_infections'):
+        base = np.interp(data_days, np.arange(sim.npts), res[key].values)
+        vals = np.round(base * rng.uniform(0.7, 1.3, len(base)) + rng.poisson(2, len(base)))
+        vals[rng.rand(len(vals)) < 0.15] = np.nan
+        dcols[key] = vals
+    data = _Frame(dcols, index=data_dates)
+
+    class FitSim:
+        def __init__(self):
+            self.data = data
+            self.results_ready = True
+            self.results = dict(res, t=np.arange(sim.npts), date=np.array(sim_dates, dtype=object))
+            self.npts = sim.npts
+            self.datevec = np.array(sim_dates, dtype=object)
+
+        def result_keys(self):
+            return [k for k in res]
+
+    fit_cases = [dict(), dict(keys=['cum_diagnoses', 'new_infections'], weights={'new_infections': 2.0}),
+                 dict(use_frac=True, as_scalar='sum'),
+                 dict(weights={'cum_tests': np.linspace(0.5, 2, sim.npts)}),
+                 dict(custom={'extra': {'data': np.array([1.0, 2.0, 4.0]), 'sim': np.array([1.5, 2.0, 3.0]), 'weight': 3.0}})]
+    out['fit.cases'] = np.array(json.dumps(jsonable(fit_cases)))
+    for i, kw in enumerate(fit_cases):
+        f = classes['Fit'](FitSim(), **copy.deepcopy(kw))
+        out[f'fit.mismatch{i}'] = np.array(f.mismatch, dtype=np.float64)
+        out[f'fit.keys{i}'] = np.array(list(f.mismatches.keys()))
+        out[f'fit.mismatches{i}'] = np.array(list(f.mismatches.values()), dtype=np.float64)
+    for key, vals in dcols.items():
+        out[f'data.{key}'] = vals
+    out['data.days'] = data_days
+    for key in ('cum_diagnoses', 'cum_deaths', 'cum_tests', 'new_infections', 'cum_infections'):
+        out[f'simres.{key}'] = res[key].values.copy()
+    np.savez_compressed(os.path.join(HERE, 'ref_analysis.npz'), **out)
+    print('ref_analysis.npz written', len(log), 'records')
+
+
 def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
     keys = ['new_infections', 'new_severe', 'new_deaths', 'new_infectious', 'new_recoveries', 'new_critical',
             'new_symptomatic', 'n_exposed']
@@ -525,6 +769,7 @@ def main():
     ref = refload.Reference()
     groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
                   sims=make_sims_fixture, testing=make_testing_fixture, reporting=make_reporting_fixture,
+                  analysis=make_analysis_fixture,
                   distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
     for name, fn in groups.items():
         if args.only is None or args.only == name:
