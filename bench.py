@@ -670,7 +670,7 @@ def profile_run(args):
     if args.profile_testing:
         from covasim_gb300.adjoint import Parameters
         pars['interventions'] = [cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)]
-        sim = cv.Sim(pars)
+        sim = cv.Sim(pars, edge_tile=None if args.edge_tile == 'auto' else args.edge_tile)
         sim.initialize()
         st = sim.state
         st.enable_lik(grad=True)
@@ -678,7 +678,7 @@ def profile_run(args):
         st.set_lik_factor(params.factor(params.theta0))
         st.zero_lik()
     else:
-        sim = cv.Sim(pars)
+        sim = cv.Sim(pars, edge_tile=None if args.edge_tile == 'auto' else args.edge_tile)
     sim.run(use_graph=False)
     torch.cuda.synchronize()
     print(json.dumps({'profile_run': True, 'pop_size': args.pop_size, 'days': args.days,

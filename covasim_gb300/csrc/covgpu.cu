@@ -33,7 +33,11 @@ constexpr int EDGE_VEC = 4;            // edges per 128-bit load
 constexpr int EDGE_ROUND = EDGE_THREADS * EDGE_VEC;  // edges one block reads per round
 constexpr int64_t EDGE_TILE_MAX = 8192;  // edge tiles: 1024, 2048, 4096 or 8192 edges (covgpu_state.edge_tile)
 constexpr int EQ_ROUND = 32 * EDGE_VEC;  // most candidates one warp appends per round (one per edge)
-constexpr int EQ_CAP = 256;            // candidate queue entries per warp (drained when a round could overflow)
+#ifndef COVGPU_EQ_CAP
+#define COVGPU_EQ_CAP 256
+#endif
+constexpr int EQ_CAP = COVGPU_EQ_CAP;  // candidate queue entries per warp (drained when a round could overflow);
+                                       // 192 and 160, which leave L1 more room, measured slower
 static_assert(2 * EDGE_TILE_MAX <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
 constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
 constexpr int INF_THREADS = 256;
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, i
 // (susceptible with rel_sus != 0) of agent a: two separate bitmaps, so that the
 // source bitmap (n/8 bytes), tested for both endpoints of every edge, stays in L1
 __device__ __forceinline__ uint32_t src_bit(const uint32_t* __restrict__ roles, int32_t a) {
-  return (__ldg(roles + (a >> 5)) >> (a & 31)) & 1u;
+  return (ld_keep_u32(roles + (a >> 5)) >> (a & 31)) & 1u;
 }
 __device__ __forceinline__ uint32_t tgt_bit(const covgpu_state& st, int32_t a) {
   return (__ldg(st.roles + roles_words(st) + (a >> 5)) >> (a & 31)) & 1u;
@@ -649,27 +653,47 @@ __device__ __forceinline__ double warp_sum_d(double x) {
 }
 
 // The segment owning a tile: the last segment with tile_begin <= tile.
-__device__ __forceinline__ int segment_of_tile(const covgpu_state& st, int64_t tile) {
-  int lo = 0, hi = st.n_segments - 1;
+__device__ __forceinline__ int segment_of_tile(const covgpu_layer* segs, int n_segments, int64_t tile) {
+  int lo = 0, hi = n_segments - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (st.segments[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
 
+// The fields of a sim's parameter block that the edge pass reads
+struct SimLite {
+  const float* beta_tab;
+  const float* beta_layer_tab;
+  int64_t n_agents, agent_off;
+  float asymp_factor;
+  uint32_t key0, key1;
+  int32_t nv, n_layers;
+};
+__device__ __forceinline__ void load_sim_lite(SimLite& o, const covgpu_sim_params& sp) {
+  o.beta_tab = sp.beta_tab;
+  o.beta_layer_tab = sp.beta_layer_tab;
+  o.n_agents = sp.n_agents;
+  o.agent_off = sp.agent_off;
+  o.asymp_factor = sp.asymp_factor;
+  o.key0 = sp.key0;
+  o.key1 = sp.key1;
+  o.nv = sp.n_variants;
+  o.n_layers = sp.n_layers;
+}
+
 // One tile (TILE edges) of one segment, NT threads: phase A streams the edges
 // and queues the candidate directions of each warp, phase B drains the queues.
+// The segment record L and its sim's constants sp are shared-memory copies.
 // RES: the sim's source bitmap is resident in shared memory (s_src, one sim).
 template <bool LIK, int NT, int64_t TILE, bool RES>
-__device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg, int64_t tile,
-                                          const uint32_t* s_src, EdgeQueue& q, LikAcc& acc) {
+__device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg, int64_t tile, const covgpu_layer* L,
+                                          const SimLite* sp, const uint32_t* s_src, EdgeQueue& q, LikAcc& acc) {
   constexpr int ROUNDS = (int)(TILE / ((int64_t)NT * EDGE_VEC));
   static_assert(ROUNDS >= 1 && TILE % ((int64_t)NT * EDGE_VEC) == 0, "whole rounds per tile");
-  const covgpu_layer* L = st.segments + seg;
-  const covgpu_sim_params* sp = st.sims + L->sim;
   SegCtx c;
-  c.L = L;
+  c.L = st.segments + seg;
   c.seg = seg;
   c.layer = L->layer;
   c.n_edges = L->n_edges;
@@ -678,7 +702,7 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
   c.quar_factor = L->quar_factor;
   c.iso_factor = L->iso_factor;
   c.asymp_factor = sp->asymp_factor;
-  c.nv = sp->n_variants;
+  c.nv = sp->nv;
   c.key0 = sp->key0;
   c.key1 = sp->key1;
   c.beta_t = sp->beta_tab + (int64_t)t * c.nv;
@@ -704,8 +728,8 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
         dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)c.layer, c.key0, c.key1, (uint32_t)n_local, thr,
                      off, a[j], b[j], a[j + 1], b[j + 1]);
     } else if (eb + EDGE_VEC <= e1) {
-      const int4 pa = __ldg(reinterpret_cast<const int4*>(p1 + eb));
-      const int4 pb = __ldg(reinterpret_cast<const int4*>(p2 + eb));
+      const int4 pa = ld_stream_v4(p1 + eb);
+      const int4 pb = ld_stream_v4(p2 + eb);
       a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
       b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
     } else {
@@ -764,11 +788,19 @@ template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
   constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
+  __shared__ covgpu_layer s_L;
+  __shared__ SimLite s_sp;
   __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
-  if (threadIdx.x == 0) s_seg = segment_of_tile(st, (int64_t)blockIdx.x);
+  if (threadIdx.x == 0) {
+    const int seg = segment_of_tile(st.segments, st.n_segments, (int64_t)blockIdx.x);
+    s_seg = seg;
+    s_L = st.segments[seg];
+    load_sim_lite(s_sp, st.sims[s_L.sim]);
+  }
   __syncthreads();
   LikAcc acc;
-  edge_tile<LIK, EDGE_THREADS, TILE, false>(st, t, s_seg, (int64_t)blockIdx.x, nullptr, s_q[threadIdx.x >> 5], acc);
+  edge_tile<LIK, EDGE_THREADS, TILE, false>(st, t, s_seg, (int64_t)blockIdx.x, &s_L, &s_sp, nullptr,
+                                            s_q[threadIdx.x >> 5], acc);
   if (LIK) {  // the tile's sums: one sim, one layer
     __shared__ double s_acc[EDGE_THREADS / 32][2];
     const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
@@ -779,10 +811,9 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
       double x = 0.0, y = 0.0;
       for (int k = 0; k < EDGE_THREADS / 32; ++k) { x += s_acc[k][0]; y += s_acc[k][1]; }
       const covgpu_lik& K = st.lik;
-      const covgpu_layer& L = st.segments[s_seg];
-      const int64_t day = (int64_t)L.sim * K.npts_max + t;
+      const int64_t day = (int64_t)s_L.sim * K.npts_max + t;
       if (x != 0.0) atomicAdd(K.ll + day, x);
-      if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + L.layer, y);
+      if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + s_L.layer, y);
     }
   }
 }
@@ -792,27 +823,37 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
 // with a stride of the grid (stored and redrawn layers interleave, which
 // balances the blocks); the per-warp queues follow the bitmap in shared memory.
 constexpr int RES_THREADS = 1024;
+constexpr int RES_MAX_SEGS = COVGPU_MAX_LAYERS;  // one sim: at most one segment per layer
 template <bool LIK, int64_t TILE>
 __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state st, int t) {
   extern __shared__ uint4 s_dyn[];
+  __shared__ covgpu_layer s_segs[RES_MAX_SEGS];
+  __shared__ SimLite s_sp;
   uint32_t* s_src = reinterpret_cast<uint32_t*>(s_dyn);
   const int64_t words = (st.n + 31) >> 5;
-  for (int64_t k = threadIdx.x; k < words; k += RES_THREADS) s_src[k] = __ldg(st.roles + k);
+  const int n_segs = st.n_segments;
+  // bitmap words four at a time (the bitmap has room for whole uint4s)
+  const uint4* g4 = reinterpret_cast<const uint4*>(st.roles);
+  for (int64_t k = threadIdx.x; k < (words >> 2); k += RES_THREADS) s_dyn[k] = __ldg(g4 + k);
+  for (int64_t k = (words & ~3ll) + threadIdx.x; k < words; k += RES_THREADS) s_src[k] = __ldg(st.roles + k);
+  if (threadIdx.x < n_segs) s_segs[threadIdx.x] = st.segments[threadIdx.x];
+  if (threadIdx.x == 0) load_sim_lite(s_sp, st.sims[0]);
   EdgeQueue* s_q = reinterpret_cast<EdgeQueue*>(s_dyn + ((words + 3) >> 2));
   EdgeQueue& q = s_q[threadIdx.x >> 5];
   __syncthreads();
   LikAcc acc;
   for (int64_t tile = blockIdx.x; tile < st.n_tiles; tile += gridDim.x) {
-    const int seg = segment_of_tile(st, tile);
-    edge_tile<LIK, RES_THREADS, TILE, true>(st, t, seg, tile, s_src, q, acc);
-    if (LIK) lik_flush_warp(st, t, st.segments[seg].sim, st.segments[seg].layer, acc);
+    const int seg = segment_of_tile(s_segs, n_segs, tile);
+    edge_tile<LIK, RES_THREADS, TILE, true>(st, t, seg, tile, s_segs + seg, &s_sp, s_src, q, acc);
+    if (LIK) lik_flush_warp(st, t, s_segs[seg].sim, s_segs[seg].layer, acc);
   }
 }
 
 // shared memory of the resident-bitmap variant, 0 when it cannot run
 int64_t edge_res_smem(const covgpu_state* st) {
-  if (st->n_sims != 1 || st->edge_tile < RES_THREADS * EDGE_VEC) return 0;
+  if (st->n_sims != 1 || st->edge_tile < RES_THREADS * EDGE_VEC || st->n_segments > RES_MAX_SEGS) return 0;
   const int64_t words = (st->n + 31) >> 5;
+  const int64_t static_bytes = (int64_t)sizeof(covgpu_layer) * RES_MAX_SEGS + (int64_t)sizeof(SimLite) + 64;
   const int64_t bytes = 16 * ((words + 3) >> 2) + (int64_t)(RES_THREADS / 32) * (int64_t)sizeof(EdgeQueue);
   static int max_optin = -1;
   if (max_optin < 0) {
@@ -821,7 +862,7 @@ int64_t edge_res_smem(const covgpu_state* st) {
         cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
       max_optin = 0;
   }
-  return bytes <= max_optin ? bytes : 0;
+  return bytes + static_bytes <= max_optin ? bytes : 0;
 }
 
 int n_sms() {
@@ -1724,7 +1765,7 @@ static int check_state(const covgpu_state* st) {
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
   if (st->edge_tile != 1024 && st->edge_tile != 2048 && st->edge_tile != 4096 && st->edge_tile != 8192)
     return COVGPU_BADARG;
-  if (st->edge_resident && !edge_res_smem(st)) return COVGPU_BADARG;
+  if (st->edge_resident && (!edge_res_smem(st) || (reinterpret_cast<uintptr_t>(st->roles) & 15u))) return COVGPU_BADARG;
   if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
                           st->pending_slots < 1 || st->n_contact_layers < 1))
     return COVGPU_BADARG;
