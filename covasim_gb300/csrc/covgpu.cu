@@ -28,6 +28,26 @@ using namespace covgpu;
 namespace {
 
 constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
+// resident blocks per SM that the register budget of the agent / infect pass
+// must allow (0: the compiler's choice). Six agent blocks (40 registers, a
+// few spilled) ran the agent pass of a 1M-agent run 10% faster than the
+// compiler's 58 registers (four blocks); the infect pass showed no change.
+#ifndef COVGPU_AGENT_MIN_BLOCKS
+#define COVGPU_AGENT_MIN_BLOCKS 6
+#endif
+#ifndef COVGPU_INFECT_MIN_BLOCKS
+#define COVGPU_INFECT_MIN_BLOCKS 0
+#endif
+#if COVGPU_AGENT_MIN_BLOCKS
+#define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS, COVGPU_AGENT_MIN_BLOCKS)
+#else
+#define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS)
+#endif
+#if COVGPU_INFECT_MIN_BLOCKS
+#define INFECT_BOUNDS __launch_bounds__(256, COVGPU_INFECT_MIN_BLOCKS)
+#else
+#define INFECT_BOUNDS
+#endif
 constexpr int EDGE_THREADS = 256;
 constexpr int EDGE_VEC = 4;            // edges per 128-bit load
 constexpr int EDGE_ROUND = EDGE_THREADS * EDGE_VEC;  // edges one block reads per round
@@ -206,7 +226,7 @@ __global__ void __launch_bounds__(INF_THREADS) k_infections_write(InfArgs a, int
 // ============================================================ fused agent pass
 
 
-__global__ void __launch_bounds__(AGENT_THREADS) k_agent_step(covgpu_state st, int t, int do_prev, int do_day) {
+__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day) {
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const int nv = sp.n_variants;
@@ -1215,7 +1235,7 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
   icu = sp.n_beds_icu >= 0 && r[COVGPU_RES_CRITICAL_NOW] > sp.n_beds_icu;
 }
 
-__global__ void k_infect_claims(covgpu_state st, int t) {
+__global__ void INFECT_BOUNDS k_infect_claims(covgpu_state st, int t) {
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
   // warp-uniform trip count (infect_tally's ballots need every lane)
