@@ -1218,46 +1218,41 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
       }
     }
   }
-  // this lane's normals and samples
-  double s0 = 0.0, s1 = 0.0;  // lane 0: exp2inf, inf2sym; lane 1: sym2sev, sev2crit; lane 2: recovery / death
-  float peak = 0.0f;          // lane 3: the new peak NAb
-  const bool need = act && (r == 0 || (r == 1 && sev) || r == 2 || (r == 3 && sp.use_waning));
-  if (need) {
+  // This lane's normals and samples, in converged code: every lane of an acting
+  // group runs the same Philox, Box-Muller and sampler instructions on its own
+  // inputs (divergent per-lane branches would run one after another).
+  // Lane 0: exp2inf, inf2sym (normals z0, z1); lane 1: sym2sev, sev2crit (z2, z3);
+  // lane 2: the recovery or death duration (z4); lane 3: the initial NAb (z5).
+  double s0 = 0.0, s1 = 0.0;
+  float peak = 0.0f;
+  if (act) {
     ff za, zb;
     if (injected) {
       const int k = 2 * (r < 2 ? r : 2);
       za = d2ff(tab[k]);
       zb = d2ff(tab[k + 1]);
     } else {
-      uint32_t wa, wb;
-      if (r < 2) {
-        const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
-        wa = r == 0 ? b0.x : b0.z;
-        wb = r == 0 ? b0.y : b0.w;
-      } else {
-        wa = b1.x;
-        wb = b1.y;
-      }
+      const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
+      const uint32_t wa = r == 0 ? b0.x : (r == 1 ? b0.z : b1.x);
+      const uint32_t wb = r == 0 ? b0.y : (r == 1 ? b0.w : b1.y);
       box_muller_ff(wa, wb, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, za, zb);
     }
-    if (r == 0) {
-      s0 = sample_ff(sp.dur[COVGPU_D_EXP2INF], za);
-      if (symp) s1 = sample_ff(sp.dur[COVGPU_D_INF2SYM], zb);
-    } else if (r == 1) {
-      s0 = sample_ff(sp.dur[COVGPU_D_SYM2SEV], za);
-      if (crit) s1 = sample_ff(sp.dur[COVGPU_D_SEV2CRIT], zb);
-    } else if (r == 2) {
-      const int d = !symp ? COVGPU_D_ASYM2REC : (!sev ? COVGPU_D_MILD2REC : (!crit ? COVGPU_D_SEV2REC
-                                                                                  : (dead ? COVGPU_D_CRIT2DIE
-                                                                                          : COVGPU_D_CRIT2REC)));
-      s0 = sample_ff(sp.dur[d], za);
-    } else {  // immunity.py:138-202 update_peak_nab (natural infection)
+    const int rec_d = !symp ? COVGPU_D_ASYM2REC : (!sev ? COVGPU_D_MILD2REC : (!crit ? COVGPU_D_SEV2REC
+                                                                                : (dead ? COVGPU_D_CRIT2DIE
+                                                                                        : COVGPU_D_CRIT2REC)));
+    // first sample of every lane; the second of lanes 0 and 1 (the others repeat a
+    // harmless one to stay converged)
+    const covgpu_dur_par& p0 = r == 0 ? sp.dur[COVGPU_D_EXP2INF]
+                                      : (r == 1 ? sp.dur[COVGPU_D_SYM2SEV] : (r == 2 ? sp.dur[rec_d] : sp.nab_init));
+    const covgpu_dur_par& p1 = r == 0 ? sp.dur[COVGPU_D_INF2SYM] : (r == 1 ? sp.dur[COVGPU_D_SEV2CRIT] : p0);
+    s0 = sample_ff(p0, r == 3 ? zb : za);
+    s1 = sample_ff(p1, r < 2 ? zb : (r == 3 ? zb : za));
+    if (r == 3 && sp.use_waning) {  // immunity.py:138-202 update_peak_nab (natural infection)
       if (st.nab[i] > 0.0f) {
         peak = __fmul_rn(st.peak_nab[i], sp.nab_boost);
       } else {
-        const double init = sample_ff(sp.nab_init, zb);
         const double rel = !symp ? sp.rel_imm_asymp : (!sev ? sp.rel_imm_mild : sp.rel_imm_severe);
-        peak = (float)__dmul_rn(__dmul_rn(exp2_ff(d2ff(init)), rel), sp.nab_norm);
+        peak = (float)__dmul_rn(__dmul_rn(exp2_ff(d2ff(s0)), rel), sp.nab_norm);
       }
     }
   }

@@ -138,29 +138,30 @@ __device__ __forceinline__ ff ff_sqrt(ff x) {
   return fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
 }
 
-// the uniform (a + 1/2) * 2^-32 of a 32-bit word, exactly, as float-float
+// the uniform (a + 1/2) * 2^-32 of a 32-bit word, exactly, as float-float: the
+// odd 33-bit k = 2a + 1 is kh * 2^16 + kl with both halves exact in float32,
+// and the two-sum of the halves is (k rounded to float32, the exact remainder);
+// 32-bit operations only (64-bit conversions are slow on GB300)
 __device__ __forceinline__ ff u01_ff(uint32_t a) {
-  const unsigned long long k = 2ull * a + 1ull;                   // 33 bits
-  const float hi = __ull2float_rn(k);
-  const float lo = (float)((long long)k - (long long)__float2ull_rz(hi));  // |k - hi| < 2^9: exact
-  return ff{__fmul_rn(hi, 0x1p-33f), __fmul_rn(lo, 0x1p-33f)};
+  const float kh = (float)(a >> 15), kl = (float)(((a << 1) | 1u) & 0xFFFFu);
+  const ff k = two_sum(__fmul_rn(kh, 65536.0f), kl);
+  return ff{__fmul_rn(k.hi, 0x1p-33f), __fmul_rn(k.lo, 0x1p-33f)};
 }
 
-// a 64-bit integer (|k| < 2^48) as float-float, exactly
-__device__ __forceinline__ ff ll_to_ff(long long k) {
-  const float hi = __ll2float_rn(k);
-  return ff{hi, (float)(k - __float2ll_rz(hi))};
+// a 32-bit integer as float-float, exactly (the same split)
+__device__ __forceinline__ ff i32_to_ff(int32_t k) {
+  return two_sum(__fmul_rn((float)(k >> 12), 4096.0f), (float)(k & 0xFFF));
 }
 
 // cos and sin of 2 pi u for u = (b + 1/2) * 2^-32: the quadrant and the nearest
 // of the points j pi / 64 from the word's bits (exact), then the Taylor series
 // of the residual angle |phi| <= pi / 128 (tables: COVGPU_SINCOS_TAB)
 __device__ __forceinline__ void ff_cossin_2pi(uint32_t b, const float (*tab)[4], ff& c, ff& s) {
-  const unsigned long long k = 2ull * b + 1ull;                    // 4u = k * 2^-31
-  const unsigned q = (unsigned)(k >> 31);                          // quadrant 0..3
-  const unsigned long long fk = k & 0x7FFFFFFFull;                 // f = fk * 2^-31 in [0, 1)
-  const unsigned j = (unsigned)((fk + (1ull << 25)) >> 26);        // nearest j / 32, j = 0..32
-  const ff r = ll_to_ff((long long)fk - ((long long)j << 26));     // (f - j/32) * 2^31
+  // k = 2b + 1 (33 bits), 4u = k * 2^-31, in 32-bit pieces
+  const unsigned q = b >> 30;                                      // quadrant 0..3
+  const uint32_t fk = ((b << 1) | 1u) & 0x7FFFFFFFu;               // f = fk * 2^-31 in [0, 1)
+  const uint32_t j = (fk + (1u << 25)) >> 26;                      // nearest j / 32, j = 0..32
+  const ff r = i32_to_ff((int32_t)(fk - (j << 26)));               // (f - j/32) * 2^31, |.| <= 2^25
   const ff phi = ff_mul(ff{COVGPU_PI_2_HI, COVGPU_PI_2_LO}, ff{__fmul_rn(r.hi, 0x1p-31f), __fmul_rn(r.lo, 0x1p-31f)});
   const ff p2 = ff_mul(phi, phi);
   const float x2 = p2.hi;
@@ -211,24 +212,37 @@ __device__ __forceinline__ ff d2ff(double x) {
 }
 __device__ __forceinline__ double ff2d(ff x) { return __dadd_rn((double)x.hi, (double)x.lo); }
 
+// A distribution parameter pair (a, b) of covgpu_dur_par as float-float, so that
+// the float64 conversions can be issued ahead of the normal they are applied to.
+struct DistFF {
+  int code;
+  ff a, b;
+};
+__device__ __forceinline__ DistFF dist_ff(const covgpu_dur_par& d) { return DistFF{d.code, d2ff(d.a), d2ff(d.b)}; }
+
 // utils.py:156-236 sample() of a distribution that is a function of one standard
-// normal z, in float-float; the result as the float64 the reference stores
-__device__ __forceinline__ double sample_ff(const covgpu_dur_par& d, ff z) {
-  const ff y = ff_add(d2ff(d.a), ff_mul(d2ff(d.b), z));
+// normal z, in float-float; the result as the float64 the reference stores.
+// etab: COVGPU_EXP_TAB or its shared-memory copy.
+__device__ __forceinline__ double sample_ff(const DistFF& d, ff z, const float (*etab)[2]) {
+  const ff y = ff_add(d.a, ff_mul(d.b, z));
   switch (d.code) {
-    case COVGPU_DIST_LOGNORMAL_INT: return (double)ff_rint(ff_exp(y, COVGPU_EXP_TAB));
-    case COVGPU_DIST_LOGNORMAL: return ff2d(ff_exp(y, COVGPU_EXP_TAB));
+    case COVGPU_DIST_LOGNORMAL_INT: return (double)ff_rint(ff_exp(y, etab));
+    case COVGPU_DIST_LOGNORMAL: return ff2d(ff_exp(y, etab));
     case COVGPU_DIST_NORMAL: return ff2d(y);
     case COVGPU_DIST_NORMAL_INT: return (double)ff_rint(y.hi < 0.0f ? ff{-y.hi, -y.lo} : y);
     case COVGPU_DIST_NORMAL_POS: return fabs(ff2d(y));
     default: return 0.0;
   }
 }
+__device__ __forceinline__ double sample_ff(const covgpu_dur_par& d, ff z) {
+  return sample_ff(dist_ff(d), z, COVGPU_EXP_TAB);
+}
 
 // 2^x for a float-float x: exp(x ln 2)
-__device__ __forceinline__ double exp2_ff(ff x) {
-  return ff2d(ff_exp(ff_mul(x, ff{COVGPU_LN2_FF_HI, COVGPU_LN2_FF_LO}), COVGPU_EXP_TAB));
+__device__ __forceinline__ double exp2_ff(ff x, const float (*etab)[2]) {
+  return ff2d(ff_exp(ff_mul(x, ff{COVGPU_LN2_FF_HI, COVGPU_LN2_FF_LO}), etab));
 }
+__device__ __forceinline__ double exp2_ff(ff x) { return exp2_ff(x, COVGPU_EXP_TAB); }
 
 // calc_VE (immunity.py:216-247) for eff = nab * imm with ln(imm) given:
 // exp(alpha) * eff^beta / (1 + exp(alpha) * eff^beta) = logistic(z),
