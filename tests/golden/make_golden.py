@@ -25,6 +25,7 @@ Fixtures:
                        inputs and outputs on a reference run (sciris' smooth restated)
   ref_analysis.npz     TransTree / Fit / compute_gof outputs of the reference's own code on a
                        reference run with testing (pandas and sciris replaced by stand-ins)
+  state_diagram.json   the state-implication matrices of tests/state_diagram.xlsx
   ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
                        20k-agent random sim (60 days), reference code with MT19937 streams
 """
@@ -743,6 +744,51 @@ def make_analysis_fixture(ref):
     print('ref_analysis.npz written', len(log), 'records')
 
 
+def make_state_diagram_fixture(ref=None):
+    """The state-implication matrices of the reference's tests/state_diagram.xlsx
+    (sheets 'Without waning' and 'With waning', read by test_immunity.py's
+    test_states): relation[s1][s2] = 1 if being s1 implies s2, -1 if it implies
+    not s2, 0 if either. Read with zipfile and the sheet XML (no openpyxl)."""
+    import re
+    import zipfile
+    import xml.etree.ElementTree as ET
+    path = os.path.join(refload.REF_ROOT, 'tests', 'state_diagram.xlsx')
+    z = zipfile.ZipFile(path)
+    ns = {'m': 'http://schemas.openxmlformats.org/spreadsheetml/2006/main'}
+    rel_ns = '{http://schemas.openxmlformats.org/officeDocument/2006/relationships}id'
+    strings = [''.join(t.text or '' for t in si.iter(f'{{{ns["m"]}}}t'))
+               for si in ET.fromstring(z.read('xl/sharedStrings.xml')).findall('m:si', ns)]
+    rels = ET.fromstring(z.read('xl/_rels/workbook.xml.rels'))
+    targets = {r.get('Id'): r.get('Target') for r in rels}
+    wb = ET.fromstring(z.read('xl/workbook.xml'))
+    out = {}
+    for sheet in wb.find('m:sheets', ns):
+        name = sheet.get('name')
+        if name not in ('Without waning', 'With waning'):
+            continue
+        xml = ET.fromstring(z.read('xl/' + targets[sheet.get(rel_ns)].lstrip('/').replace('xl/', '')))
+        rows = []
+        for row in xml.find('m:sheetData', ns):
+            cells = {}
+            for c in row:
+                v = c.find('m:v', ns)
+                if v is None:
+                    continue
+                col = re.match(r'[A-Z]+', c.get('r')).group(0)
+                cells[col] = strings[int(v.text)] if c.get('t') == 's' else v.text
+            rows.append(cells)
+        cols = sorted((k for k in rows[0] if k != 'A'), key=lambda c: (len(c), c))
+        states = [rows[0][c] for c in cols]
+        rel = {}
+        for r in rows[1:]:
+            if r.get('A') in states:
+                rel[r['A']] = {states[j]: int(float(r[c])) for j, c in enumerate(cols)}
+        out[name] = {'states': states, 'relation': rel}
+    with open(os.path.join(HERE, 'state_diagram.json'), 'w') as f:
+        json.dump(out, f, indent=1, ensure_ascii=False)
+    print('state_diagram.json written', {k: len(v['relation']) for k, v in out.items()})
+
+
 def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
     keys = ['new_infections', 'new_severe', 'new_deaths', 'new_infectious', 'new_recoveries', 'new_critical',
             'new_symptomatic', 'n_exposed']
@@ -769,7 +815,7 @@ def main():
     ref = refload.Reference()
     groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
                   sims=make_sims_fixture, testing=make_testing_fixture, reporting=make_reporting_fixture,
-                  analysis=make_analysis_fixture,
+                  analysis=make_analysis_fixture, states=make_state_diagram_fixture,
                   distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
     for name, fn in groups.items():
         if args.only is None or args.only == name:
