@@ -259,18 +259,24 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
 
   // ---------------------------------------------------------- close day t-1
   if (do_prev) {
-    // sim.py:652-656: stocks at the end of day t-1
+    // sim.py:652-656: stocks at the end of day t-1. Warp counts by ballot: lane k
+    // keeps count k and adds it to the block's counter (one atomic per lane)
+    const uint32_t fv = valid ? f : 0u;
+    uint32_t mine = 0;
 #pragma unroll
     for (int k = 0; k < N_STOCKS; ++k) {
-      const unsigned c = __reduce_add_sync(0xffffffffu, (valid && (f & STOCK_BITS[k])) ? 1u : 0u);
-      if (lane == 0 && c) atomicAdd(&s_prev[k], c);
+      const unsigned c = __popc(__ballot_sync(0xffffffffu, (fv & STOCK_BITS[k]) != 0u));
+      if (lane == k) mine = c;
     }
+    if (mine) atomicAdd(&s_prev[lane], mine);
+    mine = 0;  // by variant: lane 2v exposed, lane 2v + 1 infectious
     for (int v = 0; v < nv; ++v) {
-      const unsigned ce = __reduce_add_sync(0xffffffffu, (valid && ((f >> (EXPV_SHIFT + v)) & 1u)) ? 1u : 0u);
-      const unsigned ci = __reduce_add_sync(0xffffffffu, (valid && ((f >> (INFV_SHIFT + v)) & 1u)) ? 1u : 0u);
-      if (lane == 0 && ce) atomicAdd(&s_var[RV_N_EXPOSED * COVGPU_MAX_VARIANTS + v], ce);
-      if (lane == 0 && ci) atomicAdd(&s_var[RV_N_INFECTIOUS * COVGPU_MAX_VARIANTS + v], ci);
+      const unsigned ce = __popc(__ballot_sync(0xffffffffu, (fv >> (EXPV_SHIFT + v)) & 1u));
+      const unsigned ci = __popc(__ballot_sync(0xffffffffu, (fv >> (INFV_SHIFT + v)) & 1u));
+      if (lane == 2 * v) mine = ce;
+      if (lane == 2 * v + 1) mine = ci;
     }
+    if (mine) atomicAdd(&s_var[((lane & 1) ? RV_N_INFECTIOUS : RV_N_EXPOSED) * COVGPU_MAX_VARIANTS + (lane >> 1)], mine);
     if (valid) {
       float nab = 0.0f;
       if (sp.use_waning) {
@@ -403,20 +409,30 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       if (f != f_in) st.flags[i] = f;
       if (vs != vs_in) st.vstate[i] = vs;
     }
-    // flows (people.py:172-180) and the severe/critical counts of sim.py:579-580
+    // flows (people.py:172-180) and the severe/critical counts of sim.py:579-580,
+    // counted by ballot as the stocks are; lane k adds count k to its slot
     const unsigned cv[9] = {c_inf, c_symp, c_sev, c_crit, c_rec, c_dead, c_kdead,
                             (valid && (f & B_SEV)) ? 1u : 0u, (valid && (f & B_CRIT)) ? 1u : 0u};
-    const int slot[9] = {R_INFECTIOUS, R_SYMPTOMATIC, R_SEVERE, R_CRITICAL, R_RECOVERIES, R_DEATHS,
-                         R_KNOWN_DEATHS, COVGPU_RES_SEVERE_NOW, COVGPU_RES_CRITICAL_NOW};
+    // the slots of the nine counts, six bits each
+    constexpr uint64_t FLOW_SLOTS =
+        (uint64_t)R_INFECTIOUS | (uint64_t)R_SYMPTOMATIC << 6 |
+        (uint64_t)R_SEVERE << 12 | (uint64_t)R_CRITICAL << 18 | (uint64_t)R_RECOVERIES << 24 |
+        (uint64_t)R_DEATHS << 30 | (uint64_t)R_KNOWN_DEATHS << 36 | (uint64_t)COVGPU_RES_SEVERE_NOW << 42 |
+        (uint64_t)COVGPU_RES_CRITICAL_NOW << 48;
+    static_assert(COVGPU_N_RES_INT <= 64, "six-bit slots");
+    uint32_t mine = 0;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const unsigned c = __reduce_add_sync(0xffffffffu, cv[k]);
-      if (lane == 0 && c) atomicAdd(&s_cnt[slot[k]], c);
+      const unsigned c = __popc(__ballot_sync(0xffffffffu, cv[k] != 0u));
+      if (lane == k) mine = c;
     }
+    if (mine) atomicAdd(&s_cnt[(FLOW_SLOTS >> (6 * (lane % 10))) & 63u], mine);  // lanes 0-8
+    mine = 0;
     for (int v = 0; v < nv; ++v) {
-      const unsigned c = __reduce_add_sync(0xffffffffu, inf_v == v ? 1u : 0u);
-      if (lane == 0 && c) atomicAdd(&s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + v], c);
+      const unsigned c = __popc(__ballot_sync(0xffffffffu, inf_v == v));
+      if (lane == v) mine = c;
     }
+    if (mine) atomicAdd(&s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + lane], mine);
     // role bitmaps: warp w of this block covers the 32-aligned word (i - lane) / 32
     const uint32_t sm = __ballot_sync(0xffffffffu, src_bit), tm = __ballot_sync(0xffffffffu, tgt_bit);
     if (lane == 0 && blk.begin + warp * 32 < blk.end) {
