@@ -443,9 +443,9 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   }
 
   // ---------------------------------------------------------- block totals
-  nab_fx = warp_sum_ll(nab_fx);
-  sus_fx = warp_sum_ll(sus_fx);
-  symp_fx = warp_sum_ll(symp_fx);
+  nab_fx = warp_sum_fx(nab_fx);
+  sus_fx = warp_sum_fx(sus_fx);
+  symp_fx = warp_sum_fx(symp_fx);
   if (lane == 0) { s_f[warp][0] = nab_fx; s_f[warp][1] = sus_fx; s_f[warp][2] = symp_fx; }
   __syncthreads();
   const int npts = sp.npts;

@@ -157,5 +157,14 @@ __device__ __forceinline__ long long warp_sum_ll(long long x) {
   for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
   return x;
 }
+// warp sum of the non-negative fixed-point values: two 32-bit reductions of the
+// 20-bit low and 27-bit high parts when every lane's x < 2^47 (their sums over 32
+// lanes cannot overflow), else the 64-bit shuffle sum
+__device__ __forceinline__ long long warp_sum_fx(long long x) {
+  if (__any_sync(0xffffffffu, (unsigned long long)x >= (1ull << 47))) return warp_sum_ll(x);
+  const unsigned lo = __reduce_add_sync(0xffffffffu, (unsigned)(x & 0xFFFFF));
+  const unsigned hi = __reduce_add_sync(0xffffffffu, (unsigned)(x >> 20));
+  return ((long long)hi << 20) + (long long)lo;
+}
 
 }  // namespace covgpu
