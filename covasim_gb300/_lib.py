@@ -118,6 +118,7 @@ class State(C.Structure):
         ('imm_stride_variants', C.c_int32), ('_pad0', C.c_int32),
         ('dates', C.c_void_p), ('durs', C.c_void_p),
         ('viral_load', C.c_void_p), ('roles', C.c_void_p), ('claim', C.c_void_p),
+        ('src_rec', C.c_void_p),
         ('events', C.c_void_p), ('event_capacity', C.c_int64), ('event_count', C.c_void_p),
         ('log', C.c_void_p), ('log_capacity', C.c_int64), ('log_count', C.c_void_p),
         ('status', C.c_void_p), ('hospicu', C.c_void_p),

@@ -395,13 +395,17 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
         }
       }
 
-      // viral load (sim.py:601-608) and edge-pass roles for the infectious / susceptible
+      // viral load (sim.py:601-608) and edge-pass roles for the infectious / susceptible,
+      // with the records the edge pass gathers for its candidates (one 16-byte load
+      // per endpoint instead of one per field)
       if (f & B_INF) {
         const float rt = st.rel_trans[i];
-        st.viral_load[i] = viral_load_one(t, date_row(st, COVGPU_DATE_INFECTIOUS)[i],
-                                          date_row(st, COVGPU_DATE_RECOVERED)[i], date_row(st, COVGPU_DATE_DEAD)[i],
-                                          sp.frac_time, sp.load_ratio, sp.high_cap);
+        const float vl = viral_load_one(t, date_row(st, COVGPU_DATE_INFECTIOUS)[i],
+                                        date_row(st, COVGPU_DATE_RECOVERED)[i], date_row(st, COVGPU_DATE_DEAD)[i],
+                                        sp.frac_time, sp.load_ratio, sp.high_cap);
+        st.viral_load[i] = vl;
         src_bit = (rt != 0.0f && iv < (uint32_t)nv) ? 1u : 0u;
+        if (src_bit) reinterpret_cast<float4*>(st.src_rec)[i] = make_float4(rt, vl, __uint_as_float(vs), 0.0f);
       }
       // exclusive by construction (the infectious are never susceptible); the edge
       // pass relies on it to queue at most one direction per edge
@@ -583,11 +587,12 @@ __device__ __forceinline__ void lik_terms(const covgpu_state& st, const SegCtx& 
 template <bool LIK>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
                                          int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
-  const uint32_t vs = __ldg(st.vstate + s);
+  const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
   const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
-  const float rt = __ldg(st.rel_trans + s), vl = __ldg(st.viral_load + s), rs = __ldg(st.rel_sus + g);
+  const float rs = __ldg(st.rel_sus + g);
   const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
-  const uint32_t v = (vs >> 8) & 0xFFu;
+  const float rt = sr.x, vl = sr.y;
+  const uint32_t v = (__float_as_uint(sr.z) >> 8) & 0xFFu;
   const uint32_t vc = v < (uint32_t)c.nv ? v : 0u;
   const float si = __ldg(st.sus_imm + (int64_t)vc * st.n + g);
   const float beta = __ldg(c.beta_t + vc);
@@ -1974,7 +1979,8 @@ int covgpu_infections_noalloc(float beta, const int32_t* p1, const int32_t* p2, 
 
 static int check_state(const covgpu_state* st) {
   if (!st || st->n <= 0 || st->n_sims <= 0 || st->n_agent_blocks <= 0) return COVGPU_BADARG;
-  if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->events ||
+  if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->src_rec ||
+      !st->events ||
       !st->event_count || !st->status)
     return COVGPU_BADARG;
   if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0))

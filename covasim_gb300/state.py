@@ -194,6 +194,7 @@ class BatchState:
         t['durs'] = torch.full((L.N_DURS, n), float('nan'), dtype=F32, device=dev)
         t['roles'] = torch.zeros(2 * ((n + 31) // 32), dtype=I32, device=dev)
         t['claim'] = torch.full((n,), -1, dtype=I64, device=dev)
+        t['src_rec'] = torch.zeros((n, 4), dtype=F32, device=dev)  # the edge pass's record of each source
         n_real = sum(sp.n for sp in self.specs)
         self.event_capacity = int(event_capacity or (2 * n_real + 65536))
         t['events'] = torch.zeros((self.event_capacity, 4), dtype=I32, device=dev)
@@ -502,7 +503,8 @@ class BatchState:
         st.edge_resident = int(self.edge_resident)
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
-                  'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'events', 'event_count',
+                  'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'src_rec',
+                  'events', 'event_count',
                   'log_count', 'status'):
             setattr(st, k, t[k].data_ptr())
         st.imm_stride_variants = self.nv_max
@@ -790,7 +792,7 @@ class BatchState:
             self.t['durs'][cvd.DURS.index(key), s].copy_(torch.as_tensor(np.asarray(values, np.float32)))
         elif key in cvd.IMM_STATES:
             self.t[key][:self.specs[sim].nv, s].copy_(torch.as_tensor(np.asarray(values, np.float32)))
-        elif key in self.t and key not in ('roles', 'claim', 'events', 'log', 'status'):
+        elif key in self.t and key not in ('roles', 'claim', 'src_rec', 'events', 'log', 'status'):
             dst = self.t[key][s]
             dst.copy_(torch.as_tensor(np.asarray(values), dtype=dst.dtype))
         else:
