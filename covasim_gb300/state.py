@@ -264,6 +264,7 @@ class BatchState:
         self.segments = []   # (ctypes Layer, tensors kept alive)
         self.layer_tensors = []
         self.segment_index = {}  # (sim, layer) -> segment index
+        checks, deferred = [], []  # device checks of torch layer inputs; their index builds
         for s, (sp, off) in enumerate(zip(self.specs, self.offsets)):
             for li, ly in enumerate(sp.layers):
                 p1 = ly['p1'] if torch.is_tensor(ly['p1']) else np.asarray(ly['p1'], dtype=np.int64)
@@ -281,21 +282,23 @@ class BatchState:
                     rec.dynamic = 1
                     rec.beta_const = 1.0
                 elif torch.is_tensor(ly['p1']):
-                    # torch inputs (e.g. pinned host memory): uploaded as they are, checked on the device
+                    # torch inputs (e.g. pinned host memory): uploaded as they are, checked on the
+                    # device; the checks of every layer are read back together below, before
+                    # anything indexes with them
                     tp1 = ly['p1'].to(self.device, torch.int32, non_blocking=True)
                     tp2 = ly['p2'].to(self.device, torch.int32, non_blocking=True)
                     lo1, hi1 = torch.aminmax(tp1)
                     lo2, hi2 = torch.aminmax(tp2)
-                    if bool((tp1[1:] < tp1[:-1]).any()):
-                        raise ValueError(f'layer {ly["key"]}: p1 must be sorted')
-                    if min(int(lo1), int(lo2)) < 0 or max(int(hi1), int(hi2)) >= sp.n:
-                        raise ValueError(f'layer {ly["key"]}: agent index out of range')
+                    unsorted = (tp1[1:] < tp1[:-1]).any() if n_edges > 1 else torch.zeros((), dtype=torch.bool,
+                                                                                          device=self.device)
+                    checks.append((ly['key'], sp.n, torch.stack([unsorted.to(torch.int64), torch.minimum(lo1, lo2).to(
+                        torch.int64), torch.maximum(hi1, hi2).to(torch.int64)])))
                     if off:  # out of place: .to() returns the caller's tensor when it is already on the device
                         tp1 = tp1 + off
                         tp2 = tp2 + off
                     rec.p1, rec.p2 = tp1.data_ptr(), tp2.data_ptr()
                     keep += [tp1, tp2]
-                    keep += self._trace_index(rec, sp, off, n_edges)
+                    deferred.append((rec, sp, off, n_edges, keep))
                     b = ly.get('beta')
                     if b is None or bool((b == b[0]).all()):
                         rec.beta = None
@@ -329,6 +332,15 @@ class BatchState:
                 self.segment_index[(s, li)] = len(self.segments)
                 self.segments.append(rec)
                 self.layer_tensors.append(keep)
+        if checks:  # one read-back for all torch layers
+            got = torch.stack([c[2] for c in checks]).cpu().tolist()
+            for (key, n, _), (unsorted, lo, hi) in zip(checks, got):
+                if unsorted:
+                    raise ValueError(f'layer {key}: p1 must be sorted')
+                if lo < 0 or hi >= n:
+                    raise ValueError(f'layer {key}: agent index out of range')
+        for rec, sp, off, n_edges, keep in deferred:
+            keep += self._trace_index(rec, sp, off, n_edges)
         self._tile_segments()
 
     def _trace_index(self, rec, sp, off, n_edges):
