@@ -1,18 +1,20 @@
 // covgpu: GB300-native (sm_103a) kernels for Covasim 3.1.7's per-day step.
 //
 // Kernels (all HBM/L2-bound integer and float32 work; no tensor cores):
-//   k_viral_load / k_trans_sus / k_infections_*  the reference's three numba
-//       functions (covasim/utils.py:38-128) as standalone drop-ins;
 //   k_agent_step     one dense pass per agent per day: update_states_pre
 //       (people.py:164-312,368-374) + check_immunity (immunity.py:303-350) +
 //       update_nab (immunity.py:205-213) + stocks/flows (sim.py:651-674) +
-//       viral load and source/target role bitmaps for the edge pass;
+//       viral load, source/target role bitmaps and source records for the edge pass;
 //   k_edge_pass      every layer segment and variant of every sim: edges streamed with
 //       128-bit reads, source->target candidates queued per warp in shared
 //       memory, then compute_trans_sus folded in lane-packed, Philox Bernoullis,
-//       warp-ballot compaction of events, atomicMin first-infector claim;
+//       warp-ballot compaction of events, atomicMin first-infector claim
+//       (k_edge_pass_res: the same with the source bitmap in shared memory);
 //   k_infect_claims / k_infect_list   People.infect (people.py:435-586) +
 //       update_peak_nab (immunity.py:138-202).
+// The reference's standalone numba functions are in covgpu_reference.cu, the
+// testing and tracing passes in covgpu_testing.cu, the population builders in
+// covgpu_pop.cu.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -21,37 +23,24 @@
 #include "covgpu.h"
 #include "covgpu_device.cuh"
 #include "covgpu_ff.cuh"
-#include "covgpu_scan.cuh"
+#include "covgpu_launch.cuh"
 
 using namespace covgpu;
 
 namespace {
 
-constexpr int AGENT_THREADS = 256;     // one agent per thread; agent blocks hold <= 256 agents
-// resident blocks per SM that the register budget of the agent / infect pass
-// must allow (0: the compiler's choice). Six agent blocks (40 registers, a
-// few spilled) ran the agent pass of a 1M-agent run 10% faster than the
-// compiler's 58 registers (four blocks); the infect pass showed no change.
+// resident blocks per SM that the register budget of the agent pass must allow
+// (0: the compiler's choice). Six blocks (40 registers, a few spilled) ran the
+// agent pass of a 1M-agent run 10% faster than the compiler's 58 registers (four
+// blocks); bounding the infect pass the same way changed nothing.
 #ifndef COVGPU_AGENT_MIN_BLOCKS
 #define COVGPU_AGENT_MIN_BLOCKS 6
-#endif
-#ifndef COVGPU_INFECT_MIN_BLOCKS
-#define COVGPU_INFECT_MIN_BLOCKS 0
 #endif
 #if COVGPU_AGENT_MIN_BLOCKS
 #define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS, COVGPU_AGENT_MIN_BLOCKS)
 #else
 #define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS)
 #endif
-#if COVGPU_INFECT_MIN_BLOCKS
-#define INFECT_BOUNDS __launch_bounds__(256, COVGPU_INFECT_MIN_BLOCKS)
-#else
-#define INFECT_BOUNDS
-#endif
-constexpr int EDGE_THREADS = 256;
-constexpr int EDGE_VEC = 4;            // edges per 128-bit load
-constexpr int EDGE_ROUND = EDGE_THREADS * EDGE_VEC;  // edges one block reads per round
-constexpr int64_t EDGE_TILE_MAX = 8192;  // edge tiles: 1024, 2048, 4096 or 8192 edges (covgpu_state.edge_tile)
 constexpr int EQ_ROUND = 32 * EDGE_VEC;  // most candidates one warp appends per round (one per edge)
 #ifndef COVGPU_EQ_CAP
 #define COVGPU_EQ_CAP 256
@@ -59,169 +48,8 @@ constexpr int EQ_ROUND = 32 * EDGE_VEC;  // most candidates one warp appends per
 constexpr int EQ_CAP = COVGPU_EQ_CAP;  // candidate queue entries per warp (drained when a round could overflow);
                                        // 192 and 160, which leave L1 more room, measured slower
 static_assert(2 * EDGE_TILE_MAX <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
-constexpr int INF_TILE = 2048;         // edges per block of the ordered compute_infections
-constexpr int INF_THREADS = 256;
-constexpr int INF_PER_THREAD = INF_TILE / INF_THREADS;
 constexpr int CALL_TAG_SEED = 1;       // covgpu_infect_list call_tag of the day-0 seed infections
 
-inline int launch_status() {
-  return cudaGetLastError() == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
-}
-inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
-
-// ============================================================ standalone kernels
-
-__global__ void k_viral_load(int t, const float* __restrict__ ts, const float* __restrict__ tr,
-                             const float* __restrict__ td, int64_t n, float frac_time, float load_ratio,
-                             float high_cap, float* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = viral_load_one(t, ts[i], tr[i], td[i], frac_time, load_ratio, high_cap);
-}
-
-// utils.py:82-90: rel_trans*inf*f_quar*f_asymp*f_iso*beta_layer*viral_load and
-// rel_sus*sus*f_quar*(1-immunity), float32 left to right (a factor of 1.0 is exact).
-__global__ void k_trans_sus(const float* __restrict__ rt, const float* __restrict__ rs,
-                            const uint8_t* __restrict__ inf, const uint8_t* __restrict__ sus, float beta_layer,
-                            const float* __restrict__ vl, const uint8_t* __restrict__ symp,
-                            const uint8_t* __restrict__ iso, const uint8_t* __restrict__ quar, float asymp_factor,
-                            float iso_factor, float quar_factor, const float* __restrict__ imm, int64_t n,
-                            float* __restrict__ ort, float* __restrict__ ors) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const bool q = quar[i];
-    float a = __fmul_rn(rt[i], inf[i] ? 1.0f : 0.0f);
-    a = __fmul_rn(a, q ? quar_factor : 1.0f);
-    a = __fmul_rn(a, symp[i] ? 1.0f : asymp_factor);
-    a = __fmul_rn(a, iso[i] ? iso_factor : 1.0f);
-    a = __fmul_rn(a, beta_layer);
-    a = __fmul_rn(a, vl[i]);
-    float b = __fmul_rn(rs[i], sus[i] ? 1.0f : 0.0f);
-    b = __fmul_rn(b, q ? quar_factor : 1.0f);
-    b = __fmul_rn(b, __fsub_rn(1.0f, imm[i]));
-    ort[i] = a;
-    ors[i] = b;
-  }
-}
-
-// utils.py:113-124 for one (direction, edge): in inf_inds (source trans != 0),
-// drawn (beta != 0) and u < p in float64.
-struct InfArgs {
-  float beta; const int32_t* p1; const int32_t* p2; const float* lb; int64_t E;
-  const float* rt; const float* rs; int64_t n_agents; const double* uni; uint32_t k0, k1; int day, variant, layer;
-  int32_t* status;
-};
-__device__ __forceinline__ bool inf_hit(const InfArgs& a, int dir, int64_t e, int32_t& src, int32_t& tgt) {
-  src = dir ? a.p2[e] : a.p1[e];
-  tgt = dir ? a.p1[e] : a.p2[e];
-  if ((uint32_t)src >= (uint64_t)a.n_agents || (uint32_t)tgt >= (uint64_t)a.n_agents) {  // bad index: skip
-    if (a.status) atomicOr(a.status, COVGPU_BADARG);
-    return false;
-  }
-  const float st = a.rt[src];
-  if (st == 0.0f) return false;
-  const float p = __fmul_rn(__fmul_rn(__fmul_rn(a.beta, a.lb[e]), st), a.rs[tgt]);
-  if (p == 0.0f) return false;
-  double u;
-  if (a.uni) {
-    u = a.uni[(int64_t)dir * a.E + e];
-  } else {
-    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)a.day,
-                                      TAG_EDGE | ((uint32_t)a.variant << 8) | (uint32_t)a.layer), a.k0, a.k1);
-    return dir ? bern52(w.z, w.w, p) : bern52(w.x, w.y, p);
-  }
-  return u < (double)p;
-}
-
-__global__ void __launch_bounds__(INF_THREADS) k_infections_count(InfArgs a, int64_t ntiles, int32_t* counts) {
-  const int dir = blockIdx.y;
-  const int64_t tile = blockIdx.x;
-  const int64_t e0 = tile * INF_TILE + (int64_t)threadIdx.x * INF_PER_THREAD;
-  int c = 0;
-  for (int j = 0; j < INF_PER_THREAD; ++j) {
-    const int64_t e = e0 + j;
-    int32_t s, g;
-    if (e < a.E && inf_hit(a, dir, e, s, g)) ++c;
-  }
-  __shared__ int s_sum;
-  if (threadIdx.x == 0) s_sum = 0;
-  __syncthreads();
-  c = __reduce_add_sync(0xffffffffu, (unsigned)c);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_sum, c);
-  __syncthreads();
-  if (threadIdx.x == 0) counts[(int64_t)dir * ntiles + tile] = s_sum;
-}
-
-// single-block exclusive scan of m counts into int64 offsets; total into *total
-__global__ void __launch_bounds__(1024) k_scan(const int32_t* counts, int64_t m, int64_t* offs, int64_t* total,
-                                               int64_t capacity, int32_t* status) {
-  __shared__ int64_t s_part[1024];
-  const int64_t per = (m + blockDim.x - 1) / blockDim.x;
-  const int64_t b = threadIdx.x * per, e = min(b + per, m);
-  int64_t sum = 0;
-  for (int64_t i = b; i < e; ++i) sum += counts[i];
-  s_part[threadIdx.x] = sum;
-  __syncthreads();
-  for (int off = 1; off < (int)blockDim.x; off <<= 1) {  // Hillis-Steele inclusive scan
-    const int64_t v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0;
-    __syncthreads();
-    s_part[threadIdx.x] += v;
-    __syncthreads();
-  }
-  int64_t run = s_part[threadIdx.x] - sum;
-  for (int64_t i = b; i < e; ++i) { offs[i] = run; run += counts[i]; }
-  if (threadIdx.x == blockDim.x - 1) {
-    *total = s_part[threadIdx.x];
-    if (s_part[threadIdx.x] > capacity && status) atomicOr(status, COVGPU_OVERFLOW);
-  }
-}
-
-// ordered write: block-level exclusive scan of per-thread hit counts keeps edge order
-__global__ void __launch_bounds__(INF_THREADS) k_infections_write(InfArgs a, int64_t ntiles, const int64_t* offs,
-                                                                  int32_t* out_src, int32_t* out_tgt, int64_t cap) {
-  const int dir = blockIdx.y;
-  const int64_t tile = blockIdx.x;
-  const int64_t e0 = tile * INF_TILE + (int64_t)threadIdx.x * INF_PER_THREAD;
-  uint32_t hits = 0;
-  int32_t hs[INF_PER_THREAD], ht[INF_PER_THREAD];
-#pragma unroll
-  for (int j = 0; j < INF_PER_THREAD; ++j) {
-    const int64_t e = e0 + j;
-    int32_t s = 0, g = 0;
-    if (e < a.E && inf_hit(a, dir, e, s, g)) hits |= 1u << j;
-    hs[j] = s;
-    ht[j] = g;
-  }
-  const int c = __popc(hits);
-  // block exclusive scan of c (warp shuffle scan + warp totals in shared memory)
-  __shared__ int s_warp[INF_THREADS / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int incl = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    int w = lane < INF_THREADS / 32 ? s_warp[lane] : 0;
-    int wi = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += v;
-    }
-    if (lane < INF_THREADS / 32) s_warp[lane] = wi - w;
-  }
-  __syncthreads();
-  int64_t pos = offs[(int64_t)dir * ntiles + tile] + s_warp[warp] + (incl - c);
-#pragma unroll
-  for (int j = 0; j < INF_PER_THREAD; ++j) {
-    if (hits & (1u << j)) {
-      if (pos < cap) { out_src[pos] = hs[j]; out_tgt[pos] = ht[j]; }
-      ++pos;
-    }
-  }
-}
 
 // ============================================================ fused agent pass
 
@@ -1429,7 +1257,7 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
   icu = sp.n_beds_icu >= 0 && r[COVGPU_RES_CRITICAL_NOW] > sp.n_beds_icu;
 }
 
-__global__ void INFECT_BOUNDS k_infect_claims(covgpu_state st, int t) {
+__global__ void k_infect_claims(covgpu_state st, int t) {
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
   // IG lanes per event, 32 / IG events per warp and iteration; warp-uniform trip
@@ -1498,315 +1326,6 @@ __global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1
   }
 }
 
-// ============================================================ testing and tracing
-//
-// Day t with a test_prob / contact_tracing sim, after the agent pass and any
-// importations (sim.py:596-600): k_test_pass draws who tests and marks the
-// agents to trace, k_trace_scan marks their contacts layer by layer, and
-// k_post_pass notifies the contacts and runs update_states_post.
-
-__device__ __forceinline__ bool day_active(int t, int start, int end) { return t >= start && t <= end; }
-
-// interventions.py:682-710: is agent i a quarantined tester on day t?
-__device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu_testing& T, int64_t i, int t,
-                                            uint32_t f) {
-  const int qp = T.quar_policy;
-  if (!qp) return false;
-  bool q = false;
-  if (qp & (COVGPU_QP_START | COVGPU_QP_OFFSETS)) {
-    const float dq = date_row(st, COVGPU_DATE_QUARANTINED)[i];
-    if ((qp & COVGPU_QP_START) && dq == (float)(t - 1)) q = true;
-    if ((qp & COVGPU_QP_OFFSETS) && defined(dq)) {
-      const float back = (float)(t - 1) - dq;  // exact: both are small integers when it matters
-      if (back >= 0.0f && back < 32.0f && back == floorf(back) && ((T.quar_offsets >> (int)back) & 1u)) q = true;
-    }
-  }
-  if ((qp & COVGPU_QP_END) && date_row(st, COVGPU_DATE_END_QUARANTINE)[i] == (float)(t + 1)) q = true;
-  if ((qp & COVGPU_QP_DAILY) && (f & B_QUAR)) q = true;
-  return q;
-}
-
-// test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
-// then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
-__global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
-  const covgpu_sim_params& sp = st.sims[blk.sim];
-  const covgpu_testing& T = sp.testing;
-  const bool test_on = day_active(t, T.test_start, T.test_end);
-  const bool trace_on = day_active(t, T.trace_start, T.trace_end);
-  if (!test_on && !trace_on) return;  // uniform over the block (one sim per block)
-  const int64_t i = blk.begin + threadIdx.x;
-  const bool valid = i < blk.end;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t tested = 0, trace = 0;
-  if (valid) {
-    uint32_t f = st.flags[i];
-    float* d_diag = date_row(st, COVGPU_DATE_DIAGNOSED) + i;
-    if (test_on) {
-      uint64_t thr = 0;
-      if (!(f & B_DIAG)) {  // the diagnosed do not test
-        const bool symp = f & B_SYMP;
-        thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
-                                          : (symp ? T.thr_symp : T.thr_asymp);
-      }
-      if (thr) {
-        const uint32_t local = (uint32_t)(i - sp.agent_off);
-        const uint4 w = philox(make_uint4(local, 0u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
-        if (bern52_thr(w.x, w.y, thr)) {
-          tested = 1;
-          st.flags[i] = f | B_TESTED;
-          date_row(st, COVGPU_DATE_TESTED)[i] = (float)t;
-          if ((f & B_INF) && bern52_thr(w.z, w.w, T.thr_sensitivity) && isnan(*d_diag)) {
-            const uint4 w1 = philox(make_uint4(local, 1u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
-            if (bern52_thr(w1.x, w1.y, T.thr_not_lost)) {
-              *d_diag = (float)(t + T.test_delay);
-              date_row(st, COVGPU_DATE_POS_TEST)[i] = (float)t;
-            }
-          }
-        }
-      }
-    }
-    if (trace_on) {
-      if (T.presumptive)
-        trace = (date_row(st, COVGPU_DATE_TESTED)[i] == (float)t && (f & B_EXP)) ? 1u : 0u;
-      else
-        trace = (*d_diag == (float)t) ? 1u : 0u;
-    }
-  }
-  const uint32_t tm = __ballot_sync(0xffffffffu, trace);
-  if (trace_on && lane == 0 && blk.begin + warp * 32 < blk.end) st.trace_bits[(blk.begin + warp * 32) >> 5] = tm;
-  const unsigned n_tested = __reduce_add_sync(0xffffffffu, tested);
-  if (lane == 0 && n_tested)
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
-              (unsigned long long)n_tested);
-  if (lane == 0 && tm) atomicAdd(st.trace_count + blk.sim, (unsigned)__popc(tm));
-}
-
-__device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, int32_t a) {
-  return (__ldg(bits + (a >> 5)) >> (a & 31)) & 1u;
-}
-
-// contact_tracing.identify_contacts, the find_contacts half (utils.py:131-147):
-// every edge with a traced endpoint marks the other endpoint in its layer's bitmap
-template <int ROUNDS>
-__global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
-  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
-  __shared__ int s_seg;
-  if (threadIdx.x == 0) {
-    int lo = 0, hi = st.n_segments - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
-    }
-    s_seg = lo;
-  }
-  __syncthreads();
-  const covgpu_layer* L = st.segments + s_seg;
-  const covgpu_sim_params& sp = st.sims[L->sim];
-  const covgpu_testing& T = sp.testing;
-  if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
-  if (!L->dynamic && L->rp1) return;  // indexed: k_trace_csr visits the traced agents' edges
-  const int64_t words = (st.n + 31) >> 5;
-  uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
-  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
-  const int64_t e1 = min(e0 + TILE, L->n_edges);
-  const int32_t off = (int32_t)sp.agent_off;
-  const uint32_t thr = L->dynamic ? bounded_thr((uint32_t)sp.n_agents) : 0u;
-  for (int r = 0; r < ROUNDS; ++r) {
-    const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
-    if (eb >= e1) break;
-    int32_t a[EDGE_VEC], b[EDGE_VEC];
-    if (L->dynamic) {
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; j += 2)
-        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)L->layer, sp.key0, sp.key1,
-                     (uint32_t)sp.n_agents, thr, off, a[j], b[j], a[j + 1], b[j + 1]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        a[j] = eb + j < e1 ? __ldg(L->p1 + eb + j) : off;
-        b[j] = eb + j < e1 ? __ldg(L->p2 + eb + j) : off;
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) {
-      if (eb + j >= e1) break;
-      if (bit_of(st.trace_bits, a[j])) atomicOr(contact + (b[j] >> 5), 1u << (b[j] & 31));
-      if (bit_of(st.trace_bits, b[j])) atomicOr(contact + (a[j] >> 5), 1u << (a[j] & 31));
-    }
-  }
-}
-
-// find_contacts through the index of each stored layer: a traced agent marks the
-// other endpoint of each of its edges, as p1 and as p2
-__global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
-  const covgpu_sim_params& sp = st.sims[blk.sim];
-  const covgpu_testing& T = sp.testing;
-  if (!day_active(t, T.trace_start, T.trace_end) || st.trace_count[blk.sim] == 0) return;
-  const int64_t i = blk.begin + threadIdx.x;
-  if (i >= blk.end || !((st.trace_bits[i >> 5] >> (i & 31)) & 1u)) return;
-  const int64_t words = (st.n + 31) >> 5;
-  const int64_t local = i - sp.agent_off;
-  for (int l = 0; l < sp.n_layers; ++l) {
-    const int seg = sp.seg_of_layer[l];
-    if (seg < 0 || T.thr_trace[l] == 0) continue;
-    const covgpu_layer& L = st.segments[seg];
-    if (L.dynamic || !L.rp1) continue;
-    uint32_t* contact = st.contact_bits + (int64_t)l * words;
-    for (uint32_t k = L.rp1[local]; k < L.rp1[local + 1]; ++k) {
-      const int32_t b = L.p2[k];
-      atomicOr(contact + (b >> 5), 1u << (b & 31));
-    }
-    for (uint32_t k = L.rp2[local]; k < L.rp2[local + 1]; ++k) {
-      const int32_t a = L.p1[L.perm2[k]];
-      atomicOr(contact + (a >> 5), 1u << (a & 31));
-    }
-  }
-}
-
-// contact_tracing.notify_contacts (interventions.py:1120-1145) with the
-// binomial_filter of identify_contacts, then update_states_post
-// (people.py:189-196: check_diagnosed, check_quar, check_enter_iso)
-__global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
-  const covgpu_sim_params& sp = st.sims[blk.sim];
-  const covgpu_testing& T = sp.testing;
-  const int64_t i = blk.begin + threadIdx.x;
-  const bool valid = i < blk.end;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t words = (st.n + 31) >> 5;
-  const int64_t w = (blk.begin + warp * 32) >> 5;
-  const bool warp_in = blk.begin + warp * 32 < blk.end;
-  const float tf = (float)t;
-  const int R = st.pending_slots;
-  unsigned c_diag = 0, c_quar = 0, c_iso = 0;
-  uint32_t f = valid ? st.flags[i] : 0u;
-  const uint32_t f_in = f;
-
-  // ---- notify the contacts found by the scan (only on tracing days)
-  if (day_active(t, T.trace_start, T.trace_end) && warp_in) {
-    for (int l = 0; l < sp.n_layers; ++l) {
-      uint32_t* cw = st.contact_bits + (int64_t)l * words + w;
-      const uint32_t word = *cw;
-      __syncwarp();
-      if (!word) continue;
-      if (lane == 0) *cw = 0u;  // leave the bitmap clear for the next tracing day
-      if (!valid || !((word >> lane) & 1u)) continue;
-      const uint32_t local = (uint32_t)(i - sp.agent_off);
-      const uint4 u = philox(make_uint4(local, (uint32_t)l, (uint32_t)t, TAG_TRACE), sp.key0, sp.key1);
-      if (!bern52_thr(u.x, u.y, T.thr_trace[l]) || (f & B_DEAD)) continue;
-      f |= B_KCONT;
-      float* dkc = date_row(st, COVGPU_DATE_KNOWN_CONTACT) + i;
-      const float cand = __double2float_rn(__dadd_rn((double)t, T.trace_time[l]));
-      if (isnan(*dkc) || cand < *dkc) *dkc = cand;  // np.fmin
-      const int start = t + T.trace_start_off[l];
-      int32_t* pq = st.pending_quar + (int64_t)(start % R) * st.n + i;
-      const int32_t end = start + T.trace_period[l];
-      if (*pq < 0 || end > *pq) *pq = end;  // check_quar keeps the latest end of a day's requests
-    }
-  }
-
-  if (valid) {
-    // ---- check_diagnosed, people.py:315-332
-    float* dpt = date_row(st, COVGPU_DATE_POS_TEST) + i;
-    const float dd = date_row(st, COVGPU_DATE_DIAGNOSED)[i];
-    if (!(f & B_DIAG)) {
-      if (defined(*dpt) && tf >= *dpt) { *dpt = __int_as_float(0x7fc00000); c_diag = 1; }
-      if (defined(dd) && tf >= dd) f |= B_DIAG;
-    }
-    // ---- check_quar, people.py:335-358
-    int32_t* pq = st.pending_quar + (int64_t)(t % R) * st.n + i;
-    const int32_t end = *pq;
-    float* deq = date_row(st, COVGPU_DATE_END_QUARANTINE) + i;
-    if (end >= 0) {
-      *pq = -1;
-      if (f & B_QUAR) {
-        if ((float)end > *deq) *deq = (float)end;  // max(current, end_day), first argument kept on ties/NaN
-      } else if (!(f & (B_DEAD | B_REC | B_DIAG | B_ISO))) {
-        f |= B_QUAR;
-        date_row(st, COVGPU_DATE_QUARANTINED)[i] = tf;
-        *deq = (float)end;
-        c_quar = 1;
-      }
-    }
-    if ((f & B_QUAR) && dd == tf) *deq = tf;
-    if ((f & B_QUAR) && defined(*deq) && tf >= *deq) f &= ~B_QUAR;
-    // ---- check_enter_iso, people.py:361-366
-    if (dd == tf) {
-      f |= B_ISO;
-      date_row(st, COVGPU_DATE_END_ISOLATION)[i] = date_row(st, COVGPU_DATE_RECOVERED)[i];
-      c_iso = 1;
-    }
-    if (f != f_in) st.flags[i] = f;
-  }
-  const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
-                 ci = __reduce_add_sync(0xffffffffu, c_iso);
-  int64_t* res = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
-  if (lane == 0 && t < sp.npts) {
-    if (cd) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_DIAGNOSES), (unsigned long long)cd);
-    if (cq) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_QUARANTINED), (unsigned long long)cq);
-    if (ci) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_ISOLATED), (unsigned long long)ci);
-  }
-  // the day's trace count is read only by k_trace_scan, which has finished
-  if (threadIdx.x == 0 && blk.begin == sp.agent_off) st.trace_count[blk.sim] = 0u;
-}
-
-int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
-  if (!st->has_testing) return COVGPU_OK;
-  k_test_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
-  if (st->n_tiles > 0) {
-    const dim3 grid((unsigned)st->n_tiles);
-    switch (st->edge_tile) {
-      case 1024: k_trace_scan<1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-      case 2048: k_trace_scan<2><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-      case 8192: k_trace_scan<8><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-      default: k_trace_scan<4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-    }
-  }
-  k_trace_csr<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
-  k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
-  return launch_status();
-}
-
-// ------------------------------------------------------------ contact-tracing index
-__global__ void k_row_ptr(const int32_t* p, int64_t n_edges, int64_t off, int64_t n_local, uint32_t* rp) {
-  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a > n_local) return;
-  const int64_t key = off + a;  // first edge with p >= key
-  int64_t lo = 0, hi = n_edges;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    if ((int64_t)p[mid] < key) lo = mid + 1; else hi = mid;
-  }
-  rp[a] = (uint32_t)lo;
-}
-__global__ void k_rev_count(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* counts) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n_edges) return;
-  const int64_t a = (int64_t)p2[e] - off;
-  if (a >= 0 && a < n_local) atomicAdd(reinterpret_cast<unsigned long long*>(counts + a), 1ull);
-}
-__global__ void k_rev_offsets(const int64_t* offsets, int64_t n, uint32_t* rp2) {
-  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a <= n) rp2[a] = (uint32_t)offsets[a];
-}
-__global__ void k_rev_place(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* cursor,
-                            uint32_t* perm2) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n_edges) return;
-  const int64_t a = (int64_t)p2[e] - off;
-  if (a < 0 || a >= n_local) return;
-  const unsigned long long pos = atomicAdd(reinterpret_cast<unsigned long long*>(cursor + a), 1ull);
-  perm2[pos] = (uint32_t)e;
-}
-
-int grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
-  int64_t b = (n + threads - 1) / threads;
-  if (b < 1) b = 1;
-  if (b > max_blocks) b = max_blocks;
-  return (int)b;
-}
 
 // ------------------------------------------------------------ graph cache for covgpu_run_days
 struct GraphEntry {
@@ -1836,148 +1355,9 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
 
 // ============================================================ C ABI
 
-extern "C" {
+namespace covgpu {
 
-int covgpu_version(void) { return 1; }
-
-int covgpu_abi_layout(int64_t* out, int32_t n) {
-  const int64_t v[] = {(int64_t)sizeof(covgpu_sim_params), (int64_t)sizeof(covgpu_layer),
-                       (int64_t)sizeof(covgpu_agent_block), (int64_t)sizeof(covgpu_event),
-                       (int64_t)sizeof(covgpu_log_rec), (int64_t)sizeof(covgpu_state),
-                       (int64_t)offsetof(covgpu_state, sims), (int64_t)offsetof(covgpu_state, edge_uniforms),
-                       (int64_t)offsetof(covgpu_sim_params, res_fx), (int64_t)sizeof(covgpu_testing),
-                       (int64_t)offsetof(covgpu_sim_params, testing), (int64_t)offsetof(covgpu_state, pending_quar),
-                       (int64_t)offsetof(covgpu_state, trace_count), (int64_t)sizeof(covgpu_lik),
-                       (int64_t)offsetof(covgpu_state, lik)};
-  const int m = (int)(sizeof(v) / sizeof(v[0]));
-  for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
-  return m;
-}
-
-int covgpu_viral_load(int32_t t, const float* date_inf, const float* date_rec, const float* date_dead, int64_t n,
-                      float frac_time, float load_ratio, float high_cap, float* out_load, void* stream) {
-  if (n < 0 || (n > 0 && (!date_inf || !date_rec || !date_dead || !out_load))) return COVGPU_BADARG;
-  if (n == 0) return COVGPU_OK;
-  k_viral_load<<<grid_for(n, 256), 256, 0, S(stream)>>>(t, date_inf, date_rec, date_dead, n, frac_time, load_ratio,
-                                                         high_cap, out_load);
-  return launch_status();
-}
-
-int covgpu_trans_sus(const float* rel_trans, const float* rel_sus, const uint8_t* inf, const uint8_t* sus,
-                     float beta_layer, const float* viral_load, const uint8_t* symp, const uint8_t* iso,
-                     const uint8_t* quar, float asymp_factor, float iso_factor, float quar_factor,
-                     const float* immunity_factors, int64_t n, float* out_rel_trans, float* out_rel_sus,
-                     void* stream) {
-  if (n < 0) return COVGPU_BADARG;
-  if (n == 0) return COVGPU_OK;
-  if (!rel_trans || !rel_sus || !inf || !sus || !viral_load || !symp || !iso || !quar || !immunity_factors ||
-      !out_rel_trans || !out_rel_sus)
-    return COVGPU_BADARG;
-  k_trans_sus<<<grid_for(n, 256), 256, 0, S(stream)>>>(rel_trans, rel_sus, inf, sus, beta_layer, viral_load, symp, iso,
-                                                        quar, asymp_factor, iso_factor, quar_factor, immunity_factors,
-                                                        n, out_rel_trans, out_rel_sus);
-  return launch_status();
-}
-
-int64_t covgpu_infections_scratch_bytes(int64_t n_edges) {
-  if (n_edges < 0) return -1;
-  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
-  const int64_t m = 2 * (ntiles > 0 ? ntiles : 1);
-  return m * (int64_t)sizeof(int64_t) + m * (int64_t)sizeof(int32_t) + 256;
-}
-
-int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas, int64_t n_edges,
-                      const float* rel_trans, const float* rel_sus, int64_t n_agents, const double* uniforms,
-                      uint64_t seed, int32_t day,
-                      int32_t variant, int32_t layer, int32_t* out_src, int32_t* out_tgt, int64_t capacity,
-                      int64_t* out_count, int32_t* status, void* scratch, int64_t scratch_bytes, void* stream) {
-  if (n_edges < 0 || capacity < 0 || n_agents < 0 || !out_count) return COVGPU_BADARG;
-  if (variant < 0 || variant >= COVGPU_MAX_VARIANTS || layer < 0 || layer >= COVGPU_MAX_LAYERS) return COVGPU_BADARG;
-  if (scratch_bytes < covgpu_infections_scratch_bytes(n_edges) || !scratch) return COVGPU_BADARG;
-  cudaStream_t s = S(stream);
-  if (n_edges == 0) {
-    return cudaMemsetAsync(out_count, 0, sizeof(int64_t), s) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
-  }
-  if (!p1 || !p2 || !layer_betas || !rel_trans || !rel_sus || (capacity > 0 && (!out_src || !out_tgt)))
-    return COVGPU_BADARG;
-  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
-  if (ntiles > 0x7FFFFFFF) return COVGPU_BADARG;
-  const int64_t m = 2 * ntiles;
-  int64_t* offs = reinterpret_cast<int64_t*>(scratch);
-  int32_t* counts = reinterpret_cast<int32_t*>(offs + m);
-  InfArgs a;
-  a.beta = beta; a.p1 = p1; a.p2 = p2; a.lb = layer_betas; a.E = n_edges; a.rt = rel_trans; a.rs = rel_sus;
-  a.n_agents = n_agents; a.status = status; a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32); a.day = day; a.variant = variant;
-  a.layer = layer;
-  dim3 grid((unsigned)ntiles, 2);
-  k_infections_count<<<grid, INF_THREADS, 0, s>>>(a, ntiles, counts);
-  k_scan<<<1, 1024, 0, s>>>(counts, m, offs, out_count, capacity, status);
-  k_infections_write<<<grid, INF_THREADS, 0, s>>>(a, ntiles, offs, out_src, out_tgt, capacity);
-  return launch_status();
-}
-
-// ---- compute_infections without allocation: scratch in a file-scope device array
-//
-// For callers that may not allocate device memory at all (see the declaration in
-// covgpu.h). The tile counts and offsets that covgpu_infections keeps in caller
-// scratch live here instead; every call rewrites all of the part it reads, so
-// nothing needs clearing between calls, and calls whose kernels overlap on the
-// GPU race on it.
-constexpr int64_t NOALLOC_MAX_EDGES = COVGPU_NOALLOC_MAX_EDGES;
-constexpr int64_t NOALLOC_TILES = (NOALLOC_MAX_EDGES + INF_TILE - 1) / INF_TILE;
-constexpr int64_t NOALLOC_SCRATCH = 2 * NOALLOC_TILES * (int64_t)(sizeof(int64_t) + sizeof(int32_t));
-static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH];
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of g_noalloc_scratch, per device
-
-// The array's host-side name is not a device address: look the address up once
-// per device, with that device current.
-static int noalloc_scratch(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return COVGPU_CUDA_ERROR;
-  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return COVGPU_BADARG;
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return COVGPU_CUDA_ERROR;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
-  return COVGPU_OK;
-}
-
-int covgpu_infections_noalloc(float beta, const int32_t* p1, const int32_t* p2, const float* layer_betas,
-                              int64_t n_edges, const float* rel_trans, const float* rel_sus, int64_t n_agents,
-                              const double* uniforms, uint64_t seed, int32_t day, int32_t variant, int32_t layer,
-                              int32_t* out_src, int32_t* out_tgt, int64_t capacity, int64_t* out_count,
-                              int32_t* status, void* stream) {
-  if (n_edges < 0 || n_edges > NOALLOC_MAX_EDGES) return COVGPU_BADARG;
-  if (capacity < 0 || n_agents < 0 || !out_count) return COVGPU_BADARG;
-  if (variant < 0 || variant >= COVGPU_MAX_VARIANTS || layer < 0 || layer >= COVGPU_MAX_LAYERS) return COVGPU_BADARG;
-  cudaStream_t s = S(stream);
-  if (n_edges == 0) {
-    return cudaMemsetAsync(out_count, 0, sizeof(int64_t), s) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
-  }
-  if (!p1 || !p2 || !layer_betas || !rel_trans || !rel_sus || (capacity > 0 && (!out_src || !out_tgt)))
-    return COVGPU_BADARG;
-  void* scratch = nullptr;
-  const int rc = noalloc_scratch(&scratch);
-  if (rc != COVGPU_OK) return rc;
-  const int64_t ntiles = (n_edges + INF_TILE - 1) / INF_TILE;
-  const int64_t m = 2 * ntiles;
-  int64_t* offs = reinterpret_cast<int64_t*>(scratch);
-  int32_t* counts = reinterpret_cast<int32_t*>(offs + m);
-  InfArgs a;
-  a.beta = beta; a.p1 = p1; a.p2 = p2; a.lb = layer_betas; a.E = n_edges; a.rt = rel_trans; a.rs = rel_sus;
-  a.n_agents = n_agents; a.status = status; a.uni = uniforms; a.k0 = (uint32_t)seed; a.k1 = (uint32_t)(seed >> 32);
-  a.day = day; a.variant = variant; a.layer = layer;
-  dim3 grid((unsigned)ntiles, 2);
-  k_infections_count<<<grid, INF_THREADS, 0, s>>>(a, ntiles, counts);
-  k_scan<<<1, 1024, 0, s>>>(counts, m, offs, out_count, capacity, status);
-  k_infections_write<<<grid, INF_THREADS, 0, s>>>(a, ntiles, offs, out_src, out_tgt, capacity);
-  return launch_status();
-}
-
-static int check_state(const covgpu_state* st) {
+int check_state(const covgpu_state* st) {
   if (!st || st->n <= 0 || st->n_sims <= 0 || st->n_agent_blocks <= 0) return COVGPU_BADARG;
   if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->src_rec ||
       !st->events ||
@@ -1998,6 +1378,28 @@ static int check_state(const covgpu_state* st) {
     return COVGPU_BADARG;
   return COVGPU_OK;
 }
+
+}  // namespace covgpu
+
+
+extern "C" {
+
+int covgpu_version(void) { return 1; }
+
+int covgpu_abi_layout(int64_t* out, int32_t n) {
+  const int64_t v[] = {(int64_t)sizeof(covgpu_sim_params), (int64_t)sizeof(covgpu_layer),
+                       (int64_t)sizeof(covgpu_agent_block), (int64_t)sizeof(covgpu_event),
+                       (int64_t)sizeof(covgpu_log_rec), (int64_t)sizeof(covgpu_state),
+                       (int64_t)offsetof(covgpu_state, sims), (int64_t)offsetof(covgpu_state, edge_uniforms),
+                       (int64_t)offsetof(covgpu_sim_params, res_fx), (int64_t)sizeof(covgpu_testing),
+                       (int64_t)offsetof(covgpu_sim_params, testing), (int64_t)offsetof(covgpu_state, pending_quar),
+                       (int64_t)offsetof(covgpu_state, trace_count), (int64_t)sizeof(covgpu_lik),
+                       (int64_t)offsetof(covgpu_state, lik)};
+  const int m = (int)(sizeof(v) / sizeof(v[0]));
+  for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
+  return m;
+}
+
 
 int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_t do_day, void* stream) {
   int rc = check_state(st);
@@ -2021,36 +1423,6 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   rc = configure_edge_pass(st);
   if (rc) return rc;
   return launch_edge_pass(st, t, S(stream));
-}
-
-int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream) {
-  int rc = check_state(st);
-  if (rc) return rc;
-  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  return launch_test_trace(st, t, S(stream));
-}
-
-int64_t covgpu_trace_index_scratch(int64_t n_local) {
-  return 2 * (n_local + 1) + (int64_t)scan_blocks_for(n_local, SCAN_TILE) + 1;
-}
-
-int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, int64_t agent_off, int64_t n_local,
-                       uint32_t* rp1, uint32_t* rp2, uint32_t* perm2, int64_t* scratch, void* stream) {
-  if (n_edges < 1 || n_edges > 0xFFFFFFFFLL || n_local < 1 || agent_off < 0 || !p1 || !p2 || !rp1 || !rp2 ||
-      !perm2 || !scratch)
-    return COVGPU_BADARG;
-  cudaStream_t s = S(stream);
-  int64_t* counts = scratch;
-  int64_t* offsets = scratch + (n_local + 1);
-  int64_t* tiles = scratch + 2 * (n_local + 1);
-  k_row_ptr<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(p1, n_edges, agent_off, n_local, rp1);
-  if (cudaMemsetAsync(counts, 0, sizeof(int64_t) * (size_t)n_local, s) != cudaSuccess) return COVGPU_CUDA_ERROR;
-  k_rev_count<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, counts);
-  int rc = scan_i64(counts, offsets, n_local, tiles, s);
-  if (rc) return rc;
-  k_rev_offsets<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(offsets, n_local, rp2);
-  k_rev_place<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, offsets, perm2);
-  return launch_status();
 }
 
 int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream) {

@@ -1,0 +1,359 @@
+// covgpu_testing: test_prob, contact_tracing and update_states_post on the device
+// (covasim/interventions.py:858-1145, covasim/people.py:189-196,315-366,589-640),
+// and the agent index of stored layers that tracing walks.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <math.h>
+#include "covgpu.h"
+#include "covgpu_device.cuh"
+#include "covgpu_ff.cuh"
+#include "covgpu_scan.cuh"
+#include "covgpu_launch.cuh"
+
+using namespace covgpu;
+
+namespace {
+
+// ============================================================ testing and tracing
+//
+// Day t with a test_prob / contact_tracing sim, after the agent pass and any
+// importations (sim.py:596-600): k_test_pass draws who tests and marks the
+// agents to trace, k_trace_scan marks their contacts layer by layer, and
+// k_post_pass notifies the contacts and runs update_states_post.
+
+__device__ __forceinline__ bool day_active(int t, int start, int end) { return t >= start && t <= end; }
+
+// interventions.py:682-710: is agent i a quarantined tester on day t?
+__device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu_testing& T, int64_t i, int t,
+                                            uint32_t f) {
+  const int qp = T.quar_policy;
+  if (!qp) return false;
+  bool q = false;
+  if (qp & (COVGPU_QP_START | COVGPU_QP_OFFSETS)) {
+    const float dq = date_row(st, COVGPU_DATE_QUARANTINED)[i];
+    if ((qp & COVGPU_QP_START) && dq == (float)(t - 1)) q = true;
+    if ((qp & COVGPU_QP_OFFSETS) && defined(dq)) {
+      const float back = (float)(t - 1) - dq;  // exact: both are small integers when it matters
+      if (back >= 0.0f && back < 32.0f && back == floorf(back) && ((T.quar_offsets >> (int)back) & 1u)) q = true;
+    }
+  }
+  if ((qp & COVGPU_QP_END) && date_row(st, COVGPU_DATE_END_QUARANTINE)[i] == (float)(t + 1)) q = true;
+  if ((qp & COVGPU_QP_DAILY) && (f & B_QUAR)) q = true;
+  return q;
+}
+
+// test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
+// then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
+__global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  const bool test_on = day_active(t, T.test_start, T.test_end);
+  const bool trace_on = day_active(t, T.trace_start, T.trace_end);
+  if (!test_on && !trace_on) return;  // uniform over the block (one sim per block)
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t tested = 0, trace = 0;
+  if (valid) {
+    uint32_t f = st.flags[i];
+    float* d_diag = date_row(st, COVGPU_DATE_DIAGNOSED) + i;
+    if (test_on) {
+      uint64_t thr = 0;
+      if (!(f & B_DIAG)) {  // the diagnosed do not test
+        const bool symp = f & B_SYMP;
+        thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
+                                          : (symp ? T.thr_symp : T.thr_asymp);
+      }
+      if (thr) {
+        const uint32_t local = (uint32_t)(i - sp.agent_off);
+        const uint4 w = philox(make_uint4(local, 0u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
+        if (bern52_thr(w.x, w.y, thr)) {
+          tested = 1;
+          st.flags[i] = f | B_TESTED;
+          date_row(st, COVGPU_DATE_TESTED)[i] = (float)t;
+          if ((f & B_INF) && bern52_thr(w.z, w.w, T.thr_sensitivity) && isnan(*d_diag)) {
+            const uint4 w1 = philox(make_uint4(local, 1u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
+            if (bern52_thr(w1.x, w1.y, T.thr_not_lost)) {
+              *d_diag = (float)(t + T.test_delay);
+              date_row(st, COVGPU_DATE_POS_TEST)[i] = (float)t;
+            }
+          }
+        }
+      }
+    }
+    if (trace_on) {
+      if (T.presumptive)
+        trace = (date_row(st, COVGPU_DATE_TESTED)[i] == (float)t && (f & B_EXP)) ? 1u : 0u;
+      else
+        trace = (*d_diag == (float)t) ? 1u : 0u;
+    }
+  }
+  const uint32_t tm = __ballot_sync(0xffffffffu, trace);
+  if (trace_on && lane == 0 && blk.begin + warp * 32 < blk.end) st.trace_bits[(blk.begin + warp * 32) >> 5] = tm;
+  const unsigned n_tested = __reduce_add_sync(0xffffffffu, tested);
+  if (lane == 0 && n_tested)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
+              (unsigned long long)n_tested);
+  if (lane == 0 && tm) atomicAdd(st.trace_count + blk.sim, (unsigned)__popc(tm));
+}
+
+__device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, int32_t a) {
+  return (__ldg(bits + (a >> 5)) >> (a & 31)) & 1u;
+}
+
+// contact_tracing.identify_contacts, the find_contacts half (utils.py:131-147):
+// every edge with a traced endpoint marks the other endpoint in its layer's bitmap
+template <int ROUNDS>
+__global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
+  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
+  __shared__ int s_seg;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = st.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (st.segments[mid].tile_begin <= (int64_t)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    s_seg = lo;
+  }
+  __syncthreads();
+  const covgpu_layer* L = st.segments + s_seg;
+  const covgpu_sim_params& sp = st.sims[L->sim];
+  const covgpu_testing& T = sp.testing;
+  if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
+  if (!L->dynamic && L->rp1) return;  // indexed: k_trace_csr visits the traced agents' edges
+  const int64_t words = (st.n + 31) >> 5;
+  uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
+  const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
+  const int64_t e1 = min(e0 + TILE, L->n_edges);
+  const int32_t off = (int32_t)sp.agent_off;
+  const uint32_t thr = L->dynamic ? bounded_thr((uint32_t)sp.n_agents) : 0u;
+  for (int r = 0; r < ROUNDS; ++r) {
+    const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
+    if (eb >= e1) break;
+    int32_t a[EDGE_VEC], b[EDGE_VEC];
+    if (L->dynamic) {
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; j += 2)
+        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)L->layer, sp.key0, sp.key1,
+                     (uint32_t)sp.n_agents, thr, off, a[j], b[j], a[j + 1], b[j + 1]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < EDGE_VEC; ++j) {
+        a[j] = eb + j < e1 ? __ldg(L->p1 + eb + j) : off;
+        b[j] = eb + j < e1 ? __ldg(L->p2 + eb + j) : off;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < EDGE_VEC; ++j) {
+      if (eb + j >= e1) break;
+      if (bit_of(st.trace_bits, a[j])) atomicOr(contact + (b[j] >> 5), 1u << (b[j] & 31));
+      if (bit_of(st.trace_bits, b[j])) atomicOr(contact + (a[j] >> 5), 1u << (a[j] & 31));
+    }
+  }
+}
+
+// find_contacts through the index of each stored layer: a traced agent marks the
+// other endpoint of each of its edges, as p1 and as p2
+__global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  if (!day_active(t, T.trace_start, T.trace_end) || st.trace_count[blk.sim] == 0) return;
+  const int64_t i = blk.begin + threadIdx.x;
+  if (i >= blk.end || !((st.trace_bits[i >> 5] >> (i & 31)) & 1u)) return;
+  const int64_t words = (st.n + 31) >> 5;
+  const int64_t local = i - sp.agent_off;
+  for (int l = 0; l < sp.n_layers; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg < 0 || T.thr_trace[l] == 0) continue;
+    const covgpu_layer& L = st.segments[seg];
+    if (L.dynamic || !L.rp1) continue;
+    uint32_t* contact = st.contact_bits + (int64_t)l * words;
+    for (uint32_t k = L.rp1[local]; k < L.rp1[local + 1]; ++k) {
+      const int32_t b = L.p2[k];
+      atomicOr(contact + (b >> 5), 1u << (b & 31));
+    }
+    for (uint32_t k = L.rp2[local]; k < L.rp2[local + 1]; ++k) {
+      const int32_t a = L.p1[L.perm2[k]];
+      atomicOr(contact + (a >> 5), 1u << (a & 31));
+    }
+  }
+}
+
+// contact_tracing.notify_contacts (interventions.py:1120-1145) with the
+// binomial_filter of identify_contacts, then update_states_post
+// (people.py:189-196: check_diagnosed, check_quar, check_enter_iso)
+__global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
+  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  const int64_t i = blk.begin + threadIdx.x;
+  const bool valid = i < blk.end;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t words = (st.n + 31) >> 5;
+  const int64_t w = (blk.begin + warp * 32) >> 5;
+  const bool warp_in = blk.begin + warp * 32 < blk.end;
+  const float tf = (float)t;
+  const int R = st.pending_slots;
+  unsigned c_diag = 0, c_quar = 0, c_iso = 0;
+  uint32_t f = valid ? st.flags[i] : 0u;
+  const uint32_t f_in = f;
+
+  // ---- notify the contacts found by the scan (only on tracing days)
+  if (day_active(t, T.trace_start, T.trace_end) && warp_in) {
+    for (int l = 0; l < sp.n_layers; ++l) {
+      uint32_t* cw = st.contact_bits + (int64_t)l * words + w;
+      const uint32_t word = *cw;
+      __syncwarp();
+      if (!word) continue;
+      if (lane == 0) *cw = 0u;  // leave the bitmap clear for the next tracing day
+      if (!valid || !((word >> lane) & 1u)) continue;
+      const uint32_t local = (uint32_t)(i - sp.agent_off);
+      const uint4 u = philox(make_uint4(local, (uint32_t)l, (uint32_t)t, TAG_TRACE), sp.key0, sp.key1);
+      if (!bern52_thr(u.x, u.y, T.thr_trace[l]) || (f & B_DEAD)) continue;
+      f |= B_KCONT;
+      float* dkc = date_row(st, COVGPU_DATE_KNOWN_CONTACT) + i;
+      const float cand = __double2float_rn(__dadd_rn((double)t, T.trace_time[l]));
+      if (isnan(*dkc) || cand < *dkc) *dkc = cand;  // np.fmin
+      const int start = t + T.trace_start_off[l];
+      int32_t* pq = st.pending_quar + (int64_t)(start % R) * st.n + i;
+      const int32_t end = start + T.trace_period[l];
+      if (*pq < 0 || end > *pq) *pq = end;  // check_quar keeps the latest end of a day's requests
+    }
+  }
+
+  if (valid) {
+    // ---- check_diagnosed, people.py:315-332
+    float* dpt = date_row(st, COVGPU_DATE_POS_TEST) + i;
+    const float dd = date_row(st, COVGPU_DATE_DIAGNOSED)[i];
+    if (!(f & B_DIAG)) {
+      if (defined(*dpt) && tf >= *dpt) { *dpt = __int_as_float(0x7fc00000); c_diag = 1; }
+      if (defined(dd) && tf >= dd) f |= B_DIAG;
+    }
+    // ---- check_quar, people.py:335-358
+    int32_t* pq = st.pending_quar + (int64_t)(t % R) * st.n + i;
+    const int32_t end = *pq;
+    float* deq = date_row(st, COVGPU_DATE_END_QUARANTINE) + i;
+    if (end >= 0) {
+      *pq = -1;
+      if (f & B_QUAR) {
+        if ((float)end > *deq) *deq = (float)end;  // max(current, end_day), first argument kept on ties/NaN
+      } else if (!(f & (B_DEAD | B_REC | B_DIAG | B_ISO))) {
+        f |= B_QUAR;
+        date_row(st, COVGPU_DATE_QUARANTINED)[i] = tf;
+        *deq = (float)end;
+        c_quar = 1;
+      }
+    }
+    if ((f & B_QUAR) && dd == tf) *deq = tf;
+    if ((f & B_QUAR) && defined(*deq) && tf >= *deq) f &= ~B_QUAR;
+    // ---- check_enter_iso, people.py:361-366
+    if (dd == tf) {
+      f |= B_ISO;
+      date_row(st, COVGPU_DATE_END_ISOLATION)[i] = date_row(st, COVGPU_DATE_RECOVERED)[i];
+      c_iso = 1;
+    }
+    if (f != f_in) st.flags[i] = f;
+  }
+  const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
+                 ci = __reduce_add_sync(0xffffffffu, c_iso);
+  int64_t* res = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
+  if (lane == 0 && t < sp.npts) {
+    if (cd) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_DIAGNOSES), (unsigned long long)cd);
+    if (cq) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_QUARANTINED), (unsigned long long)cq);
+    if (ci) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_ISOLATED), (unsigned long long)ci);
+  }
+  // the day's trace count is read only by k_trace_scan, which has finished
+  if (threadIdx.x == 0 && blk.begin == sp.agent_off) st.trace_count[blk.sim] = 0u;
+}
+
+// ------------------------------------------------------------ contact-tracing index
+__global__ void k_row_ptr(const int32_t* p, int64_t n_edges, int64_t off, int64_t n_local, uint32_t* rp) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a > n_local) return;
+  const int64_t key = off + a;  // first edge with p >= key
+  int64_t lo = 0, hi = n_edges;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if ((int64_t)p[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  rp[a] = (uint32_t)lo;
+}
+__global__ void k_rev_count(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* counts) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  const int64_t a = (int64_t)p2[e] - off;
+  if (a >= 0 && a < n_local) atomicAdd(reinterpret_cast<unsigned long long*>(counts + a), 1ull);
+}
+__global__ void k_rev_offsets(const int64_t* offsets, int64_t n, uint32_t* rp2) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a <= n) rp2[a] = (uint32_t)offsets[a];
+}
+__global__ void k_rev_place(const int32_t* p2, int64_t n_edges, int64_t off, int64_t n_local, int64_t* cursor,
+                            uint32_t* perm2) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  const int64_t a = (int64_t)p2[e] - off;
+  if (a < 0 || a >= n_local) return;
+  const unsigned long long pos = atomicAdd(reinterpret_cast<unsigned long long*>(cursor + a), 1ull);
+  perm2[pos] = (uint32_t)e;
+}
+
+}  // namespace
+
+namespace covgpu {
+
+int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
+  if (!st->has_testing) return COVGPU_OK;
+  k_test_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  if (st->n_tiles > 0) {
+    const dim3 grid((unsigned)st->n_tiles);
+    switch (st->edge_tile) {
+      case 1024: k_trace_scan<1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      case 2048: k_trace_scan<2><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      case 8192: k_trace_scan<8><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+      default: k_trace_scan<4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    }
+  }
+  k_trace_csr<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  return launch_status();
+}
+
+}  // namespace covgpu
+
+extern "C" {
+
+int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  return launch_test_trace(st, t, S(stream));
+}
+
+int64_t covgpu_trace_index_scratch(int64_t n_local) {
+  return 2 * (n_local + 1) + (int64_t)scan_blocks_for(n_local, SCAN_TILE) + 1;
+}
+
+int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, int64_t agent_off, int64_t n_local,
+                       uint32_t* rp1, uint32_t* rp2, uint32_t* perm2, int64_t* scratch, void* stream) {
+  if (n_edges < 1 || n_edges > 0xFFFFFFFFLL || n_local < 1 || agent_off < 0 || !p1 || !p2 || !rp1 || !rp2 ||
+      !perm2 || !scratch)
+    return COVGPU_BADARG;
+  cudaStream_t s = S(stream);
+  int64_t* counts = scratch;
+  int64_t* offsets = scratch + (n_local + 1);
+  int64_t* tiles = scratch + 2 * (n_local + 1);
+  k_row_ptr<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(p1, n_edges, agent_off, n_local, rp1);
+  if (cudaMemsetAsync(counts, 0, sizeof(int64_t) * (size_t)n_local, s) != cudaSuccess) return COVGPU_CUDA_ERROR;
+  k_rev_count<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, counts);
+  int rc = scan_i64(counts, offsets, n_local, tiles, s);
+  if (rc) return rc;
+  k_rev_offsets<<<grid_for(n_local + 1, 256, 1 << 30), 256, 0, s>>>(offsets, n_local, rp2);
+  k_rev_place<<<grid_for(n_edges, 256, 1 << 30), 256, 0, s>>>(p2, n_edges, agent_off, n_local, offsets, perm2);
+  return launch_status();
+}
+
+}  // extern "C"
