@@ -13,8 +13,10 @@ package's generators (same distributions as the reference's). Inputs
                host population is uploaded by cv.Sim(...).initialize(), run,
                and the results copied back (finalize)
   roofline     the dominant kernel, from per-kernel CUDA-event timing of one
-               extra ungraphed run; algorithmic bytes per launch are counted
-               from the day's state counts
+               extra ungraphed run; algorithmic bytes per launch: 28 B per
+               undirected edge per day for the edge pass (p1, p2, beta streamed,
+               rel_trans and rel_sus of both endpoints gathered), 76 + 12 nv B
+               per agent per day for the agent pass
   cpu_baseline the CPU oracle (numpy restatement) on a bounded sample of the
                same workload: a few days of the 1M hybrid sim
 
@@ -38,8 +40,8 @@ sys.path.insert(0, ROOT)
 POP = 1_000_000
 DAYS = 180
 PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
-# DRAM bytes (read + write) of one launch, from an ncu capture of that launch
-# on this workload (profiles/k_edge_pass_hybrid1M_dram.md: day 90 of the 1M run)
+# DRAM bytes (read + write) of one edge-pass launch on this workload, from an
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of day 90 of the 1M run
 MEASURED_TRAFFIC = {('edge_pass', 1_000_000): 90_250_240}
 
 
