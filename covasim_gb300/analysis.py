@@ -782,8 +782,6 @@ class Calibration(Analyzer):
             if self.die:
                 raise
             return [self.run_sim(p) for p in par_sets]
-        if any(s['variants'] for s in sims):  # not batched: one sim at a time
-            return [self.run_sim(p) for p in par_sets]
         try:
             BatchSim(sims).run().finalize()
             out = []

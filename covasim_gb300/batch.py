@@ -17,7 +17,7 @@ from . import parameters as cvpar
 from . import immunity as cvimm
 from . import defaults as cvd
 from . import _lib as L
-from .sim import Sim, build_spec, choose_seed_infections, CALL_SEED
+from .sim import Sim, build_spec, choose_seed_infections, CALL_SEED, CALL_IMPORT
 from .state import BatchState
 
 __all__ = ['BatchSim']
@@ -51,8 +51,6 @@ class BatchSim:
         specs = []
         self.npts = None
         for s in self.sims:
-            if s['variants']:
-                raise NotImplementedError('variants with importations are not batched yet; run them as single sims')
             s.validate_pars()
             s.init_variants()
             if s['prognoses'] is None:
@@ -78,12 +76,38 @@ class BatchSim:
                 inds = choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected'])
                 self.state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
 
+    def _import_variants(self, t):
+        """Each sim's variant importations of day t, with the sim's own draws
+        (immunity.py:117-130, as Sim does them)."""
+        for k, s in enumerate(self.sims):
+            for v in s['variants']:
+                if t in np.atleast_1d(v.days):
+                    sus = np.nonzero(self.state.get('susceptible', k).cpu().numpy())[0]
+                    rng = np.random.default_rng([int(s['rand_seed']), 0x1A1A, t, v.index])
+                    inds = rng.choice(sus, min(v.n_imports, len(sus)), replace=False)
+                    self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.MAX_LAYERS + 1,
+                                           call_tag=CALL_IMPORT + v.index)
+
     def run(self, use_graph=None):
         if self.state is None:
             self.initialize()
         use_graph = self.use_graph if use_graph is None else use_graph
         self.seed_infections()
-        self.state.run_days(0, self.npts, open_prev=False, close_last=True, use_graph=use_graph)
+        # the days with importations (any sim's) run as single steps, the rest as graphs
+        host_days = sorted({d for s in self.sims for d in s._variant_days() if 0 <= d < self.npts})
+        st, t = self.state, 0
+        for d in host_days + [self.npts]:
+            if d > t:
+                st.run_days(t, d, open_prev=False, close_last=True, use_graph=use_graph)
+                t = d
+            if t < self.npts:
+                st.agent_step(t, do_prev=False, do_day=True)
+                self._import_variants(t)
+                st.test_trace(t)
+                st.edge_pass(t)
+                st.infect_claims(t)
+                st.agent_step(t + 1, do_prev=True, do_day=False)
+                t += 1
         status = self.state.status()
         if status:
             raise L.CovgpuError('device status', status)

@@ -60,3 +60,20 @@ def test_batch_with_sims_of_different_sizes_including_tiny_ones():
     for k, s in enumerate(sims):
         solo = cv.Sim(dict(s.pars)).run().raw_results()['new_infections']
         np.testing.assert_array_equal(batch.results(k)['new_infections'], solo)
+
+
+def test_batch_with_variant_importations_equals_single_runs():
+    def make(k):
+        vs = [cv.variant(dict(rel_beta=1.5), days=10 + 5 * k, n_imports=5, label='v1')]
+        if k == 1:
+            vs.append(cv.variant(dict(rel_beta=1.8), days=[20, 21], n_imports=3, label='v2'))
+        return cv.Sim(pop_type='hybrid', pop_size=3000, n_days=40, rand_seed=7 + k, use_waning=True,
+                      variants=vs, dynam_layer=dict(h=0, s=0, w=0, c=1))
+    sims = [make(k) for k in range(3)] + [cv.Sim(pop_type='hybrid', pop_size=2000, n_days=40, rand_seed=3)]
+    batch = cv.BatchSim(sims).run()
+    for k in range(len(sims)):
+        solo = (make(k) if k < 3 else cv.Sim(pop_type='hybrid', pop_size=2000, n_days=40, rand_seed=3)).run()
+        ref = solo.raw_results()
+        got = batch.results(k)
+        for key in ('new_infections', 'new_infections_by_variant', 'n_exposed', 'new_deaths'):
+            np.testing.assert_array_equal(got[key], ref[key], err_msg=f'sim {k} {key}')
