@@ -60,6 +60,8 @@ def parse():
     ap.add_argument('--no-adjoint', action='store_true', help='skip the forward/adjoint cost measurement')
     ap.add_argument('--edge-tile', default='auto',
                     help="edge-pass tile (1024/2048/4096/8192, suffix 'r' for the resident bitmap) or 'auto' (autotuner)")
+    ap.add_argument('--seeds', type=int, default=1,
+                    help='large workload: this many seeds of the 20M-agent sim in one BatchSim')
     ap.add_argument('--gpu-population', action='store_true',
                     help='large / batch256 workloads: build the populations on the device')
     ap.add_argument('--workload', default='hybrid1m', choices=['hybrid1m', 'large', 'batch256'],
@@ -544,16 +546,26 @@ def large_arm(args, n=20_000_000, days=365):
                           cv.variant(dict(rel_beta=1.7), days=120, n_imports=100, label='v1.7')],
                 interventions=[cv.test_prob(symp_prob=0.1), cv.contact_tracing(trace_probs=0.5)])
     t0 = time.perf_counter()
-    sim = cv.Sim(pars, edge_tile=None if args.edge_tile == 'auto' else args.edge_tile,
-                 gpu_population=args.gpu_population)
-    sim.initialize()
+    tile = None if args.edge_tile == 'auto' else args.edge_tile
+    seeds = max(1, args.seeds)
+    if seeds == 1:
+        sim = cv.Sim(pars, edge_tile=tile, gpu_population=args.gpu_population)
+        sim.initialize()
+        st = sim.state
+    else:  # the batched form: several seeds in one BatchSim
+        sims = [cv.Sim(dict(pars, rand_seed=1 + k), gpu_population=args.gpu_population) for k in range(seeds)]
+        batch = cv.BatchSim(sims, edge_tile=tile).initialize()
+        sim, st = sims[0], batch.state
     init_s = time.perf_counter() - t0
-    st = sim.state
     snap = st.snapshot()
 
     def one_run():
-        sim.rewind(snap)
-        sim.run()
+        if seeds == 1:
+            sim.rewind(snap)
+            sim.run()
+        else:
+            st.restore(snap)
+            batch.run()
 
     for _ in range(args.warmup):
         one_run()
@@ -570,10 +582,11 @@ def large_arm(args, n=20_000_000, days=365):
     el = ev0.elapsed_time(ev1) / 1e3
     res = st.results(0)
     e_all = sum(len(ly['p1']) for ly in sim.spec.layers)
-    _line(n * days * args.steps / el, 'agent-days/s', args, 1e3 * el / args.steps,
-          f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), waning, test_prob(symp_prob=0.1), '
-          f'contact_tracing(trace_probs=0.5), {days} days',
-          {'edge_evaluations_per_s': round(2 * e_all * days * args.steps / el, 1), 'init_s': round(init_s, 1),
+    _line(seeds * n * days * args.steps / el, 'agent-days/s', args, 1e3 * el / args.steps,
+          f'{seeds} x ' * (seeds > 1) + f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), waning, '
+          f'test_prob(symp_prob=0.1), contact_tracing(trace_probs=0.5), {days} days',
+          {'edge_evaluations_per_s': round(seeds * 2 * e_all * days * args.steps / el, 1), 'init_s': round(init_s, 1),
+           'seeds': seeds,
            'population': 'device' if args.gpu_population else 'host',
            'cum_infections': float(res['new_infections'].sum() + sim['pop_infected']),
            'cum_tests': float(res['new_tests'].sum()), 'cum_quarantined': float(res['new_quarantined'].sum()),
