@@ -255,7 +255,7 @@ def gpu_arm(args, world, rank):
 
     def one_run():
         st.restore(snap)
-        st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
         st.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
 
     for _ in range(args.warmup):
@@ -285,7 +285,7 @@ def gpu_arm(args, world, rank):
 
     # per-kernel timing (one extra ungraphed run) for the roofline
     st.restore(snap)
-    st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+    st.infect_list(0, seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
     kt = kernel_profile(sim, npts)
     res = st.results(0)
     totals = {k: float(np.sum(v)) for k, v in kt.items()}
@@ -384,7 +384,7 @@ def adjoint_arm(args, n=100_000, days=120, every=10, reps=3):
         st = run.state
         st.disable_lik()
         st.restore(run.initial)
-        st.infect_list(0, run.seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.infect_list(0, run.seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
         st.run_days(0, run.npts, open_prev=False, close_last=True, use_graph=True)
         torch.cuda.synchronize()
 
@@ -427,7 +427,7 @@ def batched_arm(args, sim, plain_value, world):
     def one_run():
         st.restore(snap)
         for k in range(B):
-            st.infect_list(0, seeds[k], sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+            st.infect_list(0, seeds[k], sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
         st.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
 
     for _ in range(args.warmup):

@@ -10,6 +10,10 @@ from . import build as _build
 
 MAX_VARIANTS = 8
 MAX_LAYERS = 16
+# infection-log layer tags beyond the contact layers (people.py:508-511 records the
+# infect() call's ``layer``): seed infections, importations, layer=None, then any
+# other label passed to People.infect (registered per batch)
+LOG_SEED, LOG_IMPORT, LOG_NONE, LOG_EXTRA = MAX_LAYERS, MAX_LAYERS + 1, MAX_LAYERS + 2, MAX_LAYERS + 3
 N_DATES = 19
 N_DURS = 5
 N_DRAWS = 10
@@ -128,6 +132,8 @@ class State(C.Structure):
         ('contact_bits', C.c_void_p), ('n_contact_layers', C.c_int32), ('_pad1', C.c_int32),
         ('pending_quar', C.c_void_p), ('trace_count', C.c_void_p),
         ('lik', Lik),
+        ('import_day_off', C.c_void_p), ('imports', C.c_void_p), ('import_sims', C.c_void_p),
+        ('import_days', C.c_int32), ('_pad3', C.c_int32),
     ]
 
 
@@ -162,6 +168,7 @@ def lib():
         L.covgpu_test_trace.argtypes = [sp, i32, vp]
         L.covgpu_lik_targets.argtypes = [sp, i32, vp]
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
+        L.covgpu_import_day.argtypes = [sp, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
         L.covgpu_edge_resident_bytes.argtypes = [sp]
@@ -210,7 +217,7 @@ def abi_layout():
     mine = [C.sizeof(SimParams), C.sizeof(Layer), C.sizeof(AgentBlock), 16, 16, C.sizeof(State),
             State.sims.offset, State.edge_uniforms.offset, SimParams.res_fx.offset, C.sizeof(Testing),
             SimParams.testing.offset, State.pending_quar.offset, State.trace_count.offset, C.sizeof(Lik),
-            State.lik.offset]
+            State.lik.offset, State.import_day_off.offset]
     return list(out[:m]), mine
 
 
@@ -219,6 +226,6 @@ POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts'
 
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
-            'covgpu_infect_list', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
+            'covgpu_infect_list', 'covgpu_import_day', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
             'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index', 'covgpu_edge_resident_bytes',
             'covgpu_pop_scan_scratch'] + POP_FUNCS

@@ -171,7 +171,7 @@ class LikelihoodRun:
         st.set_lik_factor(self.params.factor(theta))
         st.zero_lik()
         st.restore(self.initial)
-        st.infect_list(0, self.seeds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        st.infect_list(0, self.seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
         self.checkpoints = []
         for t0, t1 in self._segments():
             self.checkpoints.append(st.checkpoint())

@@ -35,6 +35,8 @@ import warnings
 import numpy as np
 import torch
 
+from .people import log_layer_label
+
 __all__ = ['Analyzer', 'DataTable', 'load_data', 'compute_gof', 'Fit', 'TransTree', 'Calibration',
            'to_date', 'to_day']
 
@@ -476,6 +478,7 @@ class TransTree(Analyzer):
                           'agents are reused! Please rerun with rescale=False and pop_scale=1 for reliable results.')
         self._people = people
         self._layer_names = people.layer_keys()
+        self._log_labels = list(getattr(sim.state, 'log_labels', []))
         log = sim.state.infection_log_tensor(people._sim)
         self._log = log
         src, tgt, day = log[:, 0], log[:, 1], log[:, 2]
@@ -510,9 +513,7 @@ class TransTree(Analyzer):
             return torch.as_tensor(np.asarray(people[attr]), device=self._log.device)
 
     def _layer_name(self, layer, src, day):
-        if layer < len(self._layer_names):
-            return self._layer_names[layer]
-        return 'seed_infection' if src < 0 and day == 0 else 'importation'
+        return log_layer_label(layer, self._layer_names, self._log_labels)
 
     @property
     def infection_log(self):

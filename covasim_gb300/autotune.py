@@ -35,7 +35,7 @@ def workload_signature(state):
 def _one_run(state, snap, seeds, t1):
     state.restore(snap)
     for k, inds in enumerate(seeds):
-        state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+        state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
     state.run_days(0, t1, open_prev=False, close_last=True, use_graph=True)
 
 

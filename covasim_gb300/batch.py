@@ -74,7 +74,7 @@ class BatchSim:
         for k, s in enumerate(self.sims):
             if s['pop_infected']:
                 inds = choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected'])
-                self.state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+                self.state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
 
     def _import_variants(self, t):
         """Each sim's variant importations of day t, with the sim's own draws
@@ -85,8 +85,9 @@ class BatchSim:
                     sus = np.nonzero(self.state.get('susceptible', k).cpu().numpy())[0]
                     rng = np.random.default_rng([int(s['rand_seed']), 0x1A1A, t, v.index])
                     inds = rng.choice(sus, min(v.n_imports, len(sus)), replace=False)
-                    self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.MAX_LAYERS + 1,
+                    self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.LOG_IMPORT,
                                            call_tag=CALL_IMPORT + v.index)
+                    self.state.note_imports(k, t, len(inds))
 
     def run(self, use_graph=None):
         if self.state is None:
@@ -102,6 +103,7 @@ class BatchSim:
                 t = d
             if t < self.npts:
                 st.agent_step(t, do_prev=False, do_day=True)
+                st.import_day(t)
                 self._import_variants(t)
                 st.test_trace(t)
                 st.edge_pass(t)

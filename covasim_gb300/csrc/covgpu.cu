@@ -49,6 +49,8 @@ constexpr int EQ_CAP = COVGPU_EQ_CAP;  // candidate queue entries per warp (drai
                                        // 192 and 160, which leave L1 more room, measured slower
 static_assert(2 * EDGE_TILE_MAX <= 65536, "queue entries pack (edge within the tile, direction) in 16 bits");
 constexpr int CALL_TAG_SEED = 1;       // covgpu_infect_list call_tag of the day-0 seed infections
+constexpr int CALL_TAG_IMPORT = 2;     // the daily importations (variant importations: 2 + variant)
+constexpr int IMPORT_BLOCKS = 4;       // k_import_day grid (a day imports a handful of agents)
 
 
 // ============================================================ fused agent pass
@@ -1309,6 +1311,36 @@ __global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64
   }
 }
 
+// sim.py:582-587: the agents drawn for day t (every sim's, precomputed on the
+// host: neither the Poisson count nor the choice depends on the state) are
+// infected with the wild type from the importation "layer", on infection
+// stream CALL_TAG_IMPORT. The trip count is uniform across each block (the
+// ballots of infect_tally need every lane); lanes of one warp may belong to
+// different sims.
+__global__ void k_import_day(covgpu_state st, int t) {
+  const int64_t b = st.import_day_off[t], e = st.import_day_off[t + 1];
+  for (int64_t base = b + (int64_t)blockIdx.x * blockDim.x; base < e; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = base + threadIdx.x;
+    uint32_t out = 0;
+    int32_t tgt = 0, s = 0;
+    if (j < e) {
+      const int64_t i = st.imports[j];
+      s = st.import_sims[j];
+      if (s >= 0 && s < st.n_sims && i >= st.sims[s].agent_off && i < st.sims[s].agent_off + st.sims[s].n_agents) {
+        const covgpu_sim_params& sp = st.sims[s];
+        bool hosp, icu;
+        hosp_icu(st, sp, s, t, hosp, icu);
+        tgt = (int32_t)(i - sp.agent_off);
+        out = infect_one(st, sp, s, i, t, 0, -1, COVGPU_MAX_LAYERS + 1, CALL_TAG_IMPORT, hosp, icu);
+      } else {
+        atomicOr(st.status, COVGPU_BADARG);
+        s = 0;
+      }
+    }
+    infect_tally(st, t, out, s, 0, -1, tgt, COVGPU_MAX_LAYERS + 1);
+  }
+}
+
 __global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1, int32_t* p2) {
   const covgpu_layer& L = st.segments[seg];
   const covgpu_sim_params& sp = st.sims[L.sim];
@@ -1342,6 +1374,7 @@ cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the le
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
+    if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
     launch_edge_pass(st, t, s);
     launch_lik_targets(st, t, s);
@@ -1372,6 +1405,8 @@ int check_state(const covgpu_state* st) {
   if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
                           st->pending_slots < 1 || st->n_contact_layers < 1))
     return COVGPU_BADARG;
+  if (st->import_days < 0 || (st->import_days > 0 && (!st->import_day_off || !st->imports || !st->import_sims)))
+    return COVGPU_BADARG;
   const covgpu_lik& K = st->lik;
   if (K.factor && (!K.ll || !K.expected || !K.logq || (K.g_exp && !K.w) || K.npts_max < 1 ||
                    K.n_layers_max < 1 || K.n_layers_max > COVGPU_MAX_LAYERS || K.nv_max < 1))
@@ -1394,7 +1429,7 @@ int covgpu_abi_layout(int64_t* out, int32_t n) {
                        (int64_t)offsetof(covgpu_sim_params, res_fx), (int64_t)sizeof(covgpu_testing),
                        (int64_t)offsetof(covgpu_sim_params, testing), (int64_t)offsetof(covgpu_state, pending_quar),
                        (int64_t)offsetof(covgpu_state, trace_count), (int64_t)sizeof(covgpu_lik),
-                       (int64_t)offsetof(covgpu_state, lik)};
+                       (int64_t)offsetof(covgpu_state, lik), (int64_t)offsetof(covgpu_state, import_day_off)};
   const int m = (int)(sizeof(v) / sizeof(v[0]));
   for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
   return m;
@@ -1447,6 +1482,15 @@ int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, i
   if (n_inds == 0) return COVGPU_OK;
   if (!inds) return COVGPU_BADARG;
   k_infect_list<<<grid_for(n_inds, 128), 128, 0, S(stream)>>>(*st, t, inds, n_inds, sim, variant, layer_tag, call_tag);
+  return launch_status();
+}
+
+int covgpu_import_day(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  if (t >= st->import_days) return COVGPU_OK;
+  k_import_day<<<IMPORT_BLOCKS, 256, 0, S(stream)>>>(*st, t);
   return launch_status();
 }
 

@@ -16,6 +16,37 @@ from . import _lib as L
 __all__ = ['People', 'Layer', 'Contacts']
 
 
+def log_layer_tag(layer, layer_keys, extra):
+    """The infection-log tag of an infect() call's ``layer`` (people.py:508-511):
+    a contact layer's index, LOG_SEED / LOG_IMPORT for 'seed_infection' /
+    'importation', LOG_NONE for None, else a tag registered in ``extra``."""
+    if layer in layer_keys:
+        return layer_keys.index(layer)
+    if layer is None:
+        return L.LOG_NONE
+    named = {'seed_infection': L.LOG_SEED, 'importation': L.LOG_IMPORT}
+    if layer in named:
+        return named[layer]
+    if layer not in extra:
+        if L.LOG_EXTRA + len(extra) > 0xFF:
+            raise ValueError('too many distinct infection-log layer labels')
+        extra.append(layer)
+    return L.LOG_EXTRA + extra.index(layer)
+
+
+def log_layer_label(tag, layer_keys, extra):
+    """Inverse of log_layer_tag."""
+    if tag < len(layer_keys):
+        return layer_keys[tag]
+    if tag == L.LOG_SEED:
+        return 'seed_infection'
+    if tag == L.LOG_IMPORT:
+        return 'importation'
+    if L.LOG_EXTRA <= tag < L.LOG_EXTRA + len(extra):
+        return extra[tag - L.LOG_EXTRA]
+    return None
+
+
 class Layer(dict):
     """One contact layer (covasim/base.py:1610-1876): p1, p2, beta arrays."""
 
@@ -165,8 +196,7 @@ class People:
             return inds
         if hosp_max is not None or icu_max is not None:
             self._state.set_hospicu([[int(bool(hosp_max)), int(bool(icu_max))]] * len(self._state.specs))
-        layer_tag = L.MAX_LAYERS if layer is None else (self.layer_keys().index(layer) if layer in self.contacts
-                                                         else L.MAX_LAYERS)
+        layer_tag = log_layer_tag(layer, self.layer_keys(), self._state.log_labels)
         self._state.infect_list(self.t, inds, sim=self._sim, variant=variant, layer_tag=layer_tag, call_tag=call_tag)
         if hosp_max is not None or icu_max is not None:
             self._state.set_hospicu(None)
@@ -180,9 +210,6 @@ class People:
         vmap = self.pars['variant_map']
         out = []
         for src, tgt, day, layer, v in rec.tolist():
-            if layer < len(keys):
-                lk = keys[layer]
-            else:
-                lk = 'seed_infection' if src < 0 and day == 0 else 'importation'
+            lk = log_layer_label(layer, keys, self._state.log_labels)
             out.append(dict(source=None if src < 0 else src, target=tgt, date=day, layer=lk, variant=vmap[v]))
         return out

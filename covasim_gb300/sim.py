@@ -384,8 +384,6 @@ class Sim:
             raise NotImplementedError('pop_scale > 1 (dynamic rescaling) is not supported on the GPU path')
         if p['frac_susceptible'] != 1.0:
             raise NotImplementedError('frac_susceptible < 1 is not supported on the GPU path')
-        if p['n_imports']:
-            raise NotImplementedError('n_imports > 0 is not supported on the GPU path yet')
         if p['pop_infected'] > p['pop_size']:
             raise ValueError('pop_infected is larger than pop_size')
         for lp in cvpar.LAYER_PARS:
@@ -472,7 +470,7 @@ class Sim:
         """sim.py:505-532 (frac_susceptible == 1): seed infections on day 0."""
         if self['pop_infected'] and not self._seeded:
             inds = choose_seed_infections(self['rand_seed'], self['pop_size'], self['pop_infected'])
-            self.state.infect_list(0, inds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=CALL_SEED)
+            self.state.infect_list(0, inds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
         self._seeded = True
 
     def _variant_days(self):
@@ -489,8 +487,9 @@ class Sim:
                 rng = np.random.default_rng([int(self['rand_seed']), 0x1A1A, t, v.index])
                 n_imp = min(v.n_imports, len(sus))
                 inds = rng.choice(sus, n_imp, replace=False)
-                self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.MAX_LAYERS + 1,
+                self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.LOG_IMPORT,
                                        call_tag=CALL_IMPORT + v.index)
+                self.state.note_imports(0, t, n_imp)
 
     def step(self):
         """One day (sim.py:558-685), then that day's closing pass."""
@@ -503,6 +502,7 @@ class Sim:
             self._seed()
         self.people.__dict__['t'] = t
         self.state.agent_step(t, do_prev=self._open_day is not None, do_day=True)
+        self.state.import_day(t)  # sim.py:582-587, then the variants' importations (sim.py:590-592)
         self._apply_variants(t)
         self.state.test_trace(t)  # sim.py:596-600 interventions after importations, then update_states_post
         self.state.edge_pass(t)

@@ -115,6 +115,31 @@ class SimSpec:
         return tab
 
 
+IMPORT_TAG = 0x1B1B
+
+
+def daily_importations(seed, rate, n, npts):
+    """The agents imported on each day of a run (sim.py:582-587): a list of
+    ``npts`` sorted arrays of distinct local indices. Day t's count is
+    Poisson(rate) (cvu.poisson, utils.py:379-390, with the rate rounded to the
+    float32 of its numba signature) and its agents a uniform choice without
+    replacement among all ``n`` (cvu.choose, utils.py:430-443), both from a PCG64
+    stream keyed by (seed, 0x1B1B, t). Neither depends on the sim's state, so a
+    run's importations are drawn before it starts. A count above ``n`` raises
+    ValueError, as the reference's choice does."""
+    rate = float(np.float32(rate))
+    out = []
+    for t in range(int(npts)):
+        rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, IMPORT_TAG, t]))
+        k = int(rng.poisson(rate))
+        if k > n:
+            raise ValueError(f'day {t}: {k} importations drawn for a population of {n}: cannot take a larger '
+                             'sample than population when replace=False')
+        out.append(np.sort(rng.choice(int(n), size=k, replace=False)).astype(np.int64) if k
+                   else np.zeros(0, dtype=np.int64))
+    return out
+
+
 def prob_threshold(p):
     """ceil(p * 2^53) as an exact integer: the device's test 2k + 1 < threshold on
     the 52 random bits k of a uniform (2k + 1) / 2^53 is float64's u < p."""
@@ -239,6 +264,7 @@ class BatchState:
         self.beta_layer_tab = torch.from_numpy(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32)).to(dev)
         self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)  # float32 pairs
 
+        self._build_imports()
         self._init_people()
         self._build_layers()
         self._build_sims(beta_tabs, bl_tabs, kins)
@@ -251,6 +277,40 @@ class BatchState:
         self._refresh_state()
 
     # ------------------------------------------------------------------ building
+    def _build_imports(self):
+        """Every sim's daily importations as one device table ordered by day, then
+        sim (``covgpu_state.imports``), with the per-day counts kept on the host for
+        the ``n_imports`` result."""
+        days = max(sp.npts for sp in self.specs)
+        per_day = [[] for _ in range(days)]
+        self.import_daily = []
+        for k, (sp, off) in enumerate(zip(self.specs, self.offsets)):
+            counts = np.zeros(sp.npts)
+            rate = sp.pars.get('n_imports') or 0
+            if rate:
+                for t, inds in enumerate(daily_importations(sp.pars['rand_seed'], rate, sp.n, sp.npts)):
+                    if len(inds):
+                        per_day[t].append((inds + off, k))
+                        counts[t] = len(inds)
+            self.import_daily.append(counts)
+        self.import_variant = [np.zeros(sp.npts) for sp in self.specs]  # variant.apply's, added as they happen
+        self.log_labels = []  # infect() layer labels other than the layers, seeds, importations and None
+        day_off = np.zeros(days + 1, dtype=np.int64)
+        for t in range(days):
+            day_off[t + 1] = day_off[t] + sum(len(g) for g, _ in per_day[t])
+        self.import_days = days if day_off[-1] else 0
+        self.import_tabs = None
+        if self.import_days:
+            inds = np.concatenate([g for d in per_day for g, _ in d]).astype(np.int32)
+            sims = np.concatenate([np.full(len(g), k, dtype=np.int32) for d in per_day for g, k in d])
+            self.import_tabs = {'day_off': torch.from_numpy(day_off).to(self.device),
+                                'inds': torch.from_numpy(inds).to(self.device),
+                                'sims': torch.from_numpy(sims).to(self.device)}
+
+    def note_imports(self, sim, t, n):
+        """Count variant importations (immunity.py:129) in the sim's ``n_imports``."""
+        self.import_variant[sim][t] += n
+
     def _init_people(self):
         t = self.t
         for sp, off in zip(self.specs, self.offsets):
@@ -534,6 +594,11 @@ class BatchState:
         if self.has_testing:
             for k in ('trace_bits', 'contact_bits', 'pending_quar', 'trace_count'):
                 setattr(st, k, t[k].data_ptr())
+        st.import_days = self.import_days
+        if self.import_tabs is not None:
+            st.import_day_off = self.import_tabs['day_off'].data_ptr()
+            st.imports = self.import_tabs['inds'].data_ptr()
+            st.import_sims = self.import_tabs['sims'].data_ptr()
         if self.edge_uniform_tensors is not None:
             ptrs = np.array([u.data_ptr() for u in self.edge_uniform_tensors], dtype=np.uint64)
             self._eu_ptrs = torch.from_numpy(ptrs.view(np.int64)).to(self.device)
@@ -649,7 +714,11 @@ class BatchState:
         """Day t's testing, tracing and update_states_post (no-op without testing)."""
         L.call('covgpu_test_trace', self.cstate_ptr, int(t), _stream())
 
-    def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.MAX_LAYERS, call_tag=1):
+    def import_day(self, t):
+        """Day t's importations of every sim (sim.py:582-587; no-op without them)."""
+        L.call('covgpu_import_day', self.cstate_ptr, int(t), _stream())
+
+    def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=1):
         """Infect explicit agents of one sim (local indices; deduplicated and sorted here)."""
         inds = np.unique(np.asarray(inds, dtype=np.int64))
         if len(inds) == 0:
@@ -697,6 +766,8 @@ class BatchState:
         self.t['event_count'].zero_()
         self.t['log_count'].zero_()
         self.t['status'].zero_()
+        for a in self.import_variant:
+            a[:] = 0
         if self.has_testing:
             for k in ('trace_bits', 'contact_bits', 'trace_count'):
                 self.t[k].zero_()
@@ -707,13 +778,16 @@ class BatchState:
         keys = self.MUTABLE + (('pending_quar',) if self.has_testing else ()) + ('log_count',)
         ck = {k: self.t[k].clone() for k in keys}
         ck['_res'] = (self.res_int.clone(), self.res_var.clone(), self.res_fx.clone())
+        ck['_imp'] = [a.copy() for a in self.import_variant]
         return ck
 
     def rewind(self, ck):
         """Return to a checkpoint (day-local buffers cleared, claims reset)."""
         for k, v in ck.items():
-            if k != '_res':
+            if k not in ('_res', '_imp'):
                 self.t[k].copy_(v)
+        for a, b in zip(self.import_variant, ck['_imp']):
+            a[:] = b
         for dst, src in zip((self.res_int, self.res_var, self.res_fx), ck['_res']):
             dst.copy_(src)
         self.t['claim'].fill_(-1)
@@ -821,6 +895,7 @@ class BatchState:
         out = {}
         for k, key in enumerate(cvd.RES_INT_KEYS):
             out[key] = ints[:, k]
+        out['n_imports'] = self.import_daily[sim] + self.import_variant[sim]
         out['_severe_now'] = ints[:, L.RES_SEVERE_NOW]
         out['_critical_now'] = ints[:, L.RES_CRITICAL_NOW]
         for k, key in enumerate(cvd.RES_VAR_KEYS):

@@ -23,7 +23,9 @@
  *   covgpu_infect_claims     covasim/people.py:435-586 infect (+ immunity.py:138-202
  *                            update_peak_nab) for the day's transmissions
  *   covgpu_infect_list       covasim/people.py:435-586 infect for an explicit index list
- *                            (seed infections, sim.py:505-532; importations)
+ *                            (seed infections, sim.py:505-532; variant importations,
+ *                            immunity.py:117-130)
+ *   covgpu_import_day        covasim/sim.py:582-587 the day's Poisson importations
  *   covgpu_layer_materialize covasim/base.py:1849-1876 Layer.update (dynamic layer view)
  */
 #ifndef COVGPU_H
@@ -284,6 +286,14 @@ typedef struct covgpu_state {
   uint32_t* trace_count;          /* [n_sims] agents traced today                    */
   covgpu_lik lik;                 /* likelihood passes after each edge pass (factor
                                      NULL: off)                                      */
+  /* daily importations (sim.py:582-587; all NULL / 0 when no sim imports): the
+   * agents imported on day t are imports[import_day_off[t] .. import_day_off[t+1]),
+   * global agent indices, with the sim of each in import_sims */
+  const int64_t* import_day_off;  /* [import_days + 1]                               */
+  const int32_t* imports;
+  const int32_t* import_sims;
+  int32_t import_days;            /* days covered; 0: no importations                */
+  int32_t _pad3;
 } covgpu_state;
 
 /* ---- standalone kernels: the reference's numba functions ----------------- */
@@ -449,6 +459,14 @@ int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
  * reference seeds before update_states_pre resets them (sim.py:571-577). */
 int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds,
                        int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream);
+
+/* The day's importations (sim.py:582-587): infect() with the wild type for the
+ * agents st->imports lists for day t (all sims; infection log layer
+ * COVGPU_MAX_LAYERS + 1, Philox stream call_tag 2). covgpu_run_days runs it
+ * after each day's agent pass; a day beyond st->import_days imports nobody.
+ * Entries outside their sim's agents are skipped and set COVGPU_BADARG in the
+ * device status word. */
+int covgpu_import_day(const covgpu_state* st, int32_t t, void* stream);
 
 /* Write the day-t endpoints of one dynamic layer segment into p1/p2 (the
  * same edges the edge pass draws that day). */

@@ -38,12 +38,22 @@ CALL_SEED = 1
 CALL_IMPORT = 2
 
 SEED_INFECTION_TAG = 0x5EED
+IMPORT_TAG = 0x1B1B
 
 
 def choose_seed_infections(seed, n, k):
     """Agents infected on day 0 in philox mode: a PCG64 stream keyed by the seed."""
     rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, SEED_INFECTION_TAG]))
     return np.sort(rng.choice(n, size=int(k), replace=False)).astype(np.int64)
+
+
+def philox_mode_importations(seed, rate, n, t):
+    """Agents imported on day t in philox mode (the CUDA library's host-side
+    schedule): Poisson(float32 rate) agents chosen without replacement, from a
+    PCG64 stream keyed by (seed, 0x1B1B, t)."""
+    rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, IMPORT_TAG, int(t)]))
+    k = int(rng.poisson(float(np.float32(rate))))
+    return np.sort(rng.choice(int(n), size=k, replace=False)).astype(np.int64)
 
 
 def set_prognoses(people, pars, rs):
@@ -104,7 +114,8 @@ class OracleSim:
                 iv.initialize(self)
         self.t = 0
         self.results = {}
-        for key in FLOWS + [f'n_{k}' for k in RESULT_STOCKS] + ['pop_nabs', 'pop_protection', 'pop_symp_protection']:
+        for key in FLOWS + [f'n_{k}' for k in RESULT_STOCKS] + ['n_imports', 'pop_nabs', 'pop_protection',
+                                                                'pop_symp_protection']:
             self.results[key] = np.zeros(self.npts)
         nv = pars['n_variants']
         for key in FLOWS_VARIANT + [f'n_{k}' for k in RESULT_STOCKS_BY_VARIANT]:
@@ -155,6 +166,16 @@ class OracleSim:
         self.update_contacts()
         hosp_max = people.severe.sum() > p['n_beds_hosp'] if p['n_beds_hosp'] is not None else False
         icu_max = people.critical.sum() > p['n_beds_icu'] if p['n_beds_icu'] is not None else False
+        if p.get('n_imports'):  # sim.py:582-587
+            if self.rng == 'philox':
+                inds = philox_mode_importations(self.seed, p['n_imports'], self.n, t)
+            else:  # cvu.poisson / cvu.choose are numba functions: numba's stream; the rate is typed float32
+                k = int(self.rs_numba.poisson(float(F32(p['n_imports'])), 1)[0])
+                inds = self.rs_numba.choice(self.n, k, replace=False) if k > 0 else np.zeros(0, dtype=np.int64)
+            if len(inds):
+                people.infect(inds=inds, hosp_max=hosp_max, icu_max=icu_max, layer='importation',
+                              draws=self._draws(CALL_IMPORT))
+                self.results['n_imports'][t] += len(inds)
         if self.beta_schedule is not None:
             p['beta'] = self.beta_schedule[t]
         for iv in self.interventions:  # sim.py:596-598

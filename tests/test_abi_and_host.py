@@ -5,6 +5,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 import covasim_gb300 as cv
 from covasim_gb300 import _lib as L
@@ -134,3 +135,20 @@ def test_change_beta_schedule():
     assert b[9] == 0.016 and b[10] == 0.016 * 0.5 and b[29] == 0.016 * 0.5 and b[30] == 0.016 * 0.8
     bl = spec.beta_layer_sched[:, 0]
     assert bl[19] == 1.0 and bl[20] == 0.1 and bl[40] == 0.1
+
+
+def test_daily_importations_schedule():
+    """sim.py:582-587 drawn ahead of the run: Poisson counts, distinct agents in
+    range, the same schedule as the oracle's philox mode, and the reference's
+    error for a count above the population."""
+    from covasim_gb300.state import daily_importations
+    from oracle.sim import philox_mode_importations
+    days = daily_importations(7, 2.5, 1000, 400)
+    counts = np.array([len(d) for d in days])
+    assert abs(counts.mean() - 2.5) < 4 * np.sqrt(2.5 / 400) and abs(counts.var() - 2.5) < 0.6
+    for t, d in enumerate(days):
+        assert len(np.unique(d)) == len(d) and (d >= 0).all() and (d < 1000).all()
+        np.testing.assert_array_equal(d, philox_mode_importations(7, 2.5, 1000, t))
+    assert [len(d) for d in daily_importations(8, 2.5, 1000, 50)] != list(counts[:50])
+    with pytest.raises(ValueError):
+        daily_importations(1, 50, 5, 3)

@@ -11,6 +11,7 @@ import pytest
 import torch
 
 from covasim_gb300 import analysis as cva
+from covasim_gb300 import _lib as L
 from oracle import analysis as oa
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -60,8 +61,8 @@ class _State:
         for e in log:
             if e['layer'] in LAYERS:
                 li = LAYERS.index(e['layer'])
-            else:
-                li = 16  # seeds and importations carry tags above the layer indices
+            else:  # seeds and importations carry tags above the layer indices
+                li = {'seed_infection': L.LOG_SEED, 'importation': L.LOG_IMPORT}[e['layer']]
             rows.append([-1 if e['source'] is None else e['source'], e['target'], e['date'], li, 0])
         self._log = torch.tensor(rows, dtype=torch.int64).reshape(-1, 5)
 

@@ -11,7 +11,7 @@ from oracle import analysis as oa
 pytestmark = pytest.mark.gpu
 
 
-def testing_sim(datafile=None, **kw):
+def make_testing_sim(datafile=None, **kw):
     pars = dict(pop_type='hybrid', pop_size=4000, n_days=45, rand_seed=5, pop_infected=30, use_waning=True,
                 interventions=[cv.test_prob(symp_prob=0.2, asymp_prob=0.01), cv.contact_tracing(trace_probs=0.5)])
     pars.update(kw)
@@ -19,7 +19,7 @@ def testing_sim(datafile=None, **kw):
 
 
 def test_transtree_matches_the_oracle_on_a_gpu_run():
-    sim = testing_sim().run()
+    sim = make_testing_sim().run()
     tt = sim.make_transtree()
     people = {k: sim.people[k] for k in oa.ATTRS + oa.QUAR_ATTRS + ['date_recovered']}
     o = oa.transtree(sim.people.infection_log, people, len(sim.people), sim.people.t, start_day=5, end_day=30)
@@ -60,9 +60,9 @@ def synthetic_data(sim, every=3, shift=-4):
 
 
 def test_fit_matches_the_oracle_on_a_gpu_run():
-    truth = testing_sim(beta=0.02).run()
+    truth = make_testing_sim(beta=0.02).run()
     data = synthetic_data(truth)
-    sim = testing_sim(datafile=data)
+    sim = make_testing_sim(datafile=data)
     assert sim.day('2020-03-11') == 10 and sim.date(10) == '2020-03-11'
     sim.run()
     fit = sim.compute_fit()
@@ -76,8 +76,8 @@ def test_fit_matches_the_oracle_on_a_gpu_run():
 
 
 def test_calibration_runs_trials_in_batches():
-    truth = testing_sim(beta=0.02).run()
-    sim = testing_sim(beta=0.012, datafile=synthetic_data(truth))
+    truth = make_testing_sim(beta=0.02).run()
+    sim = make_testing_sim(beta=0.012, datafile=synthetic_data(truth))
     calib = cv.Calibration(sim, calib_pars=dict(beta=[0.012, 0.008, 0.03]), n_workers=6, n_trials=3, seed=1,
                            verbose=False)
     calib.calibrate(verbose=False)

@@ -60,6 +60,31 @@ def test_sim_matches_oracle_philox(pop_type, n, days, dyn, seed):
     compare_runs(sim, orc)
 
 
+@pytest.mark.parametrize('pop_type,n,days,rate,seed', [('hybrid', 3000, 40, 0.7, 4), ('random', 2000, 35, 6, 5)])
+def test_sim_with_daily_importations_matches_oracle_philox(pop_type, n, days, rate, seed):
+    """sim.py:582-587: Poisson(n_imports) agents infected every day (graph run and
+    step by step), against the oracle with the same draws."""
+    pars = dict(pop_type=pop_type, pop_size=n, n_days=days, rand_seed=seed, pop_infected=10, n_imports=rate,
+                dynam_layer=dict(h=0, s=0, w=0, c=1) if pop_type == 'hybrid' else dict(a=0))
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim).run()
+    assert orc.results['n_imports'].sum() > 10
+    sim.run()
+    compare_runs(sim, orc, keys=RES_KEYS + ['n_imports'])
+    stepped = cv.Sim(pars)
+    stepped.initialize()
+    for _ in range(stepped.npts):
+        stepped.step()
+    stepped.finalize()
+    ra, rb = sim.raw_results(), stepped.raw_results()
+    for k in RES_KEYS + ['n_imports']:
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+    imported = sorted((e['date'], e['target']) for e in sim.people.infection_log if e['layer'] == 'importation')
+    want = sorted((e['date'], int(e['target'])) for e in orc.people.infection_log if e['layer'] == 'importation')
+    assert imported == want and 0 < len(imported) <= ra['n_imports'].sum()
+
+
 def test_step_mode_equals_graph_run():
     pars = dict(pop_type='hybrid', pop_size=3000, n_days=30, rand_seed=7)
     a = cv.Sim(pars).run()
@@ -99,6 +124,19 @@ def test_batch_equals_single_runs():
         got = batch.results(k)
         for key in RES_KEYS + ['pop_nabs']:
             np.testing.assert_array_equal(got[key], raw[key], err_msg=f'sim {k} {key}')
+
+
+def test_batch_with_daily_importations_equals_single_runs():
+    sims = [cv.Sim(pop_type='random', pop_size=n, n_days=30, rand_seed=s, n_imports=r)
+            for n, s, r in [(3000, 1, 2.5), (1500, 2, 0), (5000, 3, 10)]]
+    singles = [cv.Sim(copy.deepcopy(s.pars)).run() for s in sims]
+    batch = cv.BatchSim([cv.Sim(copy.deepcopy(s.pars)) for s in sims]).run()
+    for k, single in enumerate(singles):
+        raw = single.raw_results()
+        got = batch.results(k)
+        for key in RES_KEYS + ['n_imports', 'pop_nabs']:
+            np.testing.assert_array_equal(got[key], raw[key], err_msg=f'sim {k} {key}')
+    assert batch.results(1)['n_imports'].sum() == 0 and batch.results(2)['n_imports'].sum() > 200
 
 
 def test_beta_zero_no_transmission():
