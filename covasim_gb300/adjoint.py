@@ -31,7 +31,7 @@ import torch
 
 from . import _lib as L
 from .interventions import change_beta
-from .sim import choose_seed_infections, CALL_SEED
+from .sim import init_infections
 
 __all__ = ['Parameters', 'LikelihoodRun', 'SimLikelihood', 'fit_parameters']
 
@@ -139,7 +139,6 @@ class LikelihoodRun:
         self.use_graph = use_graph
         self.npts = sim.npts
         self.initial = self.state.snapshot()
-        self.seeds = choose_seed_infections(sim['rand_seed'], sim['pop_size'], sim['pop_infected'])
         self.state.enable_lik(grad=False)
         self.theta = None
         self.checkpoints = []
@@ -171,7 +170,7 @@ class LikelihoodRun:
         st.set_lik_factor(self.params.factor(theta))
         st.zero_lik()
         st.restore(self.initial)
-        st.infect_list(0, self.seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+        init_infections(st, 0, self.sim.pars)
         self.checkpoints = []
         for t0, t1 in self._segments():
             self.checkpoints.append(st.checkpoint())
@@ -269,7 +268,7 @@ def fit_parameters(run, target, theta0=None, fit=('beta',), steps=40, lr=0.05, f
             loss_t = (resid ** 2).sum() / scale
             opt.zero_grad()
             loss_t.backward()
-            loss = float(loss_t)
+            loss = float(loss_t.detach())
         opt.step()
         hist.append((loss, np.exp(logt.detach().numpy()).copy()))
     out = np.array(theta0)

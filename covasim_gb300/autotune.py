@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
-from .sim import choose_seed_infections, CALL_SEED
+from .sim import init_infections
 
 __all__ = ['tune_edge_tile', 'workload_signature']
 
@@ -32,10 +32,10 @@ def workload_signature(state):
     return f'{name}|n={state.n}|sims={len(state.specs)}|stored={stored}|dynamic={dynamic}'
 
 
-def _one_run(state, snap, seeds, t1):
+def _one_run(state, snap, t1):
     state.restore(snap)
-    for k, inds in enumerate(seeds):
-        state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+    for k, sp in enumerate(state.specs):
+        init_infections(state, k, sp.pars)
     state.run_days(0, t1, open_prev=False, close_last=True, use_graph=True)
 
 
@@ -68,18 +68,17 @@ def tune_edge_tile(state, days=None, candidates=L.EDGE_TILES, reps=2, cache_file
         state.set_edge_tile(int(best.rstrip('r')), resident=best.endswith('r'))
         return best, dict(_CACHE[key]['ms'])
     t1 = min(sp.npts for sp in state.specs) if days is None else int(days)
-    seeds = [choose_seed_infections(sp.pars['rand_seed'], sp.n, sp.pars['pop_infected']) for sp in state.specs]
     stream = torch.cuda.current_stream()
     ms = {}
     for tile, resident in _candidates(state, candidates):
         state.set_edge_tile(tile, resident=resident)
-        _one_run(state, snap, seeds, t1)  # capture and warm
+        _one_run(state, snap, t1)  # capture and warm
         times = []
         for _ in range(reps):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            _one_run(state, snap, seeds, t1)
+            _one_run(state, snap, t1)
             b.record(stream)
             b.synchronize()
             times.append(a.elapsed_time(b))

@@ -17,7 +17,7 @@ from . import parameters as cvpar
 from . import immunity as cvimm
 from . import defaults as cvd
 from . import _lib as L
-from .sim import Sim, build_spec, choose_seed_infections, CALL_SEED, CALL_IMPORT
+from .sim import Sim, build_spec, init_infections, CALL_IMPORT
 from .state import BatchState
 
 __all__ = ['BatchSim']
@@ -72,9 +72,7 @@ class BatchSim:
 
     def seed_infections(self):
         for k, s in enumerate(self.sims):
-            if s['pop_infected']:
-                inds = choose_seed_infections(s['rand_seed'], s['pop_size'], s['pop_infected'])
-                self.state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+            init_infections(self.state, k, s.pars)
 
     def _import_variants(self, t):
         """Each sim's variant importations of day t, with the sim's own draws

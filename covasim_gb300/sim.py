@@ -27,7 +27,8 @@ from . import analysis as cva
 from .people import People, Layer, Contacts
 from .state import SimSpec, BatchState
 
-__all__ = ['Sim', 'Result', 'AlreadyRunError', 'choose_seed_infections', 'build_spec']
+__all__ = ['Sim', 'Result', 'AlreadyRunError', 'choose_seed_infections', 'choose_nonnaive', 'init_infections',
+           'build_spec']
 
 SEED_INFECTION_TAG = 0x5EED
 POPULATION_TAG = 0x9090
@@ -183,6 +184,28 @@ def choose_seed_infections(seed, n, k):
     PCG64 stream keyed by the sim's seed."""
     rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, SEED_INFECTION_TAG]))
     return np.sort(rng.choice(int(n), size=int(k), replace=False)).astype(np.int64)
+
+
+NONNAIVE_TAG = 0x4A4A
+
+
+def choose_nonnaive(seed, n, frac_susceptible):
+    """The agents made non-naive on day 0 when frac_susceptible < 1 (sim.py:519-522):
+    round((1 - frac_susceptible) * n) distinct agents from a PCG64 stream keyed by
+    (seed, 0x4A4A)."""
+    k = int(np.round((1 - frac_susceptible) * n))
+    rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, NONNAIVE_TAG]))
+    return np.sort(rng.choice(int(n), size=k, replace=False)).astype(np.int64)
+
+
+def init_infections(state, k, pars):
+    """sim.py:505-532 for sim ``k`` of a batch on day 0: the non-susceptible
+    fraction made non-naive (people.py:414-431), then the seed infections."""
+    if pars['frac_susceptible'] < 1:
+        state.make_nonnaive(choose_nonnaive(pars['rand_seed'], pars['pop_size'], pars['frac_susceptible']), sim=k)
+    if pars['pop_infected']:
+        inds = choose_seed_infections(pars['rand_seed'], pars['pop_size'], pars['pop_infected'])
+        state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
 
 
 def _layers_from_popdict(pars, popdict):
@@ -382,8 +405,8 @@ class Sim:
         p['pop_infected'] = int(p['pop_infected'])
         if p['pop_scale'] not in (None, 1, 1.0):
             raise NotImplementedError('pop_scale > 1 (dynamic rescaling) is not supported on the GPU path')
-        if p['frac_susceptible'] != 1.0:
-            raise NotImplementedError('frac_susceptible < 1 is not supported on the GPU path')
+        if not 0 <= p['frac_susceptible'] <= 1:
+            raise ValueError(f'frac_susceptible must be between 0 and 1, not {p["frac_susceptible"]}')
         if p['pop_infected'] > p['pop_size']:
             raise ValueError('pop_infected is larger than pop_size')
         for lp in cvpar.LAYER_PARS:
@@ -467,10 +490,9 @@ class Sim:
 
     # ------------------------------------------------------------------ day loop
     def _seed(self):
-        """sim.py:505-532 (frac_susceptible == 1): seed infections on day 0."""
-        if self['pop_infected'] and not self._seeded:
-            inds = choose_seed_infections(self['rand_seed'], self['pop_size'], self['pop_infected'])
-            self.state.infect_list(0, inds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+        """sim.py:505-532: prior immunity and seed infections on day 0."""
+        if not self._seeded:
+            init_infections(self.state, 0, self.pars)
         self._seeded = True
 
     def _variant_days(self):

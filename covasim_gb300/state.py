@@ -714,6 +714,18 @@ class BatchState:
         """Day t's testing, tracing and update_states_post (no-op without testing)."""
         L.call('covgpu_test_trace', self.cstate_ptr, int(t), _stream())
 
+    def make_nonnaive(self, inds, sim=0):
+        """people.py:414-431 make_nonnaive on agents still in their initial state:
+        susceptible and naive cleared (local indices)."""
+        inds = np.unique(np.asarray(inds, dtype=np.int64))
+        if len(inds) == 0:
+            return
+        if inds.min() < 0 or inds.max() >= self.specs[sim].n:
+            raise IndexError('agent index out of range')
+        g = torch.from_numpy(inds + self.offsets[sim]).to(self.device)
+        keep = ~((1 << STATE_BIT['susceptible']) | (1 << STATE_BIT['naive']))
+        self.t['flags'][g] &= keep
+
     def import_day(self, t):
         """Day t's importations of every sim (sim.py:582-587; no-op without them)."""
         L.call('covgpu_import_day', self.cstate_ptr, int(t), _stream())
@@ -901,7 +913,8 @@ class BatchState:
         for k, key in enumerate(cvd.RES_VAR_KEYS):
             out[key] = var[:, k, :].T.copy()
         n_alive = sp.n - out['n_dead']
-        out['pop_nabs'] = np.ldexp(fx[:, 0].astype(np.float64), -L.FX_NAB_BITS) / n_alive
+        with np.errstate(invalid='ignore', divide='ignore'):  # nobody alive: NaN, as sim.py:672 gives
+            out['pop_nabs'] = np.ldexp(fx[:, 0].astype(np.float64), -L.FX_NAB_BITS) / n_alive
         denom = nv * sp.n
         out['pop_protection'] = np.ldexp(fx[:, 1].astype(np.float64), -L.FX_IMM_BITS) / denom
         out['pop_symp_protection'] = np.ldexp(fx[:, 2].astype(np.float64), -L.FX_IMM_BITS) / denom

@@ -39,6 +39,7 @@ CALL_IMPORT = 2
 
 SEED_INFECTION_TAG = 0x5EED
 IMPORT_TAG = 0x1B1B
+NONNAIVE_TAG = 0x4A4A
 
 
 def choose_seed_infections(seed, n, k):
@@ -130,8 +131,20 @@ class OracleSim:
         return SequentialDraws(self.rs_numpy)
 
     def init_infections(self):
-        """sim.py:505-532 (frac_susceptible == 1)."""
+        """sim.py:505-532: the non-susceptible fraction made non-naive
+        (people.py:414-431 on fresh agents: susceptible and naive cleared), then
+        the seed infections."""
         p = self.pars
+        frac = p.get('frac_susceptible', 1.0)
+        if frac < 1:
+            k = int(np.round((1 - frac) * self.n))
+            if self.rng == 'philox':
+                rng = np.random.Generator(np.random.PCG64([self.seed & 0xFFFFFFFFFFFFFFFF, NONNAIVE_TAG]))
+                inds = np.sort(rng.choice(self.n, size=k, replace=False))
+            else:  # cvu.choose: numba's stream
+                inds = self.rs_numba.choice(self.n, k, replace=False)
+            self.people.susceptible[inds] = False
+            self.people.naive[inds] = False
         if p['pop_infected']:
             if self.seed_inds is not None:
                 inds = np.asarray(self.seed_inds)

@@ -365,10 +365,13 @@ def make_day_fixtures(ref):
 
 def make_sims_fixture(ref):
     out = {}
-    # (pop_type, n, days, seed, dynamic c, extra pars); the last two import agents every
-    # day (sim.py:582-587), one at a rate that float32 does not hold exactly
+    # (pop_type, n, days, seed, dynamic c, extra pars); cases 3 and 4 import agents every
+    # day (sim.py:582-587), one at a rate that float32 does not hold exactly; cases 5
+    # and 6 start with part of the population non-naive (sim.py:519-522)
     cases = [('random', 1500, 40, 3, 0, {}), ('hybrid', 1500, 50, 4, 0, {}), ('hybrid', 1200, 45, 9, 1, {}),
-             ('hybrid', 1500, 45, 12, 1, dict(n_imports=0.7)), ('random', 1200, 40, 13, 0, dict(n_imports=3))]
+             ('hybrid', 1500, 45, 12, 1, dict(n_imports=0.7)), ('random', 1200, 40, 13, 0, dict(n_imports=3)),
+             ('hybrid', 1500, 45, 14, 0, dict(frac_susceptible=0.55)),
+             ('random', 1300, 40, 15, 0, dict(frac_susceptible=0.8, n_imports=1.5, pop_infected=40))]
     for i, (pop_type, n, days, seed, dyn, extra) in enumerate(cases):
         pars = ref.make_pars(pop_size=n, n_days=days, pop_type=pop_type, rand_seed=seed, **extra)
         if dyn:

@@ -218,11 +218,13 @@ def _cast_args(args, spec):
     return out
 
 
-NUMBA_SIGNATURES = {  # covasim/utils.py:38,81,92,131
+NUMBA_SIGNATURES = {  # covasim/utils.py:38,81,92,131,378,430
     'compute_viral_load': 'iFFFfff',
     'compute_trans_sus': 'FFBBfFBBBfffF',
     'compute_infections': 'fIIFFF?',
     'find_contacts': 'IIL',
+    'poisson': 'f',
+    'choose': 'ii',
 }
 
 
@@ -261,7 +263,7 @@ class Reference:
             utils_ns[k] = f
             utils_nb_ns[k] = f
         self.cvu = types.SimpleNamespace(**fns)
-        for k in ('compute_viral_load', 'compute_trans_sus', 'compute_infections', 'find_contacts'):
+        for k in NUMBA_SIGNATURES:
             setattr(self.cvu, k, numba_wrapped(fns[k], k))
 
         def set_seed(seed=None):  # utils.py:271-298: seed both streams identically
@@ -293,7 +295,7 @@ class Reference:
                                                'check_infectious', 'check_symptomatic', 'check_severe',
                                                'check_critical', 'check_recovery', 'check_death',
                                                'check_diagnosed', 'check_quar', 'check_enter_iso',
-                                               'check_exit_iso', 'make_naive', 'infect', 'test',
+                                               'check_exit_iso', 'make_naive', 'make_nonnaive', 'infect', 'test',
                                                'schedule_quarantine'])
         base_ns = {'np': np, 'sc': sc, 'cvu': self.cvu, 'cvd': self.cvd}
         base_methods = load_functions('base.py', classname='BasePeople', namespace=base_ns,

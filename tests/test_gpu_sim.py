@@ -85,6 +85,22 @@ def test_sim_with_daily_importations_matches_oracle_philox(pop_type, n, days, ra
     assert imported == want and 0 < len(imported) <= ra['n_imports'].sum()
 
 
+@pytest.mark.parametrize('frac,rate', [(0.6, 0), (0.85, 2)])
+def test_sim_with_nonnaive_fraction_matches_oracle_philox(frac, rate):
+    """sim.py:519-522: round((1 - frac_susceptible) * n) agents start non-naive."""
+    pars = dict(pop_type='hybrid', pop_size=3000, n_days=40, rand_seed=9, pop_infected=40, frac_susceptible=frac,
+                n_imports=rate)
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim).run()
+    sim.run()
+    compare_runs(sim, orc, keys=RES_KEYS + ['n_imports'])
+    never = ~sim.people['naive'] & ~sim.people['exposed'] & ~sim.people['recovered'] & ~sim.people['dead']
+    assert never.sum() >= round((1 - frac) * 3000) - 40
+    batch = cv.BatchSim([cv.Sim(dict(pars)), cv.Sim(dict(pars, rand_seed=10, frac_susceptible=1.0))]).run()
+    np.testing.assert_array_equal(batch.results(0)['new_infections'], sim.raw_results()['new_infections'])
+
+
 def test_step_mode_equals_graph_run():
     pars = dict(pop_type='hybrid', pop_size=3000, n_days=30, rand_seed=7)
     a = cv.Sim(pars).run()
