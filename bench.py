@@ -384,12 +384,11 @@ def adjoint_arm(args, n=100_000, days=120, every=10, reps=3):
         st = run.state
         st.disable_lik()
         st.restore(run.initial)
-        st.infect_list(0, run.seeds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+        init_infections(st, 0, run.sim.pars)
         st.run_days(0, run.npts, open_prev=False, close_last=True, use_graph=True)
         torch.cuda.synchronize()
 
-    from covasim_gb300 import _lib as L
-    from covasim_gb300.sim import CALL_SEED
+    from covasim_gb300.sim import init_infections
     for _ in range(2):  # warm-up: graph captures of every segment in both modes
         plain()
         run.forward(th)

@@ -88,6 +88,8 @@ class SimParams(C.Structure):
         ('n_vaccines', C.c_int32), ('_pad2', C.c_int32),
         ('res_int', C.c_void_p), ('res_var', C.c_void_p), ('res_fx', C.c_void_p),
         ('testing', Testing), ('seg_of_layer', C.c_int32 * MAX_LAYERS),
+        ('pop_scale', C.c_double), ('rescale_threshold', C.c_double), ('rescale_vec', C.c_void_p),
+        ('nonnaive', C.c_void_p),
     ]
 
 
@@ -134,6 +136,7 @@ class State(C.Structure):
         ('lik', Lik),
         ('import_day_off', C.c_void_p), ('imports', C.c_void_p), ('import_sims', C.c_void_p),
         ('import_days', C.c_int32), ('_pad3', C.c_int32),
+        ('hold', C.c_void_p),
     ]
 
 
@@ -169,6 +172,7 @@ def lib():
         L.covgpu_lik_targets.argtypes = [sp, i32, vp]
         L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
         L.covgpu_import_day.argtypes = [sp, i32, vp]
+        L.covgpu_rescale_check.argtypes = [sp, i32, vp]
         L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
         L.covgpu_edge_resident_bytes.argtypes = [sp]
@@ -217,7 +221,7 @@ def abi_layout():
     mine = [C.sizeof(SimParams), C.sizeof(Layer), C.sizeof(AgentBlock), 16, 16, C.sizeof(State),
             State.sims.offset, State.edge_uniforms.offset, SimParams.res_fx.offset, C.sizeof(Testing),
             SimParams.testing.offset, State.pending_quar.offset, State.trace_count.offset, C.sizeof(Lik),
-            State.lik.offset, State.import_day_off.offset]
+            State.lik.offset, State.import_day_off.offset, SimParams.pop_scale.offset, State.hold.offset]
     return list(out[:m]), mine
 
 
@@ -226,6 +230,6 @@ POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts'
 
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
-            'covgpu_infect_list', 'covgpu_import_day', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
+            'covgpu_infect_list', 'covgpu_import_day', 'covgpu_rescale_check', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
             'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index', 'covgpu_edge_resident_bytes',
             'covgpu_pop_scan_scratch'] + POP_FUNCS

@@ -130,6 +130,8 @@ class LikelihoodRun:
     def __init__(self, sim, which=('beta', 'beta_layer', 'change_beta'), checkpoint_every=10, use_graph=True):
         if not sim.initialized:
             sim.initialize()
+        if sim.state.hold is not None:
+            raise NotImplementedError('likelihood runs do not support dynamic rescaling (pop_scale > 1 with rescale)')
         if sim.state.has_testing or sim['variants']:
             raise NotImplementedError('likelihood runs support sims without host-side days (no variants imports)')
         self.sim = sim

@@ -17,7 +17,7 @@ from . import parameters as cvpar
 from . import immunity as cvimm
 from . import defaults as cvd
 from . import _lib as L
-from .sim import Sim, build_spec, init_infections, CALL_IMPORT
+from .sim import Sim, build_spec, init_infections, variant_import_count, CALL_IMPORT
 from .state import BatchState
 
 __all__ = ['BatchSim']
@@ -82,7 +82,8 @@ class BatchSim:
                 if t in np.atleast_1d(v.days):
                     sus = np.nonzero(self.state.get('susceptible', k).cpu().numpy())[0]
                     rng = np.random.default_rng([int(s['rand_seed']), 0x1A1A, t, v.index])
-                    inds = rng.choice(sus, min(v.n_imports, len(sus)), replace=False)
+                    n_imp = min(variant_import_count(v, self.state.rescale_vecs[k][t], rng), len(sus))
+                    inds = rng.choice(sus, n_imp, replace=False)
                     self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.LOG_IMPORT,
                                            call_tag=CALL_IMPORT + v.index)
                     self.state.note_imports(k, t, len(inds))
@@ -96,10 +97,16 @@ class BatchSim:
         host_days = sorted({d for s in self.sims for d in s._variant_days() if 0 <= d < self.npts})
         st, t = self.state, 0
         for d in host_days + [self.npts]:
-            if d > t:
+            while d > t:
                 st.run_days(t, d, open_prev=False, close_last=True, use_graph=use_graph)
-                t = d
+                held = st.held_day()
+                if held is not None and held < d:  # a rescaling fell due on day `held` (sim.py:535-556)
+                    st.rescale_day(held)
+                    t = held
+                else:
+                    t = d
             if t < self.npts:
+                st.rescale_day(t)
                 st.agent_step(t, do_prev=False, do_day=True)
                 st.import_day(t)
                 self._import_variants(t)
@@ -127,17 +134,7 @@ class BatchSim:
             s.state = self.state
             s.t = self.npts
             s.complete = True
-            res = self.state.results(k)
-            for key, vals in res.items():
-                if key.startswith('_'):
-                    continue
-                if key in s.results['variant']:
-                    s.results['variant'][key].values[:] = vals
-                elif key in s.results:
-                    s.results[key].values[:] = vals
-            for key in cvd.result_flows:
-                s.results[f'cum_{key}'].values[:] = np.cumsum(s.results[f'new_{key}'].values)
-            s.results['cum_infections'].values += s['pop_infected']
+            s._fill_results(self.state.results(k), self.state.rescale_vecs[k])
             s.results_ready = True
             s.t -= 1
             s.compute_states()

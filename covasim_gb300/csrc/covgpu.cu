@@ -57,6 +57,12 @@ constexpr int IMPORT_BLOCKS = 4;       // k_import_day grid (a day imports a han
 
 
 __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day) {
+  if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
+    const int h = *st.hold;
+    if (h <= t - 1) return;
+    if (h <= t) do_day = 0;
+    if (!do_prev && !do_day) return;
+  }
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const int nv = sp.n_variants;
@@ -657,6 +663,7 @@ __device__ __forceinline__ void lik_flush_warp(const covgpu_state& st, int t, in
 // One block per tile.
 template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
   constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
   __shared__ covgpu_layer s_L;
@@ -697,6 +704,7 @@ constexpr int RES_THREADS = 1024;
 constexpr int RES_MAX_SEGS = COVGPU_MAX_LAYERS;  // one sim: at most one segment per layer
 template <bool LIK, int64_t TILE>
 __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state st, int t) {
+  if (held(st, t)) return;
   extern __shared__ uint4 s_dyn[];
   __shared__ covgpu_layer s_segs[RES_MAX_SEGS];
   __shared__ SimLite s_sp;
@@ -1260,6 +1268,7 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
 }
 
 __global__ void k_infect_claims(covgpu_state st, int t) {
+  if (held(st, t)) return;
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
   // IG lanes per event, 32 / IG events per warp and iteration; warp-uniform trip
@@ -1318,6 +1327,7 @@ __global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64
 // ballots of infect_tally need every lane); lanes of one warp may belong to
 // different sims.
 __global__ void k_import_day(covgpu_state st, int t) {
+  if (held(st, t)) return;
   const int64_t b = st.import_day_off[t], e = st.import_day_off[t + 1];
   for (int64_t base = b + (int64_t)blockIdx.x * blockDim.x; base < e; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = base + threadIdx.x;
@@ -1338,6 +1348,33 @@ __global__ void k_import_day(covgpu_state st, int t) {
       }
     }
     infect_tally(st, t, out, s, 0, -1, tgt, COVGPU_MAX_LAYERS + 1);
+  }
+}
+
+// sim.py:535-547, the test only: is a rescaling due at the start of day t? The
+// count of agents not naive grows by the day's first infections (infections
+// less reinfections; an agent's first infection clears naive, and only a
+// recovered agent is reinfected); the host sets it after seeding and after
+// each rescaling. One thread per sim.
+__global__ void k_rescale_check(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  for (int s = threadIdx.x; s < st.n_sims; s += blockDim.x) {
+    const covgpu_sim_params& sp = st.sims[s];
+    if (!sp.rescale_vec || t >= sp.npts) continue;
+    int64_t nn = sp.nonnaive[0];
+    for (int64_t d = sp.nonnaive[1] + 1; d <= t - 1; ++d) {
+      const int64_t* r = sp.res_int + d * COVGPU_N_RES_INT;
+      nn += r[R_INFECTIONS] - r[R_REINFECTIONS];
+    }
+    if (sp.nonnaive[1] < t - 1) {
+      sp.nonnaive[0] = nn;
+      sp.nonnaive[1] = t - 1;
+    }
+    if (sp.nonnaive[2] >= t) continue;
+    if (sp.rescale_vec[t] < sp.pop_scale && (double)nn / (double)sp.n_agents > sp.rescale_threshold)
+      atomicMin(st.hold, t);
+    else
+      sp.nonnaive[2] = t;
   }
 }
 
@@ -1373,6 +1410,7 @@ cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the le
 
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
+    if (st->hold) k_rescale_check<<<1, 128, 0, s>>>(*st, t);
     k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
@@ -1429,7 +1467,8 @@ int covgpu_abi_layout(int64_t* out, int32_t n) {
                        (int64_t)offsetof(covgpu_sim_params, res_fx), (int64_t)sizeof(covgpu_testing),
                        (int64_t)offsetof(covgpu_sim_params, testing), (int64_t)offsetof(covgpu_state, pending_quar),
                        (int64_t)offsetof(covgpu_state, trace_count), (int64_t)sizeof(covgpu_lik),
-                       (int64_t)offsetof(covgpu_state, lik), (int64_t)offsetof(covgpu_state, import_day_off)};
+                       (int64_t)offsetof(covgpu_state, lik), (int64_t)offsetof(covgpu_state, import_day_off),
+                       (int64_t)offsetof(covgpu_sim_params, pop_scale), (int64_t)offsetof(covgpu_state, hold)};
   const int m = (int)(sizeof(v) / sizeof(v[0]));
   for (int i = 0; i < n && i < m; ++i) out[i] = v[i];
   return m;
@@ -1491,6 +1530,14 @@ int covgpu_import_day(const covgpu_state* st, int32_t t, void* stream) {
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
   if (t >= st->import_days) return COVGPU_OK;
   k_import_day<<<IMPORT_BLOCKS, 256, 0, S(stream)>>>(*st, t);
+  return launch_status();
+}
+
+int covgpu_rescale_check(const covgpu_state* st, int32_t t, void* stream) {
+  int rc = check_state(st);
+  if (rc) return rc;
+  if (t < 0 || t >= 0xFFFF || !st->hold) return COVGPU_BADARG;
+  k_rescale_check<<<1, 128, 0, S(stream)>>>(*st, t);
   return launch_status();
 }
 

@@ -34,6 +34,10 @@ __device__ __constant__ uint32_t STOCK_BITS[N_STOCKS] = {
 // per-sim-day-variant slots
 enum { RV_INFECTIONS = 0, RV_SYMPTOMATIC, RV_SEVERE, RV_INFECTIOUS, RV_N_EXPOSED, RV_N_INFECTIOUS };
 
+// Day t is held back for a host step (a due rescaling): its day kernels return
+// at once. The flag is written by an earlier kernel of the same sequence.
+__device__ __forceinline__ bool held(const covgpu_state& st, int t) { return st.hold && *st.hold <= t; }
+
 // ---------------------------------------------------------------- Philox-4x32-10
 // Salmon et al., SC'11. Round constants and Weyl increments of that paper.
 constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;

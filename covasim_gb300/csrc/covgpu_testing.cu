@@ -46,6 +46,7 @@ __device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu
 // test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
 // then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
 __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;
@@ -107,6 +108,7 @@ __device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, in
 // every edge with a traced endpoint marks the other endpoint in its layer's bitmap
 template <int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
+  if (held(st, t)) return;
   constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
   if (threadIdx.x == 0) {
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
 // find_contacts through the index of each stored layer: a traced agent marks the
 // other endpoint of each of its edges, as p1 and as p2
 __global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
+  if (held(st, t)) return;
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;
@@ -186,6 +189,7 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, in
 // binomial_filter of identify_contacts, then update_states_post
 // (people.py:189-196: check_diagnosed, check_quar, check_enter_iso)
 __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
   const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;

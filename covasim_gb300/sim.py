@@ -198,6 +198,14 @@ def choose_nonnaive(seed, n, frac_susceptible):
     return np.sort(rng.choice(int(n), size=k, replace=False)).astype(np.int64)
 
 
+def variant_import_count(v, scale, rng):
+    """immunity.py:121-124: a variant's importations on one of its days, n_imports
+    over the day's scale (if the variant rescales) rounded at random (sciris'
+    randround: floor(x + u); a whole number stays as it is and draws nothing)."""
+    x = v.n_imports / (scale if getattr(v, 'rescale', True) else 1.0)
+    return int(x) if x == int(x) else int(np.floor(x + rng.random()))
+
+
 def init_infections(state, k, pars):
     """sim.py:505-532 for sim ``k`` of a batch on day 0: the non-susceptible
     fraction made non-naive (people.py:414-431), then the seed infections."""
@@ -206,6 +214,7 @@ def init_infections(state, k, pars):
     if pars['pop_infected']:
         inds = choose_seed_infections(pars['rand_seed'], pars['pop_size'], pars['pop_infected'])
         state.infect_list(0, inds, sim=k, variant=0, layer_tag=L.LOG_SEED, call_tag=CALL_SEED)
+    state.count_nonnaive(k)
 
 
 def _layers_from_popdict(pars, popdict):
@@ -403,8 +412,13 @@ class Sim:
         p = self.pars
         p['pop_size'] = int(p['pop_size'])
         p['pop_infected'] = int(p['pop_infected'])
-        if p['pop_scale'] not in (None, 1, 1.0):
-            raise NotImplementedError('pop_scale > 1 (dynamic rescaling) is not supported on the GPU path')
+        if p.get('scaled_pop') is not None:  # sim.py:208-214
+            if p['pop_scale'] in (None, 1, 1.0):
+                p['pop_scale'] = p['scaled_pop'] / p['pop_size']
+            else:
+                p['pop_size'] = int(p['scaled_pop'] / p['pop_scale'])
+        if p['pop_scale'] is None:
+            p['pop_scale'] = 1
         if not 0 <= p['frac_susceptible'] <= 1:
             raise ValueError(f'frac_susceptible must be between 0 and 1, not {p["frac_susceptible"]}')
         if p['pop_infected'] > p['pop_size']:
@@ -507,7 +521,7 @@ class Sim:
             if t in np.atleast_1d(v.days):
                 sus = np.nonzero(self.people['susceptible'])[0]
                 rng = np.random.default_rng([int(self['rand_seed']), 0x1A1A, t, v.index])
-                n_imp = min(v.n_imports, len(sus))
+                n_imp = min(variant_import_count(v, self.state.rescale_vecs[0][t], rng), len(sus))
                 inds = rng.choice(sus, n_imp, replace=False)
                 self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.LOG_IMPORT,
                                        call_tag=CALL_IMPORT + v.index)
@@ -522,6 +536,7 @@ class Sim:
         t = self.t
         if t == 0:
             self._seed()
+        self.state.rescale_day(t)  # sim.py:575, before update_states_pre
         self.people.__dict__['t'] = t
         self.state.agent_step(t, do_prev=self._open_day is not None, do_day=True)
         self.state.import_day(t)  # sim.py:582-587, then the variants' importations (sim.py:590-592)
@@ -560,6 +575,11 @@ class Sim:
             nxt = next((d for d in host_days if d >= self.t), until)
             if nxt > self.t:  # days without host work: one fused launch sequence (or graph)
                 self.state.run_days(self.t, nxt, close_last=True, use_graph=use_graph)
+                held = self.state.held_day()
+                if held is not None and held < nxt:  # a rescaling fell due: do it, go on from that day
+                    self.state.rescale_day(held)
+                    self.t = held
+                    continue
                 self.t = nxt
             if self.t < until and self.t == nxt:  # a day with host work
                 self.step()
@@ -599,27 +619,43 @@ class Sim:
         """sim.py:764-815 (no rescaling on the GPU path)."""
         if self.results_ready:
             raise AlreadyRunError('Simulation has already been finalized')
-        res = self.state.results(0)
-        for key, vals in res.items():
-            if key.startswith('_'):
-                continue
-            if key in self.results['variant']:
-                self.results['variant'][key].values[:] = vals
-            elif key in self.results:
-                self.results[key].values[:] = vals
-        for key in cvd.result_flows:
-            self.results[f'cum_{key}'].values[:] = np.cumsum(self.results[f'new_{key}'].values)
-        for key in cvd.result_flows_by_variant:
-            self.results['variant'][f'cum_{key}'].values[:] = np.cumsum(self.results['variant'][f'new_{key}'].values,
-                                                                        axis=1)
-        self.results['cum_infections'].values += self['pop_infected']
-        self.results['variant']['cum_infections_by_variant'].values[0] += self['pop_infected']
+        self._fill_results(self.state.results(0), self.state.rescale_vecs[0])
         self.results_ready = True
         self.t -= 1
         self.people.__dict__['t'] = self.t
         self.compute_results()
         self.summary = {k: v.values[-1] for k, v in self.results.items() if isinstance(v, Result)}
         return self
+
+    UNSCALED = ('prevalence', 'incidence', 'r_eff', 'doubling_time', 'test_yield', 'rel_test_yield',
+                'frac_vaccinated', 'pop_nabs', 'pop_protection', 'pop_symp_protection', 'prevalence_by_variant',
+                'incidence_by_variant')
+
+    def _fill_results(self, res, rescale_vec):
+        """sim.py:771-787: the device's per-day counts, scaled by each day's scale
+        (the results that count people), their cumulative sums, and the seed
+        infections at day 0's scale."""
+        self.rescale_vec = np.array(rescale_vec, dtype=np.float64)
+        for key, vals in res.items():
+            if key.startswith('_'):
+                continue
+            scale = 1.0 if key in self.UNSCALED else self.rescale_vec
+            if key in self.results['variant']:
+                self.results['variant'][key].values[:] = vals * scale
+            elif key in self.results:
+                self.results[key].values[:] = vals * scale
+        for key in cvd.result_flows:
+            self.results[f'cum_{key}'].values[:] = np.cumsum(self.results[f'new_{key}'].values)
+        for key in cvd.result_flows_by_variant:
+            self.results['variant'][f'cum_{key}'].values[:] = np.cumsum(self.results['variant'][f'new_{key}'].values,
+                                                                        axis=1)
+        self.results['cum_infections'].values += self['pop_infected'] * self.rescale_vec[0]
+        self.results['variant']['cum_infections_by_variant'].values[0] += self['pop_infected'] * self.rescale_vec[0]
+
+    @property
+    def scaled_pop_size(self):
+        """base.py:316-321: agents times the scale factor."""
+        return self['pop_size'] * self['pop_scale']
 
     def compute_results(self):
         """sim.py:818-825 (the summary is formed by finalize)."""
@@ -632,7 +668,7 @@ class Sim:
         """sim.py:828-850."""
         res = self.results
         count_recov = 1 - self['use_waning']
-        n = self['pop_size']
+        n = self.scaled_pop_size
         res['n_alive'].values[:] = n - res['cum_deaths'].values
         res['n_naive'].values[:] = n - res['cum_deaths'].values - res['n_recovered'].values - res['n_exposed'].values
         res['n_susceptible'].values[:] = res['n_alive'].values - res['n_exposed'].values - count_recov * res['cum_recoveries'].values

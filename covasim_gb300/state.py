@@ -116,22 +116,26 @@ class SimSpec:
 
 
 IMPORT_TAG = 0x1B1B
+RESCALE_TAG = 0x5C5C
+HOLD_NONE = 0x7FFFFFFF
 
 
-def daily_importations(seed, rate, n, npts):
-    """The agents imported on each day of a run (sim.py:582-587): a list of
-    ``npts`` sorted arrays of distinct local indices. Day t's count is
-    Poisson(rate) (cvu.poisson, utils.py:379-390, with the rate rounded to the
-    float32 of its numba signature) and its agents a uniform choice without
-    replacement among all ``n`` (cvu.choose, utils.py:430-443), both from a PCG64
-    stream keyed by (seed, 0x1B1B, t). Neither depends on the sim's state, so a
-    run's importations are drawn before it starts. A count above ``n`` raises
-    ValueError, as the reference's choice does."""
-    rate = float(np.float32(rate))
+def daily_importations(seed, rate, n, npts, start=0):
+    """The agents imported on days ``start`` .. ``npts - 1`` of a run (sim.py:582-587):
+    a list of sorted arrays of distinct local indices. Day t's count is
+    Poisson(rate[t]) (cvu.poisson, utils.py:379-390, with the rate rounded to the
+    float32 of its numba signature; ``rate`` a number or one per day, n_imports
+    over the day's scale) and its agents a uniform choice without replacement
+    among all ``n`` (cvu.choose, utils.py:430-443), both from a PCG64 stream keyed
+    by (seed, 0x1B1B, t). Neither depends on the sim's state, so a run's
+    importations are drawn before it starts (and redrawn from the day of a
+    rescaling on). A count above ``n`` raises ValueError, as the reference's
+    choice does."""
+    rates = np.broadcast_to(np.asarray(rate, dtype=np.float64), (int(npts),))
     out = []
-    for t in range(int(npts)):
+    for t in range(int(start), int(npts)):
         rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, IMPORT_TAG, t]))
-        k = int(rng.poisson(rate))
+        k = int(rng.poisson(float(np.float32(rates[t]))))
         if k > n:
             raise ValueError(f'day {t}: {k} importations drawn for a population of {n}: cannot take a larger '
                              'sample than population when replace=False')
@@ -264,6 +268,7 @@ class BatchState:
         self.beta_layer_tab = torch.from_numpy(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32)).to(dev)
         self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)  # float32 pairs
 
+        self._build_rescale()
         self._build_imports()
         self._init_people()
         self._build_layers()
@@ -281,20 +286,26 @@ class BatchState:
         """Every sim's daily importations as one device table ordered by day, then
         sim (``covgpu_state.imports``), with the per-day counts kept on the host for
         the ``n_imports`` result."""
+        self.import_sched = []
+        for sp, vec in zip(self.specs, self.rescale_vecs):
+            rate = sp.pars.get('n_imports') or 0
+            self.import_sched.append(daily_importations(sp.pars['rand_seed'], rate / vec, sp.n, sp.npts) if rate
+                                     else None)
+        self.import_variant = [np.zeros(sp.npts) for sp in self.specs]  # variant.apply's, added as they happen
+        self.log_labels = []  # infect() layer labels other than the layers, seeds, importations and None
+        self._upload_imports()
+
+    def _upload_imports(self):
         days = max(sp.npts for sp in self.specs)
         per_day = [[] for _ in range(days)]
         self.import_daily = []
-        for k, (sp, off) in enumerate(zip(self.specs, self.offsets)):
+        for k, (sp, off, sched) in enumerate(zip(self.specs, self.offsets, self.import_sched)):
             counts = np.zeros(sp.npts)
-            rate = sp.pars.get('n_imports') or 0
-            if rate:
-                for t, inds in enumerate(daily_importations(sp.pars['rand_seed'], rate, sp.n, sp.npts)):
-                    if len(inds):
-                        per_day[t].append((inds + off, k))
-                        counts[t] = len(inds)
+            for t, inds in enumerate(sched or []):
+                if len(inds):
+                    per_day[t].append((inds + off, k))
+                    counts[t] = len(inds)
             self.import_daily.append(counts)
-        self.import_variant = [np.zeros(sp.npts) for sp in self.specs]  # variant.apply's, added as they happen
-        self.log_labels = []  # infect() layer labels other than the layers, seeds, importations and None
         day_off = np.zeros(days + 1, dtype=np.int64)
         for t in range(days):
             day_off[t + 1] = day_off[t] + sum(len(g) for g, _ in per_day[t])
@@ -306,6 +317,110 @@ class BatchState:
             self.import_tabs = {'day_off': torch.from_numpy(day_off).to(self.device),
                                 'inds': torch.from_numpy(inds).to(self.device),
                                 'sims': torch.from_numpy(sims).to(self.device)}
+
+    def _build_rescale(self):
+        """The scale of each day of each sim (sim.py:342-346: 1 to start with when
+        rescaling dynamically, else pop_scale) and, when some sim rescales
+        dynamically (sim.py:535-556), the device word that holds a run back on
+        the day a rescaling is due and the counters of the day check."""
+        self.rescale_vecs, self.rescaling = [], []
+        for sp in self.specs:
+            p = sp.pars
+            pop_scale = float(p.get('pop_scale') or 1)
+            dynamic = bool(p.get('rescale', True))
+            self.rescale_vecs.append((1.0 if dynamic else pop_scale) * np.ones(sp.npts))
+            self.rescaling.append(dynamic and pop_scale > 1)
+        self.hold = self.rescale_dev = self.nonnaive = None
+        self._rescaled_day = -1
+        if any(self.rescaling):
+            dev = self.device
+            self.hold = torch.full((1,), HOLD_NONE, dtype=I32, device=dev)
+            self.rescale_dev = [torch.from_numpy(v.copy()).to(dev) for v in self.rescale_vecs]
+            self.nonnaive = torch.tensor([[0, -1, -1]] * len(self.specs), dtype=I64, device=dev)
+
+    def _reset_rescale(self):
+        if self.hold is None:
+            return
+        for k, sp in enumerate(self.specs):
+            if self.rescaling[k]:
+                self.rescale_vecs[k][:] = 1.0
+                self.rescale_dev[k].fill_(1.0)
+        self.hold.fill_(HOLD_NONE)
+        self.nonnaive.copy_(torch.tensor([[0, -1, -1]] * len(self.specs), dtype=I64))
+        self._rescaled_day = -1
+        if any(sched is not None for sched in self.import_sched):
+            self._build_imports()
+
+    def count_nonnaive(self, sim):
+        """Start the day check's count of agents not naive (after seeding)."""
+        if self.hold is None or not self.rescaling[sim]:
+            return
+        naive = (self.t['flags'][self.sl(sim)] >> STATE_BIT['naive']) & 1
+        m = int(self.specs[sim].n - int(naive.sum().item()))
+        self.nonnaive[sim] = torch.tensor([m, -1, -1], dtype=I64)
+
+    def held_day(self):
+        """The day a run was held back on (a due rescaling), or None."""
+        if self.hold is None:
+            return None
+        h = int(self.hold.item())
+        return None if h == HOLD_NONE else h
+
+    def rescale_day(self, t):
+        """sim.py:535-556 at the start of day t, for every sim that rescales
+        dynamically: when the agents not naive exceed rescale_threshold of the
+        population and the scale has room to grow, scale up by at least
+        rescale_factor and make that share of them naive again (agents drawn from
+        a PCG64 stream keyed by (seed, 0x5C5C, t)); importations are redrawn from
+        day t on. Clears the hold; the day check's counters restart from here."""
+        if self.hold is None or t <= self._rescaled_day:
+            return
+        for k, sp in enumerate(self.specs):
+            if not self.rescaling[k] or t >= sp.npts:
+                continue
+            p, vec = sp.pars, self.rescale_vecs[k]
+            naive = (self.t['flags'][self.sl(k)] >> STATE_BIT['naive']) & 1
+            not_naive = torch.nonzero(naive == 0).squeeze(1)
+            m = int(not_naive.numel())
+            pop_scale, current = float(p['pop_scale']), vec[t]
+            ratio = m / sp.n
+            if current < pop_scale and ratio > p['rescale_threshold']:
+                scaling = min(max(ratio / p['rescale_threshold'], p['rescale_factor']), pop_scale / current)
+                vec[t:] *= scaling
+                n_new = int(round(m * (1.0 - 1.0 / scaling)))
+                rng = np.random.Generator(np.random.PCG64([int(p['rand_seed']) & 0xFFFFFFFFFFFFFFFF, RESCALE_TAG, t]))
+                choices = torch.from_numpy(rng.choice(m, size=n_new, replace=False)).to(self.device)
+                self.make_naive(not_naive[choices], sim=k)
+                m -= n_new
+                self.rescale_dev[k].copy_(torch.from_numpy(vec))
+                if self.import_sched[k] is not None:
+                    self.import_sched[k][t:] = daily_importations(p['rand_seed'], p['n_imports'] / vec, sp.n,
+                                                                  sp.npts, start=t)
+                    self._upload_imports()
+                    self._refresh_state()
+            self.nonnaive[k] = torch.tensor([m, t - 1, t], dtype=I64)
+        self.hold.fill_(HOLD_NONE)
+        self._rescaled_day = t
+
+    def make_naive(self, inds, sim=0):
+        """people.py:378-412 make_naive (vaccination kept) for local indices (a
+        device tensor): states back to susceptible and naive, variant fields
+        undefined, immunity, NAb and vaccine fields of the unvaccinated zeroed,
+        every date but date_vaccinated and every duration undefined."""
+        t = self.t
+        g = inds.to(device=self.device, dtype=I64) + self.offsets[sim]
+        vacc_bit = 1 << STATE_BIT['vaccinated']
+        f = t['flags'][g]
+        t['flags'][g] = (f & vacc_bit) | SUS_NAIVE
+        t['vstate'][g] = (t['vstate'][g] & ~VSTATE_NONE) | VSTATE_NONE
+        nvx = g[(f & vacc_bit) == 0]
+        for k in ('sus_imm', 'symp_imm', 'sev_imm'):
+            t[k][:, nvx] = 0
+        for k in ('peak_nab', 'nab', 't_nab_event', 'vaccine_source'):
+            t[k][nvx] = 0
+        rows = [r for r, key in enumerate(cvd.DATES) if key != 'date_vaccinated']
+        t['dates'][torch.tensor(rows, device=self.device).unsqueeze(1), g.unsqueeze(0)] = float('nan')
+        t['durs'][:, g] = float('nan')
 
     def note_imports(self, sim, t, n):
         """Count variant importations (immunity.py:129) in the sim's ``n_imports``."""
@@ -478,6 +593,11 @@ class BatchState:
             r.n_variants = sp.nv
             r.n_layers = len(sp.layers)
             r.npts = sp.npts
+            r.pop_scale = float(p.get('pop_scale') or 1)
+            r.rescale_threshold = float(p.get('rescale_threshold') or 0)
+            if self.hold is not None and self.rescaling[s]:
+                r.rescale_vec = self.rescale_dev[s].data_ptr()
+                r.nonnaive = self.nonnaive[s].data_ptr()
             seed = int(p['rand_seed']) & 0xFFFFFFFFFFFFFFFF
             r.key0, r.key1 = seed & 0xFFFFFFFF, seed >> 32
             r.use_waning = int(bool(p['use_waning']))
@@ -594,6 +714,7 @@ class BatchState:
         if self.has_testing:
             for k in ('trace_bits', 'contact_bits', 'pending_quar', 'trace_count'):
                 setattr(st, k, t[k].data_ptr())
+        st.hold = self.hold.data_ptr() if self.hold is not None else None
         st.import_days = self.import_days
         if self.import_tabs is not None:
             st.import_day_off = self.import_tabs['day_off'].data_ptr()
@@ -780,9 +901,11 @@ class BatchState:
         self.t['status'].zero_()
         for a in self.import_variant:
             a[:] = 0
+        self._reset_rescale()
         if self.has_testing:
             for k in ('trace_bits', 'contact_bits', 'trace_count'):
                 self.t[k].zero_()
+        self._refresh_state()
 
     def checkpoint(self):
         """Device copy of the state at a day boundary (with the results so far),

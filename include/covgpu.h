@@ -162,6 +162,13 @@ typedef struct covgpu_sim_params {
   int64_t* res_fx;                /* [npts][COVGPU_N_RES_F] fixed-point sums         */
   covgpu_testing testing;
   int32_t seg_of_layer[COVGPU_MAX_LAYERS]; /* layer -> segment index (-1: no edges)   */
+  /* dynamic rescaling (sim.py:535-556; rescale_vec NULL: off). The day kernels
+   * only detect the day it is due; the host performs it (covgpu_state.hold) */
+  double pop_scale;
+  double rescale_threshold;
+  const double* rescale_vec;      /* [npts] current scale of each day               */
+  int64_t* nonnaive;              /* [3] agents not naive, the last day whose flows
+                                     are in that count, the last day checked        */
 } covgpu_sim_params;
 
 /* One contact layer of one sim (device memory, one entry per layer segment). */
@@ -294,6 +301,11 @@ typedef struct covgpu_state {
   const int32_t* import_sims;
   int32_t import_days;            /* days covered; 0: no importations                */
   int32_t _pad3;
+  /* the first day held back for a host step (a due rescaling, found by the
+   * day's rescale check); 0x7FFFFFFF: none. Every day kernel of a held day
+   * returns at once, the agent pass of the held day closes the day before it.
+   * NULL: no sim rescales dynamically */
+  int32_t* hold;
 } covgpu_state;
 
 /* ---- standalone kernels: the reference's numba functions ----------------- */
@@ -467,6 +479,14 @@ int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, i
  * Entries outside their sim's agents are skipped and set COVGPU_BADARG in the
  * device status word. */
 int covgpu_import_day(const covgpu_state* st, int32_t t, void* stream);
+
+/* The rescale check of day t (sim.py:535-547), run before the day's agent pass
+ * by covgpu_run_days when st->hold is set: for each sim with rescale_vec, the
+ * day's count of agents not naive (nonnaive[0] plus the first infections of
+ * the days since nonnaive[1]) and, unless day t was already checked
+ * (nonnaive[2] >= t), whether rescale_vec[t] < pop_scale and that count /
+ * n_agents > rescale_threshold; if so *st->hold = t (the earliest such day). */
+int covgpu_rescale_check(const covgpu_state* st, int32_t t, void* stream);
 
 /* Write the day-t endpoints of one dynamic layer segment into p1/p2 (the
  * same edges the edge pass draws that day). */

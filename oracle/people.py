@@ -171,6 +171,29 @@ class OraclePeople:
         self._pending = {}  # people.py:115 _pending_quarantine
         self.init_flows()
 
+    def make_naive(self, inds, reset_vx=False):
+        """people.py:378-412: states back to the initial ones (vaccination kept),
+        variant fields undefined, immunity, NAb and vaccine fields of the
+        unvaccinated zeroed, every date (but date_vaccinated) and duration undefined."""
+        inds = np.asarray(inds, dtype=np.int64)
+        for key in STATES:
+            if key in ('susceptible', 'naive'):
+                self[key][inds] = True
+            elif key != 'vaccinated' or reset_vx:
+                self[key][inds] = False
+        for key in VARIANT_STATES:
+            self[key][inds] = np.nan
+        for key in BY_VARIANT_STATES:
+            self[key][:, inds] = False
+        non_vx = inds if reset_vx else inds[~self.vaccinated[inds]]
+        for key in IMM_STATES:
+            self[key][:, non_vx] = 0
+        for key in NAB_STATES + VACC_STATES:
+            self[key][non_vx] = 0
+        for key in DATES + DURS:
+            if key != 'date_vaccinated' or reset_vx:
+                self[key][inds] = np.nan
+
     def __getitem__(self, key):
         return getattr(self, key)
 

@@ -40,6 +40,7 @@ CALL_IMPORT = 2
 SEED_INFECTION_TAG = 0x5EED
 IMPORT_TAG = 0x1B1B
 NONNAIVE_TAG = 0x4A4A
+RESCALE_TAG = 0x5C5C
 
 
 def choose_seed_infections(seed, n, k):
@@ -114,6 +115,9 @@ class OracleSim:
             if hasattr(iv, 'initialize'):
                 iv.initialize(self)
         self.t = 0
+        # sim.py:342-346: the scale of each day, 1 to start with when rescaling dynamically
+        pop_scale = pars.get('pop_scale') or 1
+        self.rescale_vec = (1.0 if pars.get('rescale', True) else float(pop_scale)) * np.ones(self.npts)
         self.results = {}
         for key in FLOWS + [f'n_{k}' for k in RESULT_STOCKS] + ['n_imports', 'pop_nabs', 'pop_protection',
                                                                 'pop_symp_protection']:
@@ -154,6 +158,30 @@ class OracleSim:
                 inds = self.rs_numba.choice(self.n, int(p['pop_infected']), replace=False)
             self.people.infect(inds=inds, layer='seed_infection', draws=self._draws(CALL_SEED))
 
+    def rescale(self):
+        """sim.py:535-556: once the agents not naive exceed rescale_threshold of the
+        population (and the scale has room to grow), scale up by at least
+        rescale_factor and make that share of them naive again."""
+        p = self.pars
+        if not p.get('rescale', True):
+            return
+        pop_scale = p.get('pop_scale') or 1
+        current = self.rescale_vec[self.t]
+        if current < pop_scale:
+            not_naive = np.nonzero(~self.people.naive)[0]
+            m = len(not_naive)
+            ratio = m / self.n
+            if ratio > p['rescale_threshold']:
+                scaling = min(max(ratio / p['rescale_threshold'], p['rescale_factor']), pop_scale / current)
+                self.rescale_vec[self.t:] *= scaling
+                k = int(round(m * (1.0 - 1.0 / scaling)))
+                if self.rng == 'philox':
+                    rng = np.random.Generator(np.random.PCG64([self.seed & 0xFFFFFFFFFFFFFFFF, RESCALE_TAG, self.t]))
+                    choices = rng.choice(m, size=k, replace=False)
+                else:  # cvu.choose: numba's stream, int32 arguments
+                    choices = self.rs_numba.choice(int(np.int32(m)), int(np.int32(k)), replace=False)
+                self.people.make_naive(not_naive[choices])
+
     def update_contacts(self):
         """people.py:199-206 -> base.py:1849-1876 (Layer.update, frac=1)."""
         for li, lkey in enumerate(self.layer_keys):
@@ -175,15 +203,17 @@ class OracleSim:
         people = self.people
         if t == 0:
             self.init_infections()
+        self.rescale()
         people.update_states_pre(t=t)
         self.update_contacts()
         hosp_max = people.severe.sum() > p['n_beds_hosp'] if p['n_beds_hosp'] is not None else False
         icu_max = people.critical.sum() > p['n_beds_icu'] if p['n_beds_icu'] is not None else False
         if p.get('n_imports'):  # sim.py:582-587
+            rate = p['n_imports'] / self.rescale_vec[t]
             if self.rng == 'philox':
-                inds = philox_mode_importations(self.seed, p['n_imports'], self.n, t)
+                inds = philox_mode_importations(self.seed, rate, self.n, t)
             else:  # cvu.poisson / cvu.choose are numba functions: numba's stream; the rate is typed float32
-                k = int(self.rs_numba.poisson(float(F32(p['n_imports'])), 1)[0])
+                k = int(self.rs_numba.poisson(float(F32(rate)), 1)[0])
                 inds = self.rs_numba.choice(self.n, k, replace=False) if k > 0 else np.zeros(0, dtype=np.int64)
             if len(inds):
                 people.infect(inds=inds, hosp_max=hosp_max, icu_max=icu_max, layer='importation',

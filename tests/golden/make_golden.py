@@ -371,7 +371,11 @@ def make_sims_fixture(ref):
     cases = [('random', 1500, 40, 3, 0, {}), ('hybrid', 1500, 50, 4, 0, {}), ('hybrid', 1200, 45, 9, 1, {}),
              ('hybrid', 1500, 45, 12, 1, dict(n_imports=0.7)), ('random', 1200, 40, 13, 0, dict(n_imports=3)),
              ('hybrid', 1500, 45, 14, 0, dict(frac_susceptible=0.55)),
-             ('random', 1300, 40, 15, 0, dict(frac_susceptible=0.8, n_imports=1.5, pop_infected=40))]
+             ('random', 1300, 40, 15, 0, dict(frac_susceptible=0.8, n_imports=1.5, pop_infected=40)),
+             # dynamic rescaling (sim.py:535-556), with importations scaled by it, and a fixed scale
+             ('hybrid', 2000, 60, 16, 0, dict(pop_scale=10, pop_infected=20)),
+             ('random', 1500, 50, 17, 0, dict(pop_scale=4, n_imports=2, rescale_factor=1.5, rescale_threshold=0.1)),
+             ('random', 1200, 40, 18, 0, dict(pop_scale=3, rescale=False, n_imports=3))]
     for i, (pop_type, n, days, seed, dyn, extra) in enumerate(cases):
         pars = ref.make_pars(pop_size=n, n_days=days, pop_type=pop_type, rand_seed=seed, **extra)
         if dyn:
@@ -393,6 +397,7 @@ def make_sims_fixture(ref):
                 out[f's{i}.res.{k}'] = v
         for k in ('exposed', 'recovered', 'dead', 'susceptible', 'date_recovered', 'peak_nab', 'nab'):
             out[f's{i}.final.{k}'] = sim.people[k].copy()
+        out[f's{i}.rescale_vec'] = sim.rescale_vec.copy()
     out['n'] = np.array(len(cases))
     np.savez_compressed(os.path.join(HERE, 'ref_sims.npz'), **out)
     print('ref_sims.npz written')

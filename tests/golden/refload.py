@@ -422,7 +422,7 @@ class RefSim:
         self.npts = int(pars['n_days']) + 1
         self.complete = False
         self._legacy_trans = False
-        self.rescale_vec = np.ones(self.npts)
+        self.rescale_vec = (1.0 if pars['rescale'] else pars['pop_scale']) * np.ones(self.npts)  # sim.py:342-346
         if pars['use_waning']:
             ref.cvi.init_immunity(self)
         cvd = ref.cvd

@@ -101,6 +101,58 @@ def test_sim_with_nonnaive_fraction_matches_oracle_philox(frac, rate):
     np.testing.assert_array_equal(batch.results(0)['new_infections'], sim.raw_results()['new_infections'])
 
 
+@pytest.mark.parametrize('pop_type,n,days,extra', [
+    ('hybrid', 3000, 60, dict(pop_scale=10, pop_infected=30)),
+    ('random', 2500, 50, dict(pop_scale=4, n_imports=2, rescale_factor=1.5, rescale_threshold=0.1)),
+    ('hybrid', 2000, 40, dict(pop_scale=3, rescale=False, n_imports=3))])
+def test_rescaling_matches_oracle_philox(pop_type, n, days, extra):
+    """sim.py:535-556 dynamic rescaling (the day kernels hold the run back on the
+    day one falls due, the host performs it), importations at the day's scale,
+    and finalize's scaling of the results (sim.py:771-787, 838-839)."""
+    pars = dict(pop_type=pop_type, pop_size=n, n_days=days, rand_seed=21, **extra)
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim).run()
+    sim.run()
+    compare_runs(sim, orc, keys=RES_KEYS + ['n_imports'])
+    np.testing.assert_array_equal(sim.rescale_vec, orc.rescale_vec)
+    if extra.get('rescale', True):
+        assert len(np.unique(orc.rescale_vec)) > 2
+    raw = sim.raw_results()
+    np.testing.assert_allclose(sim.results['new_infections'].values, raw['new_infections'] * orc.rescale_vec)
+    np.testing.assert_allclose(sim.results['n_alive'].values[-1],
+                               n * sim['pop_scale'] - sim.results['cum_deaths'].values[-1])
+    stepped = cv.Sim(pars)
+    stepped.initialize()
+    for _ in range(stepped.npts):
+        stepped.step()
+    stepped.finalize()
+    for k in RES_KEYS + ['n_imports']:
+        np.testing.assert_array_equal(stepped.raw_results()[k], raw[k], err_msg=k)
+    np.testing.assert_array_equal(stepped.rescale_vec, sim.rescale_vec)
+
+
+def test_batch_with_rescaling_equals_single_runs():
+    mk = [dict(pop_type='random', pop_size=2500, n_days=45, rand_seed=3, pop_scale=8),
+          dict(pop_type='random', pop_size=1800, n_days=45, rand_seed=4),
+          dict(pop_type='hybrid', pop_size=3000, n_days=45, rand_seed=5, pop_scale=5, n_imports=1.5)]
+    singles = [cv.Sim(dict(p)).run() for p in mk]
+    batch = cv.BatchSim([cv.Sim(dict(p)) for p in mk]).run()
+    finals = batch.finalize()
+    for k, single in enumerate(singles):
+        got = batch.results(k)
+        for key in RES_KEYS + ['n_imports']:
+            np.testing.assert_array_equal(got[key], single.raw_results()[key], err_msg=f'sim {k} {key}')
+        for key in ('new_infections', 'cum_infections', 'n_alive', 'n_susceptible'):
+            np.testing.assert_array_equal(finals[k].results[key].values, single.results[key].values, err_msg=key)
+    again = cv.Sim(dict(mk[0]))
+    again.initialize()
+    snap = again.state.snapshot()
+    again.run()
+    again.rewind(snap).run()  # a rerun from a snapshot starts from scale 1 again
+    np.testing.assert_array_equal(again.results['new_infections'].values, singles[0].results['new_infections'].values)
+
+
 def test_step_mode_equals_graph_run():
     pars = dict(pop_type='hybrid', pop_size=3000, n_days=30, rand_seed=7)
     a = cv.Sim(pars).run()

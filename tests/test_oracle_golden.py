@@ -102,6 +102,8 @@ def test_whole_runs_match_reference_mt_mode():
             np.testing.assert_allclose(v, ref, rtol=1e-12, atol=0, err_msg=f'sim {i} {k}')
         for k in ('exposed', 'recovered', 'dead', 'susceptible', 'date_recovered', 'peak_nab', 'nab'):
             assert np.array_equal(sim.people[k], d[f's{i}.final.{k}'], equal_nan=True), (i, k)
+        np.testing.assert_array_equal(sim.rescale_vec, d[f's{i}.rescale_vec'], err_msg=f'sim {i} rescale_vec')
+    assert len(np.unique(d['s7.rescale_vec'])) > 10  # a run that rescales many times
 
 
 def test_testing_and_tracing_runs_match_reference_mt_mode():
