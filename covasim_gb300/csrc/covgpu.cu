@@ -241,7 +241,8 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
                                         sp.frac_time, sp.load_ratio, sp.high_cap);
         st.viral_load[i] = vl;
         src_bit = (rt != 0.0f && iv < (uint32_t)nv) ? 1u : 0u;
-        if (src_bit) reinterpret_cast<float4*>(st.src_rec)[i] = make_float4(rt, vl, __uint_as_float(vs), 0.0f);
+        if (src_bit)
+          reinterpret_cast<float4*>(st.src_rec)[i] = make_float4(rt, vl, __uint_as_float(vs), __uint_as_float(f));
       }
       // exclusive by construction (the infectious are never susceptible); the edge
       // pass relies on it to queue at most one direction per edge
@@ -424,7 +425,7 @@ template <bool LIK>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
                                          int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
   const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
-  const uint32_t fs = __ldg(st.flags + s), fg = __ldg(st.flags + g);
+  const uint32_t fs = __float_as_uint(sr.w), fg = __ldg(st.flags + g);
   const float rs = __ldg(st.rel_sus + g);
   const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
   const float rt = sr.x, vl = sr.y;

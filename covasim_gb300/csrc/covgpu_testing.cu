@@ -260,6 +260,8 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
       c_iso = 1;
     }
     if (f != f_in) st.flags[i] = f;
+    // a source's record carries its flags to the edge pass: keep its quarantine / isolation current
+    if (((f ^ f_in) & (B_QUAR | B_ISO)) && ((st.roles[i >> 5] >> (i & 31)) & 1u)) st.src_rec[4 * i + 3] = __uint_as_float(f);
   }
   const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
                  ci = __reduce_add_sync(0xffffffffu, c_iso);

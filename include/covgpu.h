@@ -262,7 +262,8 @@ typedef struct covgpu_state {
   uint32_t* roles;                /* [2][ceil(n/32)]: source bitmap, target bitmap    */
   uint64_t* claim;                /* [n] first-infector claim (day-tagged)           */
   float* src_rec;                 /* [n][4] per source, written by the agent pass for
-                                     the edge pass: rel_trans, viral load, vstate bits */
+                                     the edge pass: rel_trans, viral load, vstate bits,
+                                     flags bits (the post pass updates the last) */
   covgpu_event* events;           /* [event_capacity]                                */
   int64_t event_capacity;
   unsigned long long* event_count;/* device counter                                  */
