@@ -136,7 +136,7 @@ class State(C.Structure):
         ('lik', Lik),
         ('import_day_off', C.c_void_p), ('imports', C.c_void_p), ('import_sims', C.c_void_p),
         ('import_days', C.c_int32), ('_pad3', C.c_int32),
-        ('hold', C.c_void_p),
+        ('hold', C.c_void_p), ('tgt_rec', C.c_void_p),
     ]
 
 

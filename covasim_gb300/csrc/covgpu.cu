@@ -192,6 +192,12 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       }
       vs = (vs & 0xFF000000u) | (rv << 16) | (iv << 8) | ev;
 
+      // an edge-pass target (susceptible, rel_sus nonzero) gets its susceptibility per
+      // variant, rel_sus * (1 - sus_imm[v]) as compute_trans_sus forms it unquarantined
+      // (utils.py:87), with the sign bit set when quarantined
+      const float rs = (f & B_SUS) ? st.rel_sus[i] : 0.0f;
+      const bool is_tgt = rs != 0.0f;
+      const uint32_t tq = (f & B_QUAR) ? 0x80000000u : 0u;
       if (sp.use_waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
         const float dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
         const bool was_inf = tf >= dr;  // false for NaN
@@ -226,6 +232,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
           st.sus_imm[off] = a;
           st.symp_imm[off] = b;
           st.sev_imm[off] = c;
+          if (is_tgt) st.tgt_rec[off] = __uint_as_float(__float_as_uint(__fmul_rn(rs, __fsub_rn(1.0f, a))) | tq);
           sus_fx += __float2ll_rn(__fmul_rn(a, 4294967296.0f));
           symp_fx += __float2ll_rn(__fmul_rn(b, 4294967296.0f));
         }
@@ -246,7 +253,14 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       }
       // exclusive by construction (the infectious are never susceptible); the edge
       // pass relies on it to queue at most one direction per edge
-      if ((f & B_SUS) && !src_bit && st.rel_sus[i] != 0.0f) tgt_bit = 1u;
+      if (is_tgt) {
+        tgt_bit = 1u;
+        if (!sp.use_waning)
+          for (int v = 0; v < nv; ++v) {
+            const int64_t off = (int64_t)v * st.n + i;
+            st.tgt_rec[off] = __uint_as_float(__float_as_uint(__fmul_rn(rs, __fsub_rn(1.0f, st.sus_imm[off]))) | tq);
+          }
+      }
       if (f != f_in) st.flags[i] = f;
       if (vs != vs_in) st.vstate[i] = vs;
     }
@@ -425,14 +439,24 @@ template <bool LIK>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
                                          int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
   const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
-  const uint32_t fs = __float_as_uint(sr.w), fg = __ldg(st.flags + g);
-  const float rs = __ldg(st.rel_sus + g);
+  const uint32_t fs = __float_as_uint(sr.w);
   const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
   const float rt = sr.x, vl = sr.y;
   const uint32_t v = (__float_as_uint(sr.z) >> 8) & 0xFFu;
   const uint32_t vc = v < (uint32_t)c.nv ? v : 0u;
-  const float si = __ldg(st.sus_imm + (int64_t)vc * st.n + g);
+  const int64_t gv = (int64_t)vc * st.n + g;
   const float beta = __ldg(c.beta_t + vc);
+  // the target: its record (rel_sus * (1 - sus_imm), sign bit = quarantined); the
+  // quarantined, and the likelihood's terms, take the fields themselves
+  const uint32_t tr = __float_as_uint(__ldg(st.tgt_rec + gv));
+  const bool tquar = tr >> 31;
+  uint32_t fg = tquar ? B_QUAR : 0u;
+  float rs = 0.0f, si = 0.0f;
+  if (LIK || tquar) {
+    fg = __ldg(st.flags + g);
+    rs = __ldg(st.rel_sus + g);
+    si = __ldg(st.sus_imm + gv);
+  }
   if (v >= (uint32_t)c.nv) return false;
   float rte = rt;
   if (fs & B_QUAR) rte = __fmul_rn(rte, c.quar_factor);
@@ -440,9 +464,8 @@ __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c
   if (fs & B_ISO) rte = __fmul_rn(rte, c.iso_factor);
   rte = __fmul_rn(rte, c.beta_layer);
   rte = __fmul_rn(rte, vl);
-  float rse = rs;
-  if (fg & B_QUAR) rse = __fmul_rn(rse, c.quar_factor);
-  rse = __fmul_rn(rse, __fsub_rn(1.0f, si));
+  float rse = __uint_as_float(tr & 0x7FFFFFFFu);
+  if (tquar) rse = __fmul_rn(__fmul_rn(rs, c.quar_factor), __fsub_rn(1.0f, si));
   const float p = __fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), rse);
   if (p == 0.0f) return false;
   v_out = v;
@@ -1432,6 +1455,7 @@ namespace covgpu {
 int check_state(const covgpu_state* st) {
   if (!st || st->n <= 0 || st->n_sims <= 0 || st->n_agent_blocks <= 0) return COVGPU_BADARG;
   if (!st->flags || !st->vstate || !st->sims || !st->agent_blocks || !st->roles || !st->claim || !st->src_rec ||
+      !st->tgt_rec ||
       !st->events ||
       !st->event_count || !st->status)
     return COVGPU_BADARG;

@@ -262,6 +262,12 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
     if (f != f_in) st.flags[i] = f;
     // a source's record carries its flags to the edge pass: keep its quarantine / isolation current
     if (((f ^ f_in) & (B_QUAR | B_ISO)) && ((st.roles[i >> 5] >> (i & 31)) & 1u)) st.src_rec[4 * i + 3] = __uint_as_float(f);
+    // and a target's record carries its quarantine in the sign bit
+    if (((f ^ f_in) & B_QUAR) && ((st.roles[words + (i >> 5)] >> (i & 31)) & 1u))
+      for (int v = 0; v < sp.n_variants; ++v) {
+        uint32_t* r = reinterpret_cast<uint32_t*>(st.tgt_rec + (int64_t)v * st.n + i);
+        *r = (f & B_QUAR) ? (*r | 0x80000000u) : (*r & 0x7FFFFFFFu);
+      }
   }
   const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
                  ci = __reduce_add_sync(0xffffffffu, c_iso);

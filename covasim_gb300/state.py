@@ -224,6 +224,7 @@ class BatchState:
         t['roles'] = torch.zeros(2 * ((n + 31) // 32), dtype=I32, device=dev)
         t['claim'] = torch.full((n,), -1, dtype=I64, device=dev)
         t['src_rec'] = torch.zeros((n, 4), dtype=F32, device=dev)  # the edge pass's record of each source
+        t['tgt_rec'] = torch.zeros((self.nv_max, n), dtype=F32, device=dev)  # and of each target
         n_real = sum(sp.n for sp in self.specs)
         self.event_capacity = int(event_capacity or (2 * n_real + 65536))
         t['events'] = torch.zeros((self.event_capacity, 4), dtype=I32, device=dev)
@@ -695,7 +696,7 @@ class BatchState:
         st.edge_resident = int(self.edge_resident)
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
-                  'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'src_rec',
+                  'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'src_rec', 'tgt_rec',
                   'events', 'event_count',
                   'log_count', 'status'):
             setattr(st, k, t[k].data_ptr())

@@ -307,6 +307,10 @@ typedef struct covgpu_state {
    * returns at once, the agent pass of the held day closes the day before it.
    * NULL: no sim rescales dynamically */
   int32_t* hold;
+  float* tgt_rec;                 /* [imm_stride_variants][n] per edge-pass target,
+                                     written by the agent pass: rel_sus * (1 - sus_imm[v])
+                                     with the sign bit set when quarantined (the post
+                                     pass updates the sign)                          */
 } covgpu_state;
 
 /* ---- standalone kernels: the reference's numba functions ----------------- */
