@@ -41,8 +41,9 @@ POP = 1_000_000
 DAYS = 180
 PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
 # DRAM bytes (read + write) of one edge-pass launch on this workload, from an
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of day 90 of the 1M run
-MEASURED_TRAFFIC = {('edge_pass', 1_000_000): 90_250_240}
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of day 90 of the 1M run,
+# resident edge pass with 8192-edge tiles
+MEASURED_TRAFFIC = {('edge_pass', 1_000_000): 82_782_208}
 
 
 def parse():
