@@ -96,3 +96,44 @@ def test_reporting_on_a_device_run():
     np.testing.assert_allclose(got, want, rtol=1e-12, equal_nan=True)
     g = sim.compute_gen_time()
     assert 2 < g['true'] < 10
+
+
+def test_testing_with_rescaling_and_importations_matches_oracle_philox():
+    """The held day of a dynamic rescaling (sim.py:535-556) skips the testing,
+    tracing and post passes too; daily importations at the day's scale."""
+    tp, ct = dict(symp_prob=0.2, asymp_prob=0.01), dict(trace_probs=0.5, trace_time=1)
+    pars = dict(pop_type='hybrid', pop_size=3000, n_days=50, rand_seed=8, pop_infected=20, pop_scale=6,
+                n_imports=2, dynam_layer=dict(h=0, s=0, w=0, c=1),
+                interventions=[cv.test_prob(**tp), cv.contact_tracing(**ct)])
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim)
+    orc.interventions = [TestProb(**tp), ContactTracing(**ct)]
+    for iv in orc.interventions:
+        if hasattr(iv, 'initialize'):
+            iv.initialize(orc)
+    orc.run()
+    assert len(np.unique(orc.rescale_vec)) > 3
+    sim.run()
+    compare_runs(sim, orc, keys=TESTING_KEYS + ['n_imports'])
+    np.testing.assert_array_equal(sim.rescale_vec, orc.rescale_vec)
+
+
+def test_rescaling_with_variant_importations_graph_step_and_batch_agree():
+    """Variant days run as single steps (with their own rescale check) between
+    graph segments that may be held back for a rescaling."""
+    def make(seed):
+        return cv.Sim(pop_type='hybrid', pop_size=3000, n_days=45, rand_seed=seed, pop_scale=8, use_waning=True,
+                      variants=[cv.variant(dict(rel_beta=1.6), days=[12, 25], n_imports=10, label='v')])
+    a = make(4).run()
+    b = make(4)
+    b.initialize()
+    for _ in range(b.npts):
+        b.step()
+    b.finalize()
+    batch = cv.BatchSim([make(4), make(5)]).run()
+    for k in RES_KEYS + ['n_imports', 'new_infections_by_variant']:
+        np.testing.assert_array_equal(a.raw_results()[k], b.raw_results()[k], err_msg=k)
+        np.testing.assert_array_equal(a.raw_results()[k], batch.results(0)[k], err_msg=k)
+    np.testing.assert_array_equal(a.rescale_vec, b.rescale_vec)
+    assert len(np.unique(a.rescale_vec)) > 2 and a.raw_results()['new_infections_by_variant'][1].sum() > 0
