@@ -152,3 +152,30 @@ def test_daily_importations_schedule():
     assert [len(d) for d in daily_importations(8, 2.5, 1000, 50)] != list(counts[:50])
     with pytest.raises(ValueError):
         daily_importations(1, 50, 5, 3)
+
+
+def test_importation_redraw_from_a_day_and_variant_counts():
+    """After a rescaling on day s the schedule is redrawn from s on with the new
+    rates: the days before s keep their draws, the redrawn days equal a full draw
+    with the new rates; a variant's importations at a scale (immunity.py:121-124)."""
+    from covasim_gb300.state import daily_importations
+    from covasim_gb300.sim import variant_import_count
+    n, npts, s = 5000, 60, 25
+    rates = np.full(npts, 4.0)
+    full = daily_importations(3, rates, n, npts)
+    rates[s:] /= 2.5
+    tail = daily_importations(3, rates, n, npts, start=s)
+    again = daily_importations(3, rates, n, npts)
+    assert len(tail) == npts - s
+    for t in range(npts):
+        np.testing.assert_array_equal(again[t], full[t] if t < s else tail[t - s])
+    assert sum(len(d) for d in tail) < sum(len(d) for d in full[s:])
+
+    class V:
+        n_imports, rescale = 10, True
+    rng = np.random.default_rng(1)
+    assert variant_import_count(V, 1.0, rng) == 10 and variant_import_count(V, 2.0, rng) == 5
+    counts = [variant_import_count(V, 3.0, np.random.default_rng(k)) for k in range(2000)]
+    assert set(counts) == {3, 4} and abs(np.mean(counts) - 10 / 3) < 0.05
+    V.rescale = False
+    assert variant_import_count(V, 3.0, rng) == 10
