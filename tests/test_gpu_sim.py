@@ -132,6 +132,19 @@ def test_rescaling_matches_oracle_philox(pop_type, n, days, extra):
     np.testing.assert_array_equal(stepped.rescale_vec, sim.rescale_vec)
 
 
+def test_rescaling_resume_until_equals_one_run():
+    """run(until=...) then run() with rescalings held back inside both segments."""
+    pars = dict(pop_type='random', pop_size=3000, n_days=50, rand_seed=14, pop_scale=10, n_imports=1)
+    a = cv.Sim(pars).run()
+    b = cv.Sim(pars)
+    b.run(until=23)
+    b.run()
+    for k in RES_KEYS + ['n_imports']:
+        np.testing.assert_array_equal(a.raw_results()[k], b.raw_results()[k], err_msg=k)
+    np.testing.assert_array_equal(a.rescale_vec, b.rescale_vec)
+    assert (a.rescale_vec[:23] < a.rescale_vec[-1]).all() and len(np.unique(a.rescale_vec[23:])) > 1
+
+
 def test_batch_with_rescaling_equals_single_runs():
     mk = [dict(pop_type='random', pop_size=2500, n_days=45, rand_seed=3, pop_scale=8),
           dict(pop_type='random', pop_size=1800, n_days=45, rand_seed=4),
