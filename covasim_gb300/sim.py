@@ -327,7 +327,7 @@ class Sim:
                 pars[k2] = pars.pop(k1)
         if pars.get('pop_type'):
             cvpar.reset_layer_pars(pars, force=False)
-        if pars.get('prog_by_age') is not None:
+        if pars.get('prog_by_age'):  # base.py:278-279: a truthy prog_by_age resets the prognoses
             pars['prognoses'] = cvpar.get_prognoses(by_age=pars['prog_by_age'])
         unknown = [k for k in pars if k not in self.pars]
         if unknown:

@@ -238,6 +238,35 @@ def test_exposed_to_infectious_delay_exact(delay):
     assert ch[delay] == 500 and ch[:delay].sum() == 0
 
 
+@pytest.mark.parametrize('dur', [1, 2, 5, 10, 20])
+def test_recovery_day_exact(dur):
+    """tests/unittests/test_progression.py:54-80: infectious after 1 day, all
+    asymptomatic, asym2rec `dur` days with std 0 => all recover on day 1 + dur."""
+    pars = cv.make_pars(pop_size=500, pop_infected=500, n_days=30)
+    pars['dur']['exp2inf'] = dict(dist='normal', par1=1, par2=0)
+    pars['dur']['asym2rec'] = dict(dist='normal', par1=dur, par2=0)
+    pars['rel_symp_prob'] = 0
+    ch = cv.Sim(pars).run().results['new_recoveries'].values
+    assert ch[1 + dur] == 500 and ch.sum() == 500
+
+
+@pytest.mark.parametrize('dur', [1, 2, 5, 10, 20])
+def test_time_to_die_exact(dur):
+    """tests/unittests/test_progression.py:83-108: everyone critical on day 0
+    (certain prognoses, no delays), crit2die `dur` days with std 0 => all die on day dur."""
+    pars = cv.make_pars(pop_size=500, pop_infected=500, n_days=30)
+    for k in ('exp2inf', 'inf2sym', 'sym2sev', 'sev2crit'):
+        pars['dur'][k] = dict(dist='normal', par1=0, par2=0)
+    pars['dur']['crit2die'] = dict(dist='normal', par1=dur, par2=0)
+    sim = cv.Sim(pars)
+    progs = cv.get_prognoses(sim['prog_by_age'])  # set after creation: a pars dict with prog_by_age resets them
+    for k in ('symp_probs', 'severe_probs', 'crit_probs', 'death_probs'):
+        progs[k][:] = 1.0
+    sim['prognoses'] = progs
+    ch = sim.run().results['new_deaths'].values
+    assert ch[dur] == 500 and ch.sum() == 500
+
+
 def test_everyone_dies_with_certain_death():
     """tests/unittests/test_mortality.py:13-24."""
     pars = cv.make_pars(pop_size=400, pop_infected=400, n_days=60)
