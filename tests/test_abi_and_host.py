@@ -46,6 +46,10 @@ def test_entry_points_reject_bad_arguments_without_a_gpu():
     assert lib.covgpu_run_days(None, 0, 10, 0, 1, 1, None) == L.BADARG
     st = L.State()
     assert lib.covgpu_edge_pass(C.pointer(st), 0, None) == L.BADARG
+    assert lib.covgpu_import_day(None, 0, None) == L.BADARG
+    assert lib.covgpu_import_day(C.pointer(st), 0, None) == L.BADARG
+    assert lib.covgpu_rescale_check(None, 0, None) == L.BADARG
+    assert lib.covgpu_rescale_check(C.pointer(st), 0, None) == L.BADARG
 
 
 def _same(got, want, path):
