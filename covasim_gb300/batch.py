@@ -84,8 +84,10 @@ class BatchSim:
                     rng = np.random.default_rng([int(s['rand_seed']), 0x1A1A, t, v.index])
                     n_imp = min(variant_import_count(v, self.state.rescale_vecs[k][t], rng), len(sus))
                     inds = rng.choice(sus, n_imp, replace=False)
+                    self.state.set_hospicu([[0, 0]] * len(self.sims))  # variant.apply: no bed limits
                     self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.LOG_IMPORT,
                                            call_tag=CALL_IMPORT + v.index)
+                    self.state.set_hospicu(None)
                     self.state.note_imports(k, t, len(inds))
 
     def run(self, use_graph=None):

@@ -523,8 +523,10 @@ class Sim:
                 rng = np.random.default_rng([int(self['rand_seed']), 0x1A1A, t, v.index])
                 n_imp = min(variant_import_count(v, self.state.rescale_vecs[0][t], rng), len(sus))
                 inds = rng.choice(sus, n_imp, replace=False)
+                self.state.set_hospicu([[0, 0]])  # variant.apply calls infect() without bed limits
                 self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.LOG_IMPORT,
                                        call_tag=CALL_IMPORT + v.index)
+                self.state.set_hospicu(None)
                 self.state.note_imports(0, t, n_imp)
 
     def step(self):

@@ -182,6 +182,22 @@ class OracleSim:
                     choices = self.rs_numba.choice(int(np.int32(m)), int(np.int32(k)), replace=False)
                 self.people.make_naive(not_naive[choices])
 
+    def _import_variant(self, v, t):
+        """immunity.py:117-130 in philox mode (the CUDA library's host draws): n_imports
+        over the day's scale, rounded at random, agents chosen among the susceptible
+        from a PCG64 stream keyed by (seed, 0x1A1A, day, variant); infect() without
+        bed limits, as variant.apply calls it."""
+        if self.rng != 'philox':
+            raise NotImplementedError('variant importations are replayed in philox mode only')
+        sus = np.nonzero(self.people.susceptible)[0]
+        rng = np.random.default_rng([self.seed, 0x1A1A, t, v.index])
+        x = v.n_imports / (self.rescale_vec[t] if getattr(v, 'rescale', True) else 1.0)
+        n_imp = min(int(x) if x == int(x) else int(np.floor(x + rng.random())), len(sus))
+        inds = rng.choice(sus, n_imp, replace=False)
+        if len(inds):
+            self.people.infect(inds=inds, layer='importation', variant=v.index, draws=self._draws(CALL_IMPORT + v.index))
+        self.results['n_imports'][t] += n_imp
+
     def update_contacts(self):
         """people.py:199-206 -> base.py:1849-1876 (Layer.update, frac=1)."""
         for li, lkey in enumerate(self.layer_keys):
@@ -219,6 +235,9 @@ class OracleSim:
                 people.infect(inds=inds, hosp_max=hosp_max, icu_max=icu_max, layer='importation',
                               draws=self._draws(CALL_IMPORT))
                 self.results['n_imports'][t] += len(inds)
+        for v in p.get('variants') or []:  # sim.py:590-592 -> immunity.py:117-130 variant.apply
+            if t in np.atleast_1d(v.days):
+                self._import_variant(v, t)
         if self.beta_schedule is not None:
             p['beta'] = self.beta_schedule[t]
         for iv in self.interventions:  # sim.py:596-598

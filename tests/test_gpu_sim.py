@@ -166,6 +166,25 @@ def test_batch_with_rescaling_equals_single_runs():
     np.testing.assert_array_equal(again.results['new_infections'].values, singles[0].results['new_infections'].values)
 
 
+def test_sim_with_variants_matches_oracle_philox():
+    """Variant importations (immunity.py:117-130) with bed limits in force: the
+    importations take no limits (variant.apply calls infect() without them),
+    transmission does; per-variant flows against the oracle."""
+    pars = dict(pop_type='hybrid', pop_size=4000, n_days=50, rand_seed=31, use_waning=True, pop_infected=40,
+                n_beds_hosp=3, n_beds_icu=1, n_imports=1, dynam_layer=dict(h=0, s=0, w=0, c=1),
+                variants=[cv.variant(dict(rel_beta=1.6, rel_severe_prob=2.0), days=10, n_imports=20, label='v1'),
+                          cv.variant(dict(rel_beta=1.3), days=[20, 21], n_imports=8, label='v2')])
+    sim = cv.Sim(pars)
+    sim.initialize()
+    orc = oracle_for(sim).run()
+    sim.run()
+    compare_runs(sim, orc, keys=RES_KEYS + ['n_imports'])
+    raw = sim.raw_results()
+    for k in ('new_infections_by_variant', 'new_severe_by_variant'):
+        np.testing.assert_array_equal(raw[k], orc.results[k], err_msg=k)
+    assert (raw['new_infections_by_variant'][1:].sum(axis=1) > 20).all()
+
+
 def test_step_mode_equals_graph_run():
     pars = dict(pop_type='hybrid', pop_size=3000, n_days=30, rand_seed=7)
     a = cv.Sim(pars).run()
