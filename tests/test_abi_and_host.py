@@ -183,3 +183,16 @@ def test_importation_redraw_from_a_day_and_variant_counts():
     assert set(counts) == {3, 4} and abs(np.mean(counts) - 10 / 3) < 0.05
     V.rescale = False
     assert variant_import_count(V, 3.0, rng) == 10
+
+
+def test_infection_log_layer_tags_round_trip():
+    """people.py:508-511 records the infect() call's layer: contact layers by index,
+    seed infections, importations, None and other labels by their own tags."""
+    from covasim_gb300.people import log_layer_tag, log_layer_label
+    keys, extra = ['h', 's', 'w', 'c'], []
+    for layer in keys + ['seed_infection', 'importation', None, 'custom', 'other', 'custom']:
+        tag = log_layer_tag(layer, keys, extra)
+        assert 0 <= tag <= 0xFF and log_layer_label(tag, keys, extra) == layer
+    assert extra == ['custom', 'other']
+    assert log_layer_tag('seed_infection', keys, extra) == L.LOG_SEED
+    assert log_layer_tag('importation', keys, extra) == L.LOG_IMPORT
