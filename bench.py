@@ -54,11 +54,14 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--pop-size', type=int, default=POP)
     ap.add_argument('--days', type=int, default=DAYS)
-    ap.add_argument('--cpu-days', type=int, default=3, help='days of the CPU oracle sample')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--batch', type=int, default=16, help='sims of the batched measurement (0: skip)')
     ap.add_argument('--no-adjoint', action='store_true', help='skip the forward/adjoint cost measurement')
+    ap.add_argument('--no-large', action='store_true',
+                    help='skip the 20M-agent, 365-day measurement (one run, device population) in the default line')
+    ap.add_argument('--no-batch256', action='store_true',
+                    help='skip the 256-sim batched measurement (batched vs one by one) in the default line')
     ap.add_argument('--edge-tile', default='auto',
                     help="edge-pass tile (1024/2048/4096/8192, suffix 'r' for the resident bitmap) or 'auto' (autotuner)")
     ap.add_argument('--seeds', type=int, default=1,
@@ -348,9 +351,16 @@ def gpu_arm(args, world, rank):
 
     batched = batched_arm(args, sim, value, world) if args.batch else None
     adjoint = adjoint_arm(args) if not args.no_adjoint else None
+    batch256 = None
+    if not args.no_batch256 and world == 1:
+        batch256 = batch_arm(args, steps=min(args.steps, 3), warmup=2, emit=False)
+    large = None
+    if not args.no_large and world == 1:
+        large = large_arm(args, steps=1, warmup=1, gpu_population=True, emit=False)
 
     return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched, adjoint=adjoint,
-                edge_tile=st.edge_tile_label, tile_ms=tile_ms,
+                batch256=batch256, large=large,
+                edge_tile=st.edge_tile_label, tile_ms=tile_ms, popdict=sim.popdict, person=sim._person,
                 launches=launches_per_step * args.steps, init_s=init_s, res=res, spec=sim.spec,
                 cum_infections=float(res['new_infections'].sum() + sim['pop_infected']))
 
@@ -455,18 +465,32 @@ def batched_arm(args, sim, plain_value, world):
 
 
 # ----------------------------------------------------------------------------- CPU oracle
-def _oracle_worker(args_tuple):
-    """Build a 1M hybrid sim and time `days` days of the CPU oracle (MT19937 mode)."""
-    pop_size, total_days, seed, warm, days = args_tuple
-    import numpy as np  # noqa: F811
-    sys.path.insert(0, ROOT)
+def workload_config(args):
+    """The ``config`` both arms print: the workload alone (step and sampling details are top-level keys)."""
+    return {'workload': f'hybrid {args.pop_size} agents (h/s/w/c, c redrawn daily), {args.days} days, waning, '
+                        f'pop_infected 100'}
+
+
+def host_cores():
+    """The host cores this process may use (its affinity mask) and their count."""
+    try:
+        mask = sorted(os.sched_getaffinity(0))
+    except AttributeError:
+        mask = list(range(os.cpu_count() or 1))
+    return mask, len(mask)
+
+
+def _oracle_sim(pop_size, days, seed):
+    """The workload on the CPU oracle in MT19937 mode: the reference's algorithm
+    (the whole redrawn layer every day, every edge's draw) with the reference's
+    streams; population and prognoses from the same generators as the GPU arm."""
     import covasim_gb300 as cv
     from oracle.sim import OracleSim, set_prognoses
     from oracle.people import OraclePeople
     pars = cv.make_pars(pop_size=pop_size, pop_type='hybrid', pop_infected=100, use_waning=True,
-                        n_days=total_days, rand_seed=seed, dynam_layer=dict(h=0, s=0, w=0, c=1))
+                        n_days=days, rand_seed=seed, dynam_layer=dict(h=0, s=0, w=0, c=1))
     pars['prognoses'] = cv.get_prognoses(True)
-    cv.init_immunity(pars, total_days + 1)
+    cv.init_immunity(pars, days + 1)
     pop = cv.make_randpop(pars, rng=np.random.default_rng(seed))
     tmp = OraclePeople(pars, pop_size)
     tmp.age = np.asarray(pop['age'], np.float32)
@@ -474,48 +498,96 @@ def _oracle_worker(args_tuple):
     person = {k: tmp[k] for k in ('symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus')}
     contacts = {k: dict(p1=c['p1'], p2=c['p2'], beta=np.ones(len(c['p1']), np.float32))
                 for k, c in ((k, pop['contacts'][k]) for k in pars['beta_layer'])}
-    sim = OracleSim(pars, person, contacts, rng='mt')
-    for _ in range(warm):
-        sim.step()
-    t0 = time.perf_counter()
-    for _ in range(days):
-        sim.step()
-    return time.perf_counter() - t0
+    return OracleSim(pars, person, contacts, rng='mt')
 
 
-def cpu_baseline(args, procs=1, warm=1, days=None):
-    days = args.cpu_days if days is None else days
-    if procs == 1:
-        dt = _oracle_worker((args.pop_size, args.days, 1, warm, days))
-        return args.pop_size * days / dt, dt
-    import multiprocessing as mp
-    ctx = mp.get_context('spawn')
-    with ctx.Pool(procs) as pool:
-        dts = pool.map(_oracle_worker, [(args.pop_size, args.days, 1 + i, warm, days) for i in range(procs)])
-    return procs * args.pop_size * days / max(dts), max(dts)
+def _reference_worker(job):
+    """One process of the reference arm: its own sim, ``warm`` untimed days on a
+    copy, then the whole run (days 0..days) in ``k`` timed slices of consecutive
+    days. Returns the slices' seconds and the run's cumulative infections."""
+    import copy
+    pop_size, days, seed, warm, k = job
+    sys.path.insert(0, ROOT)
+    sim = _oracle_sim(pop_size, days, seed)
+    if warm:
+        w = copy.deepcopy(sim)
+        for _ in range(warm):
+            w.step()
+        del w
+    bounds = np.linspace(0, days + 1, k + 1).round().astype(int)
+    out = []
+    for j in range(k):
+        t0 = time.perf_counter()
+        for _ in range(bounds[j], bounds[j + 1]):
+            sim.step()
+        out.append(time.perf_counter() - t0)
+    return out, float(sim.results['new_infections'].sum()) + 100
+
+
+def cpu_baseline(args, gpu_sim_factory, samples=5, days_each=2):
+    """The CPU oracle (MT19937 mode, one process) on a bounded sample of the
+    workload: ``samples`` stretches of ``days_each`` days spread evenly over the
+    epidemic, each started from the GPU run's state of the evening before (the
+    same trajectory), so early, peak and late days are all in the sample."""
+    import covasim_gb300 as cv  # noqa: F401
+    from oracle.people import (PERSON, STATES, VARIANT_STATES, BY_VARIANT_STATES, IMM_STATES, NAB_STATES,
+                               VACC_STATES, DATES, DURS)
+    keys = [k for k in PERSON + STATES + VARIANT_STATES + BY_VARIANT_STATES + IMM_STATES + NAB_STATES +
+            VACC_STATES + DATES + DURS if k not in ('age', 'sex', 'uid', 'doses')]
+    starts = np.linspace(args.days / (samples + 1), args.days * samples / (samples + 1), samples).round().astype(int)
+    sim = gpu_sim_factory()
+    orc = _oracle_sim(args.pop_size, args.days, 1)
+    total, n_days = 0.0, 0
+    for d in starts:
+        sim.run(until=int(d))
+        for k in keys:
+            orc.people[k] = np.array(sim.people.gpu(k).cpu().numpy(), dtype=orc.people[k].dtype)
+        orc.t = int(d)
+        t0 = time.perf_counter()
+        for _ in range(days_each):
+            orc.step()
+        total += time.perf_counter() - t0
+        n_days += days_each
+    mask, _ = host_cores()
+    return {'value': round(args.pop_size * n_days / total, 1), 'unit': 'agent-days/s', 'cores': 1, 'kind': 'port',
+            'sample': f'days {", ".join(f"{d}-{d + days_each - 1}" for d in starts)} of the {args.pop_size}-agent '
+                      f'hybrid sim, each stretch started from the GPU run\'s state of the evening before; numpy '
+                      f'oracle (the reference\'s algorithm restated) in MT19937 mode, one process, '
+                      f'{total:.1f} s',
+            'affinity': f'{len(mask)} cores available ({mask[0]}-{mask[-1]})'}
 
 
 def reference_arm(args, world, rank):
-    """The reference's CPU implementation of the path (the numpy restatement: the
-    reference needs numba and sciris, which are not installed), on all host cores,
-    each process running its own 1M hybrid sim; a step is one simulated day."""
+    """The reference's CPU implementation of the path (its numpy restatement: the
+    reference needs numba and sciris, which are not installed) on every host core
+    the process may use: one independent sim per core (seeds differ), each running
+    the whole 180-day epidemic. The K timed steps are K consecutive slices of that
+    run, so every day of the epidemic is timed once; the W warm-up steps are W
+    untimed days on a copy of each sim."""
     if rank != 0:
         return
-    procs = max(1, min(os.cpu_count() or 1, 16))
+    import multiprocessing as mp
+    mask, n_cores = host_cores()
+    procs = max(1, min(n_cores, 16))
     t0 = time.perf_counter()
-    value, dt = cpu_baseline(args, procs=procs, warm=max(args.warmup, 1), days=args.steps)
+    jobs = [(args.pop_size, args.days, 1 + i, args.warmup, args.steps) for i in range(procs)]
+    with mp.get_context('spawn').Pool(procs) as pool:
+        res = pool.map(_reference_worker, jobs)
+    run_s = max(sum(r[0]) for r in res)
+    value = procs * args.pop_size * args.days / run_s
     line = {'metric': 'agent-days/s', 'value': round(value, 1), 'unit': 'agent-days/s', 'impl': 'reference',
             'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': round(1e3 * dt / args.steps, 3), 'higher_is_better': True, 'scaling': 'weak',
-            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': f'hybrid {args.pop_size} agents, {args.days} days, waning, c redrawn daily',
-                       'sample': f'{args.steps} timed days after {max(args.warmup, 1)} warm-up days, '
-                                 f'{procs} independent sims in parallel'},
+            'ms_per_step': round(1e3 * run_s / args.steps, 3), 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic', 'config': workload_config(args),
+            'step': f'1/{args.steps} of one whole run ({args.days + 1} days) on each of {procs} cores; the steps '
+                    f'cover every day once',
             'cpu_baseline': {'value': round(value, 1), 'unit': 'agent-days/s', 'cores': procs, 'kind': 'port',
-                             'sample': f'{procs} x {args.pop_size}-agent hybrid sims, {args.steps} days each '
-                                       '(numpy oracle, MT19937 mode)'},
+                             'sample': f'{procs} independent {args.pop_size}-agent hybrid sims (seeds 1-{procs}), '
+                                       f'each its whole {args.days + 1}-day run (numpy oracle, MT19937 mode)',
+                             'affinity': f'{len(mask)} cores available ({mask[0]}-{mask[-1]})'},
             'e2e': {'value': round(value, 1), 'unit': 'agent-days/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0},
+            'cum_infections_per_run': round(float(np.mean([r[1] for r in res])), 1),
             'wall_s': round(time.perf_counter() - t0, 1)}
     print(json.dumps(line), flush=True)
 
@@ -532,7 +604,7 @@ def _line(metric_value, unit, args, ms, workload, extra):
             json.dump(line, f, indent=1)
 
 
-def large_arm(args, n=20_000_000, days=365):
+def large_arm(args, n=20_000_000, days=365, steps=None, warmup=None, gpu_population=None, emit=True):
     """20M-agent hybrid sim, 3 co-circulating variants (rel_beta 1.0 / 1.5 / 1.7,
     the second and third imported on days 60 and 120), waning, test_prob(symp_prob=0.1)
     and contact_tracing(trace_probs=0.5), 365 days. A step is one whole run: the
@@ -548,12 +620,15 @@ def large_arm(args, n=20_000_000, days=365):
     t0 = time.perf_counter()
     tile = None if args.edge_tile == 'auto' else args.edge_tile
     seeds = max(1, args.seeds)
+    gpu_population = args.gpu_population if gpu_population is None else gpu_population
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     if seeds == 1:
-        sim = cv.Sim(pars, edge_tile=tile, gpu_population=args.gpu_population)
+        sim = cv.Sim(pars, edge_tile=tile, gpu_population=gpu_population)
         sim.initialize()
         st = sim.state
     else:  # the batched form: several seeds in one BatchSim
-        sims = [cv.Sim(dict(pars, rand_seed=1 + k), gpu_population=args.gpu_population) for k in range(seeds)]
+        sims = [cv.Sim(dict(pars, rand_seed=1 + k), gpu_population=gpu_population) for k in range(seeds)]
         batch = cv.BatchSim(sims, edge_tile=tile).initialize()
         sim, st = sims[0], batch.state
     init_s = time.perf_counter() - t0
@@ -567,14 +642,14 @@ def large_arm(args, n=20_000_000, days=365):
             st.restore(snap)
             batch.run()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         one_run()
     torch.cuda.synchronize()
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    for _ in range(args.steps):
+    for _ in range(steps):
         one_run()
     ev1.record()
     torch.cuda.synchronize()
@@ -582,18 +657,21 @@ def large_arm(args, n=20_000_000, days=365):
     el = ev0.elapsed_time(ev1) / 1e3
     res = st.results(0)
     e_all = sum(len(ly['p1']) for ly in sim.spec.layers)
-    _line(seeds * n * days * args.steps / el, 'agent-days/s', args, 1e3 * el / args.steps,
-          f'{seeds} x ' * (seeds > 1) + f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), waning, '
-          f'test_prob(symp_prob=0.1), contact_tracing(trace_probs=0.5), {days} days',
-          {'edge_evaluations_per_s': round(seeds * 2 * e_all * days * args.steps / el, 1), 'init_s': round(init_s, 1),
-           'seeds': seeds,
-           'population': 'device' if args.gpu_population else 'host',
-           'cum_infections': float(res['new_infections'].sum() + sim['pop_infected']),
-           'cum_tests': float(res['new_tests'].sum()), 'cum_quarantined': float(res['new_quarantined'].sum()),
-           'clocks': clk})
+    workload = (f'{seeds} x ' * (seeds > 1) + f'hybrid {n} agents, {e_all} edges, 3 variants (days 0/60/120), '
+                f'waning, test_prob(symp_prob=0.1), contact_tracing(trace_probs=0.5), {days} days')
+    extra = {'edge_evaluations_per_s': round(seeds * 2 * e_all * days * steps / el, 1), 'init_s': round(init_s, 1),
+             'seeds': seeds, 'population': 'device' if gpu_population else 'host',
+             'cum_infections': float(res['new_infections'].sum() + sim['pop_infected']),
+             'cum_tests': float(res['new_tests'].sum()), 'cum_quarantined': float(res['new_quarantined'].sum()),
+             'clocks': clk}
+    value = seeds * n * days * steps / el
+    if emit:
+        _line(value, 'agent-days/s', args, 1e3 * el / steps, workload, extra)
+    return dict({'workload': workload, 'value': round(value, 1), 'unit': 'agent-days/s', 'steps': steps,
+                 'warmup': warmup, 'ms_per_step': round(1e3 * el / steps, 3)}, **extra)
 
 
-def batch_arm(args, n_sims=256, days=120):
+def batch_arm(args, n_sims=256, days=120, steps=None, warmup=None, emit=True):
     """256 random-population sims (pop_size log-uniform in [10k, 500k], contacts
     10/20/30, beta U[0.010, 0.025], change_beta(days=30, changes=U[0.3, 1])), 120
     days: all in one BatchSim (one launch sequence per day over every sim, one
@@ -643,17 +721,20 @@ def batch_arm(args, n_sims=256, days=120):
             s.state.infect_list(0, choose_seed(s), sim=0, variant=0, layer_tag=MAX_LAYERS, call_tag=CALL_SEED_TAG)
             s.state.run_days(0, npts, open_prev=False, close_last=True, use_graph=True)
 
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        for _ in range(args.steps):
+        for _ in range(steps):
             fn()
         b.record()
         torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3 / args.steps
+        return a.elapsed_time(b) / 1e3 / steps
 
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
@@ -663,13 +744,16 @@ def batch_arm(args, n_sims=256, days=120):
     agent_days = float(sizes.sum()) * days
     same = all(np.array_equal(st.results(k)['new_infections'], singles[k][0].state.results(0)['new_infections'])
                for k in range(n_sims))
-    _line(agent_days / t_batch, 'agent-days/s', args, 1e3 * t_batch,
-          f'{n_sims} random-population sims, {int(sizes.sum())} agents in all (10k-500k each), contacts 10/20/30, '
-          f'beta U[0.010,0.025], change_beta day 30 x U[0.3,1], {days} days',
-          {'one_by_one': {'value': round(agent_days / t_single, 1), 'ms_per_step': round(1e3 * t_single, 3)},
-           'batched_over_one_by_one': round(t_single / t_batch, 3), 'every_sim_equals_its_own_run': same,
-           'edge_tile': st.edge_tile, 'init_s': round(init_s, 1),
-           'population': 'device' if args.gpu_population else 'host', 'clocks': clk})
+    workload = (f'{n_sims} random-population sims, {int(sizes.sum())} agents in all (10k-500k each), contacts '
+                f'10/20/30, beta U[0.010,0.025], change_beta day 30 x U[0.3,1], {days} days')
+    extra = {'one_by_one': {'value': round(agent_days / t_single, 1), 'ms_per_step': round(1e3 * t_single, 3)},
+             'batched_over_one_by_one': round(t_single / t_batch, 3), 'every_sim_equals_its_own_run': same,
+             'edge_tile': st.edge_tile, 'init_s': round(init_s, 1),
+             'population': 'device' if args.gpu_population else 'host', 'clocks': clk}
+    if emit:
+        _line(agent_days / t_batch, 'agent-days/s', args, 1e3 * t_batch, workload, extra)
+    return dict({'workload': workload, 'value': round(agent_days / t_batch, 1), 'unit': 'agent-days/s',
+                 'steps': steps, 'warmup': warmup, 'ms_per_step': round(1e3 * t_batch, 3)}, **extra)
 
 
 def choose_seed(sim):
@@ -717,24 +801,22 @@ def main():
     out = gpu_arm(args, world, rank)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, dt = cpu_baseline(args)
-        cpu = {'value': round(v, 1), 'unit': 'agent-days/s', 'cores': 1, 'kind': 'port',
-               'sample': f'{args.cpu_days} days (after 1 warm-up day) of the {args.pop_size}-agent hybrid sim, numpy oracle in '
-                         f'MT19937 mode, one process ({dt:.1f} s)'}
+        import covasim_gb300 as cv
+        cpu = cpu_baseline(args, lambda: cv.Sim(sim_pars(args, 1), popdict=out['popdict'], person=out['person'],
+                                                 edge_tile=out['edge_tile']))
     if rank == 0:
         line = {'metric': 'agent-days/s', 'value': round(out['value'], 1), 'unit': 'agent-days/s',
                 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
                 'ms_per_step': round(1e3 * out['elapsed'] / args.steps, 3), 'higher_is_better': True,
                 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
-                'config': {'workload': f'hybrid {args.pop_size} agents (h/s/w/c, c redrawn daily), '
-                                       f'{args.days} days, waning, pop_infected 100',
-                           'step': 'one full run: rewind state in HBM, seed, 181 days as one CUDA graph',
-                           'edge_tile': out['edge_tile'], 'edge_tile_autotune_ms_per_run': out['tile_ms'],
-                           'l2': 'inputs larger than L2 (agents ~160 MB + static edges ~62 MB)',
-                           'replicas': world, 'cum_infections_per_run': out['cum_infections']},
+                'config': workload_config(args),
+                'step': f'one full run: rewind the state in HBM, seed, {args.days + 1} days as one CUDA graph',
+                'edge_tile': out['edge_tile'], 'edge_tile_autotune_ms_per_run': out['tile_ms'],
+                'l2': 'inputs larger than L2 (agents ~160 MB + stored edges ~62 MB)',
+                'replicas': world, 'cum_infections_per_run': out['cum_infections'],
                 'edge_evaluations_per_s': None,
                 'roofline': out['roofline'], 'cpu_baseline': cpu, 'e2e': out['e2e'], 'batched': out['batched'],
-                'adjoint': out['adjoint'],
+                'adjoint': out['adjoint'], 'batch256': out['batch256'], 'large': out['large'],
                 'gpu_launches': out['launches'], 'clocks': out['clocks']}
         spec = out['spec']
         e_all = sum(len(ly['p1']) for ly in spec.layers)

@@ -27,11 +27,14 @@ FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
 NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
 EDGE_TILE = 4096          # default edges per edge-pass tile (block)
+DYN_MAX_LIST = 1024       # longest contact list of an agent in a dynamic layer (COVGPU_DYN_MAX_LIST)
 EDGE_TILES = (1024, 2048, 4096, 8192)   # tile sizes the library supports (covgpu_state.edge_tile)
 AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
 AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
 
 OK, OVERFLOW, TIMEOUT, BADARG, CUDA_ERROR = 0, 1, 2, 3, 4
+# covgpu_check: which People.check_* runs (COVGPU_CHECK_*)
+CHECK_INFECTIOUS, CHECK_SYMPTOMATIC, CHECK_SEVERE, CHECK_CRITICAL, CHECK_RECOVERY, CHECK_DEATH, CHECK_EXIT_ISO = range(7)
 STATUS_NAMES = {OK: 'OK', OVERFLOW: 'OVERFLOW', TIMEOUT: 'TIMEOUT', BADARG: 'BADARG', CUDA_ERROR: 'CUDA_ERROR'}
 
 DIST_CODES = {'lognormal_int': 0, 'lognorm_int': 0, 'lognormal': 1, 'lognorm': 1, 'normal': 2, 'norm': 2,
@@ -97,7 +100,8 @@ class Layer(C.Structure):
     _fields_ = [('p1', C.c_void_p), ('p2', C.c_void_p), ('beta', C.c_void_p), ('n_edges', C.c_int64),
                 ('tile_begin', C.c_int64), ('sim', C.c_int32), ('layer', C.c_int32), ('dynamic', C.c_int32),
                 ('beta_const', C.c_float), ('iso_factor', C.c_float), ('quar_factor', C.c_float),
-                ('_pad', C.c_int32), ('rp1', C.c_void_p), ('rp2', C.c_void_p), ('perm2', C.c_void_p)]
+                ('dyn_k', C.c_int32), ('rp1', C.c_void_p), ('rp2', C.c_void_p), ('perm2', C.c_void_p),
+                ('dyn_cdf', C.c_void_p)]
 
 
 class AgentBlock(C.Structure):
@@ -135,7 +139,7 @@ class State(C.Structure):
         ('pending_quar', C.c_void_p), ('trace_count', C.c_void_p),
         ('lik', Lik),
         ('import_day_off', C.c_void_p), ('imports', C.c_void_p), ('import_sims', C.c_void_p),
-        ('import_days', C.c_int32), ('_pad3', C.c_int32),
+        ('import_days', C.c_int32), ('n_dynamic', C.c_int32),
         ('hold', C.c_void_p), ('tgt_rec', C.c_void_p),
     ]
 
@@ -170,10 +174,14 @@ def lib():
         L.covgpu_infect_claims.argtypes = [sp, i32, vp]
         L.covgpu_test_trace.argtypes = [sp, i32, vp]
         L.covgpu_lik_targets.argtypes = [sp, i32, vp]
-        L.covgpu_infect_list.argtypes = [sp, i32, vp, i64, i32, i32, i32, i32, vp]
+        L.covgpu_infect_list.argtypes = [sp, i32, vp, vp, i64, i32, i32, i32, i32, vp, vp]
+        L.covgpu_check.argtypes = [sp, i32, i32, i32, i32, vp, i64, i64, vp, i64, vp, vp]
+        L.covgpu_check_immunity.argtypes = [sp, i32, i32, C.c_uint32, vp]
+        L.covgpu_update_nab.argtypes = [sp, i32, i32, vp, i64, vp]
+        L.covgpu_update_peak_nab.argtypes = [sp, i32, i32, vp, i64, vp, DurPar, f32, C.c_double, i32, vp]
         L.covgpu_import_day.argtypes = [sp, i32, vp]
         L.covgpu_rescale_check.argtypes = [sp, i32, vp]
-        L.covgpu_layer_materialize.argtypes = [sp, i32, i32, vp, vp, vp]
+        L.covgpu_layer_lists.argtypes = [sp, i32, i32, i64, i64, vp, vp, vp, vp]
         L.covgpu_run_days.argtypes = [sp, i32, i32, i32, i32, i32, vp]
         L.covgpu_edge_resident_bytes.argtypes = [sp]
         L.covgpu_edge_resident_bytes.restype = i64
@@ -196,8 +204,10 @@ def lib():
         for name in POP_FUNCS:
             getattr(L, name).restype = C.c_int
         for name in ('covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections', 'covgpu_agent_step',
-                     'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_materialize',
-                     'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_targets'):
+                     'covgpu_edge_pass', 'covgpu_infect_claims', 'covgpu_infect_list', 'covgpu_layer_lists',
+                     'covgpu_run_days', 'covgpu_test_trace', 'covgpu_lik_targets', 'covgpu_import_day',
+                     'covgpu_rescale_check', 'covgpu_check', 'covgpu_check_immunity', 'covgpu_update_nab',
+                     'covgpu_update_peak_nab'):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -230,6 +240,7 @@ POP_FUNCS = ['covgpu_pop_ages', 'covgpu_pop_members', 'covgpu_pop_random_counts'
 
 EXPORTED = ['covgpu_version', 'covgpu_abi_layout', 'covgpu_viral_load', 'covgpu_trans_sus', 'covgpu_infections_scratch_bytes',
             'covgpu_infections', 'covgpu_infections_noalloc', 'covgpu_agent_step', 'covgpu_edge_pass', 'covgpu_infect_claims',
-            'covgpu_infect_list', 'covgpu_import_day', 'covgpu_rescale_check', 'covgpu_layer_materialize', 'covgpu_run_days', 'covgpu_test_trace',
+            'covgpu_infect_list', 'covgpu_import_day', 'covgpu_rescale_check', 'covgpu_layer_lists', 'covgpu_run_days', 'covgpu_test_trace',
             'covgpu_lik_targets', 'covgpu_trace_index_scratch', 'covgpu_trace_index', 'covgpu_edge_resident_bytes',
+            'covgpu_check', 'covgpu_check_immunity', 'covgpu_update_nab', 'covgpu_update_peak_nab',
             'covgpu_pop_scan_scratch'] + POP_FUNCS

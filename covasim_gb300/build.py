@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, 'csrc')
 INCLUDE = os.path.join(ROOT, 'include')
 LIB_NAME = 'libcovgpu.so'
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ['covgpu.cu', 'covgpu_reference.cu', 'covgpu_testing.cu', 'covgpu_pop.cu']
+SOURCES = ['covgpu.cu', 'covgpu_reference.cu', 'covgpu_testing.cu', 'covgpu_pop.cu', 'covgpu_dropin.cu']
 OBJ_DIR = os.path.join(HERE, '_build')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
@@ -37,7 +37,7 @@ def build(verbose=False, force=False, extra=()):
     """Compile each translation unit in parallel (nvcc -c), then link the shared library."""
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, f) for f in ('covgpu_device.cuh', 'covgpu_ff.cuh', 'covgpu_tables.h',
-                                                   'covgpu_scan.cuh', 'covgpu_launch.cuh')]
+                                                   'covgpu_scan.cuh', 'covgpu_launch.cuh', 'covgpu_imm.cuh')]
     deps += [os.path.join(INCLUDE, 'covgpu.h'), __file__]
     if not force and os.path.exists(LIB_PATH):
         lib_m = os.path.getmtime(LIB_PATH)

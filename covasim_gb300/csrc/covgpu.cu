@@ -24,6 +24,7 @@
 #include "covgpu_device.cuh"
 #include "covgpu_ff.cuh"
 #include "covgpu_launch.cuh"
+#include "covgpu_imm.cuh"
 
 using namespace covgpu;
 
@@ -56,7 +57,10 @@ constexpr int IMPORT_BLOCKS = 4;       // k_import_day grid (a day imports a han
 // ============================================================ fused agent pass
 
 
-__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day) {
+// full_imm: also store sev_imm (read only by infect(), which recomputes it for the
+// agents it infects; stored on the last day of a launch sequence, so that the
+// state a caller reads afterwards holds the reference's array)
+__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm) {
   if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
     const int h = *st.hold;
     if (h <= t - 1) return;
@@ -205,33 +209,20 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
         ff ln_nab = ff{0.0f, 0.0f};
         bool have_ln = false;
         for (int v = 0; v < nv; ++v) {
-          // imm = max(natural, vaccine); ln(imm) from the host's tables
-          float imm = 0.0f;
-          ff ln_imm = ff{0.0f, 0.0f};
-          if (was_inf && rv < (uint32_t)nv) {
-            const int q = v * COVGPU_MAX_VARIANTS + (int)rv;
-            imm = sp.immunity[q];
-            ln_imm = ff{sp.ln_immunity[q][0], sp.ln_immunity[q][1]};
-          }
-          if ((f & B_VACC) && sp.vx_imm && sp.vx_ln_imm) {
-            const int src = st.vaccine_source[i];
-            if (src >= 0 && src < sp.n_vaccines && sp.vx_imm[src * nv + v] > imm) {
-              imm = sp.vx_imm[src * nv + v];
-              ln_imm = ff{sp.vx_ln_imm[2 * (src * nv + v)], sp.vx_ln_imm[2 * (src * nv + v) + 1]};
-            }
-          }
+          ff ln_imm;  // imm = max(natural, vaccine); ln(imm) from the host's tables
+          const float imm = imm_of(st, sp, i, v, f, was_inf, rv, ln_imm);
           float a = 0.0f, b = 0.0f, c = 0.0f;
           if (nab > 0.0f && imm > 0.0f) {  // eff = nab * imm > 0; else every efficacy is 0
             if (!have_ln) { ln_nab = ff_log(nab, s_ln_tab); have_ln = true; }
             const ff ln_eff = ff_add(ln_nab, ln_imm);
-            a = ve_ff(ln_eff, ff{sp.ve_alpha[0][0], sp.ve_alpha[0][1]}, ff{sp.ve_beta[0][0], sp.ve_beta[0][1]}, s_exp_tab);
-            b = ve_ff(ln_eff, ff{sp.ve_alpha[1][0], sp.ve_alpha[1][1]}, ff{sp.ve_beta[1][0], sp.ve_beta[1][1]}, s_exp_tab);
-            c = ve_ff(ln_eff, ff{sp.ve_alpha[2][0], sp.ve_alpha[2][1]}, ff{sp.ve_beta[2][0], sp.ve_beta[2][1]}, s_exp_tab);
+            a = ve_axis(sp, 0, ln_eff, s_exp_tab);
+            b = ve_axis(sp, 1, ln_eff, s_exp_tab);
+            if (full_imm) c = ve_axis(sp, 2, ln_eff, s_exp_tab);
           }
           const int64_t off = (int64_t)v * st.n + i;
           st.sus_imm[off] = a;
           st.symp_imm[off] = b;
-          st.sev_imm[off] = c;
+          if (full_imm) st.sev_imm[off] = c;
           if (is_tgt) st.tgt_rec[off] = __uint_as_float(__float_as_uint(__fmul_rn(rs, __fsub_rn(1.0f, a))) | tq);
           sus_fx += __float2ll_rn(__fmul_rn(a, 4294967296.0f));
           symp_fx += __float2ll_rn(__fmul_rn(b, 4294967296.0f));
@@ -434,8 +425,9 @@ __device__ __forceinline__ void lik_terms(const covgpu_state& st, const SegCtx& 
 // compute_trans_sus folded into compute_infections for one direction s -> g
 // (utils.py:88-89 then 117-123); returns true on a transmission. Every gather
 // is issued before the first use so that they overlap. LIK: also the
-// likelihood terms of the direction, from the same gathered values.
-template <bool LIK>
+// likelihood terms of the direction, from the same gathered values. INJ: a
+// stored layer's edge, which takes the injected uniforms of test mode.
+template <bool LIK, bool INJ = true>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
                                          int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
   const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
@@ -470,7 +462,7 @@ __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c
   if (p == 0.0f) return false;
   v_out = v;
   bool hit;
-  if (st.edge_uniforms) {  // injected draws (test mode)
+  if (INJ && st.edge_uniforms) {  // injected draws (test mode)
     hit = st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
   } else {
     // one Philox block per (edge, day, variant, layer): words x,y draw direction 0, z,w direction 1
@@ -584,8 +576,8 @@ __device__ __forceinline__ void load_sim_lite(SimLite& o, const covgpu_sim_param
   o.n_layers = sp.n_layers;
 }
 
-// One tile (TILE edges) of one segment, NT threads: phase A streams the edges
-// and queues the candidate directions of each warp, phase B drains the queues.
+// One tile (TILE edges) of one stored segment, NT threads: phase A streams the
+// edges and queues the candidate directions of each warp, phase B drains the queues.
 // The segment record L and its sim's constants sp are shared-memory copies.
 // RES: the sim's source bitmap is resident in shared memory (s_src, one sim).
 template <bool LIK, int NT, int64_t TILE, bool RES>
@@ -609,26 +601,16 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
   c.beta_t = sp->beta_tab + (int64_t)t * c.nv;
   c.beta_layer = sp->beta_layer_tab[(int64_t)t * sp->n_layers + c.layer];
   c.sim = L->sim;
-  const bool dynamic = L->dynamic != 0;
   const int32_t* p1 = L->p1;
   const int32_t* p2 = L->p2;
   const int64_t e0 = (tile - L->tile_begin) * TILE;
   const int64_t e1 = min(e0 + TILE, c.n_edges);
-  const int64_t n_local = sp->n_agents;
   const int32_t off = (int32_t)sp->agent_off;
-  const uint32_t thr = dynamic ? bounded_thr((uint32_t)n_local) : 0u;
   int qn = 0;  // warp-uniform queue length
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * NT + threadIdx.x) * EDGE_VEC;
     int32_t a[EDGE_VEC], b[EDGE_VEC];
-    if (dynamic) {
-      // base.py:1849-1876 Layer.update: every edge of the layer redrawn, both
-      // endpoints uniform over the sim's agents (one Philox block per two edges)
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; j += 2)
-        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)c.layer, c.key0, c.key1, (uint32_t)n_local, thr,
-                     off, a[j], b[j], a[j + 1], b[j + 1]);
-    } else if (eb + EDGE_VEC <= e1) {
+    if (eb + EDGE_VEC <= e1) {
       const int4 pa = ld_stream_v4(p1 + eb);
       const int4 pb = ld_stream_v4(p2 + eb);
       a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
@@ -752,6 +734,173 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
   }
 }
 
+// ============================================================ redrawn layers
+//
+// Transmission over the dynamic layers (base.py:1849-1876 redrawn daily, then
+// utils.py:93-128): one warp per four source-bitmap words (128 agents of one
+// sim). The words' sources are handed to the lanes 32 at a time; for each
+// dynamic layer of the sim every lane draws its source's two contact lists
+// (covgpu_device.cuh, "redrawn layers, per agent") four partners per Philox
+// block, both lists side by side so that eight target-bitmap loads are in
+// flight, and queues the partners that are targets; the queue drains through
+// edge_try as the stored layers' does. The work follows the day's sources, not
+// the layer's edges: a quiet day costs a read of the source bitmap.
+constexpr int DYN_WARPS = 8;  // warps per thread block
+constexpr int DYN_WORDS = 4;  // source-bitmap words per warp (an agent block's eight words: two warps)
+
+// the segment constants of dynamic layer segment seg for day t
+__device__ __forceinline__ void dyn_ctx(const covgpu_state& st, const covgpu_sim_params& sp, int seg, int t, SegCtx& c) {
+  const covgpu_layer* L = st.segments + seg;
+  c.L = L;
+  c.seg = seg;
+  c.layer = L->layer;
+  c.n_edges = L->n_edges;
+  c.edge_beta = nullptr;
+  c.beta_const = L->beta_const;
+  c.quar_factor = L->quar_factor;
+  c.iso_factor = L->iso_factor;
+  c.asymp_factor = sp.asymp_factor;
+  c.nv = sp.n_variants;
+  c.key0 = sp.key0;
+  c.key1 = sp.key1;
+  c.beta_t = sp.beta_tab + (int64_t)t * c.nv;
+  c.beta_layer = sp.beta_layer_tab[(int64_t)t * sp.n_layers + c.layer];
+  c.sim = L->sim;
+}
+
+// phase B of the redrawn layers: one candidate per lane (entry j of list d of
+// source s, m = j << 1 | d), then the warp-aggregated event append
+template <bool LIK>
+__device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& c, int t, int64_t agent_off,
+                                          EdgeQueue& q, int qn, LikAcc& acc) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < qn; base += 32) {
+    const int i = base + lane;
+    bool hit = false;
+    uint32_t v = 0, m = 0;
+    int32_t s = 0, g = 0;
+    uint64_t e = 0;
+    if (i < qn) {
+      s = q.s[i]; g = q.g[i]; m = q.m[i];
+      e = dyn_edge_id((uint32_t)(s - agent_off), m >> 1, (uint32_t)t, (uint32_t)c.layer);
+      hit = edge_try<LIK, false>(st, c, t, (int64_t)e, (int)(m & 1u), s, g, v, acc);
+    }
+    emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), (int64_t)e) : 0ull, g, s);
+  }
+  __syncwarp();
+}
+
+// four partners (entries 4 qd .. 4 qd + 3) of list d of local agent a, as
+// global indices, and whether each is a target; entries past k are not targets
+__device__ __forceinline__ void dyn_four(const covgpu_state& st, uint32_t a, int d, int qd, int k, uint32_t t,
+                                         uint32_t layer, uint32_t key0, uint32_t key1, uint32_t n, uint32_t thr,
+                                         int32_t off, int32_t g[4], uint32_t tb[4]) {
+  const uint4 w = dyn_partner_block(a, d, 4 * qd, t, layer, key0, key1);
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    g[r] = off + (int32_t)dyn_partner(word_of(w, r), n, thr, a, d, 4 * qd + r, t, layer, key0, key1);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) tb[r] = 4 * qd + r < k ? tgt_bit(st, g[r]) : 0u;
+}
+
+template <bool LIK>
+__global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  __shared__ EdgeQueue s_q[DYN_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * DYN_WARPS + warp;
+  const int64_t b = gw >> 1;  // two warps per agent block
+  if (b >= st.n_agent_blocks) return;  // warp-uniform
+  const covgpu_agent_block blk = st.agent_blocks[b];
+  const int w_lo = (int)(gw & 1) * DYN_WORDS;
+  const int nwb = (int)((blk.end - blk.begin + 31) >> 5);
+  if (w_lo >= nwb) return;
+  const int nw = min(DYN_WORDS, nwb - w_lo);
+  const int64_t w0 = (blk.begin >> 5) + w_lo;  // sims start at multiples of 32
+  const WarpBits wb = warp_bits_scan(lane < nw ? __ldg(st.roles + w0 + lane) : 0u);
+  if (wb.total == 0) return;
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const uint32_t n_local = (uint32_t)sp.n_agents, thr = bounded_thr(n_local);
+  const int32_t off = (int32_t)sp.agent_off;
+  EdgeQueue& q = s_q[warp];
+  LikAcc acc;
+  for (int l = 0; l < sp.n_layers; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg < 0 || !st.segments[seg].dynamic) continue;
+    SegCtx c;
+    dyn_ctx(st, sp, seg, t, c);
+    int qn = 0;
+    for (int base = 0; base < wb.total; base += 32) {
+      const int idx = base + lane;
+      int bit;
+      const int wl = warp_bits_nth(wb, nw, idx, bit);
+      const int32_t s = (int32_t)((w0 + wl) * 32 + bit);
+      const uint32_t a = (uint32_t)(s - off);
+      int k0 = 0, k1 = 0;
+      if (idx < wb.total) dyn_counts(c.L->dyn_cdf, c.L->dyn_k, a, (uint32_t)t, (uint32_t)l, c.key0, c.key1, k0, k1);
+      const int nq = (max(k0, k1) + 3) >> 2;
+      const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)nq);
+      for (int qd = 0; qd < nq_max; ++qd) {
+        int32_t g0[4], g1[4];
+        uint32_t t0[4] = {0u, 0u, 0u, 0u}, t1[4] = {0u, 0u, 0u, 0u};
+        if (4 * qd < k0) dyn_four(st, a, 0, qd, k0, (uint32_t)t, (uint32_t)l, c.key0, c.key1, n_local, thr, off, g0, t0);
+        if (4 * qd < k1) dyn_four(st, a, 1, qd, k1, (uint32_t)t, (uint32_t)l, c.key0, c.key1, n_local, thr, off, g1, t1);
+        // each list's four entries add at most 4 * 32 candidates: drain before a half could overflow
+#pragma unroll
+        for (int r = 0; r < 4; ++r) queue_push(q, qn, t0[r] != 0u, s, g0[r], (uint32_t)(4 * qd + r) << 1);
+        if (qn > EQ_CAP - 4 * 32) {
+          dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+          qn = 0;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) queue_push(q, qn, t1[r] != 0u, s, g1[r], ((uint32_t)(4 * qd + r) << 1) | 1u);
+        if (qn > EQ_CAP - 4 * 32) {
+          dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+          qn = 0;
+        }
+      }
+    }
+    if (qn > 0) dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+    if (LIK) lik_flush_warp(st, t, blk.sim, l, acc);
+  }
+}
+
+int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->n_dynamic == 0) return COVGPU_OK;
+  const unsigned grid = (unsigned)((2 * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
+  if (st->lik.factor) k_dyn_pass<true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
+  else k_dyn_pass<false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
+  return launch_status();
+}
+
+// covgpu_layer_lists: one thread per agent; counts (offsets NULL) or partners
+__global__ void k_layer_lists(covgpu_state st, int seg, int t, int64_t begin, int64_t n, int32_t* counts,
+                              const int64_t* offsets, int32_t* partners) {
+  const covgpu_layer& L = st.segments[seg];
+  const covgpu_sim_params& sp = st.sims[L.sim];
+  const uint32_t n_local = (uint32_t)sp.n_agents, thr = bounded_thr(n_local);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = (uint32_t)(begin + i);
+    int k[2];
+    dyn_counts(L.dyn_cdf, L.dyn_k, a, (uint32_t)t, (uint32_t)L.layer, sp.key0, sp.key1, k[0], k[1]);
+    if (!offsets) {
+      counts[2 * i] = k[0];
+      counts[2 * i + 1] = k[1];
+      continue;
+    }
+    for (int d = 0; d < 2; ++d) {
+      int32_t* out = partners + offsets[2 * i + d];
+      uint4 pw = make_uint4(0u, 0u, 0u, 0u);
+      for (int j = 0; j < k[d]; ++j) {
+        if ((j & 3) == 0) pw = dyn_partner_block(a, d, j, (uint32_t)t, (uint32_t)L.layer, sp.key0, sp.key1);
+        out[j] = (int32_t)dyn_partner(word_of(pw, j & 3), n_local, thr, a, d, j, (uint32_t)t, (uint32_t)L.layer,
+                                      sp.key0, sp.key1);
+      }
+    }
+  }
+}
+
 // shared memory of the resident-bitmap variant, 0 when it cannot run
 int64_t edge_res_smem(const covgpu_state* st) {
   if (st->n_sims != 1 || st->edge_tile < RES_THREADS * EDGE_VEC || st->n_segments > RES_MAX_SEGS) return 0;
@@ -815,17 +964,21 @@ void launch_edge_res(const covgpu_state* st, int t, cudaStream_t s) {
   else k_edge_pass_res<LIK, 4096><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
 }
 
+// the stored layers' tiles, then the redrawn layers' sources
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
-  if (st->n_tiles == 0) return COVGPU_OK;
-  if (st->edge_resident) {
-    if (st->lik.factor) launch_edge_res<true>(st, t, s);
-    else launch_edge_res<false>(st, t, s);
-  } else if (st->lik.factor) {
-    launch_edge_tiles<true>(st, t, s);
-  } else {
-    launch_edge_tiles<false>(st, t, s);
+  if (st->n_tiles > 0) {
+    if (st->edge_resident) {
+      if (st->lik.factor) launch_edge_res<true>(st, t, s);
+      else launch_edge_res<false>(st, t, s);
+    } else if (st->lik.factor) {
+      launch_edge_tiles<true>(st, t, s);
+    } else {
+      launch_edge_tiles<false>(st, t, s);
+    }
+    const int rc = launch_status();
+    if (rc) return rc;
   }
-  return launch_status();
+  return launch_dyn_pass(st, t, s);
 }
 
 // per target: expected = 1 - prod(1 - p) and its per-layer sensitivities from
@@ -929,6 +1082,22 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   d.uw[3] = b2.y;
 }
 
+// sev_imm[v] of agent i (flags f) as day t's check_immunity (immunity.py:303-350)
+// forms it in the agent pass, from the same inputs (NAb, recovery date and
+// variant, vaccination: infect() changes none of them before it reads this), for
+// infect() alone reads it; the agent pass stores the array only on the last day
+// of a launch sequence. Without waning the array is as set.
+__device__ float sev_imm_of(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i, int t, int v, uint32_t f) {
+  if (!sp.use_waning) return st.sev_imm[(int64_t)v * st.n + i];
+  const float nab = st.nab[i];
+  if (!(nab > 0.0f)) return 0.0f;
+  ff ln_imm;
+  const float imm = imm_of(st, sp, i, v, f, (float)t >= date_row(st, COVGPU_DATE_RECOVERED)[i],
+                           (st.vstate[i] >> 16) & 0xFFu, ln_imm);
+  if (!(imm > 0.0f)) return 0.0f;
+  return ve_axis(sp, 2, ff_add(ff_log(nab, COVGPU_LN_TAB), ln_imm), COVGPU_EXP_TAB);
+}
+
 // people.py:435-586 for one agent (already deduplicated), plus update_peak_nab
 // outcome bits of one infect_one call, tallied per warp by infect_tally
 constexpr uint32_t O_INF = 1u, O_COUNT = 2u, O_REINF = 4u, O_SYMP = 8u, O_SEV = 16u;
@@ -993,7 +1162,7 @@ __device__ uint32_t infect_one(const covgpu_state& st, const covgpu_sim_params& 
     d_sym[i] = ds;
     out |= O_SYMP;
     const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
-                                  __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
+                                  __fsub_rn(1.0f, sev_imm_of(st, sp, i, t, v, f)));
     if (!d.lt(1, p_sev)) {  // CASE 2.1 mild, people.py:544-547
       const double dr = sample_ff(sp.dur[COVGPU_D_MILD2REC], d.z[4]);
       rec = (float)__dadd_rn((double)ds, dr);
@@ -1087,7 +1256,7 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
     symp = lt(0, sp_symp);
     if (symp) {
       const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
-                                    __fsub_rn(1.0f, st.sev_imm[(int64_t)v * st.n + i]));
+                                    __fsub_rn(1.0f, sev_imm_of(st, sp, i, t, v, f0)));
       sev = lt(1, p_sev);
       if (sev) {
         const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], st.crit_prob[i]),
@@ -1327,20 +1496,22 @@ __global__ void k_infect_claims(covgpu_state st, int t) {
   }
 }
 
-__global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, int64_t n, int sim, int v,
-                              int layer_tag, int call_tag) {
+__global__ void k_infect_list(covgpu_state st, int t, const int32_t* inds, const int32_t* sources, int64_t n, int sim,
+                              int v, int layer_tag, int call_tag, uint8_t* infected) {
   const covgpu_sim_params& sp = st.sims[sim];
   bool hosp, icu;
   hosp_icu(st, sp, sim, t, hosp, icu);
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = base + threadIdx.x;
     uint32_t out = 0;
-    int32_t tgt = 0;
+    int32_t tgt = 0, src = -1;
     if (j < n) {
       tgt = (int32_t)(inds[j] - sp.agent_off);
-      out = infect_one(st, sp, sim, inds[j], t, v, -1, layer_tag, call_tag, hosp, icu);
+      if (sources) src = sources[j];
+      out = infect_one(st, sp, sim, inds[j], t, v, src, layer_tag, call_tag, hosp, icu);
+      if (infected) infected[j] = (out & O_INF) ? 1 : 0;
     }
-    infect_tally(st, t, out, sim, v, -1, tgt, layer_tag);
+    infect_tally(st, t, out, sim, v, src, tgt, layer_tag);
   }
 }
 
@@ -1402,24 +1573,6 @@ __global__ void k_rescale_check(covgpu_state st, int t) {
   }
 }
 
-__global__ void k_layer_materialize(covgpu_state st, int seg, int t, int32_t* p1, int32_t* p2) {
-  const covgpu_layer& L = st.segments[seg];
-  const covgpu_sim_params& sp = st.sims[L.sim];
-  const uint32_t n = (uint32_t)sp.n_agents, thr = bounded_thr(n);
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; 2 * j < L.n_edges;
-       j += (int64_t)gridDim.x * blockDim.x) {
-    int32_t a0, b0, a1, b1;
-    dynamic_pair((uint64_t)j, (uint32_t)t, (uint32_t)L.layer, sp.key0, sp.key1, n, thr, 0, a0, b0, a1, b1);
-    p1[2 * j] = a0;
-    p2[2 * j] = b0;
-    if (2 * j + 1 < L.n_edges) {
-      p1[2 * j + 1] = a1;
-      p2[2 * j + 1] = b1;
-    }
-  }
-}
-
-
 // ------------------------------------------------------------ graph cache for covgpu_run_days
 struct GraphEntry {
   bool used = false;
@@ -1435,14 +1588,15 @@ cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the le
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     if (st->hold) k_rescale_check<<<1, 128, 0, s>>>(*st, t);
-    k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1);
+    k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1,
+                                                                        t == t1 - 1 ? 1 : 0);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
     launch_edge_pass(st, t, s);
     launch_lik_targets(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
-  if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0);
+  if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0, 0);
   return launch_status();
 }
 
@@ -1459,8 +1613,8 @@ int check_state(const covgpu_state* st) {
       !st->events ||
       !st->event_count || !st->status)
     return COVGPU_BADARG;
-  if (st->n_tiles > 0 && (!st->segments || st->n_segments <= 0))
-    return COVGPU_BADARG;
+  if ((st->n_tiles > 0 || st->n_dynamic > 0) && (!st->segments || st->n_segments <= 0)) return COVGPU_BADARG;
+  if (st->n_dynamic < 0 || st->n_dynamic > st->n_segments) return COVGPU_BADARG;
   if (st->n_agent_blocks > 0x7FFFFFFF || st->n_tiles > 0x7FFFFFFF) return COVGPU_BADARG;
   if (st->edge_tile != 1024 && st->edge_tile != 2048 && st->edge_tile != 4096 && st->edge_tile != 8192)
     return COVGPU_BADARG;
@@ -1504,7 +1658,7 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day);
+  k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day, 1);
   return launch_status();
 }
 
@@ -1538,14 +1692,16 @@ int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream) {
   return launch_status();
 }
 
-int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds, int32_t sim,
-                       int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream) {
+int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, const int32_t* sources, int64_t n_inds,
+                       int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, uint8_t* infected,
+                       void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (n_inds < 0 || sim < 0 || sim >= st->n_sims || variant < 0 || variant >= COVGPU_MAX_VARIANTS) return COVGPU_BADARG;
   if (n_inds == 0) return COVGPU_OK;
   if (!inds) return COVGPU_BADARG;
-  k_infect_list<<<grid_for(n_inds, 128), 128, 0, S(stream)>>>(*st, t, inds, n_inds, sim, variant, layer_tag, call_tag);
+  k_infect_list<<<grid_for(n_inds, 128), 128, 0, S(stream)>>>(*st, t, inds, sources, n_inds, sim, variant, layer_tag,
+                                                               call_tag, infected);
   return launch_status();
 }
 
@@ -1566,12 +1722,16 @@ int covgpu_rescale_check(const covgpu_state* st, int32_t t, void* stream) {
   return launch_status();
 }
 
-int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t, int32_t* p1, int32_t* p2,
-                             void* stream) {
+int covgpu_layer_lists(const covgpu_state* st, int32_t segment, int32_t t, int64_t agent_begin, int64_t n_agents,
+                       int32_t* counts, const int64_t* offsets, int32_t* partners, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
-  if (segment < 0 || segment >= st->n_segments || !p1 || !p2) return COVGPU_BADARG;
-  k_layer_materialize<<<grid_for(1 << 22, 256), 256, 0, S(stream)>>>(*st, segment, t, p1, p2);
+  if (segment < 0 || segment >= st->n_segments || t < 0 || t >= 0xFFFF || agent_begin < 0 || n_agents < 0 ||
+      (offsets ? !partners : !counts))
+    return COVGPU_BADARG;
+  if (n_agents == 0) return COVGPU_OK;
+  k_layer_lists<<<grid_for(n_agents, 256), 256, 0, S(stream)>>>(*st, segment, t, agent_begin, n_agents, counts,
+                                                                 offsets, partners);
   return launch_status();
 }
 

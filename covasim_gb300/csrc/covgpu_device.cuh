@@ -42,9 +42,8 @@ __device__ __forceinline__ bool held(const covgpu_state& st, int t) { return st.
 // Salmon et al., SC'11. Round constants and Weyl increments of that paper.
 constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
 constexpr uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
-constexpr uint32_t TAG_EDGE = 0x01000000u, TAG_LAYER = 0x02000000u, TAG_INFECT = 0x03000000u;
+constexpr uint32_t TAG_EDGE = 0x01000000u, TAG_INFECT = 0x03000000u;
 constexpr uint32_t TAG_TEST = 0x04000000u, TAG_TRACE = 0x05000000u;
-constexpr uint32_t TAG_LAYER_RETRY = 0x07000000u;
 
 __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
@@ -66,36 +65,111 @@ __device__ __forceinline__ double u01_52(uint32_t a, uint32_t b) {
 __device__ __forceinline__ double u01_32(uint32_t a) {
   return __dmul_rn(__dadd_rn((double)a, 0.5), 2.3283064365386962890625e-10);
 }
-// A uniform integer in [0, n) from a 32-bit word x, without bias (Lemire 2019,
-// "Fast random integer generation in an interval"): the high half of x * n,
-// redrawn while the low half is below thr = 2^32 mod n. Redraws (probability
-// below n / 2^32 each) come from the retry stream of (edge, endpoint):
-// Philox (edge, day, TAG_LAYER_RETRY | try << 8 | layer), word x for the first
-// endpoint and y for the second; after 16 tries (never reached in practice)
-// the last draw is kept.
-__device__ __forceinline__ uint32_t bounded_draw(uint32_t x, uint32_t n, uint32_t thr, uint64_t e, int which,
-                                                 uint32_t day, uint32_t layer, uint32_t k0, uint32_t k1) {
+// 2^32 mod n: the rejection threshold of an unbiased bounded draw (Lemire 2019,
+// "Fast random integer generation in an interval"), the high half of x * n
+// redrawn while its low half is below it
+__host__ __device__ __forceinline__ uint32_t bounded_thr(uint32_t n) { return (uint32_t)(-n) % n; }
+
+// ---------------------------------------------------------------- redrawn layers, per agent
+// A layer redrawn every day (base.py:1849-1876, Layer.update with frac = 1) has E
+// edges whose endpoints p1, p2 are i.i.d. uniform over the sim's n agents. The
+// edges of agent a as p1 and as p2 are two lists: list d of a has k_d(a) ~
+// Binomial(E, 1/n) entries, each partner uniform over the n agents. Transmission
+// only ever needs the edges of the day's sources (an edge without a source
+// endpoint infects nobody) and tracing only those of the traced agents, so the
+// library draws the lists of those agents alone, keyed by (agent, day, layer):
+//   counts   Philox (a, 0, day, TAG_DYN | layer): words x:y -> k_0, z:w -> k_1
+//            (a 64-bit uniform U, k = the first k with U < cdf[k]);
+//   partners Philox (a, 1 + d * 256 + (j >> 2), day, TAG_DYN | layer), word j & 3
+//            -> partner j of list d (unbiased bounded draw; redraw r of entry j:
+//            Philox (a, d << 10 | j, day, TAG_DYN_RETRY | r << 8 | layer), word x).
+// An edge between two sources sits in both of their lists as independent draws;
+// it carries no transmission either way (a source is never a target).
+// Entry j of list d of agent a is the edge with identity dyn_edge_id(a, j): a
+// bijection of a << 10 | j on 40 bits (a < 2^30, j < 2^10), so identities are
+// distinct and their order, which decides the first infector among one layer's
+// transmissions to the same target, is scrambled as the reference's i.i.d. edge
+// order is.
+constexpr uint32_t TAG_DYN = 0x08000000u, TAG_DYN_RETRY = 0x09000000u;
+constexpr int DYN_MAX_LIST = 1 << 10;  // entries of one list (the count table has at most this many)
+constexpr uint64_t MASK40 = (1ull << 40) - 1;
+
+__host__ __device__ __forceinline__ uint64_t dyn_edge_id(uint32_t a, uint32_t j, uint32_t day, uint32_t layer) {
+  uint64_t x = (((uint64_t)a << 10) | j) ^ ((((uint64_t)day << 8) | layer) * 0x9E3779B97Full & MASK40);
+  x = (x * 0xD6E8FEB86659Dull) & MASK40;  // odd multipliers: bijections modulo 2^40
+  x ^= x >> 21;
+  x = (x * 0xA0761D6478BDull) & MASK40;
+  x ^= x >> 19;
+  return x;
+}
+
+// the two list lengths of agent a: U = x:y (list 0), z:w (list 1); the first k with U < cdf[k]
+// (cdf[kn - 1] = 2^64 - 1, so k < kn)
+__device__ __forceinline__ int dyn_sample_k(const uint64_t* __restrict__ cdf, int kn, uint64_t u) {
+  int lo = 0, hi = kn - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (u < __ldg(reinterpret_cast<const unsigned long long*>(cdf) + mid)) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ void dyn_counts(const uint64_t* cdf, int kn, uint32_t a, uint32_t day, uint32_t layer,
+                                           uint32_t k0, uint32_t k1, int& n0, int& n1) {
+  const uint4 w = philox(make_uint4(a, 0u, day, TAG_DYN | layer), k0, k1);
+  n0 = dyn_sample_k(cdf, kn, ((uint64_t)w.x << 32) | w.y);
+  n1 = dyn_sample_k(cdf, kn, ((uint64_t)w.z << 32) | w.w);
+}
+// partner j of list d, given the word of its Philox block
+__device__ __forceinline__ uint32_t dyn_partner(uint32_t x, uint32_t n, uint32_t thr, uint32_t a, int d, int j,
+                                               uint32_t day, uint32_t layer, uint32_t k0, uint32_t k1) {
   uint64_t m = (uint64_t)x * n;
   for (uint32_t r = 0; (uint32_t)m < thr && r < 16; ++r) {
-    const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), day, TAG_LAYER_RETRY | (r << 8) | layer), k0, k1);
-    m = (uint64_t)(which ? w.y : w.x) * n;
+    const uint4 w = philox(make_uint4(a, ((uint32_t)d << 10) | (uint32_t)j, day, TAG_DYN_RETRY | (r << 8) | layer), k0, k1);
+    m = (uint64_t)w.x * n;
   }
   return (uint32_t)(m >> 32);
 }
-// 2^32 mod n (the rejection threshold of bounded_draw)
-__host__ __device__ __forceinline__ uint32_t bounded_thr(uint32_t n) { return (uint32_t)(-n) % n; }
+__device__ __forceinline__ uint4 dyn_partner_block(uint32_t a, int d, int j, uint32_t day, uint32_t layer, uint32_t k0,
+                                                   uint32_t k1) {
+  return philox(make_uint4(a, 1u + ((uint32_t)d << 8) + ((uint32_t)j >> 2), day, TAG_DYN | layer), k0, k1);
+}
+__device__ __forceinline__ uint32_t word_of(const uint4& w, int k) {
+  return k == 0 ? w.x : (k == 1 ? w.y : (k == 2 ? w.z : w.w));
+}
 
-// Endpoints of the dynamic-layer edges 2j and 2j+1 on one day (base.py:1849-1876:
-// uniform over the sim's n agents): one Philox block (j, day, TAG_LAYER | layer),
-// words x, y -> edge 2j, z, w -> edge 2j+1.
-__device__ __forceinline__ void dynamic_pair(uint64_t j, uint32_t day, uint32_t layer, uint32_t k0, uint32_t k1,
-                                             uint32_t n, uint32_t thr, int32_t off, int32_t& a0, int32_t& b0,
-                                             int32_t& a1, int32_t& b1) {
-  const uint4 w = philox(make_uint4((uint32_t)j, (uint32_t)(j >> 32), day, TAG_LAYER | layer), k0, k1);
-  a0 = off + (int32_t)bounded_draw(w.x, n, thr, 2 * j, 0, day, layer, k0, k1);
-  b0 = off + (int32_t)bounded_draw(w.y, n, thr, 2 * j, 1, day, layer, k0, k1);
-  a1 = off + (int32_t)bounded_draw(w.z, n, thr, 2 * j + 1, 0, day, layer, k0, k1);
-  b1 = off + (int32_t)bounded_draw(w.w, n, thr, 2 * j + 1, 1, day, layer, k0, k1);
+// The set bits of one agent block's bitmap words, handed to the lanes 32 at a
+// time: lanes 0..nw-1 hold the words (nw warp-uniform, <= 32), warp_bits_scan
+// forms their exclusive prefix counts, and warp_bits_nth gives the lane whose
+// word holds the idx-th set bit (idx < total) and the bit's position in it.
+// All 32 lanes call both.
+struct WarpBits {
+  uint32_t word;
+  int pre, total;
+};
+__device__ __forceinline__ WarpBits warp_bits_scan(uint32_t word) {
+  const int lane = threadIdx.x & 31;
+  const int cnt = __popc(word);
+  int inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int x = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += x;
+  }
+  WarpBits r;
+  r.word = word;
+  r.pre = inc - cnt;
+  r.total = __shfl_sync(0xffffffffu, inc, 31);
+  return r;
+}
+__device__ __forceinline__ int warp_bits_nth(const WarpBits& wb, int nw, int idx, int& bit) {
+  int src = 0;
+  for (int k = 1; k < nw; ++k)
+    if (__shfl_sync(0xffffffffu, wb.pre, k) <= idx) src = k;
+  const uint32_t wd = __shfl_sync(0xffffffffu, wb.word, src);
+  const int pk = __shfl_sync(0xffffffffu, wb.pre, src);
+  const int r = idx - pk;
+  bit = (r >= 0 && r < __popc(wd)) ? (int)__fns(wd, 0u, r + 1) : 0;
+  return src;
 }
 
 // floor(x * n / 2^64) for x = a:b

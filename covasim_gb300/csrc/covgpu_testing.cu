@@ -105,7 +105,8 @@ __device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, in
 }
 
 // contact_tracing.identify_contacts, the find_contacts half (utils.py:131-147):
-// every edge with a traced endpoint marks the other endpoint in its layer's bitmap
+// every edge of a stored layer without an index with a traced endpoint marks the
+// other endpoint in its layer's bitmap (dynamic layers: k_trace_dyn)
 template <int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, int t) {
   if (held(st, t)) return;
@@ -124,28 +125,20 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
   const covgpu_sim_params& sp = st.sims[L->sim];
   const covgpu_testing& T = sp.testing;
   if (!day_active(t, T.trace_start, T.trace_end) || T.thr_trace[L->layer] == 0 || st.trace_count[L->sim] == 0) return;
-  if (!L->dynamic && L->rp1) return;  // indexed: k_trace_csr visits the traced agents' edges
+  if (L->rp1) return;  // indexed: k_trace_csr visits the traced agents' edges
   const int64_t words = (st.n + 31) >> 5;
   uint32_t* contact = st.contact_bits + (int64_t)L->layer * words;
   const int64_t e0 = ((int64_t)blockIdx.x - L->tile_begin) * TILE;
   const int64_t e1 = min(e0 + TILE, L->n_edges);
   const int32_t off = (int32_t)sp.agent_off;
-  const uint32_t thr = L->dynamic ? bounded_thr((uint32_t)sp.n_agents) : 0u;
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * EDGE_THREADS + threadIdx.x) * EDGE_VEC;
     if (eb >= e1) break;
     int32_t a[EDGE_VEC], b[EDGE_VEC];
-    if (L->dynamic) {
 #pragma unroll
-      for (int j = 0; j < EDGE_VEC; j += 2)
-        dynamic_pair((uint64_t)(eb + j) >> 1, (uint32_t)t, (uint32_t)L->layer, sp.key0, sp.key1,
-                     (uint32_t)sp.n_agents, thr, off, a[j], b[j], a[j + 1], b[j + 1]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        a[j] = eb + j < e1 ? __ldg(L->p1 + eb + j) : off;
-        b[j] = eb + j < e1 ? __ldg(L->p2 + eb + j) : off;
-      }
+    for (int j = 0; j < EDGE_VEC; ++j) {
+      a[j] = eb + j < e1 ? __ldg(L->p1 + eb + j) : off;
+      b[j] = eb + j < e1 ? __ldg(L->p2 + eb + j) : off;
     }
 #pragma unroll
     for (int j = 0; j < EDGE_VEC; ++j) {
@@ -181,6 +174,52 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, in
     for (uint32_t k = L.rp2[local]; k < L.rp2[local + 1]; ++k) {
       const int32_t a = L.p1[L.perm2[k]];
       atomicOr(contact + (a >> 5), 1u << (a & 31));
+    }
+  }
+}
+
+// find_contacts over the dynamic layers: one warp per agent block; each traced
+// agent draws its two contact lists (the draws the edge pass makes for that agent
+// as a source) and marks every partner
+constexpr int TRACE_DYN_WARPS = 4;
+__global__ void __launch_bounds__(TRACE_DYN_WARPS * 32) k_trace_dyn(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t b = (int64_t)blockIdx.x * TRACE_DYN_WARPS + warp;
+  if (b >= st.n_agent_blocks) return;  // warp-uniform
+  const covgpu_agent_block blk = st.agent_blocks[b];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  const covgpu_testing& T = sp.testing;
+  if (!day_active(t, T.trace_start, T.trace_end) || st.trace_count[blk.sim] == 0) return;
+  const int64_t w0 = blk.begin >> 5;  // sims start at multiples of 32
+  const int nw = (int)((blk.end - blk.begin + 31) >> 5);
+  const WarpBits wb = warp_bits_scan(lane < nw ? st.trace_bits[w0 + lane] : 0u);
+  if (wb.total == 0) return;
+  const int64_t words = (st.n + 31) >> 5;
+  const uint32_t n_local = (uint32_t)sp.n_agents, thr = bounded_thr(n_local);
+  const int32_t off = (int32_t)sp.agent_off;
+  for (int l = 0; l < sp.n_layers; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg < 0 || T.thr_trace[l] == 0 || !st.segments[seg].dynamic) continue;
+    const covgpu_layer& L = st.segments[seg];
+    uint32_t* contact = st.contact_bits + (int64_t)l * words;
+    for (int base = 0; base < wb.total; base += 32) {
+      const int idx = base + lane;
+      int bit;
+      const int wl = warp_bits_nth(wb, nw, idx, bit);
+      if (idx >= wb.total) continue;
+      const uint32_t a = (uint32_t)((w0 + wl) * 32 + bit - off);
+      int k[2];
+      dyn_counts(L.dyn_cdf, L.dyn_k, a, (uint32_t)t, (uint32_t)l, sp.key0, sp.key1, k[0], k[1]);
+      for (int d = 0; d < 2; ++d) {
+        uint4 pw = make_uint4(0u, 0u, 0u, 0u);
+        for (int j = 0; j < k[d]; ++j) {
+          if ((j & 3) == 0) pw = dyn_partner_block(a, d, j, (uint32_t)t, (uint32_t)l, sp.key0, sp.key1);
+          const int32_t g = off + (int32_t)dyn_partner(word_of(pw, j & 3), n_local, thr, a, d, j, (uint32_t)t,
+                                                       (uint32_t)l, sp.key0, sp.key1);
+          atomicOr(contact + (g >> 5), 1u << (g & 31));
+        }
+      }
     }
   }
 }
@@ -330,6 +369,9 @@ int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
     }
   }
   k_trace_csr<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  if (st->n_dynamic)
+    k_trace_dyn<<<(unsigned)((st->n_agent_blocks + TRACE_DYN_WARPS - 1) / TRACE_DYN_WARPS), TRACE_DYN_WARPS * 32, 0,
+                  s>>>(*st, t);
   k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }

@@ -3,14 +3,58 @@
 The per-agent NAb and immunity work (check_immunity, update_nab,
 update_peak_nab) runs in the CUDA agent and infect kernels; this module
 builds the tables they read: ``nab_kin`` (covasim/immunity.py:356-448) and the
-cross-immunity matrix (immunity.py:269-300).
+cross-immunity matrix (immunity.py:269-300). ``check_immunity``,
+``update_nab`` and ``update_peak_nab`` are also drop-ins with the reference's
+signatures, each one CUDA kernel over a People object's agents.
 """
 import numpy as np
 
 from . import defaults as cvd
 from . import parameters as cvpar
 
-__all__ = ['nab_growth_decay', 'nab_decay', 'exp_decay', 'precompute_waning', 'init_immunity', 'variant']
+__all__ = ['nab_growth_decay', 'nab_decay', 'exp_decay', 'precompute_waning', 'init_immunity', 'variant',
+           'check_immunity', 'update_nab', 'update_peak_nab']
+
+
+# ---------------------------------------------------------------- reference-signature drop-ins
+def check_immunity(people, variants=None):
+    """immunity.py:303-350: each agent's sus_imm, symp_imm and sev_imm for the
+    given variants (all if None) from its NAbs and the larger of its natural
+    and vaccine immunity, on the device (calc_VE in float-float arithmetic,
+    rounded once, as the reference's float64)."""
+    people._state.check_immunity(people.t, sim=people._sim, variants=variants)
+
+
+def update_nab(people, inds):
+    """immunity.py:205-213: nab += nab_kin[t - t_nab_event] * peak_nab for the
+    agents inds, clamped to [0, peak_nab], on the device."""
+    people._state.update_nab(people.t, np.asarray(inds), sim=people._sim)
+
+
+def update_peak_nab(people, inds, nab_pars, symp=None):
+    """immunity.py:138-202 on the device: agents with NAbs have their peak
+    boosted by nab_pars['nab_boost']; the others get 2 ** nab_init, scaled by the
+    symptom class's rel_imm_symp and 1 + nab_eff['alpha_inf_diff'] when symp
+    (a dict of 'asymp', 'mild' and 'sev' index arrays) is given; t_nab_event = t.
+    The initial levels are drawn from the library's Philox streams."""
+    inds = np.asarray(inds, dtype=np.int64)
+    if not len(inds):
+        return
+    no_prior = ~(people['nab'][inds] > 0)
+    if no_prior.any() and nab_pars.get('nab_init') is None:
+        raise ValueError(f'Attempt to administer a vaccine without an initial NAb distribution to '
+                         f'{int(no_prior.sum())} unvaccinated people failed.')
+    cls, norm = None, 1.0
+    if symp is not None:
+        cls = np.full(len(inds), -1, dtype=np.int8)
+        for c, key in enumerate(('asymp', 'mild', 'sev')):
+            cls[np.isin(inds, np.asarray(symp.get(key, []), dtype=np.int64))] = c
+        if np.any(cls[no_prior] < 0):
+            raise ValueError('update_peak_nab: every agent without NAbs must be in one of symp\'s lists')
+        norm = 1 + nab_pars['nab_eff']['alpha_inf_diff']
+    init = nab_pars.get('nab_init') or dict(dist='normal', par1=0, par2=1)
+    people._state.update_peak_nab(people.t, inds, init, nab_pars['nab_boost'], norm_factor=norm, symp_class=cls,
+                                  sim=people._sim)
 
 
 def nab_growth_decay(length, growth_time, decay_rate1, decay_time1, decay_rate2, decay_time2):

@@ -189,18 +189,73 @@ class People:
         self._state.agent_step(t, do_prev=close_prev, do_day=True)
 
     def infect(self, inds, hosp_max=None, icu_max=None, source=None, layer=None, variant=0, call_tag=2):
-        """people.py:435-586 for an explicit list of agents (seed infections,
-        importations); transmissions are infected on the device by the edge pass."""
-        inds = np.unique(np.asarray(inds, dtype=np.int64))
+        """people.py:435-586 on the device for an explicit list of agents (seed
+        infections, importations, interventions); the day's transmissions are
+        infected on the device by the edge pass. As the reference: duplicates
+        are removed keeping each agent's first source, only the susceptible are
+        infected, each infection is logged with its source and layer, and the
+        agents actually infected are returned (sorted)."""
+        inds = np.asarray(inds, dtype=np.int64)
         if len(inds) == 0:
             return inds
+        if source is not None and len(source) != len(inds):
+            raise ValueError('infect: source must have one entry per target')
         if hosp_max is not None or icu_max is not None:
             self._state.set_hospicu([[int(bool(hosp_max)), int(bool(icu_max))]] * len(self._state.specs))
         layer_tag = log_layer_tag(layer, self.layer_keys(), self._state.log_labels)
-        self._state.infect_list(self.t, inds, sim=self._sim, variant=variant, layer_tag=layer_tag, call_tag=call_tag)
+        u, infected = self._state.infect_list(self.t, inds, sim=self._sim, variant=variant, layer_tag=layer_tag,
+                                              call_tag=call_tag, sources=source, want_infected=True)
         if hosp_max is not None or icu_max is not None:
             self._state.set_hospicu(None)
+        done = u[infected.cpu().numpy().astype(bool)]
+        self.flows['new_infections'] += len(done)
+        self.flows_variant['new_infections_by_variant'][variant] += len(done)
+        return done
+
+    # ------------------------------------------------------------------ one check at a time (people.py:222-312)
+    def _check(self, which, filter_exposed=True, inds=None):
+        got, known = self._state.check(self.t, which, sim=self._sim, filter_exposed=filter_exposed, inds=inds)
+        return got.cpu().numpy().astype(cvd.default_int), known
+
+    def check_infectious(self):
+        """people.py:222-232: the exposed whose infectious date has come become
+        infectious with their exposed variant; returns their indices."""
+        inds, _ = self._check(L.CHECK_INFECTIOUS)
+        iv = self['infectious_variant'][inds]
+        for v in range(self.pars['n_variants']):
+            self.flows_variant['new_infectious_by_variant'][v] += int(np.count_nonzero(iv == v))
         return inds
+
+    def check_symptomatic(self):
+        """people.py:235-239."""
+        return self._check(L.CHECK_SYMPTOMATIC)[0]
+
+    def check_severe(self):
+        """people.py:242-246."""
+        return self._check(L.CHECK_SEVERE)[0]
+
+    def check_critical(self):
+        """people.py:249-253."""
+        return self._check(L.CHECK_CRITICAL)[0]
+
+    def check_recovery(self, inds=None, filter_inds='is_exp'):
+        """people.py:256-291: recovery of the exposed whose date has come (or of
+        exactly ``inds`` when given); with waning they become susceptible again.
+        filter_inds 'is_exp' checks the exposed, None every agent."""
+        if inds is not None:
+            return self._check(L.CHECK_RECOVERY, inds=np.asarray(inds))[0]
+        if filter_inds is not None and not (isinstance(filter_inds, str) and filter_inds == 'is_exp'):
+            raise NotImplementedError("check_recovery: filter_inds must be 'is_exp' or None on the GPU path")
+        return self._check(L.CHECK_RECOVERY, filter_exposed=filter_inds is not None)[0]
+
+    def check_death(self):
+        """people.py:294-312: returns (indices, deaths, deaths of the diagnosed)."""
+        inds, known = self._check(L.CHECK_DEATH)
+        return inds, len(inds), int(known)
+
+    def check_exit_iso(self):
+        """people.py:368-374: isolation ends on its date; returns the released."""
+        return self._check(L.CHECK_EXIT_ISO, filter_exposed=False)[0]
 
     @property
     def infection_log(self):

@@ -25,6 +25,7 @@ import torch
 
 from . import _lib as L
 from . import defaults as cvd
+from . import torch_ops  # noqa: F401  (registers torch.ops.covgpu.*)
 
 F32, I32, I64, F64 = torch.float32, torch.int32, torch.int64, torch.float64
 getcontext().prec = 50
@@ -118,6 +119,43 @@ class SimSpec:
 IMPORT_TAG = 0x1B1B
 RESCALE_TAG = 0x5C5C
 HOLD_NONE = 0x7FFFFFFF
+
+
+def dynamic_count_table(n_edges, n_agents):
+    """The length distribution of one agent's contact list in a dynamic layer.
+
+    Layer.update (base.py:1849-1876) redraws all n_edges edges of the layer with
+    both endpoints uniform over the n_agents agents, so the edges of one agent as
+    p1 (and, separately, as p2) number Binomial(n_edges, 1 / n_agents). Returns
+    uint64 thresholds: entry k = floor(2^64 * P(count <= k)), the last entry
+    2^64 - 1 (at the first k whose upper tail is below 2^-64, at most
+    L.DYN_MAX_LIST entries). 50-digit decimal arithmetic, identical on every
+    platform."""
+    E, n = int(n_edges), int(n_agents)
+    top = (1 << 64) - 1
+    one = Decimal(1)
+    if n == 1:
+        if E >= L.DYN_MAX_LIST:
+            raise ValueError('dynamic layer: contact lists longer than the supported maximum')
+        return np.array([0] * E + [top], dtype=np.uint64)
+    p = one / Decimal(n)
+    q = one - p
+    term = (Decimal(E) * q.ln()).exp()  # P(count = 0)
+    tail_limit = Decimal(2) ** -64
+    acc = Decimal(0)
+    table = []
+    for k in range(L.DYN_MAX_LIST):
+        acc += term
+        if one - acc < tail_limit or k == E:
+            table.append(top)
+            return np.array(table, dtype=np.uint64)
+        table.append(min(int(acc * (1 << 64)), top))
+        term = term * Decimal(E - k) / Decimal(k + 1) * p / q
+    if one - acc > Decimal(2) ** -40:
+        raise ValueError('dynamic layer: contact lists longer than the supported maximum (too many contacts '
+                         'per agent)')
+    table[-1] = top
+    return np.array(table, dtype=np.uint64)
 
 
 def daily_importations(seed, rate, n, npts, start=0):
@@ -457,6 +495,9 @@ class BatchState:
                 if ly.get('dynamic'):
                     rec.dynamic = 1
                     rec.beta_const = 1.0
+                    cdf = torch.from_numpy(dynamic_count_table(n_edges, sp.n).view(np.int64)).to(self.device)
+                    rec.dyn_cdf, rec.dyn_k = cdf.data_ptr(), len(cdf)
+                    keep.append(cdf)
                 elif torch.is_tensor(ly['p1']):
                     # torch inputs (e.g. pinned host memory): uploaded as they are, checked on the
                     # device; the checks of every layer are read back together below, before
@@ -536,12 +577,15 @@ class BatchState:
         return [rp1, rp2, perm2]
 
     def _tile_segments(self):
-        """Each segment's first tile and the tile count for the current edge tile size."""
+        """Each segment's first tile and the tile count for the current edge tile size
+        (a dynamic layer has no tiles: the edge pass draws its edges from the day's sources)."""
         tiles = 0
         for rec in self.segments:
             rec.tile_begin = tiles
-            tiles += (rec.n_edges + self.edge_tile - 1) // self.edge_tile
+            if not rec.dynamic:
+                tiles += (rec.n_edges + self.edge_tile - 1) // self.edge_tile
         self.n_tiles = tiles
+        self.n_dynamic = sum(1 for rec in self.segments if rec.dynamic)
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
         self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
 
@@ -691,6 +735,7 @@ class BatchState:
         st.n_sims = len(self.specs)
         st.n_segments = len(self.segments)
         st.n_tiles = self.n_tiles
+        st.n_dynamic = self.n_dynamic
         st.n_agent_blocks = self.n_agent_blocks
         st.edge_tile = self.edge_tile
         st.edge_resident = int(self.edge_resident)
@@ -807,7 +852,7 @@ class BatchState:
 
     def lik_targets(self, t):
         """Per-target half of day t's likelihood (after edge_pass, before infect_claims)."""
-        L.call('covgpu_lik_targets', self.cstate_ptr, int(t), _stream())
+        torch.ops.covgpu.lik_targets(self._sa, int(t), self.t['status'])
 
     def set_beta_tables(self, beta_sched, beta_layer_sched, sim=0):
         """Overwrite one sim's per-day beta tables in place (float64 schedules,
@@ -822,19 +867,24 @@ class BatchState:
         self.beta_tab[b0:b0 + bt.numel()].copy_(bt)
         self.beta_layer_tab[l0:l0 + bl.numel()].copy_(bl)
 
-    # ------------------------------------------------------------------ kernels
+    # ------------------------------------------------------------------ kernels (torch.ops.covgpu.*)
+    @property
+    def _sa(self):
+        """The ops' state argument: the address of the current covgpu_state descriptor."""
+        return torch_ops.state_arg(self.cstate)
+
     def agent_step(self, t, do_prev=True, do_day=True):
-        L.call('covgpu_agent_step', self.cstate_ptr, int(t), int(do_prev), int(do_day), _stream())
+        torch.ops.covgpu.agent_step(self._sa, int(t), bool(do_prev), bool(do_day), self.t['status'])
 
     def edge_pass(self, t):
-        L.call('covgpu_edge_pass', self.cstate_ptr, int(t), _stream())
+        torch.ops.covgpu.edge_pass(self._sa, int(t), self.t['status'])
 
     def infect_claims(self, t):
-        L.call('covgpu_infect_claims', self.cstate_ptr, int(t), _stream())
+        torch.ops.covgpu.infect_claims(self._sa, int(t), self.t['status'])
 
     def test_trace(self, t):
         """Day t's testing, tracing and update_states_post (no-op without testing)."""
-        L.call('covgpu_test_trace', self.cstate_ptr, int(t), _stream())
+        torch.ops.covgpu.test_trace(self._sa, int(t), self.t['status'])
 
     def make_nonnaive(self, inds, sim=0):
         """people.py:414-431 make_nonnaive on agents still in their initial state:
@@ -850,33 +900,90 @@ class BatchState:
 
     def import_day(self, t):
         """Day t's importations of every sim (sim.py:582-587; no-op without them)."""
-        L.call('covgpu_import_day', self.cstate_ptr, int(t), _stream())
+        torch.ops.covgpu.import_day(self._sa, int(t), self.t['status'])
 
-    def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=1):
-        """Infect explicit agents of one sim (local indices; deduplicated and sorted here)."""
-        inds = np.unique(np.asarray(inds, dtype=np.int64))
+    def infect_list(self, t, inds, sim=0, variant=0, layer_tag=L.LOG_SEED, call_tag=1, sources=None,
+                    want_infected=False):
+        """Infect explicit agents of one sim (local indices; deduplicated and sorted
+        here, the first occurrence's source kept, as people.py:465-468 does). With
+        want_infected, returns (inds, mask of the agents actually infected) as
+        device tensors; the susceptible alone are infected (people.py:470-474)."""
+        inds, first = np.unique(np.asarray(inds, dtype=np.int64), return_index=True)
         if len(inds) == 0:
-            return
+            return (inds, np.zeros(0, bool)) if want_infected else None
         if inds.min() < 0 or inds.max() >= self.specs[sim].n:
             raise IndexError('agent index out of range')
         g = torch.from_numpy((inds + self.offsets[sim]).astype(np.int32)).to(self.device)
-        self._keep_inds = g
-        L.call('covgpu_infect_list', self.cstate_ptr, int(t), g.data_ptr(), len(inds), int(sim), int(variant),
-               int(layer_tag), int(call_tag), _stream())
+        src = None
+        if sources is not None:
+            src = torch.from_numpy(np.asarray(sources, dtype=np.int32)[first]).to(self.device)
+        infected = torch.empty(len(inds), dtype=torch.uint8, device=self.device) if want_infected else None
+        self._keep_inds = (g, src)
+        torch.ops.covgpu.infect_list(self._sa, int(t), g, src, int(sim), int(variant), int(layer_tag), int(call_tag),
+                                     infected, self.t['status'])
+        return (inds, infected) if want_infected else None
 
     def run_days(self, t0, t1, open_prev=False, close_last=True, use_graph=True):
-        L.call('covgpu_run_days', self.cstate_ptr, int(t0), int(t1), int(open_prev), int(close_last), int(use_graph),
-               _stream())
+        torch.ops.covgpu.run_days(self._sa, int(t0), int(t1), bool(open_prev), bool(close_last), bool(use_graph),
+                                  self.t['status'])
 
-    def materialize_layer(self, sim, layer, t):
-        """Endpoints of a dynamic layer on day t (local indices)."""
+    # ------------------------------------------------------------------ single functions of the day path
+    def check(self, t, which, sim=0, filter_exposed=True, inds=None):
+        """One of People.check_infectious ... check_death, check_exit_iso
+        (people.py:222-312, 368-374; which: L.CHECK_*) at day t: applies it and
+        returns (sorted local indices of the agents changed, known deaths)."""
+        n = self.specs[sim].n
+        ti = None
+        if inds is not None:
+            ti = torch.as_tensor(np.asarray(inds, dtype=np.int32)).to(self.device)
+        out = torch.empty(max(n if ti is None else ti.numel(), 1), dtype=I32, device=self.device)
+        counts = torch.zeros(2, dtype=I64, device=self.device)
+        torch.ops.covgpu.check(self._sa, int(t), int(which), int(sim), bool(filter_exposed), ti, n, out, counts,
+                               self.t['status'])
+        c = counts.cpu().tolist()
+        return torch.sort(out[:c[0]]).values, c[1]
+
+    def check_immunity(self, t, sim=0, variants=None):
+        """check_immunity (immunity.py:303-350) for the given variants (all if None)."""
+        nv = self.specs[sim].nv
+        mask = (1 << nv) - 1 if variants is None else sum(1 << int(v) for v in variants)
+        torch.ops.covgpu.check_immunity(self._sa, int(t), int(sim), int(mask), self.t['status'])
+
+    def update_nab(self, t, inds, sim=0):
+        """update_nab (immunity.py:205-213) for local agents inds."""
+        ti = torch.as_tensor(np.asarray(inds, dtype=np.int32)).to(self.device)
+        if ti.numel():
+            torch.ops.covgpu.update_nab(self._sa, int(t), int(sim), ti, self.t['status'])
+
+    def update_peak_nab(self, t, inds, nab_init, nab_boost, norm_factor=1.0, symp_class=None, sim=0, call_tag=2):
+        """update_peak_nab (immunity.py:138-202) for local agents inds: nab_init a
+        distribution dict, symp_class per agent (0/1/2) or None for vaccine NAbs."""
+        ti = torch.as_tensor(np.asarray(inds, dtype=np.int32)).to(self.device)
+        if not ti.numel():
+            return
+        sc = None if symp_class is None else torch.as_tensor(np.asarray(symp_class, dtype=np.int8)).to(self.device)
+        d = dur_par(nab_init)
+        torch.ops.covgpu.update_peak_nab(self._sa, int(t), int(sim), ti, sc, int(d.code), float(d.a), float(d.b),
+                                         float(nab_boost), float(norm_factor), int(call_tag), self.t['status'])
+
+    def layer_lists(self, sim, layer, t, agents=None):
+        """The day-t contact lists of a dynamic layer (covgpu_layer_lists): for the
+        local agents ``agents`` (a range start, count pair, or None for all of the
+        sim's agents) returns (counts [m, 2], offsets [2m + 1], partners) as device
+        tensors; partners[offsets[2i + d]:offsets[2i + d + 1]] are the local
+        partners of list d (0: the agent as p1, 1: as p2) of agent i."""
         seg = self.segment_index[(sim, layer)]
-        n_edges = self.segments[seg].n_edges
-        p1 = torch.empty(n_edges, dtype=I32, device=self.device)
-        p2 = torch.empty(n_edges, dtype=I32, device=self.device)
-        L.call('covgpu_layer_materialize', self.cstate_ptr, int(seg), int(t), p1.data_ptr(), p2.data_ptr(),
-               _stream())
-        return p1, p2
+        if not self.segments[seg].dynamic:
+            raise ValueError('layer_lists: the layer is not dynamic')
+        begin, m = (0, self.specs[sim].n) if agents is None else (int(agents[0]), int(agents[1]))
+        counts = torch.empty(2 * m, dtype=I32, device=self.device)
+        torch.ops.covgpu.layer_lists(self._sa, int(seg), int(t), begin, m, counts, None, None, self.t['status'])
+        offsets = torch.zeros(2 * m + 1, dtype=I64, device=self.device)
+        torch.cumsum(counts.to(I64), 0, out=offsets[1:])
+        partners = torch.empty(max(int(offsets[-1].item()), 1), dtype=I32, device=self.device)
+        torch.ops.covgpu.layer_lists(self._sa, int(seg), int(t), begin, m, counts, offsets, partners,
+                                     self.t['status'])
+        return counts.view(m, 2), offsets, partners[:int(offsets[-1].item())]
 
     # ------------------------------------------------------------------ snapshots
     MUTABLE = ('flags', 'vstate', 'rel_trans', 'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event',

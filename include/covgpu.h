@@ -26,7 +26,13 @@
  *                            (seed infections, sim.py:505-532; variant importations,
  *                            immunity.py:117-130)
  *   covgpu_import_day        covasim/sim.py:582-587 the day's Poisson importations
- *   covgpu_layer_materialize covasim/base.py:1849-1876 Layer.update (dynamic layer view)
+ *   covgpu_layer_lists       covasim/base.py:1849-1876 Layer.update: a dynamic layer's day-t
+ *                            edges, as per-agent lists
+ *   covgpu_check             covasim/people.py:222-312,368-374 People.check_infectious ...
+ *                            check_death, check_exit_iso, one at a time
+ *   covgpu_check_immunity    covasim/immunity.py:303-350 check_immunity
+ *   covgpu_update_nab        covasim/immunity.py:205-213 update_nab
+ *   covgpu_update_peak_nab   covasim/immunity.py:138-202 update_peak_nab
  */
 #ifndef COVGPU_H
 #define COVGPU_H
@@ -171,25 +177,38 @@ typedef struct covgpu_sim_params {
                                      are in that count, the last day checked        */
 } covgpu_sim_params;
 
-/* One contact layer of one sim (device memory, one entry per layer segment). */
+/* One contact layer of one sim (device memory, one entry per layer segment).
+ *
+ * A dynamic layer (base.py:1849-1876 Layer.update: every day all n_edges
+ * edges redrawn with both endpoints uniform over the sim's agents) stores no
+ * edges. Its day-t edges are drawn per agent: the edges of agent a as p1 and
+ * as p2 are two lists, each of Binomial(n_edges, 1 / n_agents) entries with
+ * uniform partners, keyed by (seed, a, day, layer). The edge pass draws the
+ * lists of the day's sources only, the tracing pass those of the traced
+ * agents (covgpu_layer_lists writes them out). dyn_cdf holds the count
+ * distribution: dyn_cdf[k] = floor(2^64 * P(count <= k)) for k < dyn_k - 1
+ * and dyn_cdf[dyn_k - 1] = 2^64 - 1, with dyn_k <= COVGPU_DYN_MAX_LIST. */
+#define COVGPU_DYN_MAX_LIST 1024
 typedef struct covgpu_layer {
   const int32_t* p1;              /* global agent indices, sorted ascending (static) */
   const int32_t* p2;
   const float* beta;              /* per-edge beta, or NULL: every edge has beta_const */
   int64_t n_edges;
-  int64_t tile_begin;             /* first edge-pass tile of this segment            */
+  int64_t tile_begin;             /* first edge-pass tile of this segment (a dynamic
+                                     layer has no tiles)                           */
   int32_t sim;
   int32_t layer;                  /* layer index within the sim (0..n_layers-1)      */
   int32_t dynamic;                /* 1: edges redrawn every day (p1/p2 unused)       */
   float beta_const;
   float iso_factor, quar_factor;
-  int32_t _pad;
+  int32_t dyn_k;                  /* dynamic: entries of dyn_cdf                    */
   /* contact-tracing index of a stored layer (NULL: none; covgpu_trace_index):
    * the agent a's edges as p1 are [rp1[a], rp1[a+1]), as p2 the edges
    * perm2[rp2[a] .. rp2[a+1]) (a local to the sim) */
   const uint32_t* rp1;
   const uint32_t* rp2;
   const uint32_t* perm2;
+  const uint64_t* dyn_cdf;        /* dynamic: [dyn_k] count distribution (above)     */
 } covgpu_layer;
 
 /* One agent block of the agent kernel: agents [begin, end) of one sim. */
@@ -301,7 +320,8 @@ typedef struct covgpu_state {
   const int32_t* imports;
   const int32_t* import_sims;
   int32_t import_days;            /* days covered; 0: no importations                */
-  int32_t _pad3;
+  int32_t n_dynamic;              /* dynamic layer segments (the edge pass draws their
+                                     edges from the day's sources' lists)           */
   /* the first day held back for a host step (a due rescaling, found by the
    * day's rescale check); 0x7FFFFFFF: none. Every day kernel of a held day
    * returns at once, the agent pass of the held day closes the day before it.
@@ -428,7 +448,9 @@ int covgpu_pop_prognoses(int64_t n, const float* age, const double* cutoffs, int
 int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_t do_day, void* stream);
 
 /* Transmission over every layer segment and variant: both directions of each
- * edge from one read, Bernoulli draws from Philox (or st->edge_uniforms),
+ * stored edge from one read, the dynamic layers' edges from the day's
+ * sources' lists, Bernoulli draws from Philox (or, for stored layers,
+ * st->edge_uniforms),
  * events appended to st->events and the first infector of each target
  * claimed with a 64-bit atomicMin on (day, variant, layer, direction, edge).
  * With st->lik.factor set, also the likelihood terms of every candidate
@@ -469,13 +491,18 @@ int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, in
 /* infect() for the winning event of each target. */
 int covgpu_infect_claims(const covgpu_state* st, int32_t t, void* stream);
 
-/* infect() for an explicit list of global agent indices (unique). layer_tag is
- * recorded in the infection log (>= COVGPU_MAX_LAYERS for non-layer sources);
+/* infect() for an explicit list of global agent indices (unique), as
+ * People.infect(inds, source=..., layer=..., variant=...) does: only the
+ * susceptible are infected. sources (or NULL: none) holds each target's
+ * source as a local index, recorded in the infection log (people.py:508-511)
+ * with layer_tag (>= COVGPU_MAX_LAYERS for non-layer sources); infected (or
+ * NULL) receives 1 for each agent actually infected, 0 for the others.
  * call_tag selects the Philox stream (1: seed infections, 2+: importations).
  * Seed infections (call_tag 1) are not counted in the day's flows: the
  * reference seeds before update_states_pre resets them (sim.py:571-577). */
-int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, int64_t n_inds,
-                       int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, void* stream);
+int covgpu_infect_list(const covgpu_state* st, int32_t t, const int32_t* inds, const int32_t* sources, int64_t n_inds,
+                       int32_t sim, int32_t variant, int32_t layer_tag, int32_t call_tag, uint8_t* infected,
+                       void* stream);
 
 /* The day's importations (sim.py:582-587): infect() with the wild type for the
  * agents st->imports lists for day t (all sims; infection log layer
@@ -493,10 +520,15 @@ int covgpu_import_day(const covgpu_state* st, int32_t t, void* stream);
  * n_agents > rescale_threshold; if so *st->hold = t (the earliest such day). */
 int covgpu_rescale_check(const covgpu_state* st, int32_t t, void* stream);
 
-/* Write the day-t endpoints of one dynamic layer segment into p1/p2 (the
- * same edges the edge pass draws that day). */
-int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t, int32_t* p1, int32_t* p2,
-                             void* stream);
+/* The day-t contact lists of agents [agent_begin, agent_begin + n_agents)
+ * (local to the segment's sim) in one dynamic layer segment: the draws the
+ * edge pass makes for a source and the tracing pass for a traced agent. With
+ * offsets NULL, counts[2 i + d] receives the length of list d (0: the agent
+ * as p1, 1: as p2) of agent agent_begin + i; with offsets (the exclusive sum
+ * of those counts, 2 n_agents + 1 entries), partners[offsets[2 i + d] + j]
+ * receives partner j of that list (local index) and counts is unused. */
+int covgpu_layer_lists(const covgpu_state* st, int32_t segment, int32_t t, int64_t agent_begin, int64_t n_agents,
+                       int32_t* counts, const int64_t* offsets, int32_t* partners, void* stream);
 
 /* Run days [t0, t1) of every sim: per day agent_step, test_trace (when
  * st->has_testing), edge_pass, lik_targets (when st->lik.factor is set),
@@ -507,6 +539,54 @@ int covgpu_layer_materialize(const covgpu_state* st, int32_t segment, int32_t t,
  * the state and the arguments are unchanged). */
 int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open_prev, int32_t close_last,
                     int32_t use_graph, void* stream);
+
+/* ---- the day path one function at a time --------------------------------
+ * For callers that keep the reference's call sequence (update_states_pre's
+ * checks one by one, check_immunity, update_nab, update_peak_nab) instead of
+ * the fused kernels. Agents are local indices of sim `sim`; each function
+ * writes the same state as the fused passes, with the same arithmetic. */
+
+/* which People.check_* covgpu_check runs */
+enum { COVGPU_CHECK_INFECTIOUS = 0, COVGPU_CHECK_SYMPTOMATIC, COVGPU_CHECK_SEVERE, COVGPU_CHECK_CRITICAL,
+       COVGPU_CHECK_RECOVERY, COVGPU_CHECK_DEATH, COVGPU_CHECK_EXIT_ISO };
+
+/* covasim/people.py:222-312, 368-374 People.check_infectious, check_symptomatic,
+ * check_severe, check_critical, check_recovery, check_death, check_exit_iso at
+ * day t over the sim's n_agents agents: applies the transition and writes the
+ * local indices of the agents it changed to out (in no particular order; at
+ * most capacity, else COVGPU_OVERFLOW in the device status word). counts
+ * (device, 2 entries, zeroed first): the agents changed, and for check_death
+ * those of them diagnosed (the known deaths). filter_exposed: only exposed
+ * agents (the reference's is_exp, its snapshot of the exposed flag at the start
+ * of update_states_pre, which equals the current flag for every check run in
+ * update_states_pre's order); check_exit_iso takes no filter. inds (recovery
+ * only, else NULL): recover exactly these n_inds agents, as check_recovery's
+ * inds argument does. Indices outside the sim set COVGPU_BADARG in the device
+ * status word and are skipped. */
+int covgpu_check(const covgpu_state* st, int32_t t, int32_t which, int32_t sim, int32_t filter_exposed,
+                 const int32_t* inds, int64_t n_inds, int64_t n_agents, int32_t* out, int64_t capacity,
+                 int64_t* counts, void* stream);
+
+/* covasim/immunity.py:303-350 check_immunity(people, variants): sus_imm,
+ * symp_imm and sev_imm of every agent of the sim for the variants whose bit is
+ * set in variant_mask, at day t. */
+int covgpu_check_immunity(const covgpu_state* st, int32_t t, int32_t sim, uint32_t variant_mask, void* stream);
+
+/* covasim/immunity.py:205-213 update_nab(people, inds) at day t: nab += nab_kin[t
+ * - t_nab_event] * peak_nab, clamped to [0, peak_nab]. */
+int covgpu_update_nab(const covgpu_state* st, int32_t t, int32_t sim, const int32_t* inds, int64_t n_inds,
+                      void* stream);
+
+/* covasim/immunity.py:138-202 update_peak_nab(people, inds, nab_pars, symp) at day
+ * t: agents with NAbs have peak_nab *= nab_boost; the others get 2^x with x ~
+ * nab_init (one standard normal per agent from the Philox stream (seed, agent,
+ * day, call_tag), block 3, which infect()'s draws leave unused), times
+ * rel_imm_symp of symp_class[i] (0 asymptomatic, 1 mild, 2 severe) and
+ * norm_factor when symp_class is given (natural infection), unscaled when it is
+ * NULL (vaccination); t_nab_event = t for all. */
+int covgpu_update_peak_nab(const covgpu_state* st, int32_t t, int32_t sim, const int32_t* inds, int64_t n_inds,
+                           const int8_t* symp_class, covgpu_dur_par nab_init, float nab_boost, double norm_factor,
+                           int32_t call_tag, void* stream);
 
 /* Library/ABI version. */
 int covgpu_version(void);

@@ -138,8 +138,11 @@ class ContactTracing:
         for lkey, prob in self.trace_probs.items():
             if prob == 0:
                 continue
-            layer = sim.contacts[lkey]
-            traceable = find_contacts(layer['p1'], layer['p2'], trace_inds)
+            if lkey in getattr(sim, 'dyn_tables', {}):  # philox mode: the traced agents' own lists
+                traceable = np.unique(sim.dynamic_lists(lkey, trace_inds)[3])
+            else:
+                layer = sim.contacts[lkey]
+                traceable = find_contacts(layer['p1'], layer['p2'], trace_inds)
             if len(traceable):
                 if sim.rng == 'philox':
                     u = ph.trace_draws(sim.k0, sim.k1, t, sim.layer_keys.index(lkey), traceable)

@@ -13,8 +13,8 @@ Stream layout (shared with the CUDA side; all words little-endian uint32):
   key     = (seed_lo, seed_hi)                        64-bit per-sim seed
   counter = (c0, c1, c2, c3)
     edge Bernoulli      : (edge_lo, edge_hi, day, TAG_EDGE  | variant << 8 | layer)
-    dynamic-layer edges : (pair_lo, pair_hi, day, TAG_LAYER | layer), one block per two edges;
-                          redraws (edge_lo, edge_hi, day, TAG_LAYER_RETRY | try << 8 | layer)
+    dynamic-layer lists : counts (agent, 0, day, TAG_DYN | layer); partners (agent, 1 + d * 256 + j // 4,
+                          day, TAG_DYN | layer); redraws (agent, d << 10 | j, day, TAG_DYN_RETRY | try << 8 | layer)
     infect draws        : (agent,   block,   day, TAG_INFECT | call_tag)
     testing draws       : (agent,   block,   day, TAG_TEST)  block 0: test, sensitivity; 1: follow-up
     tracing draws       : (agent,   layer,   day, TAG_TRACE)
@@ -32,11 +32,11 @@ PHILOX_W0 = np.uint32(0x9E3779B9)
 PHILOX_W1 = np.uint32(0xBB67AE85)
 
 TAG_EDGE = 0x01000000
-TAG_LAYER = 0x02000000
 TAG_INFECT = 0x03000000
 TAG_TEST = 0x04000000
 TAG_TRACE = 0x05000000
-TAG_LAYER_RETRY = 0x07000000
+TAG_DYN = 0x08000000
+TAG_DYN_RETRY = 0x09000000
 
 _MASK32 = np.uint64(0xFFFFFFFF)
 
@@ -116,41 +116,108 @@ def edge_uniforms(k0, k1, day, layer, variant, edges):
     return u01_52(w[0], w[1]), u01_52(w[2], w[3])
 
 
-def bounded_draw(x, n, edges, which, k0, k1, day, layer):
-    """Unbiased integers in [0, n) from 32-bit words (Lemire 2019): the high half of
-    x * n, redrawn while the low half is below 2**32 mod n; redraw r of endpoint
-    ``which`` of edge e is word x (which 0) or y (which 1) of Philox
-    (e, day, TAG_LAYER_RETRY | r << 8 | layer); at most 16 redraws."""
-    n = int(n)
-    thr = np.uint64((2 ** 32 - n) % n)
-    m = np.asarray(x, dtype=np.uint64) * np.uint64(n)
-    edges = np.asarray(edges, dtype=np.int64)
-    bad = (m & _MASK32) < thr
+# ----------------------------------------------------------------------------- redrawn layers
+# A layer redrawn every day (covasim/base.py:1849-1876, Layer.update with frac=1)
+# has E edges with i.i.d. uniform endpoints over n agents. In philox mode the
+# day's edges of agent a are two lists (d = 0: a as p1, d = 1: a as p2), each of
+# Binomial(E, 1/n) entries with uniform partners; the lists of an agent are drawn
+# only where they are needed (the day's sources for transmission, the traced
+# agents for contact tracing).
+DYN_MAX_LIST = 1024
+_M40 = (1 << 40) - 1
+
+
+def dyn_count_table(n_edges, n_agents):
+    """The list-length distribution Binomial(n_edges, 1 / n_agents) as 64-bit
+    thresholds: entry k = floor(2**64 * P(count <= k)), the last entry 2**64 - 1
+    (the first k where the upper tail falls below 2**-64, at most DYN_MAX_LIST
+    entries). Computed in 50-digit decimal arithmetic, so every platform gets
+    the same table."""
+    from decimal import Decimal, localcontext
+    E, n = int(n_edges), int(n_agents)
+    top = (1 << 64) - 1
+    with localcontext() as ctx:
+        ctx.prec = 50
+        if n == 1:  # every edge is the agent's own
+            if E >= DYN_MAX_LIST:
+                raise ValueError('dynamic layer lists longer than the supported maximum')
+            return np.array([0] * E + [top], dtype=np.uint64)
+        p = Decimal(1) / Decimal(n)
+        q = 1 - p
+        pmf = (Decimal(E) * q.ln()).exp()
+        cdf = Decimal(0)
+        eps = Decimal(2) ** -64
+        out = []
+        for k in range(DYN_MAX_LIST):
+            cdf += pmf
+            if 1 - cdf < eps or k == E:
+                out.append(top)
+                return np.array(out, dtype=np.uint64)
+            out.append(min(int(cdf * (1 << 64)), top))
+            pmf = pmf * Decimal(E - k) / Decimal(k + 1) * p / q
+        if 1 - cdf > Decimal(2) ** -40:
+            raise ValueError('dynamic layer lists longer than the supported maximum (mean contacts too high)')
+        out[-1] = top
+        return np.array(out, dtype=np.uint64)
+
+
+def dyn_edge_id(a, j, day, layer):
+    """Identity of entry j of an agent's list: a bijection of a << 10 | j on 40
+    bits, salted by the day and layer (its order decides the first infector
+    among one layer's transmissions to the same target)."""
+    a = np.asarray(a, dtype=np.uint64)
+    j = np.asarray(j, dtype=np.uint64)
+    salt = np.uint64(((((int(day) << 8) | int(layer)) * 0x9E3779B97F) & _M40))
+    m40 = np.uint64(_M40)
+    x = ((a << np.uint64(10)) | j) ^ salt
+    x = (x * np.uint64(0xD6E8FEB86659D)) & m40
+    x ^= x >> np.uint64(21)
+    x = (x * np.uint64(0xA0761D6478BD)) & m40
+    x ^= x >> np.uint64(19)
+    return x.astype(np.int64)
+
+
+def dyn_counts(k0, k1, day, layer, agents, table):
+    """Lengths of the two lists of each agent: [m, 2] int64 (64-bit uniforms from
+    words x:y and z:w of Philox (agent, 0, day, TAG_DYN | layer))."""
+    a = np.asarray(agents, dtype=np.int64)
+    w = philox4x32_10(a, 0, day, TAG_DYN | int(layer), k0, k1)
+    out = np.empty((len(a), 2), dtype=np.int64)
+    for d, (hi, lo) in enumerate(((w[0], w[1]), (w[2], w[3]))):
+        u = (hi.astype(np.uint64) << np.uint64(32)) | lo.astype(np.uint64)
+        out[:, d] = np.minimum(np.searchsorted(table, u, side='right'), len(table) - 1)
+    return out
+
+
+def dyn_lists(k0, k1, day, layer, agents, table, n_agents):
+    """Every entry of the two lists of each agent: arrays (agent, d, j, partner),
+    ordered by agent, then d, then j. Partner j of list d is word j % 4 of
+    Philox (agent, 1 + 256 d + j // 4, day, TAG_DYN | layer), made an unbiased
+    integer below n_agents (Lemire 2019: the high half of x * n, redrawn while
+    the low half is below 2**32 mod n; redraw r is word x of Philox
+    (agent, d << 10 | j, day, TAG_DYN_RETRY | r << 8 | layer), at most 16)."""
+    a = np.asarray(agents, dtype=np.int64)
+    counts = dyn_counts(k0, k1, day, layer, a, table)
+    reps = counts.reshape(-1)
+    ag = np.repeat(np.repeat(a, 2), reps)
+    dd = np.repeat(np.tile(np.array([0, 1], dtype=np.int64), len(a)), reps)
+    starts = np.cumsum(reps) - reps
+    jj = np.arange(len(ag), dtype=np.int64) - np.repeat(starts, reps)
+    w = philox4x32_10(ag, 1 + 256 * dd + (jj >> 2), day, TAG_DYN | int(layer), k0, k1)
+    x = np.choose(jj & 3, [w[0], w[1], w[2], w[3]]).astype(np.uint64)
+    n = np.uint64(n_agents)
+    thr = np.uint64((2 ** 32 - int(n_agents)) % int(n_agents))
+    m = x * n
+    mask32 = np.uint64(0xFFFFFFFF)
+    bad = (m & mask32) < thr
     for r in range(16):
         if not bad.any():
             break
         idx = np.nonzero(bad)[0]
-        e = edges[idx]
-        w = philox4x32_10(e & 0xFFFFFFFF, e >> 32, day, TAG_LAYER_RETRY | (r << 8) | int(layer), k0, k1)
-        m[idx] = w[which].astype(np.uint64) * np.uint64(n)
-        bad[idx] = (m[idx] & _MASK32) < thr
-    return (m >> np.uint64(32)).astype(np.int64)
-
-
-def dynamic_edges(k0, k1, day, layer, n_edges, n_agents):
-    """Endpoints of a dynamic layer on one day: n_edges i.i.d. uniform pairs. One
-    Philox block (j, day, TAG_LAYER | layer) serves edges 2j (words x, y) and
-    2j + 1 (words z, w)."""
-    n_pairs = (int(n_edges) + 1) // 2
-    j = np.arange(n_pairs, dtype=np.int64)
-    w = philox4x32_10(j & 0xFFFFFFFF, j >> 32, day, TAG_LAYER | int(layer), k0, k1)
-    p1 = np.empty(2 * n_pairs, dtype=np.int64)
-    p2 = np.empty(2 * n_pairs, dtype=np.int64)
-    p1[0::2] = bounded_draw(w[0], n_agents, 2 * j, 0, k0, k1, day, layer)
-    p2[0::2] = bounded_draw(w[1], n_agents, 2 * j, 1, k0, k1, day, layer)
-    p1[1::2] = bounded_draw(w[2], n_agents, 2 * j + 1, 0, k0, k1, day, layer)
-    p2[1::2] = bounded_draw(w[3], n_agents, 2 * j + 1, 1, k0, k1, day, layer)
-    return p1[:n_edges].astype(np.int32), p2[:n_edges].astype(np.int32)
+        rw = philox4x32_10(ag[idx], (dd[idx] << 10) | jj[idx], day, TAG_DYN_RETRY | (r << 8) | int(layer), k0, k1)
+        m[idx] = rw[0].astype(np.uint64) * n
+        bad[idx] = (m[idx] & mask32) < thr
+    return ag, dd, jj, (m >> np.uint64(32)).astype(np.int64)
 
 
 # Slots of the per-infection draw table (shared with the CUDA side).

@@ -7,8 +7,9 @@ Two random-number modes:
 
 * ``rng='philox'``: every draw is keyed exactly like the CUDA library keys it
   (edge Bernoullis by (seed, day, layer, variant, edge); infection draws by
-  (seed, day, agent, call); dynamic layers by (seed, day, layer, edge)), so a
-  GPU run and this loop agree draw for draw.
+  (seed, day, agent, call); a dynamic layer's day as per-agent contact lists
+  keyed by (seed, day, layer, agent), drawn for the day's sources), so a GPU
+  run and this loop agree draw for draw.
 * ``rng='mt'``: two MT19937 streams seeded with the sim's seed, one standing in
   for numba's (edge Bernoullis, ``choose``/``choose_r``) and one for numpy's
   (``infect`` and ``set_prognoses``), consumed in the reference's call order.
@@ -102,6 +103,12 @@ class OracleSim:
         self.contacts = {k: {c: np.array(v[c]) for c in ('p1', 'p2', 'beta')} for k, v in contacts.items()}
         self.layer_keys = list(self.contacts.keys())
         self.rng = rng
+        # philox mode: a dynamic layer's day is drawn as per-agent lists (ph.dyn_lists)
+        self.dyn_tables = {}
+        if rng == 'philox':
+            for lkey in self.layer_keys:
+                if pars['dynam_layer'].get(lkey, 0) and len(self.contacts[lkey]['p1']):
+                    self.dyn_tables[lkey] = ph.dyn_count_table(len(self.contacts[lkey]['p1']), self.n)
         self.seed = int(pars['rand_seed'])
         self.k0, self.k1 = ph.seed_key(self.seed)
         if rng == 'mt':
@@ -199,19 +206,61 @@ class OracleSim:
         self.results['n_imports'][t] += n_imp
 
     def update_contacts(self):
-        """people.py:199-206 -> base.py:1849-1876 (Layer.update, frac=1)."""
+        """people.py:199-206 -> base.py:1849-1876 (Layer.update, frac=1). In philox
+        mode a dynamic layer is not materialised: its day's edges are the per-agent
+        lists that ``dynamic_lists`` draws where they are needed."""
         for li, lkey in enumerate(self.layer_keys):
             if self.pars['dynam_layer'].get(lkey, 0):
                 layer = self.contacts[lkey]
                 n_new = len(layer['p1'])
                 if self.rng == 'philox':
-                    p1, p2 = ph.dynamic_edges(self.k0, self.k1, self.t, li, n_new, self.n)
-                    layer['p1'], layer['p2'] = p1, p2
-                else:
-                    inds = self.rs_numba.permutation(n_new)
-                    layer['p1'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
-                    layer['p2'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
+                    continue
+                inds = self.rs_numba.permutation(n_new)
+                layer['p1'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
+                layer['p2'][inds] = self.rs_numba.randint(0, self.n, n_new).astype(np.int32)
                 layer['beta'] = np.ones(n_new, dtype=F32)
+
+    def dynamic_lists(self, lkey, agents):
+        """Day t's contact lists of ``agents`` in dynamic layer lkey (philox mode):
+        arrays (agent, d, j, partner), d = 0 for the agent as p1, 1 as p2."""
+        li = self.layer_keys.index(lkey)
+        return ph.dyn_lists(self.k0, self.k1, self.t, li, agents, self.dyn_tables[lkey], self.n)
+
+    def exposures(self, li, rel_trans):
+        """The day's edge directions of layer li whose source has rel_trans != 0, as
+        the transmission draw keys them: arrays (source, target, direction, edge
+        identity, edge beta). Stored layers: every edge in both directions (the
+        identity is the edge index); dynamic layers in philox mode: the entries of
+        the sources' lists (identity ph.dyn_edge_id)."""
+        lkey = self.layer_keys[li]
+        if lkey in self.dyn_tables:
+            S = rel_trans.nonzero()[0]
+            a, d, j, g = self.dynamic_lists(lkey, S)
+            return (a, g, d, ph.dyn_edge_id(a, j, self.t, li), np.ones(len(a), dtype=F32))
+        layer = self.contacts[lkey]
+        e = np.arange(len(layer['p1']), dtype=np.int64)
+        src = np.concatenate([layer['p1'], layer['p2']]).astype(np.int64)
+        tgt = np.concatenate([layer['p2'], layer['p1']]).astype(np.int64)
+        d = np.repeat(np.array([0, 1], dtype=np.int64), len(e))
+        keep = rel_trans[src] != 0
+        return (src[keep], tgt[keep], d[keep], np.concatenate([e, e])[keep],
+                np.concatenate([layer['beta'], layer['beta']]).astype(F32)[keep])
+
+    def dynamic_infections(self, li, variant, beta, rel_trans, rel_sus):
+        """compute_infections (utils.py:93-128) over dynamic layer li in philox
+        mode: every list entry of a source is the edge source -> partner in its
+        direction; p = beta * 1 * rel_trans[s] * rel_sus[g] in float32, one draw
+        per edge with p != 0 keyed by its identity, and the transmissions ordered by
+        (direction, identity) as the reference orders direction then edge."""
+        s, g, d, eid, eb = self.exposures(li, rel_trans)
+        p = (F32(beta) * eb) * rel_trans[s] * rel_sus[g]
+        nz = p.nonzero()[0]
+        s, g, d, eid, p = s[nz], g[nz], d[nz], eid[nz], p[nz]
+        u0, u1 = ph.edge_uniforms(self.k0, self.k1, self.t, li, variant, eid)
+        u = np.where(d == 0, u0, u1)
+        hit = (u < p.astype(np.float64)).nonzero()[0]
+        order = np.lexsort((eid[hit], d[hit]))
+        return s[hit][order].astype(np.int32), g[hit][order].astype(np.int32)
 
     def step(self):
         p = self.pars
@@ -263,14 +312,17 @@ class OracleSim:
                     F32(p['beta_layer'][lkey]), viral_load, people.symptomatic, people.isolated,
                     people.quarantined, F32(p['asymp_factor']), F32(p['iso_factor'][lkey]),
                     F32(p['quar_factor'][lkey]), people.sus_imm[variant, :])
-                if self.rng == 'philox':
-                    u0, u1 = ph.edge_uniforms(self.k0, self.k1, t, li, variant, np.arange(len(layer['p1'])))
-                    uniforms = np.stack([u0, u1])
+                if lkey in self.dyn_tables:
+                    src, tgt = self.dynamic_infections(li, variant, beta, rel_trans, rel_sus)
                 else:
-                    rs = self.rs_numba
-                    uniforms = lambda d, edge_inds: rs.random_sample(len(edge_inds))
-                src, tgt = compute_infections(beta, layer['p1'], layer['p2'], layer['beta'],
-                                              rel_trans, rel_sus, uniforms)
+                    if self.rng == 'philox':  # keyed draws for the surviving edges only
+                        k0, k1 = self.k0, self.k1
+                        uniforms = lambda d, edge_inds: ph.edge_uniforms(k0, k1, t, li, variant, edge_inds)[d]  # noqa: E731
+                    else:
+                        rs = self.rs_numba
+                        uniforms = lambda d, edge_inds: rs.random_sample(len(edge_inds))  # noqa: E731
+                    src, tgt = compute_infections(beta, layer['p1'], layer['p2'], layer['beta'],
+                                                  rel_trans, rel_sus, uniforms)
                 people.infect(inds=tgt, hosp_max=hosp_max, icu_max=icu_max, source=src, layer=lkey,
                               variant=variant, draws=self._draws(CALL_TRANSMISSION))
 

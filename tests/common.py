@@ -93,3 +93,41 @@ def assert_state_equal(get, ref, keys=ALL_KEYS, float_rtol=0.0, label=''):
                 bad = np.nonzero(~((a == b) | (np.isnan(a.astype(float)) & np.isnan(b.astype(float)))))
                 raise AssertionError(f'{label} {k}: {len(bad[0])} mismatches, first at {bad[0][:5]}: '
                                      f'{a[bad][:5]} vs {b[bad][:5]}')
+
+
+RES_KEYS = ['new_infections', 'new_reinfections', 'new_infectious', 'new_symptomatic', 'new_severe', 'new_critical',
+            'new_recoveries', 'new_deaths', 'new_known_deaths', 'n_susceptible', 'n_exposed', 'n_infectious',
+            'n_symptomatic', 'n_severe', 'n_critical', 'n_recovered', 'n_dead']
+
+
+def _host(x):
+    import torch
+    return x.cpu().numpy() if torch.is_tensor(x) else x
+
+
+def oracle_for(sim):
+    """The oracle (Philox mode) for an initialised GPU Sim: the same population, layers and beta schedule."""
+    import copy
+    from oracle.sim import OracleSim
+    spec = sim.spec
+    contacts = {}
+    for ly in spec.layers:
+        p1 = _host(ly['p1'])
+        beta = ly['beta'] if ly.get('beta') is not None else np.ones(len(p1), dtype=np.float32)
+        contacts[ly['key']] = dict(p1=p1, p2=_host(ly['p2']), beta=_host(beta))
+    pars = copy.deepcopy(sim.pars)
+    pars['interventions'] = []
+    return OracleSim(pars, {k: _host(v) for k, v in spec.person.items()}, contacts, rng='philox',
+                     beta_schedule=spec.beta_sched)
+
+
+def compare_runs(sim, orc, keys=RES_KEYS):
+    """Every result series and the final agent state of a GPU run equal to the oracle's."""
+    raw = sim.raw_results()
+    for k in keys:
+        np.testing.assert_array_equal(raw[k], orc.results[k], err_msg=k)
+    np.testing.assert_allclose(raw['pop_nabs'], orc.results['pop_nabs'], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(raw['pop_protection'], orc.results['pop_protection'], rtol=1e-5, atol=1e-12)
+    people_keys = [k for k in ALL_KEYS if k not in ('age', 'sex', 'uid', 'doses')]
+    assert_state_equal(lambda k: sim.people.gpu(k).cpu().numpy(), {k: orc.people[k] for k in people_keys},
+                       keys=people_keys, float_rtol=1e-6, label='final state')

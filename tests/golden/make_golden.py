@@ -2,8 +2,11 @@
 
 Run from the repository root, where the reference source tree is available:
 
-    python tests/golden/make_golden.py            # all fixtures
-    python tests/golden/make_golden.py --only day # one group
+    python tests/golden/make_golden.py --reference PATH            # all fixtures
+    python tests/golden/make_golden.py --reference PATH --only day # one group
+
+(PATH is the reference source tree, the directory holding covasim/; the
+COVASIM_REFERENCE environment variable may stand in for --reference.)
 
 It executes the reference's function bodies through ``refload`` (see its
 docstring), records every random draw they make, and writes small compressed
@@ -28,6 +31,8 @@ Fixtures:
   state_diagram.json   the state-implication matrices of tests/state_diagram.xlsx
   ref_distribution.npz daily new infections / severe / deaths of 200 seeds of the default
                        20k-agent random sim (60 days), reference code with MT19937 streams
+  ref_distribution_hybrid.npz  the same for 200 seeds of a 30k-agent hybrid sim with waning
+                       immunity and the community layer redrawn daily (150 days)
 """
 import argparse
 import copy
@@ -818,16 +823,72 @@ def make_distribution_fixture(ref, n_seeds=200, pop_size=20000, n_days=60):
     print('ref_distribution.npz written', time.time() - t0, 's')
 
 
+# The hybrid distribution fixture: the model the 1M-agent benchmark runs (hybrid
+# layers, waning immunity with NAb kinetics, the community layer redrawn daily),
+# at a size the reference's code finishes in seconds per seed.
+HYBRID_DIST = dict(pop_size=30000, n_days=150, pop_type='hybrid', use_waning=True,
+                   dynam_layer=dict(h=0, s=0, w=0, c=1))
+HYBRID_DIST_KEYS = ['new_infections', 'new_severe', 'new_deaths', 'new_critical', 'new_symptomatic',
+                    'new_reinfections', 'new_recoveries', 'n_exposed', 'n_susceptible']
+
+
+def _hybrid_dist_worker(job):
+    root, seeds = job
+    refload.set_reference_root(root)
+    ref = refload.Reference()
+    rows = []
+    for s in seeds:
+        pars = ref.make_pars(rand_seed=int(s), **copy.deepcopy(HYBRID_DIST))
+        sim = refload.RefSim(ref, pars)
+        while sim.t < sim.npts:
+            sim.step()
+            ref.draws()  # drop the recorded draws as the run goes (this fixture replays none)
+        rows.append((int(s), {k: np.asarray(sim.results[k]) for k in HYBRID_DIST_KEYS},
+                     np.asarray(sim.results['pop_nabs'])))
+        del sim
+    return rows
+
+
+def make_distribution_hybrid_fixture(ref, n_seeds=200, procs=None):
+    """n_seeds runs of the reference's own Sim.step on HYBRID_DIST, seeds 0..n_seeds-1,
+    in a spawn pool (each worker loads the reference's code itself)."""
+    import multiprocessing as mp
+    procs = procs or max(1, min(os.cpu_count() or 1, 16))
+    t0 = time.time()
+    jobs = [(refload.REF_ROOT, list(range(k, n_seeds, procs))) for k in range(procs)]
+    with mp.get_context('spawn').Pool(procs) as pool:
+        parts = pool.map(_hybrid_dist_worker, jobs)
+    npts = HYBRID_DIST['n_days'] + 1
+    out = {k: np.zeros((n_seeds, npts), np.int32) for k in HYBRID_DIST_KEYS}
+    out['pop_nabs'] = np.zeros((n_seeds, npts), np.float64)
+    for rows in parts:
+        for s, r, nabs in rows:
+            for k in HYBRID_DIST_KEYS:
+                out[k][s] = r[k]
+            out['pop_nabs'][s] = nabs
+    out['meta'] = np.array([n_seeds, HYBRID_DIST['pop_size'], HYBRID_DIST['n_days']])
+    out['pars'] = np.array(json.dumps(HYBRID_DIST))
+    np.savez_compressed(os.path.join(HERE, 'ref_distribution_hybrid.npz'), **out)
+    print('ref_distribution_hybrid.npz written', round(time.time() - t0, 1), 's; mean cum infections',
+          out['new_infections'].sum(1).mean())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--only', default=None)
     ap.add_argument('--seeds', type=int, default=200)
+    ap.add_argument('--reference', default=os.environ.get('COVASIM_REFERENCE'),
+                    help='the reference source tree (the directory holding covasim/)')
     args = ap.parse_args()
+    if not args.reference:
+        ap.error('pass --reference PATH (or set COVASIM_REFERENCE)')
+    refload.set_reference_root(args.reference)
     ref = refload.Reference()
     groups = dict(pars=make_pars_fixture, kernels=make_kernels_fixture, day=make_day_fixtures,
                   sims=make_sims_fixture, testing=make_testing_fixture, reporting=make_reporting_fixture,
                   analysis=make_analysis_fixture, states=make_state_diagram_fixture,
-                  distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds))
+                  distribution=lambda r: make_distribution_fixture(r, n_seeds=args.seeds),
+                  distribution_hybrid=lambda r: make_distribution_hybrid_fixture(r, n_seeds=args.seeds))
     for name, fn in groups.items():
         if args.only is None or args.only == name:
             fn(ref)

@@ -25,8 +25,21 @@ import types
 
 import numpy as np
 
-REF_ROOT = os.environ.get('COVASIM_REFERENCE', '/root/reference')
-REF_PKG = os.path.join(REF_ROOT, 'covasim')
+# The reference source tree: set by ``set_reference_root`` (make_golden.py's
+# ``--reference`` argument) or the COVASIM_REFERENCE environment variable.
+REF_ROOT = os.environ.get('COVASIM_REFERENCE') or None
+
+
+def set_reference_root(path):
+    global REF_ROOT
+    REF_ROOT = path
+
+
+def _ref_pkg():
+    if not REF_ROOT:
+        raise RuntimeError('the reference source tree is not set: pass --reference PATH to make_golden.py '
+                           'or set COVASIM_REFERENCE')
+    return os.path.join(REF_ROOT, 'covasim')
 
 
 # ----------------------------------------------------------------------------- stand-ins
@@ -143,7 +156,7 @@ class _NpProxy(types.ModuleType):
 
 # ----------------------------------------------------------------------------- loading
 def _read_tree(fname):
-    path = os.path.join(REF_PKG, fname)
+    path = os.path.join(_ref_pkg(), fname)
     with open(path) as f:
         return path, ast.parse(f.read())
 

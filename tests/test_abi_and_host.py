@@ -50,6 +50,37 @@ def test_entry_points_reject_bad_arguments_without_a_gpu():
     assert lib.covgpu_import_day(C.pointer(st), 0, None) == L.BADARG
     assert lib.covgpu_rescale_check(None, 0, None) == L.BADARG
     assert lib.covgpu_rescale_check(C.pointer(st), 0, None) == L.BADARG
+    assert lib.covgpu_layer_lists(None, 0, 0, 0, 10, None, None, None, None) == L.BADARG
+    assert lib.covgpu_check(None, 0, L.CHECK_DEATH, 0, 1, None, 0, 10, None, 0, None, None) == L.BADARG
+    assert lib.covgpu_check_immunity(C.pointer(st), 0, 0, 1, None) == L.BADARG
+    assert lib.covgpu_update_nab(None, 0, 0, None, 5, None) == L.BADARG
+    assert lib.covgpu_update_peak_nab(None, 0, 0, None, 5, None, L.DurPar(2, 0, 0.0, 2.0), 1.5, 1.0, 2,
+                                      None) == L.BADARG
+
+
+def test_day_path_is_registered_as_torch_custom_ops():
+    """Every day-path entry point the state calls is a torch.ops.covgpu operator
+    (registration needs no GPU)."""
+    import torch
+    import covasim_gb300  # noqa: F401
+    for name in ('compute_viral_load', 'compute_trans_sus', 'compute_infections', 'agent_step', 'edge_pass',
+                 'infect_claims', 'infect_list', 'import_day', 'test_trace', 'lik_targets', 'rescale_check',
+                 'run_days', 'layer_lists', 'check', 'check_immunity', 'update_nab', 'update_peak_nab'):
+        assert hasattr(torch.ops.covgpu, name), name
+
+
+def test_dynamic_layer_count_table_matches_the_oracle():
+    """The list-length table of a redrawn layer (Binomial(E, 1/n) thresholds) is
+    the same in the library's host code and in the oracle, and is a distribution."""
+    from covasim_gb300.state import dynamic_count_table
+    from oracle.philox import dyn_count_table
+    from scipy.stats import binom
+    for E, n in [(10_000_000, 1_000_000), (300, 30), (5, 1), (123_457, 5001), (15 * 20_000, 20_000)]:
+        a, b = dynamic_count_table(E, n), dyn_count_table(E, n)
+        np.testing.assert_array_equal(a, b)
+        assert a[-1] == 2 ** 64 - 1 and np.all(np.diff(a.astype(object)) >= 0)
+        k = np.arange(len(a) - 1)
+        np.testing.assert_allclose(a[:-1].astype(np.float64) / 2.0 ** 64, binom.cdf(k, E, 1 / n), rtol=1e-9, atol=1e-15)
 
 
 def _same(got, want, path):

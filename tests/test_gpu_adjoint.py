@@ -79,7 +79,6 @@ def torch_reference(sim, run, theta):
             beta32 = np.float32(o.pars['beta'] * p['rel_beta'] * p['variant_pars'][p['variant_map'][v]]['rel_beta'])
             inf_v = pp.infectious & (pp.infectious_variant == v)
             for li, lk in enumerate(o.layer_keys):
-                ly = o.contacts[lk]
                 qf, isf, af = (np.float32(p['quar_factor'][lk]), np.float32(p['iso_factor'][lk]),
                                np.float32(p['asymp_factor']))
                 rt32, rs32 = compute_trans_sus(pp.rel_trans, pp.rel_sus, inf_v, pp.susceptible,
@@ -89,12 +88,14 @@ def torch_reference(sim, run, theta):
                     * np.where(pp.symptomatic, 1.0, af) * np.where(pp.isolated, isf, 1.0) * vl.astype(np.float64)
                 rse = pp.rel_sus.astype(np.float64) * np.where(pp.quarantined, qf, 1.0) \
                     * (1.0 - pp.sus_imm[v].astype(np.float64))
-                u = ph.edge_uniforms(o.k0, o.k1, t, li, v, np.arange(len(ly['p1'])))
-                for d, (s, g) in enumerate([(ly['p1'], ly['p2']), (ly['p2'], ly['p1'])]):
-                    p32 = beta32 * ly['beta'] * rt32[s] * rs32[g]
-                    m = (p32 > 0) & inf_v[s] & pp.susceptible[g]
-                    recs.append(dict(l=li, v=v, g=g[m], infected=u[d][m] < p32[m],
-                                     c=ly['beta'][m].astype(np.float64) * rte[s[m]] * rse[g[m]]))
+                # every exposed direction as the GPU keys it (a dynamic layer: the sources' lists)
+                s, g, d, eid, eb = o.exposures(li, rt32)
+                u0, u1 = ph.edge_uniforms(o.k0, o.k1, t, li, v, eid)
+                u = np.where(d == 0, u0, u1)
+                p32 = beta32 * eb * rt32[s] * rs32[g]
+                m = (p32 > 0) & inf_v[s] & pp.susceptible[g]
+                recs.append(dict(l=li, v=v, g=g[m], infected=u[m] < p32[m],
+                                 c=eb[m].astype(np.float64) * rte[s[m]] * rse[g[m]]))
         days.append(recs)
 
     orc.exposure_hook = hook

@@ -8,43 +8,10 @@ import pytest
 import torch
 
 import covasim_gb300 as cv
-from common import load_npz, assert_state_equal, ALL_KEYS
+from common import load_npz, assert_state_equal, ALL_KEYS, RES_KEYS, oracle_for, compare_runs
 from oracle.sim import OracleSim
 
 pytestmark = pytest.mark.gpu
-
-RES_KEYS = ['new_infections', 'new_reinfections', 'new_infectious', 'new_symptomatic', 'new_severe', 'new_critical',
-            'new_recoveries', 'new_deaths', 'new_known_deaths', 'n_susceptible', 'n_exposed', 'n_infectious',
-            'n_symptomatic', 'n_severe', 'n_critical', 'n_recovered', 'n_dead']
-
-
-def _host(x):
-    return x.cpu().numpy() if torch.is_tensor(x) else x
-
-
-def oracle_for(sim):
-    spec = sim.spec
-    contacts = {}
-    for ly in spec.layers:
-        p1 = _host(ly['p1'])
-        beta = ly['beta'] if ly.get('beta') is not None else np.ones(len(p1), dtype=np.float32)
-        contacts[ly['key']] = dict(p1=p1, p2=_host(ly['p2']), beta=_host(beta))
-    pars = copy.deepcopy(sim.pars)
-    pars['interventions'] = []
-    return OracleSim(pars, {k: _host(v) for k, v in spec.person.items()}, contacts, rng='philox',
-                     beta_schedule=spec.beta_sched)
-
-
-def compare_runs(sim, orc, keys=RES_KEYS):
-    raw = sim.raw_results()
-    for k in keys:
-        np.testing.assert_array_equal(raw[k], orc.results[k], err_msg=k)
-    np.testing.assert_allclose(raw['pop_nabs'], orc.results['pop_nabs'], rtol=1e-5, atol=1e-12)
-    np.testing.assert_allclose(raw['pop_protection'], orc.results['pop_protection'], rtol=1e-5, atol=1e-12)
-    people_keys = [k for k in ALL_KEYS if k not in ('age', 'sex', 'uid', 'doses')]
-    assert_state_equal(lambda k: sim.people.gpu(k).cpu().numpy(), {k: orc.people[k] for k in people_keys},
-                       keys=people_keys, float_rtol=1e-6, label='final state')
-
 
 @pytest.mark.parametrize('pop_type,n,days,dyn,seed', [('hybrid', 3000, 45, False, 1), ('random', 4000, 50, False, 2),
                                                      ('hybrid', 2500, 40, True, 3)])
@@ -312,42 +279,35 @@ def test_waning_raises_reinfections_and_nabs():
     assert s1.results['pop_protection'].values.max() > 0
 
 
-def test_distribution_matches_reference_200_seeds():
-    """200 seeds of the default 20k random sim against 200 seeds of the reference's
-    own code: two-sample KS p > 0.01 and means within 2 standard errors."""
-    from scipy.stats import ks_2samp
-    ref = load_npz('ref_distribution.npz')
-    n_seeds, pop_size, n_days = (int(x) for x in ref['meta'])
-    base = cv.Sim(pop_size=pop_size, n_days=n_days, pop_type='random', rand_seed=0)
-    batch = cv.BatchSim(base, n_runs=n_seeds).run()
-    got = {k: batch.series(k) for k in ('new_infections', 'new_severe', 'new_deaths')}
-    stats = {}
-    for k in ('new_infections', 'new_severe', 'new_deaths'):
-        stats[f'cum_{k}'] = (got[k].sum(1), ref[k].sum(1))
-        for day in (20, 40, 60):
-            stats[f'{k}_d{day}'] = (got[k][:, day], ref[k][:, day])
-    stats['peak_day'] = (got['new_infections'].argmax(1), ref['new_infections'].argmax(1))
-    failures = []
-    for name, (a, b) in stats.items():
-        p = ks_2samp(a, b).pvalue
-        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
-        diff = abs(a.mean() - b.mean())
-        if p <= 0.01 or (se > 0 and diff > 2 * se):
-            failures.append((name, p, a.mean(), b.mean(), se))
-    # 19 statistics at the 1% / 2-SE levels: allow one marginal miss from chance alone
-    assert len(failures) <= 1, failures
-
-
-def test_dynamic_layer_endpoints_match_oracle():
-    """The day's dynamic-layer edges (paired Philox blocks, unbiased bounded draws)."""
+def test_dynamic_layer_lists_match_oracle():
+    """A dynamic layer's day as per-agent contact lists (base.py:1849-1876 redraws
+    every edge with uniform endpoints): each agent's lists as p1 and as p2 equal
+    the oracle's draws, their lengths follow Binomial(E, 1/n) and the partners are
+    uniform over the agents."""
+    from scipy.stats import binom, chisquare
     from oracle import philox as ph
-    sim = cv.Sim(pop_type='hybrid', pop_size=5001, n_days=20, rand_seed=12, dynam_layer=dict(h=0, s=0, w=0, c=1))
+    n = 5001
+    sim = cv.Sim(pop_type='hybrid', pop_size=n, n_days=20, rand_seed=12, dynam_layer=dict(h=0, s=0, w=0, c=1))
     sim.initialize()
     keys = [ly['key'] for ly in sim.spec.layers]
     li = keys.index('c')
     n_edges = len(sim.spec.layers[li]['p1'])
     k0, k1 = ph.seed_key(sim['rand_seed'])
+    table = ph.dyn_count_table(n_edges, n)
     for t in (0, 3, 17):
-        p1, p2 = sim.state.materialize_layer(0, li, t)
-        w1, w2 = ph.dynamic_edges(k0, k1, t, li, n_edges, 5001)
-        assert np.array_equal(p1.cpu().numpy(), w1) and np.array_equal(p2.cpu().numpy(), w2), t
+        counts, offsets, partners = sim.state.layer_lists(0, li, t)
+        a, d, j, g = ph.dyn_lists(k0, k1, t, li, np.arange(n), table, n)
+        want = np.zeros((n, 2), dtype=np.int64)
+        np.add.at(want, (a, d), 1)
+        np.testing.assert_array_equal(counts.cpu().numpy(), want)
+        np.testing.assert_array_equal(partners.cpu().numpy(), g)
+        sub_c, sub_o, sub_p = sim.state.layer_lists(0, li, t, agents=(1000, 37))
+        np.testing.assert_array_equal(sub_c.cpu().numpy(), want[1000:1037])
+        np.testing.assert_array_equal(sub_p.cpu().numpy(), g[(a >= 1000) & (a < 1037)])
+    c = counts.cpu().numpy().reshape(-1)
+    lo, hi = 4, 18  # tails merged into the end bins, so every expected count is large
+    obs = np.bincount(np.clip(c, lo, hi) - lo, minlength=hi - lo + 1)
+    cdf = binom.cdf(np.arange(lo, hi), n_edges, 1 / n)
+    pk = np.diff(np.concatenate([[0.0], cdf, [1.0]]))
+    assert chisquare(obs, pk * len(c)).pvalue > 1e-3
+    assert chisquare(np.bincount(g % 50, minlength=50)).pvalue > 1e-3
