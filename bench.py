@@ -40,10 +40,11 @@ sys.path.insert(0, ROOT)
 POP = 1_000_000
 DAYS = 180
 PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
-# DRAM bytes (read + write) of one edge-pass launch on this workload, from an
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of day 90 of the 1M run,
-# resident edge pass with 8192-edge tiles
-MEASURED_TRAFFIC = {('edge_pass', 1_000_000): 82_782_208}
+# From ncu captures of the 1M-agent workload (day 85, near the epidemic's peak;
+# the launch list of a whole ungraphed run gives the kernels' shares): DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum) per launch and the share of
+# cycles the schedulers issued (smsp__issue_active), per kernel.
+MEASURED_NCU = {}
 
 
 def parse():
@@ -189,24 +190,14 @@ def agent_pass_bytes(n, nv):
     return (AGENT_BYTES_BASE + AGENT_BYTES_PER_VARIANT * nv) * n
 
 
-def edge_pass_bytes(spec):
-    return EDGE_BYTES_PER_EDGE * sum(len(ly['p1']) for ly in spec.layers)
-
-
-def edge_pass_floor_bytes(spec, n):
-    """Bytes the GPU edge pass cannot avoid: p1/p2 of every stored edge and the
-    role bitmaps (dynamic-layer edges are drawn in registers; agent state is
-    gathered only for source->target candidates)."""
-    e_static = sum(len(ly['p1']) for ly in spec.layers if not ly['dynamic'])
-    return 8 * e_static + n / 4
-
-
 # ----------------------------------------------------------------------------- GPU arm
 def kernel_profile(sim, npts):
-    """One ungraphed run with CUDA events around each kernel (on the launching stream)."""
+    """One ungraphed run with CUDA events around each kernel (on the launching
+    stream): the agent pass, the stored layers' edge pass, the dynamic layers'
+    per-source pass and the infect pass, each launched on its own."""
     import torch
     st = sim.state
-    times = {'agent_step': [], 'edge_pass': [], 'infect_claims': []}
+    times = {'agent_step': [], 'edge_stored': [], 'edge_dynamic': [], 'infect_claims': []}
     stream = torch.cuda.current_stream()
 
     def timed(name, fn):
@@ -219,11 +210,55 @@ def kernel_profile(sim, npts):
 
     for t in range(npts):
         timed('agent_step', lambda: st.agent_step(t, do_prev=t > 0, do_day=True))
-        timed('edge_pass', lambda: st.edge_pass(t))
+        timed('edge_stored', lambda: st.edge_pass(t, parts=1))
+        timed('edge_dynamic', lambda: st.edge_pass(t, parts=2))
         timed('infect_claims', lambda: st.infect_claims(t))
     timed('agent_step', lambda: st.agent_step(npts, do_prev=True, do_day=False))
     torch.cuda.synchronize()
     return {k: [a.elapsed_time(b) for a, b in v] for k, v in times.items()}
+
+
+KERNEL_NAMES = {'agent_step': 'k_agent_step', 'edge_stored': 'k_edge_pass', 'edge_dynamic': 'k_dyn_pass',
+                'infect_claims': 'k_infect_claims'}
+
+
+def roofline_block(dom, totals, kt, sim, n, st, res):
+    """The roofline of the dominant kernel: algorithmic bytes per launch (the
+    reference algorithm's per-unit bytes x the units of one launch) over its
+    CUDA-event average duration, against the measured copy bandwidth; beside it
+    the DRAM traffic ncu measured for that kernel and what bounds it."""
+    nv = 1
+    if dom == 'agent_step':
+        bytes_launch = agent_pass_bytes(n, nv)
+        unit_desc = f'{AGENT_BYTES_BASE + AGENT_BYTES_PER_VARIANT * nv} B/agent/day'
+    elif dom == 'edge_stored':
+        bytes_launch = EDGE_BYTES_PER_EDGE * sum(len(ly['p1']) for ly in sim.spec.layers if not ly['dynamic'])
+        unit_desc = f'{EDGE_BYTES_PER_EDGE} B/stored undirected edge/day'
+    elif dom == 'edge_dynamic':
+        bytes_launch = EDGE_BYTES_PER_EDGE * sum(len(ly['p1']) for ly in sim.spec.layers if ly['dynamic'])
+        unit_desc = (f'{EDGE_BYTES_PER_EDGE} B/redrawn undirected edge/day (the reference streams the whole '
+                     'redrawn layer; this pass draws the sources\' lists only)')
+    else:
+        bytes_launch = 16.0 * max(float(np.mean(res['new_infections'])), 1.0)
+        unit_desc = '16 B/new infection'
+    avg_ms = totals[dom] / len(kt[dom])
+    achieved = bytes_launch / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    m = MEASURED_NCU.get((dom, n), {})
+    traffic = m.get('dram_bytes')
+    out = {'bound': m.get('bound', 'hbm'), 'kernel': KERNEL_NAMES[dom], 'achieved': round(achieved, 1), 'peak': peak,
+           'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4), 'traffic': traffic,
+           'algorithmic_bytes_per_launch': round(bytes_launch), 'bytes_per_unit': unit_desc,
+           'avg_launch_ms': round(avg_ms, 5)}
+    if traffic:
+        out['dram_achieved'] = round(traffic / (avg_ms / 1e3) / 1e9, 1)
+        out['dram_frac'] = round(traffic / (avg_ms / 1e3) / 1e9 / peak, 4)
+        out['traffic_note'] = m.get('note')
+    if 'issue_active' in m:
+        out['issue_active'] = m['issue_active']
+    out['kernel_ms_total'] = {KERNEL_NAMES[k]: round(v, 3) for k, v in totals.items()}
+    out['kernel_share'] = {KERNEL_NAMES[k]: round(v / sum(totals.values()), 4) for k, v in totals.items()}
+    return out
 
 
 def peaks():
@@ -294,26 +329,8 @@ def gpu_arm(args, world, rank):
     res = st.results(0)
     totals = {k: float(np.sum(v)) for k, v in kt.items()}
     dom = max(totals, key=totals.get)
-    nv = 1
-    if dom == 'agent_step':
-        bytes_launch, unit_desc = agent_pass_bytes(n, nv), f'{AGENT_BYTES_BASE + AGENT_BYTES_PER_VARIANT * nv} B/agent/day'
-    elif dom == 'edge_pass':
-        bytes_launch, unit_desc = edge_pass_bytes(sim.spec), f'{EDGE_BYTES_PER_EDGE} B/undirected edge/day'
-    else:
-        bytes_launch = 16.0 * max(float(np.mean(res['new_infections'])), 1.0)
-        unit_desc = '16 B/new infection'
-    avg_ms = totals[dom] / len(kt[dom])
-    achieved = bytes_launch / (avg_ms / 1e3) / 1e9
-    peak, peak_kind = peaks()
-    traffic = MEASURED_TRAFFIC.get((dom, n)) if dom == 'edge_pass' else None
-    roofline = {'bound': 'hbm', 'kernel': f'k_{dom}', 'achieved': round(achieved, 1), 'peak': peak,
-                'peak_source': peak_kind, 'unit': 'GB/s', 'frac': round(achieved / peak, 4), 'traffic': traffic,
-                'algorithmic_bytes_per_launch': round(bytes_launch), 'bytes_per_unit': unit_desc,
-                'floor_bytes_per_launch': round(edge_pass_floor_bytes(sim.spec, st.n)) if dom == 'edge_pass' else None,
-                'avg_launch_ms': round(avg_ms, 5),
-                'kernel_ms_total': {k: round(v, 3) for k, v in totals.items()},
-                'kernel_share': {k: round(v / sum(totals.values()), 4) for k, v in totals.items()}}
-    launches_per_step = 1 + 3 * npts + 1
+    roofline = roofline_block(dom, totals, kt, sim, n, st, res)
+    launches_per_step = 1 + 4 * npts + 1  # seed infect, per day agent/stored/dynamic/infect, closing pass
 
     # end to end through the public API, from pinned host memory
     e2e = None

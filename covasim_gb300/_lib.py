@@ -101,7 +101,7 @@ class Layer(C.Structure):
                 ('tile_begin', C.c_int64), ('sim', C.c_int32), ('layer', C.c_int32), ('dynamic', C.c_int32),
                 ('beta_const', C.c_float), ('iso_factor', C.c_float), ('quar_factor', C.c_float),
                 ('dyn_k', C.c_int32), ('rp1', C.c_void_p), ('rp2', C.c_void_p), ('perm2', C.c_void_p),
-                ('dyn_cdf', C.c_void_p)]
+                ('dyn_cdf', C.c_void_p), ('dyn_rse_max', C.c_float), ('_pad2', C.c_int32)]
 
 
 class AgentBlock(C.Structure):
@@ -125,7 +125,7 @@ class State(C.Structure):
         ('peak_nab', C.c_void_p), ('nab', C.c_void_p), ('t_nab_event', C.c_void_p),
         ('vaccine_source', C.c_void_p),
         ('sus_imm', C.c_void_p), ('symp_imm', C.c_void_p), ('sev_imm', C.c_void_p),
-        ('imm_stride_variants', C.c_int32), ('_pad0', C.c_int32),
+        ('imm_stride_variants', C.c_int32), ('edge_parts', C.c_int32),
         ('dates', C.c_void_p), ('durs', C.c_void_p),
         ('viral_load', C.c_void_p), ('roles', C.c_void_p), ('claim', C.c_void_p),
         ('src_rec', C.c_void_p),

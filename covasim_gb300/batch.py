@@ -82,7 +82,7 @@ class BatchSim:
                 if t in np.atleast_1d(v.days):
                     sus = np.nonzero(self.state.get('susceptible', k).cpu().numpy())[0]
                     rng = np.random.default_rng([int(s['rand_seed']), 0x1A1A, t, v.index])
-                    n_imp = min(variant_import_count(v, self.state.rescale_vecs[k][t], rng), len(sus))
+                    n_imp = variant_import_count(v, self.state.rescale_vecs[k][t], rng)  # more than len(sus): ValueError
                     inds = rng.choice(sus, n_imp, replace=False)
                     self.state.set_hospicu([[0, 0]] * len(self.sims))  # variant.apply: no bed limits
                     self.state.infect_list(t, inds, sim=k, variant=v.index, layer_tag=L.LOG_IMPORT,

@@ -358,6 +358,7 @@ struct SegCtx {
   const float* edge_beta;    // per-edge layer weights, or null for beta_const
   const float* beta_t;       // beta_tab row of day t ([n_variants])
   float beta_const, beta_layer, quar_factor, iso_factor, asymp_factor;
+  float rse_max;             // dynamic layers: the thinning bound (covgpu_layer.dyn_rse_max)
   uint32_t key0, key1;
   int nv, layer, seg, sim;
   int64_t n_edges;
@@ -426,10 +427,13 @@ __device__ __forceinline__ void lik_terms(const covgpu_state& st, const SegCtx& 
 // (utils.py:88-89 then 117-123); returns true on a transmission. Every gather
 // is issued before the first use so that they overlap. LIK: also the
 // likelihood terms of the direction, from the same gathered values. INJ: a
-// stored layer's edge, which takes the injected uniforms of test mode.
-template <bool LIK, bool INJ = true>
+// stored layer's edge, which takes the injected uniforms of test mode. THIN: a
+// dynamic layer's list entry, which transmits only if it was a potential
+// transmission (ph, covgpu_device.cuh "Thinning") and then with probability
+// p * 2^m against the edge's uniform.
+template <bool LIK, bool INJ = true, bool THIN = false>
 __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c, int t, int64_t e, int dir,
-                                         int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc) {
+                                         int32_t s, int32_t g, uint32_t& v_out, LikAcc& acc, bool ph = true) {
   const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
   const uint32_t fs = __float_as_uint(sr.w);
   const float lb = c.edge_beta ? __ldg(c.edge_beta + e) : c.beta_const;
@@ -464,6 +468,15 @@ __device__ __forceinline__ bool edge_try(const covgpu_state& st, const SegCtx& c
   bool hit;
   if (INJ && st.edge_uniforms) {  // injected draws (test mode)
     hit = st.edge_uniforms[c.seg][((int64_t)v * 2 + dir) * c.n_edges + e] < (double)p;
+  } else if (THIN) {
+    hit = false;
+    if (ph) {
+      const int m = thin_shift(__fmul_rn(__fmul_rn(__fmul_rn(beta, lb), rte), c.rse_max));
+      const float ps = __fmul_rn(p, __int_as_float((127 + m) << 23));  // p * 2^m, exact
+      const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
+                                        TAG_EDGE | (v << 8) | (uint32_t)c.layer), c.key0, c.key1);
+      hit = dir ? bern52(w.z, w.w, ps) : bern52(w.x, w.y, ps);
+    }
   } else {
     // one Philox block per (edge, day, variant, layer): words x,y draw direction 0, z,w direction 1
     const uint4 w = philox(make_uint4((uint32_t)e, (uint32_t)(e >> 32), (uint32_t)t,
@@ -744,7 +757,9 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
 // block, both lists side by side so that eight target-bitmap loads are in
 // flight, and queues the partners that are targets; the queue drains through
 // edge_try as the stored layers' does. The work follows the day's sources, not
-// the layer's edges: a quiet day costs a read of the source bitmap.
+// the layer's edges: a quiet day costs a read of the source bitmap. Entries are
+// thinned (covgpu_device.cuh "Thinning"): only the potential transmissions, about
+// pmax of them, have their partner drawn and are queued.
 constexpr int DYN_WARPS = 8;  // warps per thread block
 constexpr int DYN_WORDS = 4;  // source-bitmap words per warp (an agent block's eight words: two warps)
 
@@ -760,6 +775,7 @@ __device__ __forceinline__ void dyn_ctx(const covgpu_state& st, const covgpu_sim
   c.quar_factor = L->quar_factor;
   c.iso_factor = L->iso_factor;
   c.asymp_factor = sp.asymp_factor;
+  c.rse_max = L->dyn_rse_max;
   c.nv = sp.n_variants;
   c.key0 = sp.key0;
   c.key1 = sp.key1;
@@ -768,8 +784,27 @@ __device__ __forceinline__ void dyn_ctx(const covgpu_state& st, const covgpu_sim
   c.sim = L->sim;
 }
 
+// the thinning shift of source s (covgpu_device.cuh "Thinning"): pmax = beta *
+// lb * rel_trans'(s) * rse_max, formed as edge_try forms p; -1 when the source
+// cannot transmit in this layer
+__device__ __forceinline__ int dyn_shift(const covgpu_state& st, const SegCtx& c, int32_t s) {
+  const float4 sr = __ldg(reinterpret_cast<const float4*>(st.src_rec) + s);
+  const uint32_t fs = __float_as_uint(sr.w);
+  const uint32_t v = (__float_as_uint(sr.z) >> 8) & 0xFFu;
+  if (v >= (uint32_t)c.nv) return -1;
+  float rte = sr.x;
+  if (fs & B_QUAR) rte = __fmul_rn(rte, c.quar_factor);
+  if (!(fs & B_SYMP)) rte = __fmul_rn(rte, c.asymp_factor);
+  if (fs & B_ISO) rte = __fmul_rn(rte, c.iso_factor);
+  rte = __fmul_rn(rte, c.beta_layer);
+  rte = __fmul_rn(rte, sr.y);
+  const float q = __fmul_rn(__fmul_rn(__ldg(c.beta_t + v), c.beta_const), rte);
+  return q == 0.0f ? -1 : thin_shift(__fmul_rn(q, c.rse_max));
+}
+
 // phase B of the redrawn layers: one candidate per lane (entry j of list d of
-// source s, m = j << 1 | d), then the warp-aggregated event append
+// source s, potential transmission ph; m = j << 2 | ph << 1 | d), then the
+// warp-aggregated event append
 template <bool LIK>
 __device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& c, int t, int64_t agent_off,
                                           EdgeQueue& q, int qn, LikAcc& acc) {
@@ -783,25 +818,12 @@ __device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& 
     uint64_t e = 0;
     if (i < qn) {
       s = q.s[i]; g = q.g[i]; m = q.m[i];
-      e = dyn_edge_id((uint32_t)(s - agent_off), m >> 1, (uint32_t)t, (uint32_t)c.layer);
-      hit = edge_try<LIK, false>(st, c, t, (int64_t)e, (int)(m & 1u), s, g, v, acc);
+      e = dyn_edge_id((uint32_t)(s - agent_off), m >> 2, (uint32_t)t, (uint32_t)c.layer);
+      hit = edge_try<LIK, false, true>(st, c, t, (int64_t)e, (int)(m & 1u), s, g, v, acc, (m >> 1) & 1u);
     }
     emit(st, hit, hit ? event_key(t, v, c.layer, (int)(m & 1u), (int64_t)e) : 0ull, g, s);
   }
   __syncwarp();
-}
-
-// four partners (entries 4 qd .. 4 qd + 3) of list d of local agent a, as
-// global indices, and whether each is a target; entries past k are not targets
-__device__ __forceinline__ void dyn_four(const covgpu_state& st, uint32_t a, int d, int qd, int k, uint32_t t,
-                                         uint32_t layer, uint32_t key0, uint32_t key1, uint32_t n, uint32_t thr,
-                                         int32_t off, int32_t g[4], uint32_t tb[4]) {
-  const uint4 w = dyn_partner_block(a, d, 4 * qd, t, layer, key0, key1);
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-    g[r] = off + (int32_t)dyn_partner(word_of(w, r), n, thr, a, d, 4 * qd + r, t, layer, key0, key1);
-#pragma unroll
-  for (int r = 0; r < 4; ++r) tb[r] = 4 * qd + r < k ? tgt_bit(st, g[r]) : 0u;
 }
 
 template <bool LIK>
@@ -823,6 +845,7 @@ __global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st,
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const uint32_t n_local = (uint32_t)sp.n_agents, thr = bounded_thr(n_local);
   const int32_t off = (int32_t)sp.agent_off;
+  const uint32_t day = (uint32_t)t;
   EdgeQueue& q = s_q[warp];
   LikAcc acc;
   for (int l = 0; l < sp.n_layers; ++l) {
@@ -837,27 +860,47 @@ __global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st,
       const int wl = warp_bits_nth(wb, nw, idx, bit);
       const int32_t s = (int32_t)((w0 + wl) * 32 + bit);
       const uint32_t a = (uint32_t)(s - off);
-      int k0 = 0, k1 = 0;
-      if (idx < wb.total) dyn_counts(c.L->dyn_cdf, c.L->dyn_k, a, (uint32_t)t, (uint32_t)l, c.key0, c.key1, k0, k1);
-      const int nq = (max(k0, k1) + 3) >> 2;
-      const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)nq);
-      for (int qd = 0; qd < nq_max; ++qd) {
-        int32_t g0[4], g1[4];
-        uint32_t t0[4] = {0u, 0u, 0u, 0u}, t1[4] = {0u, 0u, 0u, 0u};
-        if (4 * qd < k0) dyn_four(st, a, 0, qd, k0, (uint32_t)t, (uint32_t)l, c.key0, c.key1, n_local, thr, off, g0, t0);
-        if (4 * qd < k1) dyn_four(st, a, 1, qd, k1, (uint32_t)t, (uint32_t)l, c.key0, c.key1, n_local, thr, off, g1, t1);
-        // each list's four entries add at most 4 * 32 candidates: drain before a half could overflow
+      int k[2] = {0, 0}, m = -1;
+      if (idx < wb.total) {
+        m = dyn_shift(st, c, s);
+        if (m >= 0 || LIK) dyn_counts(c.L->dyn_cdf, c.L->dyn_k, a, day, (uint32_t)l, c.key0, c.key1, k[0], k[1]);
+      }
+      for (int d = 0; d < 2; ++d) {
+        const int kd = k[d];
+        const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)((kd + 3) >> 2));
+        for (int qd = 0; qd < nq_max; ++qd) {
+          const int j0 = 4 * qd;
+          // potential transmissions among entries j0 .. j0 + 3 (one Philox block)
+          uint32_t pm = 0u;
+          if (j0 < kd && m >= 0) {
+            const uint4 hw = dyn_hit_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) queue_push(q, qn, t0[r] != 0u, s, g0[r], (uint32_t)(4 * qd + r) << 1);
-        if (qn > EQ_CAP - 4 * 32) {
-          dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
-          qn = 0;
-        }
+            for (int r = 0; r < 4; ++r)
+              if (j0 + r < kd && thin_potential(word_of(hw, r), m)) pm |= 1u << r;
+          }
+          // partners: of the potential entries (all entries for the likelihood)
+          const uint32_t want = LIK ? (j0 < kd ? (0xFu >> max(0, 4 - (kd - j0))) : 0u) : pm;
+          if (!__any_sync(0xffffffffu, want != 0u)) continue;
+          int32_t g[4] = {0, 0, 0, 0};
+          uint32_t tb = 0u;
+          if (want) {
+            const uint4 pw = dyn_partner_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
 #pragma unroll
-        for (int r = 0; r < 4; ++r) queue_push(q, qn, t1[r] != 0u, s, g1[r], ((uint32_t)(4 * qd + r) << 1) | 1u);
-        if (qn > EQ_CAP - 4 * 32) {
-          dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
-          qn = 0;
+            for (int r = 0; r < 4; ++r)
+              if ((want >> r) & 1u) {
+                g[r] = off + (int32_t)dyn_partner(word_of(pw, r), n_local, thr, a, d, j0 + r, day, (uint32_t)l,
+                                                  c.key0, c.key1);
+                tb |= tgt_bit(st, g[r]) << r;
+              }
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            queue_push(q, qn, (tb >> r) & 1u, s, g[r],
+                       ((uint32_t)(j0 + r) << 2) | (((pm >> r) & 1u) << 1) | (uint32_t)d);
+          if (qn > EQ_CAP - 4 * 32) {
+            dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+            qn = 0;
+          }
         }
       }
     }
@@ -964,21 +1007,47 @@ void launch_edge_res(const covgpu_state* st, int t, cudaStream_t s) {
   else k_edge_pass_res<LIK, 4096><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
 }
 
-// the stored layers' tiles, then the redrawn layers' sources
-int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s) {
-  if (st->n_tiles > 0) {
-    if (st->edge_resident) {
-      if (st->lik.factor) launch_edge_res<true>(st, t, s);
-      else launch_edge_res<false>(st, t, s);
-    } else if (st->lik.factor) {
-      launch_edge_tiles<true>(st, t, s);
-    } else {
-      launch_edge_tiles<false>(st, t, s);
-    }
-    const int rc = launch_status();
-    if (rc) return rc;
+int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->n_tiles == 0) return COVGPU_OK;
+  if (st->edge_resident) {
+    if (st->lik.factor) launch_edge_res<true>(st, t, s);
+    else launch_edge_res<false>(st, t, s);
+  } else if (st->lik.factor) {
+    launch_edge_tiles<true>(st, t, s);
+  } else {
+    launch_edge_tiles<false>(st, t, s);
   }
-  return launch_dyn_pass(st, t, s);
+  return launch_status();
+}
+
+// the stored layers' tiles, then the redrawn layers' sources (parts: 0 both, 1 or 2 one of them)
+int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s, int parts = 0) {
+  const int rc = parts == 2 ? COVGPU_OK : launch_stored_pass(st, t, s);
+  return (rc || parts == 1) ? rc : launch_dyn_pass(st, t, s);
+}
+
+// The same two passes side by side: they read the same start-of-day state and
+// only append events and claims with atomics, so the redrawn layers' pass runs
+// on a side stream forked from s and joined back before anything after it
+// (inside a capture the fork and join become edges of the graph).
+cudaStream_t g_side_stream = nullptr;
+cudaEvent_t g_fork_ev = nullptr, g_join_ev = nullptr;
+int launch_edge_pass_forked(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->n_tiles == 0 || st->n_dynamic == 0) return launch_edge_pass(st, t, s);
+  if (!g_side_stream) {
+    if (cudaStreamCreateWithFlags(&g_side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g_fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g_join_ev, cudaEventDisableTiming) != cudaSuccess)
+      return COVGPU_CUDA_ERROR;
+  }
+  if (cudaEventRecord(g_fork_ev, s) != cudaSuccess || cudaStreamWaitEvent(g_side_stream, g_fork_ev, 0) != cudaSuccess)
+    return COVGPU_CUDA_ERROR;
+  int rc = launch_dyn_pass(st, t, g_side_stream);
+  if (rc) return rc;
+  if (cudaEventRecord(g_join_ev, g_side_stream) != cudaSuccess) return COVGPU_CUDA_ERROR;
+  rc = launch_stored_pass(st, t, s);
+  if (rc) return rc;
+  return cudaStreamWaitEvent(s, g_join_ev, 0) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
 }
 
 // per target: expected = 1 - prod(1 - p) and its per-layer sensitivities from
@@ -1592,7 +1661,8 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
                                                                         t == t1 - 1 ? 1 : 0);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
-    launch_edge_pass(st, t, s);
+    const int rc = launch_edge_pass_forked(st, t, s);
+    if (rc) return rc;
     launch_lik_targets(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
@@ -1673,9 +1743,10 @@ int covgpu_edge_pass(const covgpu_state* st, int32_t t, void* stream) {
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
+  if (st->edge_parts < 0 || st->edge_parts > 2) return COVGPU_BADARG;
   rc = configure_edge_pass(st);
   if (rc) return rc;
-  return launch_edge_pass(st, t, S(stream));
+  return launch_edge_pass(st, t, S(stream), st->edge_parts);
 }
 
 int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream) {

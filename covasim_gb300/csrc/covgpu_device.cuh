@@ -90,7 +90,7 @@ __host__ __device__ __forceinline__ uint32_t bounded_thr(uint32_t n) { return (u
 // distinct and their order, which decides the first infector among one layer's
 // transmissions to the same target, is scrambled as the reference's i.i.d. edge
 // order is.
-constexpr uint32_t TAG_DYN = 0x08000000u, TAG_DYN_RETRY = 0x09000000u;
+constexpr uint32_t TAG_DYN = 0x08000000u, TAG_DYN_RETRY = 0x09000000u, TAG_DYN_HIT = 0x0A000000u;
 constexpr int DYN_MAX_LIST = 1 << 10;  // entries of one list (the count table has at most this many)
 constexpr uint64_t MASK40 = (1ull << 40) - 1;
 
@@ -135,6 +135,28 @@ __device__ __forceinline__ uint4 dyn_partner_block(uint32_t a, int d, int j, uin
 }
 __device__ __forceinline__ uint32_t word_of(const uint4& w, int k) {
   return k == 0 ? w.x : (k == 1 ? w.y : (k == 2 ? w.z : w.w));
+}
+
+// Thinning of a source's list entries. Every entry of source s's lists in a
+// layer transmits with p(s, g) = beta * rel_trans'(s) * rel_sus'(g) <= pmax(s) =
+// beta * rel_trans'(s) * rse_max (rse_max bounds rel_sus' over the sim's agents).
+// An entry is first a potential transmission with probability 2^-m, the power
+// of two just above pmax (m = thin_shift(pmax)), decided by the top m bits of
+// one 32-bit word of Philox (a, d * 256 + j / 4, day, TAG_DYN_HIT | layer); only
+// then is its partner drawn, and it transmits when u < p * 2^m (u the edge's
+// Bernoulli uniform, p * 2^m exact in float32). So P(transmission) = p, with one
+// 32-bit word per entry instead of a partner, a gather and a Bernoulli draw.
+__device__ __forceinline__ int thin_shift(float pmax) {
+  if (pmax >= 1.0f) return 0;
+  const int ex = (int)((__float_as_uint(pmax) >> 23) & 0xffu);  // pmax in [2^(ex-127), 2^(ex-126))
+  return ex == 0 ? 32 : min(32, 126 - ex);
+}
+__device__ __forceinline__ bool thin_potential(uint32_t w, int m) {
+  return m == 0 || (w >> (32 - m)) == 0u;
+}
+__device__ __forceinline__ uint4 dyn_hit_block(uint32_t a, int d, int j, uint32_t day, uint32_t layer, uint32_t k0,
+                                               uint32_t k1) {
+  return philox(make_uint4(a, ((uint32_t)d << 8) + ((uint32_t)j >> 2), day, TAG_DYN_HIT | layer), k0, k1);
 }
 
 // The set bits of one agent block's bitmap words, handed to the lanes 32 at a

@@ -2,7 +2,9 @@
 // as standalone GPU drop-ins -- compute_viral_load, compute_trans_sus and
 // compute_infections (ordered output, bit-exact), with the allocation-free
 // variant of compute_infections.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <atomic>
 #include <stdint.h>
 #include <stddef.h>
 #include <math.h>
@@ -251,20 +253,51 @@ constexpr int64_t NOALLOC_TILES = (NOALLOC_MAX_EDGES + INF_TILE - 1) / INF_TILE;
 constexpr int64_t NOALLOC_SCRATCH = 2 * NOALLOC_TILES * (int64_t)(sizeof(int64_t) + sizeof(int32_t));
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH];
 constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of g_noalloc_scratch, per device
+// The device address of g_noalloc_scratch per device, with the context it was
+// looked up in: a device reset or a new primary context (the module loaded
+// again, possibly elsewhere) makes the next call look it up again. Atomic, so
+// that host threads calling at the same time do not race on the cache.
+struct NoallocSlot {
+  std::atomic<void*> ptr{nullptr};
+  std::atomic<void*> ctx{nullptr};
+};
+static NoallocSlot g_noalloc[NOALLOC_MAX_DEVICES];
+
+// The current CUDA context, through the driver's cuCtxGetCurrent resolved by
+// the runtime (no link against the driver library); null when unavailable.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+static CUcontext current_context() {
+  static std::atomic<CtxGetCurrentFn> fn{nullptr};
+  CtxGetCurrentFn f = fn.load(std::memory_order_acquire);
+  if (!f) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      return nullptr;
+    f = reinterpret_cast<CtxGetCurrentFn>(p);
+    fn.store(f, std::memory_order_release);
+  }
+  CUcontext c = nullptr;
+  return f(&c) == CUDA_SUCCESS ? c : nullptr;
+}
 
 // The array's host-side name is not a device address: look the address up once
-// per device, with that device current.
+// per device (and context), with that device current.
 static int noalloc_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return COVGPU_CUDA_ERROR;
   if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return COVGPU_BADARG;
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
+  NoallocSlot& slot = g_noalloc[dev];
+  void* ctx = reinterpret_cast<void*>(current_context());
+  void* p = slot.ptr.load(std::memory_order_acquire);
+  if (!p || !ctx || slot.ctx.load(std::memory_order_acquire) != ctx) {
+    p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return COVGPU_CUDA_ERROR;
-    g_noalloc_ptr[dev] = p;
+    slot.ctx.store(reinterpret_cast<void*>(current_context()), std::memory_order_release);
+    slot.ptr.store(p, std::memory_order_release);
   }
-  *out = g_noalloc_ptr[dev];
+  *out = p;
   return COVGPU_OK;
 }
 

@@ -521,7 +521,7 @@ class Sim:
             if t in np.atleast_1d(v.days):
                 sus = np.nonzero(self.people['susceptible'])[0]
                 rng = np.random.default_rng([int(self['rand_seed']), 0x1A1A, t, v.index])
-                n_imp = min(variant_import_count(v, self.state.rescale_vecs[0][t], rng), len(sus))
+                n_imp = variant_import_count(v, self.state.rescale_vecs[0][t], rng)  # more than len(sus): ValueError, as immunity.py:128
                 inds = rng.choice(sus, n_imp, replace=False)
                 self.state.set_hospicu([[0, 0]])  # variant.apply calls infect() without bed limits
                 self.state.infect_list(t, inds, sim=0, variant=v.index, layer_tag=L.LOG_IMPORT,

@@ -121,6 +121,23 @@ RESCALE_TAG = 0x5C5C
 HOLD_NONE = 0x7FFFFFFF
 
 
+def _max_of(x):
+    """The largest value of a host array or device tensor (0 when empty)."""
+    if torch.is_tensor(x):
+        return float(x.max().item()) if x.numel() else 0.0
+    x = np.asarray(x)
+    return float(x.max()) if x.size else 0.0
+
+
+def rse_bound(rel_sus_max, quar_factor):
+    """The thinning bound of a dynamic layer: a float32 value at least
+    rel_sus * (quarantined ? quar_factor : 1) * (1 - sus_imm) as the edge pass
+    forms it in float32 for any agent (sus_imm in [0, 1]), i.e. the largest
+    rel_sus, or its float32 product with quar_factor when that is larger."""
+    rs = np.float32(rel_sus_max)
+    return float(max(rs, np.float32(rs * np.float32(quar_factor))))
+
+
 def dynamic_count_table(n_edges, n_agents):
     """The length distribution of one agent's contact list in a dynamic layer.
 
@@ -497,6 +514,7 @@ class BatchState:
                     rec.beta_const = 1.0
                     cdf = torch.from_numpy(dynamic_count_table(n_edges, sp.n).view(np.int64)).to(self.device)
                     rec.dyn_cdf, rec.dyn_k = cdf.data_ptr(), len(cdf)
+                    rec.dyn_rse_max = rse_bound(_max_of(sp.person['rel_sus']), rec.quar_factor)
                     keep.append(cdf)
                 elif torch.is_tensor(ly['p1']):
                     # torch inputs (e.g. pinned host memory): uploaded as they are, checked on the
@@ -876,8 +894,15 @@ class BatchState:
     def agent_step(self, t, do_prev=True, do_day=True):
         torch.ops.covgpu.agent_step(self._sa, int(t), bool(do_prev), bool(do_day), self.t['status'])
 
-    def edge_pass(self, t):
-        torch.ops.covgpu.edge_pass(self._sa, int(t), self.t['status'])
+    def edge_pass(self, t, parts=0):
+        """Day t's transmission: parts 0 both passes, 1 the stored layers only, 2 the
+        dynamic layers only (the two are independent; a run launches both)."""
+        if parts:
+            self.cstate.edge_parts = int(parts)
+        try:
+            torch.ops.covgpu.edge_pass(self._sa, int(t), self.t['status'])
+        finally:
+            self.cstate.edge_parts = 0
 
     def infect_claims(self, t):
         torch.ops.covgpu.infect_claims(self._sa, int(t), self.t['status'])
@@ -1124,6 +1149,14 @@ class BatchState:
         elif key in self.t and key not in ('roles', 'claim', 'src_rec', 'events', 'log', 'status'):
             dst = self.t[key][s]
             dst.copy_(torch.as_tensor(np.asarray(values), dtype=dst.dtype))
+            if key == 'rel_sus':  # the dynamic layers' thinning bound follows the largest rel_sus
+                rs = _max_of(dst)
+                for (k, _), seg in self.segment_index.items():
+                    rec = self.segments[seg]
+                    if k == sim and rec.dynamic:
+                        rec.dyn_rse_max = rse_bound(rs, rec.quar_factor)
+                self._tile_segments()
+                self._refresh_state()
         else:
             raise KeyError(f'Key "{key}" cannot be set')
 

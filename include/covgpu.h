@@ -209,6 +209,11 @@ typedef struct covgpu_layer {
   const uint32_t* rp2;
   const uint32_t* perm2;
   const uint64_t* dyn_cdf;        /* dynamic: [dyn_k] count distribution (above)     */
+  float dyn_rse_max;              /* dynamic: a bound on rel_sus * quarantine factor *
+                                     (1 - sus_imm) over the sim's agents (the largest
+                                     rel_sus, times quar_factor when above 1); the
+                                     edge pass thins each source's entries by it     */
+  int32_t _pad2;
 } covgpu_layer;
 
 /* One agent block of the agent kernel: agents [begin, end) of one sim. */
@@ -273,7 +278,9 @@ typedef struct covgpu_state {
   int32_t* vaccine_source;
   float* sus_imm; float* symp_imm; float* sev_imm;   /* [n_variants_max][n]           */
   int32_t imm_stride_variants;    /* rows of the imm blocks (max variants over sims) */
-  int32_t _pad0;
+  int32_t edge_parts;             /* what covgpu_edge_pass launches: 0 both passes, 1 the
+                                     stored layers' tiles only, 2 the dynamic layers'
+                                     sources only (covgpu_run_days runs both)        */
   float* dates;                   /* [COVGPU_N_DATES][n]                             */
   float* durs;                    /* [COVGPU_N_DURS][n]                              */
   /* per-day working buffers */
@@ -377,6 +384,7 @@ int covgpu_infections(float beta, const int32_t* p1, const int32_t* p2, const fl
  * otherwise those of covgpu_infections, and it allocates nothing. The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress
  * with that device current); make that first call before any stream capture.
+ * After a device reset (a new context) the next call looks the address up again.
  * Every call shares the one array and rewrites the part it reads, so calls
  * need no clearing between them, but calls whose kernels overlap on the GPU
  * (different streams, or concurrent host threads) race on it: serialise them. */

@@ -189,6 +189,55 @@ def dyn_counts(k0, k1, day, layer, agents, table):
     return out
 
 
+TAG_DYN_HIT = 0x0A000000
+
+
+def dyn_partners(k0, k1, day, layer, agents, d, j, n_agents):
+    """Partner j of list d of each agent (the entries dyn_lists draws), for
+    given (agent, d, j) triples."""
+    ag = np.asarray(agents, dtype=np.int64)
+    dd = np.asarray(d, dtype=np.int64)
+    jj = np.asarray(j, dtype=np.int64)
+    w = philox4x32_10(ag, 1 + 256 * dd + (jj >> 2), day, TAG_DYN | int(layer), k0, k1)
+    x = np.choose(jj & 3, [w[0], w[1], w[2], w[3]]).astype(np.uint64)
+    n = np.uint64(n_agents)
+    thr = np.uint64((2 ** 32 - int(n_agents)) % int(n_agents))
+    m = x * n
+    mask32 = np.uint64(0xFFFFFFFF)
+    bad = (m & mask32) < thr
+    for r in range(16):
+        if not bad.any():
+            break
+        idx = np.nonzero(bad)[0]
+        rw = philox4x32_10(ag[idx], (dd[idx] << 10) | jj[idx], day, TAG_DYN_RETRY | (r << 8) | int(layer), k0, k1)
+        m[idx] = rw[0].astype(np.uint64) * n
+        bad[idx] = (m[idx] & mask32) < thr
+    return (m >> np.uint64(32)).astype(np.int64)
+
+
+def thin_shift(pmax):
+    """m with 2**-m the power of two just above each float32 bound pmax (0 for
+    pmax >= 1, at most 32): an entry is a potential transmission with
+    probability 2**-m."""
+    pm = np.asarray(pmax, dtype=np.float32)
+    ex = ((pm.view(np.uint32) >> np.uint32(23)) & np.uint32(0xFF)).astype(np.int64)
+    m = np.where(ex == 0, 32, np.minimum(32, 126 - ex))
+    return np.where(pm >= 1, 0, m).astype(np.int64)
+
+
+def dyn_potential(k0, k1, day, layer, agents, d, j, m):
+    """Whether entry j of list d of each agent is a potential transmission: the
+    top m bits of word j % 4 of Philox (agent, 256 d + j // 4, day,
+    TAG_DYN_HIT | layer) are zero."""
+    ag = np.asarray(agents, dtype=np.int64)
+    dd = np.asarray(d, dtype=np.int64)
+    jj = np.asarray(j, dtype=np.int64)
+    w = philox4x32_10(ag, 256 * dd + (jj >> 2), day, TAG_DYN_HIT | int(layer), k0, k1)
+    x = np.choose(jj & 3, [w[0], w[1], w[2], w[3]]).astype(np.uint64)
+    m = np.asarray(m, dtype=np.int64)
+    return (m == 0) | ((x >> (32 - np.minimum(np.maximum(m, 1), 32)).astype(np.uint64)) == 0)
+
+
 def dyn_lists(k0, k1, day, layer, agents, table, n_agents):
     """Every entry of the two lists of each agent: arrays (agent, d, j, partner),
     ordered by agent, then d, then j. Partner j of list d is word j % 4 of

@@ -105,10 +105,13 @@ class OracleSim:
         self.rng = rng
         # philox mode: a dynamic layer's day is drawn as per-agent lists (ph.dyn_lists)
         self.dyn_tables = {}
+        self.dyn_rse_max = {}  # the thinning bound of each dynamic layer: the largest rel_sus' it can meet
         if rng == 'philox':
+            rs_max = np.float32(np.max(self.people.rel_sus)) if self.n else np.float32(0)
             for lkey in self.layer_keys:
                 if pars['dynam_layer'].get(lkey, 0) and len(self.contacts[lkey]['p1']):
                     self.dyn_tables[lkey] = ph.dyn_count_table(len(self.contacts[lkey]['p1']), self.n)
+                    self.dyn_rse_max[lkey] = max(rs_max, np.float32(rs_max * F32(pars['quar_factor'][lkey])))
         self.seed = int(pars['rand_seed'])
         self.k0, self.k1 = ph.seed_key(self.seed)
         if rng == 'mt':
@@ -199,7 +202,7 @@ class OracleSim:
         sus = np.nonzero(self.people.susceptible)[0]
         rng = np.random.default_rng([self.seed, 0x1A1A, t, v.index])
         x = v.n_imports / (self.rescale_vec[t] if getattr(v, 'rescale', True) else 1.0)
-        n_imp = min(int(x) if x == int(x) else int(np.floor(x + rng.random())), len(sus))
+        n_imp = int(x) if x == int(x) else int(np.floor(x + rng.random()))  # more than len(sus): ValueError below
         inds = rng.choice(sus, n_imp, replace=False)
         if len(inds):
             self.people.infect(inds=inds, layer='importation', variant=v.index, draws=self._draws(CALL_IMPORT + v.index))
@@ -226,41 +229,71 @@ class OracleSim:
         li = self.layer_keys.index(lkey)
         return ph.dyn_lists(self.k0, self.k1, self.t, li, agents, self.dyn_tables[lkey], self.n)
 
-    def exposures(self, li, rel_trans):
-        """The day's edge directions of layer li whose source has rel_trans != 0, as
-        the transmission draw keys them: arrays (source, target, direction, edge
-        identity, edge beta). Stored layers: every edge in both directions (the
-        identity is the edge index); dynamic layers in philox mode: the entries of
-        the sources' lists (identity ph.dyn_edge_id)."""
+    def exposures(self, li, variant, beta, rel_trans, rel_sus):
+        """The day's exposed directions of layer li (source rel_trans != 0, target
+        rel_sus != 0, p != 0) with their transmission outcome, as the CUDA library
+        draws them: arrays (source, target, direction, edge identity, edge beta,
+        float32 p, transmitted). Stored layers: every edge in both directions, the
+        identity its index, transmitted when the edge's uniform u < p. Dynamic
+        layers in philox mode: every entry of every source's lists (identity
+        ph.dyn_edge_id), transmitted when it is a potential transmission of the
+        thinning and u < p * 2**m (see dynamic_infections)."""
         lkey = self.layer_keys[li]
         if lkey in self.dyn_tables:
-            S = rel_trans.nonzero()[0]
-            a, d, j, g = self.dynamic_lists(lkey, S)
-            return (a, g, d, ph.dyn_edge_id(a, j, self.t, li), np.ones(len(a), dtype=F32))
+            return self._dyn_entries(li, variant, beta, rel_trans, rel_sus, every_entry=True)
         layer = self.contacts[lkey]
         e = np.arange(len(layer['p1']), dtype=np.int64)
         src = np.concatenate([layer['p1'], layer['p2']]).astype(np.int64)
         tgt = np.concatenate([layer['p2'], layer['p1']]).astype(np.int64)
         d = np.repeat(np.array([0, 1], dtype=np.int64), len(e))
-        keep = rel_trans[src] != 0
-        return (src[keep], tgt[keep], d[keep], np.concatenate([e, e])[keep],
-                np.concatenate([layer['beta'], layer['beta']]).astype(F32)[keep])
+        eb = np.concatenate([layer['beta'], layer['beta']]).astype(F32)
+        eid = np.concatenate([e, e])
+        p = (F32(beta) * eb) * rel_trans[src] * rel_sus[tgt]
+        keep = p != 0
+        src, tgt, d, eid, eb, p = src[keep], tgt[keep], d[keep], eid[keep], eb[keep], p[keep]
+        u0, u1 = ph.edge_uniforms(self.k0, self.k1, self.t, li, variant, eid)
+        hit = np.where(d == 0, u0, u1) < p.astype(np.float64)
+        return src, tgt, d, eid, eb, p, hit
+
+    def _dyn_entries(self, li, variant, beta, rel_trans, rel_sus, every_entry=False):
+        """The list entries of dynamic layer li's sources (rel_trans != 0) with
+        p != 0: the potential transmissions of the thinning, or every entry."""
+        lkey = self.layer_keys[li]
+        t, k0, k1 = self.t, self.k0, self.k1
+        S = rel_trans.nonzero()[0].astype(np.int64)
+        q = (F32(beta) * F32(1.0)) * rel_trans[S]  # beta * layer beta (1 for a redrawn layer) * rel_trans'
+        m = ph.thin_shift(q * F32(self.dyn_rse_max[lkey]))
+        counts = ph.dyn_counts(k0, k1, t, li, S, self.dyn_tables[lkey]).reshape(-1)
+        pos = np.repeat(np.repeat(np.arange(len(S)), 2), counts)  # source position of each entry
+        d = np.repeat(np.tile(np.array([0, 1], dtype=np.int64), len(S)), counts)
+        j = np.arange(len(pos), dtype=np.int64) - np.repeat(np.cumsum(counts) - counts, counts)
+        a = S[pos]
+        pot = ph.dyn_potential(k0, k1, t, li, a, d, j, m[pos])
+        if not every_entry:
+            a, d, j, pos, pot = a[pot], d[pot], j[pot], pos[pot], pot[pot]
+        g = ph.dyn_partners(k0, k1, t, li, a, d, j, self.n)
+        p = q[pos] * rel_sus[g]
+        keep = p != 0
+        a, g, d, j, pos, pot, p = a[keep], g[keep], d[keep], j[keep], pos[keep], pot[keep], p[keep]
+        eid = ph.dyn_edge_id(a, j, t, li)
+        u0, u1 = ph.edge_uniforms(k0, k1, t, li, variant, eid)
+        scaled = p * np.ldexp(np.float32(1), m[pos]).astype(F32)  # p * 2**m, exact in float32
+        hit = pot & (np.where(d == 0, u0, u1) < scaled.astype(np.float64))
+        return a, g, d, eid, np.ones(len(a), dtype=F32), p, hit
 
     def dynamic_infections(self, li, variant, beta, rel_trans, rel_sus):
         """compute_infections (utils.py:93-128) over dynamic layer li in philox
-        mode: every list entry of a source is the edge source -> partner in its
-        direction; p = beta * 1 * rel_trans[s] * rel_sus[g] in float32, one draw
-        per edge with p != 0 keyed by its identity, and the transmissions ordered by
-        (direction, identity) as the reference orders direction then edge."""
-        s, g, d, eid, eb = self.exposures(li, rel_trans)
-        p = (F32(beta) * eb) * rel_trans[s] * rel_sus[g]
-        nz = p.nonzero()[0]
-        s, g, d, eid, p = s[nz], g[nz], d[nz], eid[nz], p[nz]
-        u0, u1 = ph.edge_uniforms(self.k0, self.k1, self.t, li, variant, eid)
-        u = np.where(d == 0, u0, u1)
-        hit = (u < p.astype(np.float64)).nonzero()[0]
-        order = np.lexsort((eid[hit], d[hit]))
-        return s[hit][order].astype(np.int32), g[hit][order].astype(np.int32)
+        mode, with the sources' list entries thinned: entry j of list d of source
+        s (p(s, g) = beta * rel_trans'[s] * rel_sus'[g] <= pmax = beta *
+        rel_trans'[s] * rse_max) is a potential transmission with probability
+        2**-m >= pmax (ph.thin_shift, ph.dyn_potential); only then is its partner
+        g drawn, and it transmits when its edge uniform u < p * 2**m. The
+        transmissions are ordered by (direction, identity), as the reference
+        orders direction then edge."""
+        s, g, d, eid, _, _, hit = self._dyn_entries(li, variant, beta, rel_trans, rel_sus)
+        s, g, d, eid = s[hit], g[hit], d[hit], eid[hit]
+        order = np.lexsort((eid, d))
+        return s[order].astype(np.int32), g[order].astype(np.int32)
 
     def step(self):
         p = self.pars

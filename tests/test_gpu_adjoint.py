@@ -11,7 +11,7 @@ import covasim_gb300 as cv
 from covasim_gb300.adjoint import LikelihoodRun, SimLikelihood, fit_parameters
 from oracle import philox as ph
 from oracle.kernels import compute_trans_sus
-from test_gpu_sim import oracle_for
+from common import oracle_for
 
 pytestmark = pytest.mark.gpu
 
@@ -88,13 +88,11 @@ def torch_reference(sim, run, theta):
                     * np.where(pp.symptomatic, 1.0, af) * np.where(pp.isolated, isf, 1.0) * vl.astype(np.float64)
                 rse = pp.rel_sus.astype(np.float64) * np.where(pp.quarantined, qf, 1.0) \
                     * (1.0 - pp.sus_imm[v].astype(np.float64))
-                # every exposed direction as the GPU keys it (a dynamic layer: the sources' lists)
-                s, g, d, eid, eb = o.exposures(li, rt32)
-                u0, u1 = ph.edge_uniforms(o.k0, o.k1, t, li, v, eid)
-                u = np.where(d == 0, u0, u1)
-                p32 = beta32 * eb * rt32[s] * rs32[g]
+                # every exposed direction with its outcome as the GPU draws it (a dynamic
+                # layer: the entries of the sources' lists, thinned)
+                s, g, d, eid, eb, p32, hit = o.exposures(li, v, beta32, rt32, rs32)
                 m = (p32 > 0) & inf_v[s] & pp.susceptible[g]
-                recs.append(dict(l=li, v=v, g=g[m], infected=u[m] < p32[m],
+                recs.append(dict(l=li, v=v, g=g[m], infected=hit[m],
                                  c=eb[m].astype(np.float64) * rte[s[m]] * rse[g[m]]))
         days.append(recs)
 

@@ -67,6 +67,17 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
         assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
 
 
+def test_noalloc_at_its_edge_limit_matches_allocating_entry_point():
+    """Exactly the largest size the array holds: every tile's count and offset slot in use."""
+    lib = L.lib()
+    E = L.NOALLOC_MAX_EDGES
+    inputs = _inputs(3, E, 2_000_000, 0.002)
+    want = _call(lib, False, 0.5, *inputs, seed=3, day=4)
+    got = _call(lib, True, 0.5, *inputs, seed=3, day=4)
+    assert len(want[0]) > 0
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+
+
 def test_noalloc_rejects_more_edges_than_its_array_holds():
     lib = L.lib()
     rc = lib.covgpu_infections_noalloc(C.c_float(0.1), None, None, None, L.NOALLOC_MAX_EDGES + 1, None, None, 10,
