@@ -867,67 +867,39 @@ __global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st,
       }
       for (int d = 0; d < 2; ++d) {
         const int kd = k[d];
-        if (LIK) {
-          // every entry (the likelihood needs the terms of every exposed direction),
-          // four partners per Philox block; potential ones flagged for the outcome
-          int hblk = -1;
-          uint4 hw = make_uint4(0u, 0u, 0u, 0u);
-          const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)((kd + 3) >> 2));
-          for (int qd = 0; qd < nq_max; ++qd) {
-            const int j0 = 4 * qd;
-            int32_t g[4] = {0, 0, 0, 0};
-            uint32_t tb = 0u, pm = 0u;
-            if (j0 < kd) {
-              const uint4 pw = dyn_partner_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
-#pragma unroll
-              for (int r = 0; r < 4; ++r)
-                if (j0 + r < kd) {
-                  g[r] = off + (int32_t)dyn_partner(word_of(pw, r), n_local, thr, a, d, j0 + r, day, (uint32_t)l,
-                                                    c.key0, c.key1);
-                  tb |= tgt_bit(st, g[r]) << r;
-                  if (m >= 0 && thin_entry(a, d, j0 + r, m, day, (uint32_t)l, c.key0, c.key1, hblk, hw))
-                    pm |= 1u << r;
-                }
-            }
+        const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)((kd + 3) >> 2));
+        for (int qd = 0; qd < nq_max; ++qd) {
+          const int j0 = 4 * qd;
+          // potential transmissions among entries j0 .. j0 + 3 (one Philox block)
+          uint32_t pm = 0u;
+          if (j0 < kd && m >= 0) {
+            const uint4 hw = dyn_hit_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
 #pragma unroll
             for (int r = 0; r < 4; ++r)
-              queue_push(q, qn, (tb >> r) & 1u, s, g[r],
-                         ((uint32_t)(j0 + r) << 2) | (((pm >> r) & 1u) << 1) | (uint32_t)d);
-            if (qn > EQ_CAP - 4 * 32) {
-              dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
-              qn = 0;
-            }
+              if (j0 + r < kd && thin_potential(word_of(hw, r), m)) pm |= 1u << r;
           }
-        } else {
-          // the potential entries only: 4c of them tested per Philox block of words,
-          // then each one's partner
-          const int E = m >= 0 ? 4 * (32 / thin_chunk_bits(m)) : 32;
-          const int nb = m >= 0 ? (kd + E - 1) / E : 0;
-          const int nb_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)nb);
-          for (int bi = 0; bi < nb_max; ++bi) {
-            uint32_t rem = 0u;
-            if (bi < nb)
-              rem = thin_block_mask(m == 0 ? make_uint4(0u, 0u, 0u, 0u)
-                                           : dyn_hit_block(a, d, bi, day, (uint32_t)l, c.key0, c.key1),
-                                    m, bi * E, kd);
-            while (__any_sync(0xffffffffu, rem != 0u)) {
-              bool cand = false;
-              int32_t g = 0;
-              uint32_t j = 0u;
-              if (rem) {
-                j = (uint32_t)(bi * E + __ffs(rem) - 1);
-                rem &= rem - 1u;
-                const uint4 pw = dyn_partner_block(a, d, (int)j, day, (uint32_t)l, c.key0, c.key1);
-                g = off + (int32_t)dyn_partner(word_of(pw, (int)(j & 3u)), n_local, thr, a, d, (int)j, day,
-                                               (uint32_t)l, c.key0, c.key1);
-                cand = tgt_bit(st, g) != 0u;
+          // partners: of the potential entries (all entries for the likelihood)
+          const uint32_t want = LIK ? (j0 < kd ? (0xFu >> max(0, 4 - (kd - j0))) : 0u) : pm;
+          if (!__any_sync(0xffffffffu, want != 0u)) continue;
+          int32_t g[4] = {0, 0, 0, 0};
+          uint32_t tb = 0u;
+          if (want) {
+            const uint4 pw = dyn_partner_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+              if ((want >> r) & 1u) {
+                g[r] = off + (int32_t)dyn_partner(word_of(pw, r), n_local, thr, a, d, j0 + r, day, (uint32_t)l,
+                                                  c.key0, c.key1);
+                tb |= tgt_bit(st, g[r]) << r;
               }
-              queue_push(q, qn, cand, s, g, (j << 2) | 2u | (uint32_t)d);
-              if (qn > EQ_CAP - 32) {
-                dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
-                qn = 0;
-              }
-            }
+          }
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            queue_push(q, qn, (tb >> r) & 1u, s, g[r],
+                       ((uint32_t)(j0 + r) << 2) | (((pm >> r) & 1u) << 1) | (uint32_t)d);
+          if (qn > EQ_CAP - 4 * 32) {
+            dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+            qn = 0;
           }
         }
       }

@@ -141,54 +141,22 @@ __device__ __forceinline__ uint32_t word_of(const uint4& w, int k) {
 // layer transmits with p(s, g) = beta * rel_trans'(s) * rel_sus'(g) <= pmax(s) =
 // beta * rel_trans'(s) * rse_max (rse_max bounds rel_sus' over the sim's agents).
 // An entry is first a potential transmission with probability 2^-m, the power
-// of two just above pmax (m = thin_shift(pmax)); only then is its partner drawn,
-// and it transmits when u < p * 2^m (u the edge's Bernoulli uniform, p * 2^m
-// exact in float32). So P(transmission) = p. The potential test of entry j of
-// list d takes a chunk of b = max(m, 4) bits: c = 32 / b chunks per 32-bit word,
-// word w = j / c being word w % 4 of Philox (a, d * 256 + w / 4, day,
-// TAG_DYN_HIT | layer) and the chunk its bits [b (j % c), b (j % c) + b); the
-// entry is potential when the chunk's top m bits are zero (m = 0: always). One
-// Philox block serves 4c entries (20 to 32 at the usual m), instead of drawing a
-// partner, two gathers and a Bernoulli per entry.
+// of two just above pmax (m = thin_shift(pmax)), decided by the top m bits of
+// one 32-bit word of Philox (a, d * 256 + j / 4, day, TAG_DYN_HIT | layer); only
+// then is its partner drawn, and it transmits when u < p * 2^m (u the edge's
+// Bernoulli uniform, p * 2^m exact in float32). So P(transmission) = p, with one
+// 32-bit word per entry instead of a partner, a gather and a Bernoulli draw.
 __device__ __forceinline__ int thin_shift(float pmax) {
   if (pmax >= 1.0f) return 0;
   const int ex = (int)((__float_as_uint(pmax) >> 23) & 0xffu);  // pmax in [2^(ex-127), 2^(ex-126))
   return ex == 0 ? 32 : min(32, 126 - ex);
 }
-__device__ __forceinline__ int thin_chunk_bits(int m) { return m < 4 ? 4 : m; }
-// Philox block `blk` of the potential-transmission words of list d
-__device__ __forceinline__ uint4 dyn_hit_block(uint32_t a, int d, int blk, uint32_t day, uint32_t layer, uint32_t k0,
+__device__ __forceinline__ bool thin_potential(uint32_t w, int m) {
+  return m == 0 || (w >> (32 - m)) == 0u;
+}
+__device__ __forceinline__ uint4 dyn_hit_block(uint32_t a, int d, int j, uint32_t day, uint32_t layer, uint32_t k0,
                                                uint32_t k1) {
-  return philox(make_uint4(a, ((uint32_t)d << 8) + (uint32_t)blk, day, TAG_DYN_HIT | layer), k0, k1);
-}
-// The potential entries among the 4c entries of hit block w (entry j0 + e is
-// bit e; entries at or past k excluded); m >= 0
-__device__ __forceinline__ uint32_t thin_block_mask(const uint4& w, int m, int j0, int k) {
-  const int b = thin_chunk_bits(m), c = 32 / b;
-  const uint32_t mask = b == 32 ? 0xffffffffu : ((1u << b) - 1u);
-  uint32_t pm = 0u;
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const uint32_t word = word_of(w, r);
-    for (int ci = 0; ci < c; ++ci) {
-      const int e = r * c + ci;
-      if (j0 + e < k && (m == 0 || ((((word >> (ci * b)) & mask) >> (b - m)) == 0u))) pm |= 1u << e;
-    }
-  }
-  return pm;
-}
-// Whether entry j of list d is potential, with the block it needs cached in (blk, w)
-__device__ __forceinline__ bool thin_entry(uint32_t a, int d, int j, int m, uint32_t day, uint32_t layer, uint32_t k0,
-                                           uint32_t k1, int& blk, uint4& w) {
-  if (m == 0) return true;
-  const int b = thin_chunk_bits(m), c = 32 / b, wi = j / c;
-  if ((wi >> 2) != blk) {
-    blk = wi >> 2;
-    w = dyn_hit_block(a, d, blk, day, layer, k0, k1);
-  }
-  const uint32_t mask = b == 32 ? 0xffffffffu : ((1u << b) - 1u);
-  const uint32_t chunk = (word_of(w, wi & 3) >> ((j - wi * c) * b)) & mask;
-  return (chunk >> (b - m)) == 0u;
+  return philox(make_uint4(a, ((uint32_t)d << 8) + ((uint32_t)j >> 2), day, TAG_DYN_HIT | layer), k0, k1);
 }
 
 // The set bits of one agent block's bitmap words, handed to the lanes 32 at a

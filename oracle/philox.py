@@ -226,23 +226,16 @@ def thin_shift(pmax):
 
 
 def dyn_potential(k0, k1, day, layer, agents, d, j, m):
-    """Whether entry j of list d of each agent is a potential transmission (m =
-    the source's thinning shift): its chunk of b = max(m, 4) bits, chunk j % c
-    (c = 32 // b chunks per word, lowest bits first) of word w = j // c, word
-    w % 4 of Philox (agent, 256 d + w // 4, day, TAG_DYN_HIT | layer), has its top
-    m bits zero (m = 0: every entry)."""
+    """Whether entry j of list d of each agent is a potential transmission: the
+    top m bits of word j % 4 of Philox (agent, 256 d + j // 4, day,
+    TAG_DYN_HIT | layer) are zero."""
     ag = np.asarray(agents, dtype=np.int64)
     dd = np.asarray(d, dtype=np.int64)
     jj = np.asarray(j, dtype=np.int64)
+    w = philox4x32_10(ag, 256 * dd + (jj >> 2), day, TAG_DYN_HIT | int(layer), k0, k1)
+    x = np.choose(jj & 3, [w[0], w[1], w[2], w[3]]).astype(np.uint64)
     m = np.asarray(m, dtype=np.int64)
-    b = np.where(m < 4, 4, m)
-    c = 32 // b
-    wi = jj // c
-    w = philox4x32_10(ag, 256 * dd + (wi >> 2), day, TAG_DYN_HIT | int(layer), k0, k1)
-    word = np.choose(wi & 3, [w[0], w[1], w[2], w[3]]).astype(np.uint64)
-    mask = np.where(b == 32, np.uint64(0xFFFFFFFF), (np.uint64(1) << b.astype(np.uint64)) - np.uint64(1))
-    chunk = (word >> ((jj - wi * c) * b).astype(np.uint64)) & mask
-    return (m == 0) | ((chunk >> (b - m).astype(np.uint64)) == 0)
+    return (m == 0) | ((x >> (32 - np.minimum(np.maximum(m, 1), 32)).astype(np.uint64)) == 0)
 
 
 def dyn_lists(k0, k1, day, layer, agents, table, n_agents):
