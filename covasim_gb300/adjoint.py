@@ -33,7 +33,7 @@ from . import _lib as L
 from .interventions import change_beta
 from .sim import init_infections
 
-__all__ = ['Parameters', 'LikelihoodRun', 'SimLikelihood', 'fit_parameters']
+__all__ = ['Parameters', 'LikelihoodRun', 'SimLikelihood', 'fit_parameters', 'delay_matrix']
 
 
 class Parameters:
@@ -132,7 +132,7 @@ class LikelihoodRun:
             sim.initialize()
         if sim.state.hold is not None:
             raise NotImplementedError('likelihood runs do not support dynamic rescaling (pop_scale > 1 with rescale)')
-        if sim.state.has_testing or sim['variants']:
+        if sim['variants']:
             raise NotImplementedError('likelihood runs support sims without host-side days (no variants imports)')
         self.sim = sim
         self.state = sim.state
@@ -208,6 +208,22 @@ class LikelihoodRun:
         G = float(g_ll) * out['G'] + np.asarray(g_expected, dtype=np.float64)[:, None] * out['H']
         return self.params.chain(theta_eval, G)
 
+    def diagnosis_kernel(self):
+        """K[k]: the fraction of the last run's infected agents diagnosed k days
+        after their exposure (date_diagnosed - date_exposed), an estimate of the
+        delay distribution from infection to a positive test result."""
+        st = self.state
+        e = st.get('date_exposed').cpu().numpy()
+        d = st.get('date_diagnosed').cpu().numpy()
+        exposed = ~np.isnan(e)
+        K = np.zeros(self.npts)
+        if not exposed.any():
+            return K
+        diag = exposed & ~np.isnan(d)
+        lag = np.clip(np.rint(d[diag] - e[diag]).astype(np.int64), 0, self.npts - 1)
+        np.add.at(K, lag, 1.0)
+        return K / exposed.sum()
+
     def loglik(self, theta_eval):
         """ll and expected[npts] at ``theta_eval`` on the last run's fixed states."""
         out = self.recompute(theta_eval, grad=False)
@@ -235,12 +251,28 @@ class SimLikelihood(torch.autograd.Function):
         return torch.from_numpy(grad), None
 
 
-def fit_parameters(run, target, theta0=None, fit=('beta',), steps=40, lr=0.05, fixed_states=False):
-    """Gradient-based calibration: minimise sum_t (expected[t] - target[t])^2 / sum(target^2)
-    over log theta of the parameters named in ``fit`` (Adam). With
+def delay_matrix(K):
+    """M[t, s] = K[t - s] (t >= s): M @ expected gives the expected diagnoses of each day."""
+    T = len(K)
+    idx = np.arange(T)
+    lag = idx[:, None] - idx[None, :]
+    return np.where(lag >= 0, np.asarray(K)[np.clip(lag, 0, T - 1)], 0.0)
+
+
+def fit_parameters(run, target, theta0=None, fit=('beta',), steps=40, lr=0.05, fixed_states=False,
+                   observe='infections'):
+    """Gradient-based calibration: minimise sum_t (model[t] - target[t])^2 / sum(target^2)
+    over log theta of the parameters named in ``fit`` (Adam). The model of the
+    target series is the expected new infections of each day (observe =
+    'infections'), or the expected diagnoses (observe = 'diagnoses': the expected
+    infections convolved with the run's own infection-to-diagnosis delay
+    distribution, ``LikelihoodRun.diagnosis_kernel``, which is held fixed within
+    a step), the series a sim with test_prob reports as new_diagnoses. With
     ``fixed_states`` the states of one run at ``theta0`` are kept and only the
     likelihood is re-evaluated; otherwise each step re-simulates at the
     current parameters. Returns (theta, history of (loss, theta))."""
+    if observe not in ('infections', 'diagnoses'):
+        raise ValueError("observe must be 'infections' or 'diagnoses'")
     names = run.params.names
     theta0 = run.params.theta0 if theta0 is None else np.asarray(theta0, dtype=np.float64)
     idx = [names.index(n) for n in fit]
@@ -257,16 +289,20 @@ def fit_parameters(run, target, theta0=None, fit=('beta',), steps=40, lr=0.05, f
         if fixed_states:
             th = theta.detach().numpy()
             ll, expected = run.loglik(th)
-            e = torch.from_numpy(expected)
+            M = delay_matrix(run.diagnosis_kernel()) if observe == 'diagnoses' else np.eye(len(expected))
+            e = torch.from_numpy(M @ expected)
             resid = e - target[:len(e)]
             loss = float((resid ** 2).sum()) / scale
-            g_exp = (2.0 * resid / scale).numpy()
+            g_exp = M.T @ (2.0 * resid / scale).numpy()
             g_theta = torch.from_numpy(run.backward(0.0, g_exp, theta_eval=th))
             opt.zero_grad()
             logt.grad = g_theta[idx] * torch.exp(logt.detach())
         else:
             _, expected = SimLikelihood.apply(theta, run)
-            resid = expected - target[:len(expected)]
+            model = expected
+            if observe == 'diagnoses':
+                model = torch.from_numpy(delay_matrix(run.diagnosis_kernel())) @ expected
+            resid = model - target[:len(model)]
             loss_t = (resid ** 2).sum() / scale
             opt.zero_grad()
             loss_t.backward()

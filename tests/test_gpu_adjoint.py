@@ -145,3 +145,20 @@ def test_autograd_function_and_calibration_recover_beta():
     assert theta.grad is not None and theta.grad[0] > 0  # more beta, more expected infections
     fitted, hist = fit_parameters(run, target, fit=('beta',), steps=30, lr=0.08)
     assert abs(fitted[0] - 0.018) < 0.1 * 0.018, hist[-5:]
+
+
+def test_calibration_to_daily_diagnoses_recovers_beta():
+    """Config 4's calibration: beta fitted to the daily diagnoses (test_prob) of a
+    sim run at beta = 0.018, through the expected infections convolved with the
+    run's infection-to-diagnosis delays, starting from beta = 0.012."""
+    tp = dict(symp_prob=0.1)
+    base = dict(pop_type='hybrid', pop_size=30000, n_days=80, pop_infected=60)
+    target_sim = cv.Sim(dict(base, rand_seed=31, beta=0.018), interventions=[cv.test_prob(**tp)])
+    target = target_sim.run().raw_results()['new_diagnoses']
+    assert target.sum() > 500
+    sim = cv.Sim(dict(base, rand_seed=32, beta=0.012), interventions=[cv.test_prob(**tp)])
+    sim.initialize()
+    run = LikelihoodRun(sim, which=('beta',))
+    fitted, hist = fit_parameters(run, target, fit=('beta',), steps=30, lr=0.08, observe='diagnoses')
+    assert abs(fitted[0] - 0.018) < 0.1 * 0.018, hist[-5:]
+
