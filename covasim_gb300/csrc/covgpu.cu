@@ -31,11 +31,11 @@ using namespace covgpu;
 namespace {
 
 // resident blocks per SM that the register budget of the agent pass must allow
-// (0: the compiler's choice). Six blocks (40 registers, a few spilled) ran the
-// agent pass of a 1M-agent run 10% faster than the compiler's 58 registers (four
-// blocks); bounding the infect pass the same way changed nothing.
+// (0: the compiler's choice). With its per-agent loads issued up front, five blocks
+// ran a whole 1M-agent run (one CUDA graph) in 20.8 ms, six in 20.9 and four in
+// 20.9; bounding the infect pass the same way changed nothing.
 #ifndef COVGPU_AGENT_MIN_BLOCKS
-#define COVGPU_AGENT_MIN_BLOCKS 6
+#define COVGPU_AGENT_MIN_BLOCKS 5
 #endif
 #if COVGPU_AGENT_MIN_BLOCKS
 #define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS, COVGPU_AGENT_MIN_BLOCKS)
@@ -74,6 +74,25 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   const bool valid = i < blk.end;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int tp = t - 1;
+  const bool waning = sp.use_waning != 0;
+
+  // Every per-agent load the pass needs for (nearly) every agent, issued before the
+  // block's table copy and barrier so that their latencies overlap with it and with
+  // each other: the state words, rel_sus, the recovery date, the NAb fields.
+  uint32_t f = 0u, vs = 0xFFFFFFFFu;
+  float a_rs = 0.0f, a_dr = f32nan(), a_nab = 0.0f, a_peak = 0.0f;
+  int a_tne = 0;
+  if (valid) {
+    f = st.flags[i];
+    vs = st.vstate[i];
+    a_rs = st.rel_sus[i];
+    a_dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
+    if (waning) {
+      a_nab = st.nab[i];
+      a_peak = st.peak_nab[i];
+      a_tne = st.t_nab_event[i];
+    }
+  }
 
   // shared counters: [0, N_RES_INT) day-t ints, then prev-day stocks, then variant slots
   __shared__ unsigned int s_cnt[COVGPU_N_RES_INT];           // day t flows + severe/critical now
@@ -90,9 +109,8 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   if (do_day && blockIdx.x == 0 && threadIdx.x == 0) *st.event_count = 0ull;
   __syncthreads();
 
-  uint32_t f = valid ? st.flags[i] : 0u;
-  uint32_t vs = valid ? st.vstate[i] : 0xFFFFFFFFu;
   const uint32_t f_in = f, vs_in = vs;
+  float nab_now = a_nab;  // the NAb level after the closing pass's update_nab
   // reporting sums as fixed point (2^24 for NAbs, 2^32 for efficacies): exact integer
   // reductions, independent of order, and no float64 work per agent
   long long nab_fx = 0, sus_fx = 0, symp_fx = 0;
@@ -119,17 +137,17 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
     if (mine) atomicAdd(&s_var[((lane & 1) ? RV_N_INFECTIOUS : RV_N_EXPOSED) * COVGPU_MAX_VARIANTS + (lane >> 1)], mine);
     if (valid) {
       float nab = 0.0f;
-      if (sp.use_waning) {
-        nab = st.nab[i];
-        const float peak = st.peak_nab[i];
-        if (peak != 0.0f) {  // sim.py:666-669 -> immunity.py:205-213 at t-1
-          int k = tp - st.t_nab_event[i];
+      if (waning) {
+        nab = a_nab;
+        if (a_peak != 0.0f) {  // sim.py:666-669 -> immunity.py:205-213 at t-1
+          int k = tp - a_tne;
           if (k < 0 || k >= sp.nab_kin_len) {
             atomicOr(st.status, COVGPU_BADARG);
             k = k < 0 ? 0 : sp.nab_kin_len - 1;
           }
-          nab = update_nab_ff(nab, peak, sp.nab_kin[2 * k], sp.nab_kin[2 * k + 1]);
+          nab = update_nab_ff(nab, a_peak, sp.nab_kin[2 * k], sp.nab_kin[2 * k + 1]);
           st.nab[i] = nab;
+          nab_now = nab;
         }
       }
       if (!(f & B_DEAD) && nab != 0.0f) nab_fx = __float2ll_rn(__fmul_rn(nab, 16777216.0f));  // sim.py:672
@@ -145,9 +163,21 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       const float tf = (float)t;
       uint32_t ev = vs & 0xFFu, iv = (vs >> 8) & 0xFFu, rv = (vs >> 16) & 0xFFu;
       const bool is_exp = f & B_EXP;  // people.py:170 snapshot
+      // the exposed agents' dates and rel_trans (the infectious are among them), and
+      // the isolated agents' end date, loaded together before the checks use them
+      float d_inf = 0.0f, d_sym = 0.0f, d_sev = 0.0f, d_crit = 0.0f, d_dead = 0.0f, d_iso = 0.0f, a_rt = 0.0f;
+      if (is_exp) {
+        d_inf = date_row(st, COVGPU_DATE_INFECTIOUS)[i];
+        d_sym = date_row(st, COVGPU_DATE_SYMPTOMATIC)[i];
+        d_sev = date_row(st, COVGPU_DATE_SEVERE)[i];
+        d_crit = date_row(st, COVGPU_DATE_CRITICAL)[i];
+        d_dead = date_row(st, COVGPU_DATE_DEAD)[i];
+        a_rt = st.rel_trans[i];
+      }
+      if (f & B_ISO) d_iso = date_row(st, COVGPU_DATE_END_ISOLATION)[i];
       if (is_exp) {
         if (!(f & B_INF)) {  // check_infectious, people.py:222-232
-          const float d = date_row(st, COVGPU_DATE_INFECTIOUS)[i];
+          const float d = d_inf;
           if (defined(d) && tf >= d) {
             f |= B_INF;
             iv = ev;
@@ -156,36 +186,36 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
           }
         }
         if (!(f & B_SYMP)) {  // check_symptomatic, people.py:235-239
-          const float d = date_row(st, COVGPU_DATE_SYMPTOMATIC)[i];
+          const float d = d_sym;
           if (defined(d) && tf >= d) { f |= B_SYMP; c_symp = 1; }
         }
         if (!(f & B_SEV)) {  // check_severe, people.py:242-246
-          const float d = date_row(st, COVGPU_DATE_SEVERE)[i];
+          const float d = d_sev;
           if (defined(d) && tf >= d) { f |= B_SEV; c_sev = 1; }
         }
         if (!(f & B_CRIT)) {  // check_critical, people.py:249-253
-          const float d = date_row(st, COVGPU_DATE_CRITICAL)[i];
+          const float d = d_crit;
           if (defined(d) && tf >= d) { f |= B_CRIT; c_crit = 1; }
         }
         if (!(f & B_REC)) {  // check_recovery, people.py:256-291
-          const float d = date_row(st, COVGPU_DATE_RECOVERED)[i];
+          const float d = a_dr;
           if (defined(d) && tf >= d) {
             f &= ~(B_EXP | B_INF | B_SYMP | B_SEV | B_CRIT | BYVAR_MASK);
             f |= B_REC;
             rv = ev;
             iv = NOV;
             ev = NOV;
-            if (sp.use_waning) { f |= B_SUS; f &= ~B_DIAG; }
+            if (waning) { f |= B_SUS; f &= ~B_DIAG; }
             c_rec = 1;
           }
         }
       }
       if (f & B_ISO) {  // check_exit_iso, people.py:368-374
-        const float d = date_row(st, COVGPU_DATE_END_ISOLATION)[i];
+        const float d = d_iso;
         if (defined(d) && tf >= d) f &= ~B_ISO;
       }
       if (is_exp && !(f & B_DEAD)) {  // check_death, people.py:294-312
-        const float d = date_row(st, COVGPU_DATE_DEAD)[i];
+        const float d = d_dead;
         if (defined(d) && tf >= d) {
           f |= B_DEAD;
           if (f & B_DIAG) { f |= B_KDEAD; c_kdead = 1; }
@@ -199,13 +229,12 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       // an edge-pass target (susceptible, rel_sus nonzero) gets its susceptibility per
       // variant, rel_sus * (1 - sus_imm[v]) as compute_trans_sus forms it unquarantined
       // (utils.py:87), with the sign bit set when quarantined
-      const float rs = (f & B_SUS) ? st.rel_sus[i] : 0.0f;
+      const float rs = (f & B_SUS) ? a_rs : 0.0f;
       const bool is_tgt = rs != 0.0f;
       const uint32_t tq = (f & B_QUAR) ? 0x80000000u : 0u;
-      if (sp.use_waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
-        const float dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
-        const bool was_inf = tf >= dr;  // false for NaN
-        const float nab = st.nab[i];
+      if (waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
+        const bool was_inf = tf >= a_dr;  // false for NaN
+        const float nab = nab_now;
         ff ln_nab = ff{0.0f, 0.0f};
         bool have_ln = false;
         for (int v = 0; v < nv; ++v) {
@@ -233,10 +262,8 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       // with the records the edge pass gathers for its candidates (one 16-byte load
       // per endpoint instead of one per field)
       if (f & B_INF) {
-        const float rt = st.rel_trans[i];
-        const float vl = viral_load_one(t, date_row(st, COVGPU_DATE_INFECTIOUS)[i],
-                                        date_row(st, COVGPU_DATE_RECOVERED)[i], date_row(st, COVGPU_DATE_DEAD)[i],
-                                        sp.frac_time, sp.load_ratio, sp.high_cap);
+        const float rt = a_rt;
+        const float vl = viral_load_one(t, d_inf, a_dr, d_dead, sp.frac_time, sp.load_ratio, sp.high_cap);
         st.viral_load[i] = vl;
         src_bit = (rt != 0.0f && iv < (uint32_t)nv) ? 1u : 0u;
         if (src_bit)
@@ -246,7 +273,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       // pass relies on it to queue at most one direction per edge
       if (is_tgt) {
         tgt_bit = 1u;
-        if (!sp.use_waning)
+        if (!waning)
           for (int v = 0; v < nv; ++v) {
             const int64_t off = (int64_t)v * st.n + i;
             st.tgt_rec[off] = __uint_as_float(__float_as_uint(__fmul_rn(rs, __fsub_rn(1.0f, st.sus_imm[off]))) | tq);
