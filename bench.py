@@ -387,8 +387,10 @@ def adjoint_arm(args, n=100_000, days=120, every=10, reps=3):
     100,000-agent hybrid sim, 120 days, change_beta on days 30 and 60, gradients
     with respect to beta, the 4 layer betas and the 2 multipliers, a state
     checkpoint every 10 days. The forward runs the sim with the likelihood
-    passes; the adjoint rewinds to each checkpoint and recomputes its days with
-    the gradient accumulators. Wall-clock with device synchronisation."""
+    passes and the gradient accumulators, so the adjoint at the forward's own
+    parameters only combines them; the adjoint at other parameters (a
+    fixed-states step) rewinds to each checkpoint and recomputes its days.
+    Wall-clock with device synchronisation."""
     import torch
     import covasim_gb300 as cv
     from covasim_gb300.adjoint import LikelihoodRun
@@ -424,12 +426,15 @@ def adjoint_arm(args, n=100_000, days=120, every=10, reps=3):
     t_plain = timed(plain)
     t_fwd = timed(lambda: run.forward(th))
     t_both = timed(lambda: (run.forward(th), run.backward(1.0, g_exp)))
+    th_other = th * 1.05
+    t_other = timed(lambda: run.backward(1.0, g_exp, theta_eval=th_other))
     grad = run.backward(1.0, g_exp)
     return {'workload': f'hybrid {n} agents, {days} days, change_beta days 30/60, {len(th)} parameters, '
                         f'checkpoint every {every} days',
             'plain_ms': round(1e3 * t_plain, 3), 'forward_ms': round(1e3 * t_fwd, 3),
             'forward_adjoint_ms': round(1e3 * t_both, 3), 'adjoint_over_forward': round(t_both / t_fwd, 3),
             'forward_over_plain': round(t_fwd / t_plain, 3),
+            'adjoint_other_theta_ms': round(1e3 * t_other, 3),
             'grad': {k: float(v) for k, v in zip(run.params.names, grad)}}
 
 

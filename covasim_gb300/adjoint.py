@@ -21,10 +21,13 @@ Each parameter theta_k enters F[t, l] with exponent A[t, l, k] in {0, 1}:
 change_beta multiplier (interventions.py:530-586) on the days and layers it
 governs. So d/d theta_k = sum over t, l of A[t, l, k] * G[t, l] / theta_k.
 
-``LikelihoodRun`` runs the sim with a state checkpoint every few days; the
-backward pass rewinds to each checkpoint and recomputes its days with the
-gradient accumulators on, so memory stays at one state per checkpoint.
-``SimLikelihood`` wraps it as a ``torch.autograd.Function``.
+``LikelihoodRun`` runs the sim with a state checkpoint every few days and the
+gradient accumulators on (with a handful of parameters the sensitivities G and
+H cost little beside the run itself), so the backward pass at the forward's
+parameters reuses them; a backward or likelihood at other parameters rewinds
+to each checkpoint and recomputes its days on the run's fixed states, so
+memory stays at one state per checkpoint. ``SimLikelihood`` wraps it as a
+``torch.autograd.Function``.
 """
 import numpy as np
 import torch
@@ -144,6 +147,8 @@ class LikelihoodRun:
         self.state.enable_lik(grad=False)
         self.theta = None
         self.checkpoints = []
+        self._ck_buffers = []  # checkpoint storage, reused by every forward
+        self._grads = None      # G and H of the last forward, at its own parameters
 
     def _segments(self):
         return [(t0, min(t0 + self.every, self.npts)) for t0 in range(0, self.npts, self.every)]
@@ -168,18 +173,23 @@ class LikelihoodRun:
         st = self.state
         self.theta = theta.copy()
         self._set_dynamics(theta)
-        st.enable_lik(grad=False)
+        st.enable_lik(grad=True)
         st.set_lik_factor(self.params.factor(theta))
         st.zero_lik()
         st.restore(self.initial)
         init_infections(st, 0, self.sim.pars)
         self.checkpoints = []
-        for t0, t1 in self._segments():
-            self.checkpoints.append(st.checkpoint())
+        for k, (t0, t1) in enumerate(self._segments()):
+            if k < len(self._ck_buffers):
+                self.checkpoints.append(st.checkpoint(into=self._ck_buffers[k]))
+            else:
+                self._ck_buffers.append(st.checkpoint())
+                self.checkpoints.append(self._ck_buffers[k])
             st.run_days(t0, t1, open_prev=t0 > 0, close_last=t1 == self.npts, use_graph=self.use_graph)
         if st.status():
             raise L.CovgpuError('likelihood run', st.status())
-        out = self._read(grad=False)
+        out = self._read(grad=True)
+        self._grads = out
         self.last = out  # per-day ll and expected of this run
         return float(out['ll'].sum()), out['expected']
 
@@ -202,9 +212,16 @@ class LikelihoodRun:
         return self._read(grad=grad)
 
     def backward(self, g_ll, g_expected, theta_eval=None):
-        """Vector-Jacobian product: d(g_ll * ll + g_expected . expected) / d theta."""
-        theta_eval = self.theta if theta_eval is None else np.asarray(theta_eval, dtype=np.float64)
-        out = self.recompute(theta_eval, grad=True)
+        """Vector-Jacobian product: d(g_ll * ll + g_expected . expected) / d theta,
+        from the forward's own sensitivities at its parameters, else by
+        recomputing from the checkpoints at ``theta_eval``."""
+        if theta_eval is None or np.array_equal(np.asarray(theta_eval, dtype=np.float64), self.theta):
+            if self._grads is None:
+                raise RuntimeError('call forward() first')
+            theta_eval, out = self.theta, self._grads
+        else:
+            theta_eval = np.asarray(theta_eval, dtype=np.float64)
+            out = self.recompute(theta_eval, grad=True)
         G = float(g_ll) * out['G'] + np.asarray(g_expected, dtype=np.float64)[:, None] * out['H']
         return self.params.chain(theta_eval, G)
 

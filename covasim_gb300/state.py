@@ -1040,10 +1040,20 @@ class BatchState:
                 self.t[k].zero_()
         self._refresh_state()
 
-    def checkpoint(self):
+    def checkpoint(self, into=None):
         """Device copy of the state at a day boundary (with the results so far),
-        for ``rewind``: recomputing from it reproduces the run exactly."""
+        for ``rewind``: recomputing from it reproduces the run exactly. ``into``:
+        an earlier checkpoint of this state whose buffers are overwritten (no
+        allocation)."""
         keys = self.MUTABLE + (('pending_quar',) if self.has_testing else ()) + ('log_count',)
+        if into is not None:
+            for k in keys:
+                into[k].copy_(self.t[k])
+            for dst, src in zip(into['_res'], (self.res_int, self.res_var, self.res_fx)):
+                dst.copy_(src)
+            for a, b in zip(into['_imp'], self.import_variant):
+                a[:] = b
+            return into
         ck = {k: self.t[k].clone() for k in keys}
         ck['_res'] = (self.res_int.clone(), self.res_var.clone(), self.res_fx.clone())
         ck['_imp'] = [a.copy() for a in self.import_variant]
