@@ -31,11 +31,12 @@ using namespace covgpu;
 namespace {
 
 // resident blocks per SM that the register budget of the agent pass must allow
-// (0: the compiler's choice). With its per-agent loads issued up front, five blocks
-// ran a whole 1M-agent run (one CUDA graph) in 20.8 ms, six in 20.9 and four in
-// 20.9; bounding the infect pass the same way changed nothing.
+// (0: the compiler's choice); the pass's grid is one wave of them. Three blocks
+// ran a whole 1M-agent run (one CUDA graph) 0.8 ms faster than four and 2.3 ms
+// faster than five (both spilling); bounding the infect pass the same way
+// changed nothing.
 #ifndef COVGPU_AGENT_MIN_BLOCKS
-#define COVGPU_AGENT_MIN_BLOCKS 5
+#define COVGPU_AGENT_MIN_BLOCKS 3
 #endif
 #if COVGPU_AGENT_MIN_BLOCKS
 #define AGENT_BOUNDS __launch_bounds__(AGENT_THREADS, COVGPU_AGENT_MIN_BLOCKS)
@@ -57,17 +58,73 @@ constexpr int IMPORT_BLOCKS = 4;       // k_import_day grid (a day imports a han
 // ============================================================ fused agent pass
 
 
-// full_imm: also store sev_imm (read only by infect(), which recomputes it for the
-// agents it infects; stored on the last day of a launch sequence, so that the
-// state a caller reads afterwards holds the reference's array)
-__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm) {
-  if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
-    const int h = *st.hold;
-    if (h <= t - 1) return;
-    if (h <= t) do_day = 0;
-    if (!do_prev && !do_day) return;
+// One agent's inputs that (nearly) every agent needs: the state words, rel_sus, the
+// recovery date and the NAb fields, loaded one agent block ahead of its processing.
+struct AgentIn {
+  uint32_t f, vs;
+  float rs, dr, nab, peak;
+  int tne;
+};
+
+__device__ __forceinline__ AgentIn agent_load(const covgpu_state& st, int64_t i, bool valid, bool waning) {
+  AgentIn a{0u, 0xFFFFFFFFu, 0.0f, f32nan(), 0.0f, 0.0f, 0};
+  if (valid) {
+    a.f = st.flags[i];
+    a.vs = st.vstate[i];
+    a.rs = st.rel_sus[i];
+    a.dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
+    if (waning) {
+      a.nab = st.nab[i];
+      a.peak = st.peak_nab[i];
+      a.tne = st.t_nab_event[i];
+    }
   }
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+  return a;
+}
+
+// The block's counters: [0, N_RES_INT) day-t ints, then the day t-1 stocks, then
+// the variant slots [slot][v], and the warps' fixed-point sums.
+struct AgentCounters {
+  unsigned int cnt[COVGPU_N_RES_INT];  // day t flows + severe/critical now
+  unsigned int prev[N_STOCKS];         // day t-1 stocks
+  unsigned int var[COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS];
+  long long f[AGENT_THREADS / 32][3];
+};
+
+__device__ __forceinline__ void agent_counters_clear(AgentCounters& c) {
+  for (int k = threadIdx.x; k < COVGPU_N_RES_INT; k += blockDim.x) c.cnt[k] = 0;
+  for (int k = threadIdx.x; k < N_STOCKS; k += blockDim.x) c.prev[k] = 0;
+  for (int k = threadIdx.x; k < COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS; k += blockDim.x) c.var[k] = 0;
+}
+
+// Bits of an agent's day word (agent_block_step): the day's flows, the severe and
+// critical now, the variant of a new infectious agent (bit 16 + v) and the two
+// edge-pass roles, the last two stored as the role bitmaps' words.
+constexpr int DW_FLOWS = 9, DW_VAR = 16, DW_SRC = 30, DW_TGT = 31;
+// result slots of day-word bits 0-8, six bits each
+constexpr uint64_t FLOW_SLOTS =
+    (uint64_t)R_INFECTIOUS | (uint64_t)R_SYMPTOMATIC << 6 |
+    (uint64_t)R_SEVERE << 12 | (uint64_t)R_CRITICAL << 18 | (uint64_t)R_RECOVERIES << 24 |
+    (uint64_t)R_DEATHS << 30 | (uint64_t)R_KNOWN_DEATHS << 36 | (uint64_t)COVGPU_RES_SEVERE_NOW << 42 |
+    (uint64_t)COVGPU_RES_CRITICAL_NOW << 48;
+static_assert(COVGPU_N_RES_INT <= 64, "six-bit slots");
+static_assert(DW_VAR + COVGPU_MAX_VARIANTS <= DW_SRC, "day-word layout");
+
+// One agent block (up to 256 agents of one sim, thread k on agent begin + k):
+// closes day t-1 and runs day t's checks for its agents. Counts go to per-lane
+// accumulators: the agents' flag words (for the stocks) and day words (for the
+// flows) are bit-transposed across the warp, so lane b counts bit b
+// (acc_prev: flag bit b, acc_day: day-word bit b) with one popcount, and the
+// sums reach the block's counters once per agent_flush. Sums of levels go to the
+// thread's fixed-point sums (2^24 for NAbs, 2^32 for efficacies: exact integer
+// reductions, independent of order, and no float64 work per agent). full_imm: also store sev_imm (read only by infect(), which
+// recomputes it for the agents it infects; stored on the last day of a launch
+// sequence, so that the state a caller reads afterwards holds the reference's array).
+__device__ __forceinline__ void agent_block_step(const covgpu_state& st, const covgpu_agent_block& blk,
+                                                 const AgentIn& in, int t, int do_prev, int do_day, int full_imm,
+                                                 const float (*s_ln_tab)[2], const float (*s_exp_tab)[2],
+                                                 long long& nab_fx, long long& sus_fx, long long& symp_fx,
+                                                 unsigned& acc_prev, unsigned& acc_day) {
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const int nv = sp.n_variants;
   const int64_t i = blk.begin + threadIdx.x;
@@ -75,66 +132,17 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int tp = t - 1;
   const bool waning = sp.use_waning != 0;
-
-  // Every per-agent load the pass needs for (nearly) every agent, issued before the
-  // block's table copy and barrier so that their latencies overlap with it and with
-  // each other: the state words, rel_sus, the recovery date, the NAb fields.
-  uint32_t f = 0u, vs = 0xFFFFFFFFu;
-  float a_rs = 0.0f, a_dr = f32nan(), a_nab = 0.0f, a_peak = 0.0f;
-  int a_tne = 0;
-  if (valid) {
-    f = st.flags[i];
-    vs = st.vstate[i];
-    a_rs = st.rel_sus[i];
-    a_dr = date_row(st, COVGPU_DATE_RECOVERED)[i];
-    if (waning) {
-      a_nab = st.nab[i];
-      a_peak = st.peak_nab[i];
-      a_tne = st.t_nab_event[i];
-    }
-  }
-
-  // shared counters: [0, N_RES_INT) day-t ints, then prev-day stocks, then variant slots
-  __shared__ unsigned int s_cnt[COVGPU_N_RES_INT];           // day t flows + severe/critical now
-  __shared__ unsigned int s_prev[N_STOCKS];                   // day t-1 stocks
-  __shared__ unsigned int s_var[COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS];  // [slot][v]
-  __shared__ long long s_f[AGENT_THREADS / 32][3];
-  __shared__ float s_ln_tab[COVGPU_LN_N][2];
-  __shared__ float s_exp_tab[COVGPU_EXP_N][2];
-  for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
-  for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
-  for (int k = threadIdx.x; k < COVGPU_N_RES_INT; k += blockDim.x) s_cnt[k] = 0;
-  for (int k = threadIdx.x; k < N_STOCKS; k += blockDim.x) s_prev[k] = 0;
-  for (int k = threadIdx.x; k < COVGPU_N_RES_VAR * COVGPU_MAX_VARIANTS; k += blockDim.x) s_var[k] = 0;
-  if (do_day && blockIdx.x == 0 && threadIdx.x == 0) *st.event_count = 0ull;
-  __syncthreads();
-
+  uint32_t f = in.f, vs = in.vs;
+  const float a_rs = in.rs, a_dr = in.dr, a_nab = in.nab, a_peak = in.peak;
+  const int a_tne = in.tne;
   const uint32_t f_in = f, vs_in = vs;
   float nab_now = a_nab;  // the NAb level after the closing pass's update_nab
-  // reporting sums as fixed point (2^24 for NAbs, 2^32 for efficacies): exact integer
-  // reductions, independent of order, and no float64 work per agent
-  long long nab_fx = 0, sus_fx = 0, symp_fx = 0;
 
   // ---------------------------------------------------------- close day t-1
   if (do_prev) {
-    // sim.py:652-656: stocks at the end of day t-1. Warp counts by ballot: lane k
-    // keeps count k and adds it to the block's counter (one atomic per lane)
-    const uint32_t fv = valid ? f : 0u;
-    uint32_t mine = 0;
-#pragma unroll
-    for (int k = 0; k < N_STOCKS; ++k) {
-      const unsigned c = __popc(__ballot_sync(0xffffffffu, (fv & STOCK_BITS[k]) != 0u));
-      if (lane == k) mine = c;
-    }
-    if (mine) atomicAdd(&s_prev[lane], mine);
-    mine = 0;  // by variant: lane 2v exposed, lane 2v + 1 infectious
-    for (int v = 0; v < nv; ++v) {
-      const unsigned ce = __popc(__ballot_sync(0xffffffffu, (fv >> (EXPV_SHIFT + v)) & 1u));
-      const unsigned ci = __popc(__ballot_sync(0xffffffffu, (fv >> (INFV_SHIFT + v)) & 1u));
-      if (lane == 2 * v) mine = ce;
-      if (lane == 2 * v + 1) mine = ci;
-    }
-    if (mine) atomicAdd(&s_var[((lane & 1) ? RV_N_INFECTIOUS : RV_N_EXPOSED) * COVGPU_MAX_VARIANTS + (lane >> 1)], mine);
+    // sim.py:652-656: stocks at the end of day t-1, one flag bit each, and the
+    // exposed / infectious by variant (flag bits EXPV_SHIFT + v, INFV_SHIFT + v)
+    acc_prev += __popc(warp_transpose32(valid ? f : 0u));
     if (valid) {
       float nab = 0.0f;
       if (waning) {
@@ -150,7 +158,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
           nab_now = nab;
         }
       }
-      if (!(f & B_DEAD) && nab != 0.0f) nab_fx = __float2ll_rn(__fmul_rn(nab, 16777216.0f));  // sim.py:672
+      if (!(f & B_DEAD) && nab != 0.0f) nab_fx += __float2ll_rn(__fmul_rn(nab, 16777216.0f));  // sim.py:672
     }
   }
 
@@ -253,8 +261,10 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
           st.symp_imm[off] = b;
           if (full_imm) st.sev_imm[off] = c;
           if (is_tgt) st.tgt_rec[off] = __uint_as_float(__float_as_uint(__fmul_rn(rs, __fsub_rn(1.0f, a))) | tq);
-          sus_fx += __float2ll_rn(__fmul_rn(a, 4294967296.0f));
-          symp_fx += __float2ll_rn(__fmul_rn(b, 4294967296.0f));
+          if (a != 0.0f || b != 0.0f) {
+            sus_fx += __float2ll_rn(__fmul_rn(a, 4294967296.0f));
+            symp_fx += __float2ll_rn(__fmul_rn(b, 4294967296.0f));
+          }
         }
       }
 
@@ -282,44 +292,54 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       if (f != f_in) st.flags[i] = f;
       if (vs != vs_in) st.vstate[i] = vs;
     }
-    // flows (people.py:172-180) and the severe/critical counts of sim.py:579-580,
-    // counted by ballot as the stocks are; lane k adds count k to its slot
-    const unsigned cv[9] = {c_inf, c_symp, c_sev, c_crit, c_rec, c_dead, c_kdead,
-                            (valid && (f & B_SEV)) ? 1u : 0u, (valid && (f & B_CRIT)) ? 1u : 0u};
-    // the slots of the nine counts, six bits each
-    constexpr uint64_t FLOW_SLOTS =
-        (uint64_t)R_INFECTIOUS | (uint64_t)R_SYMPTOMATIC << 6 |
-        (uint64_t)R_SEVERE << 12 | (uint64_t)R_CRITICAL << 18 | (uint64_t)R_RECOVERIES << 24 |
-        (uint64_t)R_DEATHS << 30 | (uint64_t)R_KNOWN_DEATHS << 36 | (uint64_t)COVGPU_RES_SEVERE_NOW << 42 |
-        (uint64_t)COVGPU_RES_CRITICAL_NOW << 48;
-    static_assert(COVGPU_N_RES_INT <= 64, "six-bit slots");
-    uint32_t mine = 0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const unsigned c = __popc(__ballot_sync(0xffffffffu, cv[k] != 0u));
-      if (lane == k) mine = c;
-    }
-    if (mine) atomicAdd(&s_cnt[(FLOW_SLOTS >> (6 * (lane % 10))) & 63u], mine);  // lanes 0-8
-    mine = 0;
-    for (int v = 0; v < nv; ++v) {
-      const unsigned c = __popc(__ballot_sync(0xffffffffu, inf_v == v));
-      if (lane == v) mine = c;
-    }
-    if (mine) atomicAdd(&s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + lane], mine);
-    // role bitmaps: warp w of this block covers the 32-aligned word (i - lane) / 32
-    const uint32_t sm = __ballot_sync(0xffffffffu, src_bit), tm = __ballot_sync(0xffffffffu, tgt_bit);
-    if (lane == 0 && blk.begin + warp * 32 < blk.end) {
+    // flows (people.py:172-180), the severe/critical counts of sim.py:579-580, the
+    // new infectious by variant and the roles, one bit each of the day word;
+    // transposed, lanes 30 and 31 hold the role bitmaps' words of this warp's 32
+    // agents (the 32-aligned word (i - lane) / 32)
+    const uint32_t dw = valid ? (c_inf | c_symp << 1 | c_sev << 2 | c_crit << 3 | c_rec << 4 | c_dead << 5 |
+                                 c_kdead << 6 | ((f & B_SEV) ? 1u << 7 : 0u) | ((f & B_CRIT) ? 1u << 8 : 0u) |
+                                 (inf_v >= 0 ? 1u << (DW_VAR + inf_v) : 0u) | src_bit << DW_SRC |
+                                 tgt_bit << DW_TGT)
+                              : 0u;
+    const uint32_t col = warp_transpose32(dw);
+    if (lane < DW_SRC) {
+      acc_day += __popc(col);
+    } else if (blk.begin + warp * 32 < blk.end) {
       const int64_t w = (blk.begin + warp * 32) >> 5;
-      st.roles[w] = sm;                        // source bitmap
-      st.roles[roles_words(st) + w] = tm;      // target bitmap
+      st.roles[(lane == DW_SRC ? 0 : roles_words(st)) + w] = col;  // source / target bitmap
     }
   }
+}
 
-  // ---------------------------------------------------------- block totals
+// Adds the block's counters and fixed-point sums of sim `sim` to its results:
+// integer atomics, bit-reproducible. With `clear` the counters restart at zero
+// for the next sim's agent blocks.
+__device__ __noinline__ void agent_flush(const covgpu_state& st, int sim, int t, int do_prev, int do_day,
+                                         AgentCounters& sc, long long& nab_fx, long long& sus_fx, long long& symp_fx,
+                                         unsigned& acc_prev, unsigned& acc_day, bool clear) {
+  const covgpu_sim_params& sp = st.sims[sim];
+  const int nv = sp.n_variants;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int tp = t - 1;
+  unsigned int* s_cnt = sc.cnt;
+  unsigned int* s_prev = sc.prev;
+  unsigned int* s_var = sc.var;
   nab_fx = warp_sum_fx(nab_fx);
   sus_fx = warp_sum_fx(sus_fx);
   symp_fx = warp_sum_fx(symp_fx);
-  if (lane == 0) { s_f[warp][0] = nab_fx; s_f[warp][1] = sus_fx; s_f[warp][2] = symp_fx; }
+  if (lane == 0) { sc.f[warp][0] = nab_fx; sc.f[warp][1] = sus_fx; sc.f[warp][2] = symp_fx; }
+  if (acc_prev) {  // lane b: flag bit b
+    if (lane >= INFV_SHIFT) atomicAdd(&s_var[RV_N_INFECTIOUS * COVGPU_MAX_VARIANTS + lane - INFV_SHIFT], acc_prev);
+    else if (lane >= EXPV_SHIFT) atomicAdd(&s_var[RV_N_EXPOSED * COVGPU_MAX_VARIANTS + lane - EXPV_SHIFT], acc_prev);
+    else
+      for (int k = 0; k < N_STOCKS; ++k)
+        if (STOCK_BITS[k] == 1u << lane) atomicAdd(&s_prev[k], acc_prev);
+  }
+  if (acc_day) {  // lane b: day-word bit b
+    if (lane >= DW_VAR) atomicAdd(&s_var[RV_INFECTIOUS * COVGPU_MAX_VARIANTS + lane - DW_VAR], acc_day);
+    else if (lane < DW_FLOWS) atomicAdd(&s_cnt[(FLOW_SLOTS >> (6 * lane)) & 63u], acc_day);
+  }
+  acc_prev = acc_day = 0;
   __syncthreads();
   const int npts = sp.npts;
   int64_t* res_t = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
@@ -346,7 +366,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   // block totals of the fixed-point sums, added with integer atomics (bit-reproducible)
   if (threadIdx.x == 0) {
     long long a = 0, b = 0, c = 0;
-    for (int w = 0; w < AGENT_THREADS / 32; ++w) { a += s_f[w][0]; b += s_f[w][1]; c += s_f[w][2]; }
+    for (int w = 0; w < AGENT_THREADS / 32; ++w) { a += sc.f[w][0]; b += sc.f[w][1]; c += sc.f[w][2]; }
     if (do_prev && tp >= 0 && a != 0)
       atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_fx[(int64_t)tp * COVGPU_N_RES_F + 0]),
                 (unsigned long long)a);
@@ -357,6 +377,69 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
                 (unsigned long long)c);
     }
   }
+  nab_fx = sus_fx = symp_fx = 0;
+  if (clear) {
+    __syncthreads();
+    agent_counters_clear(sc);
+    __syncthreads();
+  }
+}
+
+// The fused agent pass. It runs as (at most) one wave of resident blocks, each
+// walking a contiguous range of agent blocks: the next agent block's loads are in
+// flight while the current one is processed, no barrier separates agent blocks of
+// one sim, and the counters go to the results once per sim a block touched
+// instead of once per 256 agents.
+__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm) {
+  if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
+    const int h = *st.hold;
+    if (h <= t - 1) return;
+    if (h <= t) do_day = 0;
+    if (!do_prev && !do_day) return;
+  }
+  if (do_day && blockIdx.x == 0 && threadIdx.x == 0) *st.event_count = 0ull;
+  const int64_t nb = st.n_agent_blocks;
+  const int64_t per = (nb + gridDim.x - 1) / gridDim.x;
+  int64_t b = (int64_t)blockIdx.x * per;
+  const int64_t b_end = min(nb, b + per);
+  if (b >= b_end) return;  // block-uniform
+
+  covgpu_agent_block blk = st.agent_blocks[b];
+  int sim = blk.sim;
+  AgentIn cur = agent_load(st, blk.begin + threadIdx.x, blk.begin + threadIdx.x < blk.end,
+                           st.sims[sim].use_waning != 0);
+
+  __shared__ AgentCounters sc;
+  __shared__ float s_ln_tab[COVGPU_LN_N][2];
+  __shared__ float s_exp_tab[COVGPU_EXP_N][2];
+  for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
+  for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
+  agent_counters_clear(sc);
+  __syncthreads();
+
+  long long nab_fx = 0, sus_fx = 0, symp_fx = 0;
+  unsigned acc_prev = 0, acc_day = 0;
+  for (;;) {
+    const bool more = b + 1 < b_end;
+    covgpu_agent_block nblk = blk;
+    AgentIn nxt = cur;
+    if (more) {
+      nblk = st.agent_blocks[b + 1];
+      const int64_t ni = nblk.begin + threadIdx.x;
+      nxt = agent_load(st, ni, ni < nblk.end, st.sims[nblk.sim].use_waning != 0);
+    }
+    agent_block_step(st, blk, cur, t, do_prev, do_day, full_imm, s_ln_tab, s_exp_tab, nab_fx, sus_fx, symp_fx,
+                     acc_prev, acc_day);
+    if (!more) break;
+    ++b;
+    if (nblk.sim != sim) {
+      agent_flush(st, sim, t, do_prev, do_day, sc, nab_fx, sus_fx, symp_fx, acc_prev, acc_day, true);
+      sim = nblk.sim;
+    }
+    blk = nblk;
+    cur = nxt;
+  }
+  agent_flush(st, sim, t, do_prev, do_day, sc, nab_fx, sus_fx, symp_fx, acc_prev, acc_day, false);
 }
 
 // ============================================================ fused edge pass
@@ -1681,10 +1764,28 @@ GraphEntry g_graphs[N_GRAPHS];
 int g_graph_next = 0;
 cudaStream_t g_capture_stream = nullptr;  // private stream for captures (the legacy stream cannot capture)
 
+// Grid of the agent pass: one wave of resident blocks (the SM count of the current
+// device times the blocks per SM the pass's registers allow), or fewer when the
+// state has fewer agent blocks. Any grid gives the same results.
+unsigned agent_grid(const covgpu_state* st) {
+  static const int64_t wave = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_agent_step, AGENT_THREADS, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return (int64_t)1 << 30;  // no wave bound: one block per agent block
+    }
+    return (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  }();
+  const int64_t nb = st->n_agent_blocks;
+  return (unsigned)(nb < wave ? (nb > 0 ? nb : 1) : wave);
+}
+
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     if (st->hold) k_rescale_check<<<1, 128, 0, s>>>(*st, t);
-    k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1,
+    k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1,
                                                                         t == t1 - 1 ? 1 : 0);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
@@ -1693,7 +1794,7 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
     launch_lik_targets(st, t, s);
     k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
   }
-  if (close_last) k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t1, 1, 0, 0);
+  if (close_last) k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, s>>>(*st, t1, 1, 0, 0);
   return launch_status();
 }
 
@@ -1755,7 +1856,7 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  k_agent_step<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day, 1);
+  k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day, 1);
   return launch_status();
 }
 

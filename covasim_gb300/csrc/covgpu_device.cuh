@@ -159,6 +159,23 @@ __device__ __forceinline__ uint4 dyn_hit_block(uint32_t a, int d, int j, uint32_
   return philox(make_uint4(a, ((uint32_t)d << 8) + ((uint32_t)j >> 2), day, TAG_DYN_HIT | layer), k0, k1);
 }
 
+// 32 x 32 bit-matrix transpose across a warp (row j = lane j's x): bit j of lane
+// k's result is bit k of lane j's x, so lane k holds the ballot of bit k and its
+// popcount counts the lanes with bit k set. Five exchange stages, each swapping
+// the off-diagonal blocks of half the previous size. All 32 lanes call it.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int s = 16 >> k;
+    const uint32_t m = k == 0 ? 0x0000FFFFu : k == 1 ? 0x00FF00FFu : k == 2 ? 0x0F0F0F0Fu
+                     : k == 3 ? 0x33333333u : 0x55555555u;  // the bits b with (b & s) == 0
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+    x = (lane & s) ? ((x & ~m) | ((y >> s) & m)) : ((x & m) | ((y & m) << s));
+  }
+  return x;
+}
+
 // The set bits of one agent block's bitmap words, handed to the lanes 32 at a
 // time: lanes 0..nw-1 hold the words (nw warp-uniform, <= 32), warp_bits_scan
 // forms their exclusive prefix counts, and warp_bits_nth gives the lane whose
