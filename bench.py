@@ -44,7 +44,13 @@ PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
 # the launch list of a whole ungraphed run gives the kernels' shares): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum) per launch and the share of
 # cycles the schedulers issued (smsp__issue_active), per kernel.
-MEASURED_NCU = {}
+MEASURED_NCU = {
+    ('agent_step', 1_000_000): {
+        'dram_bytes': 61_234_688, 'issue_active': 0.675, 'bound': 'issue',
+        'note': 'ncu section capture, day 85 of the 1M-agent run: 61.2 MB of DRAM '
+                'traffic against 88 MB algorithmic; instruction issue 67.5% busy with 1.8 eligible warps per '
+                'scheduler, so the pass is issue-bound, not HBM-bound'},
+}
 
 
 def parse():
@@ -65,6 +71,9 @@ def parse():
                     help='skip the 256-sim batched measurement (batched vs one by one) in the default line')
     ap.add_argument('--edge-tile', default='auto',
                     help="edge-pass tile (1024/2048/4096/8192, suffix 'r' for the resident bitmap) or 'auto' (autotuner)")
+    ap.add_argument('--src-walk', type=int, default=None,
+                    help='walk of the stored layers from the day\'s sources: k walks while infectious x k < agents, '
+                         '0 never, -1 always (default: the library\'s)')
     ap.add_argument('--seeds', type=int, default=1,
                     help='large workload: this many seeds of the 20M-agent sim in one BatchSim')
     ap.add_argument('--gpu-population', action='store_true',
@@ -283,6 +292,8 @@ def gpu_arm(args, world, rank):
     init_s = time.perf_counter() - t0
     st = sim.state
     npts = sim.npts
+    if args.src_walk is not None:
+        st.set_src_walk(args.src_walk)
     tile_ms = None
     if args.edge_tile == 'auto':  # before the snapshot: tuning leaves the state rewound
         from covasim_gb300.autotune import tune_edge_tile
@@ -653,6 +664,8 @@ def large_arm(args, n=20_000_000, days=365, steps=None, warmup=None, gpu_populat
         sims = [cv.Sim(dict(pars, rand_seed=1 + k), gpu_population=gpu_population) for k in range(seeds)]
         batch = cv.BatchSim(sims, edge_tile=tile).initialize()
         sim, st = sims[0], batch.state
+    if args.src_walk is not None:
+        st.set_src_walk(args.src_walk)
     init_s = time.perf_counter() - t0
     snap = st.snapshot()
 
@@ -800,6 +813,9 @@ def profile_run(args):
         st.zero_lik()
     else:
         sim = cv.Sim(pars, edge_tile=None if args.edge_tile == 'auto' else args.edge_tile)
+        sim.initialize()
+    if args.src_walk is not None:
+        sim.state.set_src_walk(args.src_walk)
     sim.run(use_graph=False)
     torch.cuda.synchronize()
     print(json.dumps({'profile_run': True, 'pop_size': args.pop_size, 'days': args.days,

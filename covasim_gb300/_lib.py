@@ -135,7 +135,7 @@ class State(C.Structure):
         ('sims', C.c_void_p), ('segments', C.c_void_p), ('agent_blocks', C.c_void_p),
         ('draw_table', C.c_void_p), ('edge_uniforms', C.c_void_p),
         ('has_testing', C.c_int32), ('pending_slots', C.c_int32), ('trace_bits', C.c_void_p),
-        ('contact_bits', C.c_void_p), ('n_contact_layers', C.c_int32), ('_pad1', C.c_int32),
+        ('contact_bits', C.c_void_p), ('n_contact_layers', C.c_int32), ('src_walk', C.c_int32),
         ('pending_quar', C.c_void_p), ('trace_count', C.c_void_p),
         ('lik', Lik),
         ('import_day_off', C.c_void_p), ('imports', C.c_void_p), ('import_sims', C.c_void_p),

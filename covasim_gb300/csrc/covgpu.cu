@@ -240,7 +240,13 @@ __device__ __forceinline__ void agent_block_step(const covgpu_state& st, const c
       const float rs = (f & B_SUS) ? a_rs : 0.0f;
       const bool is_tgt = rs != 0.0f;
       const uint32_t tq = (f & B_QUAR) ? 0x80000000u : 0u;
-      if (waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
+      if (waning && a_peak == 0.0f && nab_now == 0.0f) {
+        // an agent that never had NAbs: every efficacy is 0, as the state has held
+        // them since initialisation (nothing to store; infect() reads symp_imm as 0
+        // for it, symp_imm_of), and the target record is rel_sus itself
+        if (is_tgt)
+          for (int v = 0; v < nv; ++v) st.tgt_rec[(int64_t)v * st.n + i] = __uint_as_float(__float_as_uint(rs) | tq);
+      } else if (waning) {  // check_immunity, immunity.py:303-350 (float-float, one rounding)
         const bool was_inf = tf >= a_dr;  // false for NaN
         const float nab = nab_now;
         ff ln_nab = ff{0.0f, 0.0f};
@@ -789,7 +795,28 @@ __device__ __forceinline__ void lik_flush_warp(const covgpu_state& st, int t, in
   acc = LikAcc();
 }
 
-// One block per tile.
+// Stored layers on quiet days. A stored layer segment with an agent index (rp1,
+// rp2, perm2: each agent's edges as p1 and as p2) is walked from the day's
+// sources (k_src_pass) instead of streamed edge by edge (the tile passes) while
+// its sim's infectious agents times st.src_walk are fewer than its agents (0:
+// never, -1: always): the number infectious at the end of day t-1 plus day t's
+// new infectious, less its recoveries and deaths, from the results the agent
+// pass of day t has written. The walk visits each source's edges (about 2 E x
+// prevalence entries, each a few dependent loads) where the tile pass tests both
+// endpoints of all E edges. Both queue the same candidates and draw, key and
+// claim them alike, so the choice moves only the cost.
+__device__ __forceinline__ bool seg_walked(const covgpu_state& st, const covgpu_layer& L, int t) {
+  if (L.dynamic || !L.rp1 || st.src_walk == 0) return false;
+  if (st.src_walk < 0) return true;
+  const covgpu_sim_params& sp = st.sims[L.sim];
+  if (t < 0 || t >= sp.npts) return false;
+  const int64_t* r = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
+  int64_t inf = r[R_INFECTIOUS] - r[R_RECOVERIES] - r[R_DEATHS];
+  if (t > 0) inf += (r - COVGPU_N_RES_INT)[R_N_FIRST + 2];  // n_infectious, end of day t-1
+  return inf * (int64_t)st.src_walk < sp.n_agents;
+}
+
+// One block per tile (none for a segment walked from its sources today).
 template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
   if (held(st, t)) return;
@@ -805,6 +832,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
     load_sim_lite(s_sp, st.sims[s_L.sim]);
   }
   __syncthreads();
+  if (seg_walked(st, s_L, t)) return;  // block-uniform
   LikAcc acc;
   edge_tile<LIK, EDGE_THREADS, TILE, false>(st, t, s_seg, (int64_t)blockIdx.x, &s_L, &s_sp, nullptr,
                                             s_q[threadIdx.x >> 5], acc);
@@ -840,11 +868,20 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
   uint32_t* s_src = reinterpret_cast<uint32_t*>(s_dyn);
   const int64_t words = (st.n + 31) >> 5;
   const int n_segs = st.n_segments;
+  __shared__ uint32_t s_walk;  // bit k: segment k is walked from its sources today
+  if (threadIdx.x < n_segs) s_segs[threadIdx.x] = st.segments[threadIdx.x];
+  if (threadIdx.x == 0) s_walk = 0u;
+  __syncthreads();
+  if (threadIdx.x < n_segs && seg_walked(st, s_segs[threadIdx.x], t)) atomicOr(&s_walk, 1u << threadIdx.x);
+  __syncthreads();
+  uint32_t streamed = 0u;  // the stored segments left to this pass
+  for (int k = 0; k < n_segs; ++k)
+    if (!s_segs[k].dynamic && !((s_walk >> k) & 1u)) streamed |= 1u << k;
+  if (!streamed) return;  // block-uniform
   // bitmap words four at a time (the bitmap has room for whole uint4s)
   const uint4* g4 = reinterpret_cast<const uint4*>(st.roles);
   for (int64_t k = threadIdx.x; k < (words >> 2); k += RES_THREADS) s_dyn[k] = __ldg(g4 + k);
   for (int64_t k = (words & ~3ll) + threadIdx.x; k < words; k += RES_THREADS) s_src[k] = __ldg(st.roles + k);
-  if (threadIdx.x < n_segs) s_segs[threadIdx.x] = st.segments[threadIdx.x];
   if (threadIdx.x == 0) load_sim_lite(s_sp, st.sims[0]);
   EdgeQueue* s_q = reinterpret_cast<EdgeQueue*>(s_dyn + ((words + 3) >> 2));
   EdgeQueue& q = s_q[threadIdx.x >> 5];
@@ -852,6 +889,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
   LikAcc acc;
   for (int64_t tile = blockIdx.x; tile < st.n_tiles; tile += gridDim.x) {
     const int seg = segment_of_tile(s_segs, n_segs, tile);
+    if (!((streamed >> seg) & 1u)) continue;
     edge_tile<LIK, RES_THREADS, TILE, true>(st, t, seg, tile, s_segs + seg, &s_sp, s_src, q, acc);
     if (LIK) lik_flush_warp(st, t, s_segs[seg].sim, s_segs[seg].layer, acc);
   }
@@ -862,14 +900,16 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
 // Transmission over the dynamic layers (base.py:1849-1876 redrawn daily, then
 // utils.py:93-128): one warp per four source-bitmap words (128 agents of one
 // sim). The words' sources are handed to the lanes 32 at a time; for each
-// dynamic layer of the sim every lane draws its source's two contact lists
-// (covgpu_device.cuh, "redrawn layers, per agent") four partners per Philox
-// block, both lists side by side so that eight target-bitmap loads are in
-// flight, and queues the partners that are targets; the queue drains through
-// edge_try as the stored layers' does. The work follows the day's sources, not
-// the layer's edges: a quiet day costs a read of the source bitmap. Entries are
-// thinned (covgpu_device.cuh "Thinning"): only the potential transmissions, about
-// pmax of them, have their partner drawn and are queued.
+// dynamic layer of the sim every lane draws its source's two list lengths
+// (covgpu_device.cuh, "redrawn layers, per agent"), and the lists' four-entry
+// blocks of all 32 sources are then spread over the lanes (a prefix count and a
+// search for each block's source), so that the Philox blocks of a warp with few
+// sources still run on full lanes. Entries are thinned (covgpu_device.cuh
+// "Thinning"): only the potential transmissions, about pmax of them, have their
+// partner drawn, and those whose partner is a target are queued; the queue
+// drains through edge_try as the stored layers' does. The work follows the
+// day's sources, not the layer's edges: a quiet day costs a read of the source
+// bitmap.
 constexpr int DYN_WARPS = 8;  // warps per thread block
 constexpr int DYN_WORDS = 4;  // source-bitmap words per warp (an agent block's eight words: two warps)
 
@@ -937,7 +977,9 @@ __device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& 
 }
 
 template <bool LIK>
-__global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st, int t) {
+// four resident blocks per SM (64 registers): the pass over a 100-day 1M-agent run
+// took 2.70 ms of kernel time against 2.89 ms with three (80 registers)
+__global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st, int t) {
   if (held(st, t)) return;
   __shared__ EdgeQueue s_q[DYN_WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -969,48 +1011,69 @@ __global__ void __launch_bounds__(DYN_WARPS * 32, 3) k_dyn_pass(covgpu_state st,
       int bit;
       const int wl = warp_bits_nth(wb, nw, idx, bit);
       const int32_t s = (int32_t)((w0 + wl) * 32 + bit);
-      const uint32_t a = (uint32_t)(s - off);
-      int k[2] = {0, 0}, m = -1;
+      int k0 = 0, k1 = 0, m = -1;
       if (idx < wb.total) {
         m = dyn_shift(st, c, s);
-        if (m >= 0 || LIK) dyn_counts(c.L->dyn_cdf, c.L->dyn_k, a, day, (uint32_t)l, c.key0, c.key1, k[0], k[1]);
+        if (m >= 0 || LIK) dyn_counts(c.L->dyn_cdf, c.L->dyn_k, (uint32_t)(s - off), day, (uint32_t)l, c.key0, c.key1, k0, k1);
       }
-      for (int d = 0; d < 2; ++d) {
-        const int kd = k[d];
-        const int nq_max = (int)__reduce_max_sync(0xffffffffu, (unsigned)((kd + 3) >> 2));
-        for (int qd = 0; qd < nq_max; ++qd) {
-          const int j0 = 4 * qd;
-          // potential transmissions among entries j0 .. j0 + 3 (one Philox block)
-          uint32_t pm = 0u;
-          if (j0 < kd && m >= 0) {
-            const uint4 hw = dyn_hit_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
+      // the lanes' four-entry blocks of both lists (one Philox block of potential
+      // transmissions each), flattened across the warp: item j belongs to the
+      // first lane whose inclusive prefix count exceeds j
+      const uint32_t nb0 = (uint32_t)(k0 + 3) >> 2, nb = nb0 + ((uint32_t)(k1 + 3) >> 2);
+      uint32_t pre = nb;
 #pragma unroll
-            for (int r = 0; r < 4; ++r)
-              if (j0 + r < kd && thin_potential(word_of(hw, r), m)) pm |= 1u << r;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += y;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+      for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+        const uint32_t j = j0 + (uint32_t)lane;
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (__shfl_sync(0xffffffffu, pre, owner + step - 1) <= j) owner += step;
+        const int32_t os = __shfl_sync(0xffffffffu, s, owner);
+        const int om = __shfl_sync(0xffffffffu, m, owner);
+        const int ok0 = __shfl_sync(0xffffffffu, k0, owner), ok1 = __shfl_sync(0xffffffffu, k1, owner);
+        const uint32_t onb0 = __shfl_sync(0xffffffffu, nb0, owner);
+        const uint32_t obeg = __shfl_sync(0xffffffffu, pre - nb, owner);
+        uint32_t pm = 0u, tb = 0u;
+        int d = 0, je = 0;
+        int32_t g[4] = {0, 0, 0, 0};
+        if (j < total) {
+          const uint32_t r = j - obeg;
+          d = r >= onb0 ? 1 : 0;
+          je = 4 * (int)(d ? r - onb0 : r);
+          const int kd = d ? ok1 : ok0;
+          const uint32_t oa = (uint32_t)(os - off);
+          if (om >= 0) {  // potential transmissions among entries je .. je + 3
+            const uint4 hw = dyn_hit_block(oa, d, je, day, (uint32_t)l, c.key0, c.key1);
+#pragma unroll
+            for (int r4 = 0; r4 < 4; ++r4)
+              if (je + r4 < kd && thin_potential(word_of(hw, r4), om)) pm |= 1u << r4;
           }
           // partners: of the potential entries (all entries for the likelihood)
-          const uint32_t want = LIK ? (j0 < kd ? (0xFu >> max(0, 4 - (kd - j0))) : 0u) : pm;
-          if (!__any_sync(0xffffffffu, want != 0u)) continue;
-          int32_t g[4] = {0, 0, 0, 0};
-          uint32_t tb = 0u;
+          const uint32_t want = LIK ? (0xFu >> max(0, 4 - (kd - je))) : pm;
           if (want) {
-            const uint4 pw = dyn_partner_block(a, d, j0, day, (uint32_t)l, c.key0, c.key1);
+            const uint4 pw = dyn_partner_block(oa, d, je, day, (uint32_t)l, c.key0, c.key1);
 #pragma unroll
-            for (int r = 0; r < 4; ++r)
-              if ((want >> r) & 1u) {
-                g[r] = off + (int32_t)dyn_partner(word_of(pw, r), n_local, thr, a, d, j0 + r, day, (uint32_t)l,
-                                                  c.key0, c.key1);
-                tb |= tgt_bit(st, g[r]) << r;
+            for (int r4 = 0; r4 < 4; ++r4)
+              if ((want >> r4) & 1u) {
+                g[r4] = off + (int32_t)dyn_partner(word_of(pw, r4), n_local, thr, oa, d, je + r4, day, (uint32_t)l,
+                                                   c.key0, c.key1);
+                tb |= tgt_bit(st, g[r4]) << r4;
               }
           }
+        }
+        if (!__any_sync(0xffffffffu, tb != 0u)) continue;
 #pragma unroll
-          for (int r = 0; r < 4; ++r)
-            queue_push(q, qn, (tb >> r) & 1u, s, g[r],
-                       ((uint32_t)(j0 + r) << 2) | (((pm >> r) & 1u) << 1) | (uint32_t)d);
-          if (qn > EQ_CAP - 4 * 32) {
-            dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
-            qn = 0;
-          }
+        for (int r4 = 0; r4 < 4; ++r4)
+          queue_push(q, qn, (tb >> r4) & 1u, os, g[r4],
+                     ((uint32_t)(je + r4) << 2) | (((pm >> r4) & 1u) << 1) | (uint32_t)d);
+        if (qn > EQ_CAP - 4 * 32) {
+          dyn_drain<LIK>(st, c, t, sp.agent_off, q, qn, acc);
+          qn = 0;
         }
       }
     }
@@ -1024,6 +1087,157 @@ int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s) {
   const unsigned grid = (unsigned)((2 * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
   if (st->lik.factor) k_dyn_pass<true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
   else k_dyn_pass<false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
+  return launch_status();
+}
+
+// The walk of the stored layers from the day's sources (seg_walked): one warp per
+// four source-bitmap words, as the redrawn layers' pass. For each indexed stored
+// layer the warp's sources' edges (as p1: [rp1[a], rp1[a + 1]); as p2: the edges
+// perm2[rp2[a] .. rp2[a + 1])) are flattened across the lanes 32 at a time, each
+// lane finding its source by a search over the lanes' prefix counts; an edge whose
+// other endpoint is a target is queued with its index and direction (1: the
+// source is p2, as in the tile pass) and drained through edge_try.
+constexpr int SRC_WARPS = 8;
+struct SrcQueue {
+  int32_t s[EQ_CAP];   // source agent
+  int32_t g[EQ_CAP];   // target agent | direction << 31
+  uint32_t e[EQ_CAP];  // edge index in the layer
+};
+
+__device__ __forceinline__ void src_push(SrcQueue& q, int& qn, bool has, int32_t s, int32_t gd, uint32_t e) {
+  const unsigned mask = __ballot_sync(0xffffffffu, has);
+  if (has) {
+    const int pos = qn + __popc(mask & ((1u << (threadIdx.x & 31)) - 1u));
+    q.s[pos] = s; q.g[pos] = gd; q.e[pos] = e;
+  }
+  qn += __popc(mask);
+}
+
+template <bool LIK>
+__device__ __forceinline__ void src_drain(const covgpu_state& st, const SegCtx& c, int t, SrcQueue& q, int qn,
+                                          LikAcc& acc) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < qn; base += 32) {
+    const int i = base + lane;
+    bool hit = false;
+    uint32_t v = 0;
+    int32_t s = 0, g = 0;
+    int d = 0;
+    int64_t e = 0;
+    if (i < qn) {
+      s = q.s[i];
+      const uint32_t gd = (uint32_t)q.g[i];
+      g = (int32_t)(gd & 0x7FFFFFFFu);
+      d = (int)(gd >> 31);
+      e = (int64_t)q.e[i];
+      hit = edge_try<LIK>(st, c, t, e, d, s, g, v, acc);
+    }
+    emit(st, hit, hit ? event_key(t, v, c.layer, d, e) : 0ull, g, s);
+  }
+  __syncwarp();
+}
+
+template <bool LIK>
+__global__ void __launch_bounds__(SRC_WARPS * 32) k_src_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  __shared__ SrcQueue s_q[SRC_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * SRC_WARPS + warp;
+  const int64_t b = gw >> 1;  // two warps per agent block
+  if (b >= st.n_agent_blocks) return;  // warp-uniform
+  const covgpu_agent_block blk = st.agent_blocks[b];
+  const covgpu_sim_params& sp = st.sims[blk.sim];
+  int first = -1;  // the sim's first walked layer
+  for (int l = 0; l < sp.n_layers && first < 0; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg >= 0 && seg_walked(st, st.segments[seg], t)) first = l;
+  }
+  if (first < 0) return;
+  const int w_lo = (int)(gw & 1) * DYN_WORDS;
+  const int nwb = (int)((blk.end - blk.begin + 31) >> 5);
+  if (w_lo >= nwb) return;
+  const int nw = min(DYN_WORDS, nwb - w_lo);
+  const int64_t w0 = (blk.begin >> 5) + w_lo;  // sims start at multiples of 32
+  const WarpBits wb = warp_bits_scan(lane < nw ? __ldg(st.roles + w0 + lane) : 0u);
+  if (wb.total == 0) return;
+  const int32_t off = (int32_t)sp.agent_off;
+  SrcQueue& q = s_q[warp];
+  LikAcc acc;
+  for (int l = first; l < sp.n_layers; ++l) {
+    const int seg = sp.seg_of_layer[l];
+    if (seg < 0) continue;
+    const covgpu_layer& L = st.segments[seg];
+    if (!seg_walked(st, L, t)) continue;
+    SegCtx c;
+    dyn_ctx(st, sp, seg, t, c);
+    c.edge_beta = L.beta;
+    const int32_t* p1 = L.p1;
+    const int32_t* p2 = L.p2;
+    int qn = 0;
+    for (int base = 0; base < wb.total; base += 32) {
+      const int idx = base + lane;
+      int bit;
+      const int wl = warp_bits_nth(wb, nw, idx, bit);
+      const int32_t s = (int32_t)((w0 + wl) * 32 + bit);
+      uint32_t k1 = 0, n1 = 0, k2 = 0, n = 0;
+      if (idx < wb.total) {
+        const uint32_t a = (uint32_t)(s - off);
+        k1 = __ldg(L.rp1 + a);
+        n1 = __ldg(L.rp1 + a + 1) - k1;
+        k2 = __ldg(L.rp2 + a);
+        n = n1 + (__ldg(L.rp2 + a + 1) - k2);
+      }
+      uint32_t pre = n;  // inclusive prefix of the lanes' entry counts
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += y;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+      for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+        const uint32_t j = j0 + (uint32_t)lane;
+        int owner = 0;  // the first lane whose inclusive prefix exceeds j
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (__shfl_sync(0xffffffffu, pre, owner + step - 1) <= j) owner += step;
+        owner = min(owner, 31);
+        const int32_t os = __shfl_sync(0xffffffffu, s, owner);
+        const uint32_t ok1 = __shfl_sync(0xffffffffu, k1, owner), on1 = __shfl_sync(0xffffffffu, n1, owner);
+        const uint32_t ok2 = __shfl_sync(0xffffffffu, k2, owner);
+        const uint32_t obeg = __shfl_sync(0xffffffffu, pre - n, owner);
+        bool has = false;
+        int32_t g = 0;
+        uint32_t e = 0, d = 0;
+        if (j < total) {
+          const uint32_t r = j - obeg;
+          if (r < on1) {
+            e = ok1 + r;
+            g = __ldg(p2 + e);
+          } else {
+            e = __ldg(L.perm2 + ok2 + (r - on1));
+            g = __ldg(p1 + e);
+            d = 1u;
+          }
+          has = tgt_bit(st, g) != 0u;
+        }
+        src_push(q, qn, has, os, (int32_t)((uint32_t)g | (d << 31)), e);
+        if (qn > EQ_CAP - 32) {
+          src_drain<LIK>(st, c, t, q, qn, acc);
+          qn = 0;
+        }
+      }
+    }
+    if (qn > 0) src_drain<LIK>(st, c, t, q, qn, acc);
+    if (LIK) lik_flush_warp(st, t, blk.sim, l, acc);
+  }
+}
+
+int launch_src_pass(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->n_tiles == 0 || st->src_walk == 0) return COVGPU_OK;
+  const unsigned grid = (unsigned)((2 * st->n_agent_blocks + SRC_WARPS - 1) / SRC_WARPS);
+  if (st->lik.factor) k_src_pass<true><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
+  else k_src_pass<false><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
   return launch_status();
 }
 
@@ -1127,7 +1341,8 @@ int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s) {
   } else {
     launch_edge_tiles<false>(st, t, s);
   }
-  return launch_status();
+  const int rc = launch_status();
+  return rc ? rc : launch_src_pass(st, t, s);
 }
 
 // the stored layers' tiles, then the redrawn layers' sources (parts: 0 both, 1 or 2 one of them)
@@ -1328,7 +1543,7 @@ __device__ uint32_t infect_one(const covgpu_state& st, const covgpu_sim_params& 
   int symp_class;  // 0 asymptomatic, 1 mild, 2 severe (immunity.py:185-188)
   // people.py:523-527
   const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
-                                  __fsub_rn(1.0f, st.symp_imm[(int64_t)v * st.n + i]));
+                                  __fsub_rn(1.0f, symp_imm_of(st, i, v)));
   if (!d.lt(0, sp_symp)) {  // CASE 1: asymptomatic, people.py:530-532
     const double dr = sample_ff(sp.dur[COVGPU_D_ASYM2REC], d.z[4]);
     rec = (float)__dadd_rn((double)di, dr);
@@ -1431,7 +1646,7 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
     }
     auto lt = [&](int k, float p) { return injected ? (tab[6 + k] < (double)p) : bern32(uw[k], p); };
     const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
-                                    __fsub_rn(1.0f, st.symp_imm[(int64_t)v * st.n + i]));
+                                    __fsub_rn(1.0f, symp_imm_of(st, i, v)));
     symp = lt(0, sp_symp);
     if (symp) {
       const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),

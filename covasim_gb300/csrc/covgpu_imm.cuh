@@ -33,6 +33,13 @@ __device__ __forceinline__ float imm_of(const covgpu_state& st, const covgpu_sim
   return imm;
 }
 
+// symp_imm of agent i against variant v as check_immunity (immunity.py:303-350)
+// leaves it: 0 for an agent that never had NAbs (peak_nab 0), whose efficacies
+// the agent pass does not rewrite each day
+__device__ __forceinline__ float symp_imm_of(const covgpu_state& st, int64_t i, int v) {
+  return st.peak_nab[i] == 0.0f ? 0.0f : st.symp_imm[(int64_t)v * st.n + i];
+}
+
 // calc_VE (immunity.py:216-247) of axis k (0 sus, 1 symp, 2 sev) for ln(nab * imm)
 __device__ __forceinline__ float ve_axis(const covgpu_sim_params& sp, int k, ff ln_eff, const float (*etab)[2]) {
   return ve_ff(ln_eff, ff{sp.ve_alpha[k][0], sp.ve_alpha[k][1]}, ff{sp.ve_beta[k][0], sp.ve_beta[k][1]}, etab);

@@ -241,6 +241,14 @@ def testing_record(spec):
     return r
 
 
+# Default of covgpu_state.src_walk: the stored layers are streamed every day.
+# Walking them from the day's sources (set_src_walk) gives the same results; on
+# a 1M-agent hybrid run (62 MB of stored edges, L2-resident) walking below an
+# eighth infectious made the run 5% slower, on a 20M-agent run (1.2 GB of stored
+# edges) walking below a sixty-fourth 2% faster.
+SRC_WALK = 0
+
+
 class BatchState:
     """Agent and layer arrays of one or more sims in device memory."""
 
@@ -249,6 +257,7 @@ class BatchState:
             raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
         self.edge_tile = int(edge_tile)
         self.edge_resident = False
+        self.src_walk = SRC_WALK
         if not torch.cuda.is_available():
             raise RuntimeError('covasim_gb300 needs a CUDA device: the GPU path has no CPU fallback')
         self.lib = L.lib()
@@ -579,9 +588,10 @@ class BatchState:
         self._tile_segments()
 
     def _trace_index(self, rec, sp, off, n_edges):
-        """Contact-tracing index of a stored layer (covgpu_trace_index) when the sim traces."""
-        T = sp.testing
-        if not (T and T.get('trace') is not None):
+        """Agent index of a stored layer (covgpu_trace_index): the edge pass walks the
+        layer from the day's sources on quiet days, and tracing visits the traced
+        agents' edges."""
+        if n_edges < 1 or n_edges > 0xFFFFFFFF:
             return []
         dev, n = self.device, sp.n
         rp1 = torch.empty(n + 1, dtype=I32, device=dev)
@@ -625,6 +635,13 @@ class BatchState:
 
     def resident_possible(self):
         return int(self.lib.covgpu_edge_resident_bytes(self.cstate_ptr)) > 0
+
+    def set_src_walk(self, k):
+        """Quiet-day walk of the stored layers (covgpu_state.src_walk): k > 0 walks
+        a layer from the day's sources while its sim's infectious agents x k are
+        fewer than its agents, 0 never, -1 always. Results do not depend on it."""
+        self.src_walk = int(k)
+        self._refresh_state()
 
     @property
     def edge_tile_label(self):
@@ -754,6 +771,7 @@ class BatchState:
         st.n_segments = len(self.segments)
         st.n_tiles = self.n_tiles
         st.n_dynamic = self.n_dynamic
+        st.src_walk = int(self.src_walk)
         st.n_agent_blocks = self.n_agent_blocks
         st.edge_tile = self.edge_tile
         st.edge_resident = int(self.edge_resident)

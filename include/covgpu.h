@@ -202,9 +202,11 @@ typedef struct covgpu_layer {
   float beta_const;
   float iso_factor, quar_factor;
   int32_t dyn_k;                  /* dynamic: entries of dyn_cdf                    */
-  /* contact-tracing index of a stored layer (NULL: none; covgpu_trace_index):
-   * the agent a's edges as p1 are [rp1[a], rp1[a+1]), as p2 the edges
-   * perm2[rp2[a] .. rp2[a+1]) (a local to the sim) */
+  /* agent index of a stored layer (NULL: none; covgpu_trace_index): the agent
+   * a's edges as p1 are [rp1[a], rp1[a+1]), as p2 the edges perm2[rp2[a] ..
+   * rp2[a+1]) (a local to the sim). With it the edge pass walks the layer from
+   * the day's sources on days its sim has few infectious agents, and the
+   * tracing pass visits only the traced agents' edges. */
   const uint32_t* rp1;
   const uint32_t* rp2;
   const uint32_t* perm2;
@@ -314,7 +316,11 @@ typedef struct covgpu_state {
   uint32_t* trace_bits;           /* [ceil(n/32)] agents traced today                */
   uint32_t* contact_bits;         /* [n_contact_layers][ceil(n/32)] contacts found   */
   int32_t n_contact_layers;       /* max layers over sims                            */
-  int32_t _pad1;
+  int32_t src_walk;               /* indexed stored layers on quiet days: k > 0 walks a
+                                     layer from the day's sources while its sim's
+                                     infectious agents x k < its agents; 0 never,
+                                     -1 always (the streamed and walked passes give
+                                     the same results)                             */
   int32_t* pending_quar;          /* [R][n] end day of a quarantine starting on day
                                      s (slot s mod R), -1: none                      */
   uint32_t* trace_count;          /* [n_sims] agents traced today                    */
@@ -487,11 +493,13 @@ int covgpu_test_trace(const covgpu_state* st, int32_t t, void* stream);
  * BADARG when st->lik.factor is NULL. */
 int covgpu_lik_targets(const covgpu_state* st, int32_t t, void* stream);
 
-/* The contact-tracing index of one stored layer segment (p1 ascending,
- * global agent indices from agent_off, n_local agents): rp1 and rp2
- * [n_local + 1], perm2 [n_edges], scratch covgpu_trace_index_scratch(n_local)
- * int64 elements. With it, covgpu_test_trace visits only the traced agents'
- * edges of that layer instead of scanning the layer. */
+/* The agent index of one stored layer segment (p1 ascending, global agent
+ * indices from agent_off, n_local agents): rp1 and rp2 [n_local + 1], perm2
+ * [n_edges], scratch covgpu_trace_index_scratch(n_local) int64 elements. With
+ * it, covgpu_edge_pass can walk the layer from the day's sources on quiet days
+ * (covgpu_state.src_walk; the same candidates and draws as the streamed pass),
+ * and covgpu_test_trace visits only the traced agents' edges of that layer
+ * instead of scanning the layer. */
 int64_t covgpu_trace_index_scratch(int64_t n_local);
 int covgpu_trace_index(const int32_t* p1, const int32_t* p2, int64_t n_edges, int64_t agent_off, int64_t n_local,
                        uint32_t* rp1, uint32_t* rp2, uint32_t* perm2, int64_t* scratch, void* stream);
