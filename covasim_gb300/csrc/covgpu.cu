@@ -1481,15 +1481,19 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
 // variant, vaccination: infect() changes none of them before it reads this), for
 // infect() alone reads it; the agent pass stores the array only on the last day
 // of a launch sequence. Without waning the array is as set.
-__device__ float sev_imm_of(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i, int t, int v, uint32_t f) {
+// (the same from the agent's nab, date_recovered and vstate, already loaded)
+__device__ float sev_imm_with(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i, int t, int v, uint32_t f,
+                              float nab, float d_rec, uint32_t vs) {
   if (!sp.use_waning) return st.sev_imm[(int64_t)v * st.n + i];
-  const float nab = st.nab[i];
   if (!(nab > 0.0f)) return 0.0f;
   ff ln_imm;
-  const float imm = imm_of(st, sp, i, v, f, (float)t >= date_row(st, COVGPU_DATE_RECOVERED)[i],
-                           (st.vstate[i] >> 16) & 0xFFu, ln_imm);
+  const float imm = imm_of(st, sp, i, v, f, (float)t >= d_rec, (vs >> 16) & 0xFFu, ln_imm);
   if (!(imm > 0.0f)) return 0.0f;
   return ve_axis(sp, 2, ff_add(ff_log(nab, COVGPU_LN_TAB), ln_imm), COVGPU_EXP_TAB);
+}
+__device__ float sev_imm_of(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i, int t, int v, uint32_t f) {
+  if (!sp.use_waning) return st.sev_imm[(int64_t)v * st.n + i];
+  return sev_imm_with(st, sp, i, t, v, f, st.nab[i], date_row(st, COVGPU_DATE_RECOVERED)[i], st.vstate[i]);
 }
 
 // people.py:435-586 for one agent (already deduplicated), plus update_peak_nab
@@ -1634,6 +1638,22 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
   const bool injected = st.draw_table != nullptr;
   const double* tab = injected ? st.draw_table + i * COVGPU_N_DRAWS : nullptr;
   const uint32_t tag = TAG_INFECT | (uint32_t)call_tag;
+  // the agent's fields that the branch, the samples and the writes read, loaded
+  // together with its flags: one round trip instead of one per level of the branch
+  float a_symp = 0.0f, a_sev = 0.0f, a_crit = 0.0f, a_death = 0.0f, a_peak = 0.0f, a_nab = 0.0f, a_simm = 0.0f;
+  float a_drec = 0.0f;
+  uint32_t a_vs = 0u;
+  if (win) {
+    a_symp = st.symp_prob[i];
+    a_sev = st.severe_prob[i];
+    a_crit = st.crit_prob[i];
+    a_death = st.death_prob[i];
+    a_peak = st.peak_nab[i];
+    a_nab = st.nab[i];
+    a_simm = st.symp_imm[(int64_t)v * st.n + i];
+    a_drec = date_row(st, COVGPU_DATE_RECOVERED)[i];
+    a_vs = st.vstate[i];
+  }
   // the branch: every lane of the group (people.py:523-566)
   bool symp = false, sev = false, crit = false, dead = false;
   uint4 b1 = make_uint4(0u, 0u, 0u, 0u);
@@ -1645,20 +1665,18 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
       uw[0] = b1.z; uw[1] = b1.w; uw[2] = b2.x; uw[3] = b2.y;
     }
     auto lt = [&](int k, float p) { return injected ? (tab[6 + k] < (double)p) : bern32(uw[k], p); };
-    const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], st.symp_prob[i]),
-                                    __fsub_rn(1.0f, symp_imm_of(st, i, v)));
+    // symp_imm as symp_imm_of reads it: 0 for an agent that never had NAbs
+    const float sp_symp = __fmul_rn(__fmul_rn(sp.rel_symp[v], a_symp), __fsub_rn(1.0f, a_peak == 0.0f ? 0.0f : a_simm));
     symp = lt(0, sp_symp);
     if (symp) {
-      const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], st.severe_prob[i]),
-                                    __fsub_rn(1.0f, sev_imm_of(st, sp, i, t, v, f0)));
+      const float p_sev = __fmul_rn(__fmul_rn(sp.rel_severe[v], a_sev),
+                                    __fsub_rn(1.0f, sev_imm_with(st, sp, i, t, v, f0, a_nab, a_drec, a_vs)));
       sev = lt(1, p_sev);
       if (sev) {
-        const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], st.crit_prob[i]),
-                                       hosp_max ? sp.no_hosp_factor : 1.0f);
+        const float p_crit = __fmul_rn(__fmul_rn(sp.rel_crit[v], a_crit), hosp_max ? sp.no_hosp_factor : 1.0f);
         crit = lt(2, p_crit);
         if (crit) {
-          const float p_death = __fmul_rn(__fmul_rn(sp.rel_death[v], st.death_prob[i]),
-                                          icu_max ? sp.no_icu_factor : 1.0f);
+          const float p_death = __fmul_rn(__fmul_rn(sp.rel_death[v], a_death), icu_max ? sp.no_icu_factor : 1.0f);
           dead = lt(3, p_death);
         }
       }
@@ -1694,8 +1712,8 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
     s0 = sample_ff(p0, r == 3 ? zb : za);
     s1 = sample_ff(p1, r < 2 ? zb : (r == 3 ? zb : za));
     if (r == 3 && sp.use_waning) {  // immunity.py:138-202 update_peak_nab (natural infection)
-      if (st.nab[i] > 0.0f) {
-        peak = __fmul_rn(st.peak_nab[i], sp.nab_boost);
+      if (a_nab > 0.0f) {
+        peak = __fmul_rn(a_peak, sp.nab_boost);
       } else {
         const double rel = !symp ? sp.rel_imm_asymp : (!sev ? sp.rel_imm_mild : sp.rel_imm_severe);
         peak = (float)__dmul_rn(__dmul_rn(exp2_ff(d2ff(s0)), rel), sp.nab_norm);
@@ -1710,15 +1728,15 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
 
   uint32_t f = f0;
   // people.py:486-491: breakthrough infections (peak_nab defined)
-  const bool breakthrough = st.peak_nab[i] != 0.0f;
+  const bool breakthrough = a_peak != 0.0f;
   if (breakthrough && st.n_breakthroughs[i] == 0) st.rel_trans[i] = __fmul_rn(st.rel_trans[i], sp.trans_redux);
   float* d_rec = date_row(st, COVGPU_DATE_RECOVERED);
-  const bool reinfection = defined(d_rec[i]);
+  const bool reinfection = defined(a_drec);
   f &= ~(B_SUS | B_NAIVE | B_REC | B_DIAG);
   f |= B_EXP | (1u << (EXPV_SHIFT + v));
   st.n_infections[i] += 1;
   if (breakthrough) st.n_breakthroughs[i] += 1;
-  st.vstate[i] = (st.vstate[i] & 0xFFFFFF00u) | (uint32_t)v;
+  st.vstate[i] = (a_vs & 0xFFFFFF00u) | (uint32_t)v;
   const bool count = call_tag != CALL_TAG_SEED;
   uint32_t out = O_INF | (count ? O_COUNT : 0u) | (reinfection ? O_REINF : 0u);
   float* d_inf = date_row(st, COVGPU_DATE_INFECTIOUS);
