@@ -46,10 +46,14 @@ PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
 # cycles the schedulers issued (smsp__issue_active), per kernel.
 MEASURED_NCU = {
     ('agent_step', 1_000_000): {
-        'dram_bytes': 61_234_688, 'issue_active': 0.675, 'bound': 'issue',
-        'note': 'ncu section capture, day 85 of the 1M-agent run: 61.2 MB of DRAM '
-                'traffic against 88 MB algorithmic; instruction issue 67.5% busy with 1.8 eligible warps per '
-                'scheduler, so the pass is issue-bound, not HBM-bound'},
+        'dram_bytes': 69_902_592, 'issue_active': 0.610, 'bound': 'issue',
+        'note': 'ncu section capture, day 85 of the 1M-agent run: 69.9 MB of DRAM traffic against 88 MB '
+                'algorithmic; instruction issue 61% busy, 35.8 M warp instructions for 1M agents, so the pass '
+                'is issue-bound on the float-float efficacies, not HBM-bound'},
+    ('edge_stored', 1_000_000): {
+        'dram_bytes': 83_027_456, 'issue_active': 0.496, 'bound': 'latency',
+        'note': 'ncu section capture, day 85: 83 MB of DRAM traffic (the 62 MB of stored edge lists and the '
+                'candidates\' records); long-scoreboard stalls dominate'},
 }
 
 
@@ -200,10 +204,14 @@ def agent_pass_bytes(n, nv):
 
 
 # ----------------------------------------------------------------------------- GPU arm
-def kernel_profile(sim, npts):
+def kernel_profile(sim, npts, head_start_cycles=2_000_000):
     """One ungraphed run with CUDA events around each kernel (on the launching
     stream): the agent pass, the stored layers' edge pass, the dynamic layers'
-    per-source pass and the infect pass, each launched on its own."""
+    per-source pass and the infect pass, each launched on its own. Each day
+    starts with a short spin of the stream (about 1 ms, outside the timed pairs)
+    so that the host has queued the day's launches and events before the GPU
+    reaches them: an event pair then times its kernel, not the host's launch
+    latency."""
     import torch
     st = sim.state
     times = {'agent_step': [], 'edge_stored': [], 'edge_dynamic': [], 'infect_claims': []}
@@ -218,10 +226,12 @@ def kernel_profile(sim, npts):
         times[name].append((a, b))
 
     for t in range(npts):
+        torch.cuda._sleep(head_start_cycles)
         timed('agent_step', lambda: st.agent_step(t, do_prev=t > 0, do_day=True))
         timed('edge_stored', lambda: st.edge_pass(t, parts=1))
         timed('edge_dynamic', lambda: st.edge_pass(t, parts=2))
         timed('infect_claims', lambda: st.infect_claims(t))
+    torch.cuda._sleep(head_start_cycles)
     timed('agent_step', lambda: st.agent_step(npts, do_prev=True, do_day=False))
     torch.cuda.synchronize()
     return {k: [a.elapsed_time(b) for a, b in v] for k, v in times.items()}
