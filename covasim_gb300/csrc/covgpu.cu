@@ -736,22 +736,30 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
   const int64_t e1 = min(e0 + TILE, c.n_edges);
   const int32_t off = (int32_t)sp->agent_off;
   int qn = 0;  // warp-uniform queue length
+  // each round's edge lists are loaded one round ahead, so that their latency
+  // overlaps the previous round's lookups and queue drain
+  auto fetch = [&](int r, int4& xa, int4& xb) {
+    const int64_t eb = e0 + ((int64_t)r * NT + threadIdx.x) * EDGE_VEC;
+    if (eb + EDGE_VEC <= e1) {
+      xa = ld_stream_v4(p1 + eb);
+      xb = ld_stream_v4(p2 + eb);
+    } else {
+      xa.x = eb < e1 ? p1[eb] : off;         xb.x = eb < e1 ? p2[eb] : off;
+      xa.y = eb + 1 < e1 ? p1[eb + 1] : off; xb.y = eb + 1 < e1 ? p2[eb + 1] : off;
+      xa.z = eb + 2 < e1 ? p1[eb + 2] : off; xb.z = eb + 2 < e1 ? p2[eb + 2] : off;
+      xa.w = eb + 3 < e1 ? p1[eb + 3] : off; xb.w = eb + 3 < e1 ? p2[eb + 3] : off;
+    }
+  };
+  static_assert(EDGE_VEC == 4, "one int4 of each list per thread and round");
+  int4 na, nb;
+  fetch(0, na, nb);
   for (int r = 0; r < ROUNDS; ++r) {
     const int64_t eb = e0 + ((int64_t)r * NT + threadIdx.x) * EDGE_VEC;
+    const int4 pa = na, pb = nb;
+    if (r + 1 < ROUNDS) fetch(r + 1, na, nb);
     int32_t a[EDGE_VEC], b[EDGE_VEC];
-    if (eb + EDGE_VEC <= e1) {
-      const int4 pa = ld_stream_v4(p1 + eb);
-      const int4 pb = ld_stream_v4(p2 + eb);
-      a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
-      b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < EDGE_VEC; ++j) {
-        const int64_t e = eb + j;
-        a[j] = e < e1 ? p1[e] : off;
-        b[j] = e < e1 ? p2[e] : off;
-      }
-    }
+    a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
+    b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
     // sources first (every edge: shared memory, or the L1-resident bitmap), then the
     // other endpoint's target bit only where one endpoint is a source; roles are
     // exclusive, so an edge has at most one candidate direction
