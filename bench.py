@@ -44,6 +44,11 @@ PEAKS = os.path.join(ROOT, 'MEASURED_PEAKS.json')
 # the launch list of a whole ungraphed run gives the kernels' shares): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum) per launch and the share of
 # cycles the schedulers issued (smsp__issue_active), per kernel.
+# Cumulative infections of the default workload's run with seed 1 (1M agents, 180
+# days). The runs are deterministic (Philox streams keyed by the seed; bit-identical
+# to the oracle's, checked at this scale by the tests), so the bench asserts it.
+RECORDED_CUM_INFECTIONS = {(1_000_000, 180, 1): 1_055_079}
+
 MEASURED_NCU = {
     ('agent_step', 1_000_000): {
         'dram_bytes': 69_902_592, 'issue_active': 0.610, 'bound': 'issue',
@@ -385,7 +390,7 @@ def gpu_arm(args, world, rank):
         e2e = {'value': round(world * agent_days * args.steps / e2e_s, 1), 'unit': 'agent-days/s',
                'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
                'ms_per_step': round(1e3 * e2e_s / args.steps, 3)}
-        assert s.results['cum_infections'].values[-1] > 100
+        check_recorded(args, seed, float(s.results['cum_infections'].values[-1]))
 
     batched = batched_arm(args, sim, value, world) if args.batch else None
     adjoint = adjoint_arm(args) if not args.no_adjoint else None
@@ -396,6 +401,7 @@ def gpu_arm(args, world, rank):
     if not args.no_large and world == 1:
         large = large_arm(args, steps=1, warmup=1, gpu_population=True, emit=False)
 
+    check_recorded(args, seed, float(res['new_infections'].sum() + sim['pop_infected']))
     return dict(value=value, elapsed=elapsed, clocks=clk, roofline=roofline, e2e=e2e, batched=batched, adjoint=adjoint,
                 batch256=batch256, large=large,
                 edge_tile=st.edge_tile_label, tile_ms=tile_ms, popdict=sim.popdict, person=sim._person,
@@ -508,6 +514,14 @@ def batched_arm(args, sim, plain_value, world):
 
 
 # ----------------------------------------------------------------------------- CPU oracle
+def check_recorded(args, seed, cum):
+    """The run's cumulative infections equal the recorded ones of its workload."""
+    want = RECORDED_CUM_INFECTIONS.get((args.pop_size, args.days, seed))
+    if want is not None and cum != want:
+        raise AssertionError(f'cum_infections {cum} differs from the recorded {want} of this workload and seed')
+    assert cum > 100
+
+
 def workload_config(args):
     """The ``config`` both arms print: the workload alone (step and sampling details are top-level keys)."""
     return {'workload': f'hybrid {args.pop_size} agents (h/s/w/c, c redrawn daily), {args.days} days, waning, '

@@ -30,6 +30,28 @@ using namespace covgpu;
 
 namespace {
 
+// Programmatic dependent launch for the day's kernels: a kernel launched with
+// launch_pdl may be scheduled while its stream predecessor's last blocks finish
+// (inside a captured graph the edge becomes a programmatic one); pdl_wait, the
+// first statement of each such kernel, holds it until the predecessor has
+// completed and its writes are visible. Launched the ordinary way, pdl_wait
+// returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <typename... K, typename... A>
+void launch_pdl(void (*kernel)(K...), unsigned grid, unsigned block, size_t smem, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // resident blocks per SM that the register budget of the agent pass must allow
 // (0: the compiler's choice); the pass's grid is one wave of them. Three blocks
 // ran a whole 1M-agent run (one CUDA graph) 0.8 ms faster than four and 2.3 ms
@@ -397,6 +419,7 @@ __device__ __noinline__ void agent_flush(const covgpu_state& st, int sim, int t,
 // one sim, and the counters go to the results once per sim a block touched
 // instead of once per 256 agents.
 __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm) {
+  pdl_wait();
   if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
     const int h = *st.hold;
     if (h <= t - 1) return;
@@ -827,6 +850,7 @@ __device__ __forceinline__ bool seg_walked(const covgpu_state& st, const covgpu_
 // One block per tile (none for a segment walked from its sources today).
 template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int t) {
+  pdl_wait();
   if (held(st, t)) return;
   constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   __shared__ int s_seg;
@@ -869,6 +893,7 @@ constexpr int RES_THREADS = 1024;
 constexpr int RES_MAX_SEGS = COVGPU_MAX_LAYERS;  // one sim: at most one segment per layer
 template <bool LIK, int64_t TILE>
 __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state st, int t) {
+  pdl_wait();
   if (held(st, t)) return;
   extern __shared__ uint4 s_dyn[];
   __shared__ covgpu_layer s_segs[RES_MAX_SEGS];
@@ -1324,10 +1349,10 @@ template <bool LIK>
 void launch_edge_tiles(const covgpu_state* st, int t, cudaStream_t s) {
   const dim3 grid((unsigned)st->n_tiles);
   switch (st->edge_tile) {
-    case 1024: k_edge_pass<LIK, 1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-    case 2048: k_edge_pass<LIK, 2><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-    case 8192: k_edge_pass<LIK, 8><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
-    default: k_edge_pass<LIK, 4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
+    case 1024: launch_pdl(k_edge_pass<LIK, 1>, grid.x, EDGE_THREADS, 0, s, *st, t); break;
+    case 2048: launch_pdl(k_edge_pass<LIK, 2>, grid.x, EDGE_THREADS, 0, s, *st, t); break;
+    case 8192: launch_pdl(k_edge_pass<LIK, 8>, grid.x, EDGE_THREADS, 0, s, *st, t); break;
+    default: launch_pdl(k_edge_pass<LIK, 4>, grid.x, EDGE_THREADS, 0, s, *st, t); break;
   }
 }
 
@@ -1335,8 +1360,8 @@ template <bool LIK>
 void launch_edge_res(const covgpu_state* st, int t, cudaStream_t s) {
   const int64_t smem = edge_res_smem(st);
   const unsigned grid = (unsigned)(st->n_tiles < n_sms() ? st->n_tiles : n_sms());
-  if (st->edge_tile == 8192) k_edge_pass_res<LIK, 8192><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
-  else k_edge_pass_res<LIK, 4096><<<grid, RES_THREADS, (size_t)smem, s>>>(*st, t);
+  if (st->edge_tile == 8192) launch_pdl(k_edge_pass_res<LIK, 8192>, grid, RES_THREADS, (size_t)smem, s, *st, t);
+  else launch_pdl(k_edge_pass_res<LIK, 4096>, grid, RES_THREADS, (size_t)smem, s, *st, t);
 }
 
 int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s) {
@@ -1881,6 +1906,7 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
 }
 
 __global__ void k_infect_claims(covgpu_state st, int t) {
+  pdl_wait();
   if (held(st, t)) return;
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
@@ -2026,16 +2052,16 @@ unsigned agent_grid(const covgpu_state* st) {
 int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int close_last, cudaStream_t s) {
   for (int t = t0; t < t1; ++t) {
     if (st->hold) k_rescale_check<<<1, 128, 0, s>>>(*st, t);
-    k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, s>>>(*st, t, (t > t0 || open_prev) ? 1 : 0, 1,
-                                                                        t == t1 - 1 ? 1 : 0);
+    launch_pdl(k_agent_step, agent_grid(st), AGENT_THREADS, 0, s, *st, t, (t > t0 || open_prev) ? 1 : 0, 1,
+               t == t1 - 1 ? 1 : 0);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
     const int rc = launch_edge_pass_forked(st, t, s);
     if (rc) return rc;
     launch_lik_targets(st, t, s);
-    k_infect_claims<<<grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s>>>(*st, t);
+    launch_pdl(k_infect_claims, (unsigned)grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s, *st, t);
   }
-  if (close_last) k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, s>>>(*st, t1, 1, 0, 0);
+  if (close_last) launch_pdl(k_agent_step, agent_grid(st), AGENT_THREADS, 0, s, *st, t1, 1, 0, 0);
   return launch_status();
 }
 
