@@ -550,9 +550,10 @@ int covgpu_layer_lists(const covgpu_state* st, int32_t segment, int32_t t, int64
  * st->has_testing), edge_pass, lik_targets (when st->lik.factor is set),
  * infect_claims. open_prev: day t0-1 still needs its closing pass (stocks,
  * update_nab), which day t0's agent pass then does first; close_last: end
- * with the closing pass of day t1-1. With use_graph the whole sequence is
- * captured once into a CUDA graph and launched (a capture is reused while
- * the state and the arguments are unchanged). */
+ * with the closing pass of day t1-1. With use_graph a sequence run again
+ * with the same state and arguments is captured into a CUDA graph on its
+ * second run and replayed from then on; its first run launches the kernels
+ * directly (a run made once does not pay for the capture). */
 int covgpu_run_days(const covgpu_state* st, int32_t t0, int32_t t1, int32_t open_prev, int32_t close_last,
                     int32_t use_graph, void* stream);
 

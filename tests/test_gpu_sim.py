@@ -169,6 +169,28 @@ def test_step_mode_equals_graph_run():
         np.testing.assert_array_equal(ra[k], rc[k], err_msg=k)
 
 
+def test_graph_capture_and_replay_equal_the_direct_run():
+    """covgpu_run_days launches a state's day range directly on its first run,
+    captures it into a CUDA graph on the second and replays the graph after
+    that: the three runs (and a run with testing, whose graph holds the testing
+    passes) are identical."""
+    for pars in (dict(pop_type='hybrid', pop_size=6000, n_days=40, rand_seed=9, use_waning=True,
+                      dynam_layer=dict(h=0, s=0, w=0, c=1)),
+                 dict(pop_type='hybrid', pop_size=4000, n_days=35, rand_seed=4,
+                      interventions=[cv.test_prob(symp_prob=0.2), cv.contact_tracing(trace_probs=0.5)])):
+        sim = cv.Sim(pars)
+        sim.initialize()
+        snap = sim.state.snapshot()
+        runs = []
+        for _ in range(3):
+            sim.rewind(snap)
+            sim.run()
+            runs.append({k: np.array(v, copy=True) for k, v in sim.raw_results().items()})
+        for r in runs[1:]:
+            for k in RES_KEYS + ['pop_nabs', 'pop_protection']:
+                np.testing.assert_array_equal(r[k], runs[0][k], err_msg=k)
+
+
 def test_resume_until_equals_one_run():
     """test_resume.py:19-52: run(until=) then run() equals one run."""
     pars = dict(pop_type='random', pop_size=5000, n_days=40, rand_seed=11)
