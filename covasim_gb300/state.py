@@ -258,6 +258,8 @@ class BatchState:
         self.edge_tile = int(edge_tile)
         self.edge_resident = False
         self.src_walk = SRC_WALK
+        self._index_pending = []  # stored segments whose agent index is built on demand
+        self._index_tensors = []
         if not torch.cuda.is_available():
             raise RuntimeError('covasim_gb300 needs a CUDA device: the GPU path has no CPU fallback')
         self.lib = L.lib()
@@ -588,11 +590,18 @@ class BatchState:
         self._tile_segments()
 
     def _trace_index(self, rec, sp, off, n_edges):
-        """Agent index of a stored layer (covgpu_trace_index): the edge pass walks the
-        layer from the day's sources on quiet days, and tracing visits the traced
-        agents' edges."""
+        """Agent index of a stored layer (covgpu_trace_index), built now when the sim
+        traces (tracing visits the traced agents' edges through it), else when the
+        walk from the sources is switched on (set_src_walk)."""
         if n_edges < 1 or n_edges > 0xFFFFFFFF:
             return []
+        T = sp.testing
+        if not (T and T.get('trace') is not None) and not self.src_walk:
+            self._index_pending.append((rec, sp, off, n_edges))
+            return []
+        return self._build_index(rec, sp, off, n_edges)
+
+    def _build_index(self, rec, sp, off, n_edges):
         dev, n = self.device, sp.n
         rp1 = torch.empty(n + 1, dtype=I32, device=dev)
         rp2 = torch.empty(n + 1, dtype=I32, device=dev)
@@ -639,8 +648,14 @@ class BatchState:
     def set_src_walk(self, k):
         """Quiet-day walk of the stored layers (covgpu_state.src_walk): k > 0 walks
         a layer from the day's sources while its sim's infectious agents x k are
-        fewer than its agents, 0 never, -1 always. Results do not depend on it."""
+        fewer than its agents, 0 never, -1 always (building the layers' agent index
+        first). Results do not depend on it."""
         self.src_walk = int(k)
+        if self.src_walk and self._index_pending:
+            for rec, sp, off, n_edges in self._index_pending:
+                self._index_tensors += self._build_index(rec, sp, off, n_edges)
+            self._index_pending = []
+            self._tile_segments()  # the segment table with the indices
         self._refresh_state()
 
     @property
