@@ -25,6 +25,26 @@ inline int grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {
   return (int)b;
 }
 
+// Blocks of one wave of `kernel` with `threads` threads: its resident blocks per
+// SM on the current device times the SM count (for the passes that walk
+// agent-block ranges; any grid gives the same results), and the grid of such a
+// pass over a state's agent blocks.
+template <class K>
+inline int64_t wave_blocks(K kernel, int threads) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return (int64_t)1 << 30;  // no wave bound: one block per agent block
+  }
+  return (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+}
+inline unsigned wave_grid(const covgpu_state* st, int64_t wave) {
+  const int64_t nb = st->n_agent_blocks;
+  return (unsigned)(nb < wave ? (nb > 0 ? nb : 1) : wave);
+}
+
 // the checks every state entry point makes before launching (covgpu.cu)
 int check_state(const covgpu_state* st);
 // the testing, tracing and post passes of day t (covgpu_testing.cu)

@@ -45,14 +45,15 @@ __device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu
 
 // test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
 // then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
-__global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
-  if (held(st, t)) return;
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+// One agent block of the test pass (thread k on agent begin + k); the tested are
+// counted into the thread's accumulator
+__device__ __forceinline__ void test_block(const covgpu_state& st, int t, const covgpu_agent_block& blk,
+                                           unsigned& tested_acc) {
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;
   const bool test_on = day_active(t, T.test_start, T.test_end);
   const bool trace_on = day_active(t, T.trace_start, T.trace_end);
-  if (!test_on && !trace_on) return;  // uniform over the block (one sim per block)
+  if (!test_on && !trace_on) return;  // uniform over the agent block (one sim per agent block)
   const int64_t i = blk.begin + threadIdx.x;
   const bool valid = i < blk.end;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, in
   if (valid) {
     uint32_t f = st.flags[i];
     float* d_diag = date_row(st, COVGPU_DATE_DIAGNOSED) + i;
+    float dd = *d_diag;  // loaded with the flags; kept current below
     if (test_on) {
       uint64_t thr = 0;
       if (!(f & B_DIAG)) {  // the diagnosed do not test
@@ -74,10 +76,11 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, in
           tested = 1;
           st.flags[i] = f | B_TESTED;
           date_row(st, COVGPU_DATE_TESTED)[i] = (float)t;
-          if ((f & B_INF) && bern52_thr(w.z, w.w, T.thr_sensitivity) && isnan(*d_diag)) {
+          if ((f & B_INF) && bern52_thr(w.z, w.w, T.thr_sensitivity) && isnan(dd)) {
             const uint4 w1 = philox(make_uint4(local, 1u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
             if (bern52_thr(w1.x, w1.y, T.thr_not_lost)) {
-              *d_diag = (float)(t + T.test_delay);
+              dd = (float)(t + T.test_delay);
+              *d_diag = dd;
               date_row(st, COVGPU_DATE_POS_TEST)[i] = (float)t;
             }
           }
@@ -88,16 +91,48 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, in
       if (T.presumptive)
         trace = (date_row(st, COVGPU_DATE_TESTED)[i] == (float)t && (f & B_EXP)) ? 1u : 0u;
       else
-        trace = (*d_diag == (float)t) ? 1u : 0u;
+        trace = (dd == (float)t) ? 1u : 0u;
     }
   }
   const uint32_t tm = __ballot_sync(0xffffffffu, trace);
   if (trace_on && lane == 0 && blk.begin + warp * 32 < blk.end) st.trace_bits[(blk.begin + warp * 32) >> 5] = tm;
-  const unsigned n_tested = __reduce_add_sync(0xffffffffu, tested);
-  if (lane == 0 && n_tested)
-    atomicAdd(reinterpret_cast<unsigned long long*>(&sp.res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
-              (unsigned long long)n_tested);
+  tested_acc += tested;
   if (lane == 0 && tm) atomicAdd(st.trace_count + blk.sim, (unsigned)__popc(tm));
+}
+
+__device__ __forceinline__ void test_flush(const covgpu_state& st, int t, int sim, unsigned& tested_acc) {
+  const unsigned n_tested = __reduce_add_sync(0xffffffffu, tested_acc);
+  if ((threadIdx.x & 31) == 0 && n_tested)
+    atomicAdd(reinterpret_cast<unsigned long long*>(&st.sims[sim].res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
+              (unsigned long long)n_tested);
+  tested_acc = 0;
+}
+
+// The passes over agents run as (at most) one wave of blocks, each walking a
+// contiguous range of agent blocks [b, b_end); counts are flushed once per sim.
+__device__ __forceinline__ bool agent_range(const covgpu_state& st, int64_t& b, int64_t& b_end) {
+  const int64_t nb = st.n_agent_blocks;
+  const int64_t per = (nb + gridDim.x - 1) / gridDim.x;
+  b = (int64_t)blockIdx.x * per;
+  b_end = min(nb, b + per);
+  return b < b_end;
+}
+
+__global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  int64_t b, b_end;
+  if (!agent_range(st, b, b_end)) return;
+  int sim = st.agent_blocks[b].sim;
+  unsigned tested_acc = 0;
+  for (; b < b_end; ++b) {
+    const covgpu_agent_block blk = st.agent_blocks[b];
+    if (blk.sim != sim) {
+      test_flush(st, t, sim, tested_acc);
+      sim = blk.sim;
+    }
+    test_block(st, t, blk, tested_acc);
+  }
+  test_flush(st, t, sim, tested_acc);
 }
 
 __device__ __forceinline__ uint32_t bit_of(const uint32_t* __restrict__ bits, int32_t a) {
@@ -151,9 +186,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_trace_scan(covgpu_state st, in
 
 // find_contacts through the index of each stored layer: a traced agent marks the
 // other endpoint of each of its edges, as p1 and as p2
-__global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
-  if (held(st, t)) return;
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+__device__ __forceinline__ void trace_csr_block(const covgpu_state& st, int t, const covgpu_agent_block& blk) {
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;
   if (!day_active(t, T.trace_start, T.trace_end) || st.trace_count[blk.sim] == 0) return;
@@ -176,6 +209,12 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, in
       atomicOr(contact + (a >> 5), 1u << (a & 31));
     }
   }
+}
+__global__ void __launch_bounds__(AGENT_THREADS) k_trace_csr(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  int64_t b, b_end;
+  if (!agent_range(st, b, b_end)) return;
+  for (; b < b_end; ++b) trace_csr_block(st, t, st.agent_blocks[b]);
 }
 
 // find_contacts over the dynamic layers: one warp per agent block; each traced
@@ -227,9 +266,10 @@ __global__ void __launch_bounds__(TRACE_DYN_WARPS * 32) k_trace_dyn(covgpu_state
 // contact_tracing.notify_contacts (interventions.py:1120-1145) with the
 // binomial_filter of identify_contacts, then update_states_post
 // (people.py:189-196: check_diagnosed, check_quar, check_enter_iso)
-__global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
-  if (held(st, t)) return;
-  const covgpu_agent_block blk = st.agent_blocks[blockIdx.x];
+// One agent block of the post pass; the day's diagnoses, quarantines and
+// isolations are counted into the thread's accumulators
+__device__ __forceinline__ void post_block(const covgpu_state& st, int t, const covgpu_agent_block& blk,
+                                           unsigned& acc_diag, unsigned& acc_quar, unsigned& acc_iso) {
   const covgpu_sim_params& sp = st.sims[blk.sim];
   const covgpu_testing& T = sp.testing;
   const int64_t i = blk.begin + threadIdx.x;
@@ -241,7 +281,20 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
   const float tf = (float)t;
   const int R = st.pending_slots;
   unsigned c_diag = 0, c_quar = 0, c_iso = 0;
-  uint32_t f = valid ? st.flags[i] : 0u;
+  // the agent's fields the checks read, loaded together (one round trip): flags,
+  // date_pos_test, date_diagnosed, today's pending-quarantine slot, date_end_quarantine
+  const float nanf_ = __int_as_float(0x7fc00000);
+  uint32_t f = 0u;
+  float a_dpt = nanf_, a_dd = nanf_, a_deq = nanf_;
+  int32_t a_pq = -1;
+  int32_t* pq_today = st.pending_quar + (int64_t)(t % R) * st.n + i;
+  if (valid) {
+    f = st.flags[i];
+    a_dpt = date_row(st, COVGPU_DATE_POS_TEST)[i];
+    a_dd = date_row(st, COVGPU_DATE_DIAGNOSED)[i];
+    a_pq = *pq_today;
+    a_deq = date_row(st, COVGPU_DATE_END_QUARANTINE)[i];
+  }
   const uint32_t f_in = f;
 
   // ---- notify the contacts found by the scan (only on tracing days)
@@ -261,37 +314,40 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
       const float cand = __double2float_rn(__dadd_rn((double)t, T.trace_time[l]));
       if (isnan(*dkc) || cand < *dkc) *dkc = cand;  // np.fmin
       const int start = t + T.trace_start_off[l];
-      int32_t* pq = st.pending_quar + (int64_t)(start % R) * st.n + i;
       const int32_t end = start + T.trace_period[l];
+      if (start == t) {  // today's slot: check_quar below reads it from a_pq
+        if (a_pq < 0 || end > a_pq) a_pq = end;
+        continue;
+      }
+      int32_t* pq = st.pending_quar + (int64_t)(start % R) * st.n + i;
       if (*pq < 0 || end > *pq) *pq = end;  // check_quar keeps the latest end of a day's requests
     }
   }
 
   if (valid) {
     // ---- check_diagnosed, people.py:315-332
-    float* dpt = date_row(st, COVGPU_DATE_POS_TEST) + i;
-    const float dd = date_row(st, COVGPU_DATE_DIAGNOSED)[i];
+    const float dd = a_dd;
     if (!(f & B_DIAG)) {
-      if (defined(*dpt) && tf >= *dpt) { *dpt = __int_as_float(0x7fc00000); c_diag = 1; }
+      if (defined(a_dpt) && tf >= a_dpt) { date_row(st, COVGPU_DATE_POS_TEST)[i] = nanf_; c_diag = 1; }
       if (defined(dd) && tf >= dd) f |= B_DIAG;
     }
     // ---- check_quar, people.py:335-358
-    int32_t* pq = st.pending_quar + (int64_t)(t % R) * st.n + i;
-    const int32_t end = *pq;
-    float* deq = date_row(st, COVGPU_DATE_END_QUARANTINE) + i;
+    const int32_t end = a_pq;
+    float deq = a_deq;
     if (end >= 0) {
-      *pq = -1;
+      *pq_today = -1;
       if (f & B_QUAR) {
-        if ((float)end > *deq) *deq = (float)end;  // max(current, end_day), first argument kept on ties/NaN
+        if ((float)end > deq) deq = (float)end;  // max(current, end_day), first argument kept on ties/NaN
       } else if (!(f & (B_DEAD | B_REC | B_DIAG | B_ISO))) {
         f |= B_QUAR;
         date_row(st, COVGPU_DATE_QUARANTINED)[i] = tf;
-        *deq = (float)end;
+        deq = (float)end;
         c_quar = 1;
       }
     }
-    if ((f & B_QUAR) && dd == tf) *deq = tf;
-    if ((f & B_QUAR) && defined(*deq) && tf >= *deq) f &= ~B_QUAR;
+    if ((f & B_QUAR) && dd == tf) deq = tf;
+    if (__float_as_uint(deq) != __float_as_uint(a_deq)) date_row(st, COVGPU_DATE_END_QUARANTINE)[i] = deq;
+    if ((f & B_QUAR) && defined(deq) && tf >= deq) f &= ~B_QUAR;
     // ---- check_enter_iso, people.py:361-366
     if (dd == tf) {
       f |= B_ISO;
@@ -308,16 +364,42 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, in
         *r = (f & B_QUAR) ? (*r | 0x80000000u) : (*r & 0x7FFFFFFFu);
       }
   }
-  const unsigned cd = __reduce_add_sync(0xffffffffu, c_diag), cq = __reduce_add_sync(0xffffffffu, c_quar),
-                 ci = __reduce_add_sync(0xffffffffu, c_iso);
+  acc_diag += c_diag;
+  acc_quar += c_quar;
+  acc_iso += c_iso;
+  // the day's trace count is read only by the tracing passes, which have finished
+  if (threadIdx.x == 0 && blk.begin == sp.agent_off) st.trace_count[blk.sim] = 0u;
+}
+
+__device__ __forceinline__ void post_flush(const covgpu_state& st, int t, int sim, unsigned& acc_diag,
+                                           unsigned& acc_quar, unsigned& acc_iso) {
+  const covgpu_sim_params& sp = st.sims[sim];
+  const unsigned cd = __reduce_add_sync(0xffffffffu, acc_diag), cq = __reduce_add_sync(0xffffffffu, acc_quar),
+                 ci = __reduce_add_sync(0xffffffffu, acc_iso);
   int64_t* res = sp.res_int + (int64_t)t * COVGPU_N_RES_INT;
-  if (lane == 0 && t < sp.npts) {
+  if ((threadIdx.x & 31) == 0 && t < sp.npts) {
     if (cd) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_DIAGNOSES), (unsigned long long)cd);
     if (cq) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_QUARANTINED), (unsigned long long)cq);
     if (ci) atomicAdd(reinterpret_cast<unsigned long long*>(res + R_ISOLATED), (unsigned long long)ci);
   }
-  // the day's trace count is read only by k_trace_scan, which has finished
-  if (threadIdx.x == 0 && blk.begin == sp.agent_off) st.trace_count[blk.sim] = 0u;
+  acc_diag = acc_quar = acc_iso = 0;
+}
+
+__global__ void __launch_bounds__(AGENT_THREADS) k_post_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  int64_t b, b_end;
+  if (!agent_range(st, b, b_end)) return;
+  int sim = st.agent_blocks[b].sim;
+  unsigned acc_diag = 0, acc_quar = 0, acc_iso = 0;
+  for (; b < b_end; ++b) {
+    const covgpu_agent_block blk = st.agent_blocks[b];
+    if (blk.sim != sim) {
+      post_flush(st, t, sim, acc_diag, acc_quar, acc_iso);
+      sim = blk.sim;
+    }
+    post_block(st, t, blk, acc_diag, acc_quar, acc_iso);
+  }
+  post_flush(st, t, sim, acc_diag, acc_quar, acc_iso);
 }
 
 // ------------------------------------------------------------ contact-tracing index
@@ -358,7 +440,8 @@ namespace covgpu {
 
 int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   if (!st->has_testing) return COVGPU_OK;
-  k_test_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  static const int64_t test_wave = wave_blocks(k_test_pass, AGENT_THREADS);
+  k_test_pass<<<wave_grid(st, test_wave), AGENT_THREADS, 0, s>>>(*st, t);
   if (st->n_tiles > 0) {
     const dim3 grid((unsigned)st->n_tiles);
     switch (st->edge_tile) {
@@ -368,11 +451,13 @@ int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
       default: k_trace_scan<4><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;
     }
   }
-  k_trace_csr<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  static const int64_t csr_wave = wave_blocks(k_trace_csr, AGENT_THREADS);
+  k_trace_csr<<<wave_grid(st, csr_wave), AGENT_THREADS, 0, s>>>(*st, t);
   if (st->n_dynamic)
     k_trace_dyn<<<(unsigned)((st->n_agent_blocks + TRACE_DYN_WARPS - 1) / TRACE_DYN_WARPS), TRACE_DYN_WARPS * 32, 0,
                   s>>>(*st, t);
-  k_post_pass<<<(unsigned)st->n_agent_blocks, AGENT_THREADS, 0, s>>>(*st, t);
+  static const int64_t post_wave = wave_blocks(k_post_pass, AGENT_THREADS);
+  k_post_pass<<<wave_grid(st, post_wave), AGENT_THREADS, 0, s>>>(*st, t);
   return launch_status();
 }
 
