@@ -5,11 +5,12 @@ it as the checker.
 
 ``TestProb`` restates ``test_prob`` (covasim/interventions.py:858-981) and
 ``ContactTracing`` restates ``contact_tracing`` (covasim/interventions.py:984-1145),
-for the options the GPU path supports (no swab-delay distribution, no ILI
-prevalence, no subtargeting, no tracing capacity). Their random draws come
+for the options the GPU path supports (ILI prevalence and fixed subtargets;
+no swab-delay distribution, no tracing capacity). Their random draws come
 from the oracle sim: the numpy MT19937 stream in the reference's call order
 (``rng='mt'``), or Philox keyed by (agent, day) and (agent, layer, day) like
-the CUDA library's (``rng='philox'``).
+the CUDA library's, with the day's ILI agents from a PCG64 stream keyed by
+(seed, 0x111E, day) (``rng='philox'``).
 """
 import numpy as np
 
@@ -46,18 +47,40 @@ def _active(t, start_day, end_day):
     return not (t < start_day or (end_day is not None and t > end_day))
 
 
+ILI_TAG = 0x111E
+
+
+def ili_agents(seed, t, n, n_ili):
+    """Philox mode: the n_ili distinct agents with influenza-like symptoms on day t
+    (interventions.py:942-947 draws them with cvu.choose), from a PCG64 stream keyed
+    by (seed, 0x111E, t): they do not depend on the sim's state."""
+    rng = np.random.Generator(np.random.PCG64([int(seed) & 0xFFFFFFFFFFFFFFFF, ILI_TAG, int(t)]))
+    return np.sort(rng.choice(int(n), int(n_ili), replace=False)).astype(np.int64)
+
+
+def daily_series(x, npts):
+    """process_daily_data (interventions.py:111-147) for a number or a sequence."""
+    if isinstance(x, (int, float, np.integer, np.floating)):
+        return np.array([x] * npts)
+    return np.asarray(x)
+
+
 class TestProb:
-    """interventions.py:858-981 (swab_delay, ili_prev and subtarget unsupported)."""
+    """interventions.py:858-981 (swab_delay unsupported; subtarget a dict of fixed
+    ``inds`` and ``vals``)."""
 
     __test__ = False  # not a pytest test class
 
     def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
-                 sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0, end_day=None):
+                 subtarget=None, ili_prev=None, sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0,
+                 end_day=None):
         self.symp_prob = symp_prob
         self.asymp_prob = asymp_prob
         self.symp_quar_prob = symp_quar_prob if symp_quar_prob is not None else symp_prob
         self.asymp_quar_prob = asymp_quar_prob if asymp_quar_prob is not None else asymp_prob
         self.quar_policy = quar_policy if quar_policy else 'start'
+        self.subtarget = subtarget
+        self.ili_prev = ili_prev
         self.sensitivity = sensitivity
         self.loss_prob = loss_prob
         self.test_delay = test_delay
@@ -71,16 +94,31 @@ class TestProb:
         people = sim.people
         n = sim.n
         symp_inds = people.symptomatic.nonzero()[0]
-        asymp_inds = np.setdiff1d(np.arange(n), symp_inds)
+        # symptomatics of influenza-like illness, drawn before the tests (interventions.py:941-947)
+        ili_inds = np.array([], dtype=np.int64)
+        if self.ili_prev is not None:
+            ili = daily_series(self.ili_prev, sim.npts)
+            rel_t = t - self.start_day
+            if rel_t < len(ili):
+                n_ili = int(ili[rel_t] * n)
+                if sim.rng == 'philox':
+                    ili_inds = ili_agents(sim.seed, t, n, n_ili)
+                else:  # cvu.choose is a numba function (utils.py:430-443): numba's stream
+                    ili_inds = sim.rs_numba.choice(n, n_ili, replace=False)
+                ili_inds = np.setdiff1d(ili_inds, symp_inds)
+        asymp_inds = np.setdiff1d(np.setdiff1d(np.arange(n), symp_inds), ili_inds)
         quar_test_inds = get_quar_inds(self.quar_policy, sim)
         symp_quar_inds = np.intersect1d(quar_test_inds, symp_inds)
         asymp_quar_inds = np.intersect1d(quar_test_inds, asymp_inds)
         diag_inds = people.diagnosed.nonzero()[0]
         test_probs = np.zeros(n)
         test_probs[symp_inds] = self.symp_prob
+        test_probs[ili_inds] = self.symp_prob
         test_probs[asymp_inds] = self.asymp_prob
         test_probs[symp_quar_inds] = self.symp_quar_prob
         test_probs[asymp_quar_inds] = self.asymp_quar_prob
+        if self.subtarget is not None:  # get_subtargets (interventions.py:150-187), fixed inds and vals
+            test_probs[np.asarray(self.subtarget['inds'], dtype=np.int64)] = self.subtarget['vals']
         test_probs[diag_inds] = 0.0
         if sim.rng == 'philox':
             u_test, u_sens, u_keep = ph.test_draws(sim.k0, sim.k1, t, np.arange(n))

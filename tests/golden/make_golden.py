@@ -418,6 +418,15 @@ TESTING_CASES = [  # (pop_type, n, days, seed, use_waning, dynamic c, test_prob 
      dict(trace_probs=0.8, presumptive=True, start_day=8)),
     ('hybrid', 1200, 40, 6, False, 0, dict(symp_prob=0.3, quar_policy=[0, 2]),
      dict(trace_probs=0.7, trace_time=0.5, quar_period=10)),
+    # influenza-like illness and fixed subtargets
+    ('hybrid', 1500, 40, 7, True, 1,
+     dict(symp_prob=0.2, asymp_prob=0.005, quar_policy='both', ili_prev=0.02,
+          subtarget=dict(inds=list(range(0, 1500, 7)), vals=0.3)),
+     dict(trace_probs=0.5, trace_time=1)),
+    ('random', 1200, 40, 8, False, 0,
+     dict(symp_prob=0.3, start_day=3, ili_prev=[0.01] * 8 + [0.05] * 12,
+          subtarget=dict(inds=list(range(3, 1200, 11)), vals=[0.05 + 0.9 * (k % 3) / 2 for k in range(109)])),
+     dict(trace_probs=0.6)),
 ]
 TESTING_FINAL = ['diagnosed', 'quarantined', 'isolated', 'known_contact', 'tested', 'date_diagnosed',
                  'date_quarantined', 'date_end_quarantine', 'date_known_contact', 'date_pos_test', 'date_tested',
