@@ -26,6 +26,7 @@ FX_NAB_BITS = 24
 FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
 NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
+NO_SUBTARGET = 0xFFFFFFFFFFFFFFFF  # covgpu_testing.sub_thr: no subtarget (COVGPU_NO_SUBTARGET)
 EDGE_TILE = 4096          # default edges per edge-pass tile (block)
 DYN_MAX_LIST = 1024       # longest contact list of an agent in a dynamic layer (COVGPU_DYN_MAX_LIST)
 EDGE_TILES = (1024, 2048, 4096, 8192)   # tile sizes the library supports (covgpu_state.edge_tile)
@@ -66,6 +67,8 @@ class Testing(C.Structure):
         ('test_delay', C.c_int32), ('trace_start', C.c_int32), ('trace_end', C.c_int32), ('presumptive', C.c_int32),
         ('trace_time', C.c_double * MAX_LAYERS), ('thr_trace', C.c_uint64 * MAX_LAYERS),
         ('trace_start_off', C.c_int32 * MAX_LAYERS), ('trace_period', C.c_int32 * MAX_LAYERS),
+        ('sub_thr', C.c_void_p), ('ili_off', C.c_void_p), ('ili_inds', C.c_void_p), ('ili_mark', C.c_void_p),
+        ('ili_days', C.c_int32), ('_pad_ili', C.c_int32),
     ]
 
 

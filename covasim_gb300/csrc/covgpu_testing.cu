@@ -66,8 +66,18 @@ __device__ __forceinline__ void test_block(const covgpu_state& st, int t, const 
       uint64_t thr = 0;
       if (!(f & B_DIAG)) {  // the diagnosed do not test
         const bool symp = f & B_SYMP;
-        thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
-                                          : (symp ? T.thr_symp : T.thr_asymp);
+        const int64_t loc = i - sp.agent_off;
+        // an influenza-like illness without COVID symptoms: the symptomatic probability,
+        // never the quarantine ones (interventions.py:966-969)
+        if (!symp && T.ili_mark && T.ili_mark[loc] == t)
+          thr = T.thr_symp;
+        else
+          thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
+                                            : (symp ? T.thr_symp : T.thr_asymp);
+        if (T.sub_thr) {  // subtargets (interventions.py:970-972)
+          const uint64_t sv = T.sub_thr[loc];
+          if (sv != COVGPU_NO_SUBTARGET) thr = sv;
+        }
       }
       if (thr) {
         const uint32_t local = (uint32_t)(i - sp.agent_off);
@@ -106,6 +116,24 @@ __device__ __forceinline__ void test_flush(const covgpu_state& st, int t, int si
     atomicAdd(reinterpret_cast<unsigned long long*>(&st.sims[sim].res_int[(int64_t)t * COVGPU_N_RES_INT + R_TESTS]),
               (unsigned long long)n_tested);
   tested_acc = 0;
+}
+
+// test_prob's influenza-like illness of day t (interventions.py:941-947): the day's
+// agents, drawn on the host (they do not depend on the state), are marked with t
+// before the test pass reads the marks; one block per sim
+__global__ void k_ili_mark(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  const int s = blockIdx.x;
+  if (s >= st.n_sims) return;
+  const covgpu_testing& T = st.sims[s].testing;
+  if (!T.ili_mark || !day_active(t, T.test_start, T.test_end)) return;
+  const int d = t - T.test_start;
+  if (d < 0 || d >= T.ili_days) return;
+  const int n = st.sims[s].n_agents;
+  for (int64_t k = T.ili_off[d] + threadIdx.x; k < T.ili_off[d + 1]; k += blockDim.x) {
+    const int32_t a = T.ili_inds[k];
+    if (a >= 0 && a < n) T.ili_mark[a] = t;
+  }
 }
 
 // The passes over agents run as (at most) one wave of blocks, each walking a
@@ -440,6 +468,7 @@ namespace covgpu {
 
 int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   if (!st->has_testing) return COVGPU_OK;
+  k_ili_mark<<<(unsigned)st->n_sims, 256, 0, s>>>(*st, t);
   static const int64_t test_wave = wave_blocks(k_test_pass, AGENT_THREADS);
   k_test_pass<<<wave_grid(st, test_wave), AGENT_THREADS, 0, s>>>(*st, t);
   if (st->n_tiles > 0) {

@@ -116,8 +116,11 @@ def _day(d, default):
 
 class test_prob(Intervention):
     """Test each agent with a probability set by its symptom and quarantine state
-    (interventions.py:858-981). Same arguments as the reference; ``swab_delay``,
-    ``ili_prev`` and ``subtarget`` are not supported on the GPU path.
+    (interventions.py:858-981). Same arguments as the reference: ``ili_prev`` a
+    number or a daily sequence (process_daily_data, interventions.py:111-147),
+    ``subtarget`` a dict of fixed ``inds`` and ``vals`` (get_subtargets,
+    interventions.py:150-187; functions of the sim are not supported on the GPU
+    path, nor is ``swab_delay``).
     """
 
     def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
@@ -140,12 +143,46 @@ class test_prob(Intervention):
 
     def initialize(self, sim):
         super().initialize()
-        for name in ('subtarget', 'ili_prev', 'swab_delay'):
-            if getattr(self, name) is not None:
-                raise NotImplementedError(f'test_prob({name}=...) is not supported on the GPU path')
+        if self.swab_delay is not None:
+            raise NotImplementedError('test_prob(swab_delay=...) is not supported on the GPU path')
         self.start_day = _day(self.start_day, 0)
         self.end_day = _day(self.end_day, None)
         self.days = [self.start_day, self.end_day]
+        self._subtarget = self._fixed_subtarget(self.subtarget, sim['pop_size'])
+        self._ili = self._daily(self.ili_prev, sim.npts)
+
+    @staticmethod
+    def _fixed_subtarget(st, n):
+        """get_subtargets (interventions.py:150-187) for fixed indices and values."""
+        if st is None:
+            return None
+        if callable(st) or (isinstance(st, dict) and (callable(st.get('inds')) or callable(st.get('vals')))):
+            raise NotImplementedError('subtargets given as functions of the sim are not supported on the GPU path')
+        if not isinstance(st, dict) or 'inds' not in st:
+            raise ValueError(f'The subtarget dict must have keys "inds" and "vals", but you supplied {st}')
+        inds = np.asarray(st['inds'], dtype=np.int64).ravel()
+        vals = st['vals']
+        if np.ndim(vals) == 0:
+            vals = np.full(len(inds), float(vals))
+        else:
+            vals = np.asarray(vals, dtype=np.float64).ravel()
+            if len(vals) != len(inds):
+                raise ValueError(f'Length of subtargeting indices ({len(inds)}) does not match length of values '
+                                 f'({len(vals)})')
+        if len(inds) and (inds.min() < 0 or inds.max() >= n):
+            raise ValueError('subtarget indices must be agents of the sim')
+        return inds, vals
+
+    @staticmethod
+    def _daily(x, npts):
+        """process_daily_data (interventions.py:111-147) for a number or a sequence."""
+        if x is None:
+            return None
+        if isinstance(x, numbers.Number):
+            return np.array([float(x)] * npts)
+        if isinstance(x, str) or not hasattr(x, '__len__'):
+            raise NotImplementedError('ili_prev from data columns or dataframes is not supported on the GPU path')
+        return np.asarray(x, dtype=np.float64).ravel()
 
     @staticmethod
     def _quar_policy(qp):
@@ -174,7 +211,8 @@ class test_prob(Intervention):
                     quar_policy=qp, quar_offsets=offs, symp_prob=float(self.symp_prob),
                     asymp_prob=float(self.asymp_prob), symp_quar_prob=float(self.symp_quar_prob),
                     asymp_quar_prob=float(self.asymp_quar_prob), sensitivity=float(self.sensitivity),
-                    loss_prob=float(self.loss_prob), test_delay=int(self.test_delay))
+                    loss_prob=float(self.loss_prob), test_delay=int(self.test_delay),
+                    subtarget=getattr(self, '_subtarget', None), ili_prev=getattr(self, '_ili', None))
 
     def apply(self, sim):
         raise NotImplementedError('test_prob runs on the device as part of the day loop')

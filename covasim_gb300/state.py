@@ -241,6 +241,17 @@ def testing_record(spec):
     return r
 
 
+ILI_TAG = 0x111E
+
+
+def ili_agents(seed, t, n, n_ili):
+    """The n_ili distinct agents with influenza-like symptoms on day t (test_prob's
+    ili_prev, interventions.py:941-947), from a PCG64 stream keyed by (seed, 0x111E,
+    t): they do not depend on the sim's state, so they are drawn on the host."""
+    rng = np.random.default_rng([int(seed) & 0xFFFFFFFFFFFFFFFF, ILI_TAG, int(t)])
+    return np.sort(rng.choice(int(n), int(n_ili), replace=False)).astype(np.int32)
+
+
 # Default of covgpu_state.src_walk: the stored layers are streamed every day.
 # Walking them from the day's sources (set_src_walk) gives the same results; on
 # a 1M-agent hybrid run (62 MB of stored edges, L2-resident) walking below an
@@ -316,6 +327,7 @@ class BatchState:
             t['contact_bits'] = torch.zeros(self.n_contact_layers * words, dtype=I32, device=dev)
             t['pending_quar'] = torch.full((self.pending_slots, n), -1, dtype=I32, device=dev)
             t['trace_count'] = torch.zeros(S, dtype=I32, device=dev)
+            self.testing_tensors = self._testing_extras(dev)
         self.t = t
 
         # per-sim tables, concatenated
@@ -349,6 +361,40 @@ class BatchState:
         self._refresh_state()
 
     # ------------------------------------------------------------------ building
+    def _testing_extras(self, dev):
+        """Device tables of test_prob's subtargets (a threshold per agent) and
+        influenza-like illness (the day's agents, drawn on the host, and the mark
+        array the device writes), set into each sim's testing record."""
+        keep = []
+        for r, sp in zip(self.testing_recs, self.specs):
+            tp = (sp.testing or {}).get('test')
+            if not tp:
+                continue
+            if tp.get('subtarget') is not None:
+                inds, vals = tp['subtarget']
+                thr = np.full(sp.n, L.NO_SUBTARGET, dtype=np.uint64)
+                thr[inds] = np.array([prob_threshold(v) for v in vals], dtype=np.uint64)
+                tt = torch.from_numpy(thr.view(np.int64)).to(dev)
+                r.sub_thr = tt.data_ptr()
+                keep.append(tt)
+            if tp.get('ili_prev') is not None:
+                daily = np.asarray(tp['ili_prev'], dtype=np.float64)
+                start = int(tp['start_day'])
+                days = max(0, min(len(daily), sp.npts - start))
+                seed = int(sp.pars['rand_seed'])
+                lists = [ili_agents(seed, start + d, sp.n, int(daily[d] * sp.n)) for d in range(days)]
+                off = np.zeros(days + 1, dtype=np.int64)
+                off[1:] = np.cumsum([len(x) for x in lists])
+                inds = np.concatenate(lists) if lists else np.zeros(0, dtype=np.int32)
+                t_off = torch.from_numpy(off).to(dev)
+                t_inds = torch.from_numpy(np.ascontiguousarray(inds, dtype=np.int32) if len(inds)
+                                          else np.zeros(1, dtype=np.int32)).to(dev)
+                t_mark = torch.full((max(sp.n, 1),), -1, dtype=I32, device=dev)
+                r.ili_off, r.ili_inds, r.ili_mark, r.ili_days = (t_off.data_ptr(), t_inds.data_ptr(),
+                                                                  t_mark.data_ptr(), days)
+                keep += [t_off, t_inds, t_mark]
+        return keep
+
     def _build_imports(self):
         """Every sim's daily importations as one device table ordered by day, then
         sim (``covgpu_state.imports``), with the per-day counts kept on the host for

@@ -130,7 +130,23 @@ typedef struct covgpu_testing {
   uint64_t thr_trace[COVGPU_MAX_LAYERS];       /* per-layer trace_probs; 0: not traced */
   int32_t trace_start_off[COVGPU_MAX_LAYERS];  /* int(trace_time): quarantine start offset */
   int32_t trace_period[COVGPU_MAX_LAYERS];     /* int(quar_period - trace_time)        */
+  /* test_prob's subtarget (interventions.py:150-187, 970-972): per local agent the
+   * threshold of its fixed test probability, COVGPU_NO_SUBTARGET for none (NULL: no
+   * subtarget); applied after the symptom and quarantine probabilities, before the
+   * diagnosed are set to 0 */
+  const uint64_t* sub_thr;
+  /* test_prob's influenza-like illness (interventions.py:941-947): the agents of day
+   * test_start + d are ili_inds[ili_off[d] .. ili_off[d + 1]) (local indices), for
+   * d < ili_days; ili_mark [n_agents] is the last day an agent was marked (written by
+   * the test pass's first kernel; NULL: no ILI). A marked agent without COVID
+   * symptoms tests with the symptomatic probability. */
+  const int64_t* ili_off;
+  const int32_t* ili_inds;
+  int32_t* ili_mark;
+  int32_t ili_days;
+  int32_t _pad_ili;
 } covgpu_testing;
+#define COVGPU_NO_SUBTARGET 0xFFFFFFFFFFFFFFFFull
 
 /* One sim's parameter block (device memory, one entry per sim). */
 typedef struct covgpu_sim_params {

@@ -227,3 +227,33 @@ def test_infection_log_layer_tags_round_trip():
     assert extra == ['custom', 'other']
     assert log_layer_tag('seed_infection', keys, extra) == L.LOG_SEED
     assert log_layer_tag('importation', keys, extra) == L.LOG_IMPORT
+
+
+def test_test_prob_subtarget_and_ili_inputs():
+    """get_subtargets (interventions.py:150-187) with fixed indices and values and
+    process_daily_data (interventions.py:111-147) for ILI prevalence, as the host
+    prepares them; the ILI agents are the oracle's draws in its Philox mode."""
+    from covasim_gb300.interventions import test_prob
+    from covasim_gb300.state import ili_agents
+    from oracle.interventions import ili_agents as oracle_ili
+    inds, vals = test_prob._fixed_subtarget(dict(inds=[4, 9, 2], vals=0.25), 10)
+    np.testing.assert_array_equal(inds, [4, 9, 2])
+    np.testing.assert_array_equal(vals, [0.25, 0.25, 0.25])
+    inds, vals = test_prob._fixed_subtarget(dict(inds=np.array([1, 3]), vals=[0.1, 0.9]), 10)
+    np.testing.assert_array_equal(vals, [0.1, 0.9])
+    with pytest.raises(ValueError):
+        test_prob._fixed_subtarget(dict(inds=[1, 2], vals=[0.1]), 10)
+    with pytest.raises(ValueError):
+        test_prob._fixed_subtarget(dict(vals=[0.1]), 10)
+    with pytest.raises(ValueError):
+        test_prob._fixed_subtarget(dict(inds=[10], vals=0.5), 10)
+    with pytest.raises(NotImplementedError):
+        test_prob._fixed_subtarget(dict(inds=lambda sim: [1], vals=0.5), 10)
+    np.testing.assert_array_equal(test_prob._daily(0.02, 4), [0.02] * 4)
+    np.testing.assert_array_equal(test_prob._daily([0.01, 0.03], 10), [0.01, 0.03])
+    with pytest.raises(NotImplementedError):
+        test_prob._daily('data', 10)
+    for seed, t, n, k in ((1, 0, 1000, 20), (7, 33, 5000, 250), (3, 2, 10, 10)):
+        got = ili_agents(seed, t, n, k)
+        assert len(np.unique(got)) == k and got.min() >= 0 and got.max() < n
+        np.testing.assert_array_equal(got, oracle_ili(seed, t, n, k))

@@ -26,6 +26,15 @@ CASES = [
      dict(trace_probs=0.8, presumptive=True, start_day=8)),
     ('hybrid', 2000, 40, 4, False, True, dict(symp_prob=0.3, quar_policy=[0, 2]),
      dict(trace_probs=0.7, trace_time=0.5, quar_period=10)),
+    # influenza-like illness (a constant and a daily prevalence) and fixed subtargets
+    ('hybrid', 3000, 45, 5, True, True,
+     dict(symp_prob=0.2, asymp_prob=0.005, quar_policy='both', ili_prev=0.02,
+          subtarget=dict(inds=list(range(0, 3000, 7)), vals=0.3)),
+     dict(trace_probs=0.5, trace_time=1)),
+    ('random', 2500, 45, 6, False, False,
+     dict(symp_prob=0.3, start_day=3, ili_prev=[0.01] * 8 + [0.05] * 12,
+          subtarget=dict(inds=list(range(3, 2500, 11)), vals=[0.05 + 0.45 * (k % 3) for k in range(227)])),
+     dict(trace_probs=0.6)),
 ]
 
 
@@ -52,6 +61,17 @@ def test_testing_and_tracing_match_oracle_philox(case):
     raw = sim.raw_results()
     assert raw['new_tests'].sum() > 0 and raw['new_diagnoses'].sum() > 0 and raw['new_quarantined'].sum() > 0
     compare_runs(sim, orc, keys=TESTING_KEYS)
+
+
+def test_ili_and_subtargets_add_tests():
+    """interventions.py:941-972: the day's influenza-like illnesses test with the
+    symptomatic probability, subtargeted agents with their own."""
+    base = dict(symp_prob=0.2, asymp_prob=0.005)
+    tests = []
+    for extra in ({}, dict(ili_prev=0.05), dict(subtarget=dict(inds=list(range(0, 3000, 5)), vals=0.5))):
+        sim = make_sim('hybrid', 3000, 30, 9, True, False, dict(base, **extra), dict(trace_probs=0.5))
+        tests.append(sim.run().raw_results()['new_tests'].sum())
+    assert tests[1] > 1.5 * tests[0] and tests[2] > 1.5 * tests[0], tests
 
 
 def test_testing_step_mode_equals_graph_run():
