@@ -5,8 +5,8 @@ it as the checker.
 
 ``TestProb`` restates ``test_prob`` (covasim/interventions.py:858-981) and
 ``ContactTracing`` restates ``contact_tracing`` (covasim/interventions.py:984-1145),
-for the options the GPU path supports (ILI prevalence and fixed subtargets;
-no swab-delay distribution, no tracing capacity). Their random draws come
+for the options the GPU path supports (swab delays, ILI prevalence and fixed
+subtargets; no tracing capacity). Their random draws come
 from the oracle sim: the numpy MT19937 stream in the reference's call order
 (``rng='mt'``), or Philox keyed by (agent, day) and (agent, layer, day) like
 the CUDA library's, with the day's ILI agents from a PCG64 stream keyed by
@@ -58,6 +58,21 @@ def ili_agents(seed, t, n, n_ili):
     return np.sort(rng.choice(int(n), int(n_ili), replace=False)).astype(np.int64)
 
 
+def swab_pdf(dist=None, par1=None, par2=None):
+    """get_pdf (utils.py:240-268): the frozen scipy distribution of the delay from
+    symptom onset to swab, or None."""
+    import scipy.stats as sps
+    if dist in ('None', 'none', None):
+        return None
+    if dist == 'uniform':
+        return sps.uniform(loc=par1, scale=par2)
+    if dist == 'lognormal':
+        mean = np.log(par1**2 / np.sqrt(par2 + par1**2))
+        sigma = np.sqrt(np.log(par2 / par1**2 + 1))
+        return sps.lognorm(sigma, loc=-0.5, scale=np.exp(mean))
+    raise NotImplementedError(f'The selected distribution "{dist}" is not implemented')
+
+
 def daily_series(x, npts):
     """process_daily_data (interventions.py:111-147) for a number or a sequence."""
     if isinstance(x, (int, float, np.integer, np.floating)):
@@ -66,14 +81,13 @@ def daily_series(x, npts):
 
 
 class TestProb:
-    """interventions.py:858-981 (swab_delay unsupported; subtarget a dict of fixed
-    ``inds`` and ``vals``)."""
+    """interventions.py:858-981 (subtarget a dict of fixed ``inds`` and ``vals``)."""
 
     __test__ = False  # not a pytest test class
 
     def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
                  subtarget=None, ili_prev=None, sensitivity=1.0, loss_prob=0.0, test_delay=0, start_day=0,
-                 end_day=None):
+                 end_day=None, swab_delay=None):
         self.symp_prob = symp_prob
         self.asymp_prob = asymp_prob
         self.symp_quar_prob = symp_quar_prob if symp_quar_prob is not None else symp_prob
@@ -81,6 +95,7 @@ class TestProb:
         self.quar_policy = quar_policy if quar_policy else 'start'
         self.subtarget = subtarget
         self.ili_prev = ili_prev
+        self.pdf = swab_pdf(**(swab_delay or {}))
         self.sensitivity = sensitivity
         self.loss_prob = loss_prob
         self.test_delay = test_delay
@@ -94,6 +109,16 @@ class TestProb:
         people = sim.people
         n = sim.n
         symp_inds = people.symptomatic.nonzero()[0]
+        symp_prob = self.symp_prob
+        if self.pdf:  # the swab delay's distribution (interventions.py:930-938)
+            symp_time = (t - people.date_symptomatic[symp_inds]).astype(np.int32)
+            inv_count = np.bincount(symp_time) / len(symp_time)
+            count = np.nan * np.ones(inv_count.shape)
+            count[inv_count != 0] = 1 / inv_count[inv_count != 0]
+            symp_prob = np.ones(len(symp_time))
+            inds = 1 > (symp_time * self.symp_prob)
+            symp_prob[inds] = self.symp_prob / (1 - symp_time[inds] * self.symp_prob)
+            symp_prob = self.pdf.pdf(symp_time) * symp_prob * count[symp_time]
         # symptomatics of influenza-like illness, drawn before the tests (interventions.py:941-947)
         ili_inds = np.array([], dtype=np.int64)
         if self.ili_prev is not None:
@@ -112,7 +137,7 @@ class TestProb:
         asymp_quar_inds = np.intersect1d(quar_test_inds, asymp_inds)
         diag_inds = people.diagnosed.nonzero()[0]
         test_probs = np.zeros(n)
-        test_probs[symp_inds] = self.symp_prob
+        test_probs[symp_inds] = symp_prob
         test_probs[ili_inds] = self.symp_prob
         test_probs[asymp_inds] = self.asymp_prob
         test_probs[symp_quar_inds] = self.symp_quar_prob

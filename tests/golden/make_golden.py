@@ -427,6 +427,13 @@ TESTING_CASES = [  # (pop_type, n, days, seed, use_waning, dynamic c, test_prob 
      dict(symp_prob=0.3, start_day=3, ili_prev=[0.01] * 8 + [0.05] * 12,
           subtarget=dict(inds=list(range(3, 1200, 11)), vals=[0.05 + 0.9 * (k % 3) / 2 for k in range(109)])),
      dict(trace_probs=0.6)),
+    # a distribution of delays from symptom onset to swab
+    ('hybrid', 1500, 40, 9, True, 0,
+     dict(symp_prob=0.25, asymp_prob=0.01, swab_delay=dict(dist='lognormal', par1=3, par2=4)),
+     dict(trace_probs=0.5, trace_time=1)),
+    ('random', 1200, 40, 10, False, 0,
+     dict(symp_prob=0.4, quar_policy='daily', swab_delay=dict(dist='uniform', par1=0, par2=5), ili_prev=0.01),
+     dict(trace_probs=0.7)),
 ]
 TESTING_FINAL = ['diagnosed', 'quarantined', 'isolated', 'known_contact', 'tested', 'date_diagnosed',
                  'date_quarantined', 'date_end_quarantine', 'date_known_contact', 'date_pos_test', 'date_tested',
