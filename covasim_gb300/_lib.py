@@ -69,6 +69,8 @@ class Testing(C.Structure):
         ('trace_start_off', C.c_int32 * MAX_LAYERS), ('trace_period', C.c_int32 * MAX_LAYERS),
         ('sub_thr', C.c_void_p), ('ili_off', C.c_void_p), ('ili_inds', C.c_void_p), ('ili_mark', C.c_void_p),
         ('ili_days', C.c_int32), ('_pad_ili', C.c_int32),
+        ('swab_pdf', C.c_void_p), ('swab_bins', C.c_void_p), ('symp_prob', C.c_double), ('swab_len', C.c_int32),
+        ('_pad_swab', C.c_int32),
     ]
 
 

@@ -43,6 +43,32 @@ __device__ __forceinline__ bool quar_tester(const covgpu_state& st, const covgpu
   return q;
 }
 
+// whole days since symptom onset, as test_prob forms them: the float32 difference
+// t - date_symptomatic truncated to int32 (cvd.default_int)
+__device__ __forceinline__ int symp_days(const covgpu_state& st, int64_t i, int t) {
+  return (int)__fsub_rn((float)t, date_row(st, COVGPU_DATE_SYMPTOMATIC)[i]);
+}
+
+// ceil(p * 2^53) (the host's prob_threshold): the Bernoulli threshold of a float64 p
+__device__ __forceinline__ uint64_t prob_thr(double p) {
+  if (!(p > 0.0)) return 0ull;
+  if (p >= 1.0) return (1ull << 53) + 1ull;
+  return __double2ull_ru(__dmul_rn(p, 9007199254740992.0));
+}
+
+// test_prob's symptomatic probability under a swab delay (interventions.py:930-938):
+// pdf(days) * adjusted symp_prob * (symptomatic agents / those with the same days),
+// in float64 with the reference's operations and order
+__device__ __forceinline__ uint64_t swab_threshold(const covgpu_state& st, const covgpu_testing& T, int64_t i, int t) {
+  const int d = symp_days(st, i, t);
+  if (d < 0 || d >= T.swab_len) return 0ull;
+  const double inv = __ddiv_rn((double)T.swab_bins[d], (double)T.swab_bins[T.swab_len]);
+  const double cnt = __ddiv_rn(1.0, inv);
+  const double x = __dmul_rn((double)d, T.symp_prob);
+  const double adj = 1.0 > x ? __ddiv_rn(T.symp_prob, __dsub_rn(1.0, x)) : 1.0;
+  return prob_thr(__dmul_rn(__dmul_rn(T.swab_pdf[d], adj), cnt));
+}
+
 // test_prob.apply (interventions.py:921-981) + People.test (people.py:589-617),
 // then the trace bits of contact_tracing.select_cases (interventions.py:1066-1072)
 // One agent block of the test pass (thread k on agent begin + k); the tested are
@@ -71,9 +97,10 @@ __device__ __forceinline__ void test_block(const covgpu_state& st, int t, const 
         // never the quarantine ones (interventions.py:966-969)
         if (!symp && T.ili_mark && T.ili_mark[loc] == t)
           thr = T.thr_symp;
+        else if (quar_tester(st, T, i, t, f))
+          thr = symp ? T.thr_symp_quar : T.thr_asymp_quar;
         else
-          thr = quar_tester(st, T, i, t, f) ? (symp ? T.thr_symp_quar : T.thr_asymp_quar)
-                                            : (symp ? T.thr_symp : T.thr_asymp);
+          thr = !symp ? T.thr_asymp : (T.swab_pdf ? swab_threshold(st, T, i, t) : T.thr_symp);
         if (T.sub_thr) {  // subtargets (interventions.py:970-972)
           const uint64_t sv = T.sub_thr[loc];
           if (sv != COVGPU_NO_SUBTARGET) thr = sv;
@@ -118,15 +145,19 @@ __device__ __forceinline__ void test_flush(const covgpu_state& st, int t, int si
   tested_acc = 0;
 }
 
-// test_prob's influenza-like illness of day t (interventions.py:941-947): the day's
-// agents, drawn on the host (they do not depend on the state), are marked with t
-// before the test pass reads the marks; one block per sim
-__global__ void k_ili_mark(covgpu_state st, int t) {
+// The per-sim preparation of day t's test pass, one block per sim:
+// test_prob's swab-delay histogram is cleared (k_swab_hist fills it), and the
+// day's influenza-like illnesses (interventions.py:941-947), drawn on the host
+// (they do not depend on the state), are marked with t.
+__global__ void k_test_prep(covgpu_state st, int t) {
   if (held(st, t)) return;
   const int s = blockIdx.x;
   if (s >= st.n_sims) return;
   const covgpu_testing& T = st.sims[s].testing;
-  if (!T.ili_mark || !day_active(t, T.test_start, T.test_end)) return;
+  if (!day_active(t, T.test_start, T.test_end)) return;
+  if (T.swab_pdf)
+    for (int k = threadIdx.x; k <= T.swab_len; k += blockDim.x) T.swab_bins[k] = 0;
+  if (!T.ili_mark) return;
   const int d = t - T.test_start;
   if (d < 0 || d >= T.ili_days) return;
   const int n = st.sims[s].n_agents;
@@ -144,6 +175,24 @@ __device__ __forceinline__ bool agent_range(const covgpu_state& st, int64_t& b, 
   b = (int64_t)blockIdx.x * per;
   b_end = min(nb, b + per);
   return b < b_end;
+}
+
+// test_prob's swab-delay histogram of day t (interventions.py:931-932): the
+// symptomatic agents by whole days since onset, and their total in the last bin
+__global__ void __launch_bounds__(AGENT_THREADS) k_swab_hist(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  int64_t b, b_end;
+  if (!agent_range(st, b, b_end)) return;
+  for (; b < b_end; ++b) {
+    const covgpu_agent_block blk = st.agent_blocks[b];
+    const covgpu_testing& T = st.sims[blk.sim].testing;
+    if (!T.swab_pdf || !day_active(t, T.test_start, T.test_end)) continue;  // uniform over the agent block
+    const int64_t i = blk.begin + threadIdx.x;
+    if (i >= blk.end || !(st.flags[i] & B_SYMP)) continue;
+    const int d = symp_days(st, i, t);
+    if (d >= 0 && d < T.swab_len) atomicAdd(T.swab_bins + d, 1);
+    atomicAdd(T.swab_bins + T.swab_len, 1);
+  }
 }
 
 __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
@@ -468,7 +517,11 @@ namespace covgpu {
 
 int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   if (!st->has_testing) return COVGPU_OK;
-  k_ili_mark<<<(unsigned)st->n_sims, 256, 0, s>>>(*st, t);
+  k_test_prep<<<(unsigned)st->n_sims, 256, 0, s>>>(*st, t);
+  if (st->has_testing & 2) {  // some sim has a swab delay
+    static const int64_t hist_wave = wave_blocks(k_swab_hist, AGENT_THREADS);
+    k_swab_hist<<<wave_grid(st, hist_wave), AGENT_THREADS, 0, s>>>(*st, t);
+  }
   static const int64_t test_wave = wave_blocks(k_test_pass, AGENT_THREADS);
   k_test_pass<<<wave_grid(st, test_wave), AGENT_THREADS, 0, s>>>(*st, t);
   if (st->n_tiles > 0) {

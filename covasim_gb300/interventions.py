@@ -116,11 +116,12 @@ def _day(d, default):
 
 class test_prob(Intervention):
     """Test each agent with a probability set by its symptom and quarantine state
-    (interventions.py:858-981). Same arguments as the reference: ``ili_prev`` a
-    number or a daily sequence (process_daily_data, interventions.py:111-147),
-    ``subtarget`` a dict of fixed ``inds`` and ``vals`` (get_subtargets,
-    interventions.py:150-187; functions of the sim are not supported on the GPU
-    path, nor is ``swab_delay``).
+    (interventions.py:858-981). Same arguments as the reference: ``swab_delay`` a
+    dict of ``dist`` ('uniform' or 'lognormal'), ``par1`` and ``par2`` (get_pdf,
+    utils.py:240-268), ``ili_prev`` a number or a daily sequence
+    (process_daily_data, interventions.py:111-147), ``subtarget`` a dict of fixed
+    ``inds`` and ``vals`` (get_subtargets, interventions.py:150-187; functions of
+    the sim are not supported on the GPU path).
     """
 
     def __init__(self, symp_prob, asymp_prob=0.0, symp_quar_prob=None, asymp_quar_prob=None, quar_policy=None,
@@ -143,13 +144,32 @@ class test_prob(Intervention):
 
     def initialize(self, sim):
         super().initialize()
-        if self.swab_delay is not None:
-            raise NotImplementedError('test_prob(swab_delay=...) is not supported on the GPU path')
         self.start_day = _day(self.start_day, 0)
         self.end_day = _day(self.end_day, None)
         self.days = [self.start_day, self.end_day]
         self._subtarget = self._fixed_subtarget(self.subtarget, sim['pop_size'])
         self._ili = self._daily(self.ili_prev, sim.npts)
+        self._swab_pdf = self._swab_table(self.swab_delay, sim.npts)
+
+    @staticmethod
+    def _swab_table(swab_delay, npts):
+        """The density of the delay from symptom onset to swab (get_pdf, utils.py:240-268:
+        uniform, or lognormal of the given mean and variance) at 0 .. npts days, or None."""
+        d = dict(swab_delay or {})
+        dist, par1, par2 = d.get('dist'), d.get('par1'), d.get('par2')
+        if dist in ('None', 'none', None):
+            return None
+        import scipy.stats as sps
+        if dist == 'uniform':
+            pdf = sps.uniform(loc=par1, scale=par2)
+        elif dist == 'lognormal':
+            mean = np.log(par1**2 / np.sqrt(par2 + par1**2))
+            sigma = np.sqrt(np.log(par2 / par1**2 + 1))
+            pdf = sps.lognorm(sigma, loc=-0.5, scale=np.exp(mean))
+        else:
+            raise NotImplementedError(f'The selected distribution "{dist}" is not implemented; choices are: none, '
+                                      'uniform, lognormal')
+        return np.asarray(pdf.pdf(np.arange(npts + 1, dtype=np.int32)), dtype=np.float64)
 
     @staticmethod
     def _fixed_subtarget(st, n):
@@ -212,7 +232,8 @@ class test_prob(Intervention):
                     asymp_prob=float(self.asymp_prob), symp_quar_prob=float(self.symp_quar_prob),
                     asymp_quar_prob=float(self.asymp_quar_prob), sensitivity=float(self.sensitivity),
                     loss_prob=float(self.loss_prob), test_delay=int(self.test_delay),
-                    subtarget=getattr(self, '_subtarget', None), ili_prev=getattr(self, '_ili', None))
+                    subtarget=getattr(self, '_subtarget', None), ili_prev=getattr(self, '_ili', None),
+                    swab_pdf=getattr(self, '_swab_pdf', None))
 
     def apply(self, sim):
         raise NotImplementedError('test_prob runs on the device as part of the day loop')

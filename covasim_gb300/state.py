@@ -314,6 +314,8 @@ class BatchState:
         # testing and tracing (interventions.py:858-1145): bitmaps, scheduled quarantines
         self.testing_recs = [testing_record(sp) for sp in self.specs]
         self.has_testing = any(sp.testing for sp in self.specs)
+        self.has_swab = any((sp.testing or {}).get('test') and sp.testing['test'].get('swab_pdf') is not None
+                            for sp in self.specs)
         self.pending_slots = 1
         self.n_contact_layers = max(len(sp.layers) for sp in self.specs) or 1
         if self.has_testing:
@@ -393,6 +395,12 @@ class BatchState:
                 r.ili_off, r.ili_inds, r.ili_mark, r.ili_days = (t_off.data_ptr(), t_inds.data_ptr(),
                                                                   t_mark.data_ptr(), days)
                 keep += [t_off, t_inds, t_mark]
+            if tp.get('swab_pdf') is not None:
+                pdf = torch.from_numpy(np.ascontiguousarray(tp['swab_pdf'], dtype=np.float64)).to(dev)
+                bins = torch.zeros(len(tp['swab_pdf']) + 1, dtype=I32, device=dev)
+                r.swab_pdf, r.swab_bins, r.swab_len = pdf.data_ptr(), bins.data_ptr(), len(tp['swab_pdf'])
+                r.symp_prob = float(tp['symp_prob'])
+                keep += [pdf, bins]
         return keep
 
     def _build_imports(self):
@@ -851,7 +859,7 @@ class BatchState:
         st.segments = self.seg_dev.data_ptr() if self.segments else None
         st.agent_blocks = self.blocks_dev.data_ptr()
         st.draw_table = self.draw_table.data_ptr() if self.draw_table is not None else None
-        st.has_testing = int(self.has_testing)
+        st.has_testing = int(self.has_testing) | (2 if self.has_swab else 0)
         st.pending_slots = self.pending_slots
         st.n_contact_layers = self.n_contact_layers
         if self.has_testing:

@@ -145,6 +145,16 @@ typedef struct covgpu_testing {
   int32_t* ili_mark;
   int32_t ili_days;
   int32_t _pad_ili;
+  /* test_prob's swab delay (interventions.py:930-938; NULL swab_pdf: none): swab_pdf
+   * [swab_len] the delay distribution's density at 0, 1, ... days (computed on the
+   * host); swab_bins [swab_len + 1] the day's symptomatic agents by whole days since
+   * symptom onset, and their total (zeroed and filled on the device before the test
+   * pass); symp_prob the float64 symptomatic probability */
+  const double* swab_pdf;
+  int32_t* swab_bins;
+  double symp_prob;
+  int32_t swab_len;
+  int32_t _pad_swab;
 } covgpu_testing;
 #define COVGPU_NO_SUBTARGET 0xFFFFFFFFFFFFFFFFull
 
@@ -327,7 +337,8 @@ typedef struct covgpu_state {
   const double* draw_table;
   const double* const* edge_uniforms; /* [n_segments] -> [n_variants][2][n_edges] */
   /* testing and tracing (all NULL / 0 when no sim tests) */
-  int32_t has_testing;            /* 1: run the testing, tracing and post passes     */
+  int32_t has_testing;            /* bit 0: run the testing, tracing and post passes;
+                                     bit 1: some sim's test_prob has a swab delay     */
   int32_t pending_slots;          /* R: days of scheduled quarantines kept ahead     */
   uint32_t* trace_bits;           /* [ceil(n/32)] agents traced today                */
   uint32_t* contact_bits;         /* [n_contact_layers][ceil(n/32)] contacts found   */

@@ -35,6 +35,13 @@ CASES = [
      dict(symp_prob=0.3, start_day=3, ili_prev=[0.01] * 8 + [0.05] * 12,
           subtarget=dict(inds=list(range(3, 2500, 11)), vals=[0.05 + 0.45 * (k % 3) for k in range(227)])),
      dict(trace_probs=0.6)),
+    # distributions of delays from symptom onset to swab
+    ('hybrid', 3000, 45, 7, True, True,
+     dict(symp_prob=0.25, asymp_prob=0.01, swab_delay=dict(dist='lognormal', par1=3, par2=4)),
+     dict(trace_probs=0.5, trace_time=1)),
+    ('random', 2500, 45, 8, False, False,
+     dict(symp_prob=0.4, quar_policy='daily', swab_delay=dict(dist='uniform', par1=0, par2=5), ili_prev=0.01),
+     dict(trace_probs=0.7)),
 ]
 
 
