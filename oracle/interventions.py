@@ -5,8 +5,8 @@ it as the checker.
 
 ``TestProb`` restates ``test_prob`` (covasim/interventions.py:858-981) and
 ``ContactTracing`` restates ``contact_tracing`` (covasim/interventions.py:984-1145),
-for the options the GPU path supports (swab delays, ILI prevalence and fixed
-subtargets; no tracing capacity). Their random draws come
+for the options the GPU path supports (swab delays, ILI prevalence, fixed
+subtargets and tracing capacity). Their random draws come
 from the oracle sim: the numpy MT19937 stream in the reference's call order
 (``rng='mt'``), or Philox keyed by (agent, day) and (agent, layer, day) like
 the CUDA library's, with the day's ILI agents from a PCG64 stream keyed by
@@ -161,16 +161,17 @@ class TestProb:
 
 
 class ContactTracing:
-    """interventions.py:984-1145 (capacity unsupported)."""
+    """interventions.py:984-1145."""
 
     def __init__(self, trace_probs=None, trace_time=None, start_day=0, end_day=None, presumptive=False,
-                 quar_period=None):
+                 quar_period=None, capacity=None):
         self.trace_probs = trace_probs
         self.trace_time = trace_time
         self.start_day = start_day
         self.end_day = end_day
         self.presumptive = presumptive
         self.quar_period = quar_period
+        self.capacity = capacity
 
     def initialize(self, sim):
         """interventions.py:1023-1041."""
@@ -195,6 +196,14 @@ class ContactTracing:
         else:
             just_tested = (people.date_tested == t).nonzero()[0]
             trace_inds = just_tested[people.exposed[just_tested]]
+        if self.capacity is not None:  # interventions.py:1074-1078
+            capacity = int(self.capacity / sim.rescale_vec[t])
+            if len(trace_inds) > capacity:
+                if sim.rng == 'philox':  # the capacity cases with the smallest keys
+                    keys = ph.capacity_keys(sim.k0, sim.k1, t, trace_inds)
+                    trace_inds = np.sort(trace_inds[np.argsort(keys, kind='stable')[:capacity]])
+                else:
+                    trace_inds = sim.rs_numpy.choice(trace_inds, capacity, replace=False)
         if not len(trace_inds):
             return {}
         contacts = {}

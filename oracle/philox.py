@@ -308,6 +308,15 @@ def test_draws(k0, k1, day, agents):
     return u01_52(b0[0], b0[1]), u01_52(b0[2], b0[3]), u01_52(b1[0], b1[1])
 
 
+def capacity_keys(k0, k1, day, agents):
+    """contact_tracing's capacity in philox mode: each case's 64-bit selection key,
+    the x word of Philox (agent, 2, day, TAG_TEST) above the agent's index (unique);
+    the day's ``capacity`` cases with the smallest keys are traced."""
+    a = np.asarray(agents, dtype=np.int64)
+    b = philox4x32_10(a, 2, day, TAG_TEST, k0, k1)
+    return (np.asarray(b[0], dtype=np.uint64) << np.uint64(32)) | a.astype(np.uint64)
+
+
 def trace_draws(k0, k1, day, layer, agents):
     """The uniform deciding whether a contact of a traced case in ``layer`` is reached."""
     a = np.asarray(agents, dtype=np.int64)

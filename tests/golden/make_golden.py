@@ -434,6 +434,10 @@ TESTING_CASES = [  # (pop_type, n, days, seed, use_waning, dynamic c, test_prob 
     ('random', 1200, 40, 10, False, 0,
      dict(symp_prob=0.4, quar_policy='daily', swab_delay=dict(dist='uniform', par1=0, par2=5), ili_prev=0.01),
      dict(trace_probs=0.7)),
+    # a tracing capacity below the day's cases
+    ('hybrid', 1500, 40, 11, True, 0, dict(symp_prob=0.4, asymp_prob=0.02), dict(trace_probs=0.8, capacity=3)),
+    ('random', 1200, 40, 12, False, 0, dict(symp_prob=0.5, test_delay=1),
+     dict(trace_probs=0.9, presumptive=True, capacity=2)),
 ]
 TESTING_FINAL = ['diagnosed', 'quarantined', 'isolated', 'known_contact', 'tested', 'date_diagnosed',
                  'date_quarantined', 'date_end_quarantine', 'date_known_contact', 'date_pos_test', 'date_tested',
