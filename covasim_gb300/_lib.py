@@ -71,6 +71,7 @@ class Testing(C.Structure):
         ('ili_days', C.c_int32), ('_pad_ili', C.c_int32),
         ('swab_pdf', C.c_void_p), ('swab_bins', C.c_void_p), ('symp_prob', C.c_double), ('swab_len', C.c_int32),
         ('_pad_swab', C.c_int32),
+        ('capacity', C.c_double), ('cap_scale', C.c_double), ('cap_list', C.c_void_p), ('cap_count', C.c_void_p),
     ]
 
 

@@ -133,6 +133,12 @@ __device__ __forceinline__ void test_block(const covgpu_state& st, int t, const 
   }
   const uint32_t tm = __ballot_sync(0xffffffffu, trace);
   if (trace_on && lane == 0 && blk.begin + warp * 32 < blk.end) st.trace_bits[(blk.begin + warp * 32) >> 5] = tm;
+  if (tm && T.cap_list) {  // the day's cases, for the capacity's selection (k_trace_cap)
+    uint32_t base = 0u;
+    if (lane == 0) base = atomicAdd(T.cap_count, (uint32_t)__popc(tm));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (trace) T.cap_list[base + __popc(tm & ((1u << lane) - 1u))] = (int32_t)(i - sp.agent_off);
+  }
   tested_acc += tested;
   if (lane == 0 && tm) atomicAdd(st.trace_count + blk.sim, (unsigned)__popc(tm));
 }
@@ -157,6 +163,7 @@ __global__ void k_test_prep(covgpu_state st, int t) {
   if (!day_active(t, T.test_start, T.test_end)) return;
   if (T.swab_pdf)
     for (int k = threadIdx.x; k <= T.swab_len; k += blockDim.x) T.swab_bins[k] = 0;
+  if (T.cap_list && threadIdx.x == 0) *T.cap_count = 0u;
   if (!T.ili_mark) return;
   const int d = t - T.test_start;
   if (d < 0 || d >= T.ili_days) return;
@@ -193,6 +200,64 @@ __global__ void __launch_bounds__(AGENT_THREADS) k_swab_hist(covgpu_state st, in
     if (d >= 0 && d < T.swab_len) atomicAdd(T.swab_bins + d, 1);
     atomicAdd(T.swab_bins + T.swab_len, 1);
   }
+}
+
+// contact_tracing's capacity (interventions.py:1074-1078), one block per sim: when
+// the day's cases exceed int(capacity / scale), a radix select over their unique
+// 64-bit keys finds the capacity-th smallest, and the trace bits of the cases above
+// it are cleared (a uniform random subset of exactly that size)
+__device__ __forceinline__ uint64_t cap_key(const covgpu_sim_params& sp, int32_t local, int t) {
+  const uint4 w = philox(make_uint4((uint32_t)local, 2u, (uint32_t)t, TAG_TEST), sp.key0, sp.key1);
+  return ((uint64_t)w.x << 32) | (uint32_t)local;
+}
+__global__ void k_trace_cap(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  const int s = blockIdx.x;
+  if (s >= st.n_sims) return;
+  const covgpu_sim_params& sp = st.sims[s];
+  const covgpu_testing& T = sp.testing;
+  if (!T.cap_list || !day_active(t, T.trace_start, T.trace_end)) return;
+  const double scale = sp.rescale_vec ? sp.rescale_vec[t] : T.cap_scale;
+  const double capd = T.capacity / scale;
+  const uint32_t c = *T.cap_count;
+  const int64_t cap = capd < 0.0 ? 0 : (int64_t)capd;
+  if ((int64_t)c <= cap) return;
+  __shared__ unsigned int hist[256];
+  __shared__ unsigned long long s_prefix;
+  __shared__ unsigned int s_rank;
+  unsigned long long prefix = 0ull, mask = 0ull;
+  unsigned int rank = (unsigned int)cap;  // the rank (1-based) of the largest key kept
+  if (rank > 0) {
+    for (int shift = 56; shift >= 0; shift -= 8) {
+      for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0u;
+      __syncthreads();
+      for (uint32_t j = threadIdx.x; j < c; j += blockDim.x) {
+        const uint64_t key = cap_key(sp, T.cap_list[j], t);
+        if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned int cum = 0u;
+        int d = 0;
+        while (d < 255 && cum + hist[d] < rank) cum += hist[d++];
+        s_prefix = prefix | ((unsigned long long)d << shift);
+        s_rank = rank - cum;
+      }
+      __syncthreads();
+      prefix = s_prefix;
+      rank = s_rank;
+      mask |= 0xFFull << shift;
+      __syncthreads();
+    }
+  }
+  for (uint32_t j = threadIdx.x; j < c; j += blockDim.x) {
+    const int32_t local = T.cap_list[j];
+    if (cap == 0 || cap_key(sp, local, t) > prefix) {
+      const int64_t i = sp.agent_off + local;
+      atomicAnd(st.trace_bits + (i >> 5), ~(1u << (i & 31)));
+    }
+  }
+  if (threadIdx.x == 0) st.trace_count[s] = (uint32_t)cap;
 }
 
 __global__ void __launch_bounds__(AGENT_THREADS) k_test_pass(covgpu_state st, int t) {
@@ -524,6 +589,7 @@ int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   }
   static const int64_t test_wave = wave_blocks(k_test_pass, AGENT_THREADS);
   k_test_pass<<<wave_grid(st, test_wave), AGENT_THREADS, 0, s>>>(*st, t);
+  if (st->has_testing & 4) k_trace_cap<<<(unsigned)st->n_sims, 256, 0, s>>>(*st, t);  // a tracing capacity
   if (st->n_tiles > 0) {
     const dim3 grid((unsigned)st->n_tiles);
     switch (st->edge_tile) {

@@ -241,7 +241,7 @@ class test_prob(Intervention):
 
 class contact_tracing(Intervention):
     """Trace the contacts of the diagnosed (interventions.py:984-1145). Same
-    arguments as the reference; ``capacity`` is not supported on the GPU path.
+    arguments as the reference.
     """
 
     def __init__(self, trace_probs=None, trace_time=None, start_day=0, end_day=None, presumptive=False,
@@ -258,8 +258,8 @@ class contact_tracing(Intervention):
     def initialize(self, sim):
         """interventions.py:1023-1041."""
         super().initialize()
-        if self.capacity is not None:
-            raise NotImplementedError('contact_tracing(capacity=...) is not supported on the GPU path')
+        if self.capacity is not None and not isinstance(self.capacity, numbers.Number):
+            raise ValueError('contact_tracing capacity must be a number')
         self.start_day = _day(self.start_day, 0)
         self.end_day = _day(self.end_day, None)
         self.days = [self.start_day, self.end_day]
@@ -278,7 +278,8 @@ class contact_tracing(Intervention):
     def device_testing(self):
         return dict(start_day=self.start_day, end_day=0xFFFE if self.end_day is None else self.end_day,
                     presumptive=bool(self.presumptive), trace_probs=dict(self.trace_probs),
-                    trace_time=dict(self.trace_time), quar_period=self.quar_period)
+                    trace_time=dict(self.trace_time), quar_period=self.quar_period,
+                    capacity=None if self.capacity is None else float(self.capacity))
 
     def apply(self, sim):
         raise NotImplementedError('contact_tracing runs on the device as part of the day loop')

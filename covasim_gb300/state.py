@@ -316,6 +316,8 @@ class BatchState:
         self.has_testing = any(sp.testing for sp in self.specs)
         self.has_swab = any((sp.testing or {}).get('test') and sp.testing['test'].get('swab_pdf') is not None
                             for sp in self.specs)
+        self.has_capacity = any((sp.testing or {}).get('trace') and sp.testing['trace'].get('capacity') is not None
+                                for sp in self.specs)
         self.pending_slots = 1
         self.n_contact_layers = max(len(sp.layers) for sp in self.specs) or 1
         if self.has_testing:
@@ -369,6 +371,15 @@ class BatchState:
         array the device writes), set into each sim's testing record."""
         keep = []
         for r, sp in zip(self.testing_recs, self.specs):
+            ct = (sp.testing or {}).get('trace')
+            if ct and ct.get('capacity') is not None:
+                cap_list = torch.zeros(max(sp.n, 1), dtype=I32, device=dev)
+                cap_count = torch.zeros(1, dtype=I32, device=dev)
+                p = sp.pars  # the day's scale without dynamic rescaling, as _build_rescale sets it
+                r.capacity = float(ct['capacity'])
+                r.cap_scale = 1.0 if bool(p.get('rescale', True)) else float(p.get('pop_scale') or 1)
+                r.cap_list, r.cap_count = cap_list.data_ptr(), cap_count.data_ptr()
+                keep += [cap_list, cap_count]
             tp = (sp.testing or {}).get('test')
             if not tp:
                 continue
@@ -859,7 +870,7 @@ class BatchState:
         st.segments = self.seg_dev.data_ptr() if self.segments else None
         st.agent_blocks = self.blocks_dev.data_ptr()
         st.draw_table = self.draw_table.data_ptr() if self.draw_table is not None else None
-        st.has_testing = int(self.has_testing) | (2 if self.has_swab else 0)
+        st.has_testing = int(self.has_testing) | (2 if self.has_swab else 0) | (4 if self.has_capacity else 0)
         st.pending_slots = self.pending_slots
         st.n_contact_layers = self.n_contact_layers
         if self.has_testing:

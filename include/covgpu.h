@@ -155,6 +155,15 @@ typedef struct covgpu_testing {
   double symp_prob;
   int32_t swab_len;
   int32_t _pad_swab;
+  /* contact_tracing's capacity (interventions.py:1074-1078; NULL cap_list: none): of
+   * the day's cases, int(capacity / scale) are traced, scale the sim's rescale_vec[t]
+   * (cap_scale without dynamic rescaling): those with the smallest keys, the x word
+   * of Philox (agent, 2, t, TAG_TEST) above the agent's index. cap_list [n_agents]
+   * and *cap_count hold the day's cases (local indices; filled by the test pass). */
+  double capacity;
+  double cap_scale;
+  int32_t* cap_list;
+  uint32_t* cap_count;
 } covgpu_testing;
 #define COVGPU_NO_SUBTARGET 0xFFFFFFFFFFFFFFFFull
 
@@ -338,7 +347,8 @@ typedef struct covgpu_state {
   const double* const* edge_uniforms; /* [n_segments] -> [n_variants][2][n_edges] */
   /* testing and tracing (all NULL / 0 when no sim tests) */
   int32_t has_testing;            /* bit 0: run the testing, tracing and post passes;
-                                     bit 1: some sim's test_prob has a swab delay     */
+                                     bit 1: some sim's test_prob has a swab delay;
+                                     bit 2: some sim's contact_tracing a capacity     */
   int32_t pending_slots;          /* R: days of scheduled quarantines kept ahead     */
   uint32_t* trace_bits;           /* [ceil(n/32)] agents traced today                */
   uint32_t* contact_bits;         /* [n_contact_layers][ceil(n/32)] contacts found   */

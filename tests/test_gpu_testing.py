@@ -42,6 +42,10 @@ CASES = [
     ('random', 2500, 45, 8, False, False,
      dict(symp_prob=0.4, quar_policy='daily', swab_delay=dict(dist='uniform', par1=0, par2=5), ili_prev=0.01),
      dict(trace_probs=0.7)),
+    # a tracing capacity below the day's cases
+    ('hybrid', 3000, 45, 9, True, True, dict(symp_prob=0.4, asymp_prob=0.02), dict(trace_probs=0.8, capacity=4)),
+    ('random', 2500, 45, 10, False, False, dict(symp_prob=0.5, test_delay=1),
+     dict(trace_probs=0.9, presumptive=True, capacity=3)),
 ]
 
 
@@ -79,6 +83,19 @@ def test_ili_and_subtargets_add_tests():
         sim = make_sim('hybrid', 3000, 30, 9, True, False, dict(base, **extra), dict(trace_probs=0.5))
         tests.append(sim.run().raw_results()['new_tests'].sum())
     assert tests[1] > 1.5 * tests[0] and tests[2] > 1.5 * tests[0], tests
+
+
+def test_tracing_capacity_limits_the_traced():
+    """interventions.py:1074-1078: at most ``capacity`` of the day's diagnosed are
+    traced, so fewer contacts are quarantined than without a capacity."""
+    quar = []
+    for cap in (None, 2):
+        sim = make_sim('hybrid', 3000, 40, 11, True, False, dict(symp_prob=0.5, asymp_prob=0.02),
+                       dict(trace_probs=1.0, capacity=cap))
+        raw = sim.run().raw_results()
+        assert raw['new_diagnoses'].max() > 2
+        quar.append(raw['new_quarantined'].sum())
+    assert quar[1] < 0.8 * quar[0], quar
 
 
 def test_testing_step_mode_equals_graph_run():
