@@ -86,16 +86,17 @@ def test_ili_and_subtargets_add_tests():
 
 
 def test_tracing_capacity_limits_the_traced():
-    """interventions.py:1074-1078: at most ``capacity`` of the day's diagnosed are
-    traced, so fewer contacts are quarantined than without a capacity."""
-    quar = []
-    for cap in (None, 2):
+    """interventions.py:1074-1078: a capacity of 0 traces nobody (no quarantines),
+    one above every day's cases gives the run without a capacity."""
+    raws = []
+    for cap in (None, 0, 10**9):
         sim = make_sim('hybrid', 3000, 40, 11, True, False, dict(symp_prob=0.5, asymp_prob=0.02),
                        dict(trace_probs=1.0, capacity=cap))
-        raw = sim.run().raw_results()
-        assert raw['new_diagnoses'].max() > 2
-        quar.append(raw['new_quarantined'].sum())
-    assert quar[1] < 0.8 * quar[0], quar
+        raws.append(sim.run().raw_results())
+    assert raws[0]['new_quarantined'].sum() > 0 and raws[0]['new_diagnoses'].max() > 2
+    assert raws[1]['new_quarantined'].sum() == 0
+    for k in TESTING_KEYS:
+        np.testing.assert_array_equal(raws[2][k], raws[0][k], err_msg=k)
 
 
 def test_testing_step_mode_equals_graph_run():
