@@ -590,7 +590,7 @@ int launch_test_trace(const covgpu_state* st, int t, cudaStream_t s) {
   static const int64_t test_wave = wave_blocks(k_test_pass, AGENT_THREADS);
   k_test_pass<<<wave_grid(st, test_wave), AGENT_THREADS, 0, s>>>(*st, t);
   if (st->has_testing & 4) k_trace_cap<<<(unsigned)st->n_sims, 256, 0, s>>>(*st, t);  // a tracing capacity
-  if (st->n_tiles > 0) {
+  if (st->n_tiles > 0 && !(st->has_testing & 8)) {  // some stored layer is traced without an index
     const dim3 grid((unsigned)st->n_tiles);
     switch (st->edge_tile) {
       case 1024: k_trace_scan<1><<<grid, EDGE_THREADS, 0, s>>>(*st, t); break;

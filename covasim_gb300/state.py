@@ -870,7 +870,10 @@ class BatchState:
         st.segments = self.seg_dev.data_ptr() if self.segments else None
         st.agent_blocks = self.blocks_dev.data_ptr()
         st.draw_table = self.draw_table.data_ptr() if self.draw_table is not None else None
-        st.has_testing = int(self.has_testing) | (2 if self.has_swab else 0) | (4 if self.has_capacity else 0)
+        st.has_testing = 0
+        if self.has_testing:  # bit 0 and its refinements
+            st.has_testing = (1 | (2 if self.has_swab else 0) | (4 if self.has_capacity else 0) |
+                              (8 if all(rec.dynamic or rec.rp1 for rec in self.segments) else 0))
         st.pending_slots = self.pending_slots
         st.n_contact_layers = self.n_contact_layers
         if self.has_testing:

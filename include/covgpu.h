@@ -348,7 +348,9 @@ typedef struct covgpu_state {
   /* testing and tracing (all NULL / 0 when no sim tests) */
   int32_t has_testing;            /* bit 0: run the testing, tracing and post passes;
                                      bit 1: some sim's test_prob has a swab delay;
-                                     bit 2: some sim's contact_tracing a capacity     */
+                                     bit 2: some sim's contact_tracing a capacity;
+                                     bit 3: every stored layer has its agent index
+                                     (the tracing scan of the tiles is skipped)      */
   int32_t pending_slots;          /* R: days of scheduled quarantines kept ahead     */
   uint32_t* trace_bits;           /* [ceil(n/32)] agents traced today                */
   uint32_t* contact_bits;         /* [n_contact_layers][ceil(n/32)] contacts found   */
