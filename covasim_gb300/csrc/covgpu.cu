@@ -1,15 +1,19 @@
 // covgpu: GB300-native (sm_103a) kernels for Covasim 3.1.7's per-day step.
 //
 // Kernels (all HBM/L2-bound integer and float32 work; no tensor cores):
-//   k_agent_step     one dense pass per agent per day: update_states_pre
-//       (people.py:164-312,368-374) + check_immunity (immunity.py:303-350) +
-//       update_nab (immunity.py:205-213) + stocks/flows (sim.py:651-674) +
-//       viral load, source/target role bitmaps and source records for the edge pass;
-//   k_edge_pass      every layer segment and variant of every sim: edges streamed with
-//       128-bit reads, source->target candidates queued per warp in shared
-//       memory, then compute_trans_sus folded in lane-packed, Philox Bernoullis,
-//       warp-ballot compaction of events, atomicMin first-infector claim
-//       (k_edge_pass_res: the same with the source bitmap in shared memory);
+//   k_agent_step     one dense pass per agent per day (one wave of blocks walking
+//       agent-block ranges): update_states_pre (people.py:164-312,368-374) +
+//       check_immunity (immunity.py:303-350) + update_nab (immunity.py:205-213) +
+//       stocks/flows (sim.py:651-674) + viral load, source/target role bitmaps and
+//       the source and target records of the edge passes;
+//   k_edge_pass      every stored layer segment and variant of every sim: edges
+//       streamed with 128-bit reads, source->target candidates queued per warp in
+//       shared memory, then compute_trans_sus folded in lane-packed, Philox
+//       Bernoullis, warp-ballot compaction of events, atomicMin first-infector
+//       claim (k_edge_pass_res: the same with the source bitmap in shared memory;
+//       k_src_pass: optionally, quiet days walked from the sources);
+//   k_dyn_pass       the redrawn layers (base.py:1849-1876): the day's sources'
+//       contact lists drawn from Philox and thinned, the same candidates' path;
 //   k_infect_claims / k_infect_list   People.infect (people.py:435-586) +
 //       update_peak_nab (immunity.py:138-202).
 // The reference's standalone numba functions are in covgpu_reference.cu, the
