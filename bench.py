@@ -232,7 +232,7 @@ def kernel_profile(sim, npts, head_start_cycles=2_000_000):
 
     for t in range(npts):
         torch.cuda._sleep(head_start_cycles)
-        timed('agent_step', lambda: st.agent_step(t, do_prev=t > 0, do_day=True))
+        timed('agent_step', lambda: st.agent_step(t, do_prev=t > 0, do_day=True, steady=t > 0))
         timed('edge_stored', lambda: st.edge_pass(t, parts=1))
         timed('edge_dynamic', lambda: st.edge_pass(t, parts=2))
         timed('infect_claims', lambda: st.infect_claims(t))
@@ -507,7 +507,7 @@ def batched_arm(args, sim, plain_value, world):
     solo = sim.state.results(0)['new_infections']
     same = bool(np.array_equal(st.results(0)['new_infections'], solo))
     cum = [float(st.results(k)['new_infections'].sum()) for k in range(B)]
-    return {'value': round(value, 1), 'unit': 'agent-days/s', 'n_sims': B, 'edge_tile': st.edge_tile,
+    return {'value': round(value, 1), 'unit': 'agent-days/s', 'n_sims': B, 'edge_tile': st.edge_tile_label,
             'ms_per_step': round(1e3 * elapsed / args.steps, 3), 'vs_plain': round(value / plain_value, 3),
             'sim0_equals_plain_run': same, 'cum_infections_mean': round(float(np.mean(cum)), 1),
             'cum_infections_sd': round(float(np.std(cum)), 1)}
@@ -807,7 +807,7 @@ def batch_arm(args, n_sims=256, days=120, steps=None, warmup=None, emit=True):
                 f'10/20/30, beta U[0.010,0.025], change_beta day 30 x U[0.3,1], {days} days')
     extra = {'one_by_one': {'value': round(agent_days / t_single, 1), 'ms_per_step': round(1e3 * t_single, 3)},
              'batched_over_one_by_one': round(t_single / t_batch, 3), 'every_sim_equals_its_own_run': same,
-             'edge_tile': st.edge_tile, 'init_s': round(init_s, 1),
+             'edge_tile': st.edge_tile_label, 'init_s': round(init_s, 1),
              'population': 'device' if args.gpu_population else 'host', 'clocks': clk}
     if emit:
         _line(agent_days / t_batch, 'agent-days/s', args, 1e3 * t_batch, workload, extra)

@@ -27,9 +27,11 @@ FX_IMM_BITS = 32
 NO_VARIANT = 0xFF
 NOALLOC_MAX_EDGES = 1 << 24   # covgpu_infections_noalloc limit (COVGPU_NOALLOC_MAX_EDGES)
 NO_SUBTARGET = 0xFFFFFFFFFFFFFFFF  # covgpu_testing.sub_thr: no subtarget (COVGPU_NO_SUBTARGET)
-EDGE_TILE = 4096          # default edges per edge-pass tile (block)
+EDGE_TILE = '2048w'       # default edge pass: 2048-edge tiles, the stored layers' pass as one wave of blocks
 DYN_MAX_LIST = 1024       # longest contact list of an agent in a dynamic layer (COVGPU_DYN_MAX_LIST)
 EDGE_TILES = (1024, 2048, 4096, 8192)   # tile sizes the library supports (covgpu_state.edge_tile)
+DAY_STEADY = 2  # COVGPU_DAY_STEADY, a flag of covgpu_agent_step's do_day
+EDGE_WAVE_MAX = 32  # covgpu_state.edge_wave for 'as many blocks per SM as fit' (the kernel's occupancy caps it)
 AGENT_BLOCK = 256         # agents per agent-pass block (covgpu.cu AGENT_THREADS)
 AGENT_ALIGN = 32          # each sim's first agent is a multiple of this
 
@@ -124,6 +126,7 @@ class State(C.Structure):
     _fields_ = [
         ('n', C.c_int64), ('n_sims', C.c_int32), ('n_segments', C.c_int32), ('n_tiles', C.c_int64),
         ('n_agent_blocks', C.c_int64), ('edge_tile', C.c_int32), ('edge_resident', C.c_int32),
+        ('edge_wave', C.c_int32), ('_pad_wave', C.c_int32),
         ('flags', C.c_void_p), ('vstate', C.c_void_p),
         ('symp_prob', C.c_void_p), ('severe_prob', C.c_void_p), ('crit_prob', C.c_void_p), ('death_prob', C.c_void_p),
         ('rel_trans', C.c_void_p), ('rel_sus', C.c_void_p),

@@ -44,7 +44,7 @@ class BatchSim:
         self.sims = list(sims)
         self.use_graph = use_graph
         self.log = log
-        self.edge_tile = edge_tile  # as Sim's: None (4096), a tile, a label such as '8192r', or 'auto'
+        self.edge_tile = edge_tile  # as Sim's: None (the default, '2048w'), a tile, a label such as '8192r', or 'auto'
         self.state = None
 
     def initialize(self):

@@ -148,6 +148,7 @@ static_assert(DW_VAR + COVGPU_MAX_VARIANTS <= DW_SRC, "day-word layout");
 // sequence, so that the state a caller reads afterwards holds the reference's array).
 __device__ __forceinline__ void agent_block_step(const covgpu_state& st, const covgpu_agent_block& blk,
                                                  const AgentIn& in, int t, int do_prev, int do_day, int full_imm,
+                                                 int steady,
                                                  const float (*s_ln_tab)[2], const float (*s_exp_tab)[2],
                                                  long long& nab_fx, long long& sus_fx, long long& symp_fx,
                                                  unsigned& acc_prev, unsigned& acc_day) {
@@ -163,6 +164,18 @@ __device__ __forceinline__ void agent_block_step(const covgpu_state& st, const c
   const int a_tne = in.tne;
   const uint32_t f_in = f, vs_in = vs;
   float nab_now = a_nab;  // the NAb level after the closing pass's update_nab
+
+  // A warp of steady agents (susceptible and naive and nothing else: never infected,
+  // so without NAbs, and not tested, quarantined, isolated or vaccinated): their day
+  // changes none of their fields, records or role bits, and closing the day before
+  // counts them as susceptible and naive. Their role words and target records are
+  // those an earlier full pass of the launch sequence wrote (steady: not its first
+  // day), since every kernel that changes an agent's flags or quarantine keeps them
+  // current; so only the stocks are counted.
+  if (steady && __all_sync(0xffffffffu, !valid || f == (B_SUS | B_NAIVE))) {
+    if (do_prev) acc_prev += (((B_SUS | B_NAIVE) >> lane) & 1u) * (unsigned)__popc(__ballot_sync(0xffffffffu, valid));
+    return;
+  }
 
   // ---------------------------------------------------------- close day t-1
   if (do_prev) {
@@ -422,7 +435,7 @@ __device__ __noinline__ void agent_flush(const covgpu_state& st, int sim, int t,
 // flight while the current one is processed, no barrier separates agent blocks of
 // one sim, and the counters go to the results once per sim a block touched
 // instead of once per 256 agents.
-__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm) {
+__global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm, int steady) {
   pdl_wait();
   if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
     const int h = *st.hold;
@@ -461,8 +474,8 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       const int64_t ni = nblk.begin + threadIdx.x;
       nxt = agent_load(st, ni, ni < nblk.end, st.sims[nblk.sim].use_waning != 0);
     }
-    agent_block_step(st, blk, cur, t, do_prev, do_day, full_imm, s_ln_tab, s_exp_tab, nab_fx, sus_fx, symp_fx,
-                     acc_prev, acc_day);
+    agent_block_step(st, blk, cur, t, do_prev, do_day, full_imm, steady, s_ln_tab, s_exp_tab, nab_fx, sus_fx,
+                     symp_fx, acc_prev, acc_day);
     if (!more) break;
     ++b;
     if (nblk.sim != sim) {
@@ -732,16 +745,9 @@ __device__ __forceinline__ void load_sim_lite(SimLite& o, const covgpu_sim_param
   o.n_layers = sp.n_layers;
 }
 
-// One tile (TILE edges) of one stored segment, NT threads: phase A streams the
-// edges and queues the candidate directions of each warp, phase B drains the queues.
-// The segment record L and its sim's constants sp are shared-memory copies.
-// RES: the sim's source bitmap is resident in shared memory (s_src, one sim).
-template <bool LIK, int NT, int64_t TILE, bool RES>
-__device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg, int64_t tile, const covgpu_layer* L,
-                                          const SimLite* sp, const uint32_t* s_src, EdgeQueue& q, LikAcc& acc) {
-  constexpr int ROUNDS = (int)(TILE / ((int64_t)NT * EDGE_VEC));
-  static_assert(ROUNDS >= 1 && TILE % ((int64_t)NT * EDGE_VEC) == 0, "whole rounds per tile");
-  SegCtx c;
+// The segment context of a stored segment's tiles (edge_tile, edge_span).
+__device__ __forceinline__ void seg_ctx(const covgpu_state& st, int t, int seg, const covgpu_layer* L,
+                                        const SimLite* sp, SegCtx& c) {
   c.L = st.segments + seg;
   c.seg = seg;
   c.layer = L->layer;
@@ -757,6 +763,53 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
   c.beta_t = sp->beta_tab + (int64_t)t * c.nv;
   c.beta_layer = sp->beta_layer_tab[(int64_t)t * sp->n_layers + c.layer];
   c.sim = L->sim;
+}
+
+// One round of phase A for this thread's edges eb .. eb + 3 (pa: their p1, pb: their
+// p2; those at or past e_hi are masked off): the sources first (every edge: shared
+// memory, or the L1-resident bitmap), then the other endpoint's target bit only
+// where one endpoint is a source (roles are exclusive, so an edge has at most one
+// candidate direction), and the warp-aggregated queue appends, with offsets from e0.
+template <bool RES>
+__device__ __forceinline__ void edge_round(const covgpu_state& st, const uint32_t* s_src, const int4& pa,
+                                           const int4& pb, int64_t eb, int64_t e_hi, int64_t e0, EdgeQueue& q,
+                                           int& qn) {
+  int32_t a[EDGE_VEC], b[EDGE_VEC];
+  a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
+  b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
+  uint32_t sa[EDGE_VEC], sb[EDGE_VEC];
+#pragma unroll
+  for (int j = 0; j < EDGE_VEC; ++j) {
+    if (RES) {
+      sa[j] = (s_src[a[j] >> 5] >> (a[j] & 31)) & 1u;
+      sb[j] = (s_src[b[j] >> 5] >> (b[j] & 31)) & 1u;
+    } else {
+      sa[j] = src_bit(st.roles, a[j]);
+      sb[j] = src_bit(st.roles, b[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < EDGE_VEC; ++j) {
+    const bool in = eb + j < e_hi;
+    const uint32_t m = (uint32_t)(eb + j - e0) << 1;
+    const bool d1 = sb[j] != 0u;  // direction p2 -> p1
+    bool cand = false;
+    if (in && (sa[j] | sb[j])) cand = tgt_bit(st, d1 ? a[j] : b[j]) != 0u;
+    queue_push(q, qn, cand, d1 ? b[j] : a[j], d1 ? a[j] : b[j], m | (d1 ? 1u : 0u));
+  }
+}
+
+// One tile (TILE edges) of one stored segment, NT threads: phase A streams the
+// edges and queues the candidate directions of each warp, phase B drains the queues.
+// The segment record L and its sim's constants sp are shared-memory copies.
+// RES: the sim's source bitmap is resident in shared memory (s_src, one sim).
+template <bool LIK, int NT, int64_t TILE, bool RES>
+__device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg, int64_t tile, const covgpu_layer* L,
+                                          const SimLite* sp, const uint32_t* s_src, EdgeQueue& q, LikAcc& acc) {
+  constexpr int ROUNDS = (int)(TILE / ((int64_t)NT * EDGE_VEC));
+  static_assert(ROUNDS >= 1 && TILE % ((int64_t)NT * EDGE_VEC) == 0, "whole rounds per tile");
+  SegCtx c;
+  seg_ctx(st, t, seg, L, sp, c);
   const int32_t* p1 = L->p1;
   const int32_t* p2 = L->p2;
   const int64_t e0 = (tile - L->tile_begin) * TILE;
@@ -784,32 +837,60 @@ __device__ __forceinline__ void edge_tile(const covgpu_state& st, int t, int seg
     const int64_t eb = e0 + ((int64_t)r * NT + threadIdx.x) * EDGE_VEC;
     const int4 pa = na, pb = nb;
     if (r + 1 < ROUNDS) fetch(r + 1, na, nb);
-    int32_t a[EDGE_VEC], b[EDGE_VEC];
-    a[0] = pa.x; a[1] = pa.y; a[2] = pa.z; a[3] = pa.w;
-    b[0] = pb.x; b[1] = pb.y; b[2] = pb.z; b[3] = pb.w;
-    // sources first (every edge: shared memory, or the L1-resident bitmap), then the
-    // other endpoint's target bit only where one endpoint is a source; roles are
-    // exclusive, so an edge has at most one candidate direction
-    uint32_t sa[EDGE_VEC], sb[EDGE_VEC];
-#pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) {
-      if (RES) {
-        sa[j] = (s_src[a[j] >> 5] >> (a[j] & 31)) & 1u;
-        sb[j] = (s_src[b[j] >> 5] >> (b[j] & 31)) & 1u;
-      } else {
-        sa[j] = src_bit(st.roles, a[j]);
-        sb[j] = src_bit(st.roles, b[j]);
+    edge_round<RES>(st, s_src, pa, pb, eb, e1, e0, q, qn);
+    if (qn > EQ_CAP - EQ_ROUND) {
+      queue_drain<LIK>(st, c, t, e0, q, qn, acc);
+      qn = 0;
+    }
+  }
+  if (qn > 0) queue_drain<LIK>(st, c, t, e0, q, qn, acc);
+}
+
+// Tiles [k_lo, k_hi) of one stored segment (L, its sim's constants sp) as one
+// stream of rounds: each round's edge lists are loaded one round ahead, across
+// the tiles' boundaries, and the warp's queue entries count edges from a base
+// that moves on (the queue drained first) when a round would reach past the
+// 2^15 edges their offsets hold.
+template <bool LIK, int64_t TILE>
+__device__ __forceinline__ void edge_span(const covgpu_state& st, int t, int seg, int64_t k_lo, int64_t k_hi,
+                                          const covgpu_layer* L, const SimLite* sp, EdgeQueue& q, LikAcc& acc) {
+  constexpr int64_t ROUND = (int64_t)EDGE_THREADS * EDGE_VEC;
+  constexpr int64_t SPAN = 32768;
+  static_assert(TILE % ROUND == 0 && SPAN % ROUND == 0, "whole rounds");
+  SegCtx c;
+  seg_ctx(st, t, seg, L, sp, c);
+  const int32_t* p1 = L->p1;
+  const int32_t* p2 = L->p2;
+  const int64_t e_lo = k_lo * TILE;
+  const int64_t e_hi = min(k_hi * TILE, c.n_edges);
+  const int32_t off = (int32_t)sp->agent_off;
+  auto fetch = [&](int64_t rb, int4& xa, int4& xb) {
+    const int64_t eb = rb + (int64_t)threadIdx.x * EDGE_VEC;
+    if (eb + EDGE_VEC <= e_hi) {
+      xa = ld_stream_v4(p1 + eb);
+      xb = ld_stream_v4(p2 + eb);
+    } else {
+      xa.x = eb < e_hi ? p1[eb] : off;         xb.x = eb < e_hi ? p2[eb] : off;
+      xa.y = eb + 1 < e_hi ? p1[eb + 1] : off; xb.y = eb + 1 < e_hi ? p2[eb + 1] : off;
+      xa.z = eb + 2 < e_hi ? p1[eb + 2] : off; xb.z = eb + 2 < e_hi ? p2[eb + 2] : off;
+      xa.w = eb + 3 < e_hi ? p1[eb + 3] : off; xb.w = eb + 3 < e_hi ? p2[eb + 3] : off;
+    }
+  };
+  int qn = 0;
+  int64_t e0 = e_lo;
+  int4 na, nb;
+  fetch(e_lo, na, nb);
+  for (int64_t rb = e_lo; rb < e_hi; rb += ROUND) {
+    if (rb + ROUND - e0 > SPAN) {
+      if (qn > 0) {
+        queue_drain<LIK>(st, c, t, e0, q, qn, acc);
+        qn = 0;
       }
+      e0 = rb;
     }
-#pragma unroll
-    for (int j = 0; j < EDGE_VEC; ++j) {
-      const bool in = eb + j < e1;
-      const uint32_t m = (uint32_t)(eb + j - e0) << 1;
-      const bool d1 = sb[j] != 0u;  // direction p2 -> p1
-      bool cand = false;
-      if (in && (sa[j] | sb[j])) cand = tgt_bit(st, d1 ? a[j] : b[j]) != 0u;
-      queue_push(q, qn, cand, d1 ? b[j] : a[j], d1 ? a[j] : b[j], m | (d1 ? 1u : 0u));
-    }
+    const int4 pa = na, pb = nb;
+    if (rb + ROUND < e_hi) fetch(rb + ROUND, na, nb);
+    edge_round<false>(st, nullptr, pa, pb, rb + (int64_t)threadIdx.x * EDGE_VEC, e_hi, e0, q, qn);
     if (qn > EQ_CAP - EQ_ROUND) {
       queue_drain<LIK>(st, c, t, e0, q, qn, acc);
       qn = 0;
@@ -886,6 +967,60 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
       if (x != 0.0) atomicAdd(K.ll + day, x);
       if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + s_L.layer, y);
     }
+  }
+}
+
+// The stored layers as one wave of resident blocks (covgpu_state.edge_wave): of the
+// T tiles, block b walks [b T / G, (b + 1) T / G), a contiguous share that differs
+// from the others' by at most one tile, segment by segment, its edge lists loaded a
+// round ahead across the tiles' boundaries. Against one block per tile it leaves
+// no partial last wave and no per-tile start (segment lookup, first round's
+// latency); the tile size only sets how finely the shares are balanced.
+template <bool LIK, int ROUNDS>
+__global__ void __launch_bounds__(EDGE_THREADS) k_edge_wave(covgpu_state st, int t) {
+  pdl_wait();
+  if (held(st, t)) return;
+  constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
+  const int64_t lo = st.n_tiles * (int64_t)blockIdx.x / gridDim.x;
+  const int64_t hi = st.n_tiles * ((int64_t)blockIdx.x + 1) / gridDim.x;
+  if (lo >= hi) return;  // block-uniform
+  __shared__ covgpu_layer s_L;
+  __shared__ SimLite s_sp;
+  __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
+  __shared__ double s_acc[EDGE_THREADS / 32][2];
+  int seg = segment_of_tile(st.segments, st.n_segments, lo);
+  int64_t tile = lo;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_L = st.segments[seg];
+      load_sim_lite(s_sp, st.sims[s_L.sim]);
+    }
+    __syncthreads();
+    const int64_t seg_end = seg + 1 < st.n_segments ? st.segments[seg + 1].tile_begin : st.n_tiles;
+    const int64_t stop = min(hi, seg_end);  // >= tile: seg is the last segment starting at or before tile
+    if (tile < stop && !seg_walked(st, s_L, t)) {  // block-uniform
+      LikAcc acc;
+      edge_span<LIK, TILE>(st, t, seg, tile - s_L.tile_begin, stop - s_L.tile_begin, &s_L, &s_sp,
+                           s_q[threadIdx.x >> 5], acc);
+      if (LIK) {  // this segment's sums: one sim, one layer
+        const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) { s_acc[warp][0] = a; s_acc[warp][1] = b; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double x = 0.0, y = 0.0;
+          for (int k = 0; k < EDGE_THREADS / 32; ++k) { x += s_acc[k][0]; y += s_acc[k][1]; }
+          const covgpu_lik& K = st.lik;
+          const int64_t day = (int64_t)s_L.sim * K.npts_max + t;
+          if (x != 0.0) atomicAdd(K.ll + day, x);
+          if (K.g_ll && y != 0.0) atomicAdd(K.g_ll + day * K.n_layers_max + s_L.layer, y);
+        }
+      }
+    }
+    if (stop > tile) tile = stop;
+    if (tile >= hi || seg + 1 >= st.n_segments) break;
+    ++seg;
+    __syncthreads();  // every thread has read s_L (and s_acc) before they are replaced
   }
 }
 
@@ -1349,8 +1484,27 @@ int configure_edge_pass(const covgpu_state* st) {
   return rc ? rc : configure_res<true>(smem);
 }
 
+// one wave of k_edge_wave<LIK, R>: at most st->edge_wave blocks per SM
+template <bool LIK, int R>
+void launch_edge_wave_r(const covgpu_state* st, int t, cudaStream_t s) {
+  static int64_t per_sm = -1;
+  if (per_sm < 0) per_sm = wave_blocks(k_edge_wave<LIK, R>, EDGE_THREADS) / n_sms();
+  const int64_t wave = (int64_t)n_sms() * (st->edge_wave < per_sm ? st->edge_wave : per_sm);
+  const unsigned grid = (unsigned)(st->n_tiles < wave ? st->n_tiles : wave);
+  launch_pdl(k_edge_wave<LIK, R>, grid, EDGE_THREADS, 0, s, *st, t);
+}
+
 template <bool LIK>
 void launch_edge_tiles(const covgpu_state* st, int t, cudaStream_t s) {
+  if (st->edge_wave > 0) {
+    switch (st->edge_tile) {
+      case 1024: launch_edge_wave_r<LIK, 1>(st, t, s); break;
+      case 2048: launch_edge_wave_r<LIK, 2>(st, t, s); break;
+      case 8192: launch_edge_wave_r<LIK, 8>(st, t, s); break;
+      default: launch_edge_wave_r<LIK, 4>(st, t, s); break;
+    }
+    return;
+  }
   const dim3 grid((unsigned)st->n_tiles);
   switch (st->edge_tile) {
     case 1024: launch_pdl(k_edge_pass<LIK, 1>, grid.x, EDGE_THREADS, 0, s, *st, t); break;
@@ -2063,7 +2217,7 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
   for (int t = t0; t < t1; ++t) {
     if (st->hold) k_rescale_check<<<1, 128, 0, s>>>(*st, t);
     launch_pdl(k_agent_step, agent_grid(st), AGENT_THREADS, 0, s, *st, t, (t > t0 || open_prev) ? 1 : 0, 1,
-               t == t1 - 1 ? 1 : 0);
+               t == t1 - 1 ? 1 : 0, t > t0 ? 1 : 0);
     if (t < st->import_days) k_import_day<<<IMPORT_BLOCKS, 256, 0, s>>>(*st, t);
     launch_test_trace(st, t, s);
     const int rc = launch_edge_pass_forked(st, t, s);
@@ -2071,7 +2225,7 @@ int enqueue_days(const covgpu_state* st, int t0, int t1, int open_prev, int clos
     launch_lik_targets(st, t, s);
     launch_pdl(k_infect_claims, (unsigned)grid_for(st->n / 8 + 1, 256, 152 * 4), 256, 0, s, *st, t);
   }
-  if (close_last) launch_pdl(k_agent_step, agent_grid(st), AGENT_THREADS, 0, s, *st, t1, 1, 0, 0);
+  if (close_last) launch_pdl(k_agent_step, agent_grid(st), AGENT_THREADS, 0, s, *st, t1, 1, 0, 0, 1);
   return launch_status();
 }
 
@@ -2094,6 +2248,7 @@ int check_state(const covgpu_state* st) {
   if (st->edge_tile != 1024 && st->edge_tile != 2048 && st->edge_tile != 4096 && st->edge_tile != 8192)
     return COVGPU_BADARG;
   if (st->edge_resident && (!edge_res_smem(st) || (reinterpret_cast<uintptr_t>(st->roles) & 15u))) return COVGPU_BADARG;
+  if (st->edge_wave < 0 || (st->edge_wave > 0 && st->edge_resident)) return COVGPU_BADARG;
   if (st->has_testing && (!st->trace_bits || !st->contact_bits || !st->pending_quar || !st->trace_count ||
                           st->pending_slots < 1 || st->n_contact_layers < 1))
     return COVGPU_BADARG;
@@ -2133,7 +2288,9 @@ int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_
   int rc = check_state(st);
   if (rc) return rc;
   if (t < 0 || t >= 0xFFFF) return COVGPU_BADARG;
-  k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, do_day, 1);
+  if (do_day & ~(1 | COVGPU_DAY_STEADY)) return COVGPU_BADARG;
+  const int day = do_day & 1, steady = (!day || (do_day & COVGPU_DAY_STEADY)) ? 1 : 0;
+  k_agent_step<<<agent_grid(st), AGENT_THREADS, 0, S(stream)>>>(*st, t, do_prev, day, 1, steady);
   return launch_status();
 }
 

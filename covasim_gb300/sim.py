@@ -275,10 +275,12 @@ class Sim:
             arguments are merged in
         popdict (dict): optional population (uid, age, sex, contacts)
         use_graph (bool): capture the day loop in a CUDA graph
-        edge_tile (int, str or 'auto'): edges per edge-pass block (1024, 2048, 4096
-            or 8192; default 4096), suffixed 'r' ('8192r') to keep the source
-            bitmap resident in shared memory; 'auto' times whole runs with each at
-            initialize (``covasim_gb300.autotune``, cached per workload)
+        edge_tile (int, str or 'auto'): edges per edge-pass tile (1024, 2048, 4096
+            or 8192), suffixed 'w' ('2048w', the default) to run the stored layers'
+            pass as one wave of blocks walking balanced ranges of tiles, or 'r'
+            ('8192r') to keep the source bitmap resident in shared memory; 'auto'
+            times whole runs with each at initialize (``covasim_gb300.autotune``,
+            cached per workload)
         gpu_population (bool): build the population (ages, layers, prognoses) on
             the device instead of the host (same distributions, Philox draws)
         datafile (str, dict or DataTable): data to compare with (``cv.load_data``),

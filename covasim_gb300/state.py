@@ -260,14 +260,29 @@ def ili_agents(seed, t, n, n_ili):
 SRC_WALK = 0
 
 
+def parse_edge_tile(choice):
+    """An edge-pass label ('4096', 4096, '8192r', '1024w', '1024w4') as
+    set_edge_tile's keyword arguments."""
+    text = str(choice)
+    if text.endswith('r'):
+        return dict(tile=int(text[:-1]), resident=True)
+    if 'w' in text:
+        tile, cap = text.split('w', 1)
+        return dict(tile=int(tile), wave=int(cap) if cap else True)
+    return dict(tile=int(text))
+
+
 class BatchState:
     """Agent and layer arrays of one or more sims in device memory."""
 
-    def __init__(self, specs, device='cuda', event_capacity=None, log_capacity=None, log=True, edge_tile=L.EDGE_TILE):
-        if int(edge_tile) not in L.EDGE_TILES:
-            raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
-        self.edge_tile = int(edge_tile)
+    def __init__(self, specs, device='cuda', event_capacity=None, log_capacity=None, log=True,
+                 edge_tile=L.EDGE_TILE):
+        et = parse_edge_tile(edge_tile)
+        if et['tile'] not in L.EDGE_TILES or et.get('resident'):
+            raise ValueError(f'edge tile must be one of {L.EDGE_TILES}, optionally with the one-wave suffix w')
+        self.edge_tile = et['tile']
         self.edge_resident = False
+        self.edge_wave = L.EDGE_WAVE_MAX if et.get('wave') is True else int(et.get('wave', 0))
         self.src_walk = SRC_WALK
         self._index_pending = []  # stored segments whose agent index is built on demand
         self._index_tensors = []
@@ -691,13 +706,20 @@ class BatchState:
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
         self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
 
-    def set_edge_tile(self, tile, resident=False):
-        """Edges per edge-pass tile (one of L.EDGE_TILES) and whether the source
-        bitmap is resident in shared memory (one sim only); the autotuner's knobs."""
+    def set_edge_tile(self, tile, resident=False, wave=0):
+        """Edges per edge-pass tile (one of L.EDGE_TILES), whether the source bitmap
+        is resident in shared memory (one sim only), and whether the stored layers'
+        pass runs as one wave of blocks walking balanced ranges of tiles (wave: at
+        most that many blocks per SM; True: as many as fit); the autotuner's knobs."""
         if int(tile) not in L.EDGE_TILES:
             raise ValueError(f'edge tile must be one of {L.EDGE_TILES}')
+        if resident and wave:
+            raise ValueError('the resident-bitmap edge pass has its own grid (one block per SM)')
         self.edge_tile = int(tile)
         self.edge_resident = False
+        self.edge_wave = L.EDGE_WAVE_MAX if wave is True else int(wave)
+        if self.edge_wave < 0:
+            raise ValueError('wave: blocks per SM, at least 1 (0: one block per tile)')
         self._tile_segments()
         self._refresh_state()
         if resident:
@@ -726,8 +748,14 @@ class BatchState:
     @property
     def edge_tile_label(self):
         """The edge-pass configuration as one value: the tile size, suffixed 'r'
-        when the source bitmap is resident in shared memory ('4096r')."""
-        return f'{self.edge_tile}r' if self.edge_resident else self.edge_tile
+        when the source bitmap is resident in shared memory ('4096r'), 'w' when the
+        stored layers' pass runs as one wave ('1024w'; '1024w4': at most four blocks
+        per SM)."""
+        if self.edge_resident:
+            return f'{self.edge_tile}r'
+        if self.edge_wave:
+            return f'{self.edge_tile}w' + ('' if self.edge_wave == L.EDGE_WAVE_MAX else str(self.edge_wave))
+        return self.edge_tile
 
     def apply_edge_tile(self, choice):
         """Set the edge pass from a user choice: None (the default tile), 'auto'
@@ -738,8 +766,7 @@ class BatchState:
             from .autotune import tune_edge_tile
             tune_edge_tile(self)
             return
-        text = str(choice)
-        self.set_edge_tile(int(text.rstrip('r')), resident=text.endswith('r'))
+        self.set_edge_tile(**parse_edge_tile(choice))
 
     def _build_sims(self, beta_tabs, bl_tabs, kins):
         recs = []
@@ -855,6 +882,7 @@ class BatchState:
         st.n_agent_blocks = self.n_agent_blocks
         st.edge_tile = self.edge_tile
         st.edge_resident = int(self.edge_resident)
+        st.edge_wave = int(self.edge_wave)
         for k in ('flags', 'vstate', 'symp_prob', 'severe_prob', 'crit_prob', 'death_prob', 'rel_trans', 'rel_sus',
                   'n_infections', 'n_breakthroughs', 'peak_nab', 'nab', 't_nab_event', 'vaccine_source', 'sus_imm',
                   'symp_imm', 'sev_imm', 'dates', 'durs', 'viral_load', 'roles', 'claim', 'src_rec', 'tgt_rec',
@@ -992,8 +1020,11 @@ class BatchState:
         """The ops' state argument: the address of the current covgpu_state descriptor."""
         return torch_ops.state_arg(self.cstate)
 
-    def agent_step(self, t, do_prev=True, do_day=True):
-        torch.ops.covgpu.agent_step(self._sa, int(t), bool(do_prev), bool(do_day), self.t['status'])
+    def agent_step(self, t, do_prev=True, do_day=True, steady=False):
+        """One agent pass (covgpu_agent_step); steady: a full pass of day t - 1 or
+        earlier has run since the state was last changed outside the day kernels
+        (as in a launch sequence), so warps of susceptible naive agents are skipped."""
+        torch.ops.covgpu.agent_step(self._sa, int(t), bool(do_prev), bool(do_day), bool(steady), self.t['status'])
 
     def edge_pass(self, t, parts=0):
         """Day t's transmission: parts 0 both passes, 1 the stored layers only, 2 the

@@ -47,9 +47,11 @@ def state_arg(cstate):
 
 
 @torch.library.custom_op('covgpu::agent_step', mutates_args=('status',))
-def agent_step(state: int, t: int, do_prev: bool, do_day: bool, status: torch.Tensor) -> None:
-    """covgpu_agent_step: update_states_pre + check_immunity + update_nab + counts (people.py:164-186)."""
-    L.call('covgpu_agent_step', _st(state), int(t), int(do_prev), int(do_day), _stream())
+def agent_step(state: int, t: int, do_prev: bool, do_day: bool, steady: bool, status: torch.Tensor) -> None:
+    """covgpu_agent_step: update_states_pre + check_immunity + update_nab + counts (people.py:164-186);
+    steady: COVGPU_DAY_STEADY (a full pass has run since the state last changed outside the day kernels)."""
+    L.call('covgpu_agent_step', _st(state), int(t), int(do_prev),
+           int(do_day) | (L.DAY_STEADY if (steady and do_day) else 0), _stream())
 
 
 @torch.library.custom_op('covgpu::edge_pass', mutates_args=('status',))

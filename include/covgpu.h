@@ -305,6 +305,11 @@ typedef struct covgpu_state {
   int32_t edge_resident;          /* 1: one sim's source bitmap resident in shared
                                      memory (one block per SM; a single sim of at
                                      most ~1.1M agents, tiles of 4096 or 8192)     */
+  int32_t edge_wave;              /* > 0: the stored layers' pass as one wave of
+                                     blocks walking balanced ranges of tiles, at
+                                     most this many blocks per SM; 0: one block per
+                                     tile. Not with edge_resident.                 */
+  int32_t _pad_wave;
   /* per-agent state */
   uint32_t* flags;
   uint32_t* vstate;               /* bytes: exposed, infectious, recovered variant   */
@@ -497,7 +502,13 @@ int covgpu_pop_prognoses(int64_t n, const float* age, const double* cutoffs, int
  * day t-1 (stock counts, update_nab, NAb sum); with do_day, then runs day t's
  * update_states_pre (all checks, in the reference's order), check_immunity,
  * the flow counts, the viral load of the infectious and the source/target
- * role bitmaps the edge pass reads. Also resets the day's event counter. */
+ * role bitmaps the edge pass reads. Also resets the day's event counter.
+ * do_day | COVGPU_DAY_STEADY: the caller has run a full pass (do_day) of this
+ * state since anything but this library's day kernels last changed it, so the
+ * pass may skip the warps whose agents are all susceptible and naive and
+ * nothing else (their records and role bits are current; covgpu_run_days
+ * does this on every day of a launch sequence but the first). */
+#define COVGPU_DAY_STEADY 2
 int covgpu_agent_step(const covgpu_state* st, int32_t t, int32_t do_prev, int32_t do_day, void* stream);
 
 /* Transmission over every layer segment and variant: both directions of each

@@ -12,37 +12,54 @@ pytestmark = pytest.mark.gpu
 
 
 def test_every_edge_tile_gives_the_same_run():
-    """Every tile size, and the resident-bitmap variant of the edge pass, with testing and tracing."""
+    """Every tile size, the one-wave stored-layer pass (as many blocks per SM as fit,
+    and one or two), and the resident-bitmap variant, with testing and tracing."""
     ref = None
-    variants = [(t, False) for t in L.EDGE_TILES] + [(4096, True), (8192, True)]
-    for tile, resident in variants:
+    variants = ([str(t) for t in L.EDGE_TILES] + [f'{t}w' for t in L.EDGE_TILES] + ['1024w1', '4096w2']
+                + ['4096r', '8192r'])
+    for label in variants:
         sim = make_sim(*CASES[0])
         sim.initialize()
         assert sim.state.resident_possible()
-        sim.state.set_edge_tile(tile, resident=resident)
+        sim.state.apply_edge_tile(label)
+        assert str(sim.state.edge_tile_label) == label
         raw = sim.run().raw_results()
         if ref is None:
             ref = raw
         else:
             for k in TESTING_KEYS:
-                np.testing.assert_array_equal(raw[k], ref[k], err_msg=f'tile {tile} resident {resident} {k}')
+                np.testing.assert_array_equal(raw[k], ref[k], err_msg=f'edge pass {label} {k}')
+
+
+def test_wave_pass_over_a_batch_equals_single_runs():
+    """The one-wave pass over many sims' segments (shares cross sims and layers)."""
+    pars = [dict(pop_type='hybrid', pop_size=n, n_days=30, rand_seed=s, pop_infected=50)
+            for n, s in ((3000, 1), (9000, 2), (500, 3), (6000, 4))]
+    solo = [cv.Sim(p).run().raw_results() for p in pars]
+    for label in ('1024w', '8192w', '2048w3'):
+        batch = cv.BatchSim([cv.Sim(p) for p in pars], edge_tile=label).run()
+        for k in range(len(pars)):
+            got = batch.results(k)
+            for key in ('new_infections', 'new_recoveries', 'n_susceptible', 'n_exposed', 'pop_nabs'):
+                np.testing.assert_array_equal(got[key], solo[k][key], err_msg=f'{label} sim {k} {key}')
 
 
 def test_resident_variant_with_the_likelihood_matches():
     from covasim_gb300.adjoint import LikelihoodRun
     out = []
-    for resident in (False, True):
+    for label in ('4096', '4096r', '1024w'):
         sim = cv.Sim(pop_type='hybrid', pop_size=6000, n_days=40, rand_seed=3, pop_infected=40,
                      dynam_layer=dict(h=0, s=0, w=0, c=1))
         sim.initialize()
-        sim.state.set_edge_tile(4096, resident=resident)
+        sim.state.apply_edge_tile(label)
         run = LikelihoodRun(sim, checkpoint_every=10)
         ll, e = run.forward(run.params.theta0)
         out.append((ll, e, run.backward(1.0, np.ones(run.npts))))
-    (l0, e0, g0), (l1, e1, g1) = out
-    assert abs(l0 - l1) <= 1e-9 * abs(l0)
-    np.testing.assert_allclose(e0, e1, rtol=1e-9)
-    np.testing.assert_allclose(g0, g1, rtol=1e-9)
+    l0, e0, g0 = out[0]
+    for l1, e1, g1 in out[1:]:
+        assert abs(l0 - l1) <= 1e-9 * abs(l0)
+        np.testing.assert_allclose(e0, e1, rtol=1e-9)
+        np.testing.assert_allclose(g0, g1, rtol=1e-9)
 
 
 def test_resident_variant_is_refused_for_batches():
@@ -58,7 +75,7 @@ def test_autotuned_sim_equals_default_run():
     a = cv.Sim(pars).run().raw_results()
     s = cv.Sim(pars, edge_tile='auto')
     s.initialize()
-    assert s.state.edge_tile in L.EDGE_TILES
+    assert s.state.edge_tile in L.EDGE_TILES and s.state.edge_tile_label is not None
     b = s.run().raw_results()
     for k in ('new_infections', 'n_exposed', 'new_deaths'):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)

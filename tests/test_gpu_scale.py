@@ -3,8 +3,9 @@ waning immunity and the community layer redrawn daily (the configuration
 bench.py times), against the oracle run with the same Philox draws.
 
 * The first 40 days, with the resident-bitmap edge pass ('8192r': the source
-  bitmap of 1M agents, 122 KB, in shared memory beside the candidate queues)
-  and with the tiled pass ('8192'): every result series and the final state.
+  bitmap of 1M agents, 122 KB, in shared memory beside the candidate queues),
+  with the tiled pass ('8192') and with the one-wave pass ('1024w'): every
+  result series and the final state.
 * One day at the epidemic's peak (the day with the most new infections of a
   GPU run), started from the GPU's state of the evening before: the most
   sources, candidates and transmission events a day of this run holds.
@@ -41,12 +42,12 @@ def oracle_40_days(population):
     return orc
 
 
-@pytest.mark.parametrize('tile', ['8192r', '8192'])
+@pytest.mark.parametrize('tile', ['8192r', '8192', '1024w'])
 def test_bench_config_first_40_days_match_oracle(population, oracle_40_days, tile):
     popdict, person = population
     sim = cv.Sim(dict(BENCH_PARS, n_days=40), popdict=popdict, person=person, edge_tile=tile)
     sim.initialize()
-    assert sim.state.edge_tile_label == (tile if tile.endswith('r') else int(tile))
+    assert str(sim.state.edge_tile_label) == tile
     sim.run()
     compare_runs(sim, oracle_40_days)
 

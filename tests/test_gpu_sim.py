@@ -169,6 +169,33 @@ def test_step_mode_equals_graph_run():
         np.testing.assert_array_equal(ra[k], rc[k], err_msg=k)
 
 
+def test_steady_agent_steps_equal_the_run():
+    """The agent pass skips warps of susceptible naive agents on the days after a
+    full pass (every day of a launch sequence but the first, or single steps flagged
+    COVGPU_DAY_STEADY): single steps with the flag, a run with waning and a redrawn
+    layer in graph launches, and the full single steps all agree."""
+    from covasim_gb300.sim import init_infections
+    pars = dict(pop_type='hybrid', pop_size=20000, n_days=70, rand_seed=5, use_waning=True, pop_infected=10,
+                dynam_layer=dict(h=0, s=0, w=0, c=1))
+    ref = cv.Sim(pars).run().raw_results()
+    for steady in (True, False):
+        sim = cv.Sim(pars)
+        sim.initialize()
+        st = sim.state
+        init_infections(st, 0, sim.pars)
+        for t in range(sim.npts):
+            st.agent_step(t, do_prev=t > 0, do_day=True, steady=steady and t > 0)
+            st.edge_pass(t)
+            st.infect_claims(t)
+        st.agent_step(sim.npts, do_prev=True, do_day=False)
+        assert st.status() == 0
+        got = st.results(0)
+        for k in RES_KEYS + ['pop_nabs', 'pop_protection']:
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=f'steady {steady} {k}')
+    cum = np.cumsum(ref['new_infections'])
+    assert cum[15] < 0.01 * pars['pop_size'] < 0.3 * pars['pop_size'] < cum[-1]  # steady warps early, few late
+
+
 def test_graph_capture_and_replay_equal_the_direct_run():
     """covgpu_run_days launches a state's day range directly on its first run,
     captures it into a CUDA graph on the second and replays the graph after
