@@ -79,7 +79,8 @@ def parse():
     ap.add_argument('--no-batch256', action='store_true',
                     help='skip the 256-sim batched measurement (batched vs one by one) in the default line')
     ap.add_argument('--edge-tile', default='auto',
-                    help="edge-pass tile (1024/2048/4096/8192, suffix 'r' for the resident bitmap) or 'auto' (autotuner)")
+                    help="edge-pass tile (1024/2048/4096/8192, suffix 'w' for the one-wave stored-layer pass, "
+                         "'r' for the resident bitmap) or 'auto' (autotuner)")
     ap.add_argument('--src-walk', type=int, default=None,
                     help='walk of the stored layers from the day\'s sources: k walks while infectious x k < agents, '
                          '0 never, -1 always (default: the library\'s)')
