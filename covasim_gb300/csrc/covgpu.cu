@@ -1148,14 +1148,12 @@ __device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& 
   __syncwarp();
 }
 
+// The redrawn layers of the day's sources for one block's worth (vblock) of
+// agent blocks: two warps per agent block, each on four source-bitmap words.
 template <bool LIK>
-// four resident blocks per SM (64 registers): the pass over a 100-day 1M-agent run
-// took 2.70 ms of kernel time against 2.89 ms with three (80 registers)
-__global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st, int t) {
-  if (held(st, t)) return;
-  __shared__ EdgeQueue s_q[DYN_WARPS];
+__device__ __forceinline__ void dyn_body(const covgpu_state& st, int t, int64_t vblock, EdgeQueue* s_q) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t gw = (int64_t)blockIdx.x * DYN_WARPS + warp;
+  const int64_t gw = vblock * DYN_WARPS + warp;
   const int64_t b = gw >> 1;  // two warps per agent block
   if (b >= st.n_agent_blocks) return;  // warp-uniform
   const covgpu_agent_block blk = st.agent_blocks[b];
@@ -1254,14 +1252,6 @@ __global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st,
   }
 }
 
-int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s) {
-  if (st->n_dynamic == 0) return COVGPU_OK;
-  const unsigned grid = (unsigned)((2 * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
-  if (st->lik.factor) k_dyn_pass<true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
-  else k_dyn_pass<false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t);
-  return launch_status();
-}
-
 // The walk of the stored layers from the day's sources (seg_walked): one warp per
 // four source-bitmap words, as the redrawn layers' pass. For each indexed stored
 // layer the warp's sources' edges (as p1: [rp1[a], rp1[a + 1]); as p2: the edges
@@ -1311,11 +1301,9 @@ __device__ __forceinline__ void src_drain(const covgpu_state& st, const SegCtx& 
 }
 
 template <bool LIK>
-__global__ void __launch_bounds__(SRC_WARPS * 32) k_src_pass(covgpu_state st, int t) {
-  if (held(st, t)) return;
-  __shared__ SrcQueue s_q[SRC_WARPS];
+__device__ __forceinline__ void src_body(const covgpu_state& st, int t, int64_t vblock, SrcQueue* s_q) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t gw = (int64_t)blockIdx.x * SRC_WARPS + warp;
+  const int64_t gw = vblock * SRC_WARPS + warp;
   const int64_t b = gw >> 1;  // two warps per agent block
   if (b >= st.n_agent_blocks) return;  // warp-uniform
   const covgpu_agent_block blk = st.agent_blocks[b];
@@ -1405,11 +1393,61 @@ __global__ void __launch_bounds__(SRC_WARPS * 32) k_src_pass(covgpu_state st, in
   }
 }
 
+static_assert(SRC_WARPS == DYN_WARPS, "the per-source passes share their launch shape");
+
+// The redrawn layers' pass (dyn_body), and with WALK also the walk of the stored
+// layers from the day's sources (src_body) in blocks [dyn_blocks, 2 dyn_blocks)
+// of the same launch: both start from the day's source bitmap, so on the days the
+// stored layers are walked the walk runs beside the redrawn layers' draws instead
+// of after the stored layers' (then empty) tile pass. Four resident blocks per SM
+// (64 registers): the redrawn layers' pass over a 100-day 1M-agent run took
+// 2.70 ms of kernel time against 2.89 ms with three (80 registers).
+template <bool LIK, bool WALK>
+__global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st, int t, int dyn_blocks) {
+  if (held(st, t)) return;
+  __shared__ union {
+    EdgeQueue e[DYN_WARPS];
+    SrcQueue s[SRC_WARPS];
+  } s_q;
+  if (!WALK || (int)blockIdx.x < dyn_blocks) dyn_body<LIK>(st, t, blockIdx.x, s_q.e);
+  else src_body<LIK>(st, t, (int64_t)blockIdx.x - dyn_blocks, s_q.s);
+}
+
+// The walk alone (a state without redrawn layers, or the stored layers' pass on
+// its own).
+template <bool LIK>
+__global__ void __launch_bounds__(SRC_WARPS * 32) k_src_pass(covgpu_state st, int t) {
+  if (held(st, t)) return;
+  __shared__ SrcQueue s_q[SRC_WARPS];
+  src_body<LIK>(st, t, blockIdx.x, s_q);
+}
+
+unsigned source_pass_blocks(const covgpu_state* st) {
+  return (unsigned)((2 * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
+}
+
 int launch_src_pass(const covgpu_state* st, int t, cudaStream_t s) {
   if (st->n_tiles == 0 || st->src_walk == 0) return COVGPU_OK;
-  const unsigned grid = (unsigned)((2 * st->n_agent_blocks + SRC_WARPS - 1) / SRC_WARPS);
+  const unsigned grid = source_pass_blocks(st);
   if (st->lik.factor) k_src_pass<true><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
   else k_src_pass<false><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
+  return launch_status();
+}
+
+// the redrawn layers' pass; with_walk: also the walk of the stored layers (when
+// src_walk is on), in the same launch
+int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s, bool with_walk) {
+  if (st->n_dynamic == 0) return COVGPU_OK;
+  const unsigned g = source_pass_blocks(st);
+  const bool walk = with_walk && st->n_tiles > 0 && st->src_walk != 0;
+  const unsigned grid = walk ? 2 * g : g;
+  if (st->lik.factor) {
+    if (walk) k_dyn_pass<true, true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
+    else k_dyn_pass<true, false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
+  } else {
+    if (walk) k_dyn_pass<false, true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
+    else k_dyn_pass<false, false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
+  }
   return launch_status();
 }
 
@@ -1522,7 +1560,9 @@ void launch_edge_res(const covgpu_state* st, int t, cudaStream_t s) {
   else launch_pdl(k_edge_pass_res<LIK, 4096>, grid, RES_THREADS, (size_t)smem, s, *st, t);
 }
 
-int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s) {
+// the stored layers' tile pass; with_walk: then the walk from the sources (when
+// src_walk is on) as its own launch
+int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s, bool with_walk) {
   if (st->n_tiles == 0) return COVGPU_OK;
   if (st->edge_resident) {
     if (st->lik.factor) launch_edge_res<true>(st, t, s);
@@ -1533,13 +1573,16 @@ int launch_stored_pass(const covgpu_state* st, int t, cudaStream_t s) {
     launch_edge_tiles<false>(st, t, s);
   }
   const int rc = launch_status();
-  return rc ? rc : launch_src_pass(st, t, s);
+  return (rc || !with_walk) ? rc : launch_src_pass(st, t, s);
 }
 
-// the stored layers' tiles, then the redrawn layers' sources (parts: 0 both, 1 or 2 one of them)
+// the stored layers' tiles, then the redrawn layers' sources (parts: 0 both, 1 or 2
+// one of them); the walk of the stored layers goes with the redrawn layers' pass
+// when both run, else with the stored layers'
 int launch_edge_pass(const covgpu_state* st, int t, cudaStream_t s, int parts = 0) {
-  const int rc = parts == 2 ? COVGPU_OK : launch_stored_pass(st, t, s);
-  return (rc || parts == 1) ? rc : launch_dyn_pass(st, t, s);
+  const bool walk_with_dyn = parts == 0 && st->n_dynamic > 0;
+  const int rc = parts == 2 ? COVGPU_OK : launch_stored_pass(st, t, s, !walk_with_dyn);
+  return (rc || parts == 1) ? rc : launch_dyn_pass(st, t, s, walk_with_dyn);
 }
 
 // The same two passes side by side: they read the same start-of-day state and
@@ -1558,10 +1601,10 @@ int launch_edge_pass_forked(const covgpu_state* st, int t, cudaStream_t s) {
   }
   if (cudaEventRecord(g_fork_ev, s) != cudaSuccess || cudaStreamWaitEvent(g_side_stream, g_fork_ev, 0) != cudaSuccess)
     return COVGPU_CUDA_ERROR;
-  int rc = launch_dyn_pass(st, t, g_side_stream);
+  int rc = launch_dyn_pass(st, t, g_side_stream, true);
   if (rc) return rc;
   if (cudaEventRecord(g_join_ev, g_side_stream) != cudaSuccess) return COVGPU_CUDA_ERROR;
-  rc = launch_stored_pass(st, t, s);
+  rc = launch_stored_pass(st, t, s, false);
   if (rc) return rc;
   return cudaStreamWaitEvent(s, g_join_ev, 0) == cudaSuccess ? COVGPU_OK : COVGPU_CUDA_ERROR;
 }

@@ -252,12 +252,15 @@ def ili_agents(seed, t, n, n_ili):
     return np.sort(rng.choice(int(n), int(n_ili), replace=False)).astype(np.int32)
 
 
-# Default of covgpu_state.src_walk: the stored layers are streamed every day.
-# Walking them from the day's sources (set_src_walk) gives the same results; on
-# a 1M-agent hybrid run (62 MB of stored edges, L2-resident) walking below an
-# eighth infectious made the run 5% slower, on a 20M-agent run (1.2 GB of stored
-# edges) walking below a sixty-fourth 2% faster.
-SRC_WALK = 0
+# Default of covgpu_state.src_walk for a state with a redrawn layer: the stored
+# layers are walked from the day's sources while fewer than 1/128 of a sim's agents
+# are infectious, and streamed otherwise (results are the same either way). The
+# walk then runs in the redrawn layers' launch, beside their draws: on the 1M-agent
+# hybrid run, 18.45 -> 18.0 ms per run (thresholds 1/64 to 1/512 within 0.1 ms of
+# each other). Without a redrawn layer the walk is a launch of its own after the
+# tile pass, which costs about 12 us a day before any source is walked, and the
+# stored layers are streamed (0).
+SRC_WALK = 128
 
 
 def parse_edge_tile(choice):
@@ -283,7 +286,7 @@ class BatchState:
         self.edge_tile = et['tile']
         self.edge_resident = False
         self.edge_wave = L.EDGE_WAVE_MAX if et.get('wave') is True else int(et.get('wave', 0))
-        self.src_walk = SRC_WALK
+        self.src_walk = SRC_WALK if any(ly.get('dynamic') for sp in specs for ly in sp.layers) else 0
         self._index_pending = []  # stored segments whose agent index is built on demand
         self._index_tensors = []
         if not torch.cuda.is_available():

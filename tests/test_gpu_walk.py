@@ -1,10 +1,11 @@
 """The quiet-day walk of the stored layers (covgpu_state.src_walk) is a pure
 performance choice: walking every indexed stored layer from the day's sources
-(-1), streaming every edge (0, the default) and the per-day choice (8: walk
-while a sim's infectious agents are under an eighth of its agents) queue the
-same candidates and draw, key and claim them alike, so whole runs are
-bit-identical, with testing and tracing, in batches and with the likelihood
-passes."""
+(-1), streaming every edge (0, the default without a redrawn layer) and the
+per-day choice (8 or 128, the default with a redrawn layer: walk while a sim's
+infectious agents are under that fraction of its agents) queue the same
+candidates and draw, key and claim them alike, so whole runs are bit-identical,
+with testing and tracing, in batches and with the likelihood passes; with a
+redrawn layer the walk runs in that layer's launch, otherwise in its own."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,7 @@ from test_gpu_testing import TESTING_KEYS, make_sim, CASES
 
 pytestmark = pytest.mark.gpu
 
-MODES = (0, -1, 8)
+MODES = (0, -1, 8, 128)
 PEOPLE_KEYS = [k for k in ALL_KEYS if k not in ('age', 'sex', 'uid', 'doses')]
 
 
@@ -27,7 +28,14 @@ def _run(make, mode):
     return sim
 
 
-@pytest.mark.parametrize('tile', ['4096', '8192r'])
+def test_walk_default_follows_the_redrawn_layers():
+    hybrid = cv.Sim(pop_type='hybrid', pop_size=3000, n_days=5, dynam_layer=dict(h=0, s=0, w=0, c=1)).initialize()
+    assert hybrid.state.src_walk == 128
+    plain = cv.Sim(pop_type='random', pop_size=3000, n_days=5).initialize()
+    assert plain.state.src_walk == 0
+
+
+@pytest.mark.parametrize('tile', ['2048w', '4096', '8192r'])
 def test_walked_and_streamed_runs_are_identical(tile):
     """Hybrid with waning and the community layer redrawn: the epidemic passes
     through quiet and busy days, so mode 8 uses both paths."""
