@@ -41,6 +41,10 @@ namespace {
 // completed and its writes are visible. Launched the ordinary way, pdl_wait
 // returns at once.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// A block's signal that the next kernel's blocks may be scheduled once every block
+// of this grid has given it or exited: their set-up before pdl_wait (tables,
+// read-only descriptors) then overlaps this grid's last blocks.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 template <typename... K, typename... A>
 void launch_pdl(void (*kernel)(K...), unsigned grid, unsigned block, size_t smem, cudaStream_t s, A... args) {
   cudaLaunchConfig_t cfg = {};
@@ -436,6 +440,23 @@ __device__ __noinline__ void agent_flush(const covgpu_state& st, int sim, int t,
 // one sim, and the counters go to the results once per sim a block touched
 // instead of once per 256 agents.
 __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, int do_day, int full_imm, int steady) {
+  const int64_t nb = st.n_agent_blocks;
+  const int64_t per = (nb + gridDim.x - 1) / gridDim.x;
+  int64_t b = (int64_t)blockIdx.x * per;
+  const int64_t b_end = min(nb, b + per);
+  if (b >= b_end) return;  // block-uniform
+
+  // set-up that reads nothing an earlier kernel writes: before pdl_wait
+  __shared__ AgentCounters sc;
+  __shared__ float s_ln_tab[COVGPU_LN_N][2];
+  __shared__ float s_exp_tab[COVGPU_EXP_N][2];
+  for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
+  for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
+  agent_counters_clear(sc);
+  covgpu_agent_block blk = st.agent_blocks[b];
+  int sim = blk.sim;
+  __syncthreads();
+
   pdl_wait();
   if (st.hold) {  // a held day t - 1 has nothing to close; a held day t closes day t - 1 only
     const int h = *st.hold;
@@ -444,24 +465,8 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
     if (!do_prev && !do_day) return;
   }
   if (do_day && blockIdx.x == 0 && threadIdx.x == 0) *st.event_count = 0ull;
-  const int64_t nb = st.n_agent_blocks;
-  const int64_t per = (nb + gridDim.x - 1) / gridDim.x;
-  int64_t b = (int64_t)blockIdx.x * per;
-  const int64_t b_end = min(nb, b + per);
-  if (b >= b_end) return;  // block-uniform
-
-  covgpu_agent_block blk = st.agent_blocks[b];
-  int sim = blk.sim;
   AgentIn cur = agent_load(st, blk.begin + threadIdx.x, blk.begin + threadIdx.x < blk.end,
                            st.sims[sim].use_waning != 0);
-
-  __shared__ AgentCounters sc;
-  __shared__ float s_ln_tab[COVGPU_LN_N][2];
-  __shared__ float s_exp_tab[COVGPU_EXP_N][2];
-  for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
-  for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
-  agent_counters_clear(sc);
-  __syncthreads();
 
   long long nab_fx = 0, sus_fx = 0, symp_fx = 0;
   unsigned acc_prev = 0, acc_day = 0;
@@ -485,6 +490,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
     blk = nblk;
     cur = nxt;
   }
+  pdl_trigger();
   agent_flush(st, sim, t, do_prev, do_day, sc, nab_fx, sus_fx, symp_fx, acc_prev, acc_day, false);
 }
 
@@ -953,6 +959,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
   LikAcc acc;
   edge_tile<LIK, EDGE_THREADS, TILE, false>(st, t, s_seg, (int64_t)blockIdx.x, &s_L, &s_sp, nullptr,
                                             s_q[threadIdx.x >> 5], acc);
+  pdl_trigger();
   if (LIK) {  // the tile's sums: one sim, one layer
     __shared__ double s_acc[EDGE_THREADS / 32][2];
     const double a = warp_sum_d(ff_to_d(acc.ll)), b = warp_sum_d(ff_to_d(acc.g));
@@ -978,8 +985,6 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_pass(covgpu_state st, int
 // latency); the tile size only sets how finely the shares are balanced.
 template <bool LIK, int ROUNDS>
 __global__ void __launch_bounds__(EDGE_THREADS) k_edge_wave(covgpu_state st, int t) {
-  pdl_wait();
-  if (held(st, t)) return;
   constexpr int64_t TILE = (int64_t)ROUNDS * EDGE_ROUND;
   const int64_t lo = st.n_tiles * (int64_t)blockIdx.x / gridDim.x;
   const int64_t hi = st.n_tiles * ((int64_t)blockIdx.x + 1) / gridDim.x;
@@ -988,7 +993,9 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_wave(covgpu_state st, int
   __shared__ SimLite s_sp;
   __shared__ EdgeQueue s_q[EDGE_THREADS / 32];
   __shared__ double s_acc[EDGE_THREADS / 32][2];
-  int seg = segment_of_tile(st.segments, st.n_segments, lo);
+  int seg = segment_of_tile(st.segments, st.n_segments, lo);  // the segment table is read-only
+  pdl_wait();
+  if (held(st, t)) return;
   int64_t tile = lo;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -1022,6 +1029,7 @@ __global__ void __launch_bounds__(EDGE_THREADS) k_edge_wave(covgpu_state st, int
     ++seg;
     __syncthreads();  // every thread has read s_L (and s_acc) before they are replaced
   }
+  pdl_trigger();
 }
 
 // Resident-bitmap variant for a single sim: one block of RES_THREADS per SM
@@ -1065,6 +1073,7 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
     edge_tile<LIK, RES_THREADS, TILE, true>(st, t, seg, tile, s_segs + seg, &s_sp, s_src, q, acc);
     if (LIK) lik_flush_warp(st, t, s_segs[seg].sim, s_segs[seg].layer, acc);
   }
+  pdl_trigger();
 }
 
 // ============================================================ redrawn layers
@@ -2108,6 +2117,7 @@ __device__ __forceinline__ void hosp_icu(const covgpu_state& st, const covgpu_si
 
 __global__ void k_infect_claims(covgpu_state st, int t) {
   pdl_wait();
+  pdl_trigger();  // the next day's agent pass may set up while the infections run
   if (held(st, t)) return;
   const unsigned long long cnt = *st.event_count;
   const int64_t n = (int64_t)cnt < st.event_capacity ? (int64_t)cnt : st.event_capacity;
