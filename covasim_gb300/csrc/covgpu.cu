@@ -1450,13 +1450,9 @@ int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s, bool with_wal
   const unsigned g = source_pass_blocks(st);
   const bool walk = with_walk && st->n_tiles > 0 && st->src_walk != 0;
   const unsigned grid = walk ? 2 * g : g;
-  if (st->lik.factor) {
-    if (walk) k_dyn_pass<true, true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
-    else k_dyn_pass<true, false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
-  } else {
-    if (walk) k_dyn_pass<false, true><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
-    else k_dyn_pass<false, false><<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
-  }
+  void (*k)(covgpu_state, int, int) = st->lik.factor ? (walk ? k_dyn_pass<true, true> : k_dyn_pass<true, false>)
+                                                     : (walk ? k_dyn_pass<false, true> : k_dyn_pass<false, false>);
+  k<<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
   return launch_status();
 }
 
