@@ -68,13 +68,17 @@ def mean_infectious_duration(d_rec, d_dead, d_inf):
     """sim.py:920-932: mean of the outcome dates minus mean of the infectious dates,
     over the agents with a recovery date then those with a death date (numpy
     arrays or device tensors; sums in float64)."""
-    if torch.is_tensor(d_rec):
+    if torch.is_tensor(d_rec):  # masked sums on the device, one read-back
         m_rec, m_dead = ~torch.isnan(d_rec), ~torch.isnan(d_dead)
-        n_out = int(m_rec.sum().item() + m_dead.sum().item())
+        zero = d_rec.new_zeros(())
+        sums = torch.stack([m_rec.sum().double() + m_dead.sum().double(),
+                            torch.where(m_rec, d_rec, zero).double().sum() +
+                            torch.where(m_dead, d_dead, zero).double().sum(),
+                            torch.where(m_rec, d_inf, zero).double().sum() +
+                            torch.where(m_dead, d_inf, zero).double().sum()])
+        n_out, s_out, s_inf = sums.tolist()
         if not n_out:
             return 0.0
-        s_out = float(d_rec[m_rec].double().sum() + d_dead[m_dead].double().sum())
-        s_inf = float(d_inf[m_rec].double().sum() + d_inf[m_dead].double().sum())
     else:
         m_rec, m_dead = ~np.isnan(d_rec), ~np.isnan(d_dead)
         n_out = int(m_rec.sum() + m_dead.sum())
