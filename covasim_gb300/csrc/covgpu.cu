@@ -153,7 +153,8 @@ static_assert(DW_VAR + COVGPU_MAX_VARIANTS <= DW_SRC, "day-word layout");
 __device__ __forceinline__ void agent_block_step(const covgpu_state& st, const covgpu_agent_block& blk,
                                                  const AgentIn& in, int t, int do_prev, int do_day, int full_imm,
                                                  int steady,
-                                                 const float (*s_ln_tab)[2], const float (*s_exp_tab)[2],
+                                                 const float (*s_ln_tab)[2], const float* s_ln_inv,
+                                                 const float (*s_exp_tab)[2],
                                                  long long& nab_fx, long long& sus_fx, long long& symp_fx,
                                                  unsigned& acc_prev, unsigned& acc_day) {
   const covgpu_sim_params& sp = st.sims[blk.sim];
@@ -299,7 +300,7 @@ __device__ __forceinline__ void agent_block_step(const covgpu_state& st, const c
           const float imm = imm_of(st, sp, i, v, f, was_inf, rv, ln_imm);
           float a = 0.0f, b = 0.0f, c = 0.0f;
           if (nab > 0.0f && imm > 0.0f) {  // eff = nab * imm > 0; else every efficacy is 0
-            if (!have_ln) { ln_nab = ff_log(nab, s_ln_tab); have_ln = true; }
+            if (!have_ln) { ln_nab = ff_log(nab, s_ln_tab, s_ln_inv); have_ln = true; }
             const ff ln_eff = ff_add(ln_nab, ln_imm);
             a = ve_axis(sp, 0, ln_eff, s_exp_tab);
             b = ve_axis(sp, 1, ln_eff, s_exp_tab);
@@ -449,8 +450,10 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
   // set-up that reads nothing an earlier kernel writes: before pdl_wait
   __shared__ AgentCounters sc;
   __shared__ float s_ln_tab[COVGPU_LN_N][2];
+  __shared__ float s_ln_inv[COVGPU_LN_N];
   __shared__ float s_exp_tab[COVGPU_EXP_N][2];
   for (int k = threadIdx.x; k < 2 * COVGPU_LN_N; k += blockDim.x) (&s_ln_tab[0][0])[k] = (&COVGPU_LN_TAB[0][0])[k];
+  for (int k = threadIdx.x; k < COVGPU_LN_N; k += blockDim.x) s_ln_inv[k] = COVGPU_LN_INV[k];
   for (int k = threadIdx.x; k < 2 * COVGPU_EXP_N; k += blockDim.x) (&s_exp_tab[0][0])[k] = (&COVGPU_EXP_TAB[0][0])[k];
   agent_counters_clear(sc);
   covgpu_agent_block blk = st.agent_blocks[b];
@@ -479,7 +482,7 @@ __global__ void AGENT_BOUNDS k_agent_step(covgpu_state st, int t, int do_prev, i
       const int64_t ni = nblk.begin + threadIdx.x;
       nxt = agent_load(st, ni, ni < nblk.end, st.sims[nblk.sim].use_waning != 0);
     }
-    agent_block_step(st, blk, cur, t, do_prev, do_day, full_imm, steady, s_ln_tab, s_exp_tab, nab_fx, sus_fx,
+    agent_block_step(st, blk, cur, t, do_prev, do_day, full_imm, steady, s_ln_tab, s_ln_inv, s_exp_tab, nab_fx, sus_fx,
                      symp_fx, acc_prev, acc_day);
     if (!more) break;
     ++b;
@@ -538,7 +541,7 @@ __device__ __forceinline__ ff ff_mul_f(ff x, float f) {
 // ln of a positive float-float: ln(hi) + lo / hi (|lo / hi| <= 2^-24, so the
 // dropped term is below 2^-49)
 __device__ __forceinline__ ff ff_log_ff(ff x) {
-  const ff l = ff_log(x.hi, COVGPU_LN_TAB);
+  const ff l = ff_log(x.hi, COVGPU_LN_TAB, COVGPU_LN_INV);
   return fast_two_sum(l.hi, __fadd_rn(l.lo, __fdiv_rn(x.lo, x.hi)));
 }
 __device__ __forceinline__ double ff_to_d(ff x) { return __dadd_rn((double)x.hi, (double)x.lo); }
@@ -1685,7 +1688,7 @@ struct DrawSet {
   __device__ __forceinline__ bool lt(int k, float p) const { return injected ? (u[k] < (double)p) : bern32(uw[k], p); }
   // the normals of the severe branch: only severe cases need them
   __device__ __forceinline__ void severe_normals() {
-    if (!injected) box_muller_ff(w23[0], w23[1], COVGPU_LN_TAB, COVGPU_SINCOS_TAB, z[2], z[3]);
+    if (!injected) box_muller_ff(w23[0], w23[1], COVGPU_LN_TAB, COVGPU_LN_INV, COVGPU_SINCOS_TAB, z[2], z[3]);
   }
 };
 
@@ -1705,10 +1708,10 @@ __device__ __forceinline__ void get_draws(const covgpu_state& st, const covgpu_s
   const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b1 = philox(make_uint4((uint32_t)local, 1u, (uint32_t)t, tag), sp.key0, sp.key1);
   const uint4 b2 = philox(make_uint4((uint32_t)local, 2u, (uint32_t)t, tag), sp.key0, sp.key1);
-  box_muller_ff(b0.x, b0.y, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, d.z[0], d.z[1]);
+  box_muller_ff(b0.x, b0.y, COVGPU_LN_TAB, COVGPU_LN_INV, COVGPU_SINCOS_TAB, d.z[0], d.z[1]);
   d.w23[0] = b0.z;
   d.w23[1] = b0.w;
-  box_muller_ff(b1.x, b1.y, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, d.z[4], d.z[5]);
+  box_muller_ff(b1.x, b1.y, COVGPU_LN_TAB, COVGPU_LN_INV, COVGPU_SINCOS_TAB, d.z[4], d.z[5]);
   d.uw[0] = b1.z;
   d.uw[1] = b1.w;
   d.uw[2] = b2.x;
@@ -1728,7 +1731,7 @@ __device__ float sev_imm_with(const covgpu_state& st, const covgpu_sim_params& s
   ff ln_imm;
   const float imm = imm_of(st, sp, i, v, f, (float)t >= d_rec, (vs >> 16) & 0xFFu, ln_imm);
   if (!(imm > 0.0f)) return 0.0f;
-  return ve_axis(sp, 2, ff_add(ff_log(nab, COVGPU_LN_TAB), ln_imm), COVGPU_EXP_TAB);
+  return ve_axis(sp, 2, ff_add(ff_log(nab, COVGPU_LN_TAB, COVGPU_LN_INV), ln_imm), COVGPU_EXP_TAB);
 }
 __device__ float sev_imm_of(const covgpu_state& st, const covgpu_sim_params& sp, int64_t i, int t, int v, uint32_t f) {
   if (!sp.use_waning) return st.sev_imm[(int64_t)v * st.n + i];
@@ -1938,7 +1941,7 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
       const uint4 b0 = philox(make_uint4((uint32_t)local, 0u, (uint32_t)t, tag), sp.key0, sp.key1);
       const uint32_t wa = r == 0 ? b0.x : (r == 1 ? b0.z : b1.x);
       const uint32_t wb = r == 0 ? b0.y : (r == 1 ? b0.w : b1.y);
-      box_muller_ff(wa, wb, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, za, zb);
+      box_muller_ff(wa, wb, COVGPU_LN_TAB, COVGPU_LN_INV, COVGPU_SINCOS_TAB, za, zb);
     }
     const int rec_d = !symp ? COVGPU_D_ASYM2REC : (!sev ? COVGPU_D_MILD2REC : (!crit ? COVGPU_D_SEV2REC
                                                                                 : (dead ? COVGPU_D_CRIT2DIE

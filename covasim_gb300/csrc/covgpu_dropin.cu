@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(DROPIN_THREADS) k_check_immunity(covgpu_state 
       const float imm = imm_of(st, sp, i, v, f, was_inf, rv, ln_imm);
       float a = 0.0f, b = 0.0f, c = 0.0f;
       if (nab > 0.0f && imm > 0.0f) {
-        if (!have_ln) { ln_nab = ff_log(nab, COVGPU_LN_TAB); have_ln = true; }
+        if (!have_ln) { ln_nab = ff_log(nab, COVGPU_LN_TAB, COVGPU_LN_INV); have_ln = true; }
         const ff ln_eff = ff_add(ln_nab, ln_imm);
         a = ve_axis(sp, 0, ln_eff, COVGPU_EXP_TAB);
         b = ve_axis(sp, 1, ln_eff, COVGPU_EXP_TAB);
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(DROPIN_THREADS) k_update_peak_nab(covgpu_state
       const uint4 w = philox(make_uint4((uint32_t)local, 3u, (uint32_t)t, TAG_INFECT | (uint32_t)call_tag), sp.key0,
                              sp.key1);
       ff z0, z1;
-      box_muller_ff(w.x, w.y, COVGPU_LN_TAB, COVGPU_SINCOS_TAB, z0, z1);
+      box_muller_ff(w.x, w.y, COVGPU_LN_TAB, COVGPU_LN_INV, COVGPU_SINCOS_TAB, z0, z1);
       double peak = exp2_ff(d2ff(sample_ff(init, z0)));
       if (symp_class) {
         const int c = symp_class[j];

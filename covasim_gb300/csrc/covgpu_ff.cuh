@@ -14,8 +14,9 @@
 // Only IEEE round-to-nearest add/sub/mul/div and fused multiply-add (used for
 // exact product residuals only) appear, in a fixed order: the numpy mirror in
 // the oracle (oracle/gpu_arith.py) performs the same operations and gets the
-// same bits. ln uses the reduction x = 2^e * c_j * (1 + r), |r| < 2^-7.5, and
-// the series of ln(1 + r); exp uses Cody-Waite reduction by ln2/64, a table
+// same bits. ln uses the reduction x = 2^e * c_j * (1 + r), |r| < 2^-7.5 (r
+// formed with a table of 1 / c_j and the exact residual), and the series of
+// ln(1 + r); exp uses Cody-Waite reduction by ln2/64, a table
 // of 2^(j/64) and the Taylor series of exp(r), |r| <= ln2/128; cos and sin of
 // 2 pi u reduce exactly to a quadrant and the nearest of the points
 // j pi / 64 and use the Taylor series of the residual |phi| <= pi / 128.
@@ -49,17 +50,23 @@ __device__ __forceinline__ ff ff_mul(ff x, ff y) {
   const ff p = two_prod(x.hi, y.hi);
   return fast_two_sum(p.hi, __fadd_rn(p.lo, __fadd_rn(__fmul_rn(x.hi, y.lo), __fmul_rn(x.lo, y.hi))));
 }
+
+// a / b as float-float with one correctly rounded reciprocal instead of two
+// divisions: q1 = a.hi * (1 / b.hi), then the residual a - q1 b (exact product
+// residual) times the same reciprocal
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const float rcp = __frcp_rn(b.hi);
+  const float q1 = __fmul_rn(a.hi, rcp);
   const ff p = two_prod(q1, b.hi);
   float r = __fsub_rn(__fsub_rn(a.hi, p.hi), p.lo);
   r = __fadd_rn(r, a.lo);
   r = __fsub_rn(r, __fmul_rn(q1, b.lo));
-  return fast_two_sum(q1, __fdiv_rn(r, b.hi));
+  return fast_two_sum(q1, __fmul_rn(r, rcp));
 }
 
-// ln(x) for finite x > 0, as float-float. tab: COVGPU_LN_TAB (shared memory copy).
-__device__ __forceinline__ ff ff_log(float x, const float (*tab)[2]) {
+// ln(x) for finite x > 0, as float-float. tab: COVGPU_LN_TAB, inv: COVGPU_LN_INV
+// (shared-memory copies or the tables themselves).
+__device__ __forceinline__ ff ff_log(float x, const float (*tab)[2], const float* inv) {
   int e_adj = 0;
   if (x < 1.17549435e-38f) { x = __fmul_rn(x, 16777216.0f); e_adj = -24; }
   const int bits = __float_as_int(x);
@@ -69,8 +76,9 @@ __device__ __forceinline__ ff ff_log(float x, const float (*tab)[2]) {
   const int j = (int)rintf(__fmul_rn(__fsub_rn(m, 1.0f), 128.0f));
   const float c = __fadd_rn(1.0f, __fmul_rn((float)j, 0.0078125f));
   const float d = __fsub_rn(m, c);
-  const float rh = __fdiv_rn(d, c);
-  const float rl = __fdiv_rn(__fmaf_rn(-rh, c, d), c);
+  const float ic = inv[j - COVGPU_LN_J0];
+  const float rh = __fmul_rn(d, ic);                  // d / c to about an ulp
+  const float rl = __fmul_rn(__fmaf_rn(-rh, c, d), ic);  // the exact residual over c
   // ln(1 + r) = r - r^2/2 + r^3 (1/3 - r/4 + r^2/5 - r^3/6 + r^4/7)
   const ff sq = two_prod(rh, rh);
   const float qh = __fmul_rn(sq.hi, 0.5f);
@@ -123,19 +131,19 @@ __device__ __forceinline__ ff ff_exp(ff y, const float (*tab)[2]) {
 }
 
 // ln of a positive float-float: ln(hi) + lo / hi (|lo / hi| <= 2^-24, so the
-// dropped term is below 2^-49)
-__device__ __forceinline__ ff ff_log_ff(ff x, const float (*tab)[2]) {
-  const ff l = ff_log(x.hi, tab);
-  return fast_two_sum(l.hi, __fadd_rn(l.lo, __fdiv_rn(x.lo, x.hi)));
+// dropped term is below 2^-49; lo / hi as lo times the reciprocal of hi)
+__device__ __forceinline__ ff ff_log_ff(ff x, const float (*tab)[2], const float* inv) {
+  const ff l = ff_log(x.hi, tab, inv);
+  return fast_two_sum(l.hi, __fadd_rn(l.lo, __fmul_rn(x.lo, __frcp_rn(x.hi))));
 }
 
 // sqrt of a positive float-float: the float32 root and one correction by the
-// exact residual x - s^2
+// exact residual x - s^2 (over 2s, as a product with its reciprocal)
 __device__ __forceinline__ ff ff_sqrt(ff x) {
   const float s = __fsqrt_rn(x.hi);
   const ff p = two_prod(s, s);
   const float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p.hi), p.lo), x.lo);
-  return fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
+  return fast_two_sum(s, __fmul_rn(r, __frcp_rn(__fmul_rn(2.0f, s))));
 }
 
 // the uniform (a + 1/2) * 2^-32 of a 32-bit word, exactly, as float-float: the
@@ -186,8 +194,8 @@ __device__ __forceinline__ void ff_cossin_2pi(uint32_t b, const float (*tab)[4],
 
 // Box-Muller in float-float: z0 = r cos(2 pi u2), z1 = r sin(2 pi u2), r = sqrt(-2 ln u1)
 __device__ __forceinline__ void box_muller_ff(uint32_t wa, uint32_t wb, const float (*ln_tab)[2],
-                                              const float (*sc_tab)[4], ff& z0, ff& z1) {
-  const ff l = ff_log_ff(u01_ff(wa), ln_tab);
+                                              const float* ln_inv, const float (*sc_tab)[4], ff& z0, ff& z1) {
+  const ff l = ff_log_ff(u01_ff(wa), ln_tab, ln_inv);
   const ff r = ff_sqrt(ff{__fmul_rn(l.hi, -2.0f), __fmul_rn(l.lo, -2.0f)});
   ff c, s;
   ff_cossin_2pi(wb, sc_tab, c, s);

@@ -1,6 +1,6 @@
 """Generate covgpu_tables.h: float-float tables for the float64 steps of the path.
 
-ln(c_j) for the reduction points c_j = 1 + j/128 (j = -40..55), 2^(j/64)
+ln(c_j) for the reduction points c_j = 1 + j/128 (j = -40..55) and 1 / c_j, 2^(j/64)
 (j = 0..63), and sin / cos of j * pi / 64 (j = 0..32), each as a pair of
 float32 (hi, lo) with hi + lo equal to the value to about 2^-48, plus pi / 2
 and ln 2 as pairs. Values come from Python's decimal module at 50 digits
@@ -13,6 +13,8 @@ import math
 import os
 import struct
 from decimal import Decimal, getcontext
+
+import numpy as np
 
 getcontext().prec = 50
 
@@ -37,6 +39,12 @@ def ln_table():
         c = Decimal(1) + Decimal(j) / Decimal(128)
         out.append(split(c.ln()))
     return out
+
+
+def ln_inv_table():
+    """1 / c_j rounded once to float32 (c_j is exact in float32; float32 division
+    is correctly rounded)."""
+    return [float(np.float32(1.0) / np.float32(1.0 + j / 128.0)) for j in range(LN_J0, LN_J1 + 1)]
 
 
 def exp_table():
@@ -126,6 +134,9 @@ def main():
               '// sin and cos of j * pi / 64, j = 0..32: {sin hi, sin lo, cos hi, cos lo}',
               '__device__ const float COVGPU_SINCOS_TAB[33][4] = {']
     lines += [f'  {{{hexf(sv[0])}, {hexf(sv[1])}, {hexf(cv[0])}, {hexf(cv[1])}}},' for sv, cv in sincos_table()]
+    lines += ['};', '// 1 / c_j of the ln reduction points, rounded once to float32',
+              '__device__ const float COVGPU_LN_INV[COVGPU_LN_N] = {']
+    lines += [f'  {hexf(v)},' for v in ln_inv_table()]
     lines += ['};', '']
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'covgpu_tables.h')
     with open(path, 'w') as f:

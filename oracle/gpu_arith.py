@@ -37,6 +37,7 @@ def _split(d):
 LN_J0, LN_J1, EXP_N = -40, 55, 64
 _LN2 = Decimal(2).ln()
 LN_TAB = np.array([_split((Decimal(1) + Decimal(j) / Decimal(128)).ln()) for j in range(LN_J0, LN_J1 + 1)], F32)
+LN_INV = np.array([F32(1) / F32(1 + j / 128) for j in range(LN_J0, LN_J1 + 1)], F32)  # 1 / c_j, one rounding
 EXP_TAB = np.array([_split((Decimal(j) / Decimal(EXP_N) * _LN2).exp()) for j in range(EXP_N)], F32)
 _ln2_hi = float(round(_LN2 * 2 ** 16) / Decimal(2 ** 16))
 LN2_HI = F32(_ln2_hi)
@@ -87,19 +88,20 @@ def ff_mul(xh, xl, yh, yl):
 
 
 def ff_div(ah, al, bh, bl):
+    """a / b with one correctly rounded reciprocal (covgpu_ff.cuh ff_div)."""
     ah, al, bh, bl = _a(ah), _a(al), _a(bh), _a(bl)
-    q1 = ah / bh
+    rcp = F32(1) / bh
+    q1 = ah * rcp
     ph, pl = two_prod(q1, bh)
     r = (ah - ph) - pl
     r = r + al
     r = r - q1 * bl
-    return fast_two_sum(q1, r / bh)
+    return fast_two_sum(q1, r * rcp)
 
 
-def _fma_residual_div(rh, c, d):
-    """fmaf(-rh, c, d) / c: the residual d - rh*c is exact in float64 and in float32."""
-    res = (d.astype(np.float64) - rh.astype(np.float64) * c.astype(np.float64)).astype(F32)
-    return res / c
+def _fma_residual(rh, c, d):
+    """fmaf(-rh, c, d): d - rh*c is exact in float64, then rounded once to float32."""
+    return (d.astype(np.float64) - rh.astype(np.float64) * c.astype(np.float64)).astype(F32)
 
 
 # ----------------------------------------------------------------- ln, exp, VE, update_nab
@@ -117,8 +119,9 @@ def ff_log(x):
     j = np.rint((m - F32(1)) * F32(128)).astype(np.int32)
     c = F32(1) + j.astype(F32) * F32(0.0078125)
     d = m - c
-    rh = d / c
-    rl = _fma_residual_div(rh, c, d)
+    ic = LN_INV[j - LN_J0]
+    rh = d * ic
+    rl = _fma_residual(rh, c, d) * ic
     sqh, sql = two_prod(rh, rh)
     qh = sqh * F32(0.5)
     ql = sql * F32(0.5) + rh * rl
@@ -311,7 +314,7 @@ def ff_exp(yh, yl):
 
 def ff_log_ff(xh, xl):
     lh, ll = ff_log(xh)
-    return fast_two_sum(lh, ll + _a(xl) / _a(xh))
+    return fast_two_sum(lh, ll + _a(xl) * (F32(1) / _a(xh)))
 
 
 def ff_sqrt(xh, xl):
@@ -319,7 +322,7 @@ def ff_sqrt(xh, xl):
     s = np.sqrt(xh)
     ph, pl = two_prod(s, s)
     r = ((xh - ph) - pl) + xl
-    return fast_two_sum(s, r / (F32(2) * s))
+    return fast_two_sum(s, r * (F32(1) / (F32(2) * s)))
 
 
 def u01_ff(a):

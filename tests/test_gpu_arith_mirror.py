@@ -58,7 +58,9 @@ def test_tables_match_the_cuda_header():
     assert np.array_equal(tab[n_ln:n_ln + n_exp].reshape(-1, 2), ga.EXP_TAB)
     rest = tab[n_ln + n_exp:]
     assert list(rest[:4]) == [ga.PI_2_HI, ga.PI_2_LO, ga.LN2_FF_HI, ga.LN2_FF_LO]
-    assert np.array_equal(rest[4:].reshape(-1, 4), ga.SINCOS_TAB)
+    n_sc = ga.SINCOS_TAB.size
+    assert np.array_equal(rest[4:4 + n_sc].reshape(-1, 4), ga.SINCOS_TAB)
+    assert np.array_equal(rest[4 + n_sc:], ga.LN_INV)
 
 
 def test_float_float_infection_draws_track_float64():
