@@ -51,14 +51,14 @@ RECORDED_CUM_INFECTIONS = {(1_000_000, 180, 1): 1_055_079}
 
 MEASURED_NCU = {
     ('agent_step', 1_000_000): {
-        'dram_bytes': 69_902_592, 'issue_active': 0.610, 'bound': 'issue',
+        'dram_bytes': 69_901_568, 'issue_active': 0.602, 'bound': 'issue',
         'note': 'ncu section capture, day 85 of the 1M-agent run: 69.9 MB of DRAM traffic against 88 MB '
-                'algorithmic; instruction issue 61% busy, 35.8 M warp instructions for 1M agents, so the pass '
+                'algorithmic; instruction issue 60% busy, 35.0 M warp instructions for 1M agents, so the pass '
                 'is issue-bound on the float-float efficacies, not HBM-bound'},
     ('edge_stored', 1_000_000): {
-        'dram_bytes': 83_027_456, 'issue_active': 0.496, 'bound': 'latency',
-        'note': 'ncu section capture, day 85: 83 MB of DRAM traffic (the 62 MB of stored edge lists and the '
-                'candidates\' records); long-scoreboard stalls dominate'},
+        'dram_bytes': 83_445_760, 'issue_active': 0.533, 'bound': 'latency',
+        'note': 'ncu section capture, day 85 (one-wave pass, 2048-edge tiles): 83 MB of DRAM traffic (the 62 MB '
+                'of stored edge lists and the candidates\' records); long-scoreboard stalls dominate'},
 }
 
 
