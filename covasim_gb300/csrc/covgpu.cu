@@ -1082,8 +1082,8 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
 // ============================================================ redrawn layers
 //
 // Transmission over the dynamic layers (base.py:1849-1876 redrawn daily, then
-// utils.py:93-128): one warp per DYN_WORDS source-bitmap words (an agent block of
-// one sim). The words' sources are handed to the lanes 32 at a time; for each
+// utils.py:93-128): one warp per agent block of one sim, or two (source_split), on its
+// source-bitmap words. The words' sources are handed to the lanes 32 at a time; for each
 // dynamic layer of the sim every lane draws its source's two list lengths
 // (covgpu_device.cuh, "redrawn layers, per agent"), and the lists' four-entry
 // blocks of all 32 sources are then spread over the lanes (a prefix count and a
@@ -1095,16 +1095,15 @@ __global__ void __launch_bounds__(RES_THREADS, 1) k_edge_pass_res(covgpu_state s
 // day's sources, not the layer's edges: a quiet day costs a read of the source
 // bitmap.
 constexpr int DYN_WARPS = 8;  // warps per thread block
-// Source-bitmap words per warp of the per-source passes (of an agent block's
-// eight): eight, one warp per agent block, ran a 1M-agent run 2.7% faster than
-// four (16.8 against 17.26 ms): half the warps to launch and scan on the quiet
-// days, when the pass is all scanning.
-#ifndef COVGPU_DYN_WORDS
-#define COVGPU_DYN_WORDS 8
-#endif
-constexpr int DYN_WORDS = COVGPU_DYN_WORDS;
-constexpr int DYN_SPLIT = AGENT_THREADS / 32 / DYN_WORDS;  // warps per agent block
-static_assert(DYN_WORDS * DYN_SPLIT * 32 == AGENT_THREADS, "whole agent blocks per warp group");
+// Warps per agent block of the per-source passes (SPLIT, a template parameter: each
+// warp takes 8 / SPLIT of the agent block's eight source-bitmap words). One warp
+// per agent block ran a 1M-agent run 2.7% faster than two (16.8 against 17.26 ms):
+// half the warps to launch and scan on the quiet days, when the pass is all
+// scanning; a state of fewer agent blocks than SPLIT_ONE_MIN keeps two, for the
+// parallelism of its busy days.
+constexpr int AB_WORDS = AGENT_THREADS / 32;  // source-bitmap words of an agent block
+constexpr int64_t SPLIT_ONE_MIN = 2048;
+inline int source_split(const covgpu_state* st) { return st->n_agent_blocks >= SPLIT_ONE_MIN ? 1 : 2; }
 
 // the segment constants of dynamic layer segment seg for day t
 __device__ __forceinline__ void dyn_ctx(const covgpu_state& st, const covgpu_sim_params& sp, int seg, int t, SegCtx& c) {
@@ -1170,15 +1169,16 @@ __device__ __forceinline__ void dyn_drain(const covgpu_state& st, const SegCtx& 
 }
 
 // The redrawn layers of the day's sources for one block's worth (vblock) of
-// agent blocks: DYN_SPLIT warps per agent block, each on DYN_WORDS source-bitmap words.
-template <bool LIK>
+// agent blocks: SPLIT warps per agent block, each on AB_WORDS / SPLIT source-bitmap words.
+template <bool LIK, int SPLIT>
 __device__ __forceinline__ void dyn_body(const covgpu_state& st, int t, int64_t vblock, EdgeQueue* s_q) {
+  constexpr int DYN_WORDS = AB_WORDS / SPLIT;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t gw = vblock * DYN_WARPS + warp;
-  const int64_t b = gw / DYN_SPLIT;  // DYN_SPLIT warps per agent block
+  const int64_t b = gw / SPLIT;  // SPLIT warps per agent block
   if (b >= st.n_agent_blocks) return;  // warp-uniform
   const covgpu_agent_block blk = st.agent_blocks[b];
-  const int w_lo = (int)(gw % DYN_SPLIT) * DYN_WORDS;
+  const int w_lo = (int)(gw % SPLIT) * DYN_WORDS;
   const int nwb = (int)((blk.end - blk.begin + 31) >> 5);
   if (w_lo >= nwb) return;
   const int nw = min(DYN_WORDS, nwb - w_lo);
@@ -1273,8 +1273,8 @@ __device__ __forceinline__ void dyn_body(const covgpu_state& st, int t, int64_t 
   }
 }
 
-// The walk of the stored layers from the day's sources (seg_walked): one warp per
-// DYN_WORDS source-bitmap words, as the redrawn layers' pass. For each indexed stored
+// The walk of the stored layers from the day's sources (seg_walked): the warps and
+// source-bitmap words of the redrawn layers' pass. For each indexed stored
 // layer the warp's sources' edges (as p1: [rp1[a], rp1[a + 1]); as p2: the edges
 // perm2[rp2[a] .. rp2[a + 1])) are flattened across the lanes 32 at a time, each
 // lane finding its source by a search over the lanes' prefix counts; an edge whose
@@ -1321,11 +1321,12 @@ __device__ __forceinline__ void src_drain(const covgpu_state& st, const SegCtx& 
   __syncwarp();
 }
 
-template <bool LIK>
+template <bool LIK, int SPLIT>
 __device__ __forceinline__ void src_body(const covgpu_state& st, int t, int64_t vblock, SrcQueue* s_q) {
+  constexpr int DYN_WORDS = AB_WORDS / SPLIT;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t gw = vblock * SRC_WARPS + warp;
-  const int64_t b = gw / DYN_SPLIT;  // DYN_SPLIT warps per agent block
+  const int64_t b = gw / SPLIT;  // SPLIT warps per agent block
   if (b >= st.n_agent_blocks) return;  // warp-uniform
   const covgpu_agent_block blk = st.agent_blocks[b];
   const covgpu_sim_params& sp = st.sims[blk.sim];
@@ -1335,7 +1336,7 @@ __device__ __forceinline__ void src_body(const covgpu_state& st, int t, int64_t 
     if (seg >= 0 && seg_walked(st, st.segments[seg], t)) first = l;
   }
   if (first < 0) return;
-  const int w_lo = (int)(gw % DYN_SPLIT) * DYN_WORDS;
+  const int w_lo = (int)(gw % SPLIT) * DYN_WORDS;
   const int nwb = (int)((blk.end - blk.begin + 31) >> 5);
   if (w_lo >= nwb) return;
   const int nw = min(DYN_WORDS, nwb - w_lo);
@@ -1423,35 +1424,37 @@ static_assert(SRC_WARPS == DYN_WARPS, "the per-source passes share their launch 
 // of after the stored layers' (then empty) tile pass. Four resident blocks per SM
 // (64 registers): the redrawn layers' pass over a 100-day 1M-agent run took
 // 2.70 ms of kernel time against 2.89 ms with three (80 registers).
-template <bool LIK, bool WALK>
+template <bool LIK, bool WALK, int SPLIT>
 __global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st, int t, int dyn_blocks) {
   if (held(st, t)) return;
   __shared__ union {
     EdgeQueue e[DYN_WARPS];
     SrcQueue s[SRC_WARPS];
   } s_q;
-  if (!WALK || (int)blockIdx.x < dyn_blocks) dyn_body<LIK>(st, t, blockIdx.x, s_q.e);
-  else src_body<LIK>(st, t, (int64_t)blockIdx.x - dyn_blocks, s_q.s);
+  if (!WALK || (int)blockIdx.x < dyn_blocks) dyn_body<LIK, SPLIT>(st, t, blockIdx.x, s_q.e);
+  else src_body<LIK, SPLIT>(st, t, (int64_t)blockIdx.x - dyn_blocks, s_q.s);
 }
 
 // The walk alone (a state without redrawn layers, or the stored layers' pass on
 // its own).
-template <bool LIK>
+template <bool LIK, int SPLIT>
 __global__ void __launch_bounds__(SRC_WARPS * 32) k_src_pass(covgpu_state st, int t) {
   if (held(st, t)) return;
   __shared__ SrcQueue s_q[SRC_WARPS];
-  src_body<LIK>(st, t, blockIdx.x, s_q);
+  src_body<LIK, SPLIT>(st, t, blockIdx.x, s_q);
 }
 
 unsigned source_pass_blocks(const covgpu_state* st) {
-  return (unsigned)((DYN_SPLIT * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
+  return (unsigned)((source_split(st) * st->n_agent_blocks + DYN_WARPS - 1) / DYN_WARPS);
 }
 
 int launch_src_pass(const covgpu_state* st, int t, cudaStream_t s) {
   if (st->n_tiles == 0 || st->src_walk == 0) return COVGPU_OK;
   const unsigned grid = source_pass_blocks(st);
-  if (st->lik.factor) k_src_pass<true><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
-  else k_src_pass<false><<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
+  const bool one = source_split(st) == 1;
+  void (*k)(covgpu_state, int) = st->lik.factor ? (one ? k_src_pass<true, 1> : k_src_pass<true, 2>)
+                                                : (one ? k_src_pass<false, 1> : k_src_pass<false, 2>);
+  k<<<grid, SRC_WARPS * 32, 0, s>>>(*st, t);
   return launch_status();
 }
 
@@ -1462,8 +1465,13 @@ int launch_dyn_pass(const covgpu_state* st, int t, cudaStream_t s, bool with_wal
   const unsigned g = source_pass_blocks(st);
   const bool walk = with_walk && st->n_tiles > 0 && st->src_walk != 0;
   const unsigned grid = walk ? 2 * g : g;
-  void (*k)(covgpu_state, int, int) = st->lik.factor ? (walk ? k_dyn_pass<true, true> : k_dyn_pass<true, false>)
-                                                     : (walk ? k_dyn_pass<false, true> : k_dyn_pass<false, false>);
+  void (*k)(covgpu_state, int, int);
+  if (source_split(st) == 1)
+    k = st->lik.factor ? (walk ? k_dyn_pass<true, true, 1> : k_dyn_pass<true, false, 1>)
+                       : (walk ? k_dyn_pass<false, true, 1> : k_dyn_pass<false, false, 1>);
+  else
+    k = st->lik.factor ? (walk ? k_dyn_pass<true, true, 2> : k_dyn_pass<true, false, 2>)
+                       : (walk ? k_dyn_pass<false, true, 2> : k_dyn_pass<false, false, 2>);
   k<<<grid, DYN_WARPS * 32, 0, s>>>(*st, t, (int)g);
   return launch_status();
 }
