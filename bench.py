@@ -758,6 +758,8 @@ def batch_arm(args, n_sims=256, days=120, steps=None, warmup=None, emit=True):
     batch = cv.BatchSim(sims, edge_tile=args.edge_tile).initialize()
     init_s = time.perf_counter() - t0
     st = batch.state
+    if args.src_walk is not None:
+        st.set_src_walk(args.src_walk)
     snap = st.snapshot()
     seeds = [choose_seed(s) for s in sims]
     npts = days + 1
@@ -773,6 +775,8 @@ def batch_arm(args, n_sims=256, days=120, steps=None, warmup=None, emit=True):
         s = cv.Sim(dict(sims[k].pars), popdict=sims[k].popdict, person=sims[k]._person,
                    edge_tile=st.edge_tile_label)
         s.initialize()
+        if args.src_walk is not None:
+            s.state.set_src_walk(args.src_walk)
         singles.append((s, s.state.snapshot()))
 
     def one_by_one():

@@ -259,8 +259,13 @@ def ili_agents(seed, t, n, n_ili):
 # hybrid run, 18.45 -> 18.0 ms per run (thresholds 1/64 to 1/512 within 0.1 ms of
 # each other). Without a redrawn layer the walk is a launch of its own after the
 # tile pass, which costs about 12 us a day before any source is walked, and the
-# stored layers are streamed (0).
+# stored layers are streamed (0), unless the state holds at least SRC_WALK_MIN_EDGES
+# stored edges: then the day's stream is long enough for the walk to pay even as a
+# launch of its own (256 random-population sims, 320M edges, 120 days: 262 -> 238 ms
+# per batched run walking below 1/64 infectious).
 SRC_WALK = 128
+SRC_WALK_BIG = 64
+SRC_WALK_MIN_EDGES = 50_000_000
 
 
 def parse_edge_tile(choice):
@@ -286,7 +291,11 @@ class BatchState:
         self.edge_tile = et['tile']
         self.edge_resident = False
         self.edge_wave = L.EDGE_WAVE_MAX if et.get('wave') is True else int(et.get('wave', 0))
-        self.src_walk = SRC_WALK if any(ly.get('dynamic') for sp in specs for ly in sp.layers) else 0
+        if any(ly.get('dynamic') for sp in specs for ly in sp.layers):
+            self.src_walk = SRC_WALK
+        else:
+            stored = sum(len(ly['p1']) for sp in specs for ly in sp.layers)
+            self.src_walk = SRC_WALK_BIG if stored >= SRC_WALK_MIN_EDGES else 0
         self._index_pending = []  # stored segments whose agent index is built on demand
         self._index_tensors = []
         if not torch.cuda.is_available():
