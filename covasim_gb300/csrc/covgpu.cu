@@ -1900,8 +1900,9 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
   // the agent's fields that the branch, the samples and the writes read, loaded
   // together with its flags: one round trip instead of one per level of the branch
   float a_symp = 0.0f, a_sev = 0.0f, a_crit = 0.0f, a_death = 0.0f, a_peak = 0.0f, a_nab = 0.0f, a_simm = 0.0f;
-  float a_drec = 0.0f;
+  float a_drec = 0.0f, a_rt = 0.0f;
   uint32_t a_vs = 0u;
+  int32_t a_ninf = 0, a_nbt = 0;
   if (win) {
     a_symp = st.symp_prob[i];
     a_sev = st.severe_prob[i];
@@ -1912,6 +1913,9 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
     a_simm = st.symp_imm[(int64_t)v * st.n + i];
     a_drec = date_row(st, COVGPU_DATE_RECOVERED)[i];
     a_vs = st.vstate[i];
+    a_ninf = st.n_infections[i];  // and the counters the writes update
+    a_nbt = st.n_breakthroughs[i];
+    a_rt = st.rel_trans[i];
   }
   // the branch: every lane of the group (people.py:523-566)
   bool symp = false, sev = false, crit = false, dead = false;
@@ -1988,13 +1992,13 @@ __device__ uint32_t infect_group(const covgpu_state& st, const covgpu_sim_params
   uint32_t f = f0;
   // people.py:486-491: breakthrough infections (peak_nab defined)
   const bool breakthrough = a_peak != 0.0f;
-  if (breakthrough && st.n_breakthroughs[i] == 0) st.rel_trans[i] = __fmul_rn(st.rel_trans[i], sp.trans_redux);
+  if (breakthrough && a_nbt == 0) st.rel_trans[i] = __fmul_rn(a_rt, sp.trans_redux);
   float* d_rec = date_row(st, COVGPU_DATE_RECOVERED);
   const bool reinfection = defined(a_drec);
   f &= ~(B_SUS | B_NAIVE | B_REC | B_DIAG);
   f |= B_EXP | (1u << (EXPV_SHIFT + v));
-  st.n_infections[i] += 1;
-  if (breakthrough) st.n_breakthroughs[i] += 1;
+  st.n_infections[i] = a_ninf + 1;
+  if (breakthrough) st.n_breakthroughs[i] = a_nbt + 1;
   st.vstate[i] = (a_vs & 0xFFFFFF00u) | (uint32_t)v;
   const bool count = call_tag != CALL_TAG_SEED;
   uint32_t out = O_INF | (count ? O_COUNT : 0u) | (reinfection ? O_REINF : 0u);
