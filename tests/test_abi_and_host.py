@@ -257,3 +257,15 @@ def test_test_prob_subtarget_and_ili_inputs():
         got = ili_agents(seed, t, n, k)
         assert len(np.unique(got)) == k and got.min() >= 0 and got.max() < n
         np.testing.assert_array_equal(got, oracle_ili(seed, t, n, k))
+
+
+def test_edge_pass_labels_parse():
+    """The edge-pass labels the autotuner and Sim(edge_tile=...) take."""
+    from covasim_gb300.state import parse_edge_tile
+    assert parse_edge_tile(4096) == dict(tile=4096)
+    assert parse_edge_tile('8192') == dict(tile=8192)
+    assert parse_edge_tile('8192r') == dict(tile=8192, resident=True)
+    assert parse_edge_tile('2048w') == dict(tile=2048, wave=True)
+    assert parse_edge_tile('1024w4') == dict(tile=1024, wave=4)
+    assert parse_edge_tile(L.EDGE_TILE) == dict(tile=2048, wave=True)  # the default
+    assert L.DAY_STEADY == 2
