@@ -6,14 +6,16 @@
 //       check_immunity (immunity.py:303-350) + update_nab (immunity.py:205-213) +
 //       stocks/flows (sim.py:651-674) + viral load, source/target role bitmaps and
 //       the source and target records of the edge passes;
-//   k_edge_pass      every stored layer segment and variant of every sim: edges
-//       streamed with 128-bit reads, source->target candidates queued per warp in
-//       shared memory, then compute_trans_sus folded in lane-packed, Philox
-//       Bernoullis, warp-ballot compaction of events, atomicMin first-infector
-//       claim (k_edge_pass_res: the same with the source bitmap in shared memory;
-//       k_src_pass: optionally, quiet days walked from the sources);
+//   k_edge_wave      every stored layer segment and variant of every sim, one wave
+//       of blocks over balanced tile ranges (k_edge_pass: one block per tile;
+//       k_edge_pass_res: the source bitmap in shared memory): edges streamed with
+//       128-bit reads, source->target candidates queued per warp in shared memory,
+//       then compute_trans_sus folded in lane-packed, Philox Bernoullis,
+//       warp-ballot compaction of events, atomicMin first-infector claim;
 //   k_dyn_pass       the redrawn layers (base.py:1849-1876): the day's sources'
 //       contact lists drawn from Philox and thinned, the same candidates' path;
+//       on quiet days its second half of blocks walks the stored layers from the
+//       sources instead of the tile pass (k_src_pass: the walk on its own);
 //   k_infect_claims / k_infect_list   People.infect (people.py:435-586) +
 //       update_peak_nab (immunity.py:138-202).
 // The reference's standalone numba functions are in covgpu_reference.cu, the
