@@ -39,6 +39,15 @@ def _align(x, a):
     return (x + a - 1) // a * a
 
 
+def _upload(x, device):
+    """A host array (numpy or CPU tensor) on the device through pinned memory, the
+    copy asynchronous on the current stream: a new state's small tables then cost
+    no synchronisation with the uploads and index builds queued before them (the
+    pinned staging block is not reused before its copy has run)."""
+    t = torch.from_numpy(x) if isinstance(x, np.ndarray) else x
+    return t.pin_memory().to(device, non_blocking=True)
+
+
 def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -374,9 +383,9 @@ class BatchState:
             hi = kin.astype(np.float32)
             lo = (kin - hi.astype(np.float64)).astype(np.float32)
             kins.append(np.stack([hi, lo], axis=1).ravel())   # float pairs: hi + lo = nab_kin to ~2^-48
-        self.beta_tab = torch.from_numpy(np.concatenate(beta_tabs)).to(dev)
-        self.beta_layer_tab = torch.from_numpy(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32)).to(dev)
-        self.nab_kin = torch.from_numpy(np.concatenate(kins)).to(dev)  # float32 pairs
+        self.beta_tab = _upload(np.concatenate(beta_tabs), dev)
+        self.beta_layer_tab = _upload(np.concatenate(bl_tabs) if bl_tabs else np.zeros(1, np.float32), dev)
+        self.nab_kin = _upload(np.concatenate(kins), dev)  # float32 pairs
 
         self._build_rescale()
         self._build_imports()
@@ -615,7 +624,7 @@ class BatchState:
                 if ly.get('dynamic'):
                     rec.dynamic = 1
                     rec.beta_const = 1.0
-                    cdf = torch.from_numpy(dynamic_count_table(n_edges, sp.n).view(np.int64)).to(self.device)
+                    cdf = _upload(dynamic_count_table(n_edges, sp.n).view(np.int64), self.device)
                     rec.dyn_cdf, rec.dyn_k = cdf.data_ptr(), len(cdf)
                     rec.dyn_rse_max = rse_bound(_max_of(sp.person['rel_sus']), rec.quar_factor)
                     keep.append(cdf)
@@ -716,7 +725,7 @@ class BatchState:
         self.n_tiles = tiles
         self.n_dynamic = sum(1 for rec in self.segments if rec.dynamic)
         arr = (L.Layer * max(len(self.segments), 1))(*self.segments)
-        self.seg_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+        self.seg_dev = _upload(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8), self.device)
 
     def set_edge_tile(self, tile, resident=False, wave=0):
         """Edges per edge-pass tile (one of L.EDGE_TILES), whether the source bitmap
@@ -866,7 +875,7 @@ class BatchState:
             recs.append(r)
         arr = (L.SimParams * len(recs))(*recs)
         self.sim_recs = recs
-        self.sims_dev = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
+        self.sims_dev = _upload(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8), self.device)
 
     def _build_agent_blocks(self):
         dt = np.dtype([('begin', '<i8'), ('end', '<i8'), ('sim', '<i4'), ('_pad', '<i4')])
@@ -880,7 +889,7 @@ class BatchState:
             parts.append(b)
         blocks = np.concatenate(parts)
         self.n_agent_blocks = len(blocks)
-        self.blocks_dev = torch.from_numpy(blocks.view(np.uint8).copy()).to(self.device)
+        self.blocks_dev = _upload(blocks.view(np.uint8).copy(), self.device)
 
     def _refresh_state(self):
         t = self.t
@@ -1082,10 +1091,10 @@ class BatchState:
             return (inds, np.zeros(0, bool)) if want_infected else None
         if inds.min() < 0 or inds.max() >= self.specs[sim].n:
             raise IndexError('agent index out of range')
-        g = torch.from_numpy((inds + self.offsets[sim]).astype(np.int32)).to(self.device)
+        g = _upload((inds + self.offsets[sim]).astype(np.int32), self.device)
         src = None
         if sources is not None:
-            src = torch.from_numpy(np.asarray(sources, dtype=np.int32)[first]).to(self.device)
+            src = _upload(np.asarray(sources, dtype=np.int32)[first], self.device)
         infected = torch.empty(len(inds), dtype=torch.uint8, device=self.device) if want_infected else None
         self._keep_inds = (g, src)
         torch.ops.covgpu.infect_list(self._sa, int(t), g, src, int(sim), int(variant), int(layer_tag), int(call_tag),
