@@ -1426,8 +1426,14 @@ static_assert(SRC_WARPS == DYN_WARPS, "the per-source passes share their launch 
 // of after the stored layers' (then empty) tile pass. Four resident blocks per SM
 // (64 registers): the redrawn layers' pass over a 100-day 1M-agent run took
 // 2.70 ms of kernel time against 2.89 ms with three (80 registers).
+// resident blocks per SM the per-source passes' registers must allow (three, 80
+// registers without spills, ran the 1M run 0.05 ms slower than four)
+#ifndef COVGPU_DYN_MIN_BLOCKS
+#define COVGPU_DYN_MIN_BLOCKS 4
+#endif
 template <bool LIK, bool WALK, int SPLIT>
-__global__ void __launch_bounds__(DYN_WARPS * 32, 4) k_dyn_pass(covgpu_state st, int t, int dyn_blocks) {
+__global__ void __launch_bounds__(DYN_WARPS * 32, COVGPU_DYN_MIN_BLOCKS) k_dyn_pass(covgpu_state st, int t,
+                                                                                   int dyn_blocks) {
   if (held(st, t)) return;
   __shared__ union {
     EdgeQueue e[DYN_WARPS];
